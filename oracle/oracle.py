@@ -1,0 +1,144 @@
+"""ctypes front end of the FP64 oracle (oracle/fg_oracle.cpp) -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker or the timed CPU baseline. The product library never
+imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libfg_oracle.so")
+SRC = os.path.join(HERE, "fg_oracle.cpp")
+
+
+def build(force=False):
+    """Compile the oracle with the host g++ (plain C++17, no GPU)."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-o", LIB, SRC])
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp, i32, i64, dp, u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32
+        L.or_create.restype = vp
+        L.or_create.argtypes = [vp]
+        L.or_destroy.argtypes = [vp]
+        L.or_num_kvectors.argtypes = [vp]
+        L.or_set_state.argtypes = [vp, i32, dp, dp, dp]
+        L.or_get_positions.argtypes = [vp, dp]
+        L.or_get_qk.argtypes = [vp, dp, dp, dp]
+        L.or_pair_energy.restype = ctypes.c_double
+        L.or_pair_energy.argtypes = [vp, i32, i32]
+        L.or_trial_du.restype = ctypes.c_double
+        L.or_trial_du.argtypes = [vp, i32, dp, dp]
+        L.or_commit.restype = ctypes.c_double
+        L.or_commit.argtypes = [vp, i32]
+        L.or_total_energy.argtypes = [vp, dp]
+        L.or_boundary.argtypes = [vp, dp]
+        L.or_draw_translation_stream.argtypes = [u32, i32, dp, i64, dp, dp, dp]
+        L.or_mc_run.restype = ctypes.c_double
+        L.or_mc_run.argtypes = [vp, u32, i64, dp, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OracleSystem:
+    """FP64 restatement of one reference system (Space + energy + Ewald state)."""
+
+    def __init__(self, params, xyz, q, ids):
+        self._p = params
+        self.h = lib().or_create(ctypes.byref(params))
+        if not self.h:
+            raise RuntimeError("oracle create failed")
+        self.n = len(xyz)
+        self.set_state(xyz, q, ids)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_destroy(self.h)
+            self.h = None
+
+    def set_state(self, xyz, q, ids):
+        self._xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self._q = np.ascontiguousarray(q, dtype=np.float64)
+        self._ids = np.ascontiguousarray(ids, dtype=np.int32)
+        self.n = len(self._xyz)
+        lib().or_set_state(self.h, self.n, _ptr(self._xyz), _ptr(self._q), _ptr(self._ids))
+
+    @property
+    def num_kvectors(self):
+        return lib().or_num_kvectors(self.h)
+
+    def positions(self):
+        out = np.empty((self.n, 3), dtype=np.float64)
+        lib().or_get_positions(self.h, _ptr(out))
+        return out
+
+    def qk(self):
+        K = self.num_kvectors
+        q = np.empty(2 * K)
+        kv = np.empty(3 * K)
+        ak = np.empty(K)
+        lib().or_get_qk(self.h, _ptr(q), _ptr(kv), _ptr(ak))
+        return q[0::2] + 1j * q[1::2], kv.reshape(K, 3), ak
+
+    def pair_energy(self, i, j):
+        return lib().or_pair_energy(self.h, i, j)
+
+    def trial_du(self, idx, new_xyz):
+        idx = np.ascontiguousarray(np.atleast_1d(idx), dtype=np.int32)
+        new_xyz = np.ascontiguousarray(np.reshape(new_xyz, (-1, 3)), dtype=np.float64)
+        return lib().or_trial_du(self.h, len(idx), _ptr(idx), _ptr(new_xyz))
+
+    def commit(self, accepted):
+        return lib().or_commit(self.h, 1 if accepted else 0)
+
+    def total_energy(self):
+        """{pairs, reciprocal, self, surface, total} (kT)."""
+        c = np.empty(5)
+        lib().or_total_energy(self.h, _ptr(c))
+        return dict(pairs=c[0], reciprocal=c[1], self=c[2], surface=c[3], total=c[4])
+
+    def boundary(self, xyz):
+        a = np.ascontiguousarray(xyz, dtype=np.float64).copy()
+        lib().or_boundary(self.h, _ptr(a))
+        return a
+
+    def mc_run(self, seed, n_trials, log=True):
+        """Metropolis run with the reference's RNG stream; returns dict."""
+        n = int(n_trials)
+        idx = np.empty(n, np.int32) if log else None
+        txyz = np.empty((n, 3)) if log else None
+        du = np.empty(n) if log else None
+        acc = np.empty(n, np.uint8) if log else None
+        utot = lib().or_mc_run(self.h, seed, n, _ptr(idx), _ptr(txyz), _ptr(du), _ptr(acc))
+        return dict(utot=utot, idx=idx, trial_xyz=txyz, du=du, acc=acc)
+
+
+def translation_stream(seed, dp_per_particle, n_trials):
+    """The reference's per-trial randoms for AtomicTranslation on one atomic
+    group: (index[n], displacement[n,3], u_metropolis[n])."""
+    dpp = np.ascontiguousarray(dp_per_particle, dtype=np.float64)
+    n = int(n_trials)
+    idx = np.empty(n, np.int32)
+    disp = np.empty((n, 3))
+    u = np.empty(n)
+    lib().or_draw_translation_stream(seed, len(dpp), _ptr(dpp), n, _ptr(idx), _ptr(disp), _ptr(u))
+    return idx, disp, u
