@@ -1,0 +1,219 @@
+"""ctypes front end of libfaunus_gb300.so (include/faunus_gb300.h).
+
+Mirrors the reference's energy/move interface for the Metropolis path:
+``System.trial_du`` + ``System.commit`` are Energybase::updateChange /
+Energy::energyChange / Energybase::update as Movebase::move calls them
+(move.h:515-555); ``System.sweep`` runs that whole loop on the device.
+Raises if the compiled library is missing: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from .params import FgParams
+
+_lib = None
+
+
+class FgError(RuntimeError):
+    pass
+
+
+class SweepStats(ctypes.Structure):
+    _fields_ = [("trials", ctypes.c_int64), ("accepted", ctypes.c_int64), ("rebuilds", ctypes.c_int64),
+                ("energy_change", ctypes.c_double), ("device_ms", ctypes.c_double),
+                ("sweep_kernel_ms", ctypes.c_double), ("sweep_launches", ctypes.c_int32),
+                ("error_flags", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=True):
+    """Load the in-tree library (building it first if allowed)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise FgError("libfaunus_gb300.so not built: run __graft_entry__.build()")
+            _build.build()
+        L = ctypes.CDLL(path)
+        vp, i32, i64, u32, dp = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32, ctypes.c_void_p
+        sig = {
+            "fg_version": ([], ctypes.c_int),
+            "fg_last_error": ([], ctypes.c_char_p),
+            "fg_create": ([vp, i32, ctypes.POINTER(vp)], ctypes.c_int),
+            "fg_destroy": ([vp], ctypes.c_int),
+            "fg_set_state": ([vp, dp, dp, dp], ctypes.c_int),
+            "fg_get_state": ([vp, dp], ctypes.c_int),
+            "fg_trial_du": ([vp, i32, dp, dp, dp], ctypes.c_int),
+            "fg_commit": ([vp, i32, dp], ctypes.c_int),
+            "fg_total_energy": ([vp, dp], ctypes.c_int),
+            "fg_num_kvectors": ([vp], ctypes.c_int),
+            "fg_get_qk": ([vp, dp], ctypes.c_int),
+            "fg_rebuild_qk": ([vp, dp], ctypes.c_int),
+            "fg_draw_translation_stream": ([vp, u32, i64, dp, dp, dp], ctypes.c_int),
+            "fg_sweep": ([vp, i64, dp, dp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_stream_upload": ([vp, i64, dp, dp, dp], ctypes.c_int),
+            "fg_stream_philox": ([vp, i64, u32, u32], ctypes.c_int),
+            "fg_stream_get": ([vp, i64, i64, dp, dp, dp], ctypes.c_int),
+            "fg_stream_run": ([vp, dp], ctypes.c_int),
+            "fg_synchronize": ([vp], ctypes.c_int),
+            "fg_set_threads": ([vp, i32], ctypes.c_int),
+            "fg_get_threads": ([vp], ctypes.c_int),
+            "fg_philox4x32_10": ([dp, dp, dp], None),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(rc):
+    if rc != 0:
+        raise FgError("%d: %s" % (rc, lib().fg_last_error().decode()))
+
+
+def philox4x32_10(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.empty(4, dtype=np.uint32)
+    lib().fg_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
+
+
+class System:
+    """One Monte Carlo system resident on the GPU."""
+
+    def __init__(self, params, xyz, charge=None, type_ids=None, threads=0):
+        if not isinstance(params, FgParams):
+            raise TypeError("params must be FgParams")
+        self.params = params
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        self.n = len(xyz)
+        h = ctypes.c_void_p()
+        _check(lib().fg_create(ctypes.byref(params), self.n, ctypes.byref(h)))
+        self.h = h
+        if threads:
+            _check(lib().fg_set_threads(self.h, threads))
+        self.set_state(xyz, charge, type_ids)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, xyz, charge=None, type_ids=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        if type_ids is None:
+            type_ids = np.zeros(self.n, dtype=np.int32)
+        self._ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+        q = None if charge is None else np.ascontiguousarray(charge, dtype=np.float64)
+        _check(lib().fg_set_state(self.h, _p(xyz), _p(q), _p(self._ids)))
+
+    @property
+    def threads(self):
+        return lib().fg_get_threads(self.h)
+
+    @threads.setter
+    def threads(self, t):
+        _check(lib().fg_set_threads(self.h, int(t)))
+
+    def positions(self):
+        out = np.empty((self.n, 3))
+        _check(lib().fg_get_state(self.h, _p(out)))
+        return out
+
+    @property
+    def num_kvectors(self):
+        return lib().fg_num_kvectors(self.h)
+
+    def qk(self):
+        K = self.num_kvectors
+        q = np.empty(2 * max(K, 1))
+        _check(lib().fg_get_qk(self.h, _p(q)))
+        return q[0:2 * K:2] + 1j * q[1:2 * K:2]
+
+    def trial_du(self, idx, new_xyz):
+        idx = np.ascontiguousarray(np.atleast_1d(idx), dtype=np.int32)
+        x = np.ascontiguousarray(new_xyz, dtype=np.float64).reshape(-1, 3)
+        du = np.zeros(1)
+        _check(lib().fg_trial_du(self.h, len(idx), _p(idx), _p(x), _p(du)))
+        return float(du[0])
+
+    def commit(self, accepted):
+        c = np.zeros(1)
+        _check(lib().fg_commit(self.h, 1 if accepted else 0, _p(c)))
+        return float(c[0])
+
+    def rebuild_qk(self):
+        c = np.zeros(1)
+        _check(lib().fg_rebuild_qk(self.h, _p(c)))
+        return float(c[0])
+
+    def total_energy(self):
+        c = np.zeros(5)
+        _check(lib().fg_total_energy(self.h, _p(c)))
+        return dict(pairs=c[0], reciprocal=c[1], self=c[2], surface=c[3], total=c[4])
+
+    def draw_translation_stream(self, seed, n):
+        n = int(n)
+        idx = np.empty(n, np.int32)
+        disp = np.empty((n, 3))
+        u = np.empty(n)
+        _check(lib().fg_draw_translation_stream(self.h, seed, n, _p(idx), _p(disp), _p(u)))
+        return idx, disp, u
+
+    def sweep(self, idx, disp, u, log=True):
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        disp = np.ascontiguousarray(disp, dtype=np.float64).reshape(-1, 3)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        n = len(idx)
+        acc = np.empty(n, np.uint8) if log else None
+        du = np.empty(n) if log else None
+        st = SweepStats()
+        _check(lib().fg_sweep(self.h, n, _p(idx), _p(disp), _p(u), _p(acc), _p(du), ctypes.byref(st)))
+        return dict(acc=acc, du=du, stats=st.as_dict())
+
+    def stream_upload(self, idx, disp, u):
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        disp = np.ascontiguousarray(disp, dtype=np.float64).reshape(-1, 3)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        _check(lib().fg_stream_upload(self.h, len(idx), _p(idx), _p(disp), _p(u)))
+
+    def stream_philox(self, n, seed, stream_id=0):
+        _check(lib().fg_stream_philox(self.h, int(n), seed, stream_id))
+
+    def stream_get(self, first, n):
+        idx = np.empty(n, np.int32)
+        disp = np.empty((n, 3))
+        u = np.empty(n)
+        _check(lib().fg_stream_get(self.h, first, n, _p(idx), _p(disp), _p(u)))
+        return idx, disp, u
+
+    def stream_run(self):
+        st = SweepStats()
+        _check(lib().fg_stream_run(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def synchronize(self):
+        _check(lib().fg_synchronize(self.h))

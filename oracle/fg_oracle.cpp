@@ -483,4 +483,27 @@ double or_mc_run(void *h, uint32_t seed, int64_t n_trials, int32_t *idx_out, dou
     return utot;
 }
 
+// Same loop as or_mc_run but from an explicit trial stream (particle index,
+// displacement, Metropolis uniform per trial), e.g. one drawn on the device.
+double or_mc_run_stream(void *h, int64_t n_trials, const int32_t *idx, const double *disp, const double *u,
+                        double *du_out, uint8_t *acc_out) {
+    System *s = (System *)h;
+    double utot = 0;
+    for (int64_t n = 0; n < n_trials; n++) {
+        int i = idx[n];
+        V3 r = s->p[i].r;
+        r.x += disp[3 * n]; r.y += disp[3 * n + 1]; r.z += disp[3 * n + 2];
+        s->geo.boundary(r);
+        double xyz[3] = {r.x, r.y, r.z};
+        double du = s->trial_du(1, &i, xyz);
+        double kT = s->P.kT_scale > 0 ? s->P.kT_scale : 1.0;
+        bool accept = !(u[n] > std::exp(-du / kT));
+        if (accept) utot += du;
+        utot += s->commit(accept);
+        if (du_out) du_out[n] = du;
+        if (acc_out) acc_out[n] = accept ? 1 : 0;
+    }
+    return utot;
+}
+
 }  // extern "C"

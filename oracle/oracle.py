@@ -51,6 +51,8 @@ def lib():
         L.or_draw_translation_stream.argtypes = [u32, i32, dp, i64, dp, dp, dp]
         L.or_mc_run.restype = ctypes.c_double
         L.or_mc_run.argtypes = [vp, u32, i64, dp, dp, dp, dp]
+        L.or_mc_run_stream.restype = ctypes.c_double
+        L.or_mc_run_stream.argtypes = [vp, i64, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -130,6 +132,21 @@ class OracleSystem:
         acc = np.empty(n, np.uint8) if log else None
         utot = lib().or_mc_run(self.h, seed, n, _ptr(idx), _ptr(txyz), _ptr(du), _ptr(acc))
         return dict(utot=utot, idx=idx, trial_xyz=txyz, du=du, acc=acc)
+
+
+def _mc_run_stream(self, idx, disp, u):
+    """Metropolis run from an explicit stream; returns dict(utot, du, acc)."""
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    disp = np.ascontiguousarray(disp, dtype=np.float64).reshape(-1, 3)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    n = len(idx)
+    du = np.empty(n)
+    acc = np.empty(n, np.uint8)
+    utot = lib().or_mc_run_stream(self.h, n, _ptr(idx), _ptr(disp), _ptr(u), _ptr(du), _ptr(acc))
+    return dict(utot=utot, du=du, acc=acc)
+
+
+OracleSystem.mc_run_stream = _mc_run_stream
 
 
 def translation_stream(seed, dp_per_particle, n_trials):

@@ -1,0 +1,183 @@
+"""GPU parity: the CUDA path against the FP64 oracle (pinned to the reference)
+on the same seeded inputs and the same random stream.
+
+Tolerance (written here, used everywhere below): every dU within 1e-6 kT of
+the FP64 oracle; acceptance sequences identical except for trials whose
+|dU - (-ln u)| is inside that tolerance band.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from beofaunus_gb300 import workloads
+from beofaunus_gb300.params import FgParams
+from oracle.oracle import OracleSystem, translation_stream
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL_DU = 1e-6
+
+
+def gpu_system(params, xyz, q, ids, **kw):
+    from beofaunus_gb300.gpu import System
+    return System(params, xyz, q, ids, **kw)
+
+
+def assert_same_chain(du_gpu, acc_gpu, du_ref, acc_ref, u):
+    """dU within TOL_DU everywhere the chains agree; acceptance identical
+    unless the threshold is inside the tolerance band (then stop comparing:
+    the chains legitimately diverge from there)."""
+    n = len(du_ref)
+    err = np.abs(du_gpu - du_ref)
+    mism = np.nonzero(acc_gpu != acc_ref)[0]
+    upto = n
+    if len(mism):
+        t = mism[0]
+        band = abs(du_ref[t] + np.log(u[t]))
+        assert band < TOL_DU, "acceptance differs at trial %d outside the band (%g)" % (t, band)
+        upto = t + 1
+    assert np.all(np.isfinite(du_gpu[:upto]))
+    assert err[:upto].max() <= TOL_DU, "max |dU err| = %g at trial %d" % (err[:upto].max(), err[:upto].argmax())
+    return err[:upto]
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def params_of(g):
+    p = FgParams.from_buffer_copy(g["params"].tobytes())
+    p.bjerrum = float(g["bjerrum"])
+    return p
+
+
+@pytest.mark.parametrize("name", ["ewald_small_uf1", "ewald_surface_uf5", "ewald_rpm800", "dhlj_small", "dhlj_500"])
+def test_sweep_reproduces_reference_log(name):
+    """Device sweep with the host replay of the reference's RNG reproduces the
+    reference's own per-trial log (dU, acceptance) and final positions."""
+    g = load(name)
+    p = params_of(g)
+    s = gpu_system(p, g["xyz"], g["q"], g["ids"])
+    n = len(g["idx"])
+    idx, disp, u = s.draw_translation_stream(int(g["seed"]), n)
+    np.testing.assert_array_equal(idx, g["idx"])
+    r = s.sweep(idx, disp, u)
+    assert_same_chain(r["du"], r["acc"], g["du"], g["acc"], u)
+    np.testing.assert_array_equal(r["acc"], g["acc"])
+    np.testing.assert_allclose(s.positions(), g["final_positions"], rtol=0, atol=1e-9)
+    assert r["stats"]["energy_change"] == pytest.approx(float(g["u_move_sum"]), abs=1e-5)
+
+
+def test_plain_trial_commit_matches_oracle_rpm800():
+    """The per-trial drop-in (fg_trial_du + fg_commit) on the 800-ion Ewald system."""
+    p, xyz, q, ids = workloads.rpm800(seed=3, update_frequency=50)
+    s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
+    dpp = np.array([p.type_dp[i] for i in ids])
+    idx, disp, u = translation_stream(77, dpp, 300)
+    errs = []
+    for t in range(300):
+        i = int(idx[t])
+        new = o.boundary(o.positions()[i] + disp[t])
+        dg = s.trial_du(i, new)
+        do = o.trial_du(i, new)
+        errs.append(abs(dg - do))
+        acc = not (u[t] > np.exp(-do))
+        cg = s.commit(acc)
+        co = o.commit(acc)
+        assert cg == pytest.approx(co, abs=1e-6)
+    assert max(errs) <= TOL_DU, max(errs)
+    np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
+
+
+def test_sweep_rpm16k_cell_list_full_size():
+    """16384 ions, L=163, |n|^2<=100 (K=2242), cell list: 2000 trials."""
+    p, xyz, q, ids = workloads.rpm16k(seed=5, update_frequency=1000)
+    s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
+    assert s.num_kvectors == o.num_kvectors == 2242
+    idx, disp, u = s.draw_translation_stream(2024, 2000)
+    r = s.sweep(idx, disp, u)
+    ro = o.mc_run_stream(idx, disp, u)
+    err = assert_same_chain(r["du"], r["acc"], ro["du"], ro["acc"], u)
+    print("rpm16k: max |dU err| %.3g rms %.3g" % (err.max(), np.sqrt(np.mean(err ** 2))))
+    np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
+    qg = s.qk()
+    qo = o.qk()[0]
+    assert np.max(np.abs(qg - qo)) < 1e-5
+
+
+def test_total_energy_matches_oracle():
+    p, xyz, q, ids = workloads.rpm800(seed=8, update_frequency=1000)
+    s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
+    eg, eo = s.total_energy(), o.total_energy()
+    assert eg["pairs"] == pytest.approx(eo["pairs"], abs=2e-4)
+    assert eg["reciprocal"] == pytest.approx(eo["reciprocal"], abs=1e-6)
+    assert eg["self"] == pytest.approx(eo["self"], rel=1e-12)
+    assert eg["surface"] == pytest.approx(eo["surface"], abs=1e-9)
+    assert eg["total"] == pytest.approx(eo["total"], abs=2e-4)
+    # and after a device sweep the running energy tracks the total
+    idx, disp, u = s.draw_translation_stream(99, 1600)
+    r = s.sweep(idx, disp, u, log=False)
+    ro = o.mc_run_stream(idx, disp, u)
+    e1 = s.total_energy()["total"]
+    assert e1 == pytest.approx(o.total_energy()["total"], abs=5e-4)
+    assert r["stats"]["energy_change"] == pytest.approx(ro["utot"], abs=1e-4)
+
+
+@pytest.mark.parametrize("n", [500, 4000])
+def test_dh_lj_sweep_matches_oracle(n):
+    p, xyz, q, ids = workloads.dh_lj_salt(n, seed=n)
+    s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
+    idx, disp, u = s.draw_translation_stream(n + 1, 3 * n)
+    r = s.sweep(idx, disp, u)
+    ro = o.mc_run_stream(idx, disp, u)
+    assert_same_chain(r["du"], r["acc"], ro["du"], ro["acc"], u)
+    np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
+
+
+def test_philox_stream_run_matches_oracle():
+    """Device-generated stream: downloaded and replayed by the oracle."""
+    p, xyz, q, ids = workloads.rpm800(seed=21, update_frequency=200)
+    s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
+    s.stream_philox(1600, seed=1234, stream_id=7)
+    idx, disp, u = s.stream_get(0, 1600)
+    assert idx.min() >= 0 and idx.max() < 800
+    assert np.all(np.abs(disp) <= 1.0 + 1e-12)
+    st = s.stream_run()
+    assert st["trials"] == 1600
+    ro = o.mc_run_stream(idx, disp, u)
+    assert st["accepted"] == int(ro["acc"].sum())
+    np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
+
+
+def test_rebuild_is_drift_free_and_correction_small():
+    p, xyz, q, ids = workloads.rpm800(seed=31, update_frequency=100000)
+    s = gpu_system(p, xyz, q, ids)
+    idx, disp, u = s.draw_translation_stream(5, 4000)
+    s.sweep(idx, disp, u, log=False)
+    q_inc = s.qk()
+    corr = s.rebuild_qk()
+    q_new = s.qk()
+    assert np.max(np.abs(q_inc - q_new)) < 1e-5
+    assert abs(corr) < 1e-5
+
+
+def test_invalid_arguments_fail_loudly():
+    from beofaunus_gb300.gpu import FgError
+    p, xyz, q, ids = workloads.rpm800(seed=1)
+    s = gpu_system(p, xyz, q, ids)
+    with pytest.raises(FgError):
+        s.trial_du(800, [0.0, 0.0, 0.0])
+    with pytest.raises(FgError):
+        s.commit(True)   # no pending trial
+    bad = FgParams.from_buffer_copy(bytes(p))
+    bad.type_charge[0] = 0.0   # ewald.h:539 would divide by zero
+    with pytest.raises(FgError):
+        gpu_system(bad, xyz, q, ids)
