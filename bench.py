@@ -178,6 +178,10 @@ def run_ours(args):
     trials = sum(st["trials"] for st in stats)
     value = trials / (dev_ms / 1e3)
 
+    if args.value_only:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": "trials/s", "ms_per_step": dev_ms / steps,
+                          "sweep_kernel_ms": sweep_ms, "sweep_launches": launches, "trials": trials}))
+        return
     # ---- e2e through fg_sweep with host buffers (H2D stream, D2H results)
     e2e_streams = [sys_.draw_translation_stream(5000 + s, T) for s in range(steps)]
     torch.cuda.synchronize()
@@ -286,6 +290,7 @@ def main():
     ap.add_argument("--cpu-trials", type=int, default=1024)
     ap.add_argument("--trials", type=int, default=N_IONS, help="trials per step (default: one sweep)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--value-only", action="store_true", help="device-resident value only (profiling)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

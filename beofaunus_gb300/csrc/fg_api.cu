@@ -1,5 +1,8 @@
-// C-ABI implementation: handle lifetime, uploads, launches and host-side
-// replay of the reference's random stream. See include/faunus_gb300.h.
+// C-ABI implementation, single systems: handle lifetime, uploads, launches
+// and the host-side replay of the reference's random stream. Batches,
+// parallel tempering and the job server are in fg_batch.cu (same
+// translation unit). See include/faunus_gb300.h.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -59,6 +62,7 @@ float2 split_df(double v) {
     float h = (float)v;
     return make_float2(h, (float)(v - (double)h));
 }
+double df_val(float hi, float lo) { return (double)hi + (double)lo; }
 
 int cell_of_h(const int64_t X[3], const int nc[3]) {
     int c[3];
@@ -67,13 +71,6 @@ int cell_of_h(const int64_t X[3], const int nc[3]) {
         c[a] = (int)(((uint64_t)u * (uint32_t)nc[a]) >> 32);
     }
     return (c[2] * nc[1] + c[1]) * nc[0] + c[0];
-}
-
-size_t smem_bytes(int N, int K, bool pos_smem, bool kspace) {
-    size_t b = 256 * 8 + 32 * 8 + 160 * 4 + 8 * 4;
-    if (kspace) b += (size_t)K * 16 + (size_t)K * 16 + (size_t)((K + 3) & ~3) * 4;
-    if (pos_smem) b += (size_t)N * 16 + (size_t)N * 8 + (size_t)N;
-    return (b + 15) & ~(size_t)15;
 }
 
 }  // namespace
@@ -89,26 +86,23 @@ struct fg_system {
     int64_t *pos64 = nullptr;
     int4 *pos4 = nullptr;
     short4 *pos_ext = nullptr, *cell_ext = nullptr;
-    float4 *core_tab = nullptr, *core_tab2 = nullptr;
     uint8_t *ptype = nullptr;
     int32_t *cell_count = nullptr, *cell_pid = nullptr, *p_cell = nullptr, *p_slot = nullptr;
     int4 *cell_pos = nullptr;
-    float4 *kvec = nullptr, *qk = nullptr;
+    float4 *kvec = nullptr, *core_tab = nullptr, *core_tab2 = nullptr;
     uint32_t *kpack = nullptr;
+    longlong2 *qfix = nullptr, *qnew = nullptr;
     SysScalars *sc = nullptr;
-    float2 *pending_dq = nullptr, *trial_out = nullptr, *energy_out = nullptr, *pair_part = nullptr;
+    float2 *trial_out = nullptr, *corr = nullptr, *pair_part = nullptr;
     int64_t *req = nullptr, *dp_fix = nullptr;
-    int32_t *flags = nullptr;
     float2 *sc_tab = nullptr;
-    float4 *axis_tab = nullptr, *qk_part = nullptr;
-    int chunk = 0, nchunk = 0;
     Trial *trials = nullptr;
     int64_t trials_cap = 0, n_trials = 0;
     float2 *log_du = nullptr;
     uint8_t *log_acc = nullptr;
     int64_t log_cap = 0;
     // host-side values
-    std::vector<double> charge;
+    std::vector<double> ak;
     std::vector<int32_t> types;
     double self_energy = 0, surf_c = 0, recip_c = 0;
     int threads = 0;
@@ -116,29 +110,41 @@ struct fg_system {
     int nc[3] = {0, 0, 0};
     int cap = 0;
     bool trial_pending = false;
-    int cnt_accepted_host = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ek0 = nullptr, ek1 = nullptr;
     bool state_set = false;
+    int cnt_accepted_host = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t device_bytes = 0;
 };
 
 namespace {
 
 void free_all(fg_system *h) {
-    void *ptrs[] = {h->d_desc, h->pos64, h->pos4, h->ptype, h->cell_count, h->cell_pid, h->p_cell, h->p_slot,
-                    h->cell_pos, h->kvec, h->qk, h->kpack, h->sc, h->pending_dq, h->trial_out, h->energy_out,
-                    h->pair_part, h->req, h->dp_fix, h->flags, h->sc_tab, h->axis_tab, h->qk_part, h->trials,
-                    h->log_du, h->log_acc, h->pos_ext, h->cell_ext, h->core_tab, h->core_tab2};
+    void *ptrs[] = {h->d_desc, h->pos64, h->pos4, h->pos_ext, h->cell_ext, h->ptype, h->cell_count, h->cell_pid,
+                    h->p_cell, h->p_slot, h->cell_pos, h->kvec, h->core_tab, h->core_tab2, h->kpack, h->qfix,
+                    h->qnew, h->sc, h->trial_out, h->corr, h->pair_part, h->req, h->dp_fix, h->sc_tab, h->trials,
+                    h->log_du, h->log_acc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
-    if (h->ek0) cudaEventDestroy(h->ek0);
-    if (h->ek1) cudaEventDestroy(h->ek1);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
+int dmalloc(fg_system *h, void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    h->device_bytes += bytes;
+    return FG_OK;
+}
+#define DMALLOC(ptr, bytes)                                        \
+    do {                                                           \
+        int rc_ = dmalloc(h, (void **)&(ptr), (size_t)(bytes));    \
+        if (rc_) return rc_;                                       \
+    } while (0)
+
 // k-vectors exactly as NonbondedEwald::kVectorChange (ewald.h:330-378),
-// non-isotropic branch; returns n-vectors and A_k.
+// non-isotropic branch; returns n-vectors, k and A_k.
 void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &ak, std::vector<double> &kv3) {
     double kc = P.ewald_cutoff_k, kc2 = kc * kc;
     int kcc = (int)std::ceil(kc);
@@ -159,21 +165,27 @@ void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &
             }
 }
 
-int pick_threads(const fg_system *h) {
-    if (h->threads > 0) return h->threads;
-    int work = std::max(h->K, 1);
-    int t;
-    if (h->model == FG_MODEL_EWALD_WCA) t = (h->K + 2) / 3;   // ~3 k-vectors per thread
-    else t = h->N / 4;                                      // ~4 particles per thread
-    (void)work;
-    t = ((t + 31) / 32) * 32;
-    t = std::max(128, std::min(1024, t));
-    // k-vectors must fit kMaxKPerThread per thread
-    while (t < 1024 && t * fg::kMaxKPerThread < h->K) t += 32;
+// Threads of the per-system CTA (multiple of 32, <= kSweepThreads).
+int sweep_threads(const fg_system *h) {
+    int t = h->threads;
+    if (t <= 0) {
+        if (h->model == FG_MODEL_EWALD_WCA) t = (h->K + 3) / 4;   // ~4 k-vectors per thread
+        else t = h->N / 8;                                      // ~8 particles per thread
+        t = ((t + 31) / 32) * 32;
+        t = std::max(128, std::min(fg::kSweepThreads, t));
+    }
     return t;
 }
 
+size_t sweep_smem(const fg_system *h, bool pos_smem) {
+    size_t off[8];
+    return fg::smem_layout(h->N, h->K, h->nc[0] * h->nc[1] * h->nc[2], h->model == FG_MODEL_EWALD_WCA, pos_smem,
+                           h->use_cells, off);
+}
+
 using SweepFn = void (*)(const SysDesc *, int64_t, const float2 *);
+using TrialFn = void (*)(const SysDesc *, const int64_t *, float2 *, const float2 *);
+using CommitFn = void (*)(const SysDesc *, const int64_t *, const float2 *, const float2 *);
 
 SweepFn sweep_fn(const fg_system *h) {
     if (h->model == FG_MODEL_EWALD_WCA) {
@@ -184,20 +196,29 @@ SweepFn sweep_fn(const fg_system *h) {
     if (h->pos_smem) return fg::sweep_kernel<fg::MODEL_DHLJ, false, true>;
     return fg::sweep_kernel<fg::MODEL_DHLJ, false, false>;
 }
-
-size_t sweep_smem(const fg_system *h) {
-    return smem_bytes(h->N, h->K, h->pos_smem, h->model == FG_MODEL_EWALD_WCA);
+TrialFn trial_fn(const fg_system *h) {
+    if (h->model == FG_MODEL_EWALD_WCA)
+        return h->use_cells ? fg::trial_kernel<fg::MODEL_EWALD, true> : fg::trial_kernel<fg::MODEL_EWALD, false>;
+    return fg::trial_kernel<fg::MODEL_DHLJ, false>;
+}
+CommitFn commit_fn(const fg_system *h) {
+    if (h->model == FG_MODEL_EWALD_WCA)
+        return h->use_cells ? fg::commit_kernel<fg::MODEL_EWALD, true> : fg::commit_kernel<fg::MODEL_EWALD, false>;
+    return fg::commit_kernel<fg::MODEL_DHLJ, false>;
 }
 
-int launch_rebuild(fg_system *h) {
-    if (h->model != FG_MODEL_EWALD_WCA) return FG_OK;
-    const int per = (h->kc + 1) + 2 * (2 * h->kc + 1);
-    int64_t total = (int64_t)h->N * per;
-    int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
-    fg::axis_phase_kernel<<<blocks, 256, 0, h->stream>>>(h->d_desc, h->kc, h->axis_tab);
-    dim3 g((h->K + 127) / 128, h->nchunk);
-    fg::qk_partial_kernel<<<g, 128, 0, h->stream>>>(h->d_desc, h->kc, h->axis_tab, h->chunk, h->qk_part);
-    fg::qk_finish_kernel<<<1, 1024, 0, h->stream>>>(h->d_desc, h->qk_part, h->nchunk, h->energy_out);
+int set_smem_attr(const void *fn, size_t bytes) {
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return FG_OK;
+}
+
+// Rebuild kernels for n systems whose descriptors are at `descs` (device).
+int launch_rebuild(const SysDesc *descs, int n, int maxN, int maxK, float2 *corr, cudaStream_t st) {
+    if (maxK == 0) return FG_OK;
+    const int chunk = 1024;
+    dim3 g((maxK + 255) / 256, (maxN + chunk - 1) / chunk, n);
+    fg::qk_rebuild_kernel<<<g, 256, 0, st>>>(descs, chunk);
+    fg::qk_rebuild_finish<<<n, 1024, 0, st>>>(descs, corr);
     CK(cudaGetLastError());
     return FG_OK;
 }
@@ -207,12 +228,18 @@ int read_scalars(fg_system *h, SysScalars &s) {
     CK(cudaStreamSynchronize(h->stream));
     return FG_OK;
 }
+int write_scalars(fg_system *h, const SysScalars &s) {
+    CK(cudaMemcpyAsync(h->sc, &s, sizeof(SysScalars), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
 
 int ensure_trials(fg_system *h, int64_t n, bool log) {
+    n = std::max<int64_t>(n, 1);
     if (n > h->trials_cap) {
         if (h->trials) cudaFree(h->trials);
         h->trials = nullptr;
-        CK(cudaMalloc(&h->trials, n * sizeof(Trial)));
+        DMALLOC(h->trials, n * sizeof(Trial));
         h->trials_cap = n;
     }
     if (log && n > h->log_cap) {
@@ -220,8 +247,8 @@ int ensure_trials(fg_system *h, int64_t n, bool log) {
         if (h->log_acc) cudaFree(h->log_acc);
         h->log_du = nullptr;
         h->log_acc = nullptr;
-        CK(cudaMalloc(&h->log_du, n * sizeof(float2)));
-        CK(cudaMalloc(&h->log_acc, n));
+        DMALLOC(h->log_du, n * sizeof(float2));
+        DMALLOC(h->log_acc, n);
         h->log_cap = n;
     }
     return FG_OK;
@@ -229,6 +256,7 @@ int ensure_trials(fg_system *h, int64_t n, bool log) {
 
 int push_desc(fg_system *h) {
     CK(cudaMemcpyAsync(h->d_desc, &h->desc, sizeof(SysDesc), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
     return FG_OK;
 }
 
@@ -248,38 +276,111 @@ void make_trials(const fg_system *h, int64_t n, const int32_t *idx, const double
     }
 }
 
+// Pair part of the total energy (device) in kT.
+int pair_energy(fg_system *h, double &out) {
+    const int nb = 1024;
+    using PairFn = void (*)(const SysDesc *, float2 *);
+    PairFn fn = h->model == FG_MODEL_EWALD_WCA ? fg::pair_total_kernel<fg::MODEL_EWALD>
+                                                : fg::pair_total_kernel<fg::MODEL_DHLJ>;
+    fn<<<nb, 256, 0, h->stream>>>(h->d_desc, h->pair_part);
+    CK(cudaGetLastError());
+    std::vector<float2> part(nb);
+    CK(cudaMemcpyAsync(part.data(), h->pair_part, nb * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    double s = 0;
+    for (auto &p : part) s += df_val(p.x, p.y);
+    out = s;
+    return FG_OK;
+}
+
+int get_qk_host(fg_system *h, std::vector<double> &q) {
+    q.assign(2 * (size_t)h->K, 0.0);
+    if (h->K == 0) return FG_OK;
+    std::vector<longlong2> v(h->K);
+    CK(cudaMemcpyAsync(v.data(), h->qfix, v.size() * sizeof(longlong2), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < h->K; k++) {
+        q[2 * k] = (double)v[k].x * (1.0 / 1099511627776.0);
+        q[2 * k + 1] = (double)v[k].y * (1.0 / 1099511627776.0);
+    }
+    return FG_OK;
+}
+
+// {pairs, reciprocal, self, surface, total} in kT
+int total_energy(fg_system *h, double *c) {
+    double pairs = 0;
+    int rc = pair_energy(h, pairs);
+    if (rc) return rc;
+    double rec = 0, self = 0, surf = 0;
+    if (h->K > 0) {
+        std::vector<double> q;
+        rc = get_qk_host(h, q);
+        if (rc) return rc;
+        for (int k = 0; k < h->K; k++) rec += h->ak[k] * (q[2 * k] * q[2 * k] + q[2 * k + 1] * q[2 * k + 1]);
+        rec *= h->recip_c;
+        self = h->self_energy;
+        SysScalars s;
+        rc = read_scalars(h, s);
+        if (rc) return rc;
+        double M2 = 0;
+        for (int a = 0; a < 3; a++) {
+            double m = df_val(s.m[a][0], s.m[a][1]);
+            M2 += m * m;
+        }
+        surf = h->surf_c * M2;
+    }
+    c[0] = pairs;
+    c[1] = rec;
+    c[2] = self;
+    c[3] = surf;
+    c[4] = (surf + rec) + (self + pairs);
+    return FG_OK;
+}
+
+// Launch config for the sweep of one system (and its batch peers).
+struct LaunchCfg {
+    SweepFn fn;
+    int threads;
+    size_t smem;
+};
+int sweep_config(const fg_system *h, LaunchCfg &c) {
+    c.fn = sweep_fn(h);
+    c.threads = sweep_threads(h);
+    c.smem = sweep_smem(h, h->pos_smem);
+    return set_smem_attr((const void *)c.fn, c.smem);
+}
+
+// Run trials [0, n) of the staged stream (sweep + rebuild until done).
 int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
     SysScalars s0;
     int rc = read_scalars(h, s0);
     if (rc) return rc;
-    // start a fresh stream: cursor 0, energy change accumulator 0
     s0.cursor = 0;
     s0.n_trials = n;
-    int64_t acc0 = s0.n_accepted;
+    const int64_t acc0 = s0.n_accepted;
+    const int rb0 = s0.n_rebuilds;
     s0.u_hi = 0.0f;
     s0.u_lo = 0.0f;
-    CK(cudaMemcpyAsync(h->sc, &s0, sizeof(SysScalars), cudaMemcpyHostToDevice, h->stream));
+    rc = write_scalars(h, s0);
+    if (rc) return rc;
     h->desc.trials = h->trials;
     h->desc.log_trials = log ? 1 : 0;
     h->desc.trial_du = h->log_du;
     h->desc.trial_acc = h->log_acc;
     rc = push_desc(h);
     if (rc) return rc;
-    const int T = pick_threads(h);
-    if ((int64_t)T * fg::kMaxKPerThread < h->K) return fail(FG_ERR_CAPACITY, "too many k-vectors (%d)", h->K);
-    SweepFn fn = sweep_fn(h);
-    size_t sm = sweep_smem(h);
-    CK(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    const int uf = h->P.ewald_update_frequency;
-    const int rb0 = s0.n_rebuilds;
+    LaunchCfg cfg;
+    rc = sweep_config(h, cfg);
+    if (rc) return rc;
+    const bool rebuilds = h->K > 0 && !h->desc.skip_rebuild;
+    const int uf = std::max(h->P.ewald_update_frequency, 1);
     int launches = 0;
     std::vector<cudaEvent_t> evs;
     CK(cudaEventRecord(h->ev0, h->stream));
     SysScalars s = s0;
     while (true) {
         // enough sweep/rebuild pairs for the worst case (every trial accepted)
-        int pairs = 1;
-        if (h->model == FG_MODEL_EWALD_WCA) pairs = (int)std::min<int64_t>(n / std::max(uf, 1) + 1, 64);
+        const int pairs = rebuilds ? (int)std::min<int64_t>((n - s.cursor) / uf + 1, 64) : 1;
         for (int p = 0; p < pairs; p++) {
             cudaEvent_t a, b;
             CK(cudaEventCreate(&a));
@@ -287,21 +388,21 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
             evs.push_back(a);
             evs.push_back(b);
             CK(cudaEventRecord(a, h->stream));
-            fn<<<1, T, sm, h->stream>>>(h->d_desc, n, h->sc_tab);
+            cfg.fn<<<1, cfg.threads, cfg.smem, h->stream>>>(h->d_desc, n, h->sc_tab);
             CK(cudaGetLastError());
             CK(cudaEventRecord(b, h->stream));
             launches++;
-            if (h->model == FG_MODEL_EWALD_WCA) {
-                rc = launch_rebuild(h);
+            if (rebuilds) {
+                rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
                 if (rc) return rc;
             }
         }
-        int64_t before = s.cursor;
+        const int64_t before = s.cursor;
         rc = read_scalars(h, s);
         if (rc) return rc;
         if (s.error) break;
         if (s.cursor >= n && !s.rebuild_pending) break;
-        if (launches > pairs && s.cursor == before && !s.rebuild_pending)
+        if (s.cursor == before && !s.rebuild_pending)
             return fail(FG_ERR_DEVICE, "sweep made no progress at trial %lld", (long long)s.cursor);
     }
     CK(cudaEventRecord(h->ev1, h->stream));
@@ -315,15 +416,16 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
         cudaEventDestroy(evs[e]);
         cudaEventDestroy(evs[e + 1]);
     }
+    h->cnt_accepted_host = s.cnt_accepted;
     if (stats) {
         stats->trials = s.cursor;
         stats->accepted = s.n_accepted - acc0;
-        stats->energy_change = (double)s.u_hi + (double)s.u_lo;
+        stats->rebuilds = s.n_rebuilds - rb0;
+        stats->energy_change = df_val(s.u_hi, s.u_lo);
         stats->device_ms = total_ms;
         stats->sweep_kernel_ms = sweep_ms;
         stats->sweep_launches = launches;
         stats->error_flags = s.error;
-        stats->rebuilds = s.n_rebuilds - rb0;
     }
     if (s.error) return fail(FG_ERR_DEVICE, "device error flags 0x%x", s.error);
     return FG_OK;
@@ -333,7 +435,7 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
 
 extern "C" {
 
-int fg_version(void) { return 100; }
+int fg_version(void) { return 200; }
 
 const char *fg_last_error(void) { return g_err.c_str(); }
 
@@ -354,11 +456,20 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         if (!(P.box[a] > 0)) return fail(FG_ERR_INVALID, "box must be positive");
     if (P.model == FG_MODEL_DH_LJ && (P.box[1] != P.box[0] || P.box[2] != P.box[0]))
         return fail(FG_ERR_INVALID, "Debye-Hueckel systems need a cubic box");
+    if (P.model == FG_MODEL_EWALD_WCA) {
+        if (!(P.ewald_alpha > 0) || !(P.ewald_cutoff > 0) || !(P.ewald_debye_length > 0))
+            return fail(FG_ERR_INVALID, "Ewald needs alpha, cutoff and debye_length > 0");
+        for (int i = 0; i < P.n_types; i++)
+            if (P.type_charge[i] == 0.0)
+                return fail(FG_ERR_INVALID, "Ewald effective charges need non-zero type charges (ewald.h:539)");
+        if (std::ceil(P.ewald_cutoff_k) > 127) return fail(FG_ERR_INVALID, "cutoffK too large");
+    } else if (!(P.dh_debye_length > 0)) {
+        return fail(FG_ERR_INVALID, "dh_debye_length must be > 0");
+    }
     fg_system *h = new fg_system();
     h->P = P;
     h->N = n_particles;
     h->model = P.model;
-    int rc = FG_OK;
     auto bail = [&](int code) {
         free_all(h);
         delete h;
@@ -369,8 +480,6 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         return bail(fail(FG_ERR_CUDA, "stream create failed"));
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
-    cudaEventCreate(&h->ek0);
-    cudaEventCreate(&h->ek1);
 
     SysDesc &d = h->desc;
     std::memset(&d, 0, sizeof(d));
@@ -382,25 +491,18 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         d.s32[a] = (float)(P.box[a] / 4294967296.0);
         d.dl32[a] = (float)(P.box[a] / TWO64);
     }
-    d.lB = (float)P.bjerrum;
     d.s32sq = (float)((P.box[0] / 4294967296.0) * (P.box[0] / 4294967296.0));
+    d.lB = (float)P.bjerrum;
     d.kT = (float)(P.kT_scale > 0 ? P.kT_scale : 1.0);
     d.update_frequency = P.ewald_update_frequency;
     const int nt = P.n_types;
-    bool uniform = true;
     double kappa = 0;
     if (P.model == FG_MODEL_EWALD_WCA) {
-        if (!(P.ewald_alpha > 0) || !(P.ewald_cutoff > 0) || !(P.ewald_debye_length > 0))
-            return bail(fail(FG_ERR_INVALID, "Ewald needs alpha, cutoff and debye_length > 0"));
         kappa = 1.0 / P.ewald_debye_length;
         d.alpha = (float)P.ewald_alpha;
         d.rc2 = (float)(P.ewald_cutoff * P.ewald_cutoff);
         d.kappa = (kappa * P.ewald_cutoff < 1e-7) ? 0.0f : (float)kappa;
-        for (int i = 0; i < nt; i++)
-            if (P.type_charge[i] == 0.0)
-                return bail(fail(FG_ERR_INVALID, "Ewald effective charges need non-zero type charges (ewald.h:539)"));
     } else {
-        if (!(P.dh_debye_length > 0)) return bail(fail(FG_ERR_INVALID, "dh_debye_length must be > 0"));
         d.kappa = (float)(1.0 / P.dh_debye_length);
         d.rc2 = 3.0e38f;
     }
@@ -409,10 +511,13 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     std::vector<double> eff(nt, 1.0);
     for (int i = 0; i < nt; i++) {
         double ri = 0.5 * P.type_sigma[i], qis = P.type_charge[i];
-        if (P.model == FG_MODEL_EWALD_WCA && std::fabs(kappa * ri) > 1e-9) qis *= std::sinh(ri * kappa) / ri / kappa;
-        if (P.model == FG_MODEL_EWALD_WCA) eff[i] = qis / P.type_charge[i];
+        if (P.model == FG_MODEL_EWALD_WCA) {
+            if (std::fabs(kappa * ri) > 1e-9) qis *= std::sinh(ri * kappa) / ri / kappa;
+            eff[i] = qis / P.type_charge[i];
+        }
         d.eff[i] = (float)eff[i];
     }
+    bool uniform = true;
     for (int i = 0; i < nt; i++)
         for (int j = 0; j < nt; j++) {
             double sig = 0.5 * (P.type_sigma[i] + P.type_sigma[j]);
@@ -431,15 +536,14 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
 
     // Ewald k-space
     std::vector<int> n3;
-    std::vector<double> ak, kv3;
-    double V = P.box[0] * P.box[1] * P.box[2];
+    std::vector<double> kv3;
+    const double V = P.box[0] * P.box[1] * P.box[2];
     if (P.model == FG_MODEL_EWALD_WCA) {
-        enumerate_k(P, n3, ak, kv3);
-        h->K = (int)ak.size();
+        enumerate_k(P, n3, h->ak, kv3);
+        h->K = (int)h->ak.size();
         h->kc = (int)std::ceil(P.ewald_cutoff_k);
-        if (h->kc > 127) return bail(fail(FG_ERR_INVALID, "cutoffK too large"));
         h->recip_c = 2 * PI / V * P.bjerrum;
-        double const_inf = (P.ewald_eps_surf < 1) ? 0.0 : 1.0;
+        const double const_inf = (P.ewald_eps_surf < 1) ? 0.0 : 1.0;
         h->surf_c = const_inf * (2 * PI / ((2 * P.ewald_eps_surf + 1) * V)) * P.bjerrum;
         d.surf_c = (float)h->surf_c;
     }
@@ -449,9 +553,8 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         int nc[3];
         for (int a = 0; a < 3; a++) nc[a] = (int)std::floor(P.box[a] / P.ewald_cutoff);
         // a stencil spans up to 4 cells per axis, so 4 distinct cells are needed
-        bool can = nc[0] >= 4 && nc[1] >= 4 && nc[2] >= 4;
-        bool want = (P.use_cell_list == 1) || (P.use_cell_list == 0 && n_particles >= 4096 && nc[0] >= 4 &&
-                                               nc[1] >= 4 && nc[2] >= 4);
+        bool can = nc[0] >= 4 && nc[1] >= 4 && nc[2] >= 4 && (long)nc[0] * nc[1] * nc[2] < (1 << 20);
+        bool want = (P.use_cell_list == 1) || (P.use_cell_list == 0 && n_particles >= 4096);
         if (P.use_cell_list == 1 && !can) return bail(fail(FG_ERR_INVALID, "cell list needs >= 4 cells per axis"));
         h->use_cells = can && want;
         if (h->use_cells)
@@ -460,53 +563,49 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     d.use_cells = h->use_cells ? 1 : 0;
     for (int a = 0; a < 3; a++) d.nc[a] = h->nc[a];
     // positions in shared memory when they fit next to the k-space tables
-    size_t sm_pos = smem_bytes(n_particles, h->K, true, P.model == FG_MODEL_EWALD_WCA);
-    h->pos_smem = !h->use_cells && sm_pos <= 200 * 1024;
+    h->pos_smem = !h->use_cells && sweep_smem(h, true) <= 200 * 1024;
 
     const int N = n_particles;
-#define ALLOC(ptr, bytes)                                                                \
-    do {                                                                                 \
-        if (cudaMalloc(&(ptr), (bytes)) != cudaSuccess)                                  \
-            return bail(fail(FG_ERR_CUDA, "cudaMalloc of %zu bytes failed", (size_t)(bytes))); \
+    int rc;
+#define ALLOC(ptr, bytes)                          \
+    do {                                           \
+        rc = dmalloc(h, (void **)&(ptr), (bytes)); \
+        if (rc) return bail(rc);                   \
     } while (0)
     ALLOC(h->d_desc, sizeof(SysDesc));
     ALLOC(h->pos64, (size_t)N * 3 * sizeof(int64_t));
     ALLOC(h->pos4, (size_t)N * sizeof(int4));
-    ALLOC(h->ptype, (size_t)N);
     ALLOC(h->pos_ext, (size_t)N * sizeof(short4));
+    ALLOC(h->ptype, (size_t)N);
     ALLOC(h->sc, sizeof(SysScalars));
     ALLOC(h->req, 8 * sizeof(int64_t));
     ALLOC(h->trial_out, 4 * sizeof(float2));
-    ALLOC(h->energy_out, 4 * sizeof(float2));
-    ALLOC(h->flags, 4 * sizeof(int32_t));
+    ALLOC(h->corr, 4 * sizeof(float2));
     ALLOC(h->sc_tab, 256 * sizeof(float2));
     ALLOC(h->dp_fix, FG_MAX_TYPES * 3 * sizeof(int64_t));
     ALLOC(h->pair_part, 1024 * sizeof(float2));
     if (h->K > 0) {
         ALLOC(h->kvec, (size_t)h->K * sizeof(float4));
-        ALLOC(h->qk, (size_t)h->K * sizeof(float4));
         ALLOC(h->kpack, (size_t)h->K * sizeof(uint32_t));
-        ALLOC(h->pending_dq, (size_t)h->K * sizeof(float2));
-        const int per = (h->kc + 1) + 2 * (2 * h->kc + 1);
-        ALLOC(h->axis_tab, (size_t)N * per * sizeof(float4));
-        h->chunk = 128;
-        h->nchunk = (N + h->chunk - 1) / h->chunk;
-        ALLOC(h->qk_part, (size_t)h->nchunk * h->K * sizeof(float4));
+        ALLOC(h->qfix, (size_t)h->K * sizeof(longlong2));
+        ALLOC(h->qnew, (size_t)h->K * sizeof(longlong2));
         std::vector<float4> kv(h->K);
         std::vector<uint32_t> kp(h->K);
         for (int k = 0; k < h->K; k++) {
             kv[k] = make_float4((float)kv3[3 * k], (float)kv3[3 * k + 1], (float)kv3[3 * k + 2],
-                                (float)(ak[k] * h->recip_c));
+                                (float)(h->ak[k] * h->recip_c));
             kp[k] = (uint32_t)(n3[3 * k] & 0xFF) | ((uint32_t)(n3[3 * k + 1] & 0xFF) << 8) |
                     ((uint32_t)(n3[3 * k + 2] & 0xFF) << 16);
         }
         cudaMemcpy(h->kvec, kv.data(), h->K * sizeof(float4), cudaMemcpyHostToDevice);
         cudaMemcpy(h->kpack, kp.data(), h->K * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        cudaMemset(h->qfix, 0, h->K * sizeof(longlong2));
+        cudaMemset(h->qnew, 0, h->K * sizeof(longlong2));
     }
     if (h->use_cells) {
-        int ncell = h->nc[0] * h->nc[1] * h->nc[2];
-        double avg = (double)N / ncell;
-        h->cap = std::max(64, (int)(((int)(2.5 * avg) + 32 + 31) / 32 * 32));
+        const int ncell = h->nc[0] * h->nc[1] * h->nc[2];
+        const double avg = (double)N / ncell;
+        h->cap = std::min(4095, std::max(64, (((int)(2.5 * avg) + 32 + 31) / 32) * 32));
         ALLOC(h->cell_count, (size_t)ncell * sizeof(int32_t));
         ALLOC(h->cell_pid, (size_t)ncell * h->cap * sizeof(int32_t));
         ALLOC(h->cell_pos, (size_t)ncell * h->cap * sizeof(int4));
@@ -515,22 +614,23 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         ALLOC(h->p_slot, (size_t)N * sizeof(int32_t));
     }
     // Taylor table of g(y) for core pairs: erfc (Ewald, kappa = 0) or exp(-y)
-    // (Debye-Hueckel) at y0 = j/128, entries f0, f1 as df and f2/2, f3/6, f4/24
+    // (Debye-Hueckel) at y0 = j/128; entries f0, f1 as df, f2/2, f3/6, f4/24
     {
-        double coef = P.model == FG_MODEL_EWALD_WCA ? P.ewald_alpha : 1.0 / P.dh_debye_length;
-        bool ok = P.model == FG_MODEL_DH_LJ || d.kappa == 0.0f;
+        const double coef = P.model == FG_MODEL_EWALD_WCA ? P.ewald_alpha : 1.0 / P.dh_debye_length;
+        const bool ok = P.model == FG_MODEL_DH_LJ || d.kappa == 0.0f;
         double smax = 0;
         for (int i = 0; i < nt; i++) smax = std::max(smax, P.type_sigma[i]);
-        int nt_ab = ok && smax > 0 ? (int)std::ceil(coef * smax * 128.0) + 4 : 0;
-        if (nt_ab > 0) {
-            ALLOC(h->core_tab, (size_t)nt_ab * sizeof(float4));
-            ALLOC(h->core_tab2, (size_t)nt_ab * sizeof(float4));
-            std::vector<float4> t0(nt_ab), t1(nt_ab);
+        const int ntab = ok && smax > 0 ? (int)std::ceil(coef * smax * 128.0) + 4 : 0;
+        if (ntab > 0) {
+            ALLOC(h->core_tab, (size_t)ntab * sizeof(float4));
+            ALLOC(h->core_tab2, (size_t)ntab * sizeof(float4));
+            std::vector<float4> t0(ntab), t1(ntab);
             const double k = 2.0 / std::sqrt(PI);
-            for (int j = 0; j < nt_ab; j++) {
-                double y = j / 128.0, f0, f1, f2, f3, f4;
+            for (int j = 0; j < ntab; j++) {
+                const double y = j / 128.0;
+                double f0, f1, f2, f3, f4;
                 if (P.model == FG_MODEL_EWALD_WCA) {
-                    double e = std::exp(-y * y);
+                    const double e = std::exp(-y * y);
                     f0 = std::erfc(y);
                     f1 = -k * e;
                     f2 = 2 * k * y * e;
@@ -540,14 +640,14 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
                     f0 = std::exp(-y);
                     f1 = -f0; f2 = f0; f3 = -f0; f4 = f0;
                 }
-                float2 a = split_df(f0), b = split_df(f1);
+                const float2 a = split_df(f0), b = split_df(f1);
                 t0[j] = make_float4(a.x, a.y, b.x, b.y);
                 t1[j] = make_float4((float)(f2 / 2), (float)(f3 / 6), (float)(f4 / 24), 0.0f);
             }
-            cudaMemcpy(h->core_tab, t0.data(), nt_ab * sizeof(float4), cudaMemcpyHostToDevice);
-            cudaMemcpy(h->core_tab2, t1.data(), nt_ab * sizeof(float4), cudaMemcpyHostToDevice);
+            cudaMemcpy(h->core_tab, t0.data(), ntab * sizeof(float4), cudaMemcpyHostToDevice);
+            cudaMemcpy(h->core_tab2, t1.data(), ntab * sizeof(float4), cudaMemcpyHostToDevice);
         }
-        d.core_tab_n = nt_ab;
+        d.core_tab_n = ntab;
         d.core_tab = h->core_tab;
         d.core_tab2 = h->core_tab2;
         d.coef_df = split_df(coef);
@@ -555,36 +655,39 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     }
 #undef ALLOC
     d.cap = h->cap;
-    d.pos_ext = h->pos_ext;
-    d.cell_ext = h->cell_ext;
     d.pos64 = h->pos64;
     d.pos4 = h->pos4;
+    d.pos_ext = h->pos_ext;
     d.ptype = h->ptype;
     d.cell_count = h->cell_count;
     d.cell_pos = h->cell_pos;
+    d.cell_ext = h->cell_ext;
     d.cell_pid = h->cell_pid;
     d.p_cell = h->p_cell;
     d.p_slot = h->p_slot;
     d.kvec = h->kvec;
     d.kpack = h->kpack;
-    d.qk = h->qk;
+    d.qfix = h->qfix;
+    d.qnew = h->qnew;
     d.sc = h->sc;
-    d.pending_dq = h->pending_dq;
-    // sincos table at multiples of 2*pi/256
+    d.sc_tab = h->sc_tab;
+    d.dp_fix = h->dp_fix;
+    // cos/sin table at multiples of 2*pi/256
     std::vector<float2> tab(256);
     for (int i = 0; i < 256; i++) tab[i] = make_float2((float)std::cos(2 * PI * i / 256), (float)std::sin(2 * PI * i / 256));
     cudaMemcpy(h->sc_tab, tab.data(), sizeof(float2) * 256, cudaMemcpyHostToDevice);
-    // displacement parameters in fixed point (Philox streams)
+    // displacement parameters in fixed point (device-generated streams)
     std::vector<int64_t> dpf(FG_MAX_TYPES * 3, 0);
     for (int t = 0; t < nt; t++)
         for (int a = 0; a < 3; a++) dpf[3 * t + a] = (int64_t)llrint(P.type_dp[t] / P.box[a] * 4294967296.0);
     cudaMemcpy(h->dp_fix, dpf.data(), dpf.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
     SysScalars s0{};
+    s0.verify_rebuild = 1;
     cudaMemcpy(h->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice);
     rc = push_desc(h);
     if (rc) return bail(rc);
-    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(FG_ERR_CUDA, "setup failed"));
-    if (cudaGetLastError() != cudaSuccess) return bail(fail(FG_ERR_CUDA, "setup failed"));
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return bail(fail(FG_ERR_CUDA, "setup failed"));
     *out = h;
     return FG_OK;
 }
@@ -605,14 +708,12 @@ int fg_set_state(fg_system *h, const double *xyz, const double *charge, const in
     std::vector<int4> p4(N);
     std::vector<short4> pe(N);
     std::vector<uint8_t> pt(N);
-    h->charge.assign(N, 0.0);
     h->types.assign(type_ids, type_ids + N);
     double self = 0, M[3] = {0, 0, 0};
     for (int i = 0; i < N; i++) {
-        int t = type_ids[i];
+        const int t = type_ids[i];
         if (t < 0 || t >= P.n_types) return fail(FG_ERR_INVALID, "type id %d out of range", t);
-        double q = charge ? charge[i] : P.type_charge[t];
-        h->charge[i] = q;
+        const double q = charge ? charge[i] : P.type_charge[t];
         int32_t hw[3];
         for (int a = 0; a < 3; a++) {
             if (!std::isfinite(xyz[3 * i + a])) return fail(FG_ERR_INVALID, "non-finite coordinate");
@@ -621,12 +722,12 @@ int fg_set_state(fg_system *h, const double *xyz, const double *charge, const in
             // surface dipole over wrapped positions (ewald.h:277-291)
             M[a] += q * h->desc.eff[t] * from_fix(p64[3 * i + a], P.box[a]);
         }
-        float qf = (float)q;
+        const float qf = (float)q;
         p4[i] = make_int4(hw[0], hw[1], hw[2], 0);
-        pe[i] = make_short4(ext16h(p64[3 * i]), ext16h(p64[3 * i + 1]), ext16h(p64[3 * i + 2]), 0);
         std::memcpy(&p4[i].w, &qf, 4);
+        pe[i] = make_short4(ext16h(p64[3 * i]), ext16h(p64[3 * i + 1]), ext16h(p64[3 * i + 2]), 0);
         pt[i] = (uint8_t)t;
-        double e = h->desc.eff[t];
+        const double e = h->desc.eff[t];
         self += q * q * e * e;
     }
     h->self_energy = (-P.ewald_alpha * self / std::sqrt(PI)) * P.bjerrum;
@@ -635,14 +736,14 @@ int fg_set_state(fg_system *h, const double *xyz, const double *charge, const in
     CK(cudaMemcpyAsync(h->ptype, pt.data(), pt.size(), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->pos_ext, pe.data(), pe.size() * sizeof(short4), cudaMemcpyHostToDevice, h->stream));
     if (h->use_cells) {
-        int ncell = h->nc[0] * h->nc[1] * h->nc[2];
+        const int ncell = h->nc[0] * h->nc[1] * h->nc[2];
         std::vector<int32_t> cnt(ncell, 0), pid((size_t)ncell * h->cap, -1), pc(N), ps(N);
         std::vector<int4> cp((size_t)ncell * h->cap, make_int4(0, 0, 0, 0));
         std::vector<short4> ce((size_t)ncell * h->cap, make_short4(0, 0, 0, 0));
         for (int i = 0; i < N; i++) {
-            int c = cell_of_h(&p64[3 * i], h->nc);
+            const int c = cell_of_h(&p64[3 * i], h->nc);
             if (cnt[c] >= h->cap) return fail(FG_ERR_CAPACITY, "cell %d over capacity %d", c, h->cap);
-            int s = cnt[c]++;
+            const int s = cnt[c]++;
             cp[(size_t)c * h->cap + s] = p4[i];
             ce[(size_t)c * h->cap + s] = pe[i];
             pid[(size_t)c * h->cap + s] = i | (type_ids[i] << 24);
@@ -659,27 +760,36 @@ int fg_set_state(fg_system *h, const double *xyz, const double *charge, const in
     }
     SysScalars s0{};
     for (int a = 0; a < 3; a++) {
-        float hi = (float)M[a];
-        s0.m[a][0] = hi;
-        s0.m[a][1] = (float)(M[a] - (double)hi);
+        const float2 m = split_df(M[a]);
+        s0.m[a][0] = m.x;
+        s0.m[a][1] = m.y;
     }
+    int rc;
     if (h->K > 0) {
-        CK(cudaMemsetAsync(h->qk, 0, (size_t)h->K * sizeof(float4), h->stream));
+        // Q(k) from scratch: adopt the rebuild without the equality check
+        CK(cudaMemsetAsync(h->qfix, 0, (size_t)h->K * sizeof(longlong2), h->stream));
+        CK(cudaMemsetAsync(h->qnew, 0, (size_t)h->K * sizeof(longlong2), h->stream));
         s0.rebuild_pending = 1;
+        s0.verify_rebuild = 0;
+        rc = write_scalars(h, s0);
+        if (rc) return rc;
+        rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
+        if (rc) return rc;
     }
-    CK(cudaMemcpyAsync(h->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice, h->stream));
-    int rc = launch_rebuild(h);
+    s0.rebuild_pending = 0;
+    s0.verify_rebuild = 1;
+    s0.n_rebuilds = 0;
+    rc = write_scalars(h, s0);
     if (rc) return rc;
-    // the initial build is not a drift correction: start the running sum at 0
-    SysScalars s1;
-    rc = read_scalars(h, s1);
+    // running total energy starts at systemEnergy of the uploaded state
+    double c[5];
+    rc = total_energy(h, c);
     if (rc) return rc;
-    s1.u_hi = 0;
-    s1.u_lo = 0;
-    s1.cnt_accepted = 0;
-    s1.n_accepted = 0;
-    CK(cudaMemcpyAsync(h->sc, &s1, sizeof(s1), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
+    const float2 ut = split_df(c[4]);
+    s0.utot_hi = ut.x;
+    s0.utot_lo = ut.y;
+    rc = write_scalars(h, s0);
+    if (rc) return rc;
     h->cnt_accepted_host = 0;
     h->trial_pending = false;
     h->state_set = true;
@@ -699,37 +809,41 @@ int fg_get_state(fg_system *h, double *xyz) {
 int fg_num_kvectors(fg_system *h) { return h ? h->K : 0; }
 
 int fg_set_threads(fg_system *h, int32_t threads) {
-    if (!h || threads < 0 || threads > 1024 || (threads % 32) != 0) return fail(FG_ERR_INVALID, "threads");
-    if (threads > 0 && threads * fg::kMaxKPerThread < h->K)
-        return fail(FG_ERR_CAPACITY, "%d threads cannot hold %d k-vectors", threads, h->K);
+    if (!h || threads < 0 || threads > fg::kSweepThreads || (threads % 32) != 0)
+        return fail(FG_ERR_INVALID, "threads must be a multiple of 32 in [0, %d]", fg::kSweepThreads);
     h->threads = threads;
     return FG_OK;
 }
 
-int fg_get_threads(fg_system *h) { return h ? pick_threads(h) : 0; }
+int fg_get_threads(fg_system *h) { return h ? sweep_threads(h) : 0; }
+
+int fg_set_rebuild_policy(fg_system *h, int32_t skip) {
+    if (!h) return fail(FG_ERR_INVALID, "null handle");
+    h->desc.skip_rebuild = skip ? 1 : 0;
+    return push_desc(h);
+}
 
 int fg_trial_du(fg_system *h, int32_t n_moved, const int32_t *idx, const double *new_xyz, double *du) {
     if (!h || !idx || !new_xyz || !du) return fail(FG_ERR_INVALID, "null argument");
     if (!h->state_set) return fail(FG_ERR_STATE, "fg_set_state first");
     if (n_moved != 1) return fail(FG_ERR_INVALID, "atomic systems move one particle per trial");
     if (idx[0] < 0 || idx[0] >= h->N) return fail(FG_ERR_INVALID, "particle index out of range");
-    int64_t req[4] = {idx[0], to_fix(new_xyz[0], h->P.box[0]), to_fix(new_xyz[1], h->P.box[1]),
-                      to_fix(new_xyz[2], h->P.box[2])};
+    for (int a = 0; a < 3; a++)
+        if (!std::isfinite(new_xyz[a])) return fail(FG_ERR_INVALID, "non-finite coordinate");
+    const int64_t req[4] = {idx[0], to_fix(new_xyz[0], h->P.box[0]), to_fix(new_xyz[1], h->P.box[1]),
+                            to_fix(new_xyz[2], h->P.box[2])};
     CK(cudaMemcpyAsync(h->req, req, sizeof(req), cudaMemcpyHostToDevice, h->stream));
-    const int T = pick_threads(h);
-    if ((int64_t)T * fg::kMaxKPerThread < h->K) return fail(FG_ERR_CAPACITY, "too many k-vectors (%d)", h->K);
-    const bool ks = h->model == FG_MODEL_EWALD_WCA;
-    size_t sm = smem_bytes(h->N, h->K, false, ks);
-    using TrialFn = void (*)(const SysDesc *, const int64_t *, float2 *, const float2 *);
-    TrialFn fn = ks ? (h->use_cells ? fg::trial_kernel<fg::MODEL_EWALD, true> : fg::trial_kernel<fg::MODEL_EWALD, false>)
-                    : fg::trial_kernel<fg::MODEL_DHLJ, false>;
-    CK(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int T = sweep_threads(h);
+    const size_t sm = sweep_smem(h, false);
+    TrialFn fn = trial_fn(h);
+    int rc = set_smem_attr((const void *)fn, sm);
+    if (rc) return rc;
     fn<<<1, T, sm, h->stream>>>(h->d_desc, h->req, h->trial_out, h->sc_tab);
     CK(cudaGetLastError());
     float2 out[3];
     CK(cudaMemcpyAsync(out, h->trial_out, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    *du = (double)out[0].x + (double)out[0].y;
+    *du = df_val(out[0].x, out[0].y);
     h->trial_pending = true;
     return FG_OK;
 }
@@ -739,22 +853,30 @@ int fg_commit(fg_system *h, int32_t accepted, double *correction) {
     if (!h->trial_pending) return fail(FG_ERR_STATE, "no pending trial");
     h->trial_pending = false;
     if (correction) *correction = 0.0;
-    using CommitFn = void (*)(const SysDesc *, const int64_t *, const float2 *, int, int32_t *);
-    CommitFn fn = h->model == FG_MODEL_EWALD_WCA ? fg::commit_kernel<fg::MODEL_EWALD> : fg::commit_kernel<fg::MODEL_DHLJ>;
-    int blocks = std::max(1, std::min(64, (h->K + 255) / 256));
-    fn<<<blocks, 256, 0, h->stream>>>(h->d_desc, h->req, h->trial_out, accepted ? 1 : 0, h->flags);
+    if (!accepted) return FG_OK;
+    const int T = sweep_threads(h);
+    const size_t sm = sweep_smem(h, false);
+    CommitFn fn = commit_fn(h);
+    int rc = set_smem_attr((const void *)fn, sm);
+    if (rc) return rc;
+    fn<<<1, T, sm, h->stream>>>(h->d_desc, h->req, h->trial_out, h->sc_tab);
     CK(cudaGetLastError());
-    if (accepted && h->model == FG_MODEL_EWALD_WCA) {
-        // the host mirrors the rebuild counter, so no read-back is needed
-        // unless a rebuild is due (NonbondedEwald::update, ewald.h:633)
+    if (h->model == FG_MODEL_EWALD_WCA && !h->desc.skip_rebuild) {
+        // the host mirrors the rebuild counter (NonbondedEwald::update, ewald.h:633)
         if (++h->cnt_accepted_host > h->P.ewald_update_frequency - 1) {
             h->cnt_accepted_host = 0;
-            int rc = launch_rebuild(h);
+            const int one = 1;
+            CK(cudaMemcpyAsync(&h->sc->rebuild_pending, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+            rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
             if (rc) return rc;
-            float2 e[2];
-            CK(cudaMemcpyAsync(e, h->energy_out, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+            float2 e;
+            CK(cudaMemcpyAsync(&e, h->corr, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
             CK(cudaStreamSynchronize(h->stream));
-            if (correction) *correction = (double)e[1].x + (double)e[1].y;
+            if (correction) *correction = df_val(e.x, e.y);
+            SysScalars s;
+            rc = read_scalars(h, s);
+            if (rc) return rc;
+            if (s.error) return fail(FG_ERR_DEVICE, "device error flags 0x%x", s.error);
         }
     }
     return FG_OK;
@@ -764,68 +886,41 @@ int fg_rebuild_qk(fg_system *h, double *correction) {
     if (!h) return fail(FG_ERR_INVALID, "null handle");
     if (correction) *correction = 0.0;
     if (h->K == 0) return FG_OK;
-    int one = 1;
+    const int one = 1;
     CK(cudaMemcpyAsync(&h->sc->rebuild_pending, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    int rc = launch_rebuild(h);
+    int rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
     if (rc) return rc;
-    float2 e[2];
-    CK(cudaMemcpyAsync(e, h->energy_out, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+    float2 e;
+    CK(cudaMemcpyAsync(&e, h->corr, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    if (correction) *correction = (double)e[1].x + (double)e[1].y;
+    if (correction) *correction = df_val(e.x, e.y);
+    SysScalars s;
+    rc = read_scalars(h, s);
+    if (rc) return rc;
+    if (s.error) return fail(FG_ERR_DEVICE, "device error flags 0x%x", s.error);
     return FG_OK;
 }
 
 int fg_get_qk(fg_system *h, double *qk) {
     if (!h || !qk) return fail(FG_ERR_INVALID, "null argument");
-    std::vector<float4> q(h->K);
-    if (h->K == 0) return FG_OK;
-    CK(cudaMemcpyAsync(q.data(), h->qk, q.size() * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    for (int k = 0; k < h->K; k++) {
-        qk[2 * k] = (double)q[k].x + (double)q[k].y;
-        qk[2 * k + 1] = (double)q[k].z + (double)q[k].w;
-    }
+    std::vector<double> q;
+    int rc = get_qk_host(h, q);
+    if (rc) return rc;
+    std::copy(q.begin(), q.end(), qk);
     return FG_OK;
 }
 
 int fg_total_energy(fg_system *h, double *c) {
     if (!h || !c) return fail(FG_ERR_INVALID, "null argument");
-    const int nb = 1024;
-    using PairFn = void (*)(const SysDesc *, float2 *);
-    PairFn fn = h->model == FG_MODEL_EWALD_WCA ? fg::pair_total_kernel<fg::MODEL_EWALD> : fg::pair_total_kernel<fg::MODEL_DHLJ>;
-    fn<<<nb, 256, 0, h->stream>>>(h->d_desc, h->pair_part);
-    CK(cudaGetLastError());
-    std::vector<float2> part(nb);
-    CK(cudaMemcpyAsync(part.data(), h->pair_part, nb * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    double pairs = 0;
-    for (auto &p : part) pairs += (double)p.x + (double)p.y;
-    double rec = 0, self = 0, surf = 0;
-    if (h->K > 0) {
-        std::vector<double> q(2 * h->K);
-        int rc = fg_get_qk(h, q.data());
-        if (rc) return rc;
-        std::vector<int> n3;
-        std::vector<double> ak, kv3;
-        enumerate_k(h->P, n3, ak, kv3);
-        for (int k = 0; k < h->K; k++) rec += ak[k] * (q[2 * k] * q[2 * k] + q[2 * k + 1] * q[2 * k + 1]);
-        rec *= h->recip_c;
-        self = h->self_energy;
-        SysScalars s;
-        rc = read_scalars(h, s);
-        if (rc) return rc;
-        double M2 = 0;
-        for (int a = 0; a < 3; a++) {
-            double m = (double)s.m[a][0] + (double)s.m[a][1];
-            M2 += m * m;
-        }
-        surf = h->surf_c * M2;
-    }
-    c[0] = pairs;
-    c[1] = rec;
-    c[2] = self;
-    c[3] = surf;
-    c[4] = (surf + rec) + (self + pairs);
+    return total_energy(h, c);
+}
+
+int fg_running_energy(fg_system *h, double *u) {
+    if (!h || !u) return fail(FG_ERR_INVALID, "null argument");
+    SysScalars s;
+    int rc = read_scalars(h, s);
+    if (rc) return rc;
+    *u = df_val(s.utot_hi, s.utot_lo);
     return FG_OK;
 }
 
@@ -840,7 +935,7 @@ int fg_draw_translation_stream(fg_system *h, uint32_t seed, int64_t n, int32_t *
         { std::uniform_int_distribution<int> g(0, 0); g(eng); }            // slump.element(groups)
         int i;
         { std::uniform_int_distribution<int> g(0, h->N - 1); i = g(eng); } // Group::random
-        double dp = h->P.type_dp[h->types[i]];
+        const double dp = h->P.type_dp[h->types[i]];
         double tx = dp, ty = dp, tz = dp;                                   // dir * dp, dir = (1,1,1)
         tx *= uni(eng) - 0.5;
         ty *= uni(eng) - 0.5;
@@ -858,11 +953,11 @@ int fg_stream_upload(fg_system *h, int64_t n, const int32_t *idx, const double *
     if (!h || n < 0 || (n > 0 && (!idx || !disp || !u))) return fail(FG_ERR_INVALID, "bad argument");
     for (int64_t t = 0; t < n; t++)
         if (idx[t] < 0 || idx[t] >= h->N) return fail(FG_ERR_INVALID, "particle index out of range at %lld", (long long)t);
-    int rc = ensure_trials(h, std::max<int64_t>(n, 1), false);
+    int rc = ensure_trials(h, n, false);
     if (rc) return rc;
     std::vector<Trial> tr;
     make_trials(h, n, idx, disp, u, tr);
-    CK(cudaMemcpyAsync(h->trials, tr.data(), n * sizeof(Trial), cudaMemcpyHostToDevice, h->stream));
+    if (n > 0) CK(cudaMemcpyAsync(h->trials, tr.data(), n * sizeof(Trial), cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->n_trials = n;
     return FG_OK;
@@ -870,11 +965,11 @@ int fg_stream_upload(fg_system *h, int64_t n, const int32_t *idx, const double *
 
 int fg_stream_philox(fg_system *h, int64_t n, uint32_t seed, uint32_t stream_id) {
     if (!h || n < 0) return fail(FG_ERR_INVALID, "bad argument");
-    int rc = ensure_trials(h, std::max<int64_t>(n, 1), false);
+    int rc = ensure_trials(h, n, false);
     if (rc) return rc;
-    int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
-    if (n > 0) fg::philox_stream_kernel<<<std::max(blocks, 1), 256, 0, h->stream>>>(h->d_desc, seed, stream_id, 0, n,
-                                                                                    h->dp_fix, h->trials);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8));
+    if (n > 0)
+        fg::philox_stream_kernel<<<blocks, 256, 0, h->stream>>>(h->d_desc, seed, stream_id, 0, n, h->dp_fix, h->trials);
     CK(cudaGetLastError());
     h->n_trials = n;
     return FG_OK;
@@ -882,15 +977,15 @@ int fg_stream_philox(fg_system *h, int64_t n, uint32_t seed, uint32_t stream_id)
 
 int fg_stream_get(fg_system *h, int64_t first, int64_t n, int32_t *idx, double *disp, double *u) {
     if (!h || first < 0 || n < 0 || first + n > h->n_trials) return fail(FG_ERR_INVALID, "range outside the stream");
-    std::vector<Trial> tr(n);
     if (n == 0) return FG_OK;
+    std::vector<Trial> tr(n);
     CK(cudaMemcpyAsync(tr.data(), h->trials + first, n * sizeof(Trial), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (int64_t t = 0; t < n; t++) {
         if (idx) idx[t] = tr[t].idx;
         for (int a = 0; a < 3; a++)
             if (disp) disp[3 * t + a] = from_fix(tr[t].d[a], h->P.box[a]);
-        if (u) u[t] = std::exp(-((double)tr[t].thr_hi + (double)tr[t].thr_lo));
+        if (u) u[t] = std::exp(-df_val(tr[t].thr_hi, tr[t].thr_lo));
     }
     return FG_OK;
 }
@@ -909,27 +1004,22 @@ int fg_sweep(fg_system *h, int64_t n, const int32_t *idx, const double *disp, co
     if (h->trial_pending) return fail(FG_ERR_STATE, "commit the pending trial first");
     int rc = fg_stream_upload(h, n, idx, disp, u);
     if (rc) return rc;
-    bool log = accepted || du;
-    rc = ensure_trials(h, std::max<int64_t>(n, 1), log);
+    const bool log = accepted || du;
+    rc = ensure_trials(h, n, log);
     if (rc) return rc;
     rc = run_stream(h, n, log, stats);
     if (rc) return rc;
-    if (log) {
+    if (log && n > 0) {
         std::vector<float2> d(n);
         std::vector<uint8_t> a(n);
         CK(cudaMemcpyAsync(d.data(), h->log_du, n * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaMemcpyAsync(a.data(), h->log_acc, n, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
         for (int64_t t = 0; t < n; t++) {
-            if (du) du[t] = (double)d[t].x + (double)d[t].y;
+            if (du) du[t] = df_val(d[t].x, d[t].y);
             if (accepted) accepted[t] = a[t];
         }
     }
-    // keep the host copy of the rebuild counter in step with the device
-    SysScalars s;
-    rc = read_scalars(h, s);
-    if (rc) return rc;
-    h->cnt_accepted_host = s.cnt_accepted;
     return FG_OK;
 }
 
@@ -939,4 +1029,8 @@ int fg_synchronize(fg_system *h) {
     return FG_OK;
 }
 
+int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0; }
+
 }  // extern "C"
+
+#include "fg_batch.cu"

@@ -1,0 +1,727 @@
+// Batches, parallel tempering and the job server (included by fg_api.cu).
+//
+// A batch is a set of independent systems advanced by one launch of the
+// persistent sweep kernel (one CTA per system). Parallel tempering runs a
+// batch whose systems sit on a temperature ladder and exchanges temperatures
+// between neighbours on the device (the configuration exchange of
+// Move::ParallelTempering, move.h:6542-6771, as a label swap). The job
+// server admits Monte Carlo jobs by device-memory footprint and advances all
+// admitted jobs together in rounds (continuous batching).
+
+namespace fg {
+
+// Reset per-system scalars for a new stream of counts[s] trials.
+__global__ void batch_reset_kernel(const SysDesc *__restrict__ descs, int n, const int64_t *__restrict__ counts) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    SysScalars *sc = descs[s].sc;
+    sc->cursor = 0;
+    sc->n_trials = counts[s];
+    sc->u_hi = 0.0f;
+    sc->u_lo = 0.0f;
+}
+
+// Philox trial streams for all systems of a batch: system s gets counts[s]
+// trials with counters starting at descs[s].stream_first + round * counts[s]
+// (round read from the device, so a captured graph can be replayed).
+__global__ void batch_philox_kernel(const SysDesc *__restrict__ descs, const int64_t *__restrict__ counts,
+                                    const int64_t *__restrict__ round) {
+    const SysDesc &d = descs[blockIdx.y];
+    const int64_t n = counts[blockIdx.y];
+    const int64_t first = d.stream_first + (round ? *round : 0) * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = first + t;
+        const u4 r = philox4x32_10(u4{(uint32_t)g, (uint32_t)(g >> 32), 0u, 0u}, d.seed, d.stream_id);
+        const u4 r2 = philox4x32_10(u4{(uint32_t)g, (uint32_t)(g >> 32), 1u, 0u}, d.seed, d.stream_id);
+        Trial tr;
+        tr.idx = (int32_t)(((uint64_t)r.x * (uint32_t)d.N) >> 32);
+        tr.pad = 0;
+        const int ty = d.ptype[tr.idx];
+        tr.d[0] = (int64_t)(int32_t)(r.y - 0x80000000u) * d.dp_fix[3 * ty + 0];
+        tr.d[1] = (int64_t)(int32_t)(r.z - 0x80000000u) * d.dp_fix[3 * ty + 1];
+        tr.d[2] = (int64_t)(int32_t)(r.w - 0x80000000u) * d.dp_fix[3 * ty + 2];
+        const double u = ((double)r2.x + 0.5) * (1.0 / 4294967296.0);
+        const double thr = -log(u);
+        const float h = (float)thr;
+        tr.thr_hi = h;
+        tr.thr_lo = (float)(thr - (double)h);
+        const_cast<Trial *>(d.trials)[t] = tr;
+    }
+}
+
+__global__ void gather_scalars_kernel(const SysDesc *__restrict__ descs, int n, SysScalars *__restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) out[s] = *descs[s].sc;
+}
+
+// Temperature exchange between neighbouring rungs (findPartner, move.h:6621-6633:
+// one shared uniform picks the pairing (0,1)(2,3).. or (1,2)(3,4)..; then per
+// pair the Metropolis test on (beta_i - beta_j)(U_a - U_b), U_a the running
+// total energy of the system at rung i). perm[rung] = system; the swap
+// exchanges perm entries and the systems' kT. One thread; n is small.
+__global__ void pt_swap_kernel(SysDesc *__restrict__ descs, int n, int *__restrict__ perm,
+                               const double *__restrict__ temps, uint32_t seed, int64_t *__restrict__ round,
+                               long long *__restrict__ attempts, long long *__restrict__ accepts) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int64_t rd = *round;
+    const u4 r = philox4x32_10(u4{(uint32_t)rd, (uint32_t)(rd >> 32), 0u, 0x50540000u}, seed, 0x50545054u);
+    const int dr = ((double)r.x * (1.0 / 4294967296.0) > 0.5) ? 1 : -1;
+    for (int i = 0; i < n; i++) {
+        const int p = (i % 2 == 0) ? i + dr : i - dr;
+        if (p <= i || p >= n) continue;
+        const int a = perm[i], b = perm[p];
+        const SysScalars *sa = descs[a].sc, *sb = descs[b].sc;
+        const double ua = (double)sa->utot_hi + (double)sa->utot_lo;
+        const double ub = (double)sb->utot_hi + (double)sb->utot_lo;
+        const double arg = (1.0 / temps[i] - 1.0 / temps[p]) * (ua - ub);
+        const u4 q = philox4x32_10(u4{(uint32_t)rd, (uint32_t)(rd >> 32), (uint32_t)i, 0x50540001u}, seed, 0x50545054u);
+        const double u = ((double)q.x + 0.5) * (1.0 / 4294967296.0);
+        attempts[i]++;
+        if (!(u > exp(arg))) {
+            accepts[i]++;
+            perm[i] = b;
+            perm[p] = a;
+            descs[a].kT = (float)temps[p];
+            descs[b].kT = (float)temps[i];
+        }
+    }
+    *round = rd + 1;
+}
+
+}  // namespace fg
+
+struct fg_batch {
+    std::vector<fg_system *> sys;
+    cudaStream_t stream = nullptr;
+    SysDesc *d_descs = nullptr;
+    SysScalars *d_gather = nullptr;
+    float2 *d_corr = nullptr;
+    int64_t *d_counts = nullptr;
+    int threads = 0;
+    LaunchCfg cfg{};
+    int maxN = 0, maxK = 0;
+    bool rebuilds = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // parallel tempering
+    int *d_perm = nullptr;
+    double *d_temps = nullptr;
+    int64_t *d_round = nullptr;
+    long long *d_att = nullptr, *d_acc = nullptr;
+    uint32_t pt_seed = 0;
+    bool pt = false;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_sweeps = -1;
+};
+
+namespace {
+
+int batch_config(fg_batch *b) {
+    fg_system *h0 = b->sys[0];
+    b->cfg.fn = sweep_fn(h0);
+    int T = b->threads;
+    size_t sm = 0;
+    b->maxN = b->maxK = 0;
+    for (fg_system *h : b->sys) {
+        if (sweep_fn(h) != b->cfg.fn) return fail(FG_ERR_INVALID, "batch members need the same kernel variant");
+        if (b->threads == 0) T = std::max(T, sweep_threads(h));
+        sm = std::max(sm, sweep_smem(h, h->pos_smem));
+        b->maxN = std::max(b->maxN, h->N);
+        b->maxK = std::max(b->maxK, h->K);
+    }
+    b->cfg.threads = T;
+    b->cfg.smem = sm;
+    b->rebuilds = b->maxK > 0 && !h0->desc.skip_rebuild;
+    return set_smem_attr((const void *)b->cfg.fn, sm);
+}
+
+int batch_push_descs(fg_batch *b) {
+    std::vector<SysDesc> v(b->sys.size());
+    for (size_t s = 0; s < b->sys.size(); s++) {
+        fg_system *h = b->sys[s];
+        h->desc.trials = h->trials;
+        h->desc.log_trials = 0;
+        v[s] = h->desc;
+    }
+    CK(cudaMemcpyAsync(b->d_descs, v.data(), v.size() * sizeof(SysDesc), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return FG_OK;
+}
+
+// Run every member's staged stream (counts already on the device).
+int batch_run(fg_batch *b, fg_sweep_stats *per, fg_sweep_stats *total) {
+    const int n = (int)b->sys.size();
+    std::vector<SysScalars> s0(n), s(n);
+    fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
+    CK(cudaMemcpyAsync(s0.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_counts);
+    std::vector<int64_t> counts(n);
+    CK(cudaMemcpyAsync(counts.data(), b->d_counts, n * sizeof(int64_t), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaEventRecord(b->ev0, b->stream));
+    int launches = 0;
+    const int uf = std::max(b->sys[0]->P.ewald_update_frequency, 1);
+    int64_t maxc = 0;
+    for (auto c : counts) maxc = std::max(maxc, c);
+    int64_t prev_done = -1;
+    while (true) {
+        const int pairs = b->rebuilds ? (int)std::min<int64_t>(maxc / uf + 1, 64) : 1;
+        for (int p = 0; p < pairs; p++) {
+            b->cfg.fn<<<n, b->cfg.threads, b->cfg.smem, b->stream>>>(b->d_descs, INT64_MAX, b->sys[0]->sc_tab);
+            CK(cudaGetLastError());
+            launches++;
+            if (b->rebuilds) {
+                int rc = launch_rebuild(b->d_descs, n, b->maxN, b->maxK, b->d_corr, b->stream);
+                if (rc) return rc;
+            }
+        }
+        fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
+        CK(cudaMemcpyAsync(s.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        bool done = true, err = false;
+        int64_t sum = 0;
+        for (int i = 0; i < n; i++) {
+            if (s[i].error) err = true;
+            if (s[i].cursor < counts[i] || s[i].rebuild_pending) done = false;
+            sum += s[i].cursor;
+        }
+        if (err || done) break;
+        if (sum == prev_done) return fail(FG_ERR_DEVICE, "batch made no progress");
+        prev_done = sum;
+    }
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    fg_sweep_stats tot{};
+    int errs = 0;
+    for (int i = 0; i < n; i++) {
+        fg_sweep_stats st{};
+        st.trials = s[i].cursor;
+        st.accepted = s[i].n_accepted - s0[i].n_accepted;
+        st.rebuilds = s[i].n_rebuilds - s0[i].n_rebuilds;
+        st.energy_change = df_val(s[i].u_hi, s[i].u_lo);
+        st.device_ms = ms;
+        st.sweep_kernel_ms = ms;
+        st.sweep_launches = launches;
+        st.error_flags = s[i].error;
+        errs |= s[i].error;
+        if (per) per[i] = st;
+        tot.trials += st.trials;
+        tot.accepted += st.accepted;
+        tot.rebuilds += st.rebuilds;
+        tot.energy_change += st.energy_change;
+    }
+    tot.device_ms = ms;
+    tot.sweep_kernel_ms = ms;
+    tot.sweep_launches = launches;
+    tot.error_flags = errs;
+    if (total) *total = tot;
+    for (fg_system *h : b->sys) h->cnt_accepted_host = 0;
+    if (errs) return fail(FG_ERR_DEVICE, "device error flags 0x%x in a batch member", errs);
+    return FG_OK;
+}
+
+void batch_free(fg_batch *b) {
+    void *ptrs[] = {b->d_descs, b->d_gather, b->d_corr, b->d_counts, b->d_perm, b->d_temps, b->d_round, b->d_att,
+                    b->d_acc};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_batch_create(fg_system *const *systems, int32_t n, fg_batch **out) {
+    if (!systems || !out || n < 1) return fail(FG_ERR_INVALID, "bad argument");
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        if (!systems[i]) return fail(FG_ERR_INVALID, "null system %d", i);
+        if (!systems[i]->state_set) return fail(FG_ERR_STATE, "system %d has no state", i);
+        if (systems[i]->trial_pending) return fail(FG_ERR_STATE, "system %d has a pending trial", i);
+        CK(cudaStreamSynchronize(systems[i]->stream));
+    }
+    fg_batch *b = new fg_batch();
+    b->sys.assign(systems, systems + n);
+    auto bail = [&](int code) {
+        batch_free(b);
+        delete b;
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(FG_ERR_CUDA, "stream create failed"));
+    cudaEventCreate(&b->ev0);
+    cudaEventCreate(&b->ev1);
+    if (cudaMalloc(&b->d_descs, n * sizeof(SysDesc)) != cudaSuccess ||
+        cudaMalloc(&b->d_gather, n * sizeof(SysScalars)) != cudaSuccess ||
+        cudaMalloc(&b->d_corr, n * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&b->d_counts, n * sizeof(int64_t)) != cudaSuccess)
+        return bail(fail(FG_ERR_CUDA, "batch allocation failed"));
+    int rc = batch_config(b);
+    if (rc) return bail(rc);
+    *out = b;
+    return FG_OK;
+}
+
+int fg_batch_destroy(fg_batch *b) {
+    if (!b) return FG_OK;
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    delete b;
+    return FG_OK;
+}
+
+int fg_batch_set_threads(fg_batch *b, int32_t threads) {
+    if (!b || threads < 0 || threads > fg::kSweepThreads || threads % 32)
+        return fail(FG_ERR_INVALID, "threads must be a multiple of 32 in [0, %d]", fg::kSweepThreads);
+    b->threads = threads;
+    return batch_config(b);
+}
+
+int fg_batch_stream_philox(fg_batch *b, const int64_t *counts, uint32_t seed, const uint32_t *stream_ids) {
+    if (!b || !counts) return fail(FG_ERR_INVALID, "bad argument");
+    const int n = (int)b->sys.size();
+    int64_t maxc = 0;
+    for (int s = 0; s < n; s++) {
+        if (counts[s] < 0) return fail(FG_ERR_INVALID, "negative trial count");
+        fg_system *h = b->sys[s];
+        int rc = ensure_trials(h, counts[s], false);
+        if (rc) return rc;
+        h->n_trials = counts[s];
+        h->desc.seed = seed;
+        h->desc.stream_id = stream_ids ? stream_ids[s] : (uint32_t)s;
+        h->desc.stream_first = 0;
+        maxc = std::max(maxc, counts[s]);
+    }
+    int rc = batch_push_descs(b);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(b->d_counts, counts, n * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+    if (maxc > 0) {
+        dim3 g((unsigned)std::min<int64_t>((maxc + 255) / 256, 64), n);
+        fg::batch_philox_kernel<<<g, 256, 0, b->stream>>>(b->d_descs, b->d_counts, nullptr);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    return FG_OK;
+}
+
+int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total) {
+    if (!b) return fail(FG_ERR_INVALID, "null batch");
+    const int n = (int)b->sys.size();
+    std::vector<int64_t> counts(n);
+    for (int s = 0; s < n; s++) counts[s] = b->sys[s]->n_trials;
+    int rc = batch_push_descs(b);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(b->d_counts, counts.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+    return batch_run(b, per_system, total);
+}
+
+// ---------------------------------------------------------------- parallel tempering
+int fg_pt_setup(fg_batch *b, const double *temperatures, uint32_t seed) {
+    if (!b || !temperatures) return fail(FG_ERR_INVALID, "bad argument");
+    const int n = (int)b->sys.size();
+    for (int i = 0; i < n; i++)
+        if (!(temperatures[i] > 0)) return fail(FG_ERR_INVALID, "temperatures must be positive");
+    if (!b->d_perm) {
+        CK(cudaMalloc(&b->d_perm, n * sizeof(int)));
+        CK(cudaMalloc(&b->d_temps, n * sizeof(double)));
+        CK(cudaMalloc(&b->d_round, sizeof(int64_t)));
+        CK(cudaMalloc(&b->d_att, n * sizeof(long long)));
+        CK(cudaMalloc(&b->d_acc, n * sizeof(long long)));
+    }
+    std::vector<int> perm(n);
+    for (int i = 0; i < n; i++) {
+        perm[i] = i;
+        b->sys[i]->desc.kT = (float)temperatures[i];
+    }
+    int64_t zero = 0;
+    CK(cudaMemcpyAsync(b->d_perm, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d_temps, temperatures, n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemcpyAsync(b->d_round, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemsetAsync(b->d_att, 0, n * sizeof(long long), b->stream));
+    CK(cudaMemsetAsync(b->d_acc, 0, n * sizeof(long long), b->stream));
+    b->pt_seed = seed;
+    b->pt = true;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->graph_sweeps = -1;
+    for (int s = 0; s < n; s++) {
+        fg_system *h = b->sys[s];
+        h->desc.seed = seed;
+        h->desc.stream_id = (uint32_t)s;
+        h->desc.stream_first = 0;
+    }
+    return FG_OK;
+}
+
+// `rounds` rounds of: sweeps_per_round sweeps on every replica (N_s trials
+// per sweep, device-generated Philox streams), then one exchange attempt per
+// neighbour pair. Captured once as a CUDA graph and replayed per round.
+int fg_pt_run(fg_batch *b, int32_t rounds, int32_t sweeps_per_round, fg_sweep_stats *total) {
+    if (!b || !b->pt) return fail(FG_ERR_STATE, "fg_pt_setup first");
+    if (rounds < 0 || sweeps_per_round < 1) return fail(FG_ERR_INVALID, "bad rounds/sweeps");
+    if (b->rebuilds) return fail(FG_ERR_INVALID, "parallel tempering supports systems without Q(k) rebuilds");
+    const int n = (int)b->sys.size();
+    std::vector<int64_t> counts(n);
+    for (int s = 0; s < n; s++) {
+        counts[s] = (int64_t)sweeps_per_round * b->sys[s]->N;
+        int rc = ensure_trials(b->sys[s], counts[s], false);
+        if (rc) return rc;
+        b->sys[s]->n_trials = counts[s];
+    }
+    // kT lives in the device descriptors (the swap kernel edits it): push the
+    // host copies only when (re)building the graph
+    if (!b->graph || b->graph_sweeps != sweeps_per_round) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        std::vector<int> perm(n);
+        CK(cudaMemcpyAsync(perm.data(), b->d_perm, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+        std::vector<double> temps(n);
+        CK(cudaMemcpyAsync(temps.data(), b->d_temps, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        for (int i = 0; i < n; i++) b->sys[perm[i]]->desc.kT = (float)temps[i];
+        int rc = batch_push_descs(b);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(b->d_counts, counts.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        int64_t maxc = 0;
+        for (auto c : counts) maxc = std::max(maxc, c);
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        dim3 pg((unsigned)std::min<int64_t>((maxc + 255) / 256, 64), n);
+        fg::batch_philox_kernel<<<pg, 256, 0, b->stream>>>(b->d_descs, b->d_counts, b->d_round);
+        fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_counts);
+        b->cfg.fn<<<n, b->cfg.threads, b->cfg.smem, b->stream>>>(b->d_descs, INT64_MAX, b->sys[0]->sc_tab);
+        fg::pt_swap_kernel<<<1, 32, 0, b->stream>>>(b->d_descs, n, b->d_perm, b->d_temps, b->pt_seed, b->d_round,
+                                                    b->d_att, b->d_acc);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess) return fail(FG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(FG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+        b->graph_sweeps = sweeps_per_round;
+    }
+    const int nth = n;
+    std::vector<SysScalars> s0(nth), s(nth);
+    fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
+    CK(cudaMemcpyAsync(s0.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaEventRecord(b->ev0, b->stream));
+    for (int r = 0; r < rounds; r++) CK(cudaGraphLaunch(b->graph, b->stream));
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
+    CK(cudaMemcpyAsync(s.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    fg_sweep_stats tot{};
+    int errs = 0;
+    for (int i = 0; i < n; i++) {
+        tot.trials += (int64_t)rounds * counts[i];
+        tot.accepted += s[i].n_accepted - s0[i].n_accepted;
+        errs |= s[i].error;
+    }
+    tot.device_ms = ms;
+    tot.sweep_kernel_ms = ms;
+    tot.sweep_launches = rounds;
+    tot.error_flags = errs;
+    if (total) *total = tot;
+    if (errs) return fail(FG_ERR_DEVICE, "device error flags 0x%x", errs);
+    return FG_OK;
+}
+
+// perm[rung] = system index; energies[system] = running total energy;
+// attempts/accepts[rung] count exchanges between rung and rung+1 (or NULL).
+int fg_pt_get(fg_batch *b, int32_t *perm, double *energies, int64_t *attempts, int64_t *accepts) {
+    if (!b || !b->pt) return fail(FG_ERR_STATE, "fg_pt_setup first");
+    const int n = (int)b->sys.size();
+    if (perm) CK(cudaMemcpyAsync(perm, b->d_perm, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    if (attempts) CK(cudaMemcpyAsync(attempts, b->d_att, n * sizeof(long long), cudaMemcpyDeviceToHost, b->stream));
+    if (accepts) CK(cudaMemcpyAsync(accepts, b->d_acc, n * sizeof(long long), cudaMemcpyDeviceToHost, b->stream));
+    std::vector<SysScalars> s(n);
+    fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
+    CK(cudaMemcpyAsync(s.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    if (energies)
+        for (int i = 0; i < n; i++) energies[i] = df_val(s[i].utot_hi, s[i].utot_lo);
+    return FG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- job server
+struct fg_job {
+    int64_t id;
+    fg_params P;
+    std::vector<double> xyz, q;
+    std::vector<int32_t> ids;
+    uint32_t seed;
+    int64_t n_trials, done = 0, accepted = 0;
+    int state = 0;   // 0 queued, 1 running, 2 done, 3 failed
+    fg_system *sys = nullptr;
+    size_t bytes = 0;
+    double energy = 0;
+};
+
+struct fg_server {
+    int64_t max_bytes;
+    int threads;
+    int64_t round_pairs;
+    int64_t used = 0, next_id = 1;
+    std::vector<fg_job *> jobs;   // all jobs not yet released
+    cudaStream_t stream = nullptr;
+    SysDesc *d_descs = nullptr;
+    SysScalars *d_gather = nullptr;
+    int64_t *d_counts = nullptr;
+    int cap = 0;
+    std::string err;
+};
+
+namespace {
+
+// Device bytes of one job: coordinates, records, types, descriptor and the
+// per-round trial stream.
+size_t job_bytes(const fg_params &P, int N, int64_t round_trials) {
+    size_t b = (size_t)N * (24 + 16 + 8 + 1) + sizeof(SysDesc) + sizeof(SysScalars) + 64 * 1024;
+    b += (size_t)round_trials * sizeof(Trial);
+    (void)P;
+    return b;
+}
+
+int64_t round_trials_of(const fg_server *s, const fg_job *j) {
+    const int64_t N = j->sys ? j->sys->N : (int64_t)j->ids.size();
+    int64_t t = std::max<int64_t>(N, s->round_pairs / std::max<int64_t>(N, 1));
+    t = std::min<int64_t>(t, 1 << 20);
+    return std::min<int64_t>(t, j->n_trials - j->done);
+}
+
+int server_grow(fg_server *s, int n) {
+    if (n <= s->cap) return FG_OK;
+    int cap = std::max(n, 2 * s->cap);
+    if (s->d_descs) cudaFree(s->d_descs);
+    if (s->d_gather) cudaFree(s->d_gather);
+    if (s->d_counts) cudaFree(s->d_counts);
+    CK(cudaMalloc(&s->d_descs, cap * sizeof(SysDesc)));
+    CK(cudaMalloc(&s->d_gather, cap * sizeof(SysScalars)));
+    CK(cudaMalloc(&s->d_counts, cap * sizeof(int64_t)));
+    s->cap = cap;
+    return FG_OK;
+}
+
+int server_admit(fg_server *s, fg_job *j) {
+    const int64_t rt = std::min<int64_t>(j->n_trials, std::max<int64_t>((int64_t)j->ids.size(),
+                                                                       s->round_pairs / std::max<size_t>(j->ids.size(), 1)));
+    j->bytes = job_bytes(j->P, (int)j->ids.size(), std::min<int64_t>(rt, 1 << 20));
+    if (s->used + (int64_t)j->bytes > s->max_bytes) return 1;   // does not fit now
+    fg_system *h = nullptr;
+    int rc = fg_create(&j->P, (int)j->ids.size(), &h);
+    if (rc) return rc;
+    if (s->threads) fg_set_threads(h, s->threads);
+    rc = fg_set_state(h, j->xyz.data(), j->q.empty() ? nullptr : j->q.data(), j->ids.data());
+    if (rc) {
+        fg_destroy(h);
+        return rc;
+    }
+    h->desc.seed = j->seed;
+    h->desc.stream_id = (uint32_t)j->id;
+    j->sys = h;
+    j->state = 1;
+    j->bytes = h->device_bytes + (size_t)std::min<int64_t>(rt, 1 << 20) * sizeof(Trial);
+    s->used += (int64_t)j->bytes;
+    return FG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_server_create(int64_t max_device_bytes, int32_t threads, int64_t round_pairs, fg_server **out) {
+    if (!out || max_device_bytes <= 0 || threads < 0 || threads > fg::kSweepThreads || threads % 32)
+        return fail(FG_ERR_INVALID, "bad argument");
+    fg_server *s = new fg_server();
+    s->max_bytes = max_device_bytes;
+    s->threads = threads;
+    s->round_pairs = round_pairs > 0 ? round_pairs : ((int64_t)1 << 28);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return fail(FG_ERR_CUDA, "stream create failed");
+    }
+    *out = s;
+    return FG_OK;
+}
+
+int fg_server_destroy(fg_server *s) {
+    if (!s) return FG_OK;
+    cudaStreamSynchronize(s->stream);
+    for (fg_job *j : s->jobs) {
+        if (j->sys) fg_destroy(j->sys);
+        delete j;
+    }
+    if (s->d_descs) cudaFree(s->d_descs);
+    if (s->d_gather) cudaFree(s->d_gather);
+    if (s->d_counts) cudaFree(s->d_counts);
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return FG_OK;
+}
+
+// Queue a job: a system (params, coordinates, charges or NULL, types), its
+// Philox seed and the number of trials to run.
+int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const double *xyz, const double *charge,
+                     const int32_t *type_ids, uint32_t seed, int64_t n_trials, int64_t *job_id) {
+    if (!s || !params || !xyz || !type_ids || !job_id || n < 2 || n_trials < 0) return fail(FG_ERR_INVALID, "bad argument");
+    if (params->model != FG_MODEL_DH_LJ && params->model != FG_MODEL_EWALD_WCA)
+        return fail(FG_ERR_INVALID, "unsupported model");
+    for (fg_job *o : s->jobs)
+        if (o->P.model != params->model) return fail(FG_ERR_INVALID, "one model per server");
+    if ((int64_t)job_bytes(*params, n, 1) > s->max_bytes) return fail(FG_ERR_CAPACITY, "job larger than the budget");
+    fg_job *j = new fg_job();
+    j->id = s->next_id++;
+    j->P = *params;
+    j->xyz.assign(xyz, xyz + 3 * (size_t)n);
+    if (charge) j->q.assign(charge, charge + n);
+    j->ids.assign(type_ids, type_ids + n);
+    j->seed = seed;
+    j->n_trials = n_trials;
+    s->jobs.push_back(j);
+    *job_id = j->id;
+    return FG_OK;
+}
+
+// One round: admit queued jobs that fit the memory budget (in submission
+// order), give every running job its next chunk of trials (about
+// round_pairs / N trials, at least one sweep) and run them all in one launch
+// of the persistent sweep kernel, then retire finished jobs.
+int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double *device_ms) {
+    if (!s) return fail(FG_ERR_INVALID, "null server");
+    for (fg_job *j : s->jobs)
+        if (j->state == 0) {
+            int rc = server_admit(s, j);
+            if (rc == 1) break;   // keep submission order: wait for memory
+            if (rc) {
+                j->state = 3;
+                continue;
+            }
+        }
+    std::vector<fg_job *> run;
+    for (fg_job *j : s->jobs)
+        if (j->state == 1) run.push_back(j);
+    if (n_running) *n_running = (int)run.size();
+    if (n_finished) *n_finished = 0;
+    if (device_ms) *device_ms = 0;
+    if (run.empty()) return FG_OK;
+    const int n = (int)run.size();
+    int rc = server_grow(s, n);
+    if (rc) return rc;
+    std::vector<SysDesc> descs(n);
+    std::vector<int64_t> counts(n);
+    LaunchCfg cfg{};
+    size_t smem = 0;
+    int T = s->threads;
+    for (int i = 0; i < n; i++) {
+        fg_job *j = run[i];
+        fg_system *h = j->sys;
+        counts[i] = round_trials_of(s, j);
+        rc = ensure_trials(h, counts[i], false);
+        if (rc) return rc;
+        h->n_trials = counts[i];
+        h->desc.trials = h->trials;
+        h->desc.log_trials = 0;
+        h->desc.skip_rebuild = 1;
+        h->desc.stream_first = j->done;
+        descs[i] = h->desc;
+        if (i == 0) cfg.fn = sweep_fn(h);
+        if (sweep_fn(h) != cfg.fn) return fail(FG_ERR_INVALID, "server jobs need one kernel variant");
+        smem = std::max(smem, sweep_smem(h, h->pos_smem));
+        if (!s->threads) T = std::max(T, sweep_threads(h));
+    }
+    rc = set_smem_attr((const void *)cfg.fn, smem);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(s->d_descs, descs.data(), n * sizeof(SysDesc), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->d_counts, counts.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, s->stream));
+    int64_t maxc = 0;
+    for (auto c : counts) maxc = std::max(maxc, c);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    CK(cudaEventRecord(e0, s->stream));
+    dim3 pg((unsigned)std::min<int64_t>((maxc + 255) / 256, 64), n);
+    fg::batch_philox_kernel<<<pg, 256, 0, s->stream>>>(s->d_descs, s->d_counts, nullptr);
+    fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(s->d_descs, n, s->d_counts);
+    cfg.fn<<<n, T, smem, s->stream>>>(s->d_descs, INT64_MAX, run[0]->sys->sc_tab);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(e1, s->stream));
+    std::vector<SysScalars> sc(n);
+    fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(s->d_descs, n, s->d_gather);
+    CK(cudaMemcpyAsync(sc.data(), s->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (device_ms) *device_ms = ms;
+    int fin = 0;
+    for (int i = 0; i < n; i++) {
+        fg_job *j = run[i];
+        if (sc[i].error) {
+            j->state = 3;
+            continue;
+        }
+        j->done += sc[i].cursor;
+        j->accepted = sc[i].n_accepted;
+        j->energy = df_val(sc[i].utot_hi, sc[i].utot_lo);
+        if (j->done >= j->n_trials) {
+            j->state = 2;
+            fin++;
+        }
+    }
+    if (n_finished) *n_finished = fin;
+    return FG_OK;
+}
+
+// state: 0 queued, 1 running, 2 done, 3 failed; trials done, accepted,
+// running total energy; positions (3N, may be NULL) once done.
+int fg_server_poll(fg_server *s, int64_t job_id, int32_t *state, int64_t *trials_done, int64_t *accepted,
+                   double *energy, double *xyz) {
+    if (!s) return fail(FG_ERR_INVALID, "null server");
+    for (fg_job *j : s->jobs)
+        if (j->id == job_id) {
+            if (state) *state = j->state;
+            if (trials_done) *trials_done = j->done;
+            if (accepted) *accepted = j->accepted;
+            if (energy) *energy = j->energy;
+            if (xyz && j->sys && j->state == 2) return fg_get_state(j->sys, xyz);
+            return FG_OK;
+        }
+    return fail(FG_ERR_INVALID, "unknown job %lld", (long long)job_id);
+}
+
+// Free a finished (or failed) job and its device memory.
+int fg_server_release(fg_server *s, int64_t job_id) {
+    if (!s) return fail(FG_ERR_INVALID, "null server");
+    for (size_t k = 0; k < s->jobs.size(); k++) {
+        fg_job *j = s->jobs[k];
+        if (j->id != job_id) continue;
+        if (j->state == 1) return fail(FG_ERR_STATE, "job %lld is running", (long long)job_id);
+        if (j->sys) {
+            s->used -= (int64_t)j->bytes;
+            fg_destroy(j->sys);
+        }
+        delete j;
+        s->jobs.erase(s->jobs.begin() + k);
+        return FG_OK;
+    }
+    return fail(FG_ERR_INVALID, "unknown job %lld", (long long)job_id);
+}
+
+int64_t fg_server_bytes_in_use(fg_server *s) { return s ? s->used : 0; }
+
+}  // extern "C"

@@ -90,25 +90,24 @@ __device__ __forceinline__ float2 sincos_turns(uint32_t ph, const float2 *__rest
     return make_float2(t.x * c - t.y * s, t.x * s + t.y * c);
 }
 
-// e^{i phi} - 1 with error relative to |phi| (Taylor series of sin and of
-// 1 - cos, Horner form); valid for |phi| <= 1.6 rad (next terms < 1e-9).
-__device__ __forceinline__ float2 expm1_i(float phi) {
-    float p2 = phi * phi;
-    float s = fmaf(p2, -1.0f / 156.0f, 1.0f);
-    s = fmaf(p2 * (-1.0f / 110.0f), s, 1.0f);
-    s = fmaf(p2 * (-1.0f / 72.0f), s, 1.0f);
-    s = fmaf(p2 * (-1.0f / 42.0f), s, 1.0f);
-    s = fmaf(p2 * (-1.0f / 20.0f), s, 1.0f);
-    s = fmaf(p2 * (-1.0f / 6.0f), s, 1.0f);
-    s = phi * s;                                        // sin(phi)
-    float c = fmaf(p2, -1.0f / 182.0f, 1.0f);
-    c = fmaf(p2 * (-1.0f / 132.0f), c, 1.0f);
-    c = fmaf(p2 * (-1.0f / 90.0f), c, 1.0f);
-    c = fmaf(p2 * (-1.0f / 56.0f), c, 1.0f);
-    c = fmaf(p2 * (-1.0f / 30.0f), c, 1.0f);
-    c = fmaf(p2 * (-1.0f / 12.0f), c, 1.0f);
-    c = 0.5f * p2 * c;                                  // 1 - cos(phi)
-    return make_float2(-c, s);
+// e^{i phi} - 1 = (cos phi - 1, sin phi) with error relative to |phi|, from
+// the Taylor series of sin and of 1 - cos in Horner form on the coefficients
+// +-1/n! (one FMA per term); valid for |phi| <= 1.6 rad (next terms < 1e-9).
+__device__ __forceinline__ float2 expm1_i_horner(float phi) {
+    const float p2 = phi * phi;
+    float s = fmaf(p2, 1.6059043836821613e-10f, -2.5052108385441720e-08f);
+    s = fmaf(p2, s, 2.7557319223985893e-06f);
+    s = fmaf(p2, s, -1.9841269841269841e-04f);
+    s = fmaf(p2, s, 8.3333333333333333e-03f);
+    s = fmaf(p2, s, -1.6666666666666667e-01f);
+    s = fmaf(p2 * phi, s, phi);                         // sin(phi)
+    float c = fmaf(p2, 1.1470745597729725e-11f, -2.0876756987868099e-09f);
+    c = fmaf(p2, c, 2.7557319223985891e-07f);
+    c = fmaf(p2, c, -2.4801587301587302e-05f);
+    c = fmaf(p2, c, 1.3888888888888889e-03f);
+    c = fmaf(p2, c, -4.1666666666666667e-02f);
+    c = fmaf(p2, c, 0.5f);
+    return make_float2(-(p2 * c), s);                   // (cos - 1, sin)
 }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {

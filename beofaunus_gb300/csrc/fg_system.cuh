@@ -9,7 +9,8 @@
 //   cells  (cell-list systems only) per cell `cap` slots of int4 positions and
 //          int32 particle ids, plus counts; p_cell/p_slot locate each particle
 //   Ewald  kvec float4[K] {kx, ky, kz, A_k * 2*pi*lB/V}, kpack uint32[K] (n
-//          vector as signed bytes), qk float4[K] {Re hi, Re lo, Im hi, Im lo}
+//          vector as signed bytes), qfix longlong2[K]: Q(k) as exact sums of
+//          per-particle contributions rounded to 2^-40 (see qk_contrib)
 #pragma once
 #include <cstdint>
 
@@ -27,6 +28,7 @@ enum : int32_t {
     kErrStencil = 2,        // a particle moved more than one cell
     kErrKCapacity = 4,      // more k-vectors than threads * kMaxKPerThread
     kErrNonFinite = 8,      // dU was NaN
+    kErrQkMismatch = 16,    // a rebuild did not reproduce the incremental Q(k)
 };
 
 // One trial of the stream (40 bytes): particle index, fixed-point
@@ -48,7 +50,10 @@ struct SysScalars {
     int32_t error;
     int32_t n_rebuilds;    // Q(k) rebuilds since upload
     float u_hi, u_lo;      // running sum of accepted dU + rebuild corrections
+    float utot_hi, utot_lo; // running total energy (set at upload, then += dU)
     float m[3][2];         // surface dipole sum(q * eff * r) as df per axis
+    int32_t verify_rebuild; // flag a rebuild that changes Q(k) as an error
+    int32_t pad2;
 };
 
 // Everything a kernel needs to find one system (passed in global memory
@@ -73,6 +78,7 @@ struct alignas(16) SysDesc {
     float surf_c;              // 2*pi*lB/((2 eps_surf+1) V) * const_inf
     float kT;                  // temperature scale of the Boltzmann factor
     int32_t update_frequency;
+    int32_t skip_rebuild;      // do not stop sweeps for Q(k) rebuilds
     int32_t log_trials;        // write per-trial dU/accept
     // per-type-pair tables (row-major nt*nt) and per-type effective charge
     float s2[kMaxTypes * kMaxTypes];
@@ -102,13 +108,17 @@ struct alignas(16) SysDesc {
     int32_t *p_slot;
     float4 *kvec;
     uint32_t *kpack;
-    float4 *qk;
+    longlong2 *qfix;
     const Trial *trials;
     float2 *trial_du;        // per-trial dU (df), optional
     uint8_t *trial_acc;      // per-trial acceptance, optional
     SysScalars *sc;
-    float2 *pending_dq;      // Delta Q(k) of the last plain trial (K)
-    float *pending;          // plain trial: [0..2]=new X hi words as float bits...
+    const float2 *sc_tab;    // cos/sin table at multiples of 2 pi / 256
+    const int64_t *dp_fix;   // per type and axis: round(dp / L * 2^32)
+    uint32_t stream_id;      // Philox key word of this system's trial stream
+    uint32_t seed;           // Philox key word (seed)
+    int64_t stream_first;    // counter of trial 0 in the current stream
+    longlong2 *qnew;         // rebuild target (K)
 };
 
 }  // namespace fg

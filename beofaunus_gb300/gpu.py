@@ -69,6 +69,24 @@ def lib(build_if_missing=True):
             "fg_set_threads": ([vp, i32], ctypes.c_int),
             "fg_get_threads": ([vp], ctypes.c_int),
             "fg_philox4x32_10": ([dp, dp, dp], None),
+            "fg_set_rebuild_policy": ([vp, i32], ctypes.c_int),
+            "fg_running_energy": ([vp, dp], ctypes.c_int),
+            "fg_device_bytes": ([vp], ctypes.c_int64),
+            "fg_batch_create": ([dp, i32, ctypes.POINTER(vp)], ctypes.c_int),
+            "fg_batch_destroy": ([vp], ctypes.c_int),
+            "fg_batch_set_threads": ([vp, i32], ctypes.c_int),
+            "fg_batch_stream_philox": ([vp, dp, u32, dp], ctypes.c_int),
+            "fg_batch_run": ([vp, dp, dp], ctypes.c_int),
+            "fg_pt_setup": ([vp, dp, u32], ctypes.c_int),
+            "fg_pt_run": ([vp, i32, i32, dp], ctypes.c_int),
+            "fg_pt_get": ([vp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_server_create": ([i64, i32, i64, ctypes.POINTER(vp)], ctypes.c_int),
+            "fg_server_destroy": ([vp], ctypes.c_int),
+            "fg_server_submit": ([vp, vp, i32, dp, dp, dp, u32, i64, dp], ctypes.c_int),
+            "fg_server_step": ([vp, dp, dp, dp], ctypes.c_int),
+            "fg_server_poll": ([vp, i64, dp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_server_release": ([vp, i64], ctypes.c_int),
+            "fg_server_bytes_in_use": ([vp], ctypes.c_int64),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -217,3 +235,124 @@ class System:
 
     def synchronize(self):
         _check(lib().fg_synchronize(self.h))
+
+    def set_rebuild_policy(self, skip):
+        _check(lib().fg_set_rebuild_policy(self.h, 1 if skip else 0))
+
+    def running_energy(self):
+        u = np.zeros(1)
+        _check(lib().fg_running_energy(self.h, _p(u)))
+        return float(u[0])
+
+    @property
+    def device_bytes(self):
+        return int(lib().fg_device_bytes(self.h))
+
+
+class Batch:
+    """Independent systems advanced together, one CTA per system."""
+
+    def __init__(self, systems, threads=0):
+        self.systems = list(systems)
+        arr = (ctypes.c_void_p * len(self.systems))(*[s.h.value for s in self.systems])
+        h = ctypes.c_void_p()
+        _check(lib().fg_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(self.systems), ctypes.byref(h)))
+        self.h = h
+        if threads:
+            _check(lib().fg_batch_set_threads(self.h, threads))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stream_philox(self, counts, seed, stream_ids=None):
+        c = np.ascontiguousarray(counts, dtype=np.int64)
+        ids = None if stream_ids is None else np.ascontiguousarray(stream_ids, dtype=np.uint32)
+        _check(lib().fg_batch_stream_philox(self.h, _p(c), seed, _p(ids)))
+
+    def run(self):
+        n = len(self.systems)
+        per = (SweepStats * n)()
+        tot = SweepStats()
+        _check(lib().fg_batch_run(self.h, ctypes.cast(per, ctypes.c_void_p), ctypes.byref(tot)))
+        return [p.as_dict() for p in per], tot.as_dict()
+
+    # parallel tempering
+    def pt_setup(self, temperatures, seed):
+        t = np.ascontiguousarray(temperatures, dtype=np.float64)
+        _check(lib().fg_pt_setup(self.h, _p(t), seed))
+
+    def pt_run(self, rounds, sweeps_per_round):
+        tot = SweepStats()
+        _check(lib().fg_pt_run(self.h, rounds, sweeps_per_round, ctypes.byref(tot)))
+        return tot.as_dict()
+
+    def pt_state(self):
+        n = len(self.systems)
+        perm = np.empty(n, np.int32)
+        e = np.empty(n)
+        att = np.empty(n, np.int64)
+        acc = np.empty(n, np.int64)
+        _check(lib().fg_pt_get(self.h, _p(perm), _p(e), _p(att), _p(acc)))
+        return dict(perm=perm, energies=e, attempts=att, accepts=acc)
+
+
+class Server:
+    """Continuous-batching job server (admission by device footprint)."""
+
+    def __init__(self, max_bytes, threads=0, round_pairs=0):
+        h = ctypes.c_void_p()
+        _check(lib().fg_server_create(int(max_bytes), threads, int(round_pairs), ctypes.byref(h)))
+        self.h = h
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, params, xyz, charge, type_ids, seed, n_trials):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        q = None if charge is None else np.ascontiguousarray(charge, dtype=np.float64)
+        ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+        jid = np.zeros(1, np.int64)
+        _check(lib().fg_server_submit(self.h, ctypes.byref(params), len(xyz), _p(xyz), _p(q), _p(ids), seed,
+                                      int(n_trials), _p(jid)))
+        self._n[int(jid[0])] = len(xyz)
+        return int(jid[0])
+
+    def step(self):
+        r = np.zeros(1, np.int32)
+        f = np.zeros(1, np.int32)
+        ms = np.zeros(1)
+        _check(lib().fg_server_step(self.h, _p(r), _p(f), _p(ms)))
+        return int(r[0]), int(f[0]), float(ms[0])
+
+    def poll(self, job_id, positions=False):
+        st = np.zeros(1, np.int32)
+        done = np.zeros(1, np.int64)
+        acc = np.zeros(1, np.int64)
+        e = np.zeros(1)
+        xyz = np.empty((self._n[job_id], 3)) if positions else None
+        _check(lib().fg_server_poll(self.h, job_id, _p(st), _p(done), _p(acc), _p(e), _p(xyz)))
+        return dict(state=int(st[0]), trials=int(done[0]), accepted=int(acc[0]), energy=float(e[0]), xyz=xyz)
+
+    def release(self, job_id):
+        _check(lib().fg_server_release(self.h, job_id))
+
+    @property
+    def bytes_in_use(self):
+        return int(lib().fg_server_bytes_in_use(self.h))

@@ -27,6 +27,8 @@ extern "C" {
 #define FG_ERR_CAPACITY -5     /* exceeds a compiled or admitted capacity */
 
 typedef struct fg_system fg_system;
+typedef struct fg_batch fg_batch;
+typedef struct fg_server fg_server;
 
 typedef struct fg_sweep_stats {
     int64_t trials;         /* trials run by this call */
@@ -129,6 +131,64 @@ int fg_get_threads(fg_system *h);
 
 /* One Philox4x32-10 block, host side (for tests of the generator). */
 void fg_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Q(k) is kept as an exact integer sum of per-particle contributions, so a
+ * rebuild reproduces it bit for bit. skip != 0: sweeps do not stop for the
+ * update_frequency rebuilds (fg_rebuild_qk still verifies on demand);
+ * skip == 0 (default): rebuild where NonbondedEwald::update would
+ * (ewald.h:633) and flag any difference as a device error. */
+int fg_set_rebuild_policy(fg_system *h, int32_t skip);
+
+/* Running total energy: systemEnergy at upload plus every accepted dU and
+ * rebuild correction since (what Propagator tracks for drift checks,
+ * move.h:7730-7731, 7911-7913). */
+int fg_running_energy(fg_system *h, double *energy);
+
+/* Device bytes held by a system. */
+int64_t fg_device_bytes(fg_system *h);
+
+/* ---- batches: many independent systems per launch -------------------------
+ * Replaces: running one Movebase::move loop per replica process. All members
+ * must use the same model and kernel variant; each keeps its own stream of
+ * trials and its own state. */
+int fg_batch_create(fg_system *const *systems, int32_t n, fg_batch **out);
+int fg_batch_destroy(fg_batch *b);
+/* Threads per system CTA for the whole batch (0 = the largest member's). */
+int fg_batch_set_threads(fg_batch *b, int32_t threads);
+/* Device-generated streams: member s gets counts[s] trials from Philox with
+ * key (seed, stream_ids[s]) (stream_ids may be NULL: s). */
+int fg_batch_stream_philox(fg_batch *b, const int64_t *counts, uint32_t seed, const uint32_t *stream_ids);
+/* Run every member's staged stream; per-member and summed statistics. */
+int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total);
+
+/* ---- parallel tempering over a batch ----------------------------------------
+ * Replaces: Move::ParallelTempering (move.h:6542-6771) with MPI ranks as
+ * temperature rungs. Member i starts at temperatures[i] (units of the
+ * energy scale: the Boltzmann factor is exp(-dU/T)). */
+int fg_pt_setup(fg_batch *b, const double *temperatures, uint32_t seed);
+/* rounds x (sweeps_per_round sweeps of every member, then one exchange
+ * attempt between each neighbouring pair picked as in findPartner,
+ * move.h:6621-6633); one CUDA graph per round. */
+int fg_pt_run(fg_batch *b, int32_t rounds, int32_t sweeps_per_round, fg_sweep_stats *total);
+/* perm[rung] = member at that temperature; energies[member]; exchange
+ * attempts/accepts per rung pair (rung, rung+1). Any pointer may be NULL. */
+int fg_pt_get(fg_batch *b, int32_t *perm, double *energies, int64_t *attempts, int64_t *accepts);
+
+/* ---- job server: continuous batching of independent Monte Carlo jobs --------
+ * No counterpart in the reference (one job per process there). Jobs are
+ * admitted in submission order while their device footprint fits
+ * max_device_bytes; every fg_server_step advances all admitted jobs in one
+ * launch (about round_pairs / N trials each, at least one sweep). */
+int fg_server_create(int64_t max_device_bytes, int32_t threads, int64_t round_pairs, fg_server **out);
+int fg_server_destroy(fg_server *s);
+int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const double *xyz, const double *charge,
+                     const int32_t *type_ids, uint32_t seed, int64_t n_trials, int64_t *job_id);
+int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double *device_ms);
+/* state: 0 queued, 1 running, 2 done, 3 failed. xyz (3N) filled once done. */
+int fg_server_poll(fg_server *s, int64_t job_id, int32_t *state, int64_t *trials_done, int64_t *accepted,
+                   double *energy, double *xyz);
+int fg_server_release(fg_server *s, int64_t job_id);
+int64_t fg_server_bytes_in_use(fg_server *s);
 
 #ifdef __cplusplus
 }

@@ -105,9 +105,11 @@ def test_sweep_rpm16k_cell_list_full_size():
     err = assert_same_chain(r["du"], r["acc"], ro["du"], ro["acc"], u)
     print("rpm16k: max |dU err| %.3g rms %.3g" % (err.max(), np.sqrt(np.mean(err ** 2))))
     np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
+    # Q(k) is the exact sum of FP32-accurate per-particle terms: its distance
+    # from the FP64 sum is bounded by ~sqrt(N) * 1e-7 (1.3e-5 here)
     qg = s.qk()
     qo = o.qk()[0]
-    assert np.max(np.abs(qg - qo)) < 1e-5
+    assert np.max(np.abs(qg - qo)) < 4e-5
 
 
 def test_total_energy_matches_oracle():
@@ -116,7 +118,7 @@ def test_total_energy_matches_oracle():
     o = OracleSystem(p, xyz, q, ids)
     eg, eo = s.total_energy(), o.total_energy()
     assert eg["pairs"] == pytest.approx(eo["pairs"], abs=2e-4)
-    assert eg["reciprocal"] == pytest.approx(eo["reciprocal"], abs=1e-6)
+    assert eg["reciprocal"] == pytest.approx(eo["reciprocal"], abs=2e-4)
     assert eg["self"] == pytest.approx(eo["self"], rel=1e-12)
     assert eg["surface"] == pytest.approx(eo["surface"], abs=1e-9)
     assert eg["total"] == pytest.approx(eo["total"], abs=2e-4)
@@ -157,16 +159,34 @@ def test_philox_stream_run_matches_oracle():
     np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
 
 
-def test_rebuild_is_drift_free_and_correction_small():
+def test_rebuild_reproduces_running_qk_exactly():
+    """Q(k) is an exact integer sum of per-particle contributions: after
+    thousands of accepted moves a rebuild from scratch gives the same bits
+    (correction exactly 0), and Q(k) stays within FP32-term accuracy of the
+    oracle's FP64 sum."""
     p, xyz, q, ids = workloads.rpm800(seed=31, update_frequency=100000)
     s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
     idx, disp, u = s.draw_translation_stream(5, 4000)
-    s.sweep(idx, disp, u, log=False)
+    r = s.sweep(idx, disp, u, log=False)
+    o.mc_run_stream(idx, disp, u)
     q_inc = s.qk()
-    corr = s.rebuild_qk()
-    q_new = s.qk()
-    assert np.max(np.abs(q_inc - q_new)) < 1e-5
-    assert abs(corr) < 1e-5
+    assert s.rebuild_qk() == 0.0
+    np.testing.assert_array_equal(s.qk(), q_inc)
+    assert np.max(np.abs(q_inc - o.qk()[0])) < 2e-5
+    assert r["stats"]["rebuilds"] == 0
+
+
+def test_update_frequency_rebuilds_verify_exactly():
+    """update_frequency=5: the sweep stops for a rebuild every 5 accepted
+    trials (as NonbondedEwald::update does); each must reproduce Q(k)."""
+    p, xyz, q, ids = workloads.rpm800(seed=32, update_frequency=5)
+    s = gpu_system(p, xyz, q, ids)
+    idx, disp, u = s.draw_translation_stream(6, 400)
+    r = s.sweep(idx, disp, u, log=False)
+    st = r["stats"]
+    assert st["rebuilds"] == st["accepted"] // 5
+    assert st["error_flags"] == 0
 
 
 def test_invalid_arguments_fail_loudly():
