@@ -13,7 +13,7 @@
 
 #include <cuda_runtime.h>
 
-#include "../../include/faunus_gb300.h"
+#include "faunus_gb300.h"
 #include "fg_kernels.cu"
 
 using fg::SysDesc;
@@ -300,8 +300,8 @@ int get_qk_host(fg_system *h, std::vector<double> &q) {
     CK(cudaMemcpyAsync(v.data(), h->qfix, v.size() * sizeof(longlong2), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (int k = 0; k < h->K; k++) {
-        q[2 * k] = (double)v[k].x * (1.0 / 1099511627776.0);
-        q[2 * k + 1] = (double)v[k].y * (1.0 / 1099511627776.0);
+        q[2 * k] = (double)v[k].x * (1.0 / 268435456.0);
+        q[2 * k + 1] = (double)v[k].y * (1.0 / 268435456.0);
     }
     return FG_OK;
 }

@@ -147,16 +147,14 @@ int batch_push_descs(fg_batch *b) {
     return FG_OK;
 }
 
-// Run every member's staged stream (counts already on the device).
-int batch_run(fg_batch *b, fg_sweep_stats *per, fg_sweep_stats *total) {
+// Run every member's staged stream of counts[s] trials (also on the device).
+int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *per, fg_sweep_stats *total) {
     const int n = (int)b->sys.size();
     std::vector<SysScalars> s0(n), s(n);
     fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
     CK(cudaMemcpyAsync(s0.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
     fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_counts);
-    std::vector<int64_t> counts(n);
-    CK(cudaMemcpyAsync(counts.data(), b->d_counts, n * sizeof(int64_t), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaEventRecord(b->ev0, b->stream));
     int launches = 0;
     const int uf = std::max(b->sys[0]->P.ewald_update_frequency, 1);
@@ -317,7 +315,7 @@ int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total)
     int rc = batch_push_descs(b);
     if (rc) return rc;
     CK(cudaMemcpyAsync(b->d_counts, counts.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
-    return batch_run(b, per_system, total);
+    return batch_run(b, counts, per_system, total);
 }
 
 // ---------------------------------------------------------------- parallel tempering
@@ -467,6 +465,7 @@ struct fg_job {
     int64_t n_trials, done = 0, accepted = 0;
     int state = 0;   // 0 queued, 1 running, 2 done, 3 failed
     fg_system *sys = nullptr;
+    std::vector<double> result;   // final coordinates, copied off the device
     size_t bytes = 0;
     double energy = 0;
 };
@@ -487,12 +486,20 @@ struct fg_server {
 
 namespace {
 
-// Device bytes of one job: coordinates, records, types, descriptor and the
-// per-round trial stream.
+// Device bytes of one job as fg_create allocates them for a Debye-Hueckel
+// system (coordinates, records, types, descriptor, scalars, tables) plus its
+// per-round trial stream; Ewald systems add their k-space arrays.
 size_t job_bytes(const fg_params &P, int N, int64_t round_trials) {
-    size_t b = (size_t)N * (24 + 16 + 8 + 1) + sizeof(SysDesc) + sizeof(SysScalars) + 64 * 1024;
-    b += (size_t)round_trials * sizeof(Trial);
-    (void)P;
+    size_t b = (size_t)N * (24 + 16 + 8 + 1) + sizeof(SysDesc) + sizeof(SysScalars) + 64 + 32 + 32 + 256 * 8 +
+               FG_MAX_TYPES * 3 * 8 + 1024 * 8;
+    double smax = 0;
+    for (int i = 0; i < P.n_types; i++) smax = std::max(smax, P.type_sigma[i]);
+    if (P.model == FG_MODEL_DH_LJ) b += 2 * 16 * (size_t)(std::ceil(smax / P.dh_debye_length * 128.0) + 4);
+    if (P.model == FG_MODEL_EWALD_WCA) {
+        const double kc = std::ceil(P.ewald_cutoff_k);
+        b += (size_t)(4.2 * kc * kc * kc + 16) * (16 + 4 + 16 + 16) + 2 * 16 * (size_t)(P.ewald_alpha * smax * 128 + 4);
+    }
+    b += (size_t)std::max<int64_t>(round_trials, 1) * sizeof(Trial);
     return b;
 }
 
@@ -530,8 +537,10 @@ int server_admit(fg_server *s, fg_job *j) {
         fg_destroy(h);
         return rc;
     }
+    // a job's stream depends on its seed only (Philox key (seed, 0)), so its
+    // result does not depend on which other jobs share the GPU
     h->desc.seed = j->seed;
-    h->desc.stream_id = (uint32_t)j->id;
+    h->desc.stream_id = 0;
     j->sys = h;
     j->state = 1;
     j->bytes = h->device_bytes + (size_t)std::min<int64_t>(rt, 1 << 20) * sizeof(Trial);
@@ -582,7 +591,8 @@ int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const dou
         return fail(FG_ERR_INVALID, "unsupported model");
     for (fg_job *o : s->jobs)
         if (o->P.model != params->model) return fail(FG_ERR_INVALID, "one model per server");
-    if ((int64_t)job_bytes(*params, n, 1) > s->max_bytes) return fail(FG_ERR_CAPACITY, "job larger than the budget");
+    const int64_t rt = std::min<int64_t>(n_trials, std::min<int64_t>(std::max<int64_t>(n, s->round_pairs / n), 1 << 20));
+    if ((int64_t)job_bytes(*params, n, rt) > s->max_bytes) return fail(FG_ERR_CAPACITY, "job larger than the budget");
     fg_job *j = new fg_job();
     j->id = s->next_id++;
     j->P = *params;
@@ -679,6 +689,13 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         j->accepted = sc[i].n_accepted;
         j->energy = df_val(sc[i].utot_hi, sc[i].utot_lo);
         if (j->done >= j->n_trials) {
+            // results to host memory; the device memory goes back to the pool
+            j->result.resize(3 * (size_t)j->sys->N);
+            rc = fg_get_state(j->sys, j->result.data());
+            if (rc) return rc;
+            s->used -= (int64_t)j->bytes;
+            fg_destroy(j->sys);
+            j->sys = nullptr;
             j->state = 2;
             fin++;
         }
@@ -698,7 +715,7 @@ int fg_server_poll(fg_server *s, int64_t job_id, int32_t *state, int64_t *trials
             if (trials_done) *trials_done = j->done;
             if (accepted) *accepted = j->accepted;
             if (energy) *energy = j->energy;
-            if (xyz && j->sys && j->state == 2) return fg_get_state(j->sys, xyz);
+            if (xyz && j->state == 2) std::copy(j->result.begin(), j->result.end(), xyz);
             return FG_OK;
         }
     return fail(FG_ERR_INVALID, "unknown job %lld", (long long)job_id);
@@ -711,10 +728,6 @@ int fg_server_release(fg_server *s, int64_t job_id) {
         fg_job *j = s->jobs[k];
         if (j->id != job_id) continue;
         if (j->state == 1) return fail(FG_ERR_STATE, "job %lld is running", (long long)job_id);
-        if (j->sys) {
-            s->used -= (int64_t)j->bytes;
-            fg_destroy(j->sys);
-        }
         delete j;
         s->jobs.erase(s->jobs.begin() + k);
         return FG_OK;

@@ -18,7 +18,7 @@
 // (potentials.h:2036-2040), NonbondedEwald::updateChange/update/external
 // (ewald.h:613-729), getSurfaceEnergy (ewald.h:277-291).
 //
-// Q(k) bookkeeping. Each particle contributes c_k(j) = round(2^40 q_j eff_j
+// Q(k) bookkeeping. Each particle contributes c_k(j) = round(2^28 q_j eff_j
 // e^{i k.r_j}) with e^{ik.r} from sincos_turns on the exact integer phase:
 // a deterministic function of the particle's fixed-point position. Q(k) is
 // kept as the exact int64 sum of these contributions, and an accepted move
@@ -78,23 +78,51 @@ __device__ __forceinline__ df df_div(df a, df b) {
 }
 
 // ------------------------------------------------------------------ pairs (FP32)
+// 1/sqrt(r2) to FP32 accuracy: hardware estimate plus one Newton step.
+__device__ __forceinline__ float rsqrt_nr(float r2) {
+    const float y = rsqrtf(r2);
+    return y * fmaf(-0.5f * r2 * y, y, 1.5f);
+}
+
+// erfc for x >= 0: the Chebyshev fit of Press, Teukolsky, Vetterling and
+// Flannery (Numerical Recipes in C, 2nd ed., section 6.2, "erfcc"),
+// fractional error below 1.2e-7 everywhere.
+__device__ __forceinline__ float erfc_nr(float z) {
+    const float t = __frcp_rn(fmaf(0.5f, z, 1.0f));
+    float p = fmaf(t, 0.17087277f, -0.82215223f);
+    p = fmaf(t, p, 1.48851587f);
+    p = fmaf(t, p, -1.13520398f);
+    p = fmaf(t, p, 0.27886807f);
+    p = fmaf(t, p, -0.18628806f);
+    p = fmaf(t, p, 0.09678418f);
+    p = fmaf(t, p, 0.37409196f);
+    p = fmaf(t, p, 1.00002368f);
+    p = fmaf(t, p, -1.26551223f);
+    return t * expf(fmaf(-z, z, p));
+}
+
 // EwaldReal (kappa-screened form, ewald.h:109) + WCA; qq = qa qb QeQe lB.
+// NEAR: correctly rounded sqrt/divide and erfcf for the few pairs close to
+// contact, whose energies are largest; otherwise reciprocal square root and
+// the Chebyshev erfc.
+template <bool NEAR>
 __device__ __forceinline__ float pair_ewald_wca(float r2, float qq, float s2, float wca2, float eps4,
                                                 const SysDesc &d) {
     float u = 0.0f;
+    const float ri = NEAR ? 1.0f / sqrtf(r2) : rsqrt_nr(r2);
     if (r2 <= d.rc2) {
-        float r = sqrtf(r2);
+        const float r = NEAR ? sqrtf(r2) : r2 * ri;
         float e;
         if (d.kappa == 0.0f) {
-            e = erfcf(d.alpha * r);
+            e = NEAR ? erfcf(d.alpha * r) : erfc_nr(d.alpha * r);
         } else {
-            float k2a = d.kappa / (2.0f * d.alpha);
+            const float k2a = d.kappa / (2.0f * d.alpha);
             e = 0.5f * (erfcf(d.alpha * r + k2a) * expf(d.kappa * r) + erfcf(d.alpha * r - k2a) * expf(-d.kappa * r));
         }
-        u = qq * e / r;
+        u = NEAR ? qq * e / r : qq * e * ri;
     }
     if (r2 <= wca2) {
-        float x = s2 / r2;
+        float x = NEAR ? s2 / r2 : s2 * ri * ri;
         x = x * x * x;
         u += eps4 * (x * x - x + 0.25f);
     }
@@ -103,16 +131,17 @@ __device__ __forceinline__ float pair_ewald_wca(float r2, float qq, float s2, fl
 
 // DebyeHuckel + LennardJonesMixed; qq = qa qb lB.
 __device__ __forceinline__ float pair_dh_lj(float r2, float qq, float s2, float eps4, const SysDesc &d) {
-    float r = sqrtf(r2);
-    float u = qq * expf(-d.kappa * r) / r;
+    const float r = sqrtf(r2);
+    const float u = qq * expf(-d.kappa * r) / r;
     float x = s2 / r2;
     x = x * x * x;
     return u + eps4 * (x * x - x);
 }
 
-template <int MODEL>
+template <int MODEL, bool NEAR = true>
 __device__ __forceinline__ float pair_u(float r2, float qi, float qj, int t, const SysDesc &d) {
-    if (MODEL == MODEL_EWALD) return pair_ewald_wca(r2, qi * qj * d.qeqe[t] * d.lB, d.s2[t], d.wca2[t], d.eps4[t], d);
+    if (MODEL == MODEL_EWALD)
+        return pair_ewald_wca<NEAR>(r2, qi * qj * d.qeqe[t] * d.lB, d.s2[t], d.wca2[t], d.eps4[t], d);
     return pair_dh_lj(r2, qi * qj * d.lB, d.s2[t], d.eps4[t], d);
 }
 
@@ -221,13 +250,11 @@ __device__ __forceinline__ void pair_candidate(const Move &m, int4 pj, int tj, c
     const int t = d.uniform_types ? 0 : m.ti * d.n_types + tj;
     const float s2 = d.core_tab_n > 0 ? d.s2[t] : 0.0f;   // no core table: FP32 throughout
     const bool cn = r2n < s2, co = r2o < s2;
-    if (MODEL == MODEL_DHLJ && !cn && !co) {
-        // Difference form, so the rounding error scales with |u(new) - u(old)|
-        // and not with |u| (no cutoff: every pair contributes). With
-        // r_n^2 - r_o^2 = sum_a (dn_a - do_a)(dn_a + do_a) exact in integers
-        // (minimum images taken separately, as the reference's sqdist does):
-        //   DH: u_o expm1(-kappa (r_n - r_o) - log1p((r_n - r_o)/r_o))
-        //   LJ: 4eps x_o^3 (t^3 - 1)(x_o^3 (t^3 + 1) - 1), t = r_o^2 / r_n^2
+    // near: within 2 sigma (DH) or 1.5 sigma (Ewald) of either position
+    const float near2 = d.s2[t] * (MODEL == MODEL_DHLJ ? 4.0f : 2.25f);
+    const bool near = r2n < near2 || r2o < near2;
+    if (MODEL == MODEL_DHLJ && !cn && !co && near) {
+        // accurate difference form: u_o expm1(-kappa dr - log1p(dr / r_o))
         long long S = 0;
         const int pjv[3] = {pj.x, pj.y, pj.z};
 #pragma unroll
@@ -247,8 +274,55 @@ __device__ __forceinline__ void pair_candidate(const Move &m, int4 pj, int tj, c
         accf += fmaf(uo, expm1f(z), d.eps4[t] * xo3 * t3m1 * fmaf(xo3, t3m1 + 2.0f, -1.0f));
         return;
     }
-    const float un = cn ? 0.0f : pair_u<MODEL>(r2n, m.q, qj, t, d);
-    const float uo = co ? 0.0f : pair_u<MODEL>(r2o, m.q, qj, t, d);
+    if (MODEL == MODEL_DHLJ && !cn && !co) {
+        // Difference form, so the rounding error scales with |u(new) - u(old)|
+        // and not with |u| (no cutoff: every pair contributes). With
+        // r_n^2 - r_o^2 = sum_a (dn_a - do_a)(dn_a + do_a) exact in integers
+        // (minimum images taken separately, as the reference's sqdist does):
+        //   LJ: 4eps x_o^3 (t^3 - 1)(x_o^3 (t^3 + 1) - 1), t = r_o^2 / r_n^2
+        long long S = 0;
+        const int pjv[3] = {pj.x, pj.y, pj.z};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            long long dn = (int)(pjv[a] - m.hn[a]), dO = (int)(pjv[a] - m.ho[a]);
+            S += (dn - dO) * (dn + dO);
+        }
+        // DH: u_n/u_o - 1 = (expm1(-kappa dr) - t)/(1 + t), t = dr/r_o, with
+        // expm1 by its Taylor series (|kappa dr| is small) or expm1f.
+        const float dR2 = (float)S * d.s32sq;
+        const float rio = rsqrt_nr(r2o), rin = rsqrt_nr(r2n);
+        const float ro = r2o * rio, rn = r2n * rin;
+        const float dr = dR2 * __frcp_rn(rn + ro);
+        const float tt = dr * rio;
+        const float y = -d.kappa * dr;
+        float em1;
+        if (fabsf(y) < 0.25f) {
+            em1 = fmaf(y, 1.0f / 5040.0f, 1.0f / 720.0f);
+            em1 = fmaf(y, em1, 1.0f / 120.0f);
+            em1 = fmaf(y, em1, 1.0f / 24.0f);
+            em1 = fmaf(y, em1, 1.0f / 6.0f);
+            em1 = fmaf(y, em1, 0.5f);
+            em1 = fmaf(y * y, em1, y);
+        } else {
+            em1 = expm1f(y);
+        }
+        const float uo = m.q * qj * d.lB * expf(-d.kappa * ro) * rio;
+        const float ddh = uo * (em1 - tt) * __frcp_rn(1.0f + tt);
+        const float xo = d.s2[t] * rio * rio;
+        const float xo3 = xo * xo * xo;
+        const float tau = -dR2 * (rin * rin);
+        const float t3m1 = tau * fmaf(tau, tau + 3.0f, 3.0f);
+        accf += fmaf(d.eps4[t] * xo3, t3m1 * fmaf(xo3, t3m1 + 2.0f, -1.0f), ddh);
+        return;
+    }
+    float un, uo;
+    if (near) {
+        un = cn ? 0.0f : pair_u<MODEL, true>(r2n, m.q, qj, t, d);
+        uo = co ? 0.0f : pair_u<MODEL, true>(r2o, m.q, qj, t, d);
+    } else {
+        un = pair_u<MODEL, false>(r2n, m.q, qj, t, d);
+        uo = pair_u<MODEL, false>(r2o, m.q, qj, t, d);
+    }
     accf += un - uo;
     if (cn || co) {
         const short4 e = *ext;
@@ -270,6 +344,7 @@ struct Smem {
     uint32_t *kpack;    // K: n vector
     longlong2 *qfix;    // K: Q(k), exact fixed point
     float2 *qf;         // K: Q(k) rounded to float (energy)
+    float2 *eold;       // K: e^{ik.r_old} of the current trial
     int4 *pos;          // N (positions in shared memory)
     short4 *pos_ext;    // N
     uint8_t *ptype;     // N
@@ -287,8 +362,8 @@ __host__ __device__ __forceinline__ size_t smem_layout(int N, int K, int ncell, 
     if (kspace) b += (size_t)K * 16;
     off[1] = b;                                   // qfix
     if (kspace) b += (size_t)K * 16;
-    off[2] = b;                                   // qf
-    if (kspace) b += (size_t)K * 8;
+    off[2] = b;                                   // qf, eold
+    if (kspace) b += (size_t)K * 16;
     off[3] = b;                                   // kpack
     if (kspace) b = align16(b + (size_t)K * 4);
     off[4] = b;                                   // pos, pos_ext, ptype
@@ -310,6 +385,7 @@ __device__ __forceinline__ Smem carve(char *base, const SysDesc &d, bool kspace,
     s.kvec = (float4 *)(base + off[0]);
     s.qfix = (longlong2 *)(base + off[1]);
     s.qf = (float2 *)(base + off[2]);
+    s.eold = (float2 *)(base + off[2] + (size_t)d.K * 8);
     s.kpack = (uint32_t *)(base + off[3]);
     s.pos = (int4 *)(base + off[4]);
     s.pos_ext = (short4 *)(base + off[4] + (size_t)d.N * 16);
@@ -327,9 +403,13 @@ __device__ __forceinline__ void load_desc(SysDesc &dst, const SysDesc *__restric
     __syncthreads();
 }
 
-__device__ __forceinline__ float2 q_to_float(longlong2 q) {
-    return make_float2(__ll2float_rn(q.x) * 9.094947017729282e-13f, __ll2float_rn(q.y) * 9.094947017729282e-13f);
+// Q(k) fixed point (units of 2^-28) to float, by 32-bit halves.
+__device__ __forceinline__ float fix28_to_float(long long v) {
+    const int hi = (int)(v >> 32);
+    const unsigned lo = (unsigned)v;
+    return fmaf((float)hi, 16.0f, (float)lo * 3.7252902984619141e-09f);
 }
+__device__ __forceinline__ float2 q_to_float(longlong2 q) { return make_float2(fix28_to_float(q.x), fix28_to_float(q.y)); }
 
 __device__ __forceinline__ void load_smem(const SysDesc &d, const Smem &s, bool kspace, bool pos_smem, bool cells,
                                           const float2 *sc_tab) {
@@ -423,6 +503,7 @@ __device__ __forceinline__ float kspace_energy(const Move &m, const SysDesc &d, 
         unpack_n(s.kpack[k], nx, ny, nz);
         const uint32_t ph = phase(nx, ny, nz, m.ho);
         const float2 e = sincos_turns(ph, s.sc_tab);
+        s.eold[k] = e;
         const float4 kv = s.kvec[k];
         const float phi = fmaf(kv.x, m.dxf[0], fmaf(kv.y, m.dxf[1], kv.z * m.dxf[2]));
         float2 w;
@@ -441,23 +522,25 @@ __device__ __forceinline__ float kspace_energy(const Move &m, const SysDesc &d, 
     return acc;
 }
 
-// One particle's exact contribution to Q(k) (see the file comment).
-__device__ __forceinline__ longlong2 qk_contrib(float qe, uint32_t ph, const float2 *tab) {
-    const float2 e = sincos_turns(ph, tab);
-    return make_longlong2(__float2ll_rn(qe * e.x * 1099511627776.0f), __float2ll_rn(qe * e.y * 1099511627776.0f));
+// One particle's exact contribution to Q(k) (see the file comment), from
+// e = sincos_turns of its phase: round(2^28 q eff e), a 32-bit integer for
+// |q eff| < 8.
+__device__ __forceinline__ int2 qk_contrib(float qe, float2 e) {
+    return make_int2(__float2int_rn(qe * e.x * 268435456.0f), __float2int_rn(qe * e.y * 268435456.0f));
 }
 
-// Accepted move: Q(k) += c_k(new) - c_k(old) for this thread's k-vectors.
+// Accepted move: Q(k) += c_k(new) - c_k(old) for this thread's k-vectors;
+// e^{ik.r_old} was left in shared memory by kspace_energy.
 __device__ __forceinline__ void kspace_commit(const Move &m, const SysDesc &d, const Smem &s) {
     const float qe = m.q * d.eff[m.ti];
     for (int k = threadIdx.x; k < d.K; k += blockDim.x) {
         int nx, ny, nz;
         unpack_n(s.kpack[k], nx, ny, nz);
-        const longlong2 cn = qk_contrib(qe, phase(nx, ny, nz, m.hn), s.sc_tab);
-        const longlong2 co = qk_contrib(qe, phase(nx, ny, nz, m.ho), s.sc_tab);
+        const int2 cn = qk_contrib(qe, sincos_turns(phase(nx, ny, nz, m.hn), s.sc_tab));
+        const int2 co = qk_contrib(qe, s.eold[k]);
         longlong2 q = s.qfix[k];
-        q.x += cn.x - co.x;
-        q.y += cn.y - co.y;
+        q.x += (long long)cn.x - (long long)co.x;
+        q.y += (long long)cn.y - (long long)co.y;
         s.qfix[k] = q;
         s.qf[k] = q_to_float(q);
     }
@@ -798,7 +881,7 @@ __global__ void __launch_bounds__(256) qk_rebuild_kernel(const SysDesc *__restri
         if (k < d.K)
             for (int t = 0; t < nb; t++) {
                 const int h[3] = {pj[t].x, pj[t].y, pj[t].z};
-                const longlong2 c = qk_contrib(qe[t], phase(nx, ny, nz, h), tab);
+                const int2 c = qk_contrib(qe[t], sincos_turns(phase(nx, ny, nz, h), tab));
                 sx += c.x;
                 sy += c.y;
             }
@@ -833,8 +916,8 @@ __global__ void __launch_bounds__(1024) qk_rebuild_finish(const SysDesc *__restr
         if (qo.x != qn.x || qo.y != qn.y) {
             bad = 1;
             const float2 fo = q_to_float(qo), fn = q_to_float(qn);
-            const float dre = __ll2float_rn(qn.x - qo.x) * 9.094947017729282e-13f;
-            const float dim = __ll2float_rn(qn.y - qo.y) * 9.094947017729282e-13f;
+            const float dre = fix28_to_float(qn.x - qo.x);
+            const float dim = fix28_to_float(qn.y - qo.y);
             e = df_add_f(e, d.kvec[k].w * fmaf(dre, fo.x + fn.x, dim * (fo.y + fn.y)));
         }
         d.qfix[k] = qn;

@@ -184,7 +184,9 @@ int fg_server_destroy(fg_server *s);
 int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const double *xyz, const double *charge,
                      const int32_t *type_ids, uint32_t seed, int64_t n_trials, int64_t *job_id);
 int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double *device_ms);
-/* state: 0 queued, 1 running, 2 done, 3 failed. xyz (3N) filled once done. */
+/* state: 0 queued, 1 running, 2 done, 3 failed. xyz (3N) filled once done
+ * (finished jobs keep their results in host memory; their device memory is
+ * returned to the budget at once). */
 int fg_server_poll(fg_server *s, int64_t job_id, int32_t *state, int64_t *trials_done, int64_t *accepted,
                    double *energy, double *xyz);
 int fg_server_release(fg_server *s, int64_t job_id);

@@ -506,4 +506,52 @@ double or_mc_run_stream(void *h, int64_t n_trials, const int32_t *idx, const dou
     return utot;
 }
 
+// ---------------------------------------------------------------- Philox
+// Philox4x32-10 (Salmon et al., SC'11): the counter-based generator the GPU
+// library uses for device-generated trial streams, restated here so those
+// streams can be regenerated and checked on the host.
+static void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; r++) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1, n3 = (uint32_t)p0;
+        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+void or_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    philox(c, key[0], key[1]);
+    for (int i = 0; i < 4; i++) out[i] = c[i];
+}
+
+// The device trial-stream definition: for trial g (counter), r = philox(g, 0),
+// r2 = philox(g, 1) under key (seed, stream): particle floor(r0 N / 2^32),
+// displacement_a = (r_a - 2^31) * round(dp_type / L_a * 2^32) in units of
+// L_a / 2^64, u = (r2_0 + 0.5) / 2^32.
+void or_philox_stream(uint32_t seed, uint32_t stream, int64_t first, int64_t n, int32_t n_particles,
+                      const int32_t *types, const double *type_dp, const double *box, int32_t *idx, double *disp,
+                      double *u) {
+    for (int64_t t = 0; t < n; t++) {
+        const int64_t g = first + t;
+        uint32_t r[4] = {(uint32_t)g, (uint32_t)(g >> 32), 0u, 0u};
+        uint32_t r2[4] = {(uint32_t)g, (uint32_t)(g >> 32), 1u, 0u};
+        philox(r, seed, stream);
+        philox(r2, seed, stream);
+        const int i = (int)(((uint64_t)r[0] * (uint32_t)n_particles) >> 32);
+        idx[t] = i;
+        for (int a = 0; a < 3; a++) {
+            const int64_t dpf = (int64_t)llrint(type_dp[types[i]] / box[a] * 4294967296.0);
+            const int64_t dfix = (int64_t)(int32_t)(r[1 + a] - 0x80000000u) * dpf;
+            disp[3 * t + a] = (double)dfix * (box[a] / 18446744073709551616.0);
+        }
+        u[t] = ((double)r2[0] + 0.5) * (1.0 / 4294967296.0);
+    }
+}
+
+void or_set_kT(void *h, double kT) { ((System *)h)->P.kT_scale = kT; }
+
 }  // extern "C"

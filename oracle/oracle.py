@@ -51,6 +51,9 @@ def lib():
         L.or_draw_translation_stream.argtypes = [u32, i32, dp, i64, dp, dp, dp]
         L.or_mc_run.restype = ctypes.c_double
         L.or_mc_run.argtypes = [vp, u32, i64, dp, dp, dp, dp]
+        L.or_philox.argtypes = [dp, dp, dp]
+        L.or_philox_stream.argtypes = [u32, u32, i64, i64, ctypes.c_int32, dp, dp, dp, dp, dp, dp]
+        L.or_set_kT.argtypes = [vp, ctypes.c_double]
         L.or_mc_run_stream.restype = ctypes.c_double
         L.or_mc_run_stream.argtypes = [vp, i64, dp, dp, dp, dp, dp]
         _lib = L
@@ -147,6 +150,28 @@ def _mc_run_stream(self, idx, disp, u):
 
 
 OracleSystem.mc_run_stream = _mc_run_stream
+OracleSystem.set_kT = lambda self, kT: lib().or_set_kT(self.h, float(kT))
+
+
+def philox(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.empty(4, dtype=np.uint32)
+    lib().or_philox(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def philox_stream(seed, stream, first, n, types, type_dp, box):
+    """The device trial-stream definition regenerated on the host."""
+    types = np.ascontiguousarray(types, dtype=np.int32)
+    tdp = np.ascontiguousarray(type_dp, dtype=np.float64)
+    b = np.ascontiguousarray(box, dtype=np.float64)
+    idx = np.empty(n, np.int32)
+    disp = np.empty((n, 3))
+    u = np.empty(n)
+    lib().or_philox_stream(seed, stream, first, n, len(types), _ptr(types), _ptr(tdp), _ptr(b), _ptr(idx),
+                           _ptr(disp), _ptr(u))
+    return idx, disp, u
 
 
 def translation_stream(seed, dp_per_particle, n_trials):

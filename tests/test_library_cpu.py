@@ -54,3 +54,14 @@ def test_params_layout_matches_header():
     # 2 int32, 3+1 double, 4x16 double, 5 double, 2 int32, 5 double, 1 double, 8 int32
     expected = 8 + 32 + 4 * 16 * 8 + 5 * 8 + 8 + 4 * 8 + 8 + 8 * 4
     assert ctypes.sizeof(FgParams) == expected
+
+
+def test_oracle_philox_matches_library():
+    """The oracle's Philox restatement and the library's agree."""
+    from beofaunus_gb300.gpu import philox4x32_10
+    from oracle.oracle import philox
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        c = rng.integers(0, 2 ** 32, 4, dtype=np.uint64).astype(np.uint32)
+        k = rng.integers(0, 2 ** 32, 2, dtype=np.uint64).astype(np.uint32)
+        np.testing.assert_array_equal(philox(c, k), philox4x32_10(c, k))
