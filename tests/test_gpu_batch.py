@@ -113,13 +113,13 @@ def test_server_result_same_alone_and_mixed():
     assert mixed["A"]["energy"] == alone["A"]["energy"]
     # a budget that holds one job at a time: jobs queue and still all finish,
     # with unchanged results
+    from beofaunus_gb300.gpu import System
     one_job = 0
     for k in "ABC":
-        srv = Server(1 << 30, threads=256, round_pairs=1 << 18)
         (p, x, q, t), seed = jobs[k]
-        srv.submit(p, x, q, t, seed, 3 * len(x))
-        srv.step()
-        one_job = max(one_job, srv.bytes_in_use)
+        n = len(x)
+        stream = min(3 * n, max(n, (1 << 18) // n)) * 40
+        one_job = max(one_job, System(p, x, q, t, threads=256).device_bytes + stream)
     tight, maxr1, _ = run(["B", "A", "C"], int(1.3 * one_job))
     assert maxr1 == 1
     np.testing.assert_array_equal(tight["A"]["xyz"], alone["A"]["xyz"])
