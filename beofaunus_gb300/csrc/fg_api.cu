@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <string>
 #include <vector>
@@ -1034,3 +1035,4 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 }  // extern "C"
 
 #include "fg_batch.cu"
+#include "fg_noalloc.cu"

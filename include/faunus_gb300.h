@@ -192,6 +192,28 @@ int fg_server_poll(fg_server *s, int64_t job_id, int32_t *state, int64_t *trials
 int fg_server_release(fg_server *s, int64_t job_id);
 int64_t fg_server_bytes_in_use(fg_server *s);
 
+/* ---- pair energy without device allocation ---------------------------------
+ * No counterpart in the reference. For callers that cannot call cudaMalloc:
+ * a plugin inside a host application that owns the whole GPU memory pool and
+ * only hands out buffers it allocated itself, or a time-critical loop that
+ * must not call the allocator (cudaMalloc/cudaFree may synchronize the
+ * device). Computes the pair part of systemEnergy (energy.h:169-180; the
+ * same value as component 0 of fg_total_energy) for n particles given in
+ * caller-owned DEVICE buffers: d_xyz[3n], d_charge[n] (or NULL for the type
+ * charges), d_types[n]; writes one double to d_energy, on `stream` (a
+ * cudaStream_t, or NULL for the default stream). Asynchronous: synchronize
+ * the stream before reading d_energy.
+ * Every temporary lives in one fixed __device__ array of about 1.7 MB, held
+ * by every GPU that loads this library until the process exits; the call
+ * allocates nothing. n is limited to FG_NOALLOC_MAX_PARTICLES (larger n:
+ * FG_ERR_CAPACITY). The first call on a device looks up that array's device
+ * address, with the device current; make that first call before any stream
+ * capture. All calls share the array: calls that overlap on the GPU race and
+ * give wrong results, so serialize them. */
+#define FG_NOALLOC_MAX_PARTICLES 65536
+int fg_pair_energy_noalloc(const fg_params *params, int32_t n, const double *d_xyz, const double *d_charge,
+                           const int32_t *d_types, double *d_energy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
