@@ -427,6 +427,7 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
         stats->sweep_kernel_ms = sweep_ms;
         stats->sweep_launches = launches;
         stats->error_flags = s.error;
+        stats->kernel_launches = (int64_t)launches * (rebuilds ? 3 : 1);
     }
     if (s.error) return fail(FG_ERR_DEVICE, "device error flags 0x%x", s.error);
     return FG_OK;

@@ -161,17 +161,29 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
     int64_t maxc = 0;
     for (auto c : counts) maxc = std::max(maxc, c);
     int64_t prev_done = -1;
+    int64_t kernels = 2;   // the reset and the first gather
+    std::vector<cudaEvent_t> evs;
     while (true) {
         const int pairs = b->rebuilds ? (int)std::min<int64_t>(maxc / uf + 1, 64) : 1;
         for (int p = 0; p < pairs; p++) {
+            cudaEvent_t e0, e1;
+            CK(cudaEventCreate(&e0));
+            CK(cudaEventCreate(&e1));
+            evs.push_back(e0);
+            evs.push_back(e1);
+            CK(cudaEventRecord(e0, b->stream));
             b->cfg.fn<<<n, b->cfg.threads, b->cfg.smem, b->stream>>>(b->d_descs, INT64_MAX, b->sys[0]->sc_tab);
             CK(cudaGetLastError());
+            CK(cudaEventRecord(e1, b->stream));
             launches++;
+            kernels++;
             if (b->rebuilds) {
                 int rc = launch_rebuild(b->d_descs, n, b->maxN, b->maxK, b->d_corr, b->stream);
                 if (rc) return rc;
+                kernels += 2;
             }
         }
+        kernels++;
         fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
         CK(cudaMemcpyAsync(s.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
         CK(cudaStreamSynchronize(b->stream));
@@ -188,8 +200,15 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
     }
     CK(cudaEventRecord(b->ev1, b->stream));
     CK(cudaEventSynchronize(b->ev1));
-    float ms = 0.0f;
+    float ms = 0.0f, sweep_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    for (size_t e = 0; e + 1 < evs.size(); e += 2) {
+        float t = 0.0f;
+        CK(cudaEventElapsedTime(&t, evs[e], evs[e + 1]));
+        sweep_ms += t;
+        cudaEventDestroy(evs[e]);
+        cudaEventDestroy(evs[e + 1]);
+    }
     fg_sweep_stats tot{};
     int errs = 0;
     for (int i = 0; i < n; i++) {
@@ -199,9 +218,10 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
         st.rebuilds = s[i].n_rebuilds - s0[i].n_rebuilds;
         st.energy_change = df_val(s[i].u_hi, s[i].u_lo);
         st.device_ms = ms;
-        st.sweep_kernel_ms = ms;
+        st.sweep_kernel_ms = sweep_ms;
         st.sweep_launches = launches;
         st.error_flags = s[i].error;
+        st.kernel_launches = kernels;
         errs |= s[i].error;
         if (per) per[i] = st;
         tot.trials += st.trials;
@@ -210,9 +230,10 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
         tot.energy_change += st.energy_change;
     }
     tot.device_ms = ms;
-    tot.sweep_kernel_ms = ms;
+    tot.sweep_kernel_ms = sweep_ms;
     tot.sweep_launches = launches;
     tot.error_flags = errs;
+    tot.kernel_launches = kernels;
     if (total) *total = tot;
     for (fg_system *h : b->sys) h->cnt_accepted_host = 0;
     if (errs) return fail(FG_ERR_DEVICE, "device error flags 0x%x in a batch member", errs);
@@ -305,6 +326,12 @@ int fg_batch_stream_philox(fg_batch *b, const int64_t *counts, uint32_t seed, co
     }
     CK(cudaStreamSynchronize(b->stream));
     return FG_OK;
+}
+
+int fg_batch_stream_upload(fg_batch *b, int32_t member, int64_t n, const int32_t *idx, const double *disp,
+                           const double *u) {
+    if (!b || member < 0 || member >= (int)b->sys.size()) return fail(FG_ERR_INVALID, "bad member");
+    return fg_stream_upload(b->sys[member], n, idx, disp, u);
 }
 
 int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total) {
@@ -431,6 +458,7 @@ int fg_pt_run(fg_batch *b, int32_t rounds, int32_t sweeps_per_round, fg_sweep_st
     tot.sweep_kernel_ms = ms;
     tot.sweep_launches = rounds;
     tot.error_flags = errs;
+    tot.kernel_launches = 4 * (int64_t)rounds + 2;   // philox, reset, sweep, swap per round
     if (total) *total = tot;
     if (errs) return fail(FG_ERR_DEVICE, "device error flags 0x%x", errs);
     return FG_OK;

@@ -25,7 +25,7 @@ class SweepStats(ctypes.Structure):
     _fields_ = [("trials", ctypes.c_int64), ("accepted", ctypes.c_int64), ("rebuilds", ctypes.c_int64),
                 ("energy_change", ctypes.c_double), ("device_ms", ctypes.c_double),
                 ("sweep_kernel_ms", ctypes.c_double), ("sweep_launches", ctypes.c_int32),
-                ("error_flags", ctypes.c_int32)]
+                ("error_flags", ctypes.c_int32), ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -77,6 +77,7 @@ def lib(build_if_missing=True):
             "fg_batch_set_threads": ([vp, i32], ctypes.c_int),
             "fg_batch_stream_philox": ([vp, dp, u32, dp], ctypes.c_int),
             "fg_batch_run": ([vp, dp, dp], ctypes.c_int),
+            "fg_batch_stream_upload": ([vp, i32, i64, dp, dp, dp], ctypes.c_int),
             "fg_pt_setup": ([vp, dp, u32], ctypes.c_int),
             "fg_pt_run": ([vp, i32, i32, dp], ctypes.c_int),
             "fg_pt_get": ([vp, dp, dp, dp, dp], ctypes.c_int),
@@ -276,6 +277,12 @@ class Batch:
         c = np.ascontiguousarray(counts, dtype=np.int64)
         ids = None if stream_ids is None else np.ascontiguousarray(stream_ids, dtype=np.uint32)
         _check(lib().fg_batch_stream_philox(self.h, _p(c), seed, _p(ids)))
+
+    def stream_upload(self, member, idx, disp, u):
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        disp = np.ascontiguousarray(disp, dtype=np.float64).reshape(-1, 3)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        _check(lib().fg_batch_stream_upload(self.h, member, len(idx), _p(idx), _p(disp), _p(u)))
 
     def run(self):
         n = len(self.systems)

@@ -54,6 +54,43 @@ def rsa_positions(n, box, min_dist, seed):
     return out
 
 
+def scatter_positions(n, box, min_dist, seed, max_rounds=1000):
+    """n points uniform in [-L/2, L/2)^3 with no two closer than ``min_dist``
+    (minimum image): draw all points at once, then redraw one point of every
+    overlapping pair until none is left. Vectorised, so large systems start in
+    well under a second; at the low packing fractions used here it converges
+    in a handful of rounds. Unlike rsa_positions this is not sequential
+    addition, but the result has the same property the workloads need: a
+    seeded, uniform, overlap-free start."""
+    from scipy.spatial import cKDTree
+    rng = np.random.default_rng(seed)
+    L = np.asarray(box if hasattr(box, "__len__") else (box, box, box), dtype=np.float64)
+    pts = rng.random((n, 3)) * L
+    pairs = cKDTree(pts, boxsize=L).query_pairs(min_dist, output_type="ndarray")
+    redo = np.unique(pairs.max(axis=1)) if len(pairs) else np.empty(0, dtype=np.int64)
+    for _ in range(max_rounds):
+        if len(redo) == 0:
+            return pts - 0.5 * L
+        pts[redo] = rng.random((len(redo), 3)) * L
+        # only redrawn points can overlap now; each one counts itself once
+        cnt = cKDTree(pts, boxsize=L).query_ball_point(pts[redo], min_dist, return_length=True)
+        redo = redo[cnt > 1]
+    raise RuntimeError("scatter_positions did not converge: density too high")
+
+
+def start_positions(n, box, min_dist, seed, start):
+    """Start configuration: 'rsa', 'scatter', or given positions (n, 3)."""
+    if isinstance(start, np.ndarray):
+        if start.shape != (n, 3):
+            raise ValueError("given start positions must have shape (n, 3)")
+        return np.array(start, dtype=np.float64)
+    if start == "rsa":
+        return rsa_positions(n, box, min_dist, seed)
+    if start == "scatter":
+        return scatter_positions(n, box, min_dist, seed)
+    raise ValueError("start must be 'rsa' or 'scatter'")
+
+
 def salt_types(sigma, eps, dp):
     """A 1:1 salt: type 0 has q=+1, type 1 has q=-1."""
     return [dict(q=1.0, sigma=sigma, eps=eps, dp=dp), dict(q=-1.0, sigma=sigma, eps=eps, dp=dp)]
@@ -67,7 +104,7 @@ def salt_ids(n):
 
 
 def rpm_ewald(n, box, kc, seed, update_frequency=1000, bjerrum=7.1, alpha=0.2, cutoff=20.0,
-              wca_eps=0.1, sigma=4.0, dp=2.0, eps_surf=1e11, use_cell_list=0):
+              wca_eps=0.1, sigma=4.0, dp=2.0, eps_surf=1e11, use_cell_list=0, start="rsa"):
     """Restricted primitive model with Ewald (alpha, real cutoff, |n|<=kc)
     plus WCA repulsion. Returns (params, xyz[n,3], charges[n], type_ids[n])."""
     types = salt_types(sigma, wca_eps, dp)
@@ -75,7 +112,7 @@ def rpm_ewald(n, box, kc, seed, update_frequency=1000, bjerrum=7.1, alpha=0.2, c
                     ewald_cutoff_k=float(kc), ewald_debye_length=1e30, ewald_eps_surf=eps_surf,
                     ewald_spherical_sum=1, ewald_update_frequency=update_frequency,
                     use_cell_list=use_cell_list)
-    xyz = rsa_positions(n, box, sigma, seed)
+    xyz = start_positions(n, box, sigma, seed, start)
     ids = salt_ids(n)
     q = np.where(ids == 0, 1.0, -1.0)
     return p, xyz, q, ids
@@ -93,13 +130,13 @@ def rpm16k(seed=1, **kw):
 
 
 def dh_lj_salt(n, seed, density=0.002, debye_length=10.0, bjerrum=7.1, sigma=4.0, lj_eps=0.2,
-               dp=2.0, kT_scale=1.0):
+               dp=2.0, kT_scale=1.0, start="rsa"):
     """Debye-Hueckel + Lennard-Jones salt at number density ``density``."""
     box = (n / density) ** (1.0 / 3.0)
     types = salt_types(sigma, lj_eps, dp)
     p = make_params(FG_MODEL_DH_LJ, box, bjerrum, types, dh_debye_length=debye_length,
                     kT_scale=kT_scale)
-    xyz = rsa_positions(n, box, sigma, seed)
+    xyz = start_positions(n, box, sigma, seed, start)
     ids = salt_ids(n)
     q = np.where(ids == 0, 1.0, -1.0)
     return p, xyz, q, ids

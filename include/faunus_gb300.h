@@ -40,6 +40,8 @@ typedef struct fg_sweep_stats {
     double sweep_kernel_ms; /* of which in the sweep kernel */
     int32_t sweep_launches; /* sweep kernel launches */
     int32_t error_flags;    /* device error bits (0 = none) */
+    int64_t kernel_launches; /* all kernels this call launched (sweep, Q(k)
+                                rebuild, gather, reset, swap, stream draw) */
 } fg_sweep_stats;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -158,6 +160,9 @@ int fg_batch_set_threads(fg_batch *b, int32_t threads);
 /* Device-generated streams: member s gets counts[s] trials from Philox with
  * key (seed, stream_ids[s]) (stream_ids may be NULL: s). */
 int fg_batch_stream_philox(fg_batch *b, const int64_t *counts, uint32_t seed, const uint32_t *stream_ids);
+/* Stage a host trial stream (fg_stream_upload format) for one member. */
+int fg_batch_stream_upload(fg_batch *b, int32_t member, int64_t n, const int32_t *idx, const double *disp,
+                           const double *u);
 /* Run every member's staged stream; per-member and summed statistics. */
 int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total);
 
