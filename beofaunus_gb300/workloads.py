@@ -9,7 +9,7 @@ import math
 
 import numpy as np
 
-from .params import FG_MODEL_DH_LJ, FG_MODEL_EWALD_WCA, make_params
+from .params import FG_MODEL_DH_LJ, FG_MODEL_EWALD_WCA, FG_MODEL_MULTIPOLE_RF, make_params
 
 
 def rsa_positions(n, box, min_dist, seed):
@@ -152,3 +152,67 @@ def pt_ladder_sizes(n_replicas=64, n_min=500, n_max=4000, seed=7):
 def pt_temperatures(n_replicas=64, t_min=0.8, t_max=2.0):
     """Geometric temperature ladder (reduced units)."""
     return t_min * (t_max / t_min) ** (np.arange(n_replicas) / max(n_replicas - 1, 1))
+
+
+# ---------------------------------------------------------------- rigid dipolar molecules
+def bjerrum_unit(temperature=298.0):
+    """pc::lB(1.0): the Bjerrum length at eps_r = 1 with the reference's
+    constants (physconst.h:52-64, 91-94), in Angstrom."""
+    e, e0, kB = 1.602177e-19, 8.85419e-12, 1.380658e-23
+    return e * e / (4 * math.pi * e0 * 1.0 * 1e-10 * kB * temperature)
+
+
+def molecule_conformation(rng, molsize, radius, min_dist):
+    """One rigid molecule: ``molsize`` sites uniform in a ball of ``radius``,
+    no two closer than ``min_dist``, centred on their geometric centre."""
+    pts = []
+    while len(pts) < molsize:
+        v = rng.uniform(-radius, radius, 3)
+        if v @ v > radius * radius:
+            continue
+        if all(np.sum((v - q) ** 2) >= min_dist * min_dist for q in pts):
+            pts.append(v)
+    pts = np.array(pts)
+    return pts - pts.mean(axis=0)
+
+
+def dipolar_molecules(n_mol=1000, seed=1, molsize=20, box=None, sigma=3.5, lj_eps=0.2, mu=1.5, bjerrum=7.1,
+                      cutoff=15.0, eps_rf=1e11, mol_radius=4.0, temperature=298.0):
+    """Rigid ``molsize``-site molecules: site charges from {-1, 0, +1} with net
+    zero per molecule (half the sites drawn, the other half their negatives),
+    site LJ sigma, one point dipole |mu| (e*Angstrom) in random orientation on
+    site 0. Default box keeps 1000 molecules in a 150 Angstrom cube.
+
+    Returns (params, xyz[N,3], mu_unit[N,3], mu_scalar[N], type_ids[N]);
+    types 0, 1, 2 carry q = -1, 0, +1."""
+    rng = np.random.default_rng(seed)
+    if box is None:
+        box = 150.0 * (n_mol / 1000.0) ** (1.0 / 3.0)
+    L = float(box)
+    types = [dict(q=-1.0, sigma=sigma, eps=lj_eps), dict(q=0.0, sigma=sigma, eps=lj_eps),
+             dict(q=1.0, sigma=sigma, eps=lj_eps)]
+    eps_r = bjerrum_unit(temperature) / bjerrum
+    p = make_params(FG_MODEL_MULTIPOLE_RF, L, bjerrum, types, rf_cutoff=cutoff, rf_eps_rf=eps_rf,
+                    rf_eps_r=eps_r)
+    # molecule centres at least 2 R + sigma apart: no two sites of different
+    # molecules overlap at the start
+    centres = scatter_positions(n_mol, L, 2 * mol_radius + sigma, int(rng.integers(1 << 31)))
+    n = n_mol * molsize
+    xyz = np.empty((n, 3))
+    mu_u = np.zeros((n, 3))
+    mu_s = np.zeros(n)
+    ids = np.empty(n, dtype=np.int32)
+    half = molsize // 2
+    for m in range(n_mol):
+        conf = molecule_conformation(rng, molsize, mol_radius, 2.0)
+        r = centres[m] + conf
+        r -= L * np.round(r / L)
+        xyz[m * molsize:(m + 1) * molsize] = r
+        q = rng.integers(-1, 2, half)
+        qs = np.concatenate([q, -q, np.zeros(molsize - 2 * half, dtype=q.dtype)])
+        rng.shuffle(qs)
+        ids[m * molsize:(m + 1) * molsize] = qs + 1
+        v = rng.normal(size=3)
+        mu_u[m * molsize] = v / np.linalg.norm(v)
+        mu_s[m * molsize] = mu
+    return p, xyz, mu_u, mu_s, ids

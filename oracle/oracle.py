@@ -12,15 +12,16 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libfg_oracle.so")
-SRC = os.path.join(HERE, "fg_oracle.cpp")
+SRCS = [os.path.join(HERE, f) for f in ("fg_oracle.cpp", "fg_oracle_mol.cpp", "or_common.h")]
 
 
 def build(force=False):
     """Compile the oracle with the host g++ (plain C++17, no GPU)."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(f) for f in SRCS):
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-o", LIB, SRC])
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-o", LIB] +
+                          [f for f in SRCS if f.endswith(".cpp")])
     return LIB
 
 
@@ -56,6 +57,20 @@ def lib():
         L.or_set_kT.argtypes = [vp, ctypes.c_double]
         L.or_mc_run_stream.restype = ctypes.c_double
         L.or_mc_run_stream.argtypes = [vp, i64, dp, dp, dp, dp, dp]
+        L.or_mol_create.restype = vp
+        L.or_mol_create.argtypes = [vp, i32, i32]
+        L.or_mol_destroy.argtypes = [vp]
+        L.or_mol_set_state.argtypes = [vp, dp, dp, dp, dp, dp]
+        L.or_mol_get_state.argtypes = [vp, dp, dp, dp]
+        L.or_mol_pair.restype = ctypes.c_double
+        L.or_mol_pair.argtypes = [vp, i32, i32]
+        L.or_mol_trial_du_explicit.restype = ctypes.c_double
+        L.or_mol_trial_du_explicit.argtypes = [vp, i32, dp, dp]
+        L.or_mol_commit.argtypes = [vp, i32]
+        L.or_mol_total_energy.argtypes = [vp, dp]
+        L.or_mol_draw_stream.argtypes = [u32, i32, ctypes.c_double, ctypes.c_double, i32, i64, dp, dp, dp, dp, dp, dp]
+        L.or_mol_run_stream.restype = ctypes.c_double
+        L.or_mol_run_stream.argtypes = [vp, i64, dp, dp, dp, dp, dp, dp, i32, i32, dp, dp]
         _lib = L
     return _lib
 
@@ -184,3 +199,78 @@ def translation_stream(seed, dp_per_particle, n_trials):
     u = np.empty(n)
     lib().or_draw_translation_stream(seed, len(dpp), _ptr(dpp), n, _ptr(idx), _ptr(disp), _ptr(u))
     return idx, disp, u
+
+
+class OracleMol:
+    """FP64 restatement of a reference system of rigid dipolar molecules
+    (NonbondedVector + CoulombGalore/LJ/IonDipole/DipoleDipoleGalore RF,
+    TranslateRotate)."""
+
+    def __init__(self, params, xyz, mu, mus, type_ids, group_size, cms=None):
+        n = len(type_ids)
+        self.n, self.gs, self.m = n, group_size, n // group_size
+        self.h = lib().or_mol_create(ctypes.byref(params), n, group_size)
+        if not self.h:
+            raise ValueError("bad molecule system")
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        mu = np.ascontiguousarray(mu, dtype=np.float64).reshape(-1, 3)
+        mus = np.ascontiguousarray(mus, dtype=np.float64)
+        ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+        c = None if cms is None else np.ascontiguousarray(cms, dtype=np.float64).reshape(-1, 3)
+        lib().or_mol_set_state(self.h, _ptr(xyz), _ptr(mu), _ptr(mus), _ptr(ids), _ptr(c))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_mol_destroy(self.h)
+            self.h = None
+
+    def state(self):
+        xyz = np.empty((self.n, 3))
+        mu = np.empty((self.n, 3))
+        cm = np.empty((self.m, 3))
+        lib().or_mol_get_state(self.h, _ptr(xyz), _ptr(mu), _ptr(cm))
+        return xyz, mu, cm
+
+    def pair(self, i, j):
+        return lib().or_mol_pair(self.h, i, j)
+
+    def trial_du(self, g, xyz, mu=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        mu = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64).reshape(-1, 3)
+        return lib().or_mol_trial_du_explicit(self.h, g, _ptr(xyz), _ptr(mu))
+
+    def commit(self, accepted):
+        lib().or_mol_commit(self.h, 1 if accepted else 0)
+
+    def total_energy(self):
+        """(intermolecular, intramolecular, total) as systemEnergy sums them."""
+        c = np.empty(3)
+        lib().or_mol_total_energy(self.h, _ptr(c))
+        return c
+
+    def run_stream(self, st, rotate=True, translate=True):
+        n = len(st["group"])
+        du = np.empty(n)
+        acc = np.empty(n, np.uint8)
+        g = np.ascontiguousarray(st["group"], dtype=np.int32)
+        ax = np.ascontiguousarray(st["axis"], dtype=np.float64)
+        ce = np.ascontiguousarray(st["center"], dtype=np.int32)
+        an = np.ascontiguousarray(st["angle"], dtype=np.float64)
+        tr = np.ascontiguousarray(st["trans"], dtype=np.float64)
+        u = np.ascontiguousarray(st["u"], dtype=np.float64)
+        usum = lib().or_mol_run_stream(self.h, n, _ptr(g), _ptr(ax), _ptr(ce), _ptr(an), _ptr(tr), _ptr(u),
+                                       1 if rotate else 0, 1 if translate else 0, _ptr(du), _ptr(acc))
+        return dict(usum=usum, du=du, acc=acc)
+
+
+def mol_stream(seed, n_groups, dp, dprot, center_rotation, n):
+    """The reference's global-slump draws for n TranslateRotate trials."""
+    g = np.empty(n, np.int32)
+    ax = np.empty((n, 3))
+    ce = np.empty(n, np.int32)
+    an = np.empty(n)
+    tr = np.empty((n, 3))
+    u = np.empty(n)
+    lib().or_mol_draw_stream(seed, n_groups, dp, dprot, 1 if center_rotation else 0, n, _ptr(g), _ptr(ax),
+                             _ptr(ce), _ptr(an), _ptr(tr), _ptr(u))
+    return dict(group=g, axis=ax, center=ce, angle=an, trans=tr, u=u)

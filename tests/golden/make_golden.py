@@ -1,11 +1,11 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Runs the reference harness (oracle/ref/ref_harness.cpp, linked against the
-reference library built from its own sources by oracle/ref/Makefile) on
-seeded synthetic systems and stores what the reference computed: per-trial
-particle index, trial position, dU and acceptance, plus the total energies
-before and after. Needs the reference checkout; the committed .npz files are
-what the tests read.
+Runs the reference harnesses (oracle/ref/ref_harness.cpp and
+ref_harness_mol.cpp, linked against the reference library built from its own
+sources by oracle/ref/Makefile) on seeded synthetic systems and stores what
+the reference computed: per-trial particle (or molecule) index, trial
+position, dU and acceptance, plus the total energies before and after. Needs
+the reference checkout; the committed .npz files are what the tests read.
 
     python tests/golden/make_golden.py [--ref /root/reference]
 """
@@ -64,6 +64,68 @@ CASES = {
 }
 
 
+# rigid dipolar molecules: (n_molecules, workload seed, RNG seed, sweeps, center_rotation)
+MOL_CASES = {
+    "mol_small": (40, 21, 201, 3, True),
+    "mol_endrot": (27, 22, 202, 3, False),
+    "mol_125": (125, 23, 203, 1, True),
+}
+
+
+def mol_input(mode, params, xyz, mu, mus, ids, seed, sweeps, center_rotation, molsize=20, dp=1.0, dprot=0.3):
+    types = [dict(q=params.type_charge[t], sigma=params.type_sigma[t], eps=params.type_eps[t])
+             for t in range(params.n_types)]
+    return dict(mode=mode, box=params.box[0], temperature=298.0, bjerrum=params.bjerrum, cutoff=params.rf_cutoff,
+                eps_rf=params.rf_eps_rf, types=types, molsize=molsize, n_mol=len(ids) // molsize,
+                type_ids=[int(i) for i in ids], positions=xyz.tolist(), mu=mu.tolist(),
+                muscalar=[float(m) for m in mus], dp=dp, dprot=dprot, center_rotation=center_rotation,
+                seed=seed, sweeps=sweeps)
+
+
+def make_mol(exe, name, n_mol, wseed, seed, sweeps, center_rotation):
+    params, xyz, mu, mus, ids = workloads.dipolar_molecules(n_mol, seed=wseed)
+    out = run_harness(exe, mol_input("mol_mc", params, xyz, mu, mus, ids, seed, sweeps, center_rotation))
+    n = len(out["du"])
+    extra = {}
+    if name == "mol_small":
+        # pair energies on chosen site pairs: random ones, every dipole site
+        # against sites within 16 A, near contacts
+        rng = np.random.default_rng(5)
+        N = len(ids)
+        pairs = set()
+        while len(pairs) < 300:
+            a, b = rng.integers(0, N, 2)
+            if a // 20 != b // 20:
+                pairs.add((int(a), int(b)))
+        L = params.box[0]
+        d = xyz[:, None, :] - xyz[None, :, :]
+        d -= L * np.round(d / L)
+        r = np.sqrt((d ** 2).sum(-1))
+        for a in np.nonzero(mus)[0]:
+            for b in np.nonzero((r[a] < 16.0) & (np.arange(N) // 20 != a // 20))[0]:
+                pairs.add((int(a), int(b)))
+        close = np.argwhere((r < 4.0) & ((np.arange(N)[:, None] // 20) != (np.arange(N)[None, :] // 20)))
+        for a, b in close[:100]:
+            pairs.add((int(a), int(b)))
+        pairs = sorted(pairs)
+        pu = run_harness(exe, dict(mol_input("mol_pairs", params, xyz, mu, mus, ids, seed, 0, center_rotation),
+                                   pairs=pairs))
+        extra = dict(pairs=np.asarray(pairs, dtype=np.int32), pair_u=np.asarray(pu["u"]),
+                     pair_total=np.float64(pu["total"][0]))
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        params=np.frombuffer(bytes(params), dtype=np.uint8), xyz=xyz, mu=mu, mus=mus, ids=ids,
+        seed=np.int64(seed), sweeps=np.int64(sweeps), center_rotation=np.int64(center_rotation),
+        dp=np.float64(1.0), dprot=np.float64(0.3), cm0=np.asarray(out["cm0"]).reshape(-1, 3),
+        u0=np.float64(out["u0"][0]), u1=np.float64(out["u1"][0]), u_move_sum=np.float64(out["u_move_sum"][0]),
+        group=np.asarray(out["group"], dtype=np.int32), first_xyz=np.asarray(out["first_xyz"]).reshape(n, 3),
+        first_mu=np.asarray(out["first_mu"]).reshape(n, 3), du=np.asarray(out["du"]),
+        acc=np.asarray(out["acc"], dtype=np.uint8), final_positions=np.asarray(out["final_positions"]).reshape(-1, 3),
+        final_mu=np.asarray(out["final_mu"]).reshape(-1, 3), final_cm=np.asarray(out["final_cm"]).reshape(-1, 3),
+        **extra)
+    print(name, "trials", n, "acceptance %.3f" % np.mean(out["acc"]), "u0 %.6f" % out["u0"][0])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -71,6 +133,13 @@ def main():
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "REF=" + a.ref])
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    exe_mol = os.path.join(ROOT, "oracle", "_ref", "ref_harness_mol")
+    for name, case in MOL_CASES.items():
+        if a.only and name != a.only:
+            continue
+        make_mol(exe_mol, name, *case)
+    if a.only and a.only in MOL_CASES:
+        return
 
     known = run_harness(exe, dict(mode="ewald_known"))
     np.savez_compressed(os.path.join(HERE, "ewald_known.npz"),
