@@ -1037,3 +1037,4 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 
 #include "fg_batch.cu"
 #include "fg_noalloc.cu"
+#include "fg_mol.cu"

@@ -1,0 +1,1563 @@
+// Rigid dipolar molecules on the device: the TranslateRotate trial
+// (move.h:1620-1705) and the whole-molecule energy change of
+// NonbondedVector::g2All/g2g (energy.h:182-215, 1156-1196) over
+//     CoulombGalore (multipole.h:569-598, the live operator: lB q q Q5(r/rc)/r)
+//   + LennardJonesLB (potentials.h:2036-2040, no cutoff)
+//   + IonDipole (multipole.h:993-996 -> q2mu 269-277, no cutoff)
+//   + DipoleDipoleGalore reaction field (multipole.h:767-782, 910-920).
+//
+// Included by fg_api.cu (one translation unit).
+//
+// Work split. One system runs on a thread-block cluster of C CTAs (C <= 16,
+// one per SM). A trial moves one molecule of gs sites; its energy change is a
+// sum over the gs moved sites against all N - gs other sites. CTA r owns the
+// site slice [r N/C, (r+1) N/C) and the dipole-site slice [r D/C, (r+1) D/C),
+// kept in its shared memory, and sums its part; the C partial sums meet
+// through distributed shared memory after one cluster barrier per trial, and
+// every CTA then makes the same Metropolis decision from the same numbers.
+// Each CTA keeps its own replica of the FP64-exact state (64-bit fixed-point
+// positions, FP64 dipole vectors, mass centres) in global memory, so no CTA
+// ever reads what another CTA wrote during the sweep.
+//
+// Precision. Positions are 64-bit fixed point (X = x/L 2^64). The rotation
+// of a trial runs in FP64 on offsets from the rotation centre (20 sites per
+// trial). Pair terms are FP32 except where that would exceed the 1e-6 kT
+// budget:
+//  * far pairs (both r_old, r_new >= rc): LJ and ion-dipole are small; LJ
+//    uses 22-bit-truncated coordinate differences converted without the
+//    conversion pipe, ion-dipole exact 32-bit differences;
+//  * near pairs (r_old or r_new < rc) are queued and evaluated afterwards,
+//    densely: LJ and Coulomb as differences u(r_new) - u(r_old) whose
+//    rounding error scales with the difference, from r_new^2 - r_old^2
+//    computed in FP64 from exact 48-bit coordinate differences; terms with a
+//    dipole in FP64 (a few per trial);
+//  * per-trial sums are double-float (df).
+// The image convention is the reference's minimum image (Cuboid::vdist),
+// taken on exact integer differences.
+namespace fgm {
+
+using fg::df;
+using fg::df_add;
+using fg::df_add_f;
+using fg::df_gt;
+using fg::hi32;
+using fg::warp_sum_df;
+
+constexpr int kMolThreads = 512;
+constexpr int kMaxGroupSites = 32;
+constexpr int kQueueCap = 3072;
+constexpr int kMaxCluster = 16;
+
+// Error bits
+constexpr int kMolErrNonFinite = 8;
+
+struct MolTrial {
+    int32_t g;       // molecule index
+    int32_t flags;   // 1 rotate, 2 translate, 4 explicit new coordinates (expl_*)
+    int32_t center;  // rotation centre: 0 mass centre, 1 first site, 2 last site
+    float thr_hi, thr_lo;  // -ln u as df: reject iff dU > threshold
+    int32_t pad;
+    double qw, qx, qy, qz;  // rotation quaternion (w, v)
+    int64_t t[3];           // translation, fixed point
+};
+
+struct MolScalars {
+    int64_t cursor;      // next trial
+    int64_t n_trials;    // trials in the stream
+    int64_t n_accepted;  // accepted so far (cumulative)
+    int32_t error;
+    int32_t pad;
+    float u_hi, u_lo;        // sum of accepted dU of the current stream
+    float utot_hi, utot_lo;  // running total energy
+};
+
+struct alignas(16) MolDesc {
+    int32_t N, gs, M, D, nt, C, uniform_lj, pad;
+    float s32[3];       // L / 2^32 (one unit of the high word)
+    float sc9[3];       // 512 L / 2^32 (unit of the high word >> 9)
+    double s48d[3];     // L / 2^48
+    double s64d[3];     // L / 2^64
+    double inv64d[3];   // 2^64 / L
+    float lB, rc2, rc2near, rc1i, A5, B5, kT, pad2;
+    double lBd, rcd, rfBd, pad3;
+    float s2[256], eps4[256], lbqq[256];
+    float qtype[16];
+    double s2d[256], eps4d[256];  // FP64 copies for the total energy
+    int64_t *rep_pos;  // C replicas x N x 3, fixed point
+    double *rep_mu;    // C replicas x N x 3, dipole unit vectors
+    int64_t *rep_cm;   // C replicas x M x 3, mass centres
+    int4 *pos4;        // N: rounded high words (x, y, z), type
+    short4 *pos_ext;   // N: next 16 bits
+    int32_t *site_dip; // N: index in the dipole list, or -1
+    int32_t *dip_site; // D: site of each dipole
+    double *mus;       // N: dipole scalars (e Angstrom)
+    float4 *dip4;      // D: mu-hat * mu (x, y, z), mu
+    int4 *dip_pos4;    // D: positions of the dipole sites
+    short4 *dip_ext;   // D
+    const MolTrial *trials;
+    float2 *log_du;
+    uint8_t *log_acc;
+    MolScalars *sc;
+    const int64_t *expl_pos;  // gs x 3 new positions (explicit trials)
+    const double *expl_mu;    // gs x 3 new dipole unit vectors
+    const int64_t *expl_cm;   // 3, new mass centre
+    double *eval_du;          // dU of an evaluated (not decided) trial
+};
+
+// ---------------------------------------------------------------- cluster PTX
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Load a float2 from the shared memory of CTA `rank` of this cluster.
+__device__ __forceinline__ float2 ld_cluster_f2(const float2 *p, unsigned rank) {
+    unsigned a = (unsigned)__cvta_generic_to_shared(p), ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    float2 v;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ra) : "memory");
+    return v;
+}
+
+// ---------------------------------------------------------------- helpers
+// a - b with two's-complement wrap (the minimum image of high words).
+__device__ __forceinline__ int wsub(int a, int b) { return (int)((uint32_t)a - (uint32_t)b); }
+
+// Exact float of |m| < 2^22 without the conversion pipe.
+__device__ __forceinline__ float small_to_float(int m) { return __int_as_float(0x4B400000 + m) - 12582912.0f; }
+
+__device__ __forceinline__ int16_t ext16d(int64_t X) {
+    int32_t h = hi32(X);
+    int32_t rem = (int32_t)((uint64_t)X - ((uint64_t)(uint32_t)h << 32));
+    return (int16_t)(rem >> 16);
+}
+
+struct D3 {
+    double x, y, z;
+};
+__device__ __forceinline__ double dot3(const D3 &a, const D3 &b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ D3 cross3(const D3 &a, const D3 &b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// Quaternion rotation as Eigen applies it: uv = v x p; uv += uv; p + w uv + v x uv.
+__device__ __forceinline__ D3 qrot(double w, const D3 &v, const D3 &p) {
+    D3 uv = cross3(v, p);
+    uv = {uv.x + uv.x, uv.y + uv.y, uv.z + uv.z};
+    D3 c = cross3(v, uv);
+    return {p.x + w * uv.x + c.x, p.y + w * uv.y + c.y, p.z + w * uv.z + c.z};
+}
+
+// 48-bit difference a - b (units L / 2^48) from high words and extensions.
+__device__ __forceinline__ int64_t d48(int ha, int hb, int ea, int eb) {
+    return (int64_t)wsub(ha, hb) * 65536 + (int64_t)(ea - eb);
+}
+
+// ---------------------------------------------------------------- shared memory
+struct MolSmem {
+    int4 *spos;     // site slice
+    short4 *sext;
+    float4 *sdip;   // dipole slice
+    int4 *sdpos;
+    short4 *sdext;
+    int4 *go, *gn;      // moved sites: old/new high words + type | dipole flag
+    short4 *geo, *gen;  // old/new extensions
+    double *gmu;        // [gs][6]: old unit dipole (3), new (3)
+    int64_t *gX;        // [gs][3]: new fixed-point positions
+    int64_t *gcm;       // [3]: new mass centre
+    uint32_t *queue;
+    int *qcount;
+    float2 *red;   // [32]
+    float2 *part;  // [2] cluster partial sums (double-buffered by trial parity)
+    int *flag;     // [4]: decision, error
+};
+
+__host__ __device__ inline size_t mol_align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline void mol_smem_layout(int ns, int nd, int gs, bool slice_smem, size_t off[16]) {
+    size_t o = 0;
+    off[0] = o; o += mol_align16(slice_smem ? (size_t)ns * 16 : 0);   // spos
+    off[1] = o; o += mol_align16(slice_smem ? (size_t)ns * 8 : 0);    // sext
+    off[2] = o; o += mol_align16((size_t)nd * 16);                    // sdip
+    off[3] = o; o += mol_align16((size_t)nd * 16);                    // sdpos
+    off[4] = o; o += mol_align16((size_t)nd * 8);                     // sdext
+    off[5] = o; o += mol_align16((size_t)gs * 16 * 2);                // go, gn
+    off[6] = o; o += mol_align16((size_t)gs * 8 * 2);                 // geo, gen
+    off[7] = o; o += mol_align16((size_t)gs * 6 * 8);                 // gmu
+    off[8] = o; o += mol_align16((size_t)gs * 3 * 8 + 3 * 8);         // gX, gcm
+    off[9] = o; o += mol_align16((size_t)kQueueCap * 4 + 16);         // queue, qcount
+    off[10] = o; o += mol_align16(32 * 8 + 2 * 8 + 16);               // red, part, flag
+    off[11] = o;
+}
+
+__device__ inline MolSmem mol_carve(unsigned char *base, int ns, int nd, int gs, bool slice_smem) {
+    size_t off[16];
+    mol_smem_layout(ns, nd, gs, slice_smem, off);
+    MolSmem s;
+    s.spos = (int4 *)(base + off[0]);
+    s.sext = (short4 *)(base + off[1]);
+    s.sdip = (float4 *)(base + off[2]);
+    s.sdpos = (int4 *)(base + off[3]);
+    s.sdext = (short4 *)(base + off[4]);
+    s.go = (int4 *)(base + off[5]);
+    s.gn = s.go + gs;
+    s.geo = (short4 *)(base + off[6]);
+    s.gen = s.geo + gs;
+    s.gmu = (double *)(base + off[7]);
+    s.gX = (int64_t *)(base + off[8]);
+    s.gcm = s.gX + 3 * gs;
+    s.queue = (uint32_t *)(base + off[9]);
+    s.qcount = (int *)(s.queue + kQueueCap);
+    s.red = (float2 *)(base + off[10]);
+    s.part = s.red + 32;
+    s.flag = (int *)(s.part + 2);
+    return s;
+}
+
+// ---------------------------------------------------------------- pair terms
+// Far LJ for one position pair from high words: 22-bit truncated differences
+// (error < 2e-5 Angstrom, i.e. < 2e-6 relative at r >= rc), squared distance
+// in units of sc9^2 folded into s2u.
+__device__ __forceinline__ float far_r2(int4 a, int4 b, float3 sc9) {
+    const float dx = small_to_float(wsub(a.x, b.x) >> 9) * sc9.x;
+    const float dy = small_to_float(wsub(a.y, b.y) >> 9) * sc9.y;
+    const float dz = small_to_float(wsub(a.z, b.z) >> 9) * sc9.z;
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+__device__ __forceinline__ float lj_r2(float r2, float s2, float e4) {
+    const float x = s2 * __frcp_rn(r2);
+    const float x3 = x * x * x;
+    return e4 * fmaf(x3, x3, -x3);
+}
+
+// Exact 32-bit difference vector a - b in Angstrom (FP32).
+__device__ __forceinline__ float3 diff32(int4 a, int4 b, float3 s32) {
+    return make_float3((float)wsub(a.x, b.x) * s32.x, (float)wsub(a.y, b.y) * s32.y, (float)wsub(a.z, b.z) * s32.z);
+}
+
+// Coulomb Q5(q) = (q-1)^3 (A5 q^2 + B5 q - 1) / r part: f(r) = Q5(r/rc)/r.
+__device__ __forceinline__ float coul_f(float r, const MolDesc &d) {
+    const float q = r * d.rc1i;
+    const float qm = q - 1.0f;
+    return qm * qm * qm * fmaf(fmaf(d.A5, q, d.B5), q, -1.0f) / r;
+}
+
+// FP64 position difference of sites with high words/extensions (a - b).
+__device__ __forceinline__ D3 diff48(int4 ha, short4 ea, int4 hb, short4 eb, const MolDesc &d) {
+    return {(double)d48(ha.x, hb.x, ea.x, eb.x) * d.s48d[0], (double)d48(ha.y, hb.y, ea.y, eb.y) * d.s48d[1],
+            (double)d48(ha.z, hb.z, ea.z, eb.z) * d.s48d[2]};
+}
+
+// IonDipole (q2mu, multipole.h:269-277) in FP64 with r = r_a - r_b:
+// lB [qa mub (mub.r) - qb mua (mua.r)] / r^3, mu vectors already scaled.
+__device__ __forceinline__ double ion_dipole64(double qa, const D3 &mua, double qb, const D3 &mub, const D3 &r,
+                                               double lB) {
+    const double r2i = 1.0 / dot3(r, r);
+    const double r3i = sqrt(r2i) * r2i;
+    return lB * (qa * dot3(mub, r) * r3i - qb * dot3(mua, r) * r3i);
+}
+// DipoleDipoleGalore with the reaction field (multipole.h:287-299, 767-782, 910-920).
+__device__ __forceinline__ double dipole_dipole64(const D3 &ua, double ma, const D3 &ub, double mb, const D3 &r,
+                                                  const MolDesc &d) {
+    const double r2 = dot3(r, r);
+    const double r1 = sqrt(r2);
+    if (!(r1 < d.rcd)) return 0.0;
+    const double q = r1 / d.rcd;
+    const double bf = d.rfBd * q * q * q;
+    const double r2i = 1.0 / r2;
+    const double dt = dot3(ua, ub);
+    const double T = (3.0 * dot3(ua, r) * dot3(ub, r) * r2i - dt) + dt * bf;
+    return d.lBd * (-(ma * mb) * T * sqrt(r2i) * r2i);
+}
+
+// Near pair, kind A: moved site i against slice site j (LJ + Coulomb, and the
+// ion-dipole term of the moved dipole with j's charge).
+__device__ __noinline__ df near_pair_a(int i, int4 pj, short4 ej, const MolSmem &s, const MolDesc &d, bool idip) {
+    const int4 po = s.go[i], pn = s.gn[i];
+    const short4 eo = s.geo[i], en = s.gen[i];
+    const D3 ro = diff48(po, eo, pj, ej, d), rn = diff48(pn, en, pj, ej, d);
+    const double ro2d = dot3(ro, ro), rn2d = dot3(rn, rn);
+    // r_n^2 - r_o^2 from exact 48-bit integers: sum_a (dn - do)(dn + do)
+    double S = 0.0;
+    {
+        const int64_t dno[3] = {d48(pn.x, pj.x, en.x, ej.x) - d48(po.x, pj.x, eo.x, ej.x),
+                                d48(pn.y, pj.y, en.y, ej.y) - d48(po.y, pj.y, eo.y, ej.y),
+                                d48(pn.z, pj.z, en.z, ej.z) - d48(po.z, pj.z, eo.z, ej.z)};
+        const int64_t spo[3] = {d48(pn.x, pj.x, en.x, ej.x) + d48(po.x, pj.x, eo.x, ej.x),
+                                d48(pn.y, pj.y, en.y, ej.y) + d48(po.y, pj.y, eo.y, ej.y),
+                                d48(pn.z, pj.z, en.z, ej.z) + d48(po.z, pj.z, eo.z, ej.z)};
+#pragma unroll
+        for (int a = 0; a < 3; a++) S = fma((double)dno[a] * d.s48d[a], (double)spo[a] * d.s48d[a], S);
+    }
+    const int ti = po.w & 0xFF, tj = pj.w & 0xFF;
+    const int t = d.uniform_lj ? 0 : ti * d.nt + tj;
+    const float ro2 = (float)ro2d, rn2 = (float)rn2d, dR2 = (float)S;
+    // LJ: 4eps x_o^3 (t^3 - 1)(x_o^3 (t^3 + 1) - 1), t^3 - 1 from tau = -dR2 / r_n^2
+    const float xo = d.s2[t] / ro2;
+    const float xo3 = xo * xo * xo;
+    const float tau = -dR2 / rn2;
+    const float t3m1 = tau * fmaf(tau, tau + 3.0f, 3.0f);
+    float acc = d.eps4[t] * xo3 * t3m1 * fmaf(xo3, t3m1 + 2.0f, -1.0f);
+    // Coulomb (CoulombGalore): cutoff tested on FP64 squared distances
+    const float A = d.lbqq[ti * d.nt + tj];
+    if (A != 0.0f) {
+        const bool io = ro2d < (double)d.rc2 , in_ = rn2d < (double)d.rc2;
+        const float r_o = sqrtf(ro2), r_n = sqrtf(rn2);
+        if (io && in_) {
+            // f_n - f_o = [Q5(q_n) - Q5(q_o)] / r_n + Q5(q_o) (1/r_n - 1/r_o)
+            const float dr = dR2 / (r_n + r_o);
+            const float qo = r_o * d.rc1i, qn = r_n * d.rc1i, dq = dr * d.rc1i;
+            const float mo = qo - 1.0f, mn = qn - 1.0f;
+            const float Po = fmaf(fmaf(d.A5, qo, d.B5), qo, -1.0f);
+            const float Pn = fmaf(fmaf(d.A5, qn, d.B5), qn, -1.0f);
+            const float dcube = dq * fmaf(mn, mn + mo, mo * mo);      // (q_n-1)^3 - (q_o-1)^3
+            const float dP = dq * fmaf(d.A5, qn + qo, d.B5);          // P(q_n) - P(q_o)
+            const float dQ = fmaf(dcube, Pn, mo * mo * mo * dP);
+            const float Qo = mo * mo * mo * Po;
+            acc += A * (dQ / r_n - Qo * dr / (r_n * r_o));
+        } else if (io) {
+            acc -= A * coul_f(r_o, d);
+        } else if (in_) {
+            acc += A * coul_f(r_n, d);
+        }
+    }
+    df out = {acc, 0.0f};
+    if (idip) {
+        // moved dipole i with j's charge: W2 of IonDipole(a = i, b = j)
+        const double qj = d.qtype[tj];
+        const D3 muo = {s.gmu[6 * i + 0], s.gmu[6 * i + 1], s.gmu[6 * i + 2]};
+        const D3 mun = {s.gmu[6 * i + 3], s.gmu[6 * i + 4], s.gmu[6 * i + 5]};
+        const int site = pn.w >> 8;
+        const double mi = d.mus[site];
+        const D3 z = {0, 0, 0};
+        const D3 mo_ = {muo.x * mi, muo.y * mi, muo.z * mi}, mn_ = {mun.x * mi, mun.y * mi, mun.z * mi};
+        const double w = ion_dipole64(0.0, mn_, qj, z, rn, d.lBd) - ion_dipole64(0.0, mo_, qj, z, ro, d.lBd);
+        const float wh = (float)w;
+        out = df_add(out, df{wh, (float)(w - (double)wh)});
+    }
+    return out;
+}
+
+// Near pair, kind B: moved site i against dipole k (ion-dipole with i's
+// charge, dipole-dipole when i carries a dipole), FP64.
+__device__ __noinline__ df near_pair_b(int i, int kk, const MolSmem &s, const MolDesc &d, int rank, bool idip,
+                                       int k0) {
+    const int4 po = s.go[i], pn = s.gn[i];
+    const short4 eo = s.geo[i], en = s.gen[i];
+    const int4 pk = s.sdpos[kk];
+    const short4 ek = s.sdext[kk];
+    const D3 ro = diff48(po, eo, pk, ek, d), rn = diff48(pn, en, pk, ek, d);
+    const int ksite = d.dip_site[k0 + kk];
+    const double *mk = d.rep_mu + ((size_t)rank * d.N + ksite) * 3;
+    const D3 uk = {mk[0], mk[1], mk[2]};
+    const double muk = d.mus[ksite];
+    const D3 vk = {uk.x * muk, uk.y * muk, uk.z * muk};
+    const double qi = d.qtype[po.w & 0xFF];
+    const D3 z = {0, 0, 0};
+    double w = ion_dipole64(qi, z, 0.0, vk, rn, d.lBd) - ion_dipole64(qi, z, 0.0, vk, ro, d.lBd);
+    if (idip) {
+        const int site = pn.w >> 8;
+        const double mi = d.mus[site];
+        const D3 uo = {s.gmu[6 * i + 0], s.gmu[6 * i + 1], s.gmu[6 * i + 2]};
+        const D3 un = {s.gmu[6 * i + 3], s.gmu[6 * i + 4], s.gmu[6 * i + 5]};
+        w += dipole_dipole64(un, mi, uk, muk, rn, d) - dipole_dipole64(uo, mi, uk, muk, ro, d);
+    }
+    const float wh = (float)w;
+    return df{wh, (float)(w - (double)wh)};
+}
+
+// ---------------------------------------------------------------- trial setup
+// New coordinates of the moved molecule (FP64 rotation of offsets from the
+// centre, then translation), exactly one thread per site; thread gs does the
+// mass centre. Old data come from this CTA's replica.
+__device__ __forceinline__ void setup_trial(const MolTrial &tr, const MolDesc &d, const MolSmem &s, int rank) {
+    const int tid = threadIdx.x, gs = d.gs, g = tr.g;
+    const int64_t *P = d.rep_pos + (size_t)rank * d.N * 3;
+    const double *MU = d.rep_mu + (size_t)rank * d.N * 3;
+    const int64_t *CM = d.rep_cm + (size_t)rank * d.M * 3;
+    if (tid > gs) return;
+    const bool explicit_ = tr.flags & 4;
+    int64_t c[3];
+    if (!explicit_) {
+        if (tr.center == 0) {
+            for (int a = 0; a < 3; a++) c[a] = CM[3 * g + a];
+        } else {
+            const int cs = g * gs + (tr.center == 1 ? 0 : gs - 1);
+            for (int a = 0; a < 3; a++) c[a] = P[3 * cs + a];
+        }
+    }
+    const D3 qv = {tr.qx, tr.qy, tr.qz};
+    auto move_point = [&](const int64_t X[3], int64_t out[3]) {
+        int64_t Y[3] = {X[0], X[1], X[2]};
+        if (tr.flags & 1) {
+            const D3 a = {(double)(int64_t)((uint64_t)X[0] - (uint64_t)c[0]) * d.s64d[0],
+                          (double)(int64_t)((uint64_t)X[1] - (uint64_t)c[1]) * d.s64d[1],
+                          (double)(int64_t)((uint64_t)X[2] - (uint64_t)c[2]) * d.s64d[2]};
+            const D3 b = qrot(tr.qw, qv, a);
+            Y[0] = (int64_t)((uint64_t)c[0] + (uint64_t)__double2ll_rn(b.x * d.inv64d[0]));
+            Y[1] = (int64_t)((uint64_t)c[1] + (uint64_t)__double2ll_rn(b.y * d.inv64d[1]));
+            Y[2] = (int64_t)((uint64_t)c[2] + (uint64_t)__double2ll_rn(b.z * d.inv64d[2]));
+        }
+        if (tr.flags & 2)
+            for (int a = 0; a < 3; a++) Y[a] = (int64_t)((uint64_t)Y[a] + (uint64_t)tr.t[a]);
+        for (int a = 0; a < 3; a++) out[a] = Y[a];
+    };
+    if (tid == gs) {
+        int64_t cn[3];
+        if (explicit_) {
+            for (int a = 0; a < 3; a++) cn[a] = d.expl_cm ? d.expl_cm[a] : CM[3 * g + a];
+        } else {
+            const int64_t co[3] = {CM[3 * g], CM[3 * g + 1], CM[3 * g + 2]};
+            move_point(co, cn);
+        }
+        for (int a = 0; a < 3; a++) s.gcm[a] = cn[a];
+        return;
+    }
+    const int site = g * gs + tid;
+    const int64_t Xo[3] = {P[3 * site], P[3 * site + 1], P[3 * site + 2]};
+    int64_t Xn[3];
+    D3 uo = {MU[3 * site], MU[3 * site + 1], MU[3 * site + 2]}, un;
+    if (explicit_) {
+        for (int a = 0; a < 3; a++) Xn[a] = d.expl_pos[3 * tid + a];
+        un = d.expl_mu ? D3{d.expl_mu[3 * tid], d.expl_mu[3 * tid + 1], d.expl_mu[3 * tid + 2]} : uo;
+    } else {
+        move_point(Xo, Xn);
+        un = (tr.flags & 1) ? qrot(tr.qw, qv, uo) : uo;  // DipoleParticle::rotate (point.h:672-679)
+    }
+    const int type = d.pos4[site].w & 0xFF;
+    const int dipflag = d.site_dip[site] >= 0 ? 0x100 : 0;
+    // .w of go/gn: type | dipole flag in bit 8 | site << 8 (site in bits 8..31 of gn)
+    s.go[tid] = make_int4(hi32(Xo[0]), hi32(Xo[1]), hi32(Xo[2]), type | dipflag);
+    s.gn[tid] = make_int4(hi32(Xn[0]), hi32(Xn[1]), hi32(Xn[2]), type | (site << 8));
+    s.geo[tid] = make_short4(ext16d(Xo[0]), ext16d(Xo[1]), ext16d(Xo[2]), 0);
+    s.gen[tid] = make_short4(ext16d(Xn[0]), ext16d(Xn[1]), ext16d(Xn[2]), 0);
+    double *gm = s.gmu + 6 * tid;
+    gm[0] = uo.x; gm[1] = uo.y; gm[2] = uo.z;
+    gm[3] = un.x; gm[4] = un.y; gm[5] = un.z;
+    for (int a = 0; a < 3; a++) s.gX[3 * tid + a] = Xn[a];
+}
+
+// ---------------------------------------------------------------- energy change
+// This CTA's part of dU for the trial set up in shared memory.
+template <bool SLICE_SMEM>
+__device__ df mol_partial(const MolDesc &d, const MolSmem &s, int g, int rank, int j0, int ns, int k0, int nd) {
+    const int tid = threadIdx.x, gs = d.gs;
+    const int g_lo = g * gs, g_hi = g_lo + gs;
+    const float3 sc9 = make_float3(d.sc9[0], d.sc9[1], d.sc9[2]);
+    const float3 s32 = make_float3(d.s32[0], d.s32[1], d.s32[2]);
+    const float rc2near = d.rc2near, lB = d.lB;
+    const int nt = d.nt;
+    const float s2u = d.s2[0], e4u = d.eps4[0];
+    const bool uni = d.uniform_lj != 0;
+    float acc = 0.0f;
+    df accd = {0.0f, 0.0f};
+    // loop A: every slice site against every moved site
+    for (int jj = tid; jj < ns; jj += blockDim.x) {
+        const int j = j0 + jj;
+        if (j >= g_lo && j < g_hi) continue;
+        const int4 pj = SLICE_SMEM ? s.spos[jj] : d.pos4[j];
+        const int tj = pj.w & 0xFF;
+        const float qj = d.qtype[tj];
+        for (int i = 0; i < gs; i++) {
+            const int4 po = s.go[i], pn = s.gn[i];
+            const int t = (po.w & 0xFF) * nt + tj;
+            const float s2 = uni ? s2u : d.s2[t], e4 = uni ? e4u : d.eps4[t];
+            const float r2o = far_r2(po, pj, sc9), r2n = far_r2(pn, pj, sc9);
+            const bool near = (r2o < rc2near) | (r2n < rc2near);
+            const bool idip = (po.w & 0x100) != 0;
+            if (near) {
+                const int slot = atomicAdd(s.qcount, 1);
+                if (slot < kQueueCap) {
+                    s.queue[slot] = ((uint32_t)i << 24) | (uint32_t)jj;
+                } else {
+                    const short4 ej = SLICE_SMEM ? s.sext[jj] : d.pos_ext[j];
+                    accd = df_add(accd, near_pair_a(i, pj, ej, s, d, idip));
+                }
+            } else {
+                acc += lj_r2(r2n, s2, e4) - lj_r2(r2o, s2, e4);
+                if (idip && qj != 0.0f) {
+                    // W2 of IonDipole(a = i, b = j): -lB qj mu_i (mu_i . r) / r^3
+                    const float3 ro = diff32(po, pj, s32), rn = diff32(pn, pj, s32);
+                    const float4 fo = make_float4(s.gmu[6 * i], s.gmu[6 * i + 1], s.gmu[6 * i + 2], 0.0f);
+                    const float4 fn = make_float4(s.gmu[6 * i + 3], s.gmu[6 * i + 4], s.gmu[6 * i + 5], 0.0f);
+                    const float ro2 = fmaf(ro.x, ro.x, fmaf(ro.y, ro.y, ro.z * ro.z));
+                    const float rn2 = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rn.z * rn.z));
+                    const float io = rsqrtf(ro2), in_ = rsqrtf(rn2);
+                    const float wo = fmaf(fo.x, ro.x, fmaf(fo.y, ro.y, fo.z * ro.z)) * io * io * io;
+                    const float wn = fmaf(fn.x, rn.x, fmaf(fn.y, rn.y, fn.z * rn.z)) * in_ * in_ * in_;
+                    const float mi = (float)d.mus[pn.w >> 8];
+                    acc -= lB * qj * mi * (wn - wo);
+                }
+            }
+        }
+    }
+    // loop B: dipoles of this slice against every moved site's charge (and dipole)
+    for (int kk = tid; kk < nd; kk += blockDim.x) {
+        const int4 pk = s.sdpos[kk];
+        const int ksite = pk.w >> 8;
+        if (ksite >= g_lo && ksite < g_hi) continue;
+        const float4 vk = s.sdip[kk];
+        for (int i = 0; i < gs; i++) {
+            const int4 po = s.go[i], pn = s.gn[i];
+            const float3 ro = diff32(po, pk, s32), rn = diff32(pn, pk, s32);
+            const float ro2 = fmaf(ro.x, ro.x, fmaf(ro.y, ro.y, ro.z * ro.z));
+            const float rn2 = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rn.z * rn.z));
+            const bool near = (ro2 < rc2near) | (rn2 < rc2near);
+            if (near) {
+                const int slot = atomicAdd(s.qcount, 1);
+                if (slot < kQueueCap) {
+                    s.queue[slot] = 0x800000u | ((uint32_t)i << 24) | (uint32_t)kk;
+                } else {
+                    accd = df_add(accd, near_pair_b(i, kk, s, d, rank, (po.w & 0x100) != 0, k0));
+                }
+            } else {
+                const float qi = d.qtype[po.w & 0xFF];
+                if (qi != 0.0f) {
+                    // W1 of IonDipole(a = i, b = k): lB qi mu_k (mu_k . r) / r^3
+                    const float io = rsqrtf(ro2), in_ = rsqrtf(rn2);
+                    const float wo = fmaf(vk.x, ro.x, fmaf(vk.y, ro.y, vk.z * ro.z)) * io * io * io;
+                    const float wn = fmaf(vk.x, rn.x, fmaf(vk.y, rn.y, vk.z * rn.z)) * in_ * in_ * in_;
+                    acc += lB * qi * (wn - wo);
+                }
+                // dipole-dipole is zero beyond the cutoff
+            }
+        }
+    }
+    __syncthreads();
+    // near queue, densely
+    const int nq = min(*s.qcount, kQueueCap);
+    for (int e = tid; e < nq; e += blockDim.x) {
+        const uint32_t q = s.queue[e];
+        const int i = (int)(q >> 24);
+        const bool idip = (s.go[i].w & 0x100) != 0;
+        if (q & 0x800000u) {
+            accd = df_add(accd, near_pair_b(i, (int)(q & 0x7FFFFF), s, d, rank, idip, k0));
+        } else {
+            const int jj = (int)(q & 0x7FFFFF);
+            const int4 pj = SLICE_SMEM ? s.spos[jj] : d.pos4[j0 + jj];
+            const short4 ej = SLICE_SMEM ? s.sext[jj] : d.pos_ext[j0 + jj];
+            accd = df_add(accd, near_pair_a(i, pj, ej, s, d, idip));
+        }
+    }
+    return df_add_f(accd, acc);
+}
+
+// ---------------------------------------------------------------- the sweep
+// One cluster of C CTAs per system (blockIdx.x / C). EVAL: evaluate trial 0
+// only, write its dU to eval_du, decide and commit nothing.
+template <bool SLICE_SMEM, bool CLUSTER, bool EVAL>
+__global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc *__restrict__ descs) {
+    extern __shared__ __align__(16) unsigned char mol_smem_raw[];
+    const int C = CLUSTER ? (int)descs[0].C : 1;
+    const int sys = blockIdx.x / C;
+    const int rank = CLUSTER ? (int)cluster_rank() : 0;
+    const MolDesc &d = descs[sys];
+    const int tid = threadIdx.x;
+    const int ns_full = (d.N + C - 1) / C, nd_full = (d.D + C - 1) / C;
+    const int j0 = min(rank * ns_full, d.N), j1 = min(j0 + ns_full, d.N), ns = j1 - j0;
+    const int k0 = min(rank * nd_full, d.D), k1 = min(k0 + nd_full, d.D), nd = k1 - k0;
+    MolSmem s = mol_carve(mol_smem_raw, ns_full, nd_full, d.gs, SLICE_SMEM);
+    if (SLICE_SMEM)
+        for (int jj = tid; jj < ns; jj += blockDim.x) {
+            s.spos[jj] = d.pos4[j0 + jj];
+            s.sext[jj] = d.pos_ext[j0 + jj];
+        }
+    for (int kk = tid; kk < nd; kk += blockDim.x) {
+        s.sdip[kk] = d.dip4[k0 + kk];
+        s.sdpos[kk] = d.dip_pos4[k0 + kk];
+        s.sdext[kk] = d.dip_ext[k0 + kk];
+    }
+    int64_t cursor = EVAL ? 0 : d.sc->cursor;
+    const int64_t n = EVAL ? 1 : d.sc->n_trials;
+    df usum = {d.sc->u_hi, d.sc->u_lo};
+    df utot = {d.sc->utot_hi, d.sc->utot_lo};
+    int64_t nacc = d.sc->n_accepted;
+    int err = 0;
+    if (tid == 0) {
+        s.part[0] = s.part[1] = make_float2(0.0f, 0.0f);
+        s.flag[0] = s.flag[1] = 0;
+    }
+    if (CLUSTER) cluster_barrier();
+    else __syncthreads();
+    for (; cursor < n; cursor++) {
+        const MolTrial tr = d.trials[cursor];
+        if (tid == 0) *s.qcount = 0;
+        setup_trial(tr, d, s, rank);
+        __syncthreads();
+        df part = mol_partial<SLICE_SMEM>(d, s, tr.g, rank, j0, ns, k0, nd);
+        part = warp_sum_df(part);
+        if ((tid & 31) == 0) s.red[tid >> 5] = make_float2(part.hi, part.lo);
+        __syncthreads();
+        const int slot = (int)(cursor & 1);
+        if (tid < 32) {
+            df v = {0.0f, 0.0f};
+            if (tid < (int)(blockDim.x >> 5)) v = df{s.red[tid].x, s.red[tid].y};
+            v = warp_sum_df(v);
+            if (tid == 0) s.part[slot] = make_float2(v.hi, v.lo);
+        }
+        if (CLUSTER) cluster_barrier();
+        else __syncthreads();
+        if (tid < 32) {
+            df v = {0.0f, 0.0f};
+            if (tid < C) {
+                const float2 p = CLUSTER ? ld_cluster_f2(&s.part[slot], (unsigned)tid) : s.part[slot];
+                v = df{p.x, p.y};
+            }
+            v = warp_sum_df(v);
+            v.hi = __shfl_sync(0xffffffffu, v.hi, 0);
+            v.lo = __shfl_sync(0xffffffffu, v.lo, 0);
+            if (tid == 0) {
+                int dec;
+                if (!isfinite(v.hi)) dec = 2;
+                else dec = df_gt(v, df{tr.thr_hi, tr.thr_lo}) ? 0 : 1;
+                s.flag[0] = dec;
+                s.red[0] = make_float2(v.hi, v.lo);
+                if (*s.qcount > kQueueCap) s.flag[1]++;   // overflowed pairs were evaluated in place
+            }
+        }
+        __syncthreads();
+        const int dec = s.flag[0];
+        const df du = {s.red[0].x, s.red[0].y};
+        if (EVAL) {
+            if (rank == 0 && tid == 0) *d.eval_du = (double)du.hi + (double)du.lo;
+            break;
+        }
+        if (dec == 2) {
+            err |= kMolErrNonFinite;
+            break;
+        }
+        if (rank == 0 && tid == 0) {
+            if (d.log_du) d.log_du[cursor] = make_float2(du.hi, du.lo);
+            if (d.log_acc) d.log_acc[cursor] = (uint8_t)dec;
+        }
+        if (dec == 1) {
+            nacc++;
+            usum = df_add(usum, du);
+            utot = df_add(utot, du);
+            const int gs = d.gs, g = tr.g;
+            if (tid < gs) {
+                const int site = g * gs + tid;
+                int64_t *P = d.rep_pos + ((size_t)rank * d.N + site) * 3;
+                double *MU = d.rep_mu + ((size_t)rank * d.N + site) * 3;
+                for (int a = 0; a < 3; a++) {
+                    P[a] = s.gX[3 * tid + a];
+                    MU[a] = s.gmu[6 * tid + 3 + a];
+                }
+                const int4 pn = make_int4(s.gn[tid].x, s.gn[tid].y, s.gn[tid].z, s.go[tid].w & 0xFF);
+                const short4 en = s.gen[tid];
+                if (site >= j0 && site < j1) {
+                    if (SLICE_SMEM) {
+                        s.spos[site - j0] = pn;
+                        s.sext[site - j0] = en;
+                    } else {
+                        d.pos4[site] = pn;
+                        d.pos_ext[site] = en;
+                    }
+                }
+                const int k = d.site_dip[site];
+                if (k >= k0 && k < k1) {
+                    const double m = d.mus[site];
+                    s.sdpos[k - k0] = make_int4(pn.x, pn.y, pn.z, (site << 8) | (pn.w & 0xFF));
+                    s.sdext[k - k0] = en;
+                    s.sdip[k - k0] = make_float4((float)(s.gmu[6 * tid + 3] * m), (float)(s.gmu[6 * tid + 4] * m),
+                                                 (float)(s.gmu[6 * tid + 5] * m), (float)m);
+                }
+            } else if (tid == gs) {
+                int64_t *CM = d.rep_cm + ((size_t)rank * d.M + g) * 3;
+                for (int a = 0; a < 3; a++) CM[a] = s.gcm[a];
+            }
+        }
+        __syncthreads();
+    }
+    // write the slices back (each CTA its own range) and the scalars
+    if (!EVAL) {
+        if (SLICE_SMEM)
+            for (int jj = tid; jj < ns; jj += blockDim.x) {
+                d.pos4[j0 + jj] = s.spos[jj];
+                d.pos_ext[j0 + jj] = s.sext[jj];
+            }
+        for (int kk = tid; kk < nd; kk += blockDim.x) {
+            d.dip4[k0 + kk] = s.sdip[kk];
+            d.dip_pos4[k0 + kk] = s.sdpos[kk];
+            d.dip_ext[k0 + kk] = s.sdext[kk];
+        }
+        if (rank == 0 && tid == 0) {
+            MolScalars *sc = d.sc;
+            sc->cursor = cursor;
+            sc->n_accepted = nacc;
+            sc->u_hi = usum.hi;
+            sc->u_lo = usum.lo;
+            sc->utot_hi = utot.hi;
+            sc->utot_lo = utot.lo;
+            sc->error |= err;
+        }
+    }
+    if (CLUSTER) cluster_barrier();   // no CTA leaves while another may read its shared memory
+}
+
+// Apply an evaluated explicit trial (fg_mol_commit): new positions, dipoles
+// and mass centre into every replica, the site/dipole records and the
+// running energy. One block of >= gs + 1 threads.
+__global__ void mol_commit_kernel(const MolDesc *__restrict__ descs, int g, int accepted, int nrep) {
+    const MolDesc &d = descs[0];
+    const int tid = threadIdx.x, gs = d.gs;
+    if (!accepted) return;
+    if (tid < gs) {
+        const int site = g * gs + tid;
+        int64_t X[3];
+        for (int a = 0; a < 3; a++) X[a] = d.expl_pos[3 * tid + a];
+        for (int r = 0; r < nrep; r++) {
+            int64_t *P = d.rep_pos + ((size_t)r * d.N + site) * 3;
+            double *MU = d.rep_mu + ((size_t)r * d.N + site) * 3;
+            for (int a = 0; a < 3; a++) {
+                P[a] = X[a];
+                if (d.expl_mu) MU[a] = d.expl_mu[3 * tid + a];
+            }
+        }
+        const int type = d.pos4[site].w & 0xFF;
+        const int4 p4 = make_int4(hi32(X[0]), hi32(X[1]), hi32(X[2]), type);
+        const short4 e4 = make_short4(ext16d(X[0]), ext16d(X[1]), ext16d(X[2]), 0);
+        d.pos4[site] = p4;
+        d.pos_ext[site] = e4;
+        const int k = d.site_dip[site];
+        if (k >= 0) {
+            const double m = d.mus[site];
+            const double *u = d.rep_mu + (size_t)site * 3;
+            d.dip_pos4[k] = make_int4(p4.x, p4.y, p4.z, (site << 8) | type);
+            d.dip_ext[k] = e4;
+            d.dip4[k] = make_float4((float)(u[0] * m), (float)(u[1] * m), (float)(u[2] * m), (float)m);
+        }
+    } else if (tid == gs && d.expl_cm) {
+        for (int r = 0; r < nrep; r++)
+            for (int a = 0; a < 3; a++) d.rep_cm[((size_t)r * d.M + g) * 3 + a] = d.expl_cm[a];
+    }
+}
+
+// Total energy in FP64, as Energybase::systemEnergy sums it (energy.h:169-180):
+// out[0] += intermolecular pairs, out[1] += intramolecular pairs
+// (NonbondedVector::g_internal, energy.h:1207-1216). Grid: x over sites i
+// (256 per block), y over chunks of j.
+__global__ void mol_total_kernel(const MolDesc *__restrict__ descs, int chunk, double *out) {
+    const MolDesc &d = descs[0];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int jb = blockIdx.y * chunk, je = min(jb + chunk, d.N);
+    double inter = 0.0, intra = 0.0;
+    if (i < d.N) {
+        const int64_t *P = d.rep_pos;
+        const int ti = d.pos4[i].w & 0xFF;
+        const double qi = d.qtype[ti], mi = d.mus[i];
+        const D3 ui = {d.rep_mu[3 * i], d.rep_mu[3 * i + 1], d.rep_mu[3 * i + 2]};
+        const D3 vi = {ui.x * mi, ui.y * mi, ui.z * mi};
+        for (int j = max(jb, i + 1); j < je; j++) {
+            const int tj = d.pos4[j].w & 0xFF;
+            const D3 r = {(double)(int64_t)((uint64_t)P[3 * i] - (uint64_t)P[3 * j]) * d.s64d[0],
+                          (double)(int64_t)((uint64_t)P[3 * i + 1] - (uint64_t)P[3 * j + 1]) * d.s64d[1],
+                          (double)(int64_t)((uint64_t)P[3 * i + 2] - (uint64_t)P[3 * j + 2]) * d.s64d[2]};
+            const double r2 = dot3(r, r);
+            double u = 0.0;
+            // CoulombGalore (kappa = 0)
+            const int t = ti * d.nt + tj;
+            if (r2 < (double)d.rc2) {
+                const double rr = sqrt(r2);
+                const double q = rr / d.rcd, q2 = q * q;
+                const double a2 = -66.0 * 1494.0 / 56916.0;
+                const double Q = (q - 1.0) * (q - 1.0) * (q - 1.0) *
+                                 (5.0 / 22.0 * q2 * a2 + 9.0 / 22.0 * q * a2 - 0.6 * q2 - 1.2 * q - 1.0);
+                u += d.lBd * (double)d.qtype[ti] * (double)d.qtype[tj] / rr * Q;
+            }
+            // LennardJonesLB
+            {
+                double x = d.s2d[t] / r2;
+                x = x * x * x;
+                u += d.eps4d[t] * (x * x - x);
+            }
+            const double mj = d.mus[j];
+            if (mi != 0.0 || mj != 0.0) {
+                const D3 uj = {d.rep_mu[3 * j], d.rep_mu[3 * j + 1], d.rep_mu[3 * j + 2]};
+                const D3 vj = {uj.x * mj, uj.y * mj, uj.z * mj};
+                u += ion_dipole64(qi, vi, (double)d.qtype[tj], vj, r, d.lBd);
+                if (mi != 0.0 && mj != 0.0) u += dipole_dipole64(ui, mi, uj, mj, r, d);
+            }
+            if (i / d.gs == j / d.gs) intra += u;
+            else inter += u;
+        }
+    }
+    // block sums, then one atomic per block
+    __shared__ double red[2][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        inter += __shfl_xor_sync(0xffffffffu, inter, o);
+        intra += __shfl_xor_sync(0xffffffffu, intra, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = inter;
+        red[1][threadIdx.x >> 5] = intra;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            a += red[0][w];
+            b += red[1][w];
+        }
+        atomicAdd(&out[0], a);
+        atomicAdd(&out[1], b);
+    }
+}
+
+}  // namespace fgm
+
+// ==================================================================== host side
+struct fg_molsys {
+    fg_params P{};
+    int N = 0, gs = 0, M = 0, D = 0;
+    int device = 0;
+    int C = 1;          // CTAs per system (thread-block cluster)
+    int max_cluster = 1;
+    cudaStream_t stream = nullptr;
+    fgm::MolDesc desc{};
+    fgm::MolDesc *d_desc = nullptr;
+    int64_t *rep_pos = nullptr, *rep_cm = nullptr;
+    double *rep_mu = nullptr, *mus = nullptr;
+    int4 *pos4 = nullptr, *dip_pos4 = nullptr;
+    short4 *pos_ext = nullptr, *dip_ext = nullptr;
+    int32_t *site_dip = nullptr, *dip_site = nullptr;
+    float4 *dip4 = nullptr;
+    fgm::MolTrial *trials = nullptr;
+    int64_t trials_cap = 0;
+    float2 *log_du = nullptr;
+    uint8_t *log_acc = nullptr;
+    int64_t log_cap = 0;
+    fgm::MolScalars *sc = nullptr;
+    int64_t *expl_pos = nullptr;
+    double *expl_mu = nullptr, *eval_du = nullptr, *tot = nullptr;
+    int64_t *expl_cm = nullptr;
+    int pending = -1;   // molecule of an evaluated explicit trial awaiting fg_mol_commit
+    double pending_du = 0.0;
+    bool has_cm = false;
+    bool state_set = false;
+    std::vector<int32_t> types;
+    std::vector<double> mus_h;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t device_bytes = 0;
+};
+
+namespace {
+
+int mol_dmalloc(fg_molsys *h, void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    h->device_bytes += bytes;
+    return FG_OK;
+}
+#define MOL_DMALLOC(ptr, bytes)                                        \
+    do {                                                               \
+        int rc_ = mol_dmalloc(h, (void **)&(ptr), (size_t)(bytes));    \
+        if (rc_) return rc_;                                           \
+    } while (0)
+
+void mol_free(fg_molsys *h) {
+    void *ptrs[] = {h->d_desc, h->rep_pos, h->rep_cm, h->rep_mu, h->mus, h->pos4, h->dip_pos4, h->pos_ext,
+                    h->dip_ext, h->site_dip, h->dip_site, h->dip4, h->trials, h->log_du, h->log_acc, h->sc,
+                    h->expl_pos, h->expl_mu, h->eval_du, h->tot, h->expl_cm};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+// Geometry::anyCenter with equal masses (geometry.h:714-738) in fixed point:
+// origin at the middle site, minimum-image offsets, mean, wrapped.
+void mol_mass_center(const int64_t *X, int front, int gs, int64_t out[3]) {
+    const int o = front + (int)((gs - 1) * 0.5);
+    for (int a = 0; a < 3; a++) {
+        long double s = 0;
+        for (int i = front; i < front + gs; i++) s += (long double)(int64_t)((uint64_t)X[3 * i + a] - (uint64_t)X[3 * o + a]);
+        out[a] = (int64_t)((uint64_t)X[3 * o + a] + (uint64_t)(int64_t)llroundl(s / gs));
+    }
+}
+
+size_t mol_smem_bytes(const fg_molsys *h, int C, bool slice_smem) {
+    size_t off[16];
+    fgm::mol_smem_layout((h->N + C - 1) / C, (h->D + C - 1) / C, h->gs, slice_smem, off);
+    return off[11];
+}
+
+struct MolLaunch {
+    void (*fn)(const fgm::MolDesc *);
+    size_t smem;
+    bool cluster;
+};
+
+template <bool EVAL>
+int mol_pick(const fg_molsys *h, MolLaunch &L) {
+    const bool slice = mol_smem_bytes(h, h->C, true) <= 200 * 1024;
+    const bool cl = h->C > 1;
+    L.smem = mol_smem_bytes(h, h->C, slice);
+    L.cluster = cl;
+    if (slice) L.fn = cl ? fgm::mol_sweep_kernel<true, true, EVAL> : fgm::mol_sweep_kernel<true, false, EVAL>;
+    else L.fn = cl ? fgm::mol_sweep_kernel<false, true, EVAL> : fgm::mol_sweep_kernel<false, false, EVAL>;
+    cudaError_t e = cudaFuncSetAttribute((const void *)L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "shared memory attribute: %s", cudaGetErrorString(e));
+    if (cl) {
+        e = cudaFuncSetAttribute((const void *)L.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return fail(FG_ERR_CUDA, "cluster attribute: %s", cudaGetErrorString(e));
+    }
+    return FG_OK;
+}
+
+int mol_launch(const fg_molsys *h, const MolLaunch &L, const fgm::MolDesc *descs, int n_systems, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(n_systems * h->C));
+    cfg.blockDim = dim3(fgm::kMolThreads);
+    cfg.dynamicSmemBytes = L.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    if (L.cluster) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)h->C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    cudaError_t e = cudaLaunchKernelEx(&cfg, L.fn, descs);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "molecule sweep launch: %s", cudaGetErrorString(e));
+    return FG_OK;
+}
+
+// Largest cluster the device runs for this kernel's shared memory (<= 16).
+int mol_max_cluster(fg_molsys *h) {
+    int best = 1;
+    for (int c : {16, 8, 4, 2}) {
+        const int saved = h->C;
+        h->C = c;
+        MolLaunch L;
+        int rc = mol_pick<false>(h, L);
+        h->C = saved;
+        if (rc) continue;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)c);
+        cfg.blockDim = dim3(fgm::kMolThreads);
+        cfg.dynamicSmemBytes = L.smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)c;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, (const void *)L.fn, &cfg) == cudaSuccess && n > 0) {
+            best = c;
+            break;
+        }
+        cudaGetLastError();
+    }
+    return best;
+}
+
+int mol_alloc_replicas(fg_molsys *h, int C) {
+    if (h->rep_pos) cudaFree(h->rep_pos);
+    if (h->rep_mu) cudaFree(h->rep_mu);
+    if (h->rep_cm) cudaFree(h->rep_cm);
+    h->rep_pos = nullptr;
+    h->rep_mu = nullptr;
+    h->rep_cm = nullptr;
+    MOL_DMALLOC(h->rep_pos, (size_t)C * h->N * 3 * sizeof(int64_t));
+    MOL_DMALLOC(h->rep_mu, (size_t)C * h->N * 3 * sizeof(double));
+    MOL_DMALLOC(h->rep_cm, (size_t)C * h->M * 3 * sizeof(int64_t));
+    h->desc.rep_pos = h->rep_pos;
+    h->desc.rep_mu = h->rep_mu;
+    h->desc.rep_cm = h->rep_cm;
+    return FG_OK;
+}
+
+int mol_push_desc(fg_molsys *h) {
+    h->desc.C = h->C;
+    CK(cudaMemcpyAsync(h->d_desc, &h->desc, sizeof(fgm::MolDesc), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+int mol_ensure_trials(fg_molsys *h, int64_t n, bool log) {
+    n = std::max<int64_t>(n, 1);
+    if (n > h->trials_cap) {
+        if (h->trials) cudaFree(h->trials);
+        h->trials = nullptr;
+        MOL_DMALLOC(h->trials, n * sizeof(fgm::MolTrial));
+        h->trials_cap = n;
+    }
+    if (log && n > h->log_cap) {
+        if (h->log_du) cudaFree(h->log_du);
+        if (h->log_acc) cudaFree(h->log_acc);
+        h->log_du = nullptr;
+        h->log_acc = nullptr;
+        MOL_DMALLOC(h->log_du, n * sizeof(float2));
+        MOL_DMALLOC(h->log_acc, n);
+        h->log_cap = n;
+    }
+    h->desc.trials = h->trials;
+    return FG_OK;
+}
+
+int mol_read_scalars(fg_molsys *h, fgm::MolScalars &s) {
+    CK(cudaMemcpyAsync(&s, h->sc, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+int mol_write_scalars(fg_molsys *h, const fgm::MolScalars &s) {
+    CK(cudaMemcpyAsync(h->sc, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+// Copy replica 0 into replicas 1..C-1 (after the state changed through it).
+int mol_sync_replicas(fg_molsys *h) {
+    for (int r = 1; r < h->C; r++) {
+        CK(cudaMemcpyAsync(h->rep_pos + (size_t)r * h->N * 3, h->rep_pos, (size_t)h->N * 3 * sizeof(int64_t),
+                           cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->rep_mu + (size_t)r * h->N * 3, h->rep_mu, (size_t)h->N * 3 * sizeof(double),
+                           cudaMemcpyDeviceToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->rep_cm + (size_t)r * h->M * 3, h->rep_cm, (size_t)h->M * 3 * sizeof(int64_t),
+                           cudaMemcpyDeviceToDevice, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+int mol_total(fg_molsys *h, double out[2]) {
+    CK(cudaMemsetAsync(h->tot, 0, 2 * sizeof(double), h->stream));
+    const int chunk = 2048;
+    dim3 grid((unsigned)((h->N + 255) / 256), (unsigned)((h->N + chunk - 1) / chunk));
+    fgm::mol_total_kernel<<<grid, 256, 0, h->stream>>>(h->d_desc, chunk, h->tot);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, h->tot, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+// MolTrial records from the reference's draws (or any explicit stream).
+void mol_make_trials(const fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, const double *angle,
+                     const int32_t *center, const double *trans, const double *u, int rotate, int translate,
+                     std::vector<fgm::MolTrial> &out) {
+    out.resize(n);
+    for (int64_t k = 0; k < n; k++) {
+        fgm::MolTrial &t = out[k];
+        t = fgm::MolTrial{};
+        t.g = mol[k];
+        t.flags = (rotate ? 1 : 0) | (translate ? 2 : 0);
+        t.center = center ? center[k] : 0;
+        t.qw = 1.0;
+        if (rotate) {
+            double ax = axis[3 * k], ay = axis[3 * k + 1], az = axis[3 * k + 2];
+            const double nrm = std::sqrt(ax * ax + ay * ay + az * az);
+            ax /= nrm; ay /= nrm; az /= nrm;
+            const double ha = 0.5 * angle[k], sh = std::sin(ha);
+            t.qw = std::cos(ha);
+            t.qx = sh * ax; t.qy = sh * ay; t.qz = sh * az;
+        }
+        if (translate)
+            for (int a = 0; a < 3; a++) t.t[a] = to_fix(trans[3 * k + a], h->P.box[a]);
+        // Movebase::metropolis (move.h:567-573): reject iff u > exp(-dU)
+        const double thr = -std::log(u[k]);
+        const float2 f = split_df(thr);
+        t.thr_hi = f.x;
+        t.thr_lo = f.y;
+        if (u[k] <= 0.0) { t.thr_hi = INFINITY; t.thr_lo = 0.0f; }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_mol_create(const fg_params *params, int32_t n_sites, int32_t sites_per_molecule, fg_molsys **out) {
+    if (!params || !out) return fail(FG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const fg_params &P = *params;
+    if (P.model != FG_MODEL_MULTIPOLE_RF) return fail(FG_ERR_INVALID, "fg_mol_create needs FG_MODEL_MULTIPOLE_RF");
+    if (sites_per_molecule < 1 || sites_per_molecule > fgm::kMaxGroupSites)
+        return fail(FG_ERR_INVALID, "sites per molecule must be 1..%d", fgm::kMaxGroupSites);
+    if (n_sites < 2 * sites_per_molecule || n_sites % sites_per_molecule)
+        return fail(FG_ERR_INVALID, "site count must be a multiple (>= 2) of the molecule size");
+    if (n_sites >= (1 << 23)) return fail(FG_ERR_CAPACITY, "at most 2^23 sites");
+    if (P.n_types < 1 || P.n_types > FG_MAX_TYPES) return fail(FG_ERR_INVALID, "bad type count");
+    const double Lmin = std::min(P.box[0], std::min(P.box[1], P.box[2]));
+    if (!(P.rf_cutoff > 0) || !(P.rf_cutoff < 0.5 * Lmin)) return fail(FG_ERR_INVALID, "cutoff must be in (0, L/2)");
+    if (!(P.bjerrum > 0) || !(P.rf_eps_r > 0) || !(P.rf_eps_rf > 0)) return fail(FG_ERR_INVALID, "bad dielectric");
+    fg_molsys *h = new fg_molsys();
+    h->P = P;
+    h->N = n_sites;
+    h->gs = sites_per_molecule;
+    h->M = n_sites / sites_per_molecule;
+    auto bail = [&](int rc) {
+        mol_free(h);
+        delete h;
+        return rc;
+    };
+    if (cudaGetDevice(&h->device) != cudaSuccess) return bail(fail(FG_ERR_CUDA, "no CUDA device"));
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(FG_ERR_CUDA, "stream"));
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    fgm::MolDesc &d = h->desc;
+    d.N = h->N;
+    d.gs = h->gs;
+    d.M = h->M;
+    d.nt = P.n_types;
+    bool uniform = true;
+    for (int i = 0; i < P.n_types; i++)
+        if (P.type_sigma[i] != P.type_sigma[0] || P.type_eps[i] != P.type_eps[0]) uniform = false;
+    d.uniform_lj = uniform ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        d.s32[a] = (float)(P.box[a] / 4294967296.0);
+        d.sc9[a] = (float)(512.0 * P.box[a] / 4294967296.0);
+        d.s48d[a] = P.box[a] / 281474976710656.0;
+        d.s64d[a] = P.box[a] / TWO64;
+        d.inv64d[a] = TWO64 / P.box[a];
+    }
+    const double rc = P.rf_cutoff;
+    d.lB = (float)P.bjerrum;
+    d.lBd = P.bjerrum;
+    d.rc2 = (float)(rc * rc);
+    d.rc2near = (float)((rc + 0.05) * (rc + 0.05));
+    d.rc1i = (float)(1.0 / rc);
+    d.rcd = rc;
+    const double a2 = -66.0 * 1494.0 / 56916.0;   // CoulombGalore Q5 coefficient at kappa = 0
+    d.A5 = (float)(5.0 / 22.0 * a2 - 0.6);
+    d.B5 = (float)(9.0 / 22.0 * a2 - 1.2);
+    d.rfBd = -(2 * (P.rf_eps_rf - P.rf_eps_r) / (2 * P.rf_eps_rf + P.rf_eps_r)) / P.rf_eps_r;
+    d.kT = (float)(P.kT_scale > 0 ? P.kT_scale : 1.0);
+    const int nt = P.n_types;
+    for (int i = 0; i < nt; i++) {
+        d.qtype[i] = (float)P.type_charge[i];
+        for (int j = 0; j < nt; j++) {
+            const double sig = 0.5 * (P.type_sigma[i] + P.type_sigma[j]);
+            const double e4 = 4 * std::sqrt(P.type_eps[i] * P.type_eps[j]);
+            d.s2[i * nt + j] = (float)(sig * sig);
+            d.eps4[i * nt + j] = (float)e4;
+            d.s2d[i * nt + j] = sig * sig;
+            d.eps4d[i * nt + j] = e4;
+            d.lbqq[i * nt + j] = (float)(P.bjerrum * P.type_charge[i] * P.type_charge[j]);
+        }
+    }
+    if (uniform) {
+        d.s2[0] = (float)(P.type_sigma[0] * P.type_sigma[0]);
+        d.eps4[0] = (float)(4 * P.type_eps[0]);
+    }
+    int rc_;
+#define TRY(x)                 \
+    do {                       \
+        rc_ = (x);             \
+        if (rc_) return bail(rc_); \
+    } while (0)
+    TRY(mol_dmalloc(h, (void **)&h->d_desc, sizeof(fgm::MolDesc)));
+    TRY(mol_dmalloc(h, (void **)&h->mus, (size_t)h->N * sizeof(double)));
+    TRY(mol_dmalloc(h, (void **)&h->pos4, (size_t)h->N * sizeof(int4)));
+    TRY(mol_dmalloc(h, (void **)&h->pos_ext, (size_t)h->N * sizeof(short4)));
+    TRY(mol_dmalloc(h, (void **)&h->site_dip, (size_t)h->N * sizeof(int32_t)));
+    TRY(mol_dmalloc(h, (void **)&h->sc, sizeof(fgm::MolScalars)));
+    TRY(mol_dmalloc(h, (void **)&h->expl_pos, (size_t)h->gs * 3 * sizeof(int64_t)));
+    TRY(mol_dmalloc(h, (void **)&h->expl_mu, (size_t)h->gs * 3 * sizeof(double)));
+    TRY(mol_dmalloc(h, (void **)&h->expl_cm, 3 * sizeof(int64_t)));
+    TRY(mol_dmalloc(h, (void **)&h->eval_du, sizeof(double)));
+    TRY(mol_dmalloc(h, (void **)&h->tot, 2 * sizeof(double)));
+    d.mus = h->mus;
+    d.pos4 = h->pos4;
+    d.pos_ext = h->pos_ext;
+    d.site_dip = h->site_dip;
+    d.sc = h->sc;
+    d.eval_du = h->eval_du;
+    h->max_cluster = mol_max_cluster(h);
+    // default: enough CTAs that each owns <= ~1250 sites, within what the device runs
+    int C = 1;
+    while (C < h->max_cluster && (h->N + C - 1) / C > 1250) C *= 2;
+    h->C = C;
+    TRY(mol_alloc_replicas(h, C));
+    TRY(mol_ensure_trials(h, 1, false));
+    fgm::MolScalars s{};
+    TRY(mol_write_scalars(h, s));
+#undef TRY
+    *out = h;
+    return FG_OK;
+}
+
+int fg_mol_destroy(fg_molsys *h) {
+    if (!h) return FG_OK;
+    cudaStreamSynchronize(h->stream);
+    mol_free(h);
+    delete h;
+    return FG_OK;
+}
+
+int fg_mol_set_state(fg_molsys *h, const double *xyz, const double *mu_unit, const double *mu_scalar,
+                     const int32_t *type_ids, const double *mass_centers) {
+    if (!h || !xyz || !type_ids) return fail(FG_ERR_INVALID, "null argument");
+    const int N = h->N;
+    std::vector<int64_t> X(3 * (size_t)N), CM(3 * (size_t)h->M);
+    std::vector<double> MU(3 * (size_t)N, 0.0);
+    std::vector<int4> p4(N);
+    std::vector<short4> e4(N);
+    std::vector<int32_t> sd(N, -1), ds;
+    h->types.assign(type_ids, type_ids + N);
+    h->mus_h.assign(N, 0.0);
+    for (int i = 0; i < N; i++) {
+        if (type_ids[i] < 0 || type_ids[i] >= h->P.n_types) return fail(FG_ERR_INVALID, "bad type id at %d", i);
+        for (int a = 0; a < 3; a++) {
+            if (!std::isfinite(xyz[3 * i + a])) return fail(FG_ERR_INVALID, "non-finite position at %d", i);
+            X[3 * i + a] = to_fix(xyz[3 * i + a], h->P.box[a]);
+        }
+        const double m = mu_scalar ? mu_scalar[i] : 0.0;
+        if (m != 0.0) {
+            if (!mu_unit) return fail(FG_ERR_INVALID, "dipole scalars need unit vectors");
+            for (int a = 0; a < 3; a++) MU[3 * i + a] = mu_unit[3 * i + a];
+            sd[i] = (int32_t)ds.size();
+            ds.push_back(i);
+        } else if (mu_unit) {
+            for (int a = 0; a < 3; a++) MU[3 * i + a] = mu_unit[3 * i + a];
+        }
+        h->mus_h[i] = m;
+        p4[i] = make_int4(hi32h(X[3 * i]), hi32h(X[3 * i + 1]), hi32h(X[3 * i + 2]), type_ids[i]);
+        e4[i] = make_short4(ext16h(X[3 * i]), ext16h(X[3 * i + 1]), ext16h(X[3 * i + 2]), 0);
+    }
+    for (int g = 0; g < h->M; g++) {
+        if (mass_centers)
+            for (int a = 0; a < 3; a++) CM[3 * g + a] = to_fix(mass_centers[3 * g + a], h->P.box[a]);
+        else
+            mol_mass_center(X.data(), g * h->gs, h->gs, &CM[3 * g]);
+    }
+    const int D = (int)ds.size();
+    if (D != h->D || !h->dip4) {
+        if (h->dip4) cudaFree(h->dip4);
+        if (h->dip_pos4) cudaFree(h->dip_pos4);
+        if (h->dip_ext) cudaFree(h->dip_ext);
+        if (h->dip_site) cudaFree(h->dip_site);
+        h->dip4 = nullptr;
+        h->dip_pos4 = nullptr;
+        h->dip_ext = nullptr;
+        h->dip_site = nullptr;
+        MOL_DMALLOC(h->dip4, (size_t)std::max(D, 1) * sizeof(float4));
+        MOL_DMALLOC(h->dip_pos4, (size_t)std::max(D, 1) * sizeof(int4));
+        MOL_DMALLOC(h->dip_ext, (size_t)std::max(D, 1) * sizeof(short4));
+        MOL_DMALLOC(h->dip_site, (size_t)std::max(D, 1) * sizeof(int32_t));
+        h->D = D;
+    }
+    std::vector<float4> d4(std::max(D, 1));
+    std::vector<int4> dp4(std::max(D, 1));
+    std::vector<short4> de4(std::max(D, 1));
+    for (int k = 0; k < D; k++) {
+        const int i = ds[k];
+        const double m = h->mus_h[i];
+        d4[k] = make_float4((float)(MU[3 * i] * m), (float)(MU[3 * i + 1] * m), (float)(MU[3 * i + 2] * m), (float)m);
+        dp4[k] = make_int4(p4[i].x, p4[i].y, p4[i].z, (i << 8) | type_ids[i]);
+        de4[k] = e4[i];
+    }
+    fgm::MolDesc &d = h->desc;
+    d.D = D;
+    d.dip4 = h->dip4;
+    d.dip_pos4 = h->dip_pos4;
+    d.dip_ext = h->dip_ext;
+    d.dip_site = h->dip_site;
+    cudaStream_t st = h->stream;
+    for (int r = 0; r < h->C; r++) {
+        CK(cudaMemcpyAsync(h->rep_pos + (size_t)r * N * 3, X.data(), X.size() * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->rep_mu + (size_t)r * N * 3, MU.data(), MU.size() * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->rep_cm + (size_t)r * h->M * 3, CM.data(), CM.size() * 8, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemcpyAsync(h->mus, h->mus_h.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->pos4, p4.data(), (size_t)N * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->pos_ext, e4.data(), (size_t)N * sizeof(short4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->site_dip, sd.data(), (size_t)N * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->dip4, d4.data(), (size_t)std::max(D, 1) * sizeof(float4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->dip_pos4, dp4.data(), (size_t)std::max(D, 1) * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->dip_ext, de4.data(), (size_t)std::max(D, 1) * sizeof(short4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->dip_site, ds.empty() ? sd.data() : ds.data(), (size_t)std::max(D, 1) * 4,
+                       cudaMemcpyHostToDevice, st));
+    int rc = mol_push_desc(h);
+    if (rc) return rc;
+    double tot[2];
+    rc = mol_total(h, tot);
+    if (rc) return rc;
+    fgm::MolScalars s{};
+    const float2 u = split_df(tot[0] + tot[1]);
+    s.utot_hi = u.x;
+    s.utot_lo = u.y;
+    rc = mol_write_scalars(h, s);
+    if (rc) return rc;
+    h->pending = -1;
+    h->state_set = true;
+    return FG_OK;
+}
+
+int fg_mol_get_state(fg_molsys *h, double *xyz, double *mu_unit, double *mass_centers) {
+    if (!h || !h->state_set) return fail(FG_ERR_STATE, "no state");
+    const int N = h->N;
+    std::vector<int64_t> X(3 * (size_t)N), CM(3 * (size_t)h->M);
+    std::vector<double> MU(3 * (size_t)N);
+    CK(cudaMemcpyAsync(X.data(), h->rep_pos, X.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(MU.data(), h->rep_mu, MU.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(CM.data(), h->rep_cm, CM.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < N; i++)
+        for (int a = 0; a < 3; a++) {
+            if (xyz) xyz[3 * i + a] = from_fix(X[3 * i + a], h->P.box[a]);
+            if (mu_unit) mu_unit[3 * i + a] = MU[3 * i + a];
+        }
+    if (mass_centers)
+        for (int g = 0; g < h->M; g++)
+            for (int a = 0; a < 3; a++) mass_centers[3 * g + a] = from_fix(CM[3 * g + a], h->P.box[a]);
+    return FG_OK;
+}
+
+int fg_mol_set_cluster(fg_molsys *h, int32_t ctas) {
+    if (!h) return fail(FG_ERR_INVALID, "null handle");
+    if (ctas < 1 || ctas > h->max_cluster || (ctas & (ctas - 1)))
+        return fail(FG_ERR_INVALID, "cluster size must be a power of two in 1..%d", h->max_cluster);
+    if (ctas == h->C) return FG_OK;
+    std::vector<int64_t> X, CM;
+    std::vector<double> MU;
+    if (h->state_set) {
+        X.resize(3 * (size_t)h->N);
+        MU.resize(3 * (size_t)h->N);
+        CM.resize(3 * (size_t)h->M);
+        CK(cudaMemcpyAsync(X.data(), h->rep_pos, X.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(MU.data(), h->rep_mu, MU.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(CM.data(), h->rep_cm, CM.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    int rc = mol_alloc_replicas(h, ctas);
+    if (rc) return rc;
+    h->C = ctas;
+    if (h->state_set) {
+        for (int r = 0; r < ctas; r++) {
+            CK(cudaMemcpyAsync(h->rep_pos + (size_t)r * h->N * 3, X.data(), X.size() * 8, cudaMemcpyHostToDevice,
+                               h->stream));
+            CK(cudaMemcpyAsync(h->rep_mu + (size_t)r * h->N * 3, MU.data(), MU.size() * 8, cudaMemcpyHostToDevice,
+                               h->stream));
+            CK(cudaMemcpyAsync(h->rep_cm + (size_t)r * h->M * 3, CM.data(), CM.size() * 8, cudaMemcpyHostToDevice,
+                               h->stream));
+        }
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    return mol_push_desc(h);
+}
+
+int fg_mol_get_cluster(fg_molsys *h, int32_t *ctas, int32_t *max_ctas) {
+    if (!h) return fail(FG_ERR_INVALID, "null handle");
+    if (ctas) *ctas = h->C;
+    if (max_ctas) *max_ctas = h->max_cluster;
+    return FG_OK;
+}
+
+int fg_mol_trial_du(fg_molsys *h, int32_t molecule, const double *new_xyz, const double *new_mu_unit,
+                    const double *new_mass_center, double *du) {
+    if (!h || !new_xyz || !du) return fail(FG_ERR_INVALID, "null argument");
+    if (!h->state_set) return fail(FG_ERR_STATE, "fg_mol_set_state first");
+    if (h->pending >= 0) return fail(FG_ERR_STATE, "a trial is pending: call fg_mol_commit");
+    if (molecule < 0 || molecule >= h->M) return fail(FG_ERR_INVALID, "molecule index out of range");
+    std::vector<int64_t> X(3 * (size_t)h->gs);
+    for (int s = 0; s < h->gs; s++)
+        for (int a = 0; a < 3; a++) X[3 * s + a] = to_fix(new_xyz[3 * s + a], h->P.box[a]);
+    CK(cudaMemcpyAsync(h->expl_pos, X.data(), X.size() * 8, cudaMemcpyHostToDevice, h->stream));
+    if (new_mu_unit)
+        CK(cudaMemcpyAsync(h->expl_mu, new_mu_unit, (size_t)h->gs * 3 * 8, cudaMemcpyHostToDevice, h->stream));
+    int64_t cm[3];
+    if (new_mass_center) {
+        for (int a = 0; a < 3; a++) cm[a] = to_fix(new_mass_center[a], h->P.box[a]);
+        CK(cudaMemcpyAsync(h->expl_cm, cm, sizeof(cm), cudaMemcpyHostToDevice, h->stream));
+    }
+    fgm::MolTrial t{};
+    t.g = molecule;
+    t.flags = 4;
+    t.qw = 1.0;
+    CK(cudaMemcpyAsync(h->trials, &t, sizeof(t), cudaMemcpyHostToDevice, h->stream));
+    h->desc.expl_pos = h->expl_pos;
+    h->desc.expl_mu = new_mu_unit ? h->expl_mu : nullptr;
+    h->desc.expl_cm = new_mass_center ? h->expl_cm : nullptr;
+    h->desc.trials = h->trials;
+    int rc = mol_push_desc(h);
+    if (rc) return rc;
+    MolLaunch L;
+    rc = mol_pick<true>(h, L);
+    if (rc) return rc;
+    rc = mol_launch(h, L, h->d_desc, 1, h->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(du, h->eval_du, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->pending = molecule;
+    h->pending_du = *du;
+    return FG_OK;
+}
+
+int fg_mol_commit(fg_molsys *h, int32_t accepted) {
+    if (!h) return fail(FG_ERR_INVALID, "null handle");
+    if (h->pending < 0) return fail(FG_ERR_STATE, "no pending trial");
+    const int g = h->pending;
+    h->pending = -1;
+    if (!accepted) return FG_OK;
+    fgm::mol_commit_kernel<<<1, 64, 0, h->stream>>>(h->d_desc, g, 1, h->C);
+    CK(cudaGetLastError());
+    fgm::MolScalars s;
+    int rc = mol_read_scalars(h, s);
+    if (rc) return rc;
+    s.n_accepted++;
+    const double ut = df_val(s.utot_hi, s.utot_lo) + h->pending_du;
+    const float2 f = split_df(ut);
+    s.utot_hi = f.x;
+    s.utot_lo = f.y;
+    return mol_write_scalars(h, s);
+}
+
+// Reference draws for n TranslateRotate trials on one molecule kind
+// ("permol"), consuming the global slump as move.h:1624-1685 and 567-573 do.
+int fg_mol_draw_stream(uint32_t seed, int32_t n_molecules, int64_t n, double dp, double dprot,
+                       int32_t center_rotation, int32_t *mol, double *axis, int32_t *center, double *angle,
+                       double *trans, double *u) {
+    if (n_molecules < 1 || n < 0 || (n > 0 && (!mol || !u))) return fail(FG_ERR_INVALID, "bad argument");
+    std::mt19937 eng(seed);
+    std::uniform_real_distribution<double> U(0, 1);
+    for (int64_t k = 0; k < n; k++) {
+        std::uniform_int_distribution<int> pick(0, n_molecules - 1);
+        mol[k] = pick(eng);                                     // slump.element(gvec)
+        double v[3] = {0, 0, 0}, ang = 0.0, t[3] = {0, 0, 0};
+        int c = 0;
+        if (dprot > 1e-6) {
+            double r2;
+            do {                                                // Point::ranunit (point.h:74-88)
+                for (int a = 0; a < 3; a++) v[a] = (2 * U(eng) - 1) * 1.0;
+                r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            } while (r2 > 1);
+            const double s = std::sqrt(r2);
+            for (int a = 0; a < 3; a++) v[a] /= s;
+            if (!center_rotation) c = (U(eng) < 0.5) ? 1 : 2;
+            ang = dprot * (U(eng) - 0.5);                       // slump.half()
+        }
+        if (dp > 1e-6)
+            for (int a = 0; a < 3; a++) t[a] = 1.0 * dp * (U(eng) - 0.5);
+        const double um = U(eng);                               // Movebase::metropolis
+        for (int a = 0; a < 3; a++) {
+            if (axis) axis[3 * k + a] = v[a];
+            if (trans) trans[3 * k + a] = t[a];
+        }
+        if (center) center[k] = c;
+        if (angle) angle[k] = ang;
+        u[k] = um;
+    }
+    return FG_OK;
+}
+
+// n TranslateRotate trials on the device. rotate/translate say whether the
+// move has dprot/dp above 1e-6 (move.h:1642, 1671); the arrays are the draws
+// (fg_mol_draw_stream). acc/du (may be NULL) receive per-trial results.
+int fg_mol_sweep(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, const double *angle,
+                 const int32_t *center, const double *trans, const double *u, int32_t rotate, int32_t translate,
+                 uint8_t *acc, double *du, fg_sweep_stats *stats) {
+    if (!h || n < 0 || (n > 0 && (!mol || !u))) return fail(FG_ERR_INVALID, "bad argument");
+    if (rotate && n > 0 && (!axis || !angle)) return fail(FG_ERR_INVALID, "rotation needs axis and angle");
+    if (translate && n > 0 && !trans) return fail(FG_ERR_INVALID, "translation needs trans");
+    if (!h->state_set) return fail(FG_ERR_STATE, "fg_mol_set_state first");
+    if (h->pending >= 0) return fail(FG_ERR_STATE, "a trial is pending: call fg_mol_commit");
+    for (int64_t k = 0; k < n; k++) {
+        if (mol[k] < 0 || mol[k] >= h->M) return fail(FG_ERR_INVALID, "molecule index out of range at %lld", (long long)k);
+        if (center && (center[k] < 0 || center[k] > 2)) return fail(FG_ERR_INVALID, "bad centre kind");
+    }
+    const bool log = acc || du;
+    int rc = mol_ensure_trials(h, n, log);
+    if (rc) return rc;
+    std::vector<fgm::MolTrial> tr;
+    mol_make_trials(h, n, mol, axis, angle, center, trans, u, rotate, translate, tr);
+    if (n > 0) CK(cudaMemcpyAsync(h->trials, tr.data(), n * sizeof(fgm::MolTrial), cudaMemcpyHostToDevice, h->stream));
+    fgm::MolScalars s0;
+    rc = mol_read_scalars(h, s0);
+    if (rc) return rc;
+    fgm::MolScalars s = s0;
+    s.cursor = 0;
+    s.n_trials = n;
+    s.u_hi = s.u_lo = 0.0f;
+    s.error = 0;
+    rc = mol_write_scalars(h, s);
+    if (rc) return rc;
+    h->desc.log_du = log ? h->log_du : nullptr;
+    h->desc.log_acc = log ? h->log_acc : nullptr;
+    h->desc.expl_pos = nullptr;
+    h->desc.expl_mu = nullptr;
+    h->desc.expl_cm = nullptr;
+    rc = mol_push_desc(h);
+    if (rc) return rc;
+    MolLaunch L;
+    rc = mol_pick<false>(h, L);
+    if (rc) return rc;
+    // launches of at most kChunk trials (the kernel runs from the stored cursor
+    // to the stored end; each launch moves the end forward)
+    const int64_t kChunk = 65536;
+    const int64_t nl = (n + kChunk - 1) / kChunk;
+    std::vector<int64_t> ends(nl);
+    CK(cudaEventRecord(h->ev0, h->stream));
+    for (int64_t c = 0; c < nl; c++) {
+        ends[c] = std::min(n, (c + 1) * kChunk);
+        CK(cudaMemcpyAsync(&h->sc->n_trials, &ends[c], sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+        rc = mol_launch(h, L, h->d_desc, 1, h->stream);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaEventSynchronize(h->ev1));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    rc = mol_read_scalars(h, s);
+    if (rc) return rc;
+    if (log && n > 0) {
+        std::vector<float2> l(n);
+        std::vector<uint8_t> a(n);
+        CK(cudaMemcpyAsync(l.data(), h->log_du, n * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(a.data(), h->log_acc, n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        for (int64_t k = 0; k < n; k++) {
+            if (du) du[k] = df_val(l[k].x, l[k].y);
+            if (acc) acc[k] = a[k];
+        }
+    }
+    if (stats) {
+        *stats = fg_sweep_stats{};
+        stats->trials = s.cursor;
+        stats->accepted = s.n_accepted - s0.n_accepted;
+        stats->energy_change = df_val(s.u_hi, s.u_lo);
+        stats->device_ms = ms;
+        stats->sweep_kernel_ms = ms;
+        stats->sweep_launches = (int32_t)nl;
+        stats->error_flags = s.error;
+        stats->kernel_launches = nl;
+    }
+    if (s.error) return fail(FG_ERR_DEVICE, "device error flags 0x%x", s.error);
+    return FG_OK;
+}
+
+// comp = {intermolecular, intramolecular, total} in FP64 (systemEnergy).
+int fg_mol_total_energy(fg_molsys *h, double *comp) {
+    if (!h || !comp) return fail(FG_ERR_INVALID, "null argument");
+    if (!h->state_set) return fail(FG_ERR_STATE, "no state");
+    double t[2];
+    int rc = mol_total(h, t);
+    if (rc) return rc;
+    comp[0] = t[0];
+    comp[1] = t[1];
+    comp[2] = t[1] + t[0];
+    return FG_OK;
+}
+
+// Running total energy (initial total + accepted dU since fg_mol_set_state).
+int fg_mol_running_energy(fg_molsys *h, double *u) {
+    if (!h || !u) return fail(FG_ERR_INVALID, "null argument");
+    fgm::MolScalars s;
+    int rc = mol_read_scalars(h, s);
+    if (rc) return rc;
+    *u = df_val(s.utot_hi, s.utot_lo);
+    return FG_OK;
+}
+
+int64_t fg_mol_device_bytes(fg_molsys *h) { return h ? (int64_t)h->device_bytes : 0; }
+
+}  // extern "C"

@@ -88,6 +88,20 @@ def lib(build_if_missing=True):
             "fg_server_poll": ([vp, i64, dp, dp, dp, dp, dp], ctypes.c_int),
             "fg_server_release": ([vp, i64], ctypes.c_int),
             "fg_server_bytes_in_use": ([vp], ctypes.c_int64),
+            "fg_mol_create": ([vp, i32, i32, ctypes.POINTER(vp)], ctypes.c_int),
+            "fg_mol_destroy": ([vp], ctypes.c_int),
+            "fg_mol_set_state": ([vp, dp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_mol_get_state": ([vp, dp, dp, dp], ctypes.c_int),
+            "fg_mol_set_cluster": ([vp, i32], ctypes.c_int),
+            "fg_mol_get_cluster": ([vp, dp, dp], ctypes.c_int),
+            "fg_mol_trial_du": ([vp, i32, dp, dp, dp, dp], ctypes.c_int),
+            "fg_mol_commit": ([vp, i32], ctypes.c_int),
+            "fg_mol_draw_stream": ([u32, i32, i64, ctypes.c_double, ctypes.c_double, i32, dp, dp, dp, dp, dp, dp],
+                                   ctypes.c_int),
+            "fg_mol_sweep": ([vp, i64, dp, dp, dp, dp, dp, dp, i32, i32, dp, dp, dp], ctypes.c_int),
+            "fg_mol_total_energy": ([vp, dp], ctypes.c_int),
+            "fg_mol_running_energy": ([vp, dp], ctypes.c_int),
+            "fg_mol_device_bytes": ([vp], ctypes.c_int64),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -363,3 +377,115 @@ class Server:
     @property
     def bytes_in_use(self):
         return int(lib().fg_server_bytes_in_use(self.h))
+
+
+def mol_draw_stream(seed, n_molecules, n, dp=1.0, dprot=0.3, center_rotation=True):
+    """The reference's draws for n TranslateRotate trials (host only)."""
+    g = np.empty(n, np.int32)
+    ax = np.empty((n, 3))
+    ce = np.empty(n, np.int32)
+    an = np.empty(n)
+    tr = np.empty((n, 3))
+    u = np.empty(n)
+    _check(lib().fg_mol_draw_stream(seed, n_molecules, n, dp, dprot, 1 if center_rotation else 0, _p(g), _p(ax),
+                                    _p(ce), _p(an), _p(tr), _p(u)))
+    return dict(group=g, axis=ax, center=ce, angle=an, trans=tr, u=u)
+
+
+class MolSystem:
+    """Rigid dipolar molecules on one GPU (fg_mol_* C-ABI)."""
+
+    def __init__(self, params, xyz, mu_unit, mu_scalar, type_ids, sites_per_molecule, mass_centers=None,
+                 cluster=0):
+        n = len(type_ids)
+        h = ctypes.c_void_p()
+        _check(lib().fg_mol_create(ctypes.byref(params), n, sites_per_molecule, ctypes.byref(h)))
+        self.h = h
+        self.n, self.gs, self.m = n, sites_per_molecule, n // sites_per_molecule
+        if cluster:
+            self.cluster = cluster
+        self.set_state(xyz, mu_unit, mu_scalar, type_ids, mass_centers)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fg_mol_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, xyz, mu_unit, mu_scalar, type_ids, mass_centers=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        mu = None if mu_unit is None else np.ascontiguousarray(mu_unit, dtype=np.float64).reshape(-1, 3)
+        ms = None if mu_scalar is None else np.ascontiguousarray(mu_scalar, dtype=np.float64)
+        ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+        cm = None if mass_centers is None else np.ascontiguousarray(mass_centers, dtype=np.float64).reshape(-1, 3)
+        _check(lib().fg_mol_set_state(self.h, _p(xyz), _p(mu), _p(ms), _p(ids), _p(cm)))
+
+    def state(self):
+        xyz = np.empty((self.n, 3))
+        mu = np.empty((self.n, 3))
+        cm = np.empty((self.m, 3))
+        _check(lib().fg_mol_get_state(self.h, _p(xyz), _p(mu), _p(cm)))
+        return xyz, mu, cm
+
+    @property
+    def cluster(self):
+        c = np.zeros(2, np.int32)
+        _check(lib().fg_mol_get_cluster(self.h, _p(c[:1]), _p(c[1:])))
+        return int(c[0])
+
+    @cluster.setter
+    def cluster(self, c):
+        _check(lib().fg_mol_set_cluster(self.h, int(c)))
+
+    @property
+    def max_cluster(self):
+        c = np.zeros(2, np.int32)
+        _check(lib().fg_mol_get_cluster(self.h, _p(c[:1]), _p(c[1:])))
+        return int(c[1])
+
+    def trial_du(self, molecule, new_xyz, new_mu=None, new_cm=None):
+        x = np.ascontiguousarray(new_xyz, dtype=np.float64).reshape(-1, 3)
+        m = None if new_mu is None else np.ascontiguousarray(new_mu, dtype=np.float64).reshape(-1, 3)
+        c = None if new_cm is None else np.ascontiguousarray(new_cm, dtype=np.float64)
+        du = np.zeros(1)
+        _check(lib().fg_mol_trial_du(self.h, molecule, _p(x), _p(m), _p(c), _p(du)))
+        return float(du[0])
+
+    def commit(self, accepted):
+        _check(lib().fg_mol_commit(self.h, 1 if accepted else 0))
+
+    def sweep(self, st, rotate=True, translate=True, log=True):
+        n = len(st["group"])
+        g = np.ascontiguousarray(st["group"], dtype=np.int32)
+        ax = np.ascontiguousarray(st["axis"], dtype=np.float64)
+        an = np.ascontiguousarray(st["angle"], dtype=np.float64)
+        ce = np.ascontiguousarray(st["center"], dtype=np.int32)
+        tr = np.ascontiguousarray(st["trans"], dtype=np.float64)
+        u = np.ascontiguousarray(st["u"], dtype=np.float64)
+        acc = np.empty(n, np.uint8) if log else None
+        du = np.empty(n) if log else None
+        stats = SweepStats()
+        _check(lib().fg_mol_sweep(self.h, n, _p(g), _p(ax), _p(an), _p(ce), _p(tr), _p(u), 1 if rotate else 0,
+                                  1 if translate else 0, _p(acc), _p(du), ctypes.byref(stats)))
+        out = stats.as_dict()
+        out.update(acc=acc, du=du)
+        return out
+
+    def total_energy(self):
+        c = np.empty(3)
+        _check(lib().fg_mol_total_energy(self.h, _p(c)))
+        return c
+
+    def running_energy(self):
+        u = np.zeros(1)
+        _check(lib().fg_mol_running_energy(self.h, _p(u)))
+        return float(u[0])
+
+    @property
+    def device_bytes(self):
+        return int(lib().fg_mol_device_bytes(self.h))

@@ -219,6 +219,68 @@ int64_t fg_server_bytes_in_use(fg_server *s);
 int fg_pair_energy_noalloc(const fg_params *params, int32_t n, const double *d_xyz, const double *d_charge,
                            const int32_t *d_types, double *d_energy, void *stream);
 
+/* ------------------------------------------------------------------ rigid dipolar molecules
+ * Space<Cuboid, DipoleParticle> with equal-size rigid molecules (contiguous
+ * sites), energy NonbondedVector over CoulombGalore + LennardJonesLB +
+ * IonDipole + DipoleDipoleGalore (reaction field, FG_MODEL_MULTIPOLE_RF), and
+ * the TranslateRotate move. One system runs on a thread-block cluster of
+ * CTAs (fg_mol_set_cluster). */
+typedef struct fg_molsys fg_molsys;
+
+/* Create a system of n_sites sites in molecules of sites_per_molecule (<= 32)
+ * consecutive sites. Replaces: Space(json) with a molecular "moleculelist"
+ * entry + NonbondedVector<Tspace, CombinedPairPotential<...>>(json)
+ * (energy.h:1062-1090, multipole.h:600-640, 836-870, 983-990). */
+int fg_mol_create(const fg_params *params, int32_t n_sites, int32_t sites_per_molecule, fg_molsys **out);
+int fg_mol_destroy(fg_molsys *h);
+
+/* Positions (3N), dipole unit vectors (3N, may be NULL: no dipoles), dipole
+ * scalars in e*Angstrom (N, may be NULL), atom types (N), molecule mass
+ * centres (3M, may be NULL: computed as Geometry::massCenter with equal
+ * masses, geometry.h:714-738). Replaces: Energybase::setSpace
+ * (energy.h:88-92) after Group::setMassCenter (group.h:174-179). */
+int fg_mol_set_state(fg_molsys *h, const double *xyz, const double *mu_unit, const double *mu_scalar,
+                     const int32_t *type_ids, const double *mass_centers);
+int fg_mol_get_state(fg_molsys *h, double *xyz, double *mu_unit, double *mass_centers);
+
+/* CTAs per system (power of two up to the device's cluster limit). */
+int fg_mol_set_cluster(fg_molsys *h, int32_t ctas);
+int fg_mol_get_cluster(fg_molsys *h, int32_t *ctas, int32_t *max_ctas);
+
+/* dU of moving molecule `molecule` to new site positions (3*gs) and dipole
+ * unit vectors (3*gs, may be NULL: unchanged), with its new mass centre (3,
+ * may be NULL). Replaces: Energy::energyChange (energy.h:3577-3621) with a
+ * whole-group Change (move.h:1685) -> g2All -> NonbondedVector::g2g. */
+int fg_mol_trial_du(fg_molsys *h, int32_t molecule, const double *new_xyz, const double *new_mu_unit,
+                    const double *new_mass_center, double *du);
+/* Accept or reject the pending trial. Replaces: TranslateRotate::_acceptMove
+ * / _rejectMove (move.h:1688-1705, Group::accept/undo group.h:370-385). */
+int fg_mol_commit(fg_molsys *h, int32_t accepted);
+
+/* The reference's global-slump draws of n TranslateRotate trials on one
+ * molecule kind with "permol" (move.h:1624-1685, point.h:74-88, 567-573):
+ * molecule, unit axis (3n), centre kind (0 mass centre, 1 first site, 2 last
+ * site; only when center_rotation is 0), angle, translation (3n),
+ * Metropolis uniform. Host only (no device). */
+int fg_mol_draw_stream(uint32_t seed, int32_t n_molecules, int64_t n, double dp, double dprot,
+                       int32_t center_rotation, int32_t *mol, double *axis, int32_t *center, double *angle,
+                       double *trans, double *u);
+
+/* n TranslateRotate trials on the device from those draws; rotate/translate
+ * say whether dprot/dp exceed 1e-6 (move.h:1642, 1671). acc and du (may be
+ * NULL) receive per-trial results. Replaces: Movebase::move with
+ * TranslateRotate (move.h:515-555, 1620-1705). */
+int fg_mol_sweep(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, const double *angle,
+                 const int32_t *center, const double *trans, const double *u, int32_t rotate, int32_t translate,
+                 uint8_t *acc, double *du, fg_sweep_stats *stats);
+
+/* comp = {intermolecular, intramolecular, total}, FP64. Replaces:
+ * Energybase::systemEnergy (energy.h:169-180). */
+int fg_mol_total_energy(fg_molsys *h, double *comp);
+/* Total energy at fg_mol_set_state plus every accepted dU since. */
+int fg_mol_running_energy(fg_molsys *h, double *u);
+int64_t fg_mol_device_bytes(fg_molsys *h);
+
 #ifdef __cplusplus
 }
 #endif
