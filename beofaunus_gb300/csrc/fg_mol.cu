@@ -44,7 +44,7 @@ using fg::hi32;
 using fg::warp_sum_df;
 
 constexpr int kMolThreads = 512;
-constexpr int kMaxGroupSites = 32;
+constexpr int kMaxGroupSites = 31;   // lane gs of the setup warp computes the mass centre
 constexpr int kQueueCap = 3072;
 constexpr int kMaxCluster = 16;
 
@@ -72,14 +72,17 @@ struct MolScalars {
 };
 
 struct alignas(16) MolDesc {
-    int32_t N, gs, M, D, nt, C, uniform_lj, pad;
+    int32_t N, gs, M, D, nt, C, uniform_lj, cubic;
     float s32[3];       // L / 2^32 (one unit of the high word)
     float sc9[3];       // 512 L / 2^32 (unit of the high word >> 9)
-    double s48d[3];     // L / 2^48
     double s64d[3];     // L / 2^64
     double inv64d[3];   // 2^64 / L
-    float lB, rc2, rc2near, rc1i, A5, B5, kT, pad2;
+    float lB, rc2, rc2near, rc1i, A5, B5, kT, rfB;
+    float s32sq, pad2[3];  // (L / 2^32)^2 for cubic boxes
     double lBd, rcd, rfBd, pad3;
+    long long rc2int;  // ceil(rc^2) in squared high-word units (cubic boxes)
+    long long pad4;
+    double s32sqd[3];
     float s2[256], eps4[256], lbqq[256];
     float qtype[16];
     double s2d[256], eps4d[256];  // FP64 copies for the total energy
@@ -87,13 +90,11 @@ struct alignas(16) MolDesc {
     double *rep_mu;    // C replicas x N x 3, dipole unit vectors
     int64_t *rep_cm;   // C replicas x M x 3, mass centres
     int4 *pos4;        // N: rounded high words (x, y, z), type
-    short4 *pos_ext;   // N: next 16 bits
     int32_t *site_dip; // N: index in the dipole list, or -1
     int32_t *dip_site; // D: site of each dipole
     double *mus;       // N: dipole scalars (e Angstrom)
     float4 *dip4;      // D: mu-hat * mu (x, y, z), mu
-    int4 *dip_pos4;    // D: positions of the dipole sites
-    short4 *dip_ext;   // D
+    int4 *dip_pos4;    // D: positions of the dipole sites, .w = site << 8 | type
     const MolTrial *trials;
     float2 *log_du;
     uint8_t *log_acc;
@@ -129,12 +130,6 @@ __device__ __forceinline__ int wsub(int a, int b) { return (int)((uint32_t)a - (
 // Exact float of |m| < 2^22 without the conversion pipe.
 __device__ __forceinline__ float small_to_float(int m) { return __int_as_float(0x4B400000 + m) - 12582912.0f; }
 
-__device__ __forceinline__ int16_t ext16d(int64_t X) {
-    int32_t h = hi32(X);
-    int32_t rem = (int32_t)((uint64_t)X - ((uint64_t)(uint32_t)h << 32));
-    return (int16_t)(rem >> 16);
-}
-
 struct D3 {
     double x, y, z;
 };
@@ -150,46 +145,45 @@ __device__ __forceinline__ D3 qrot(double w, const D3 &v, const D3 &p) {
     return {p.x + w * uv.x + c.x, p.y + w * uv.y + c.y, p.z + w * uv.z + c.z};
 }
 
-// 48-bit difference a - b (units L / 2^48) from high words and extensions.
-__device__ __forceinline__ int64_t d48(int ha, int hb, int ea, int eb) {
-    return (int64_t)wsub(ha, hb) * 65536 + (int64_t)(ea - eb);
-}
-
 // ---------------------------------------------------------------- shared memory
+// Moved-molecule data, double-buffered: while the CTA sums trial t, the last
+// warp prepares trial t+1 (its rotation runs in FP64 and is latency-bound).
+struct GroupBuf {
+    int4 *go, *gn;    // old/new high words; .w = type | dipole flag (go) / site << 8 | type (gn)
+    float4 *gfo;      // old dipole vector mu-hat * mu (x, y, z), mu
+    float4 *gfn;      // new dipole vector
+    double *gmu;      // [gs][3] new unit dipole (FP64, for the replica)
+    int64_t *gX;      // [gs][3] new fixed-point positions
+    int64_t *gcm;     // [3] new mass centre
+};
+
 struct MolSmem {
-    int4 *spos;     // site slice
-    short4 *sext;
-    float4 *sdip;   // dipole slice
-    int4 *sdpos;
-    short4 *sdext;
-    int4 *go, *gn;      // moved sites: old/new high words + type | dipole flag
-    short4 *geo, *gen;  // old/new extensions
-    double *gmu;        // [gs][6]: old unit dipole (3), new (3)
-    int64_t *gX;        // [gs][3]: new fixed-point positions
-    int64_t *gcm;       // [3]: new mass centre
+    int4 *spos;     // site slice: high words, .w = type
+    float4 *sdip;   // dipole slice: mu-hat * mu, mu
+    int4 *sdpos;    // dipole slice positions, .w = site << 8 | type
+    GroupBuf buf[2];
     uint32_t *queue;
     int *qcount;
     float2 *red;   // [32]
     float2 *part;  // [2] cluster partial sums (double-buffered by trial parity)
-    int *flag;     // [4]: decision, error
+    int *flag;     // [4]: decision, speculation invalid
 };
 
 __host__ __device__ inline size_t mol_align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
+__host__ __device__ inline size_t mol_group_bytes(int gs) {
+    return mol_align16((size_t)gs * 16 * 4) + mol_align16((size_t)gs * 3 * 8 * 2 + 3 * 8);
+}
+
 __host__ __device__ inline void mol_smem_layout(int ns, int nd, int gs, bool slice_smem, size_t off[16]) {
     size_t o = 0;
     off[0] = o; o += mol_align16(slice_smem ? (size_t)ns * 16 : 0);   // spos
-    off[1] = o; o += mol_align16(slice_smem ? (size_t)ns * 8 : 0);    // sext
-    off[2] = o; o += mol_align16((size_t)nd * 16);                    // sdip
-    off[3] = o; o += mol_align16((size_t)nd * 16);                    // sdpos
-    off[4] = o; o += mol_align16((size_t)nd * 8);                     // sdext
-    off[5] = o; o += mol_align16((size_t)gs * 16 * 2);                // go, gn
-    off[6] = o; o += mol_align16((size_t)gs * 8 * 2);                 // geo, gen
-    off[7] = o; o += mol_align16((size_t)gs * 6 * 8);                 // gmu
-    off[8] = o; o += mol_align16((size_t)gs * 3 * 8 + 3 * 8);         // gX, gcm
-    off[9] = o; o += mol_align16((size_t)kQueueCap * 4 + 16);         // queue, qcount
-    off[10] = o; o += mol_align16(32 * 8 + 2 * 8 + 16);               // red, part, flag
-    off[11] = o;
+    off[1] = o; o += mol_align16((size_t)nd * 16);                    // sdip
+    off[2] = o; o += mol_align16((size_t)nd * 16);                    // sdpos
+    off[3] = o; o += 2 * mol_group_bytes(gs);                         // group buffers
+    off[4] = o; o += mol_align16((size_t)kQueueCap * 4 + 16);         // queue, qcount
+    off[5] = o; o += mol_align16(32 * 8 + 2 * 8 + 16);                // red, part, flag
+    off[6] = o;
 }
 
 __device__ inline MolSmem mol_carve(unsigned char *base, int ns, int nd, int gs, bool slice_smem) {
@@ -197,29 +191,37 @@ __device__ inline MolSmem mol_carve(unsigned char *base, int ns, int nd, int gs,
     mol_smem_layout(ns, nd, gs, slice_smem, off);
     MolSmem s;
     s.spos = (int4 *)(base + off[0]);
-    s.sext = (short4 *)(base + off[1]);
-    s.sdip = (float4 *)(base + off[2]);
-    s.sdpos = (int4 *)(base + off[3]);
-    s.sdext = (short4 *)(base + off[4]);
-    s.go = (int4 *)(base + off[5]);
-    s.gn = s.go + gs;
-    s.geo = (short4 *)(base + off[6]);
-    s.gen = s.geo + gs;
-    s.gmu = (double *)(base + off[7]);
-    s.gX = (int64_t *)(base + off[8]);
-    s.gcm = s.gX + 3 * gs;
-    s.queue = (uint32_t *)(base + off[9]);
+    s.sdip = (float4 *)(base + off[1]);
+    s.sdpos = (int4 *)(base + off[2]);
+    for (int b = 0; b < 2; b++) {
+        unsigned char *g = base + off[3] + b * mol_group_bytes(gs);
+        GroupBuf &B = s.buf[b];
+        B.go = (int4 *)g;
+        B.gn = B.go + gs;
+        B.gfo = (float4 *)(B.gn + gs);
+        B.gfn = B.gfo + gs;
+        B.gmu = (double *)(g + mol_align16((size_t)gs * 16 * 4));
+        B.gX = (int64_t *)(B.gmu + 3 * gs);
+        B.gcm = B.gX + 3 * gs;
+    }
+    s.queue = (uint32_t *)(base + off[4]);
     s.qcount = (int *)(s.queue + kQueueCap);
-    s.red = (float2 *)(base + off[10]);
+    s.red = (float2 *)(base + off[5]);
     s.part = s.red + 32;
     s.flag = (int *)(s.part + 2);
     return s;
 }
 
 // ---------------------------------------------------------------- pair terms
-// Far LJ for one position pair from high words: 22-bit truncated differences
-// (error < 2e-5 Angstrom, i.e. < 2e-6 relative at r >= rc), squared distance
-// in units of sc9^2 folded into s2u.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Far pairs: squared distance from 22-bit-truncated high-word differences
+// (error < 2e-5 Angstrom, < 2e-6 relative at r >= rc), converted without the
+// conversion pipe.
 __device__ __forceinline__ float far_r2(int4 a, int4 b, float3 sc9) {
     const float dx = small_to_float(wsub(a.x, b.x) >> 9) * sc9.x;
     const float dy = small_to_float(wsub(a.y, b.y) >> 9) * sc9.y;
@@ -227,7 +229,7 @@ __device__ __forceinline__ float far_r2(int4 a, int4 b, float3 sc9) {
     return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 __device__ __forceinline__ float lj_r2(float r2, float s2, float e4) {
-    const float x = s2 * __frcp_rn(r2);
+    const float x = s2 * rcp_approx(r2);
     const float x3 = x * x * x;
     return e4 * fmaf(x3, x3, -x3);
 }
@@ -236,150 +238,133 @@ __device__ __forceinline__ float lj_r2(float r2, float s2, float e4) {
 __device__ __forceinline__ float3 diff32(int4 a, int4 b, float3 s32) {
     return make_float3((float)wsub(a.x, b.x) * s32.x, (float)wsub(a.y, b.y) * s32.y, (float)wsub(a.z, b.z) * s32.z);
 }
+__device__ __forceinline__ float dot3f(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
 
-// Coulomb Q5(q) = (q-1)^3 (A5 q^2 + B5 q - 1) / r part: f(r) = Q5(r/rc)/r.
-__device__ __forceinline__ float coul_f(float r, const MolDesc &d) {
-    const float q = r * d.rc1i;
+// Coulomb part f(r) = Q5(r/rc) / r with Q5(q) = (q-1)^3 (A5 q^2 + B5 q - 1).
+__device__ __forceinline__ float coul_f(float r, float rc1i, float A5, float B5) {
+    const float q = r * rc1i;
     const float qm = q - 1.0f;
-    return qm * qm * qm * fmaf(fmaf(d.A5, q, d.B5), q, -1.0f) / r;
+    return qm * qm * qm * fmaf(fmaf(A5, q, B5), q, -1.0f) / r;
 }
 
-// FP64 position difference of sites with high words/extensions (a - b).
-__device__ __forceinline__ D3 diff48(int4 ha, short4 ea, int4 hb, short4 eb, const MolDesc &d) {
-    return {(double)d48(ha.x, hb.x, ea.x, eb.x) * d.s48d[0], (double)d48(ha.y, hb.y, ea.y, eb.y) * d.s48d[1],
-            (double)d48(ha.z, hb.z, ea.z, eb.z) * d.s48d[2]};
-}
-
-// IonDipole (q2mu, multipole.h:269-277) in FP64 with r = r_a - r_b:
-// lB [qa mub (mub.r) - qb mua (mua.r)] / r^3, mu vectors already scaled.
-__device__ __forceinline__ double ion_dipole64(double qa, const D3 &mua, double qb, const D3 &mub, const D3 &r,
-                                               double lB) {
-    const double r2i = 1.0 / dot3(r, r);
-    const double r3i = sqrt(r2i) * r2i;
-    return lB * (qa * dot3(mub, r) * r3i - qb * dot3(mua, r) * r3i);
-}
-// DipoleDipoleGalore with the reaction field (multipole.h:287-299, 767-782, 910-920).
-__device__ __forceinline__ double dipole_dipole64(const D3 &ua, double ma, const D3 &ub, double mb, const D3 &r,
-                                                  const MolDesc &d) {
-    const double r2 = dot3(r, r);
-    const double r1 = sqrt(r2);
-    if (!(r1 < d.rcd)) return 0.0;
-    const double q = r1 / d.rcd;
-    const double bf = d.rfBd * q * q * q;
-    const double r2i = 1.0 / r2;
-    const double dt = dot3(ua, ub);
-    const double T = (3.0 * dot3(ua, r) * dot3(ub, r) * r2i - dt) + dt * bf;
-    return d.lBd * (-(ma * mb) * T * sqrt(r2i) * r2i);
-}
-
-// Near pair, kind A: moved site i against slice site j (LJ + Coulomb, and the
-// ion-dipole term of the moved dipole with j's charge).
-__device__ __noinline__ df near_pair_a(int i, int4 pj, short4 ej, const MolSmem &s, const MolDesc &d, bool idip) {
-    const int4 po = s.go[i], pn = s.gn[i];
-    const short4 eo = s.geo[i], en = s.gen[i];
-    const D3 ro = diff48(po, eo, pj, ej, d), rn = diff48(pn, en, pj, ej, d);
-    const double ro2d = dot3(ro, ro), rn2d = dot3(rn, rn);
-    // r_n^2 - r_o^2 from exact 48-bit integers: sum_a (dn - do)(dn + do)
-    double S = 0.0;
-    {
-        const int64_t dno[3] = {d48(pn.x, pj.x, en.x, ej.x) - d48(po.x, pj.x, eo.x, ej.x),
-                                d48(pn.y, pj.y, en.y, ej.y) - d48(po.y, pj.y, eo.y, ej.y),
-                                d48(pn.z, pj.z, en.z, ej.z) - d48(po.z, pj.z, eo.z, ej.z)};
-        const int64_t spo[3] = {d48(pn.x, pj.x, en.x, ej.x) + d48(po.x, pj.x, eo.x, ej.x),
-                                d48(pn.y, pj.y, en.y, ej.y) + d48(po.y, pj.y, eo.y, ej.y),
-                                d48(pn.z, pj.z, en.z, ej.z) + d48(po.z, pj.z, eo.z, ej.z)};
+// r_new^2 - r_old^2 (Angstrom^2) from exact integer arithmetic on the high
+// words: sum_a (dn_a - do_a)(dn_a + do_a), each minimum image taken
+// separately as Cuboid::vdist does; |product| < 2^62 always.
+__device__ __forceinline__ float dr2_exact(int4 pn, int4 po, int4 pj, const MolDesc &d) {
+    const int dn[3] = {wsub(pn.x, pj.x), wsub(pn.y, pj.y), wsub(pn.z, pj.z)};
+    const int dO[3] = {wsub(po.x, pj.x), wsub(po.y, pj.y), wsub(po.z, pj.z)};
+    if (d.cubic) {
+        long long S = 0;
 #pragma unroll
-        for (int a = 0; a < 3; a++) S = fma((double)dno[a] * d.s48d[a], (double)spo[a] * d.s48d[a], S);
+        for (int a = 0; a < 3; a++) S += ((long long)dn[a] - dO[a]) * ((long long)dn[a] + dO[a]);
+        return (float)S * d.s32sq;
     }
+    double S = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        S += (double)(((long long)dn[a] - dO[a]) * ((long long)dn[a] + dO[a])) * d.s32sqd[a];
+    return (float)S;
+}
+
+// Near pair, kind A: moved site i (old po, new pn) against site j: LJ and
+// Coulomb as differences whose rounding scales with the difference, and the
+// ion-dipole term of i's dipole with j's charge (FP32, a few per trial).
+__device__ __noinline__ float near_pair_a(int4 po, int4 pn, float4 fo, float4 fn, int4 pj, const MolDesc &d) {
+    const float3 s32 = make_float3(d.s32[0], d.s32[1], d.s32[2]);
+    const float3 ro = diff32(po, pj, s32), rn = diff32(pn, pj, s32);
+    const float ro2 = dot3f(ro, ro), rn2 = dot3f(rn, rn);
+    const float dR2 = dr2_exact(pn, po, pj, d);
     const int ti = po.w & 0xFF, tj = pj.w & 0xFF;
-    const int t = d.uniform_lj ? 0 : ti * d.nt + tj;
-    const float ro2 = (float)ro2d, rn2 = (float)rn2d, dR2 = (float)S;
+    const int t = ti * d.nt + tj;
     // LJ: 4eps x_o^3 (t^3 - 1)(x_o^3 (t^3 + 1) - 1), t^3 - 1 from tau = -dR2 / r_n^2
     const float xo = d.s2[t] / ro2;
     const float xo3 = xo * xo * xo;
     const float tau = -dR2 / rn2;
     const float t3m1 = tau * fmaf(tau, tau + 3.0f, 3.0f);
     float acc = d.eps4[t] * xo3 * t3m1 * fmaf(xo3, t3m1 + 2.0f, -1.0f);
-    // Coulomb (CoulombGalore): cutoff tested on FP64 squared distances
-    const float A = d.lbqq[ti * d.nt + tj];
+    // Coulomb (CoulombGalore)
+    const float A = d.lbqq[t];
     if (A != 0.0f) {
-        const bool io = ro2d < (double)d.rc2 , in_ = rn2d < (double)d.rc2;
+        const bool io = ro2 < d.rc2, in_ = rn2 < d.rc2;
         const float r_o = sqrtf(ro2), r_n = sqrtf(rn2);
         if (io && in_) {
-            // f_n - f_o = [Q5(q_n) - Q5(q_o)] / r_n + Q5(q_o) (1/r_n - 1/r_o)
+            // f_n - f_o = [Q5(q_n) - Q5(q_o)] / r_n - Q5(q_o) dr / (r_n r_o)
             const float dr = dR2 / (r_n + r_o);
             const float qo = r_o * d.rc1i, qn = r_n * d.rc1i, dq = dr * d.rc1i;
             const float mo = qo - 1.0f, mn = qn - 1.0f;
             const float Po = fmaf(fmaf(d.A5, qo, d.B5), qo, -1.0f);
             const float Pn = fmaf(fmaf(d.A5, qn, d.B5), qn, -1.0f);
-            const float dcube = dq * fmaf(mn, mn + mo, mo * mo);      // (q_n-1)^3 - (q_o-1)^3
-            const float dP = dq * fmaf(d.A5, qn + qo, d.B5);          // P(q_n) - P(q_o)
+            const float dcube = dq * fmaf(mn, mn + mo, mo * mo);   // (q_n-1)^3 - (q_o-1)^3
+            const float dP = dq * fmaf(d.A5, qn + qo, d.B5);       // P(q_n) - P(q_o)
             const float dQ = fmaf(dcube, Pn, mo * mo * mo * dP);
-            const float Qo = mo * mo * mo * Po;
-            acc += A * (dQ / r_n - Qo * dr / (r_n * r_o));
+            acc += A * (dQ / r_n - mo * mo * mo * Po * dr / (r_n * r_o));
         } else if (io) {
-            acc -= A * coul_f(r_o, d);
+            acc -= A * coul_f(r_o, d.rc1i, d.A5, d.B5);
         } else if (in_) {
-            acc += A * coul_f(r_n, d);
+            acc += A * coul_f(r_n, d.rc1i, d.A5, d.B5);
         }
     }
-    df out = {acc, 0.0f};
-    if (idip) {
-        // moved dipole i with j's charge: W2 of IonDipole(a = i, b = j)
-        const double qj = d.qtype[tj];
-        const D3 muo = {s.gmu[6 * i + 0], s.gmu[6 * i + 1], s.gmu[6 * i + 2]};
-        const D3 mun = {s.gmu[6 * i + 3], s.gmu[6 * i + 4], s.gmu[6 * i + 5]};
-        const int site = pn.w >> 8;
-        const double mi = d.mus[site];
-        const D3 z = {0, 0, 0};
-        const D3 mo_ = {muo.x * mi, muo.y * mi, muo.z * mi}, mn_ = {mun.x * mi, mun.y * mi, mun.z * mi};
-        const double w = ion_dipole64(0.0, mn_, qj, z, rn, d.lBd) - ion_dipole64(0.0, mo_, qj, z, ro, d.lBd);
-        const float wh = (float)w;
-        out = df_add(out, df{wh, (float)(w - (double)wh)});
+    if (po.w & 0x100) {
+        // W2 of IonDipole(a = i, b = j): -lB q_j (mu_i . r) / r^3
+        const float qj = d.qtype[tj];
+        const float io = rsqrtf(ro2), in_ = rsqrtf(rn2);
+        const float w = dot3f(make_float3(fn.x, fn.y, fn.z), rn) * in_ * in_ * in_ -
+                        dot3f(make_float3(fo.x, fo.y, fo.z), ro) * io * io * io;
+        acc -= d.lB * qj * w;
     }
-    return out;
+    return acc;
 }
 
-// Near pair, kind B: moved site i against dipole k (ion-dipole with i's
-// charge, dipole-dipole when i carries a dipole), FP64.
-__device__ __noinline__ df near_pair_b(int i, int kk, const MolSmem &s, const MolDesc &d, int rank, bool idip,
-                                       int k0) {
-    const int4 po = s.go[i], pn = s.gn[i];
-    const short4 eo = s.geo[i], en = s.gen[i];
-    const int4 pk = s.sdpos[kk];
-    const short4 ek = s.sdext[kk];
-    const D3 ro = diff48(po, eo, pk, ek, d), rn = diff48(pn, en, pk, ek, d);
-    const int ksite = d.dip_site[k0 + kk];
-    const double *mk = d.rep_mu + ((size_t)rank * d.N + ksite) * 3;
-    const D3 uk = {mk[0], mk[1], mk[2]};
-    const double muk = d.mus[ksite];
-    const D3 vk = {uk.x * muk, uk.y * muk, uk.z * muk};
-    const double qi = d.qtype[po.w & 0xFF];
-    const D3 z = {0, 0, 0};
-    double w = ion_dipole64(qi, z, 0.0, vk, rn, d.lBd) - ion_dipole64(qi, z, 0.0, vk, ro, d.lBd);
-    if (idip) {
-        const int site = pn.w >> 8;
-        const double mi = d.mus[site];
-        const D3 uo = {s.gmu[6 * i + 0], s.gmu[6 * i + 1], s.gmu[6 * i + 2]};
-        const D3 un = {s.gmu[6 * i + 3], s.gmu[6 * i + 4], s.gmu[6 * i + 5]};
-        w += dipole_dipole64(un, mi, uk, muk, rn, d) - dipole_dipole64(uo, mi, uk, muk, ro, d);
+// Near pair, kind B: moved site i against dipole k: ion-dipole with i's charge
+// and, when i carries a dipole, dipole-dipole with the reaction field; the
+// cutoff test is exact on the integer squared distance.
+__device__ __noinline__ float near_pair_b(int4 po, int4 pn, float4 fo, float4 fn, int4 pk, float4 vk,
+                                          const MolDesc &d) {
+    const float3 s32 = make_float3(d.s32[0], d.s32[1], d.s32[2]);
+    const float3 ro = diff32(po, pk, s32), rn = diff32(pn, pk, s32);
+    const float ro2 = dot3f(ro, ro), rn2 = dot3f(rn, rn);
+    const float io = rsqrtf(ro2), in_ = rsqrtf(rn2);
+    const float3 v = make_float3(vk.x, vk.y, vk.z);
+    const float qi = d.qtype[po.w & 0xFF];
+    float acc = d.lB * qi * (dot3f(v, rn) * in_ * in_ * in_ - dot3f(v, ro) * io * io * io);
+    if (po.w & 0x100) {
+        auto dd = [&](float4 f, float3 r, float r2, float ri, int4 p) {
+            const int dx = wsub(p.x, pk.x), dy = wsub(p.y, pk.y), dz = wsub(p.z, pk.z);
+            bool inside;
+            if (d.cubic) {
+                // exact: |r|^2 < rc^2 on integers (rc2int = ceil(rc^2) in high-word units)
+                inside = (long long)dx * dx + (long long)dy * dy + (long long)dz * dz < d.rc2int;
+            } else {
+                inside = (double)dx * dx * d.s32sqd[0] + (double)dy * dy * d.s32sqd[1] +
+                             (double)dz * dz * d.s32sqd[2] < d.rcd * d.rcd;
+            }
+            if (!inside) return 0.0f;
+            const float3 u = make_float3(f.x, f.y, f.z);
+            const float r1 = r2 * ri;
+            const float q = r1 * d.rc1i;
+            const float dt = dot3f(u, v);
+            // mu2mu with A = 1, B = rfB q^3: -(3 (u.r)(v.r)/r^2 - u.v + u.v B) / r^3
+            const float T = fmaf(3.0f * dot3f(u, r), dot3f(v, r) * (ri * ri), -dt) + dt * (d.rfB * q * q * q);
+            return -d.lB * T * ri * ri * ri;
+        };
+        acc += dd(fn, rn, rn2, in_, pn) - dd(fo, ro, ro2, io, po);
     }
-    const float wh = (float)w;
-    return df{wh, (float)(w - (double)wh)};
+    return acc;
 }
 
 // ---------------------------------------------------------------- trial setup
-// New coordinates of the moved molecule (FP64 rotation of offsets from the
-// centre, then translation), exactly one thread per site; thread gs does the
-// mass centre. Old data come from this CTA's replica.
-__device__ __forceinline__ void setup_trial(const MolTrial &tr, const MolDesc &d, const MolSmem &s, int rank) {
-    const int tid = threadIdx.x, gs = d.gs, g = tr.g;
+// New coordinates of the moved molecule: FP64 rotation of offsets from the
+// centre, then translation, one lane per site; lane gs does the mass centre.
+// Old data come from this CTA's replica. Called by one warp.
+__device__ __forceinline__ void setup_trial(const MolTrial &tr, const MolDesc &d, const GroupBuf &B, int rank,
+                                            int lane) {
+    const int gs = d.gs, g = tr.g;
     const int64_t *P = d.rep_pos + (size_t)rank * d.N * 3;
     const double *MU = d.rep_mu + (size_t)rank * d.N * 3;
     const int64_t *CM = d.rep_cm + (size_t)rank * d.M * 3;
-    if (tid > gs) return;
+    if (lane > gs) return;
     const bool explicit_ = tr.flags & 4;
-    int64_t c[3];
+    int64_t c[3] = {0, 0, 0};
     if (!explicit_) {
         if (tr.center == 0) {
             for (int a = 0; a < 3; a++) c[a] = CM[3 * g + a];
@@ -404,7 +389,7 @@ __device__ __forceinline__ void setup_trial(const MolTrial &tr, const MolDesc &d
             for (int a = 0; a < 3; a++) Y[a] = (int64_t)((uint64_t)Y[a] + (uint64_t)tr.t[a]);
         for (int a = 0; a < 3; a++) out[a] = Y[a];
     };
-    if (tid == gs) {
+    if (lane == gs) {
         int64_t cn[3];
         if (explicit_) {
             for (int a = 0; a < 3; a++) cn[a] = d.expl_cm ? d.expl_cm[a] : CM[3 * g + a];
@@ -412,141 +397,154 @@ __device__ __forceinline__ void setup_trial(const MolTrial &tr, const MolDesc &d
             const int64_t co[3] = {CM[3 * g], CM[3 * g + 1], CM[3 * g + 2]};
             move_point(co, cn);
         }
-        for (int a = 0; a < 3; a++) s.gcm[a] = cn[a];
+        for (int a = 0; a < 3; a++) B.gcm[a] = cn[a];
         return;
     }
-    const int site = g * gs + tid;
+    const int site = g * gs + lane;
     const int64_t Xo[3] = {P[3 * site], P[3 * site + 1], P[3 * site + 2]};
     int64_t Xn[3];
-    D3 uo = {MU[3 * site], MU[3 * site + 1], MU[3 * site + 2]}, un;
+    const D3 uo = {MU[3 * site], MU[3 * site + 1], MU[3 * site + 2]};
+    D3 un;
     if (explicit_) {
-        for (int a = 0; a < 3; a++) Xn[a] = d.expl_pos[3 * tid + a];
-        un = d.expl_mu ? D3{d.expl_mu[3 * tid], d.expl_mu[3 * tid + 1], d.expl_mu[3 * tid + 2]} : uo;
+        for (int a = 0; a < 3; a++) Xn[a] = d.expl_pos[3 * lane + a];
+        un = d.expl_mu ? D3{d.expl_mu[3 * lane], d.expl_mu[3 * lane + 1], d.expl_mu[3 * lane + 2]} : uo;
     } else {
         move_point(Xo, Xn);
         un = (tr.flags & 1) ? qrot(tr.qw, qv, uo) : uo;  // DipoleParticle::rotate (point.h:672-679)
     }
     const int type = d.pos4[site].w & 0xFF;
-    const int dipflag = d.site_dip[site] >= 0 ? 0x100 : 0;
-    // .w of go/gn: type | dipole flag in bit 8 | site << 8 (site in bits 8..31 of gn)
-    s.go[tid] = make_int4(hi32(Xo[0]), hi32(Xo[1]), hi32(Xo[2]), type | dipflag);
-    s.gn[tid] = make_int4(hi32(Xn[0]), hi32(Xn[1]), hi32(Xn[2]), type | (site << 8));
-    s.geo[tid] = make_short4(ext16d(Xo[0]), ext16d(Xo[1]), ext16d(Xo[2]), 0);
-    s.gen[tid] = make_short4(ext16d(Xn[0]), ext16d(Xn[1]), ext16d(Xn[2]), 0);
-    double *gm = s.gmu + 6 * tid;
-    gm[0] = uo.x; gm[1] = uo.y; gm[2] = uo.z;
-    gm[3] = un.x; gm[4] = un.y; gm[5] = un.z;
-    for (int a = 0; a < 3; a++) s.gX[3 * tid + a] = Xn[a];
+    const bool has_dip = d.site_dip[site] >= 0;
+    const double m = d.mus[site];
+    B.go[lane] = make_int4(hi32(Xo[0]), hi32(Xo[1]), hi32(Xo[2]), type | (has_dip ? 0x100 : 0));
+    B.gn[lane] = make_int4(hi32(Xn[0]), hi32(Xn[1]), hi32(Xn[2]), type | (site << 8));
+    B.gfo[lane] = make_float4((float)(uo.x * m), (float)(uo.y * m), (float)(uo.z * m), (float)m);
+    B.gfn[lane] = make_float4((float)(un.x * m), (float)(un.y * m), (float)(un.z * m), (float)m);
+    B.gmu[3 * lane] = un.x;
+    B.gmu[3 * lane + 1] = un.y;
+    B.gmu[3 * lane + 2] = un.z;
+    for (int a = 0; a < 3; a++) B.gX[3 * lane + a] = Xn[a];
 }
 
 // ---------------------------------------------------------------- energy change
-// This CTA's part of dU for the trial set up in shared memory.
+// Warp-aggregated append of near pairs to the queue; a full queue makes the
+// lanes evaluate their pair in place (returned in `inplace`).
+__device__ __forceinline__ bool enqueue(const MolSmem &s, bool near, uint32_t code) {
+    const unsigned active = __activemask();
+    const unsigned m = __ballot_sync(active, near);
+    if (!m) return false;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(s.qcount, __popc(m));
+    base = __shfl_sync(active, base, leader);
+    if (!near) return false;
+    const int slot = base + __popc(m & ((1u << lane) - 1u));
+    if (slot < kQueueCap) {
+        s.queue[slot] = code;
+        return false;
+    }
+    return true;
+}
+
+// This CTA's part of dU for the trial in buffer B. Pair loops use threads
+// [0, nwork); the queue is drained by all threads.
 template <bool SLICE_SMEM>
-__device__ df mol_partial(const MolDesc &d, const MolSmem &s, int g, int rank, int j0, int ns, int k0, int nd) {
+__device__ float mol_partial_loops(const MolDesc &d, const MolSmem &s, const GroupBuf &B, int g, int j0, int ns,
+                                   int nd, int nwork) {
     const int tid = threadIdx.x, gs = d.gs;
     const int g_lo = g * gs, g_hi = g_lo + gs;
     const float3 sc9 = make_float3(d.sc9[0], d.sc9[1], d.sc9[2]);
     const float3 s32 = make_float3(d.s32[0], d.s32[1], d.s32[2]);
     const float rc2near = d.rc2near, lB = d.lB;
     const int nt = d.nt;
-    const float s2u = d.s2[0], e4u = d.eps4[0];
     const bool uni = d.uniform_lj != 0;
+    const float s2u = d.s2[0], e4u = d.eps4[0];
     float acc = 0.0f;
-    df accd = {0.0f, 0.0f};
-    // loop A: every slice site against every moved site
-    for (int jj = tid; jj < ns; jj += blockDim.x) {
+    if (tid >= nwork) return 0.0f;
+    // loop A: slice sites j (one per thread) against every moved site i;
+    // whole warps iterate together so the queue appends stay warp-wide
+    for (int jb = tid - (tid & 31); jb < ns; jb += nwork) {
+        const int jj = jb + (tid & 31);
         const int j = j0 + jj;
-        if (j >= g_lo && j < g_hi) continue;
-        const int4 pj = SLICE_SMEM ? s.spos[jj] : d.pos4[j];
+        const bool valid = jj < ns && !(j >= g_lo && j < g_hi);
+        const int4 pj = SLICE_SMEM ? s.spos[min(jj, ns - 1)] : d.pos4[j0 + min(jj, ns - 1)];
         const int tj = pj.w & 0xFF;
         const float qj = d.qtype[tj];
+#pragma unroll 2
         for (int i = 0; i < gs; i++) {
-            const int4 po = s.go[i], pn = s.gn[i];
+            const int4 po = B.go[i], pn = B.gn[i];
             const int t = (po.w & 0xFF) * nt + tj;
             const float s2 = uni ? s2u : d.s2[t], e4 = uni ? e4u : d.eps4[t];
             const float r2o = far_r2(po, pj, sc9), r2n = far_r2(pn, pj, sc9);
-            const bool near = (r2o < rc2near) | (r2n < rc2near);
-            const bool idip = (po.w & 0x100) != 0;
-            if (near) {
-                const int slot = atomicAdd(s.qcount, 1);
-                if (slot < kQueueCap) {
-                    s.queue[slot] = ((uint32_t)i << 24) | (uint32_t)jj;
-                } else {
-                    const short4 ej = SLICE_SMEM ? s.sext[jj] : d.pos_ext[j];
-                    accd = df_add(accd, near_pair_a(i, pj, ej, s, d, idip));
-                }
-            } else {
+            const bool near = valid && ((r2o < rc2near) | (r2n < rc2near));
+            if (enqueue(s, near, ((uint32_t)i << 24) | (uint32_t)jj))
+                acc += near_pair_a(po, pn, B.gfo[i], B.gfn[i], pj, d);
+            if (valid && !near) {
                 acc += lj_r2(r2n, s2, e4) - lj_r2(r2o, s2, e4);
-                if (idip && qj != 0.0f) {
-                    // W2 of IonDipole(a = i, b = j): -lB qj mu_i (mu_i . r) / r^3
+                if ((po.w & 0x100) && qj != 0.0f) {
+                    // W2 of IonDipole(a = i, b = j): -lB q_j (mu_i . r) / r^3
                     const float3 ro = diff32(po, pj, s32), rn = diff32(pn, pj, s32);
-                    const float4 fo = make_float4(s.gmu[6 * i], s.gmu[6 * i + 1], s.gmu[6 * i + 2], 0.0f);
-                    const float4 fn = make_float4(s.gmu[6 * i + 3], s.gmu[6 * i + 4], s.gmu[6 * i + 5], 0.0f);
-                    const float ro2 = fmaf(ro.x, ro.x, fmaf(ro.y, ro.y, ro.z * ro.z));
-                    const float rn2 = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rn.z * rn.z));
+                    const float4 fo = B.gfo[i], fn = B.gfn[i];
+                    const float ro2 = dot3f(ro, ro), rn2 = dot3f(rn, rn);
                     const float io = rsqrtf(ro2), in_ = rsqrtf(rn2);
-                    const float wo = fmaf(fo.x, ro.x, fmaf(fo.y, ro.y, fo.z * ro.z)) * io * io * io;
-                    const float wn = fmaf(fn.x, rn.x, fmaf(fn.y, rn.y, fn.z * rn.z)) * in_ * in_ * in_;
-                    const float mi = (float)d.mus[pn.w >> 8];
-                    acc -= lB * qj * mi * (wn - wo);
+                    const float w = dot3f(make_float3(fn.x, fn.y, fn.z), rn) * in_ * in_ * in_ -
+                                    dot3f(make_float3(fo.x, fo.y, fo.z), ro) * io * io * io;
+                    acc -= lB * qj * w;
                 }
             }
         }
     }
-    // loop B: dipoles of this slice against every moved site's charge (and dipole)
-    for (int kk = tid; kk < nd; kk += blockDim.x) {
+    // loop B: (dipole k of this slice, moved site i) items spread over threads
+    const int nitems = nd * gs;
+    for (int eb = tid - (tid & 31); eb < nitems; eb += nwork) {
+        const int e = eb + (tid & 31);
+        const int kk = min(e, nitems - 1) / gs, i = min(e, nitems - 1) - kk * gs;
         const int4 pk = s.sdpos[kk];
         const int ksite = pk.w >> 8;
-        if (ksite >= g_lo && ksite < g_hi) continue;
-        const float4 vk = s.sdip[kk];
-        for (int i = 0; i < gs; i++) {
-            const int4 po = s.go[i], pn = s.gn[i];
-            const float3 ro = diff32(po, pk, s32), rn = diff32(pn, pk, s32);
-            const float ro2 = fmaf(ro.x, ro.x, fmaf(ro.y, ro.y, ro.z * ro.z));
-            const float rn2 = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rn.z * rn.z));
-            const bool near = (ro2 < rc2near) | (rn2 < rc2near);
-            if (near) {
-                const int slot = atomicAdd(s.qcount, 1);
-                if (slot < kQueueCap) {
-                    s.queue[slot] = 0x800000u | ((uint32_t)i << 24) | (uint32_t)kk;
-                } else {
-                    accd = df_add(accd, near_pair_b(i, kk, s, d, rank, (po.w & 0x100) != 0, k0));
-                }
-            } else {
-                const float qi = d.qtype[po.w & 0xFF];
-                if (qi != 0.0f) {
-                    // W1 of IonDipole(a = i, b = k): lB qi mu_k (mu_k . r) / r^3
-                    const float io = rsqrtf(ro2), in_ = rsqrtf(rn2);
-                    const float wo = fmaf(vk.x, ro.x, fmaf(vk.y, ro.y, vk.z * ro.z)) * io * io * io;
-                    const float wn = fmaf(vk.x, rn.x, fmaf(vk.y, rn.y, vk.z * rn.z)) * in_ * in_ * in_;
-                    acc += lB * qi * (wn - wo);
-                }
-                // dipole-dipole is zero beyond the cutoff
+        const bool valid = e < nitems && !(ksite >= g_lo && ksite < g_hi);
+        const int4 po = B.go[i], pn = B.gn[i];
+        const float3 ro = diff32(po, pk, s32), rn = diff32(pn, pk, s32);
+        const float ro2 = dot3f(ro, ro), rn2 = dot3f(rn, rn);
+        const bool near = valid && ((ro2 < rc2near) | (rn2 < rc2near));
+        if (enqueue(s, near, 0x800000u | ((uint32_t)i << 24) | (uint32_t)kk))
+            acc += near_pair_b(po, pn, B.gfo[i], B.gfn[i], pk, s.sdip[kk], d);
+        if (valid && !near) {
+            const float qi = d.qtype[po.w & 0xFF];
+            if (qi != 0.0f) {
+                // W1 of IonDipole(a = i, b = k): lB q_i (mu_k . r) / r^3 (dipole-dipole is 0 beyond rc)
+                const float4 vk = s.sdip[kk];
+                const float3 v = make_float3(vk.x, vk.y, vk.z);
+                const float io = rsqrtf(ro2), in_ = rsqrtf(rn2);
+                acc += lB * qi * (dot3f(v, rn) * in_ * in_ * in_ - dot3f(v, ro) * io * io * io);
             }
         }
     }
-    __syncthreads();
-    // near queue, densely
+    return acc;
+}
+
+template <bool SLICE_SMEM>
+__device__ float mol_partial_queue(const MolDesc &d, const MolSmem &s, const GroupBuf &B, int j0) {
     const int nq = min(*s.qcount, kQueueCap);
-    for (int e = tid; e < nq; e += blockDim.x) {
+    float acc = 0.0f;
+    for (int e = threadIdx.x; e < nq; e += blockDim.x) {
         const uint32_t q = s.queue[e];
-        const int i = (int)(q >> 24);
-        const bool idip = (s.go[i].w & 0x100) != 0;
+        const int i = (int)((q >> 24) & 0x7F);
+        const int idx = (int)(q & 0x7FFFFF);
         if (q & 0x800000u) {
-            accd = df_add(accd, near_pair_b(i, (int)(q & 0x7FFFFF), s, d, rank, idip, k0));
+            acc += near_pair_b(B.go[i], B.gn[i], B.gfo[i], B.gfn[i], s.sdpos[idx], s.sdip[idx], d);
         } else {
-            const int jj = (int)(q & 0x7FFFFF);
-            const int4 pj = SLICE_SMEM ? s.spos[jj] : d.pos4[j0 + jj];
-            const short4 ej = SLICE_SMEM ? s.sext[jj] : d.pos_ext[j0 + jj];
-            accd = df_add(accd, near_pair_a(i, pj, ej, s, d, idip));
+            const int4 pj = SLICE_SMEM ? s.spos[idx] : d.pos4[j0 + idx];
+            acc += near_pair_a(B.go[i], B.gn[i], B.gfo[i], B.gfn[i], pj, d);
         }
     }
-    return df_add_f(accd, acc);
+    return acc;
 }
 
 // ---------------------------------------------------------------- the sweep
 // One cluster of C CTAs per system (blockIdx.x / C). EVAL: evaluate trial 0
-// only, write its dU to eval_du, decide and commit nothing.
+// only, write its dU to eval_du, decide and commit nothing. The last warp
+// prepares the next trial's coordinates while the others sum pairs; the
+// prepared buffer is discarded when an accepted trial moved the same molecule.
 template <bool SLICE_SMEM, bool CLUSTER, bool EVAL>
 __global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc *__restrict__ descs) {
     extern __shared__ __align__(16) unsigned char mol_smem_raw[];
@@ -554,20 +552,18 @@ __global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc
     const int sys = blockIdx.x / C;
     const int rank = CLUSTER ? (int)cluster_rank() : 0;
     const MolDesc &d = descs[sys];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int nwork = (int)blockDim.x - 32;           // threads on the pair loops
+    const bool setup_warp = tid >= nwork;
     const int ns_full = (d.N + C - 1) / C, nd_full = (d.D + C - 1) / C;
     const int j0 = min(rank * ns_full, d.N), j1 = min(j0 + ns_full, d.N), ns = j1 - j0;
     const int k0 = min(rank * nd_full, d.D), k1 = min(k0 + nd_full, d.D), nd = k1 - k0;
     MolSmem s = mol_carve(mol_smem_raw, ns_full, nd_full, d.gs, SLICE_SMEM);
     if (SLICE_SMEM)
-        for (int jj = tid; jj < ns; jj += blockDim.x) {
-            s.spos[jj] = d.pos4[j0 + jj];
-            s.sext[jj] = d.pos_ext[j0 + jj];
-        }
+        for (int jj = tid; jj < ns; jj += blockDim.x) s.spos[jj] = d.pos4[j0 + jj];
     for (int kk = tid; kk < nd; kk += blockDim.x) {
         s.sdip[kk] = d.dip4[k0 + kk];
         s.sdpos[kk] = d.dip_pos4[k0 + kk];
-        s.sdext[kk] = d.dip_ext[k0 + kk];
     }
     int64_t cursor = EVAL ? 0 : d.sc->cursor;
     const int64_t n = EVAL ? 1 : d.sc->n_trials;
@@ -579,18 +575,32 @@ __global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc
         s.part[0] = s.part[1] = make_float2(0.0f, 0.0f);
         s.flag[0] = s.flag[1] = 0;
     }
+    if (cursor < n && setup_warp) setup_trial(d.trials[cursor], d, s.buf[cursor & 1], rank, lane);
     if (CLUSTER) cluster_barrier();
     else __syncthreads();
     for (; cursor < n; cursor++) {
+        const int b = (int)(cursor & 1);
         const MolTrial tr = d.trials[cursor];
+        if (s.flag[1]) {   // the prepared buffer is stale (same molecule, accepted)
+            __syncthreads();
+            if (setup_warp) setup_trial(tr, d, s.buf[b], rank, lane);
+            if (tid == 0) s.flag[1] = 0;
+        }
         if (tid == 0) *s.qcount = 0;
-        setup_trial(tr, d, s, rank);
         __syncthreads();
-        df part = mol_partial<SLICE_SMEM>(d, s, tr.g, rank, j0, ns, k0, nd);
-        part = warp_sum_df(part);
-        if ((tid & 31) == 0) s.red[tid >> 5] = make_float2(part.hi, part.lo);
+        float part;
+        if (!setup_warp) {
+            part = mol_partial_loops<SLICE_SMEM>(d, s, s.buf[b], tr.g, j0, ns, nd, nwork);
+        } else {
+            part = 0.0f;
+            if (!EVAL && cursor + 1 < n) setup_trial(d.trials[cursor + 1], d, s.buf[b ^ 1], rank, lane);
+        }
         __syncthreads();
-        const int slot = (int)(cursor & 1);
+        part += mol_partial_queue<SLICE_SMEM>(d, s, s.buf[b], j0);
+        df pd = warp_sum_df(df{part, 0.0f});
+        if (lane == 0) s.red[tid >> 5] = make_float2(pd.hi, pd.lo);
+        __syncthreads();
+        const int slot = b;
         if (tid < 32) {
             df v = {0.0f, 0.0f};
             if (tid < (int)(blockDim.x >> 5)) v = df{s.red[tid].x, s.red[tid].y};
@@ -614,7 +624,7 @@ __global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc
                 else dec = df_gt(v, df{tr.thr_hi, tr.thr_lo}) ? 0 : 1;
                 s.flag[0] = dec;
                 s.red[0] = make_float2(v.hi, v.lo);
-                if (*s.qcount > kQueueCap) s.flag[1]++;   // overflowed pairs were evaluated in place
+                if (dec == 1 && cursor + 1 < n && d.trials[cursor + 1].g == tr.g) s.flag[1] = 1;
             }
         }
         __syncthreads();
@@ -637,36 +647,28 @@ __global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc
             usum = df_add(usum, du);
             utot = df_add(utot, du);
             const int gs = d.gs, g = tr.g;
+            const GroupBuf &B = s.buf[b];
             if (tid < gs) {
                 const int site = g * gs + tid;
                 int64_t *P = d.rep_pos + ((size_t)rank * d.N + site) * 3;
                 double *MU = d.rep_mu + ((size_t)rank * d.N + site) * 3;
                 for (int a = 0; a < 3; a++) {
-                    P[a] = s.gX[3 * tid + a];
-                    MU[a] = s.gmu[6 * tid + 3 + a];
+                    P[a] = B.gX[3 * tid + a];
+                    MU[a] = B.gmu[3 * tid + a];
                 }
-                const int4 pn = make_int4(s.gn[tid].x, s.gn[tid].y, s.gn[tid].z, s.go[tid].w & 0xFF);
-                const short4 en = s.gen[tid];
+                const int4 pn = make_int4(B.gn[tid].x, B.gn[tid].y, B.gn[tid].z, B.go[tid].w & 0xFF);
                 if (site >= j0 && site < j1) {
-                    if (SLICE_SMEM) {
-                        s.spos[site - j0] = pn;
-                        s.sext[site - j0] = en;
-                    } else {
-                        d.pos4[site] = pn;
-                        d.pos_ext[site] = en;
-                    }
+                    if (SLICE_SMEM) s.spos[site - j0] = pn;
+                    else d.pos4[site] = pn;
                 }
                 const int k = d.site_dip[site];
                 if (k >= k0 && k < k1) {
-                    const double m = d.mus[site];
                     s.sdpos[k - k0] = make_int4(pn.x, pn.y, pn.z, (site << 8) | (pn.w & 0xFF));
-                    s.sdext[k - k0] = en;
-                    s.sdip[k - k0] = make_float4((float)(s.gmu[6 * tid + 3] * m), (float)(s.gmu[6 * tid + 4] * m),
-                                                 (float)(s.gmu[6 * tid + 5] * m), (float)m);
+                    s.sdip[k - k0] = B.gfn[tid];
                 }
             } else if (tid == gs) {
                 int64_t *CM = d.rep_cm + ((size_t)rank * d.M + g) * 3;
-                for (int a = 0; a < 3; a++) CM[a] = s.gcm[a];
+                for (int a = 0; a < 3; a++) CM[a] = B.gcm[a];
             }
         }
         __syncthreads();
@@ -674,14 +676,10 @@ __global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc
     // write the slices back (each CTA its own range) and the scalars
     if (!EVAL) {
         if (SLICE_SMEM)
-            for (int jj = tid; jj < ns; jj += blockDim.x) {
-                d.pos4[j0 + jj] = s.spos[jj];
-                d.pos_ext[j0 + jj] = s.sext[jj];
-            }
+            for (int jj = tid; jj < ns; jj += blockDim.x) d.pos4[j0 + jj] = s.spos[jj];
         for (int kk = tid; kk < nd; kk += blockDim.x) {
             d.dip4[k0 + kk] = s.sdip[kk];
             d.dip_pos4[k0 + kk] = s.sdpos[kk];
-            d.dip_ext[k0 + kk] = s.sdext[kk];
         }
         if (rank == 0 && tid == 0) {
             MolScalars *sc = d.sc;
@@ -718,21 +716,40 @@ __global__ void mol_commit_kernel(const MolDesc *__restrict__ descs, int g, int 
         }
         const int type = d.pos4[site].w & 0xFF;
         const int4 p4 = make_int4(hi32(X[0]), hi32(X[1]), hi32(X[2]), type);
-        const short4 e4 = make_short4(ext16d(X[0]), ext16d(X[1]), ext16d(X[2]), 0);
         d.pos4[site] = p4;
-        d.pos_ext[site] = e4;
         const int k = d.site_dip[site];
         if (k >= 0) {
             const double m = d.mus[site];
             const double *u = d.rep_mu + (size_t)site * 3;
             d.dip_pos4[k] = make_int4(p4.x, p4.y, p4.z, (site << 8) | type);
-            d.dip_ext[k] = e4;
             d.dip4[k] = make_float4((float)(u[0] * m), (float)(u[1] * m), (float)(u[2] * m), (float)m);
         }
     } else if (tid == gs && d.expl_cm) {
         for (int r = 0; r < nrep; r++)
             for (int a = 0; a < 3; a++) d.rep_cm[((size_t)r * d.M + g) * 3 + a] = d.expl_cm[a];
     }
+}
+
+// IonDipole (q2mu, multipole.h:269-277) in FP64 with r = r_a - r_b:
+// lB [qa mub (mub.r) - qb mua (mua.r)] / r^3, mu vectors already scaled.
+__device__ __forceinline__ double ion_dipole64(double qa, const D3 &mua, double qb, const D3 &mub, const D3 &r,
+                                               double lB) {
+    const double r2i = 1.0 / dot3(r, r);
+    const double r3i = sqrt(r2i) * r2i;
+    return lB * (qa * dot3(mub, r) * r3i - qb * dot3(mua, r) * r3i);
+}
+// DipoleDipoleGalore with the reaction field (multipole.h:287-299, 767-782, 910-920).
+__device__ __forceinline__ double dipole_dipole64(const D3 &ua, double ma, const D3 &ub, double mb, const D3 &r,
+                                                  const MolDesc &d) {
+    const double r2 = dot3(r, r);
+    const double r1 = sqrt(r2);
+    if (!(r1 < d.rcd)) return 0.0;
+    const double q = r1 / d.rcd;
+    const double bf = d.rfBd * q * q * q;
+    const double r2i = 1.0 / r2;
+    const double dt = dot3(ua, ub);
+    const double T = (3.0 * dot3(ua, r) * dot3(ub, r) * r2i - dt) + dt * bf;
+    return d.lBd * (-(ma * mb) * T * sqrt(r2i) * r2i);
 }
 
 // Total energy in FP64, as Energybase::systemEnergy sums it (energy.h:169-180):
@@ -821,7 +838,6 @@ struct fg_molsys {
     int64_t *rep_pos = nullptr, *rep_cm = nullptr;
     double *rep_mu = nullptr, *mus = nullptr;
     int4 *pos4 = nullptr, *dip_pos4 = nullptr;
-    short4 *pos_ext = nullptr, *dip_ext = nullptr;
     int32_t *site_dip = nullptr, *dip_site = nullptr;
     float4 *dip4 = nullptr;
     fgm::MolTrial *trials = nullptr;
@@ -859,8 +875,8 @@ int mol_dmalloc(fg_molsys *h, void **p, size_t bytes) {
     } while (0)
 
 void mol_free(fg_molsys *h) {
-    void *ptrs[] = {h->d_desc, h->rep_pos, h->rep_cm, h->rep_mu, h->mus, h->pos4, h->dip_pos4, h->pos_ext,
-                    h->dip_ext, h->site_dip, h->dip_site, h->dip4, h->trials, h->log_du, h->log_acc, h->sc,
+    void *ptrs[] = {h->d_desc, h->rep_pos, h->rep_cm, h->rep_mu, h->mus, h->pos4, h->dip_pos4,
+                    h->site_dip, h->dip_site, h->dip4, h->trials, h->log_du, h->log_acc, h->sc,
                     h->expl_pos, h->expl_mu, h->eval_du, h->tot, h->expl_cm};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -883,7 +899,7 @@ void mol_mass_center(const int64_t *X, int front, int gs, int64_t out[3]) {
 size_t mol_smem_bytes(const fg_molsys *h, int C, bool slice_smem) {
     size_t off[16];
     fgm::mol_smem_layout((h->N + C - 1) / C, (h->D + C - 1) / C, h->gs, slice_smem, off);
-    return off[11];
+    return off[6];
 }
 
 struct MolLaunch {
@@ -1116,7 +1132,7 @@ int fg_mol_create(const fg_params *params, int32_t n_sites, int32_t sites_per_mo
     for (int a = 0; a < 3; a++) {
         d.s32[a] = (float)(P.box[a] / 4294967296.0);
         d.sc9[a] = (float)(512.0 * P.box[a] / 4294967296.0);
-        d.s48d[a] = P.box[a] / 281474976710656.0;
+        d.s32sqd[a] = (P.box[a] / 4294967296.0) * (P.box[a] / 4294967296.0);
         d.s64d[a] = P.box[a] / TWO64;
         d.inv64d[a] = TWO64 / P.box[a];
     }
@@ -1131,6 +1147,13 @@ int fg_mol_create(const fg_params *params, int32_t n_sites, int32_t sites_per_mo
     d.A5 = (float)(5.0 / 22.0 * a2 - 0.6);
     d.B5 = (float)(9.0 / 22.0 * a2 - 1.2);
     d.rfBd = -(2 * (P.rf_eps_rf - P.rf_eps_r) / (2 * P.rf_eps_rf + P.rf_eps_r)) / P.rf_eps_r;
+    d.rfB = (float)d.rfBd;
+    d.cubic = (P.box[0] == P.box[1] && P.box[1] == P.box[2]) ? 1 : 0;
+    d.s32sq = (float)((P.box[0] / 4294967296.0) * (P.box[0] / 4294967296.0));
+    {
+        const double u = rc / (P.box[0] / 4294967296.0);   // rc in high-word units
+        d.rc2int = (long long)std::ceil(u * u);
+    }
     d.kT = (float)(P.kT_scale > 0 ? P.kT_scale : 1.0);
     const int nt = P.n_types;
     for (int i = 0; i < nt; i++) {
@@ -1158,7 +1181,6 @@ int fg_mol_create(const fg_params *params, int32_t n_sites, int32_t sites_per_mo
     TRY(mol_dmalloc(h, (void **)&h->d_desc, sizeof(fgm::MolDesc)));
     TRY(mol_dmalloc(h, (void **)&h->mus, (size_t)h->N * sizeof(double)));
     TRY(mol_dmalloc(h, (void **)&h->pos4, (size_t)h->N * sizeof(int4)));
-    TRY(mol_dmalloc(h, (void **)&h->pos_ext, (size_t)h->N * sizeof(short4)));
     TRY(mol_dmalloc(h, (void **)&h->site_dip, (size_t)h->N * sizeof(int32_t)));
     TRY(mol_dmalloc(h, (void **)&h->sc, sizeof(fgm::MolScalars)));
     TRY(mol_dmalloc(h, (void **)&h->expl_pos, (size_t)h->gs * 3 * sizeof(int64_t)));
@@ -1168,7 +1190,6 @@ int fg_mol_create(const fg_params *params, int32_t n_sites, int32_t sites_per_mo
     TRY(mol_dmalloc(h, (void **)&h->tot, 2 * sizeof(double)));
     d.mus = h->mus;
     d.pos4 = h->pos4;
-    d.pos_ext = h->pos_ext;
     d.site_dip = h->site_dip;
     d.sc = h->sc;
     d.eval_du = h->eval_du;
@@ -1201,7 +1222,6 @@ int fg_mol_set_state(fg_molsys *h, const double *xyz, const double *mu_unit, con
     std::vector<int64_t> X(3 * (size_t)N), CM(3 * (size_t)h->M);
     std::vector<double> MU(3 * (size_t)N, 0.0);
     std::vector<int4> p4(N);
-    std::vector<short4> e4(N);
     std::vector<int32_t> sd(N, -1), ds;
     h->types.assign(type_ids, type_ids + N);
     h->mus_h.assign(N, 0.0);
@@ -1222,7 +1242,6 @@ int fg_mol_set_state(fg_molsys *h, const double *xyz, const double *mu_unit, con
         }
         h->mus_h[i] = m;
         p4[i] = make_int4(hi32h(X[3 * i]), hi32h(X[3 * i + 1]), hi32h(X[3 * i + 2]), type_ids[i]);
-        e4[i] = make_short4(ext16h(X[3 * i]), ext16h(X[3 * i + 1]), ext16h(X[3 * i + 2]), 0);
     }
     for (int g = 0; g < h->M; g++) {
         if (mass_centers)
@@ -1234,33 +1253,27 @@ int fg_mol_set_state(fg_molsys *h, const double *xyz, const double *mu_unit, con
     if (D != h->D || !h->dip4) {
         if (h->dip4) cudaFree(h->dip4);
         if (h->dip_pos4) cudaFree(h->dip_pos4);
-        if (h->dip_ext) cudaFree(h->dip_ext);
         if (h->dip_site) cudaFree(h->dip_site);
         h->dip4 = nullptr;
         h->dip_pos4 = nullptr;
-        h->dip_ext = nullptr;
         h->dip_site = nullptr;
         MOL_DMALLOC(h->dip4, (size_t)std::max(D, 1) * sizeof(float4));
         MOL_DMALLOC(h->dip_pos4, (size_t)std::max(D, 1) * sizeof(int4));
-        MOL_DMALLOC(h->dip_ext, (size_t)std::max(D, 1) * sizeof(short4));
         MOL_DMALLOC(h->dip_site, (size_t)std::max(D, 1) * sizeof(int32_t));
         h->D = D;
     }
     std::vector<float4> d4(std::max(D, 1));
     std::vector<int4> dp4(std::max(D, 1));
-    std::vector<short4> de4(std::max(D, 1));
     for (int k = 0; k < D; k++) {
         const int i = ds[k];
         const double m = h->mus_h[i];
         d4[k] = make_float4((float)(MU[3 * i] * m), (float)(MU[3 * i + 1] * m), (float)(MU[3 * i + 2] * m), (float)m);
         dp4[k] = make_int4(p4[i].x, p4[i].y, p4[i].z, (i << 8) | type_ids[i]);
-        de4[k] = e4[i];
     }
     fgm::MolDesc &d = h->desc;
     d.D = D;
     d.dip4 = h->dip4;
     d.dip_pos4 = h->dip_pos4;
-    d.dip_ext = h->dip_ext;
     d.dip_site = h->dip_site;
     cudaStream_t st = h->stream;
     for (int r = 0; r < h->C; r++) {
@@ -1270,11 +1283,9 @@ int fg_mol_set_state(fg_molsys *h, const double *xyz, const double *mu_unit, con
     }
     CK(cudaMemcpyAsync(h->mus, h->mus_h.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->pos4, p4.data(), (size_t)N * sizeof(int4), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(h->pos_ext, e4.data(), (size_t)N * sizeof(short4), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->site_dip, sd.data(), (size_t)N * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->dip4, d4.data(), (size_t)std::max(D, 1) * sizeof(float4), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->dip_pos4, dp4.data(), (size_t)std::max(D, 1) * sizeof(int4), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(h->dip_ext, de4.data(), (size_t)std::max(D, 1) * sizeof(short4), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(h->dip_site, ds.empty() ? sd.data() : ds.data(), (size_t)std::max(D, 1) * 4,
                        cudaMemcpyHostToDevice, st));
     int rc = mol_push_desc(h);

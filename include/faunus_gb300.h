@@ -227,7 +227,7 @@ int fg_pair_energy_noalloc(const fg_params *params, int32_t n, const double *d_x
  * CTAs (fg_mol_set_cluster). */
 typedef struct fg_molsys fg_molsys;
 
-/* Create a system of n_sites sites in molecules of sites_per_molecule (<= 32)
+/* Create a system of n_sites sites in molecules of sites_per_molecule (<= 31)
  * consecutive sites. Replaces: Space(json) with a molecular "moleculelist"
  * entry + NonbondedVector<Tspace, CombinedPairPotential<...>>(json)
  * (energy.h:1062-1090, multipole.h:600-640, 836-870, 983-990). */

@@ -69,8 +69,10 @@ def test_mol_cluster_sizes_agree():
     n = len(g["group"])
     res = []
     p, s = golden_system(g)
+    cmax = s.max_cluster
+    s.close()
     for c in [1, 2, 4, 8]:
-        if c > s.max_cluster:
+        if c > cmax:
             continue
         p, s = golden_system(g, cluster=c)
         assert s.cluster == c
