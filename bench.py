@@ -9,6 +9,14 @@ this path). One "step" = one sweep (16384 AtomicTranslation trials) of every
 system.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload rpm16k|rpm800|pt64|molecules|serving]
+
+The default workload is the batched 16384-ion Ewald one below; the others
+measure the remaining configurations of the path the same way (one JSON line
+each): rpm800 = 800-ion Ewald systems (L = 60, |n|^2 <= 49), pt64 = 64-replica
+Debye-Hueckel + LJ parallel tempering, molecules = 1000 rigid 20-site dipolar
+molecules per system (TranslateRotate), serving = Poisson job stream through
+the continuous-batching server with p50/p99 job latency.
 
 value         batched: B independent systems (default B = number of SMs, one
               persistent CTA per system) advanced by the batched sweep; each
@@ -33,6 +41,7 @@ cpu_baseline  the FP64 oracle port of the reference's per-trial work, one
               reference arm).
 """
 import argparse
+import math
 import concurrent.futures as cf
 import json
 import multiprocessing as mp
@@ -146,42 +155,68 @@ def make_positions(seeds):
 _cpu_cache = {}
 
 
-def _cpu_task(args):
-    """Time-bounded sample of the oracle port on one core: trials in chunks of
-    64 until ``seconds`` have passed. The system is built once per process."""
-    seed, seconds = args
+def _cpu_system(kind, seed):
+    """One FP64 oracle system of the given workload kind (built once per process)."""
     import numpy as np
     from beofaunus_gb300 import workloads
-    from oracle.oracle import OracleSystem, translation_stream
-    if seed not in _cpu_cache:
+    from oracle.oracle import OracleMol, OracleSystem
+    if kind == "molecules":
+        p, xyz, mu, mus, ids = workloads.dipolar_molecules(1000, seed=seed)
+        return OracleMol(p, xyz, mu, mus, ids, 20), None
+    if kind == "rpm16k":
         p, xyz, q, ids = workloads.rpm16k(seed=seed, update_frequency=1000, start="scatter")
-        _cpu_cache[seed] = (OracleSystem(p, xyz, q, ids), np.array([p.type_dp[i] for i in ids]), [0])
-    o, dpp, chunk = _cpu_cache[seed]
+    elif kind == "rpm800":
+        p, xyz, q, ids = workloads.rpm800(seed=seed, update_frequency=1000)
+    elif kind.startswith("dhlj"):
+        n, kT = kind[4:].split("@") if "@" in kind else (kind[4:], "1.0")
+        p, xyz, q, ids = workloads.dh_lj_salt(int(n), seed, kT_scale=float(kT), start="scatter")
+    else:
+        raise ValueError(kind)
+    return OracleSystem(p, xyz, q, ids), np.array([p.type_dp[i] for i in ids])
+
+
+def _cpu_task(args):
+    """Time-bounded sample of the oracle port on one core: chunks of trials
+    until ``seconds`` of trial time have passed. Returns (trials, seconds)."""
+    kind, seed, seconds = args
+    from oracle.oracle import mol_stream, translation_stream
+    key = (kind, seed)
+    if key not in _cpu_cache:
+        _cpu_cache[key] = _cpu_system(kind, seed) + ([0],)
+    o, dpp, chunk = _cpu_cache[key]
     n, t_run = 0, 0.0
     while t_run < seconds:
-        idx, disp, u = translation_stream(seed * 100000 + chunk[0], dpp, 64)
-        chunk[0] += 1
-        t0 = time.perf_counter()
-        o.mc_run_stream(idx, disp, u)
+        if kind == "molecules":
+            st = mol_stream(seed * 100000 + chunk[0], 1000, 1.0, 0.3, True, 4)
+            t0 = time.perf_counter()
+            o.run_stream(st)
+            k = 4
+        else:
+            k = 64 if kind == "rpm16k" else 256
+            idx, disp, u = translation_stream(seed * 100000 + chunk[0], dpp, k)
+            t0 = time.perf_counter()
+            o.mc_run_stream(idx, disp, u)
         t_run += time.perf_counter() - t0
-        n += 64
+        chunk[0] += 1
+        n += k
     return n, t_run
 
 
 class CpuPath:
-    """The FP64 oracle port of the reference's per-trial work (all-pairs
-    EwaldReal + WCA, 2K complex exponentials, self and surface sums, Q(k)
-    rebuild every 1000 accepted) on every host core: one process per core,
-    each its own system and seed, as independent reference runs would be."""
+    """The FP64 oracle port of the reference's per-trial work on every host
+    core: one process per core, each its own system and seed, as independent
+    reference runs would be. ``kinds`` gives each process its workload kind
+    (cycled)."""
 
-    def __init__(self, cores=None):
+    def __init__(self, kinds, cores=None):
         from oracle import oracle
         oracle.build()
         self.cores = cores or os.cpu_count() or 1
+        self.kinds = [kinds[c % len(kinds)] for c in range(self.cores)]
         self.pool = mp.get_context("spawn").Pool(self.cores)
 
     def sample(self, seconds):
-        res = self.pool.map(_cpu_task, [(1000 + c, seconds) for c in range(self.cores)], chunksize=1)
+        res = self.pool.map(_cpu_task, [(k, 1000 + c, seconds) for c, k in enumerate(self.kinds)], chunksize=1)
         rate = sum(n / t for n, t in res)
         trials = sum(n for n, _ in res)
         return rate, trials
@@ -191,14 +226,16 @@ class CpuPath:
         self.pool.join()
 
     def describe(self, seconds, trials):
-        return ("%d processes (one per host core), each its own 16384-ion Ewald system, ~%.0f s of FP64 "
-                "trials (%d in total); value = sum of per-process trial rates" % (self.cores, seconds, trials))
+        ks = sorted(set(self.kinds))
+        return ("%d processes (one per host core), each its own system (%s), ~%.0f s of FP64 trials (%d in total); "
+                "value = sum of per-process trial rates" % (self.cores, ", ".join(ks[:6]) + (" ..." if len(ks) > 6 else ""),
+                                                             seconds, trials))
 
 
-def cpu_baseline(seconds):
-    cp = CpuPath()
+def cpu_baseline(seconds, kinds=("rpm16k",)):
+    cp = CpuPath(list(kinds))
     try:
-        cp.sample(0.5)                      # build each process's system outside the sample
+        cp.sample(0.2)                      # build each process's system outside the sample
         rate, trials = cp.sample(seconds)
     finally:
         cp.close()
@@ -426,13 +463,409 @@ def run_ours(args, rank, world):
         print(json.dumps(out))
 
 
+def _pt_sizes():
+    from beofaunus_gb300 import workloads
+    return [int(n) for n in workloads.pt_ladder_sizes(64)]
+
+
+def _serving_sizes(n_jobs, seed=5):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(math.log(256), math.log(16384), n_jobs))
+    return [int(2 * round(x / 2)) for x in n], list(rng.uniform(0.8, 2.0, n_jobs))
+
+
+def cpu_kinds(workload):
+    if workload == "rpm16k":
+        return ["rpm16k"]
+    if workload == "rpm800":
+        return ["rpm800"]
+    if workload == "molecules":
+        return ["molecules"]
+    if workload == "pt64":
+        return ["dhlj%d" % n for n in _pt_sizes()]
+    if workload == "serving":
+        sizes, temps = _serving_sizes(64)
+        return ["dhlj%d@%.3f" % (n, t) for n, t in zip(sizes, temps)]
+    raise ValueError(workload)
+
+
+WORKLOAD_NAMES = {"rpm16k": WORKLOAD, "rpm800": "rpm800_ewald_wca_batched", "pt64": "pt64_dh_lj_ladder",
+                  "molecules": "dipolar_molecules_1000x20_batched", "serving": "serving_dh_lj_poisson"}
+
+
+def base_line(metric_value, steps, warm, ms_per_step, world, config, dtype, data):
+    return {"metric": METRIC, "value": metric_value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warm,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": dtype, "data": data, "config": config}
+
+
+def gpu_setup(args):
+    import torch
+    from beofaunus_gb300 import build
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    return torch, dev, local, torch.cuda.get_device_properties(dev).multi_processor_count
+
+
+# ----------------------------------------------------------------- 800-ion Ewald
+def run_rpm800(args, rank, world):
+    import numpy as np
+    from beofaunus_gb300 import workloads
+    from beofaunus_gb300.gpu import Batch, System
+    torch, dev, local, sms = gpu_setup(args)
+    B = args.systems or sms
+    T = args.trials or 800
+    steps, warm = args.steps, args.warmup
+    systems = []
+    for b in range(B):
+        p, xyz, q, ids = workloads.rpm_ewald(800, 60.0, 7, seed=1 + rank * 1000003 + b, update_frequency=1000,
+                                             start="scatter")
+        systems.append(System(p, xyz, q, ids))
+    batch = Batch(systems)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def step(seed):
+        batch.stream_philox([T] * B, seed)
+        flush.fill_(seed & 0xFF)
+        torch.cuda.synchronize()
+        return batch.run()[1]
+
+    for s_ in range(warm):
+        step(10 + s_)
+    clocks = ClockSampler(local)
+    clocks.start()
+    stats = [step(1000 + s_) for s_ in range(steps)]
+    clk = clocks.stop()
+    ms = sum(st["device_ms"] for st in stats)
+    trials = sum(st["trials"] for st in stats)
+    value = trials / (ms / 1e3)
+    # e2e: host mt19937 streams in, scalars out
+    e2e_s, e2e_t = 0.0, 0
+    for s_ in range(steps):
+        host = [systems[b].draw_translation_stream(7000 + 100 * s_ + b, T) for b in range(B)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b in range(B):
+            batch.stream_upload(b, *host[b])
+        _, tot = batch.run()
+        e2e_s += time.perf_counter() - t0
+        e2e_t += tot["trials"]
+    one = systems[0]
+    one.stream_philox(4 * T, 5)
+    r1 = one.stream_run()
+    single = r1["trials"] / (r1["device_ms"] / 1e3)
+    idx, disp, u = one.draw_translation_stream(777, 300)
+    pos = one.positions()
+    t0 = time.perf_counter()
+    for t in range(300):
+        i = int(idx[t])
+        new = pos[i] + disp[t]
+        new -= 60.0 * np.round(new / 60.0)
+        du = one.trial_du(i, new)
+        acc = not (u[t] > np.exp(-du))
+        one.commit(acc)
+        if acc:
+            pos[i] = new
+    plain = 300 / (time.perf_counter() - t0)
+    cfg = {"workload": WORKLOAD_NAMES["rpm800"], "systems": B, "n_particles_per_system": 800, "box_A": 60.0,
+           "ewald": {"alpha": 0.2, "cutoff_A": 20.0, "kvectors": systems[0].num_kvectors, "n2_max": 49,
+                     "update_frequency": 1000}, "trials_per_system_per_step": T,
+           "l2": "L2 flushed (256 MiB write) between timed steps"}
+    out = base_line(value, steps, warm, ms / steps, world, cfg, "f32 pair and k terms; df sums; int64 Q(k)",
+                    "synthetic (seeded overlap-free starts)")
+    out.update({"e2e": {"value": e2e_t / e2e_s, "unit": UNIT, "h2d_bytes_per_step": B * T * 40,
+                        "d2h_bytes_per_step": B * SYS_SCALARS_BYTES * 2},
+                "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
+                "single_chain": {"value": single, "unit": UNIT}, "plain_per_trial_api": {"value": plain, "unit": UNIT},
+                "batched_over_plain": value / plain, "clocks": clk})
+    batch.close()
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("rpm800"))
+    if rank == 0:
+        print(json.dumps(out))
+
+
+# ----------------------------------------------------------------- parallel tempering
+def run_pt(args, rank, world):
+    from beofaunus_gb300 import workloads
+    from beofaunus_gb300.gpu import Batch, System
+    torch, dev, local, sms = gpu_setup(args)
+    sizes = _pt_sizes()
+    temps = workloads.pt_temperatures(64)
+    sweeps = args.pt_sweeps
+    systems = []
+    for r, n in enumerate(sizes):
+        p, xyz, q, ids = workloads.dh_lj_salt(n, 100 + r + rank * 1000003, start="scatter")
+        systems.append(System(p, xyz, q, ids))
+    batch = Batch(systems)
+    batch.pt_setup(temps, 1234 + rank)
+    steps, warm = args.steps, args.warmup
+    for _ in range(warm):
+        batch.pt_run(1, sweeps)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stats = [batch.pt_run(1, sweeps) for _ in range(steps)]
+    clk = clocks.stop()
+    ms = sum(st["device_ms"] for st in stats)
+    trials = sum(st["trials"] for st in stats)
+    value = trials / (ms / 1e3)
+    state = batch.pt_state()
+    acc_swaps = [int(a) for a in state["accepts"][:63]]
+    att_swaps = [int(a) for a in state["attempts"][:63]]
+    # largest replica alone: the bound of one fused launch over uneven sizes
+    big = int(max(range(64), key=lambda r: sizes[r]))
+    cfg = {"workload": WORKLOAD_NAMES["pt64"], "replicas": 64, "n_min": min(sizes), "n_max": max(sizes),
+           "n_total": sum(sizes), "density_per_A3": 0.002, "debye_length_A": 10.0, "lj_sigma_A": 4.0,
+           "lj_eps_kT": 0.2, "temperatures": [0.8, 2.0], "sweeps_per_swap": sweeps,
+           "launch": "one graph per round: Philox draws, persistent sweep over all replicas, swap kernel"}
+    out = base_line(value, steps, warm, ms / steps, world, cfg, "f32 pair terms; df sums",
+                    "synthetic (seeded overlap-free starts, Philox streams)")
+    out.update({"gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
+                "swap_acceptance": sum(acc_swaps) / max(sum(att_swaps), 1),
+                "largest_replica": sizes[big], "clocks": clk,
+                "e2e": None})
+    # e2e: the same rounds driven through the host stream path are the batch
+    # e2e of the other workloads; for PT every input is generated on the
+    # device, so the end-to-end line is the round plus the state read-back.
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        batch.pt_run(1, sweeps)
+        batch.pt_state()
+    e2e_s = time.perf_counter() - t0
+    out["e2e"] = {"value": trials / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+                  "d2h_bytes_per_step": 64 * (4 + 8 + 8 + 8)}
+    batch.close()
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("pt64"))
+    if rank == 0:
+        print(json.dumps(out))
+
+
+# ----------------------------------------------------------------- rigid dipolar molecules
+def _mol_system(seed):
+    from beofaunus_gb300 import workloads
+    return workloads.dipolar_molecules(1000, seed=seed)
+
+
+# Cost model of one molecule trial (algorithmic FP32 work, FMA = 2 FLOP), per
+# position (old and new) of each of the 20 moved sites:
+#   LJ against every other site (no cutoff in LennardJonesLB): distance,
+#     r^2, 1/r^2, (s/r)^6, 4eps(x^2 - x): 15 FLOP;
+#   ion-dipole (no cutoff in IonDipole) for pairs with a dipole: the moved
+#     molecule's dipole against every other site plus every moved site
+#     against every other dipole: 20 FLOP more;
+#   inside rc = 15 A (about 84 sites per moved site at this density):
+#     Coulomb Q5/r and the reaction-field dipole-dipole: 40 FLOP more.
+MOL_LJ_FLOP, MOL_ID_FLOP, MOL_NEAR_FLOP, MOL_NEAR_SITES = 15, 20, 40, 84
+
+
+def mol_flop_per_trial(n_sites=20000, n_dipoles=1000, gs=20):
+    lj = 2 * gs * (n_sites - gs) * MOL_LJ_FLOP
+    idp = 2 * ((n_sites - gs) + gs * (n_dipoles - 1)) * MOL_ID_FLOP
+    near = 2 * gs * MOL_NEAR_SITES * MOL_NEAR_FLOP
+    return lj + idp + near
+
+
+def run_molecules(args, rank, world):
+    import numpy as np
+    from beofaunus_gb300.gpu import MolSystem, mol_draw_stream, mol_run_many
+    torch, dev, local, sms = gpu_setup(args)
+    C = args.cluster
+    B = args.systems or max(1, sms // C)
+    T = args.trials or 1000
+    steps, warm = args.steps, args.warmup
+    with mp.get_context("spawn").Pool(min(B, os.cpu_count() or 1)) as pool:
+        data = pool.map(_mol_system, [11 + rank * 1000003 + b for b in range(B)])
+    systems = []
+    for b, (p, xyz, mu, mus, ids) in enumerate(data):
+        s_ = MolSystem(p, xyz, mu, mus, ids, 20, cluster=C)
+        systems.append(s_)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def step(seed):
+        for b, s_ in enumerate(systems):
+            s_.stream_upload(mol_draw_stream(seed * 1000 + b, 1000, T, 1.0, 0.3, True))
+        flush.fill_(seed & 0xFF)
+        torch.cuda.synchronize()
+        return mol_run_many(systems)[1]
+
+    for s_ in range(warm):
+        step(10 + s_)
+    clocks = ClockSampler(local)
+    clocks.start()
+    stats = [step(1000 + s_) for s_ in range(steps)]
+    clk = clocks.stop()
+    ms = sum(st["device_ms"] for st in stats)
+    trials = sum(st["trials"] for st in stats)
+    value = trials / (ms / 1e3)
+    # e2e: host draws (the reference's mt19937) uploaded inside the timed region
+    e2e_s, e2e_t = 0.0, 0
+    for s_ in range(steps):
+        host = [mol_draw_stream(50000 + 100 * s_ + b, 1000, T, 1.0, 0.3, True) for b in range(B)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b, s2 in enumerate(systems):
+            s2.stream_upload(host[b])
+        _, tot = mol_run_many(systems)
+        e2e_s += time.perf_counter() - t0
+        e2e_t += tot["trials"]
+    # one system alone on the largest cluster: the single-system latency
+    one = systems[0]
+    single = {}
+    for c in sorted({one.max_cluster, C}):
+        one.cluster = c
+        st = mol_draw_stream(99, 1000, 2000, 1.0, 0.3, True)
+        one.sweep(st, log=False)
+        r = one.sweep(mol_draw_stream(98, 1000, 2000, 1.0, 0.3, True), log=False)
+        single["cluster_%d" % c] = {"value": r["trials"] / (r["device_ms"] / 1e3), "unit": UNIT,
+                                    "us_per_trial": r["device_ms"] * 1e3 / r["trials"]}
+    one.cluster = C
+    # plain per-trial path: host-computed rotation + fg_mol_trial_du + fg_mol_commit
+    xyz, mu, cm = one.state()
+    L = 150.0
+    st = mol_draw_stream(77, 1000, 200, 1.0, 0.3, True)
+    t0 = time.perf_counter()
+    for k in range(200):
+        g = int(st["group"][k])
+        sl = slice(20 * g, 20 * g + 20)
+        ax, ang = st["axis"][k], st["angle"][k]
+        K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+        R = np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+        off = xyz[sl] - cm[g]
+        off -= L * np.round(off / L)
+        new = cm[g] + off @ R.T + st["trans"][k]
+        new -= L * np.round(new / L)
+        newmu = mu[sl] @ R.T
+        newcm = cm[g] + st["trans"][k]
+        newcm -= L * np.round(newcm / L)
+        du = one.trial_du(g, new, newmu, newcm)
+        acc = not (st["u"][k] > np.exp(-du))
+        one.commit(acc)
+        if acc:
+            xyz[sl], mu[sl], cm[g] = new, newmu, newcm
+    plain = 200 / (time.perf_counter() - t0)
+    # roofline (FP32): algorithmic FLOP per trial (cost model above)
+    flop = mol_flop_per_trial()
+    achieved = flop * value / 1e12
+    fp32_peak = fp32_gemm_tflops(torch, dev)
+    cfg = {"workload": WORKLOAD_NAMES["molecules"], "systems": B, "ctas_per_system": C, "molecules_per_system": 1000,
+           "sites_per_molecule": 20, "box_A": 150.0, "site_sigma_A": 3.5, "lj_eps_kT": 0.2, "dipole_eA": 1.5,
+           "rf_cutoff_A": 15.0, "eps_rf": 1e11, "dp_A": 1.0, "drot_rad": 0.3, "trials_per_system_per_step": T,
+           "l2": "L2 flushed (256 MiB write) between timed steps"}
+    out = base_line(value, steps, warm, ms / steps, world, cfg,
+                    "f32 pair terms; exact int64 r^2 differences near; FP64 rigid rotation; df sums",
+                    "synthetic (seeded molecules, reference mt19937 TranslateRotate draws)")
+    out.update({"e2e": {"value": e2e_t / e2e_s, "unit": UNIT, "h2d_bytes_per_step": B * T * 80,
+                        "d2h_bytes_per_step": B * 48},
+                "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
+                "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                             "frac": achieved / fp32_peak, "traffic": None,
+                             "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (best of 5)",
+                             "flop_per_trial": flop,
+                             "note": "whole-launch rate over all systems; each system is one sequential chain"},
+                "single_system": single, "plain_per_trial_api": {"value": plain, "unit": UNIT},
+                "batched_over_plain": value / plain, "clocks": clk})
+    for s_ in systems:
+        s_.close()
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("molecules"))
+    if rank == 0:
+        print(json.dumps(out))
+
+
+# ----------------------------------------------------------------- serving
+def _serving_job(args):
+    n, temp, seed = args
+    from beofaunus_gb300 import workloads
+    return workloads.dh_lj_salt(n, seed, kT_scale=temp, start="scatter")
+
+
+def run_serving(args, rank, world):
+    """Poisson job stream through the continuous-batching server. Each job is
+    a DH+LJ salt with N log-uniform in [256, 16384], its own temperature in
+    [0.8, 2.0] and seed, running ``--job-sweeps`` sweeps (the named 2000 are
+    scaled down so the run ends within minutes; the scale is in the line).
+    Capacity is measured first with every job submitted at once; the timed
+    run then feeds the same job mix at 80 % of that capacity."""
+    import numpy as np
+    from beofaunus_gb300.gpu import Server
+    torch, dev, local, sms = gpu_setup(args)
+    n_jobs = args.jobs
+    sizes, temps = _serving_sizes(n_jobs, seed=5 + rank)
+    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+        jobs = pool.map(_serving_job, [(n, t, 100 + i) for i, (n, t) in enumerate(zip(sizes, temps))])
+    sweeps = args.job_sweeps
+    budget = int(args.serve_gib * (1 << 30))
+
+    def run_stream(arrivals):
+        srv = Server(budget, round_pairs=args.round_pairs)
+        t0 = time.perf_counter()
+        submitted, finish, ids = 0, {}, {}
+        order = list(range(n_jobs))
+        dev_ms = 0.0
+        while len(finish) < n_jobs:
+            now = time.perf_counter() - t0
+            while submitted < n_jobs and arrivals[submitted] <= now:
+                j = order[submitted]
+                p, xyz, q, ids_ = jobs[j]
+                ids[srv.submit(p, xyz, q, ids_, 1000 + j, sweeps * len(ids_))] = j
+                submitted += 1
+            if len(ids) == len(finish):
+                time.sleep(max(0.0, min(arrivals[submitted] - now, 0.01)) if submitted < n_jobs else 0)
+                continue
+            running, fin, ms = srv.step()
+            dev_ms += ms
+            tnow = time.perf_counter() - t0
+            for jid, j in ids.items():
+                if j in finish:
+                    continue
+                if srv.poll(jid)["state"] >= 2:
+                    finish[j] = tnow
+                    srv.release(jid)
+        srv.close()
+        return finish, time.perf_counter() - t0, dev_ms
+
+    total_trials = sweeps * sum(sizes)
+    # capacity: everything at t = 0
+    fin0, span0, _ = run_stream([0.0] * n_jobs)
+    capacity = n_jobs / span0
+    rate = 0.8 * capacity
+    rng = np.random.default_rng(11)
+    arrivals = list(np.cumsum(rng.exponential(1.0 / rate, n_jobs)))
+    clocks = ClockSampler(local)
+    clocks.start()
+    finish, span, dev_ms = run_stream(arrivals)
+    clk = clocks.stop()
+    lat = np.array([finish[j] - arrivals[j] for j in range(n_jobs)])
+    value = total_trials / span
+    cfg = {"workload": WORKLOAD_NAMES["serving"], "jobs": n_jobs, "n_range": [256, 16384],
+           "temperature_range": [0.8, 2.0], "sweeps_per_job": sweeps, "sweeps_per_job_named": 2000,
+           "arrival": "Poisson at 0.8 x measured capacity", "capacity_jobs_per_s": capacity,
+           "device_budget_GiB": args.serve_gib, "round_pairs": args.round_pairs}
+    out = base_line(value, 1, 1, 1e3 * span, world, cfg, "f32 pair terms; df sums",
+                    "synthetic (seeded overlap-free starts, Philox streams per job)")
+    out.update({"latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                              "mean": float(lat.mean()), "max": float(lat.max())},
+                "device_busy_frac": dev_ms / 1e3 / span, "clocks": clk,
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(sum(24 * n + 16 for n in sizes)),
+                        "d2h_bytes_per_step": int(sum(24 * n for n in sizes))}})
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("serving"))
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def run_reference(args):
     """The reference's CPU path on the host cores: the FP64 oracle port (the
     reference binary built from source is x86-only here and does not travel)."""
     warm, steps = args.warmup, args.steps
-    cp = CpuPath()
+    cp = CpuPath(cpu_kinds(args.workload))
     try:
-        cp.sample(0.5)
+        cp.sample(0.2)
         for _ in range(warm):
             cp.sample(args.ref_seconds)
         vals, trials = [], 0
@@ -443,11 +876,13 @@ def run_reference(args):
     finally:
         cp.close()
     value = statistics.mean(vals)
+    cfg = workload_config(cp.cores, "time-bounded sample per step") if args.workload == "rpm16k" else \
+        {"workload": WORKLOAD_NAMES[args.workload], "systems": cp.cores, "per_step": "time-bounded sample"}
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * args.ref_seconds,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded overlap-free starts, reference mt19937 stream)",
-           "config": workload_config(cp.cores, "time-bounded sample per step"),
+           "config": cfg,
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cp.cores, "kind": "port",
                             "sample": cp.describe(args.ref_seconds, trials // max(steps, 1))},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -460,8 +895,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--systems", type=int, default=0, help="systems per GPU (default: SM count)")
-    ap.add_argument("--trials", type=int, default=N_IONS, help="trials per system per step (default: one sweep)")
+    ap.add_argument("--workload", default="rpm16k", choices=["rpm16k", "rpm800", "pt64", "molecules", "serving"])
+    ap.add_argument("--systems", type=int, default=0, help="systems per GPU (default: SM count, or SMs / cluster)")
+    ap.add_argument("--trials", type=int, default=0, help="trials per system per step (default: one sweep)")
+    ap.add_argument("--cluster", type=int, default=4, help="molecules: CTAs per system")
+    ap.add_argument("--pt-sweeps", type=int, default=100, help="pt64: sweeps between swaps")
+    ap.add_argument("--jobs", type=int, default=120, help="serving: jobs in the stream")
+    ap.add_argument("--job-sweeps", type=int, default=20, help="serving: sweeps per job")
+    ap.add_argument("--serve-gib", type=float, default=8.0, help="serving: device budget for jobs")
+    ap.add_argument("--round-pairs", type=int, default=1 << 24, help="serving: pair evaluations per job per round")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample per core")
     ap.add_argument("--ref-seconds", type=float, default=3.0, help="reference arm: seconds per step")
     ap.add_argument("--no-cpu", action="store_true")
@@ -473,7 +915,16 @@ def main():
         if rank == 0:
             run_reference(args)
         return
-    run_ours(args, rank, world)
+    if args.workload == "rpm16k":
+        args.trials = args.trials or N_IONS
+        run_ours(args, rank, world)
+    else:
+        if world > 1:
+            import torch.distributed as dist
+            import torch
+            dist.init_process_group("nccl", device_id=torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
+        {"rpm800": run_rpm800, "pt64": run_pt, "molecules": run_molecules, "serving": run_serving}[args.workload](
+            args, rank, world)
 
 
 if __name__ == "__main__":

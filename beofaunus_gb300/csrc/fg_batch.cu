@@ -505,6 +505,8 @@ struct fg_server {
     int64_t used = 0, next_id = 1;
     std::vector<fg_job *> jobs;   // all jobs not yet released
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;            // second kernel variant of a round
+    cudaEvent_t fork = nullptr, join = nullptr;
     SysDesc *d_descs = nullptr;
     SysScalars *d_gather = nullptr;
     int64_t *d_counts = nullptr;
@@ -605,6 +607,12 @@ int fg_server_destroy(fg_server *s) {
     if (s->d_descs) cudaFree(s->d_descs);
     if (s->d_gather) cudaFree(s->d_gather);
     if (s->d_counts) cudaFree(s->d_counts);
+    if (s->stream2) {
+        cudaStreamSynchronize(s->stream2);
+        cudaStreamDestroy(s->stream2);
+        cudaEventDestroy(s->fork);
+        cudaEventDestroy(s->join);
+    }
     cudaStreamDestroy(s->stream);
     delete s;
     return FG_OK;
@@ -656,14 +664,22 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
     if (n_finished) *n_finished = 0;
     if (device_ms) *device_ms = 0;
     if (run.empty()) return FG_OK;
+    // jobs of one kernel variant run in one launch; variants run side by side
+    // on their own streams (sizes that fit shared memory and those that do not)
+    std::stable_sort(run.begin(), run.end(), [](const fg_job *a, const fg_job *b) {
+        return (const void *)sweep_fn(a->sys) < (const void *)sweep_fn(b->sys);
+    });
     const int n = (int)run.size();
     int rc = server_grow(s, n);
     if (rc) return rc;
     std::vector<SysDesc> descs(n);
     std::vector<int64_t> counts(n);
-    LaunchCfg cfg{};
-    size_t smem = 0;
-    int T = s->threads;
+    struct Group {
+        SweepFn fn;
+        int first, count, threads;
+        size_t smem;
+    };
+    std::vector<Group> groups;
     for (int i = 0; i < n; i++) {
         fg_job *j = run[i];
         fg_system *h = j->sys;
@@ -676,13 +692,23 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         h->desc.skip_rebuild = 1;
         h->desc.stream_first = j->done;
         descs[i] = h->desc;
-        if (i == 0) cfg.fn = sweep_fn(h);
-        if (sweep_fn(h) != cfg.fn) return fail(FG_ERR_INVALID, "server jobs need one kernel variant");
-        smem = std::max(smem, sweep_smem(h, h->pos_smem));
-        if (!s->threads) T = std::max(T, sweep_threads(h));
+        const SweepFn fn = sweep_fn(h);
+        if (groups.empty() || groups.back().fn != fn) groups.push_back(Group{fn, i, 0, s->threads, 0});
+        Group &g = groups.back();
+        g.count++;
+        g.smem = std::max(g.smem, sweep_smem(h, h->pos_smem));
+        if (!s->threads) g.threads = std::max(g.threads, sweep_threads(h));
     }
-    rc = set_smem_attr((const void *)cfg.fn, smem);
-    if (rc) return rc;
+    for (Group &g : groups) {
+        rc = set_smem_attr((const void *)g.fn, g.smem);
+        if (rc) return rc;
+    }
+    if (groups.size() > 1 && !s->stream2) {
+        if (cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(FG_ERR_CUDA, "stream create failed");
+        cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
+    }
     CK(cudaMemcpyAsync(s->d_descs, descs.data(), n * sizeof(SysDesc), cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(s->d_counts, counts.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, s->stream));
     int64_t maxc = 0;
@@ -694,8 +720,21 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
     dim3 pg((unsigned)std::min<int64_t>((maxc + 255) / 256, 64), n);
     fg::batch_philox_kernel<<<pg, 256, 0, s->stream>>>(s->d_descs, s->d_counts, nullptr);
     fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(s->d_descs, n, s->d_counts);
-    cfg.fn<<<n, T, smem, s->stream>>>(s->d_descs, INT64_MAX, run[0]->sys->sc_tab);
-    CK(cudaGetLastError());
+    for (size_t g = 0; g < groups.size(); g++) {
+        const Group &G = groups[g];
+        cudaStream_t st = s->stream;
+        if (g > 0) {
+            CK(cudaEventRecord(s->fork, s->stream));
+            CK(cudaStreamWaitEvent(s->stream2, s->fork, 0));
+            st = s->stream2;
+        }
+        G.fn<<<G.count, G.threads, G.smem, st>>>(s->d_descs + G.first, INT64_MAX, run[G.first]->sys->sc_tab);
+        CK(cudaGetLastError());
+    }
+    if (groups.size() > 1) {
+        CK(cudaEventRecord(s->join, s->stream2));
+        CK(cudaStreamWaitEvent(s->stream, s->join, 0));
+    }
     CK(cudaEventRecord(e1, s->stream));
     std::vector<SysScalars> sc(n);
     fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, s->stream>>>(s->d_descs, n, s->d_gather);

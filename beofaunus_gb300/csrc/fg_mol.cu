@@ -851,6 +851,8 @@ struct fg_molsys {
     int64_t *expl_cm = nullptr;
     int pending = -1;   // molecule of an evaluated explicit trial awaiting fg_mol_commit
     double pending_du = 0.0;
+    int64_t n_stream = 0;   // trials in the staged stream
+    int64_t acc0 = 0;       // accepted count when the stream was staged
     bool has_cm = false;
     bool state_set = false;
     std::vector<int32_t> types;
@@ -1085,6 +1087,135 @@ void mol_make_trials(const fg_molsys *h, int64_t n, const int32_t *mol, const do
         t.thr_lo = f.y;
         if (u[k] <= 0.0) { t.thr_hi = INFINITY; t.thr_lo = 0.0f; }
     }
+}
+
+// Stage a trial stream: validate, build MolTrial records, upload, reset the
+// stream cursor and per-stream sums.
+int mol_upload(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, const double *angle,
+               const int32_t *center, const double *trans, const double *u, int rotate, int translate, bool log) {
+    if (!h || n < 0 || (n > 0 && (!mol || !u))) return fail(FG_ERR_INVALID, "bad argument");
+    if (rotate && n > 0 && (!axis || !angle)) return fail(FG_ERR_INVALID, "rotation needs axis and angle");
+    if (translate && n > 0 && !trans) return fail(FG_ERR_INVALID, "translation needs trans");
+    if (!h->state_set) return fail(FG_ERR_STATE, "fg_mol_set_state first");
+    if (h->pending >= 0) return fail(FG_ERR_STATE, "a trial is pending: call fg_mol_commit");
+    for (int64_t k = 0; k < n; k++) {
+        if (mol[k] < 0 || mol[k] >= h->M) return fail(FG_ERR_INVALID, "molecule index out of range at %lld", (long long)k);
+        if (center && (center[k] < 0 || center[k] > 2)) return fail(FG_ERR_INVALID, "bad centre kind");
+    }
+    int rc = mol_ensure_trials(h, n, log);
+    if (rc) return rc;
+    std::vector<fgm::MolTrial> tr;
+    mol_make_trials(h, n, mol, axis, angle, center, trans, u, rotate, translate, tr);
+    if (n > 0) CK(cudaMemcpyAsync(h->trials, tr.data(), n * sizeof(fgm::MolTrial), cudaMemcpyHostToDevice, h->stream));
+    fgm::MolScalars s0;
+    rc = mol_read_scalars(h, s0);
+    if (rc) return rc;
+    h->acc0 = s0.n_accepted;
+    fgm::MolScalars s = s0;
+    s.cursor = 0;
+    s.n_trials = n;
+    s.u_hi = s.u_lo = 0.0f;
+    s.error = 0;
+    rc = mol_write_scalars(h, s);
+    if (rc) return rc;
+    h->n_stream = n;
+    h->desc.log_du = log ? h->log_du : nullptr;
+    h->desc.log_acc = log ? h->log_acc : nullptr;
+    h->desc.expl_pos = nullptr;
+    h->desc.expl_mu = nullptr;
+    h->desc.expl_cm = nullptr;
+    return mol_push_desc(h);
+}
+
+// Run the staged streams of several systems in one launch per chunk (one
+// cluster of C CTAs per system); launches hold at most kChunk trials each.
+int mol_run(fg_molsys *const *sys, int n, fg_sweep_stats *per, fg_sweep_stats *total) {
+    if (!sys || n < 1) return fail(FG_ERR_INVALID, "bad argument");
+    fg_molsys *h0 = sys[0];
+    size_t smem_slice = 0, smem_flat = 0;
+    bool all_slice = true;
+    int64_t maxn = 0;
+    for (int i = 0; i < n; i++) {
+        fg_molsys *h = sys[i];
+        if (!h || !h->state_set) return fail(FG_ERR_STATE, "system %d has no state", i);
+        if (h->C != h0->C) return fail(FG_ERR_INVALID, "systems must share the cluster size");
+        if (h->device != h0->device) return fail(FG_ERR_INVALID, "systems must share the device");
+        const size_t a = mol_smem_bytes(h, h->C, true);
+        if (a > 200 * 1024) all_slice = false;
+        smem_slice = std::max(smem_slice, a);
+        smem_flat = std::max(smem_flat, mol_smem_bytes(h, h->C, false));
+        maxn = std::max(maxn, h->n_stream);
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    MolLaunch L;
+    L.cluster = h0->C > 1;
+    L.smem = all_slice ? smem_slice : smem_flat;
+    if (all_slice) L.fn = L.cluster ? fgm::mol_sweep_kernel<true, true, false> : fgm::mol_sweep_kernel<true, false, false>;
+    else L.fn = L.cluster ? fgm::mol_sweep_kernel<false, true, false> : fgm::mol_sweep_kernel<false, false, false>;
+    CK(cudaFuncSetAttribute((const void *)L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+    if (L.cluster) CK(cudaFuncSetAttribute((const void *)L.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaStream_t st = h0->stream;
+    const fgm::MolDesc *descs = h0->d_desc;
+    fgm::MolDesc *tmp = nullptr;
+    if (n > 1) {
+        std::vector<fgm::MolDesc> v(n);
+        for (int i = 0; i < n; i++) v[i] = sys[i]->desc;
+        CK(cudaMalloc(&tmp, n * sizeof(fgm::MolDesc)));
+        CK(cudaMemcpyAsync(tmp, v.data(), n * sizeof(fgm::MolDesc), cudaMemcpyHostToDevice, st));
+        descs = tmp;
+    }
+    std::vector<fgm::MolScalars> s0(n), s1(n);
+    for (int i = 0; i < n; i++) {
+        CK(cudaMemcpyAsync(&s0[i], sys[i]->sc, sizeof(fgm::MolScalars), cudaMemcpyDeviceToHost, st));
+    }
+    const int64_t kChunk = 65536;
+    const int64_t nl = (maxn + kChunk - 1) / kChunk;
+    std::vector<int64_t> ends((size_t)nl * n);
+    CK(cudaEventRecord(h0->ev0, st));
+    int rc = FG_OK;
+    for (int64_t c = 0; c < nl && !rc; c++) {
+        for (int i = 0; i < n; i++) {
+            int64_t &e = ends[(size_t)c * n + i];
+            e = std::min(sys[i]->n_stream, (c + 1) * kChunk);
+            CK(cudaMemcpyAsync(&sys[i]->sc->n_trials, &e, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        }
+        rc = mol_launch(h0, L, descs, n, st);
+    }
+    CK(cudaEventRecord(h0->ev1, st));
+    CK(cudaEventSynchronize(h0->ev1));
+    if (tmp) cudaFree(tmp);
+    if (rc) return rc;
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, h0->ev0, h0->ev1));
+    for (int i = 0; i < n; i++)
+        CK(cudaMemcpyAsync(&s1[i], sys[i]->sc, sizeof(fgm::MolScalars), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    fg_sweep_stats tot{};
+    int errs = 0;
+    for (int i = 0; i < n; i++) {
+        fg_sweep_stats x{};
+        x.trials = s1[i].cursor;
+        x.accepted = s1[i].n_accepted - sys[i]->acc0;
+        x.energy_change = df_val(s1[i].u_hi, s1[i].u_lo);
+        x.device_ms = ms;
+        x.sweep_kernel_ms = ms;
+        x.sweep_launches = (int32_t)nl;
+        x.error_flags = s1[i].error;
+        x.kernel_launches = nl;
+        errs |= s1[i].error;
+        if (per) per[i] = x;
+        tot.trials += x.trials;
+        tot.accepted += x.accepted;
+        tot.energy_change += x.energy_change;
+    }
+    tot.device_ms = ms;
+    tot.sweep_kernel_ms = ms;
+    tot.sweep_launches = (int32_t)nl;
+    tot.kernel_launches = nl;
+    tot.error_flags = errs;
+    if (total) *total = tot;
+    if (errs) return fail(FG_ERR_DEVICE, "device error flags 0x%x", errs);
+    return FG_OK;
 }
 
 }  // namespace
@@ -1464,61 +1595,25 @@ int fg_mol_draw_stream(uint32_t seed, int32_t n_molecules, int64_t n, double dp,
 // n TranslateRotate trials on the device. rotate/translate say whether the
 // move has dprot/dp above 1e-6 (move.h:1642, 1671); the arrays are the draws
 // (fg_mol_draw_stream). acc/du (may be NULL) receive per-trial results.
+int fg_mol_stream_upload(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, const double *angle,
+                         const int32_t *center, const double *trans, const double *u, int32_t rotate,
+                         int32_t translate) {
+    return mol_upload(h, n, mol, axis, angle, center, trans, u, rotate, translate, false);
+}
+
+int fg_mol_run_many(fg_molsys *const *systems, int32_t n_systems, fg_sweep_stats *per_system, fg_sweep_stats *total) {
+    return mol_run(systems, n_systems, per_system, total);
+}
+
 int fg_mol_sweep(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, const double *angle,
                  const int32_t *center, const double *trans, const double *u, int32_t rotate, int32_t translate,
                  uint8_t *acc, double *du, fg_sweep_stats *stats) {
-    if (!h || n < 0 || (n > 0 && (!mol || !u))) return fail(FG_ERR_INVALID, "bad argument");
-    if (rotate && n > 0 && (!axis || !angle)) return fail(FG_ERR_INVALID, "rotation needs axis and angle");
-    if (translate && n > 0 && !trans) return fail(FG_ERR_INVALID, "translation needs trans");
-    if (!h->state_set) return fail(FG_ERR_STATE, "fg_mol_set_state first");
-    if (h->pending >= 0) return fail(FG_ERR_STATE, "a trial is pending: call fg_mol_commit");
-    for (int64_t k = 0; k < n; k++) {
-        if (mol[k] < 0 || mol[k] >= h->M) return fail(FG_ERR_INVALID, "molecule index out of range at %lld", (long long)k);
-        if (center && (center[k] < 0 || center[k] > 2)) return fail(FG_ERR_INVALID, "bad centre kind");
-    }
     const bool log = acc || du;
-    int rc = mol_ensure_trials(h, n, log);
+    int rc = mol_upload(h, n, mol, axis, angle, center, trans, u, rotate, translate, log);
     if (rc) return rc;
-    std::vector<fgm::MolTrial> tr;
-    mol_make_trials(h, n, mol, axis, angle, center, trans, u, rotate, translate, tr);
-    if (n > 0) CK(cudaMemcpyAsync(h->trials, tr.data(), n * sizeof(fgm::MolTrial), cudaMemcpyHostToDevice, h->stream));
-    fgm::MolScalars s0;
-    rc = mol_read_scalars(h, s0);
-    if (rc) return rc;
-    fgm::MolScalars s = s0;
-    s.cursor = 0;
-    s.n_trials = n;
-    s.u_hi = s.u_lo = 0.0f;
-    s.error = 0;
-    rc = mol_write_scalars(h, s);
-    if (rc) return rc;
-    h->desc.log_du = log ? h->log_du : nullptr;
-    h->desc.log_acc = log ? h->log_acc : nullptr;
-    h->desc.expl_pos = nullptr;
-    h->desc.expl_mu = nullptr;
-    h->desc.expl_cm = nullptr;
-    rc = mol_push_desc(h);
-    if (rc) return rc;
-    MolLaunch L;
-    rc = mol_pick<false>(h, L);
-    if (rc) return rc;
-    // launches of at most kChunk trials (the kernel runs from the stored cursor
-    // to the stored end; each launch moves the end forward)
-    const int64_t kChunk = 65536;
-    const int64_t nl = (n + kChunk - 1) / kChunk;
-    std::vector<int64_t> ends(nl);
-    CK(cudaEventRecord(h->ev0, h->stream));
-    for (int64_t c = 0; c < nl; c++) {
-        ends[c] = std::min(n, (c + 1) * kChunk);
-        CK(cudaMemcpyAsync(&h->sc->n_trials, &ends[c], sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
-        rc = mol_launch(h, L, h->d_desc, 1, h->stream);
-        if (rc) return rc;
-    }
-    CK(cudaEventRecord(h->ev1, h->stream));
-    CK(cudaEventSynchronize(h->ev1));
-    float ms = 0.0f;
-    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-    rc = mol_read_scalars(h, s);
+    fg_sweep_stats st{};
+    rc = mol_run(&h, 1, nullptr, &st);
+    if (stats) *stats = st;
     if (rc) return rc;
     if (log && n > 0) {
         std::vector<float2> l(n);
@@ -1531,18 +1626,6 @@ int fg_mol_sweep(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis
             if (acc) acc[k] = a[k];
         }
     }
-    if (stats) {
-        *stats = fg_sweep_stats{};
-        stats->trials = s.cursor;
-        stats->accepted = s.n_accepted - s0.n_accepted;
-        stats->energy_change = df_val(s.u_hi, s.u_lo);
-        stats->device_ms = ms;
-        stats->sweep_kernel_ms = ms;
-        stats->sweep_launches = (int32_t)nl;
-        stats->error_flags = s.error;
-        stats->kernel_launches = nl;
-    }
-    if (s.error) return fail(FG_ERR_DEVICE, "device error flags 0x%x", s.error);
     return FG_OK;
 }
 

@@ -100,6 +100,8 @@ def lib(build_if_missing=True):
                                    ctypes.c_int),
             "fg_mol_sweep": ([vp, i64, dp, dp, dp, dp, dp, dp, i32, i32, dp, dp, dp], ctypes.c_int),
             "fg_mol_total_energy": ([vp, dp], ctypes.c_int),
+            "fg_mol_stream_upload": ([vp, i64, dp, dp, dp, dp, dp, dp, i32, i32], ctypes.c_int),
+            "fg_mol_run_many": ([dp, i32, dp, dp], ctypes.c_int),
             "fg_mol_running_energy": ([vp, dp], ctypes.c_int),
             "fg_mol_device_bytes": ([vp], ctypes.c_int64),
         }
@@ -379,6 +381,16 @@ class Server:
         return int(lib().fg_server_bytes_in_use(self.h))
 
 
+def mol_run_many(systems):
+    """Run the staged streams of several MolSystems in one launch."""
+    arr = (ctypes.c_void_p * len(systems))(*[s.h.value for s in systems])
+    per = (SweepStats * len(systems))()
+    tot = SweepStats()
+    _check(lib().fg_mol_run_many(ctypes.cast(arr, ctypes.c_void_p), len(systems), ctypes.cast(per, ctypes.c_void_p),
+                                 ctypes.byref(tot)))
+    return [p.as_dict() for p in per], tot.as_dict()
+
+
 def mol_draw_stream(seed, n_molecules, n, dp=1.0, dprot=0.3, center_rotation=True):
     """The reference's draws for n TranslateRotate trials (host only)."""
     g = np.empty(n, np.int32)
@@ -475,6 +487,16 @@ class MolSystem:
         out = stats.as_dict()
         out.update(acc=acc, du=du)
         return out
+
+    def stream_upload(self, st, rotate=True, translate=True):
+        g = np.ascontiguousarray(st["group"], dtype=np.int32)
+        ax = np.ascontiguousarray(st["axis"], dtype=np.float64)
+        an = np.ascontiguousarray(st["angle"], dtype=np.float64)
+        ce = np.ascontiguousarray(st["center"], dtype=np.int32)
+        tr = np.ascontiguousarray(st["trans"], dtype=np.float64)
+        u = np.ascontiguousarray(st["u"], dtype=np.float64)
+        _check(lib().fg_mol_stream_upload(self.h, len(g), _p(g), _p(ax), _p(an), _p(ce), _p(tr), _p(u),
+                                          1 if rotate else 0, 1 if translate else 0))
 
     def total_energy(self):
         c = np.empty(3)

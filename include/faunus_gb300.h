@@ -274,6 +274,15 @@ int fg_mol_sweep(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis
                  const int32_t *center, const double *trans, const double *u, int32_t rotate, int32_t translate,
                  uint8_t *acc, double *du, fg_sweep_stats *stats);
 
+/* Stage a trial stream (fg_mol_sweep's arguments) without running it. */
+int fg_mol_stream_upload(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, const double *angle,
+                         const int32_t *center, const double *trans, const double *u, int32_t rotate,
+                         int32_t translate);
+/* Run the staged streams of independent systems (same cluster size) in one
+ * launch: one cluster per system. per_system (may be NULL) gets n_systems
+ * records. No counterpart in the reference (one system per process there). */
+int fg_mol_run_many(fg_molsys *const *systems, int32_t n_systems, fg_sweep_stats *per_system, fg_sweep_stats *total);
+
 /* comp = {intermolecular, intramolecular, total}, FP64. Replaces:
  * Energybase::systemEnergy (energy.h:169-180). */
 int fg_mol_total_energy(fg_molsys *h, double *comp);

@@ -138,3 +138,25 @@ def test_server_job_matches_oracle():
     r = o.mc_run_stream(idx, disp, u)
     assert res["accepted"] == int(r["acc"].sum())
     np.testing.assert_allclose(res["xyz"], o.positions(), rtol=0, atol=1e-9)
+
+
+def test_server_mixes_kernel_variants():
+    """Jobs small enough for shared-memory coordinates and jobs that are not
+    run in the same round (two launches side by side) with unchanged results."""
+    from beofaunus_gb300.gpu import Server
+    small, big = _job(300, 31, 1.1), _job(9000, 32, 1.0)
+
+    def run(items):
+        srv = Server(1 << 32, round_pairs=1 << 20)
+        ids = [srv.submit(p, x, q, t, seed, n_trials) for (p, x, q, t), seed, n_trials in items]
+        for _ in range(100000):
+            srv.step()
+            if all(srv.poll(j)["state"] == 2 for j in ids):
+                break
+        return [srv.poll(j, positions=True) for j in ids]
+
+    alone = run([(small, 31, 3000)])
+    mixed = run([(big, 32, 18000), (small, 31, 3000)])
+    assert all(m["state"] == 2 for m in mixed)
+    np.testing.assert_array_equal(mixed[1]["xyz"], alone[0]["xyz"])
+    assert mixed[1]["accepted"] == alone[0]["accepted"]

@@ -150,3 +150,24 @@ def test_mol_invalid_arguments():
         s.commit(True)   # nothing pending
     with pytest.raises(FgError):
         s.cluster = 3
+
+
+@pytest.mark.gpu
+def test_mol_run_many_equals_alone():
+    """Independent systems in one launch end exactly where each ends alone."""
+    from beofaunus_gb300.gpu import mol_run_many
+    data = [workloads.dipolar_molecules(50, seed=s) for s in (61, 62, 63)]
+    alone = []
+    for k, (p, xyz, mu, mus, ids) in enumerate(data):
+        s = MolSystem(p, xyz, mu, mus, ids, 20, cluster=2)
+        s.sweep(mol_draw_stream(300 + k, 50, 400, 1.0, 0.3, True), log=False)
+        alone.append(s.state())
+        s.close()
+    many = [MolSystem(p, xyz, mu, mus, ids, 20, cluster=2) for (p, xyz, mu, mus, ids) in data]
+    for k, s in enumerate(many):
+        s.stream_upload(mol_draw_stream(300 + k, 50, 400, 1.0, 0.3, True))
+    per, tot = mol_run_many(many)
+    assert tot["trials"] == 1200
+    for k, s in enumerate(many):
+        for a, b in zip(s.state(), alone[k]):
+            np.testing.assert_array_equal(a, b)
