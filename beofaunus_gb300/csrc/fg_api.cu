@@ -16,6 +16,7 @@
 
 #include "faunus_gb300.h"
 #include "fg_kernels.cu"
+#include "fg_dh_block.cu"
 
 using fg::SysDesc;
 using fg::SysScalars;
@@ -213,6 +214,216 @@ int set_smem_attr(const void *fn, size_t bytes) {
     return FG_OK;
 }
 
+// ---------------------------------------------------------------- DH block sweeps
+// Debye-Hueckel systems without a cell list run the block-of-trials kernel
+// (fg_dh_block.cu), large ones on a cluster of CTAs.
+using BlkFn = void (*)(const SysDesc *, const int *, int, int64_t);
+
+bool dh_block_ok(const fg_system *h) { return h->model == FG_MODEL_DH_LJ && !h->use_cells; }
+
+// Shared memory of the block kernel for N particles on C CTAs; slice = the
+// CTA's particles are staged in shared memory.
+size_t dh_block_smem(int N, int C, bool *slice) {
+    const int ns = (N + C - 1) / C;
+    const size_t with = fg::blk_smem_bytes(ns, true);
+    const bool fits = with + sizeof(SysDesc) + 1024 <= 227 * 1024;
+    if (slice) *slice = fits;
+    return fits ? with : fg::blk_smem_bytes(ns, false);
+}
+
+BlkFn dh_block_fn(bool slice, bool cluster) {
+    if (slice) return cluster ? fg::dh_block_kernel<true, true> : fg::dh_block_kernel<true, false>;
+    return cluster ? fg::dh_block_kernel<false, true> : fg::dh_block_kernel<false, false>;
+}
+
+int dh_block_attrs(BlkFn fn, size_t smem, bool cluster) {
+    CK(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (cluster) CK(cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    return FG_OK;
+}
+
+// Largest cluster (<= 16) the device co-schedules for the block kernel.
+int dh_block_max_cluster() {
+    static int cached[64];
+    static bool init[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dev = std::min(std::max(dev, 0), 63);
+    if (init[dev]) return cached[dev];
+    int best = 1;
+    for (int c : {16, 8, 4, 2}) {
+        bool slice;
+        const size_t smem = dh_block_smem(16384, c, &slice);
+        BlkFn fn = dh_block_fn(slice, true);
+        if (dh_block_attrs(fn, smem, true)) continue;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)c);
+        cfg.blockDim = dim3(fg::kBlkThreads);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)c;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, (const void *)fn, &cfg) == cudaSuccess && n > 0) {
+            best = c;
+            break;
+        }
+        cudaGetLastError();
+    }
+    cached[dev] = best;
+    init[dev] = true;
+    return best;
+}
+
+// CTAs for one system alone: about 2048 particles per CTA.
+int dh_block_ctas(int N) {
+    const int maxc = dh_block_max_cluster();
+    int C = 1;
+    while (C < maxc && (N + C - 1) / C > 2048) C <<= 1;
+    return C;
+}
+
+int dh_sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(n, 1);
+}
+
+// CTAs per system for systems run side by side: start at one each, then keep
+// doubling the system with the most work per CTA (weight / CTAs) while the
+// SMs hold every CTA at once, the device allows the cluster and each CTA keeps
+// at least 256 particles. weight ~ pair evaluations of the launch.
+std::vector<int> dh_block_ctas_many(const std::vector<int> &N, const std::vector<double> &w) {
+    const int n = (int)N.size();
+    std::vector<int> C(n, 1);
+    const int maxc = dh_block_max_cluster();
+    long spare = (long)dh_sm_count() - n;
+    while (spare > 0) {
+        int best = -1;
+        double bw = 0;
+        for (int i = 0; i < n; i++) {
+            if (2 * C[i] > maxc || N[i] / (2 * C[i]) < 256 || C[i] > spare) continue;
+            const double x = w[i] / C[i];
+            if (x > bw) {
+                bw = x;
+                best = i;
+            }
+        }
+        if (best < 0) break;
+        spare -= C[best];
+        C[best] *= 2;
+    }
+    return C;
+}
+
+// One launch of the block kernel over n systems (members: indices into descs,
+// device memory, or nullptr for 0..n-1) with C CTAs each.
+int dh_block_launch(const SysDesc *descs, const int *members, int n, int C, int maxN, int64_t end, cudaStream_t st) {
+    bool slice;
+    const size_t smem = dh_block_smem(maxN, C, &slice);
+    BlkFn fn = dh_block_fn(slice, C > 1);
+    int rc = dh_block_attrs(fn, smem, C > 1);
+    if (rc) return rc;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(n * C));
+    cfg.blockDim = dim3(fg::kBlkThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    if (C > 1) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    cudaError_t e = cudaLaunchKernelEx(&cfg, fn, descs, members, C, end);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "block sweep launch: %s", cudaGetErrorString(e));
+    return FG_OK;
+}
+
+// Systems grouped by their CTA count, each group one launch; groups after the
+// first run on side streams forked from and joined back into `st`.
+struct DhGroups {
+    std::vector<int> C;                 // per group
+    std::vector<std::vector<int>> mem;  // per group: member indices
+    std::vector<int> maxN;
+    int *d_members = nullptr;           // all groups' members, concatenated
+    std::vector<int> offset;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> ev;        // fork + one join per side stream
+    void release() {
+        if (d_members) cudaFree(d_members);
+        d_members = nullptr;
+        for (auto x : side) cudaStreamDestroy(x);
+        for (auto x : ev) cudaEventDestroy(x);
+        side.clear();
+        ev.clear();
+        C.clear();
+        mem.clear();
+        maxN.clear();
+        offset.clear();
+    }
+};
+
+int dh_groups_build(DhGroups &g, const std::vector<int> &N, const std::vector<double> &w) {
+    if (g.d_members) cudaFree(g.d_members);
+    g.d_members = nullptr;
+    g.C.clear();
+    g.mem.clear();
+    g.maxN.clear();
+    g.offset.clear();
+    const std::vector<int> C = dh_block_ctas_many(N, w);
+    for (size_t i = 0; i < N.size(); i++) {
+        size_t k = 0;
+        while (k < g.C.size() && g.C[k] != C[i]) k++;
+        if (k == g.C.size()) {
+            g.C.push_back(C[i]);
+            g.mem.emplace_back();
+            g.maxN.push_back(0);
+        }
+        g.mem[k].push_back((int)i);
+        g.maxN[k] = std::max(g.maxN[k], N[i]);
+    }
+    std::vector<int> all;
+    for (auto &m : g.mem) {
+        g.offset.push_back((int)all.size());
+        all.insert(all.end(), m.begin(), m.end());
+    }
+    CK(cudaMalloc(&g.d_members, std::max<size_t>(all.size(), 1) * sizeof(int)));
+    CK(cudaMemcpy(g.d_members, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+    while (g.side.size() + 1 < g.C.size()) {   // side streams and events are kept across rebuilds
+        cudaStream_t x;
+        CK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+        g.side.push_back(x);
+    }
+    while (g.ev.size() < g.C.size()) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        g.ev.push_back(e);
+    }
+    return FG_OK;
+}
+
+int dh_groups_launch(const DhGroups &g, const SysDesc *descs, int64_t end, cudaStream_t st) {
+    if (g.C.size() > 1) CK(cudaEventRecord(g.ev[0], st));
+    for (size_t k = 0; k < g.C.size(); k++) {
+        cudaStream_t s = k == 0 ? st : g.side[k - 1];
+        if (k > 0) CK(cudaStreamWaitEvent(s, g.ev[0], 0));
+        int rc = dh_block_launch(descs, g.d_members + g.offset[k], (int)g.mem[k].size(), g.C[k], g.maxN[k], end, s);
+        if (rc) return rc;
+        if (k > 0) CK(cudaEventRecord(g.ev[k], s));
+    }
+    for (size_t k = 1; k < g.C.size(); k++) CK(cudaStreamWaitEvent(st, g.ev[k], 0));
+    return FG_OK;
+}
+
 // Rebuild kernels for n systems whose descriptors are at `descs` (device).
 int launch_rebuild(const SysDesc *descs, int n, int maxN, int maxK, float2 *corr, cudaStream_t st) {
     if (maxK == 0) return FG_OK;
@@ -389,7 +600,12 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
             evs.push_back(a);
             evs.push_back(b);
             CK(cudaEventRecord(a, h->stream));
-            cfg.fn<<<1, cfg.threads, cfg.smem, h->stream>>>(h->d_desc, n, h->sc_tab);
+            if (dh_block_ok(h)) {
+                rc = dh_block_launch(h->d_desc, nullptr, 1, dh_block_ctas(h->N), h->N, n, h->stream);
+                if (rc) return rc;
+            } else {
+                cfg.fn<<<1, cfg.threads, cfg.smem, h->stream>>>(h->d_desc, n, h->sc_tab);
+            }
             CK(cudaGetLastError());
             CK(cudaEventRecord(b, h->stream));
             launches++;

@@ -111,6 +111,9 @@ struct fg_batch {
     bool pt = false;
     cudaGraphExec_t graph = nullptr;
     int64_t graph_sweeps = -1;
+    // Debye-Hueckel members without a cell list run the block kernel
+    bool dh_block = false;
+    DhGroups dh;
 };
 
 namespace {
@@ -131,7 +134,27 @@ int batch_config(fg_batch *b) {
     b->cfg.threads = T;
     b->cfg.smem = sm;
     b->rebuilds = b->maxK > 0 && !h0->desc.skip_rebuild;
+    b->dh_block = true;
+    std::vector<int> Ns;
+    std::vector<double> w;
+    for (fg_system *h : b->sys) {
+        if (!dh_block_ok(h)) b->dh_block = false;
+        Ns.push_back(h->N);
+        w.push_back((double)h->N * h->N);   // a sweep of N trials over N partners
+    }
+    if (b->dh_block) {
+        int rc = dh_groups_build(b->dh, Ns, w);
+        if (rc) return rc;
+    }
     return set_smem_attr((const void *)b->cfg.fn, sm);
+}
+
+// The sweep launch(es) of one pass over all members.
+int batch_sweep(fg_batch *b, int64_t end) {
+    if (b->dh_block) return dh_groups_launch(b->dh, b->d_descs, end, b->stream);
+    b->cfg.fn<<<(int)b->sys.size(), b->cfg.threads, b->cfg.smem, b->stream>>>(b->d_descs, end, b->sys[0]->sc_tab);
+    CK(cudaGetLastError());
+    return FG_OK;
 }
 
 int batch_push_descs(fg_batch *b) {
@@ -172,8 +195,10 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
             evs.push_back(e0);
             evs.push_back(e1);
             CK(cudaEventRecord(e0, b->stream));
-            b->cfg.fn<<<n, b->cfg.threads, b->cfg.smem, b->stream>>>(b->d_descs, INT64_MAX, b->sys[0]->sc_tab);
-            CK(cudaGetLastError());
+            {
+                int rc = batch_sweep(b, INT64_MAX);
+                if (rc) return rc;
+            }
             CK(cudaEventRecord(e1, b->stream));
             launches++;
             kernels++;
@@ -246,6 +271,7 @@ void batch_free(fg_batch *b) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->dh.release();
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -424,7 +450,15 @@ int fg_pt_run(fg_batch *b, int32_t rounds, int32_t sweeps_per_round, fg_sweep_st
         dim3 pg((unsigned)std::min<int64_t>((maxc + 255) / 256, 64), n);
         fg::batch_philox_kernel<<<pg, 256, 0, b->stream>>>(b->d_descs, b->d_counts, b->d_round);
         fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_counts);
-        b->cfg.fn<<<n, b->cfg.threads, b->cfg.smem, b->stream>>>(b->d_descs, INT64_MAX, b->sys[0]->sc_tab);
+        {
+            const int rc_ = batch_sweep(b, INT64_MAX);
+            if (rc_) {
+                cudaGraph_t gg;
+                cudaStreamEndCapture(b->stream, &gg);
+                if (gg) cudaGraphDestroy(gg);
+                return rc_;
+            }
+        }
         fg::pt_swap_kernel<<<1, 32, 0, b->stream>>>(b->d_descs, n, b->d_perm, b->d_temps, b->pt_seed, b->d_round,
                                                     b->d_att, b->d_acc);
         cudaError_t e = cudaStreamEndCapture(b->stream, &g);
@@ -507,6 +541,7 @@ struct fg_server {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;            // second kernel variant of a round
     cudaEvent_t fork = nullptr, join = nullptr;
+    DhGroups dh;                               // block-kernel jobs of the current round
     SysDesc *d_descs = nullptr;
     SysScalars *d_gather = nullptr;
     int64_t *d_counts = nullptr;
@@ -533,11 +568,16 @@ size_t job_bytes(const fg_params &P, int N, int64_t round_trials) {
     return b;
 }
 
+// Trials of one round: about round_pairs pair evaluations for every job, so
+// a round takes about as long for a small job as for a large one (at least 32
+// trials, at most 2^20).
+int64_t round_trials_for(const fg_server *s, int64_t N) {
+    int64_t t = std::max<int64_t>(32, s->round_pairs / std::max<int64_t>(N, 1));
+    return std::min<int64_t>(t, 1 << 20);
+}
 int64_t round_trials_of(const fg_server *s, const fg_job *j) {
     const int64_t N = j->sys ? j->sys->N : (int64_t)j->ids.size();
-    int64_t t = std::max<int64_t>(N, s->round_pairs / std::max<int64_t>(N, 1));
-    t = std::min<int64_t>(t, 1 << 20);
-    return std::min<int64_t>(t, j->n_trials - j->done);
+    return std::min<int64_t>(round_trials_for(s, N), j->n_trials - j->done);
 }
 
 int server_grow(fg_server *s, int n) {
@@ -554,9 +594,8 @@ int server_grow(fg_server *s, int n) {
 }
 
 int server_admit(fg_server *s, fg_job *j) {
-    const int64_t rt = std::min<int64_t>(j->n_trials, std::max<int64_t>((int64_t)j->ids.size(),
-                                                                       s->round_pairs / std::max<size_t>(j->ids.size(), 1)));
-    j->bytes = job_bytes(j->P, (int)j->ids.size(), std::min<int64_t>(rt, 1 << 20));
+    const int64_t rt = std::min<int64_t>(j->n_trials, round_trials_for(s, (int64_t)j->ids.size()));
+    j->bytes = job_bytes(j->P, (int)j->ids.size(), rt);
     if (s->used + (int64_t)j->bytes > s->max_bytes) return 1;   // does not fit now
     fg_system *h = nullptr;
     int rc = fg_create(&j->P, (int)j->ids.size(), &h);
@@ -607,6 +646,7 @@ int fg_server_destroy(fg_server *s) {
     if (s->d_descs) cudaFree(s->d_descs);
     if (s->d_gather) cudaFree(s->d_gather);
     if (s->d_counts) cudaFree(s->d_counts);
+    s->dh.release();
     if (s->stream2) {
         cudaStreamSynchronize(s->stream2);
         cudaStreamDestroy(s->stream2);
@@ -627,7 +667,7 @@ int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const dou
         return fail(FG_ERR_INVALID, "unsupported model");
     for (fg_job *o : s->jobs)
         if (o->P.model != params->model) return fail(FG_ERR_INVALID, "one model per server");
-    const int64_t rt = std::min<int64_t>(n_trials, std::min<int64_t>(std::max<int64_t>(n, s->round_pairs / n), 1 << 20));
+    const int64_t rt = std::min<int64_t>(n_trials, round_trials_for(s, n));
     if ((int64_t)job_bytes(*params, n, rt) > s->max_bytes) return fail(FG_ERR_CAPACITY, "job larger than the budget");
     fg_job *j = new fg_job();
     j->id = s->next_id++;
@@ -644,7 +684,7 @@ int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const dou
 
 // One round: admit queued jobs that fit the memory budget (in submission
 // order), give every running job its next chunk of trials (about
-// round_pairs / N trials, at least one sweep) and run them all in one launch
+// round_pairs / N trials) and run them all in one launch
 // of the persistent sweep kernel, then retire finished jobs.
 int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double *device_ms) {
     if (!s) return fail(FG_ERR_INVALID, "null server");
@@ -666,7 +706,11 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
     if (run.empty()) return FG_OK;
     // jobs of one kernel variant run in one launch; variants run side by side
     // on their own streams (sizes that fit shared memory and those that do not)
+    // classic-kernel jobs first (grouped by variant), then the block-kernel
+    // (Debye-Hueckel, all-pairs) jobs as one contiguous range
     std::stable_sort(run.begin(), run.end(), [](const fg_job *a, const fg_job *b) {
+        const bool ba = dh_block_ok(a->sys), bb = dh_block_ok(b->sys);
+        if (ba != bb) return bb;
         return (const void *)sweep_fn(a->sys) < (const void *)sweep_fn(b->sys);
     });
     const int n = (int)run.size();
@@ -680,6 +724,9 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         size_t smem;
     };
     std::vector<Group> groups;
+    int first_dh = -1;
+    std::vector<int> dh_n;
+    std::vector<double> dh_w;
     for (int i = 0; i < n; i++) {
         fg_job *j = run[i];
         fg_system *h = j->sys;
@@ -692,6 +739,12 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         h->desc.skip_rebuild = 1;
         h->desc.stream_first = j->done;
         descs[i] = h->desc;
+        if (dh_block_ok(h)) {
+            if (first_dh < 0) first_dh = i;
+            dh_n.push_back(h->N);
+            dh_w.push_back((double)counts[i] * h->N);   // this round's pair evaluations
+            continue;
+        }
         const SweepFn fn = sweep_fn(h);
         if (groups.empty() || groups.back().fn != fn) groups.push_back(Group{fn, i, 0, s->threads, 0});
         Group &g = groups.back();
@@ -734,6 +787,12 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
     if (groups.size() > 1) {
         CK(cudaEventRecord(s->join, s->stream2));
         CK(cudaStreamWaitEvent(s->stream, s->join, 0));
+    }
+    if (first_dh >= 0) {
+        rc = dh_groups_build(s->dh, dh_n, dh_w);
+        if (rc) return rc;
+        rc = dh_groups_launch(s->dh, s->d_descs + first_dh, INT64_MAX, s->stream);
+        if (rc) return rc;
     }
     CK(cudaEventRecord(e1, s->stream));
     std::vector<SysScalars> sc(n);

@@ -118,7 +118,7 @@ def test_server_result_same_alone_and_mixed():
     for k in "ABC":
         (p, x, q, t), seed = jobs[k]
         n = len(x)
-        stream = min(3 * n, max(n, (1 << 18) // n)) * 40
+        stream = min(3 * n, min(max(32, (1 << 18) // n), 1 << 20)) * 40
         one_job = max(one_job, System(p, x, q, t, threads=256).device_bytes + stream)
     tight, maxr1, _ = run(["B", "A", "C"], int(1.3 * one_job))
     assert maxr1 == 1
