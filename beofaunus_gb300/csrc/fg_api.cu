@@ -372,14 +372,27 @@ struct DhGroups {
     }
 };
 
+int dh_groups_build_c(DhGroups &g, const std::vector<int> &N, const std::vector<int> &C);
+
 int dh_groups_build(DhGroups &g, const std::vector<int> &N, const std::vector<double> &w) {
+    return dh_groups_build_c(g, N, dh_block_ctas_many(N, w));
+}
+
+// Largest CTA count a system of N particles is given (>= 256 particles per CTA).
+int dh_block_ctas_cap(int N) {
+    const int maxc = dh_block_max_cluster();
+    int C = 1;
+    while (2 * C <= maxc && N / (2 * C) >= 256) C *= 2;
+    return C;
+}
+
+int dh_groups_build_c(DhGroups &g, const std::vector<int> &N, const std::vector<int> &C) {
     if (g.d_members) cudaFree(g.d_members);
     g.d_members = nullptr;
     g.C.clear();
     g.mem.clear();
     g.maxN.clear();
     g.offset.clear();
-    const std::vector<int> C = dh_block_ctas_many(N, w);
     for (size_t i = 0; i < N.size(); i++) {
         size_t k = 0;
         while (k < g.C.size() && g.C[k] != C[i]) k++;

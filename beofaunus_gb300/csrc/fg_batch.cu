@@ -579,6 +579,11 @@ int64_t round_trials_of(const fg_server *s, const fg_job *j) {
     const int64_t N = j->sys ? j->sys->N : (int64_t)j->ids.size();
     return std::min<int64_t>(round_trials_for(s, N), j->n_trials - j->done);
 }
+// Block-kernel jobs on C CTAs do C times the work of a round.
+int64_t round_trials_dh(const fg_server *s, int64_t N, int C, int64_t remaining) {
+    int64_t t = std::max<int64_t>(32, (int64_t)C * s->round_pairs / std::max<int64_t>(N, 1));
+    return std::min<int64_t>(std::min<int64_t>(t, 1 << 20), remaining);
+}
 
 int server_grow(fg_server *s, int n) {
     if (n <= s->cap) return FG_OK;
@@ -594,7 +599,10 @@ int server_grow(fg_server *s, int n) {
 }
 
 int server_admit(fg_server *s, fg_job *j) {
-    const int64_t rt = std::min<int64_t>(j->n_trials, round_trials_for(s, (int64_t)j->ids.size()));
+    const int64_t Nj = (int64_t)j->ids.size();
+    const bool blk = j->P.model == FG_MODEL_DH_LJ && !j->P.use_cell_list;
+    const int64_t rt = blk ? round_trials_dh(s, Nj, dh_block_ctas_cap((int)Nj), j->n_trials)
+                           : std::min<int64_t>(j->n_trials, round_trials_for(s, Nj));
     j->bytes = job_bytes(j->P, (int)j->ids.size(), rt);
     if (s->used + (int64_t)j->bytes > s->max_bytes) return 1;   // does not fit now
     fg_system *h = nullptr;
@@ -667,7 +675,9 @@ int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const dou
         return fail(FG_ERR_INVALID, "unsupported model");
     for (fg_job *o : s->jobs)
         if (o->P.model != params->model) return fail(FG_ERR_INVALID, "one model per server");
-    const int64_t rt = std::min<int64_t>(n_trials, round_trials_for(s, n));
+    const bool blk = params->model == FG_MODEL_DH_LJ && !params->use_cell_list;
+    const int64_t rt = blk ? round_trials_dh(s, n, dh_block_ctas_cap(n), n_trials)
+                           : std::min<int64_t>(n_trials, round_trials_for(s, n));
     if ((int64_t)job_bytes(*params, n, rt) > s->max_bytes) return fail(FG_ERR_CAPACITY, "job larger than the budget");
     fg_job *j = new fg_job();
     j->id = s->next_id++;
@@ -725,12 +735,23 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
     };
     std::vector<Group> groups;
     int first_dh = -1;
-    std::vector<int> dh_n;
+    std::vector<int> dh_n, dh_c;
     std::vector<double> dh_w;
+    // block-kernel jobs: CTAs in proportion to the work each has left, so the
+    // largest jobs get the most SMs; a job on C CTAs runs C rounds of work
+    for (int i = 0; i < n; i++)
+        if (dh_block_ok(run[i]->sys)) {
+            dh_n.push_back(run[i]->sys->N);
+            dh_w.push_back((double)(run[i]->n_trials - run[i]->done) * run[i]->sys->N);
+        }
+    if (!dh_n.empty()) dh_c = dh_block_ctas_many(dh_n, dh_w);
+    int k_dh = 0;
     for (int i = 0; i < n; i++) {
         fg_job *j = run[i];
         fg_system *h = j->sys;
-        counts[i] = round_trials_of(s, j);
+        counts[i] = dh_block_ok(h) ? round_trials_dh(s, h->N, std::min(dh_c[k_dh++], dh_block_ctas_cap(h->N)),
+                                                     j->n_trials - j->done)
+                                   : round_trials_of(s, j);
         rc = ensure_trials(h, counts[i], false);
         if (rc) return rc;
         h->n_trials = counts[i];
@@ -741,8 +762,6 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         descs[i] = h->desc;
         if (dh_block_ok(h)) {
             if (first_dh < 0) first_dh = i;
-            dh_n.push_back(h->N);
-            dh_w.push_back((double)counts[i] * h->N);   // this round's pair evaluations
             continue;
         }
         const SweepFn fn = sweep_fn(h);
@@ -789,7 +808,8 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         CK(cudaStreamWaitEvent(s->stream, s->join, 0));
     }
     if (first_dh >= 0) {
-        rc = dh_groups_build(s->dh, dh_n, dh_w);
+        for (size_t k = 0; k < dh_c.size(); k++) dh_c[k] = std::min(dh_c[k], dh_block_ctas_cap(dh_n[k]));
+        rc = dh_groups_build_c(s->dh, dh_n, dh_c);
         if (rc) return rc;
         rc = dh_groups_launch(s->dh, s->d_descs + first_dh, INT64_MAX, s->stream);
         if (rc) return rc;

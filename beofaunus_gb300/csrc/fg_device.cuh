@@ -70,6 +70,12 @@ __device__ __forceinline__ df warp_sum_df(df v) {
     return v;
 }
 
+// int64 -> float through two 32-bit conversions (the 64-bit conversion runs
+// on the FP64 pipe): hi * 2^32 + lo, one FMA rounding.
+__device__ __forceinline__ float i64_to_float(long long v) {
+    return fmaf((float)(int)(v >> 32), 4294967296.0f, (float)(unsigned)v);
+}
+
 // Fixed point helpers ------------------------------------------------------
 // High 32 bits of a 64-bit coordinate, rounded to nearest.
 __device__ __forceinline__ int32_t hi32(int64_t X) {

@@ -33,6 +33,11 @@ __device__ __forceinline__ unsigned blk_cluster_rank() {
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
     return r;
 }
+__device__ __forceinline__ unsigned blk_cluster_size() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
 __device__ __forceinline__ void blk_cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
@@ -121,7 +126,7 @@ __device__ __forceinline__ bool blk_far(const Move &m, int4 pj, int tj, const Sy
             S += (dn - dO) * (dn + dO);
         }
     }
-    const float dR2 = (float)S * d.s32sq;
+    const float dR2 = i64_to_float(S) * d.s32sq;
     const float rio = rsqrt_nr(r2o), rin = rsqrt_nr(r2n);
     const float ro = r2o * rio, rn = r2n * rin;
     const float dr = dR2 * blk_rcp(rn + ro);
@@ -167,6 +172,12 @@ __global__ void __launch_bounds__(kBlkThreads, 1) dh_block_kernel(const SysDesc 
     extern __shared__ __align__(16) unsigned char blk_smem_raw[];
     __shared__ __align__(16) SysDesc sd;
     const int sys = members ? members[blockIdx.x / C] : (int)(blockIdx.x / C);
+    // launch-shape check: the partial sums are read from C CTAs of this
+    // cluster; anything else records an error and touches no other CTA
+    if (CLUSTER ? (int)blk_cluster_size() != C : C != 1) {
+        if (threadIdx.x == 0) atomicOr(&descs[sys].sc->error, kErrLaunch);
+        return;
+    }
     const int rank = CLUSTER ? (int)blk_cluster_rank() : 0;
     load_desc(sd, descs + sys);
     const SysDesc &d = sd;

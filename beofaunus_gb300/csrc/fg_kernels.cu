@@ -231,7 +231,7 @@ __device__ __forceinline__ void move_setup(Move &m, int i, const int64_t xo[3], 
         m.eo[a] = ext16(xo[a]);
         m.en[a] = ext16(xn[a]);
         int64_t dd = (int64_t)((uint64_t)xn[a] - (uint64_t)xo[a]);
-        m.dxf[a] = (float)dd * d.dl32[a];
+        m.dxf[a] = i64_to_float(dd) * d.dl32[a];
     }
     if (d.use_cells) {
         m.co = cell_of(m.ho, d);
@@ -262,7 +262,7 @@ __device__ __forceinline__ void pair_candidate(const Move &m, int4 pj, int tj, c
             long long dn = (int)(pjv[a] - m.hn[a]), dO = (int)(pjv[a] - m.ho[a]);
             S += (dn - dO) * (dn + dO);
         }
-        const float dR2 = (float)S * d.s32sq;
+        const float dR2 = i64_to_float(S) * d.s32sq;
         const float ro = sqrtf(r2o), rn = sqrtf(r2n);
         const float dr = dR2 / (rn + ro);
         const float z = fmaf(-d.kappa, dr, -log1pf(dr / ro));
@@ -289,7 +289,7 @@ __device__ __forceinline__ void pair_candidate(const Move &m, int4 pj, int tj, c
         }
         // DH: u_n/u_o - 1 = (expm1(-kappa dr) - t)/(1 + t), t = dr/r_o, with
         // expm1 by its Taylor series (|kappa dr| is small) or expm1f.
-        const float dR2 = (float)S * d.s32sq;
+        const float dR2 = i64_to_float(S) * d.s32sq;
         const float rio = rsqrt_nr(r2o), rin = rsqrt_nr(r2n);
         const float ro = r2o * rio, rn = r2n * rin;
         const float dr = dR2 * __frcp_rn(rn + ro);

@@ -50,6 +50,7 @@ constexpr int kMaxCluster = 16;
 
 // Error bits
 constexpr int kMolErrNonFinite = 8;
+constexpr int kMolErrLaunch = 64;   // launched with another cluster shape than requested
 
 struct MolTrial {
     int32_t g;       // molecule index
@@ -109,6 +110,11 @@ struct alignas(16) MolDesc {
 __device__ __forceinline__ unsigned cluster_rank() {
     unsigned r;
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
     return r;
 }
 __device__ __forceinline__ void cluster_barrier() {
@@ -257,7 +263,7 @@ __device__ __forceinline__ float dr2_exact(int4 pn, int4 po, int4 pj, const MolD
         long long S = 0;
 #pragma unroll
         for (int a = 0; a < 3; a++) S += ((long long)dn[a] - dO[a]) * ((long long)dn[a] + dO[a]);
-        return (float)S * d.s32sq;
+        return fg::i64_to_float(S) * d.s32sq;
     }
     double S = 0.0;
 #pragma unroll
@@ -550,6 +556,11 @@ __global__ void __launch_bounds__(kMolThreads, 1) mol_sweep_kernel(const MolDesc
     extern __shared__ __align__(16) unsigned char mol_smem_raw[];
     const int C = CLUSTER ? (int)descs[0].C : 1;
     const int sys = blockIdx.x / C;
+    // launch-shape check: partial sums are read from C CTAs of this cluster
+    if (CLUSTER && (int)cluster_size() != C) {
+        if (threadIdx.x == 0) atomicOr(&descs[sys].sc->error, kMolErrLaunch);
+        return;
+    }
     const int rank = CLUSTER ? (int)cluster_rank() : 0;
     const MolDesc &d = descs[sys];
     const int tid = threadIdx.x, lane = tid & 31;
