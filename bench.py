@@ -208,17 +208,26 @@ class CpuPath:
     reference runs would be. ``kinds`` gives each process its workload kind
     (cycled)."""
 
-    def __init__(self, kinds, cores=None):
+    def __init__(self, kinds, weights=None, cores=None):
         from oracle import oracle
         oracle.build()
         self.cores = cores or os.cpu_count() or 1
         self.kinds = [kinds[c % len(kinds)] for c in range(self.cores)]
+        self.weights = None if weights is None else [weights[c % len(weights)] for c in range(self.cores)]
         self.pool = mp.get_context("spawn").Pool(self.cores)
 
     def sample(self, seconds):
+        """Trial rate of all cores. Identical systems: the sum of per-process
+        rates. A mix of system sizes (weights = each kind's share of the
+        workload's trials): cores / (weighted mean time per trial), i.e. the
+        rate at which the cores clear that mix."""
         res = self.pool.map(_cpu_task, [(k, 1000 + c, seconds) for c, k in enumerate(self.kinds)], chunksize=1)
-        rate = sum(n / t for n, t in res)
         trials = sum(n for n, _ in res)
+        if self.weights is None:
+            rate = sum(n / t for n, t in res)
+        else:
+            tau = [t / n for n, t in res]
+            rate = self.cores * sum(self.weights) / sum(w * x for w, x in zip(self.weights, tau))
         return rate, trials
 
     def close(self):
@@ -227,13 +236,14 @@ class CpuPath:
 
     def describe(self, seconds, trials):
         ks = sorted(set(self.kinds))
+        how = ("sum of per-process trial rates" if self.weights is None else
+               "cores / trial-weighted mean time per trial over the workload's size mix")
         return ("%d processes (one per host core), each its own system (%s), ~%.0f s of FP64 trials (%d in total); "
-                "value = sum of per-process trial rates" % (self.cores, ", ".join(ks[:6]) + (" ..." if len(ks) > 6 else ""),
-                                                             seconds, trials))
+                "value = %s" % (self.cores, ", ".join(ks[:6]) + (" ..." if len(ks) > 6 else ""), seconds, trials, how))
 
 
-def cpu_baseline(seconds, kinds=("rpm16k",)):
-    cp = CpuPath(list(kinds))
+def cpu_baseline(seconds, kinds=("rpm16k",), weights=None):
+    cp = CpuPath(list(kinds), weights)
     try:
         cp.sample(0.2)                      # build each process's system outside the sample
         rate, trials = cp.sample(seconds)
@@ -475,19 +485,28 @@ def _serving_sizes(n_jobs, seed=5):
     return [int(2 * round(x / 2)) for x in n], list(rng.uniform(0.8, 2.0, n_jobs))
 
 
-def cpu_kinds(workload):
-    if workload == "rpm16k":
-        return ["rpm16k"]
-    if workload == "rpm800":
-        return ["rpm800"]
-    if workload == "molecules":
-        return ["molecules"]
+def cpu_kinds(workload, cores=None):
+    """(kinds, weights) of the CPU path for a workload: the systems the host
+    processes run and, for size mixes, each one's share of the trials (16
+    quantiles of the mix; a size's trials are proportional to its N)."""
+    cores = cores or os.cpu_count() or 1
+    if workload in ("rpm16k", "rpm800", "molecules"):
+        return [workload], None
     if workload == "pt64":
-        return ["dhlj%d" % n for n in _pt_sizes()]
-    if workload == "serving":
-        sizes, temps = _serving_sizes(64)
-        return ["dhlj%d@%.3f" % (n, t) for n, t in zip(sizes, temps)]
-    raise ValueError(workload)
+        sizes = sorted(_pt_sizes())
+        temps = [1.0] * len(sizes)
+    elif workload == "serving":
+        s_, t_ = _serving_sizes(200)
+        order = sorted(range(len(s_)), key=lambda i: s_[i])
+        sizes, temps = [s_[i] for i in order], [t_[i] for i in order]
+    else:
+        raise ValueError(workload)
+    k = min(cores, len(sizes))
+    picks = [int((q + 0.5) * len(sizes) / k) for q in range(k)]
+    kinds = ["dhlj%d@%.3f" % (sizes[i], temps[i]) for i in picks]
+    # each pick stands for len(sizes)/k systems; trials per system ~ N
+    weights = [float(sizes[i]) for i in picks]
+    return kinds, weights
 
 
 WORKLOAD_NAMES = {"rpm16k": WORKLOAD, "rpm800": "rpm800_ewald_wca_batched", "pt64": "pt64_dh_lj_ladder",
@@ -583,7 +602,7 @@ def run_rpm800(args, rank, world):
                 "batched_over_plain": value / plain, "clocks": clk})
     batch.close()
     if rank == 0 and world == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("rpm800"))
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, *cpu_kinds("rpm800"))
     if rank == 0:
         print(json.dumps(out))
 
@@ -640,7 +659,7 @@ def run_pt(args, rank, world):
                   "d2h_bytes_per_step": 64 * (4 + 8 + 8 + 8)}
     batch.close()
     if rank == 0 and world == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("pt64"))
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, *cpu_kinds("pt64"))
     if rank == 0:
         print(json.dumps(out))
 
@@ -772,7 +791,7 @@ def run_molecules(args, rank, world):
     for s_ in systems:
         s_.close()
     if rank == 0 and world == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("molecules"))
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, *cpu_kinds("molecules"))
     if rank == 0:
         print(json.dumps(out))
 
@@ -830,9 +849,13 @@ def run_serving(args, rank, world):
         return finish, time.perf_counter() - t0, dev_ms
 
     total_trials = sweeps * sum(sizes)
-    # capacity: everything at t = 0
+    # capacity: everything submitted at t = 0; the sustained completion rate
+    # between 10 % and 70 % of the jobs done (the start-up and the drain, where
+    # the GPU holds few jobs, are left out)
     fin0, span0, _ = run_stream([0.0] * n_jobs)
-    capacity = n_jobs / span0
+    f = sorted(fin0.values())
+    i10, i70 = int(0.1 * n_jobs), int(0.7 * n_jobs)
+    capacity = (i70 - i10) / max(f[i70] - f[i10], 1e-9)
     rate = 0.8 * capacity
     rng = np.random.default_rng(11)
     arrivals = list(np.cumsum(rng.exponential(1.0 / rate, n_jobs)))
@@ -845,6 +868,8 @@ def run_serving(args, rank, world):
     cfg = {"workload": WORKLOAD_NAMES["serving"], "jobs": n_jobs, "n_range": [256, 16384],
            "temperature_range": [0.8, 2.0], "sweeps_per_job": sweeps, "sweeps_per_job_named": 2000,
            "arrival": "Poisson at 0.8 x measured capacity", "capacity_jobs_per_s": capacity,
+           "capacity_definition": "completions per s between 10% and 70% of jobs done, all submitted at t=0",
+           "all_at_once_makespan_s": span0,
            "device_budget_GiB": args.serve_gib, "round_pairs": args.round_pairs}
     out = base_line(value, 1, 1, 1e3 * span, world, cfg, "f32 pair terms; df sums",
                     "synthetic (seeded overlap-free starts, Philox streams per job)")
@@ -854,7 +879,7 @@ def run_serving(args, rank, world):
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(sum(24 * n + 16 for n in sizes)),
                         "d2h_bytes_per_step": int(sum(24 * n for n in sizes))}})
     if rank == 0 and world == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, cpu_kinds("serving"))
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, *cpu_kinds("serving"))
     if rank == 0:
         print(json.dumps(out))
 
@@ -863,7 +888,7 @@ def run_reference(args):
     """The reference's CPU path on the host cores: the FP64 oracle port (the
     reference binary built from source is x86-only here and does not travel)."""
     warm, steps = args.warmup, args.steps
-    cp = CpuPath(cpu_kinds(args.workload))
+    cp = CpuPath(*cpu_kinds(args.workload))
     try:
         cp.sample(0.2)
         for _ in range(warm):
@@ -900,7 +925,7 @@ def main():
     ap.add_argument("--trials", type=int, default=0, help="trials per system per step (default: one sweep)")
     ap.add_argument("--cluster", type=int, default=4, help="molecules: CTAs per system")
     ap.add_argument("--pt-sweeps", type=int, default=100, help="pt64: sweeps between swaps")
-    ap.add_argument("--jobs", type=int, default=120, help="serving: jobs in the stream")
+    ap.add_argument("--jobs", type=int, default=200, help="serving: jobs in the stream")
     ap.add_argument("--job-sweeps", type=int, default=20, help="serving: sweeps per job")
     ap.add_argument("--serve-gib", type=float, default=8.0, help="serving: device budget for jobs")
     ap.add_argument("--round-pairs", type=int, default=1 << 24, help="serving: pair evaluations per job per round")

@@ -58,8 +58,12 @@ struct BlkSmem {
     uint32_t *col;   // [32] earlier trials of the block on the same particle
     float2 *corr;    // [32][32] c(a, m) as df
     float2 *part;    // [2][32] this CTA's partial sums (double-buffered)
-    int *info;       // [4]: trials resolved in the block, decisions bitmask
+    int *info;       // [4]: trials resolved in the block, decisions bitmask, queue length
+    uint32_t *queue; // near pairs (trial << 24 | slice index), evaluated densely after the sums
+    unsigned long long *fix;  // [32] near-pair sums per trial, fixed point 2^-40
 };
+
+constexpr int kBlkQueue = 2048;
 
 __host__ __device__ inline size_t blk_align(size_t x) { return (x + 15) & ~(size_t)15; }
 
@@ -69,6 +73,7 @@ __host__ __device__ inline size_t blk_smem_bytes(int ns, bool slice) {
     o += blk_align(sizeof(Move) * kBlkTrials);
     o += blk_align(8 * kBlkTrials) + blk_align(4 * kBlkTrials);
     o += blk_align(8 * kBlkTrials * kBlkTrials) + blk_align(8 * 2 * kBlkTrials) + 16;
+    o += blk_align(4 * 2048) + blk_align(8 * kBlkTrials);
     return o;
 }
 
@@ -87,8 +92,23 @@ __device__ inline BlkSmem blk_carve(unsigned char *b, int ns, bool slice) {
     s.col = (uint32_t *)(b + o); o += blk_align(4 * kBlkTrials);
     s.corr = (float2 *)(b + o); o += blk_align(8 * kBlkTrials * kBlkTrials);
     s.part = (float2 *)(b + o); o += blk_align(8 * 2 * kBlkTrials);
-    s.info = (int *)(b + o);
+    s.info = (int *)(b + o); o += 16;
+    s.queue = (uint32_t *)(b + o); o += blk_align(4 * 2048);
+    s.fix = (unsigned long long *)(b + o);
     return s;
+}
+
+// df -> fixed point (2^-40) and back, for order-independent sums of near pairs
+__device__ __forceinline__ unsigned long long blk_to_fix(df v) {
+    const long long a = __float2ll_rn(v.hi * 1099511627776.0f);
+    const long long b = __float2ll_rn(v.lo * 1099511627776.0f);
+    return (unsigned long long)(a + b);
+}
+__device__ __forceinline__ df blk_from_fix(unsigned long long u) {
+    const long long v = (long long)u;
+    const float h = i64_to_float(v);
+    const long long r = v - __float2ll_rn(h);
+    return fast_two_sum(h * 9.094947017729282e-13f, i64_to_float(r) * 9.094947017729282e-13f);
 }
 
 __device__ __forceinline__ float blk_rcp(float x) {
@@ -163,6 +183,26 @@ __device__ __forceinline__ df blk_pair(const Move &m, int4 pj, int tj, const sho
     return df_add_f(ad, a);
 }
 
+// Warp-aggregated append to the near-pair queue; true = the queue is full and
+// the lane evaluates its pair in place.
+__device__ __forceinline__ bool blk_enqueue(const BlkSmem &s, bool near, uint32_t code) {
+    const unsigned active = __activemask();
+    const unsigned m = __ballot_sync(active, near);
+    if (!m) return false;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&s.info[2], __popc(m));
+    base = __shfl_sync(active, base, leader);
+    if (!near) return false;
+    const int slot = base + __popc(m & ((1u << lane) - 1u));
+    if (slot < kBlkQueue) {
+        s.queue[slot] = code;
+        return false;
+    }
+    return true;
+}
+
 // One cluster of C CTAs per system; system members[blockIdx.x / C] of descs
 // (members == nullptr: blockIdx.x / C). C == 1 runs without a cluster.
 template <bool SLICE, bool CLUSTER>
@@ -221,6 +261,8 @@ __global__ void __launch_bounds__(kBlkThreads, 1) dh_block_kernel(const SysDesc 
             if (d.kT != 1.0f) thr = dfm_f(thr, d.kT);
             s.thr[tid] = make_float2(thr.hi, thr.lo);
         }
+        if (tid < kBlkTrials) s.fix[tid] = 0ull;
+        if (tid == 0) s.info[2] = 0;
         __syncthreads();
         if (tid < kb) {
             uint32_t c = 0;
@@ -259,14 +301,36 @@ __global__ void __launch_bounds__(kBlkThreads, 1) dh_block_kernel(const SysDesc 
                 const int ta = SLICE ? s.stype[jj] : d.ptype[ja];
                 const int4 pb = vb ? (SLICE ? s.spos[jj + 32] : d.pos4[jb]) : pa;
                 const int tb = vb ? (SLICE ? s.stype[jj + 32] : d.ptype[jb]) : ta;
-                if (ja != mv.i && !blk_far(mv, pa, ta, d, kl2e, accf))
+                // pairs inside 2 sigma go to the queue (evaluated densely below)
+                const bool na = ja != mv.i && !blk_far(mv, pa, ta, d, kl2e, accf);
+                const bool nb = vb && jb != mv.i && !blk_far(mv, pb, tb, d, kl2e, accf2);
+                if (blk_enqueue(s, na, ((uint32_t)m << 24) | (uint32_t)jj))
                     pair_candidate<MODEL_DHLJ>(mv, pa, ta, SLICE ? &s.sext[jj] : &d.pos_ext[ja], d, accf, accd);
-                if (vb && jb != mv.i && !blk_far(mv, pb, tb, d, kl2e, accf2))
+                if (blk_enqueue(s, nb, ((uint32_t)m << 24) | (uint32_t)(jj + 32)))
                     pair_candidate<MODEL_DHLJ>(mv, pb, tb, SLICE ? &s.sext[jj + 32] : &d.pos_ext[jb], d, accf2,
                                                accd);
             }
             const df p = warp_sum_df(df_add_f(df_add_f(accd, accf), accf2));
             if (lane == 0) s.part[slot * kBlkTrials + m] = make_float2(p.hi, p.lo);
+        }
+        __syncthreads();
+        {
+            const int nq = min(s.info[2], kBlkQueue);
+            for (int e = tid; e < nq; e += blockDim.x) {
+                const uint32_t q = s.queue[e];
+                const int m = (int)(q >> 24), jj = (int)(q & 0xFFFFFF);
+                const int j = j0 + jj;
+                const int4 pj = SLICE ? s.spos[jj] : d.pos4[j];
+                const int tj = SLICE ? s.stype[jj] : d.ptype[j];
+                const df v = blk_pair(s.mv[m], pj, tj, SLICE ? &s.sext[jj] : &d.pos_ext[j], d);
+                atomicAdd(&s.fix[m], blk_to_fix(v));
+            }
+        }
+        __syncthreads();
+        if (tid < kb) {
+            const float2 p = s.part[slot * kBlkTrials + tid];
+            const df v = df_add(df{p.x, p.y}, blk_from_fix(s.fix[tid]));
+            s.part[slot * kBlkTrials + tid] = make_float2(v.hi, v.lo);
         }
         if (CLUSTER) blk_cluster_barrier();
         else __syncthreads();
