@@ -17,6 +17,7 @@
 #include "faunus_gb300.h"
 #include "fg_kernels.cu"
 #include "fg_dh_block.cu"
+#include "fg_ewald_block.cu"
 
 using fg::SysDesc;
 using fg::SysScalars;
@@ -189,7 +190,19 @@ using SweepFn = void (*)(const SysDesc *, int64_t, const float2 *);
 using TrialFn = void (*)(const SysDesc *, const int64_t *, float2 *, const float2 *);
 using CommitFn = void (*)(const SysDesc *, const int64_t *, const float2 *, const float2 *);
 
+// Ewald systems run the block-of-trials kernel (fg_ewald_block.cu) when its
+// shared memory fits; 512 threads per system.
+size_t ewald_block_smem(const fg_system *h) {
+    size_t off[16];
+    return fg::eb_layout(h->N, h->K, h->nc[0] * h->nc[1] * h->nc[2], h->use_cells, off);
+}
+bool ewald_block_ok(const fg_system *h) {
+    return h->model == FG_MODEL_EWALD_WCA && h->K > 0 && h->N < (1 << 24) &&
+           ewald_block_smem(h) + sizeof(SysDesc) + 1024 <= 227 * 1024;
+}
+
 SweepFn sweep_fn(const fg_system *h) {
+    if (ewald_block_ok(h)) return h->use_cells ? fg::ewald_block_kernel<true> : fg::ewald_block_kernel<false>;
     if (h->model == FG_MODEL_EWALD_WCA) {
         if (h->use_cells) return fg::sweep_kernel<fg::MODEL_EWALD, true, false>;
         if (h->pos_smem) return fg::sweep_kernel<fg::MODEL_EWALD, false, true>;
@@ -441,8 +454,8 @@ int dh_groups_launch(const DhGroups &g, const SysDesc *descs, int64_t end, cudaS
 int launch_rebuild(const SysDesc *descs, int n, int maxN, int maxK, float2 *corr, cudaStream_t st) {
     if (maxK == 0) return FG_OK;
     const int chunk = 1024;
-    dim3 g((maxK + 255) / 256, (maxN + chunk - 1) / chunk, n);
-    fg::qk_rebuild_kernel<<<g, 256, 0, st>>>(descs, chunk);
+    dim3 g((maxK + 2 * fg::kQkThreads - 1) / (2 * fg::kQkThreads), (maxN + chunk - 1) / chunk, n);
+    fg::qk_rebuild_kernel<<<g, fg::kQkThreads, 0, st>>>(descs, chunk);
     fg::qk_rebuild_finish<<<n, 1024, 0, st>>>(descs, corr);
     CK(cudaGetLastError());
     return FG_OK;
@@ -568,10 +581,17 @@ struct LaunchCfg {
     int threads;
     size_t smem;
 };
+// Threads and shared memory of the sweep launch (the per-trial kernels keep
+// sweep_threads / sweep_smem).
+int sweep_launch_threads(const fg_system *h) { return ewald_block_ok(h) ? fg::kEbThreads : sweep_threads(h); }
+size_t sweep_launch_smem(const fg_system *h) {
+    return ewald_block_ok(h) ? ewald_block_smem(h) : sweep_smem(h, h->pos_smem);
+}
+
 int sweep_config(const fg_system *h, LaunchCfg &c) {
     c.fn = sweep_fn(h);
-    c.threads = sweep_threads(h);
-    c.smem = sweep_smem(h, h->pos_smem);
+    c.threads = sweep_launch_threads(h);
+    c.smem = sweep_launch_smem(h);
     return set_smem_attr((const void *)c.fn, c.smem);
 }
 

@@ -126,8 +126,8 @@ int batch_config(fg_batch *b) {
     b->maxN = b->maxK = 0;
     for (fg_system *h : b->sys) {
         if (sweep_fn(h) != b->cfg.fn) return fail(FG_ERR_INVALID, "batch members need the same kernel variant");
-        if (b->threads == 0) T = std::max(T, sweep_threads(h));
-        sm = std::max(sm, sweep_smem(h, h->pos_smem));
+        if (b->threads == 0 || ewald_block_ok(h)) T = std::max(T, sweep_launch_threads(h));
+        sm = std::max(sm, sweep_launch_smem(h));
         b->maxN = std::max(b->maxN, h->N);
         b->maxK = std::max(b->maxK, h->K);
     }
@@ -768,8 +768,8 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         if (groups.empty() || groups.back().fn != fn) groups.push_back(Group{fn, i, 0, s->threads, 0});
         Group &g = groups.back();
         g.count++;
-        g.smem = std::max(g.smem, sweep_smem(h, h->pos_smem));
-        if (!s->threads) g.threads = std::max(g.threads, sweep_threads(h));
+        g.smem = std::max(g.smem, sweep_launch_smem(h));
+        if (!s->threads || ewald_block_ok(h)) g.threads = std::max(g.threads, sweep_launch_threads(h));
     }
     for (Group &g : groups) {
         rc = set_smem_attr((const void *)g.fn, g.smem);

@@ -86,9 +86,15 @@ __device__ __forceinline__ int32_t hi32(int64_t X) {
 // Table of cos/sin at multiples of 2*pi/256 (in shared memory) times a short
 // Taylor polynomial of the remainder angle |d| <= pi/256 (truncation < 1e-11).
 __device__ __forceinline__ float2 sincos_turns(uint32_t ph, const float2 *__restrict__ tab) {
-    uint32_t i = (ph + (1u << 23)) >> 24;
-    int32_t rem = (int32_t)(ph - (i << 24));           // in [-2^23, 2^23): exact in float
-    float d = (float)rem * kRadPerTurnUnit;
+    const uint32_t i = (ph + (1u << 23)) >> 24;
+    // rem = ph - i 2^24 in [-2^23, 2^23) is the sign-extended low 24 bits of
+    // ph; h = floor(rem / 2) enters the mantissa of 1.5 2^23 (|h| <= 2^22),
+    // so the angle is one FMA with no conversion. Folding the magic constant
+    // into the FMA shifts every angle by the same < 2e-9 rad: a global phase
+    // of all e^{ik.r}, which no energy (|Q|^2, Re conj(Q) D) can see.
+    const int32_t h = (int32_t)(ph << 8) >> 9;
+    const float d = fmaf(__int_as_float(0x4B400000 + h), 2.0f * kRadPerTurnUnit,
+                         -12582912.0f * (2.0f * kRadPerTurnUnit));
     float d2 = d * d;
     float s = fmaf(d2 * (-1.0f / 6.0f), d, d);
     float c = fmaf(d2, fmaf(d2, 1.0f / 24.0f, -0.5f), 1.0f);

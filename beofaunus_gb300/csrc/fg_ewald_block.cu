@@ -1,0 +1,506 @@
+// Ewald + WCA sweeps in blocks of trials (one CTA per system).
+//
+// Included by fg_api.cu after fg_kernels.cu (one translation unit).
+//
+// Same idea as the Debye-Hueckel block kernel (fg_dh_block.cu): a block of up
+// to 32 trials is evaluated against the configuration at the block start, and
+// one warp resolves it in order with exact corrections for the trials it
+// accepts. For Ewald the correction of trial m after an accepted trial a has
+// three parts:
+//   real space   [u(n_m,n_a) - u(o_m,n_a)] - [u(n_m,o_a) - u(o_m,o_a)]
+//   surface      2 c dM_a . dM_m                 (E_surf = c |M|^2)
+//   reciprocal   sum_k A'_k 2 Re(conj(D_a,k) D_m,k)
+// with D_m,k = q e^{ik.r_old}(e^{ik.d} - 1) the same increment the energy uses.
+// The reciprocal parts of all pairs of the block form a 32 x 32 Gram matrix
+// over k of the trials' increments; it is accumulated in 4 x 4 register tiles
+// while the increments stream through shared memory in chunks of k-vectors.
+// Q(k) itself stays the exact fixed-point sum: after the block each accepted
+// trial's integer contributions are applied in order. A trial whose particle
+// an accepted trial of the block already moved ends the block, and so does
+// the accepted trial that makes a Q(k) rebuild due (the kernel then exits for
+// the rebuild, as the one-trial kernel does).
+namespace fg {
+
+constexpr int kEbTrials = 32;
+constexpr int kEbThreads = 512;
+constexpr int kEbKc = 128;   // k-vectors per chunk
+
+struct EbSmem {
+    Smem b;          // sc_tab, qfix, kpack, cells as in the one-trial kernel; kvec here holds
+                     // {A'_k, Q(k) as float (re, im), 0}: k itself comes from the integer n
+    Move *mv;        // [32]
+    float2 *thr;     // [32] threshold (df, times kT)
+    uint32_t *col;   // [32] earlier trials on the same particle
+    int *info;       // [8] resolved count, accepted mask, rebuild
+    float2 *partR;   // [32] real-space base (df)
+    float2 *kbase;   // [32] reciprocal base (df)
+    float2 *corr;    // [32][32] real-space + surface corrections (df)
+    float *G;        // [32][32] reciprocal cross terms
+    float2 *delta;   // [kEbKc][32] increments of the current chunk
+    float2 *Mdf;     // [3] surface dipole M (df)
+};
+
+__host__ __device__ inline size_t eb_layout(int N, int K, int ncell, bool cells, size_t off[16]) {
+    size_t b = 256 * 8 + 32 * 8;            // sc_tab, red
+    off[0] = b; b += (size_t)K * 16;        // kvec
+    off[1] = b; b += (size_t)K * 16;        // qfix
+    off[2] = b; b = align16(b + (size_t)K * 4);            // kpack
+    off[3] = b; if (cells) b = align16(b + (size_t)ncell * 4);   // ccount
+    off[4] = b; if (cells) b = align16(b + (size_t)N * 4);       // pcs
+    off[5] = b; b = align16(b + sizeof(Move) * kEbTrials);      // mv
+    off[6] = b; b = align16(b + 8 * kEbTrials);                 // thr
+    off[7] = b; b = align16(b + 4 * kEbTrials);                 // col
+    off[8] = b; b = align16(b + 4 * 8);                         // info
+    off[9] = b; b = align16(b + 8 * kEbTrials);                 // partR
+    off[10] = b; b = align16(b + 8 * kEbTrials);                // kbase
+    off[11] = b; b = align16(b + 8 * kEbTrials * kEbTrials);    // corr
+    off[12] = b; b = align16(b + 4 * kEbTrials * kEbTrials);    // G
+    off[13] = b; b = align16(b + 8 * kEbKc * kEbTrials);        // delta
+    off[14] = b; b = align16(b + 8 * 3);                        // Mdf
+    off[15] = b;
+    return b;
+}
+
+__device__ inline EbSmem eb_carve(char *base, const SysDesc &d, bool cells) {
+    size_t off[16];
+    const int ncell = d.nc[0] * d.nc[1] * d.nc[2];
+    eb_layout(d.N, d.K, ncell, cells, off);
+    EbSmem s;
+    s.b.sc_tab = (float2 *)base;
+    s.b.red = (float2 *)(base + 256 * 8);
+    s.b.kvec = (float4 *)(base + off[0]);
+    s.b.qfix = (longlong2 *)(base + off[1]);
+    s.b.qf = nullptr;
+    s.b.eold = nullptr;
+    s.b.kpack = (uint32_t *)(base + off[2]);
+    s.b.pos = nullptr;
+    s.b.pos_ext = nullptr;
+    s.b.ptype = nullptr;
+    s.b.ccount = (int *)(base + off[3]);
+    s.b.pcs = (uint32_t *)(base + off[4]);
+    s.mv = (Move *)(base + off[5]);
+    s.thr = (float2 *)(base + off[6]);
+    s.col = (uint32_t *)(base + off[7]);
+    s.info = (int *)(base + off[8]);
+    s.partR = (float2 *)(base + off[9]);
+    s.kbase = (float2 *)(base + off[10]);
+    s.corr = (float2 *)(base + off[11]);
+    s.G = (float *)(base + off[12]);
+    s.delta = (float2 *)(base + off[13]);
+    s.Mdf = (float2 *)(base + off[14]);
+    return s;
+}
+
+// Real-space sum of one trial by one warp: every stencil cell (cell list) or
+// every particle (no cell list), lanes over the slots.
+template <bool CELLS>
+__device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, const Smem &s, float &accf, df &accd) {
+    const int lane = threadIdx.x & 31;
+    if (!CELLS) {
+        for (int j = lane; j < d.N; j += 32) {
+            if (j == m.i) continue;
+            pair_candidate<MODEL_EWALD>(m, d.pos4[j], d.ptype[j], &d.pos_ext[j], d, accf, accd);
+        }
+        return;
+    }
+    int co[3], cn[3], lo[3], len[3];
+    co[0] = m.co % d.nc[0]; co[1] = (m.co / d.nc[0]) % d.nc[1]; co[2] = m.co / (d.nc[0] * d.nc[1]);
+    cn[0] = m.cn % d.nc[0]; cn[1] = (m.cn / d.nc[0]) % d.nc[1]; cn[2] = m.cn / (d.nc[0] * d.nc[1]);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        int delta = cn[a] - co[a];
+        if (delta > 1) delta -= d.nc[a];
+        if (delta < -1) delta += d.nc[a];
+        if ((delta > 1 || delta < -1) && lane == 0) atomicOr(&d.sc->error, kErrStencil);
+        lo[a] = co[a] + min(delta, 0) - 1;
+        len[a] = 3 + (delta != 0 ? 1 : 0);
+    }
+    const int ncell = len[0] * len[1] * len[2];
+    // two stencil cells per pass: their loads are independent, so a warp
+    // keeps two cell records in flight (four spill at 128 registers)
+    for (int k0 = 0; k0 < ncell; k0 += 2) {
+        int cid[2], cnt[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int k = k0 + u;
+            cid[u] = 0;
+            cnt[u] = 0;
+            if (k < ncell) {
+                const int ix = k % len[0], iy = (k / len[0]) % len[1], iz = k / (len[0] * len[1]);
+                int cx = lo[0] + ix, cy = lo[1] + iy, cz = lo[2] + iz;
+                cx += (cx < 0) ? d.nc[0] : 0; cx -= (cx >= d.nc[0]) ? d.nc[0] : 0;
+                cy += (cy < 0) ? d.nc[1] : 0; cy -= (cy >= d.nc[1]) ? d.nc[1] : 0;
+                cz += (cz < 0) ? d.nc[2] : 0; cz -= (cz >= d.nc[2]) ? d.nc[2] : 0;
+                cid[u] = (cz * d.nc[1] + cy) * d.nc[0] + cx;
+                cnt[u] = s.ccount[cid[u]];
+            }
+        }
+        const int cmax = max(cnt[0], cnt[1]);
+        for (int slot = lane; slot < cmax; slot += 32) {
+            int pid[2];
+            int4 pos[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int idx = cid[u] * d.cap + slot;
+                pid[u] = slot < cnt[u] ? d.cell_pid[idx] : -1;
+                pos[u] = slot < cnt[u] ? d.cell_pos[idx] : make_int4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                if (pid[u] < 0 || (pid[u] & 0xFFFFFF) == m.i) continue;
+                pair_candidate<MODEL_EWALD>(m, pos[u], pid[u] >> 24, &d.cell_ext[cid[u] * d.cap + slot], d, accf,
+                                            accd);
+            }
+        }
+    }
+}
+
+// dU of trial m from one partner at high words p (charge bits in .w), type t,
+// extension e, as a df number.
+__device__ __forceinline__ df eb_pair(const Move &m, int4 p, int t, const short4 *e, const SysDesc &d) {
+    float a = 0.0f;
+    df ad = {0.0f, 0.0f};
+    pair_candidate<MODEL_EWALD>(m, p, t, e, d, a, ad);
+    return df_add_f(ad, a);
+}
+
+// Surface dipole change of a trial (Angstrom e), as surface_delta computes it.
+__device__ __forceinline__ void eb_dM(const Move &m, const SysDesc &d, float dM[3]) {
+    const float qe = m.q * d.eff[m.ti];
+#pragma unroll
+    for (int a = 0; a < 3; a++) dM[a] = qe * ((float)m.hn[a] * d.s32[a] - (float)m.ho[a] * d.s32[a]);
+}
+
+template <bool CELLS>
+__global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDesc *__restrict__ descs, int64_t end,
+                                                                    const float2 *__restrict__ sc_tab) {
+    extern __shared__ __align__(16) char eb_smem_raw[];
+    __shared__ __align__(16) SysDesc sd;
+    load_desc(sd, descs + blockIdx.x);
+    const SysDesc &d = sd;
+    EbSmem s = eb_carve(eb_smem_raw, d, CELLS);
+    SysScalars *sc = d.sc;
+    if (sc->rebuild_pending || sc->cursor >= min(end, sc->n_trials)) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    const int K = d.K;
+    // tables
+    for (int t = tid; t < 256; t += blockDim.x) s.b.sc_tab[t] = sc_tab[t];
+    for (int k = tid; k < K; k += blockDim.x) {
+        const longlong2 q = d.qfix[k];
+        const float2 qf = q_to_float(q);
+        s.b.kvec[k] = make_float4(d.kvec[k].w, qf.x, qf.y, 0.0f);
+        s.b.kpack[k] = d.kpack[k];
+        s.b.qfix[k] = q;
+    }
+    // 2 pi / L per axis: k.d = sum_a n_a (2 pi / L_a) d_a
+    const float tpl[3] = {6.283185307179586f / d.L[0], 6.283185307179586f / d.L[1], 6.283185307179586f / d.L[2]};
+    if (CELLS) {
+        const int ncell = d.nc[0] * d.nc[1] * d.nc[2];
+        for (int c = tid; c < ncell; c += blockDim.x) s.b.ccount[c] = d.cell_count[c];
+        for (int j = tid; j < d.N; j += blockDim.x)
+            s.b.pcs[j] = ((uint32_t)d.p_cell[j] << 12) | (uint32_t)d.p_slot[j];
+    }
+    if (tid < 3) s.Mdf[tid] = make_float2(sc->m[tid][0], sc->m[tid][1]);
+    __syncthreads();
+    int64_t cur = sc->cursor;
+    const int64_t stop = min(end, sc->n_trials);
+    df U = {sc->u_hi, sc->u_lo};
+    df Ut = {sc->utot_hi, sc->utot_lo};
+    int cnt_acc = sc->cnt_accepted;
+    int64_t nacc = sc->n_accepted;
+    const int uf = d.update_frequency;
+    bool rebuild = false;
+    int err = 0;
+    // k-space work split: 16 threads per trial, each a fixed set of k-vectors
+    const int mt = tid >> 4, sub = tid & 15;
+    // Gram tiles: 4 x 4 trial tiles on and above the diagonal (36), each split
+    // over 14 groups of k-vectors of a chunk
+    constexpr int kTiles = 36, kGroups = 14;
+    int ta = 0, tm = 0;
+    {
+        int t = tid % kTiles, r = 0;
+        while (t >= 8 - r) { t -= 8 - r; r++; }
+        ta = r;
+        tm = r + t;
+    }
+    const int tgroup = tid / kTiles;   // < kGroups for tid < 504
+    while (cur < stop) {
+        const int kb = (int)((stop - cur) < (int64_t)kEbTrials ? (stop - cur) : (int64_t)kEbTrials);
+        // ---- trials of the block (old coordinates: the block start)
+        if (tid < kb) {
+            const Trial tr = d.trials[cur + tid];
+            int64_t xo[3], xn[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                xo[a] = d.pos64[3 * tr.idx + a];
+                xn[a] = (int64_t)((uint64_t)xo[a] + (uint64_t)tr.d[a]);
+            }
+            Move m;
+            move_setup(m, tr.idx, xo, xn, __int_as_float(d.pos4[tr.idx].w), d.ptype[tr.idx], d);
+            s.mv[tid] = m;
+            df thr = {tr.thr_hi, tr.thr_lo};
+            if (d.kT != 1.0f) thr = dfm_f(thr, d.kT);
+            s.thr[tid] = make_float2(thr.hi, thr.lo);
+        }
+        __syncthreads();
+        if (tid < kb) {
+            uint32_t c = 0;
+            const int i = s.mv[tid].i;
+            for (int a = 0; a < tid; a++)
+                if (s.mv[a].i == i) c |= 1u << a;
+            s.col[tid] = c;
+        }
+        // ---- real-space and surface corrections c(a, m), a < m
+        for (int e = tid; e < kEbTrials * kEbTrials; e += blockDim.x) {
+            const int a = e / kEbTrials, m = e - a * kEbTrials;
+            float2 out = make_float2(0.0f, 0.0f);
+            if (a < m && m < kb && s.mv[a].i != s.mv[m].i) {
+                const Move &A = s.mv[a];
+                const Move &Mm = s.mv[m];
+                const int4 pn = make_int4(A.hn[0], A.hn[1], A.hn[2], __float_as_int(A.q));
+                const int4 po = make_int4(A.ho[0], A.ho[1], A.ho[2], __float_as_int(A.q));
+                const short4 en = make_short4((short)A.en[0], (short)A.en[1], (short)A.en[2], 0);
+                const short4 eo = make_short4((short)A.eo[0], (short)A.eo[1], (short)A.eo[2], 0);
+                df c = df_add(eb_pair(Mm, pn, A.ti, &en, d), df_neg(eb_pair(Mm, po, A.ti, &eo, d)));
+                if (d.surf_c != 0.0f) {
+                    float da[3], dm[3];
+                    eb_dM(A, d, da);
+                    eb_dM(Mm, d, dm);
+                    c = df_add_f(c, 2.0f * d.surf_c * fmaf(da[0], dm[0], fmaf(da[1], dm[1], da[2] * dm[2])));
+                }
+                out = make_float2(c.hi, c.lo);
+            }
+            s.corr[e] = out;
+        }
+        // ---- real-space base: warp w sums trials w, w + nwarp, ...
+        for (int m = warp; m < kb; m += nwarp) {
+            const Move mv = s.mv[m];
+            float accf = 0.0f;
+            df accd = {0.0f, 0.0f};
+            eb_pairs_warp<CELLS>(mv, d, s.b, accf, accd);
+            const df p = warp_sum_df(df_add_f(accd, accf));
+            if (lane == 0) s.partR[m] = make_float2(p.hi, p.lo);
+        }
+        // ---- reciprocal base and Gram matrix, streaming the increments by chunks
+        int hm[3] = {0, 0, 0}, hn3[3] = {0, 0, 0};
+        float dxs[3] = {0.0f, 0.0f, 0.0f}, qe = 0.0f;   // displacement times 2 pi / L
+        if (mt < kb) {
+            const Move &M = s.mv[mt];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                hm[a] = M.ho[a];
+                hn3[a] = M.hn[a];
+                dxs[a] = M.dxf[a] * tpl[a];
+            }
+            qe = M.q * d.eff[M.ti];
+        }
+        float kacc = 0.0f;
+        float g[4][4];
+#pragma unroll
+        for (int x = 0; x < 4; x++)
+#pragma unroll
+            for (int y = 0; y < 4; y++) g[x][y] = 0.0f;
+        for (int kc0 = 0; kc0 < K; kc0 += kEbKc) {
+            __syncthreads();   // the previous chunk's Gram reads are done
+            for (int kl = sub; kl < kEbKc; kl += 16) {
+                const int k = kc0 + kl;
+                float2 dd = make_float2(0.0f, 0.0f);
+                if (mt < kb && k < K) {
+                    int nx, ny, nz;
+                    unpack_n(s.b.kpack[k], nx, ny, nz);
+                    const uint32_t ph = phase(nx, ny, nz, hm);
+                    const float2 e = sincos_turns(ph, s.b.sc_tab);
+                    const float4 kv = s.b.kvec[k];   // {A', Re Q, Im Q, 0}
+                    const float phi = fmaf(small_int_to_float(nx), dxs[0],
+                                           fmaf(small_int_to_float(ny), dxs[1], small_int_to_float(nz) * dxs[2]));
+                    float2 w;
+                    if (fabsf(phi) <= 1.6f) {
+                        w = expm1_i_horner(phi);
+                    } else {
+                        const float2 en = sincos_turns(phase(nx, ny, nz, hn3) - ph, s.b.sc_tab);
+                        w = make_float2(en.x - 1.0f, en.y);
+                    }
+                    dd = cmul(e, w);
+                    dd.x *= qe;
+                    dd.y *= qe;
+                    kacc = fmaf(kv.x, fmaf(2.0f, fmaf(kv.y, dd.x, kv.z * dd.y), fmaf(dd.x, dd.x, dd.y * dd.y)), kacc);
+                }
+                s.delta[kl * kEbTrials + mt] = dd;
+            }
+            __syncthreads();
+            if (tid < kTiles * kGroups) {
+                const int kend = min(kEbKc, K - kc0);
+                for (int kl = tgroup; kl < kend; kl += kGroups) {
+                    const float A = s.b.kvec[kc0 + kl].x;
+                    const float2 *row = s.delta + kl * kEbTrials;
+                    float2 va[4], vm[4];
+#pragma unroll
+                    for (int x = 0; x < 4; x++) {
+                        va[x] = row[4 * ta + x];
+                        vm[x] = row[4 * tm + x];
+                    }
+#pragma unroll
+                    for (int x = 0; x < 4; x++) {
+                        const float ax = A * va[x].x, ay = A * va[x].y;
+#pragma unroll
+                        for (int y = 0; y < 4; y++) g[x][y] = fmaf(ax, vm[y].x, fmaf(ay, vm[y].y, g[x][y]));
+                    }
+                }
+            }
+        }
+        // reciprocal base: the 16 threads of trial mt, in df
+        {
+            df v = {kacc, 0.0f};
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1) {
+                df w;
+                w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+                w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+                v = df_add(v, w);
+            }
+            if (sub == 0 && mt < kEbTrials) s.kbase[mt] = make_float2(v.hi, v.lo);
+        }
+        // Gram tiles: the k groups' partial tiles meet in the (now free) chunk
+        // buffer and are summed in a fixed order, so the result does not
+        // depend on timing
+        __syncthreads();
+        float *P = reinterpret_cast<float *>(s.delta);   // [kGroups][kTiles][16]
+        if (tid < kTiles * kGroups) {
+            const int tile = tid % kTiles;
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+                for (int y = 0; y < 4; y++) P[(tgroup * kTiles + tile) * 16 + 4 * x + y] = g[x][y];
+        }
+        __syncthreads();
+        for (int e = tid; e < kTiles * 16; e += blockDim.x) {
+            const int tile = e >> 4, xy = e & 15;
+            float v = 0.0f;
+            for (int gg = 0; gg < kGroups; gg++) v += P[(gg * kTiles + tile) * 16 + xy];
+            int t = tile, r = 0;
+            while (t >= 8 - r) { t -= 8 - r; r++; }
+            s.G[(4 * r + (xy >> 2)) * kEbTrials + 4 * (r + t) + (xy & 3)] = 2.0f * v;
+        }
+        __syncthreads();
+        // ---- resolve the block in order (warp 0; lane m = trial m)
+        if (warp == 0) {
+            df S = {0.0f, 0.0f};
+            float dMl[3] = {0.0f, 0.0f, 0.0f};
+            if (lane < kb) {
+                const float2 r = s.partR[lane], kk = s.kbase[lane];
+                S = df_add(df{r.x, r.y}, df{kk.x, kk.y});
+                const df Mb[3] = {{s.Mdf[0].x, s.Mdf[0].y}, {s.Mdf[1].x, s.Mdf[1].y}, {s.Mdf[2].x, s.Mdf[2].y}};
+                S = df_add(S, surface_delta(s.mv[lane], d, Mb, dMl));
+            }
+            const uint32_t colm = lane < kb ? s.col[lane] : 0u;
+            const float2 th = lane < kb ? s.thr[lane] : make_float2(0.0f, 0.0f);
+            uint32_t accm = 0;
+            int done = kb;
+            for (int a = 0; a < kb; a++) {
+                const bool coll = __shfl_sync(0xffffffffu, (colm & accm) != 0u ? 1 : 0, a) != 0;
+                if (coll) {
+                    done = a;
+                    break;
+                }
+                const df du = {__shfl_sync(0xffffffffu, S.hi, a), __shfl_sync(0xffffffffu, S.lo, a)};
+                const df t = {__shfl_sync(0xffffffffu, th.x, a), __shfl_sync(0xffffffffu, th.y, a)};
+                const bool nan = !(du.hi == du.hi);
+                // Movebase::metropolis (move.h:567-573): reject iff dU > kT (-ln u);
+                // a NaN dU compares false there: accepted
+                const bool acc = nan || !df_gt(du, t);
+                if (nan) err |= kErrNonFinite;
+                if (lane == 0 && d.log_trials) {
+                    d.trial_du[cur + a] = make_float2(du.hi, du.lo);
+                    d.trial_acc[cur + a] = acc ? 1 : 0;
+                }
+                if (acc) {
+                    accm |= 1u << a;
+                    U = df_add(U, du);
+                    Ut = df_add(Ut, du);
+                    nacc++;
+                    if (lane > a && lane < kb) {
+                        const float2 c = s.corr[a * kEbTrials + lane];
+                        S = df_add(df_add(S, df{c.x, c.y}), df{s.G[a * kEbTrials + lane], 0.0f});
+                    }
+                    // NonbondedEwald::update (ewald.h:633): a rebuild after
+                    // update_frequency accepted trials ends the block here
+                    if (++cnt_acc > uf - 1) {
+                        cnt_acc = 0;
+                        if (!d.skip_rebuild) {
+                            rebuild = true;
+                            done = a + 1;
+                            break;
+                        }
+                    }
+                }
+            }
+            if (lane == 0) {
+                s.info[0] = done;
+                s.info[1] = (int)accm;
+                s.info[2] = rebuild ? 1 : 0;
+                s.info[3] = cnt_acc;
+            }
+        }
+        __syncthreads();
+        const int done = s.info[0];
+        const uint32_t accm = (uint32_t)s.info[1];
+        rebuild = s.info[2] != 0;
+        cnt_acc = s.info[3];
+        // ---- apply the accepted trials in order
+        if (tid == 0) {
+            df M[3] = {{s.Mdf[0].x, s.Mdf[0].y}, {s.Mdf[1].x, s.Mdf[1].y}, {s.Mdf[2].x, s.Mdf[2].y}};
+            for (int a = 0; a < done; a++) {
+                if (!((accm >> a) & 1u)) continue;
+                commit_position(s.mv[a], d, s.b, false, CELLS);
+                float dm[3];
+                eb_dM(s.mv[a], d, dm);
+#pragma unroll
+                for (int x = 0; x < 3; x++) M[x] = df_add_f(M[x], dm[x]);
+            }
+#pragma unroll
+            for (int x = 0; x < 3; x++) s.Mdf[x] = make_float2(M[x].hi, M[x].lo);
+        }
+        if (accm & ((done >= 32) ? 0xffffffffu : ((1u << done) - 1u))) {
+            for (int k = tid; k < K; k += blockDim.x) {
+                int nx, ny, nz;
+                unpack_n(s.b.kpack[k], nx, ny, nz);
+                longlong2 q = s.b.qfix[k];
+                for (int a = 0; a < done; a++) {
+                    if (!((accm >> a) & 1u)) continue;
+                    const Move &A = s.mv[a];
+                    const float qa = A.q * d.eff[A.ti];
+                    const int2 cn = qk_contrib(qa, sincos_turns(phase(nx, ny, nz, A.hn), s.b.sc_tab));
+                    const int2 co = qk_contrib(qa, sincos_turns(phase(nx, ny, nz, A.ho), s.b.sc_tab));
+                    q.x += (long long)cn.x - (long long)co.x;
+                    q.y += (long long)cn.y - (long long)co.y;
+                }
+                s.b.qfix[k] = q;
+                const float2 qf = q_to_float(q);
+                s.b.kvec[k].y = qf.x;
+                s.b.kvec[k].z = qf.y;
+            }
+        }
+        cur += done;
+        __syncthreads();
+        if (rebuild) break;
+    }
+    // write back Q(k), cells and the scalars
+    store_back(d, s.b, true, CELLS);
+    if (tid == 0) {
+        sc->cursor = cur;
+        sc->u_hi = U.hi;
+        sc->u_lo = U.lo;
+        sc->utot_hi = Ut.hi;
+        sc->utot_lo = Ut.lo;
+        sc->n_accepted = nacc;
+        for (int a = 0; a < 3; a++) {
+            sc->m[a][0] = s.Mdf[a].x;
+            sc->m[a][1] = s.Mdf[a].y;
+        }
+        sc->cnt_accepted = cnt_acc;
+        if (rebuild) sc->rebuild_pending = 1;
+        sc->error |= err;
+    }
+}
+
+}  // namespace fg

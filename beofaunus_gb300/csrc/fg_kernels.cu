@@ -855,40 +855,58 @@ __global__ void __launch_bounds__(kSweepThreads) commit_kernel(const SysDesc *__
 // updateAllComplexNumbers (ewald.h:388-415) as the exact integer sum of the
 // per-particle contributions; blockIdx.z selects the system of a batch.
 // Only systems with rebuild_pending set do work.
-__global__ void __launch_bounds__(256) qk_rebuild_kernel(const SysDesc *__restrict__ descs, int chunk) {
+// Each thread owns two k-vectors (kQkThreads threads, 2 kQkThreads k per
+// block) so one broadcast of a particle serves two phase evaluations; the
+// charge is staged as 2^28 q eff, which leaves qk_contrib's product unchanged
+// (scaling by a power of two is exact).
+constexpr int kQkThreads = 128;
+constexpr int kQkStage = 256;   // particles staged per pass
+__global__ void __launch_bounds__(kQkThreads) qk_rebuild_kernel(const SysDesc *__restrict__ descs, int chunk) {
     __shared__ float2 tab[256];
-    __shared__ int4 pj[256];
-    __shared__ float qe[256];
+    __shared__ int4 pj[kQkStage];
+    __shared__ float qe[kQkStage];
     const SysDesc &d = descs[blockIdx.z];
     if (d.K == 0 || d.sc->rebuild_pending == 0) return;
     const int j0 = blockIdx.y * chunk, j1 = min(d.N, j0 + chunk);
     if (j0 >= d.N) return;
     for (int t = threadIdx.x; t < 256; t += blockDim.x) tab[t] = d.sc_tab[t];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int nx = 0, ny = 0, nz = 0;
-    if (k < d.K) unpack_n(d.kpack[k], nx, ny, nz);
-    long long sx = 0, sy = 0;
-    for (int b = j0; b < j1; b += 256) {
+    const int k0 = blockIdx.x * (2 * kQkThreads) + threadIdx.x, k1 = k0 + kQkThreads;
+    int n0[3] = {0, 0, 0}, n1[3] = {0, 0, 0};
+    if (k0 < d.K) unpack_n(d.kpack[k0], n0[0], n0[1], n0[2]);
+    if (k1 < d.K) unpack_n(d.kpack[k1], n1[0], n1[1], n1[2]);
+    long long s0x = 0, s0y = 0, s1x = 0, s1y = 0;
+    for (int b = j0; b < j1; b += kQkStage) {
         __syncthreads();
-        const int j = b + threadIdx.x;
-        if (j < j1) {
-            const int4 p = d.pos4[j];
-            pj[threadIdx.x] = p;
-            qe[threadIdx.x] = __int_as_float(p.w) * d.eff[d.ptype[j]];
+        for (int t = threadIdx.x; t < kQkStage; t += kQkThreads) {
+            const int j = b + t;
+            if (j < j1) {
+                const int4 p = d.pos4[j];
+                pj[t] = p;
+                qe[t] = __int_as_float(p.w) * d.eff[d.ptype[j]] * 268435456.0f;
+            }
         }
         __syncthreads();
-        const int nb = min(256, j1 - b);
-        if (k < d.K)
+        const int nb = min(kQkStage, j1 - b);
+        if (k0 < d.K)
             for (int t = 0; t < nb; t++) {
-                const int h[3] = {pj[t].x, pj[t].y, pj[t].z};
-                const int2 c = qk_contrib(qe[t], sincos_turns(phase(nx, ny, nz, h), tab));
-                sx += c.x;
-                sy += c.y;
+                const int4 p = pj[t];
+                const int h[3] = {p.x, p.y, p.z};
+                const float q28 = qe[t];
+                const float2 e0 = sincos_turns(phase(n0[0], n0[1], n0[2], h), tab);
+                const float2 e1 = sincos_turns(phase(n1[0], n1[1], n1[2], h), tab);
+                s0x += __float2int_rn(q28 * e0.x);
+                s0y += __float2int_rn(q28 * e0.y);
+                s1x += __float2int_rn(q28 * e1.x);
+                s1y += __float2int_rn(q28 * e1.y);
             }
     }
-    if (k < d.K) {
-        atomicAdd((unsigned long long *)&d.qnew[k].x, (unsigned long long)sx);
-        atomicAdd((unsigned long long *)&d.qnew[k].y, (unsigned long long)sy);
+    if (k0 < d.K) {
+        atomicAdd((unsigned long long *)&d.qnew[k0].x, (unsigned long long)s0x);
+        atomicAdd((unsigned long long *)&d.qnew[k0].y, (unsigned long long)s0y);
+    }
+    if (k1 < d.K) {
+        atomicAdd((unsigned long long *)&d.qnew[k1].x, (unsigned long long)s1x);
+        atomicAdd((unsigned long long *)&d.qnew[k1].y, (unsigned long long)s1y);
     }
 }
 
