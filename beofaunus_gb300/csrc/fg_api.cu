@@ -94,6 +94,8 @@ struct fg_system {
     int4 *cell_pos = nullptr;
     float4 *kvec = nullptr, *core_tab = nullptr, *core_tab2 = nullptr;
     uint32_t *kpack = nullptr;
+    int2 *kseg = nullptr;
+    int nseg = 0;
     longlong2 *qfix = nullptr, *qnew = nullptr;
     SysScalars *sc = nullptr;
     float2 *trial_out = nullptr, *corr = nullptr, *pair_part = nullptr;
@@ -125,7 +127,7 @@ void free_all(fg_system *h) {
     void *ptrs[] = {h->d_desc, h->pos64, h->pos4, h->pos_ext, h->cell_ext, h->ptype, h->cell_count, h->cell_pid,
                     h->p_cell, h->p_slot, h->cell_pos, h->kvec, h->core_tab, h->core_tab2, h->kpack, h->qfix,
                     h->qnew, h->sc, h->trial_out, h->corr, h->pair_part, h->req, h->dp_fix, h->sc_tab, h->trials,
-                    h->log_du, h->log_acc};
+                    h->log_du, h->log_acc, h->kseg};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -182,7 +184,7 @@ int sweep_threads(const fg_system *h) {
 
 size_t sweep_smem(const fg_system *h, bool pos_smem) {
     size_t off[8];
-    return fg::smem_layout(h->N, h->K, h->nc[0] * h->nc[1] * h->nc[2], h->model == FG_MODEL_EWALD_WCA, pos_smem,
+    return fg::smem_layout(h->N, h->K, h->kc, h->nc[0] * h->nc[1] * h->nc[2], h->model == FG_MODEL_EWALD_WCA, pos_smem,
                            h->use_cells, off);
 }
 
@@ -450,12 +452,22 @@ int dh_groups_launch(const DhGroups &g, const SysDesc *descs, int64_t end, cudaS
     return FG_OK;
 }
 
-// Rebuild kernels for n systems whose descriptors are at `descs` (device).
-int launch_rebuild(const SysDesc *descs, int n, int maxN, int maxK, float2 *corr, cudaStream_t st) {
-    if (maxK == 0) return FG_OK;
-    const int chunk = 1024;
-    dim3 g((maxK + 2 * fg::kQkThreads - 1) / (2 * fg::kQkThreads), (maxN + chunk - 1) / chunk, n);
-    fg::qk_rebuild_kernel<<<g, fg::kQkThreads, 0, st>>>(descs, chunk);
+// Rebuild kernels for n systems whose descriptors are at `descs` (device):
+// maxN particles, maxSeg k-vector runs and axis bound maxKcc at most.
+int launch_rebuild(const SysDesc *descs, int n, int maxN, int maxSeg, int maxKcc, float2 *corr, cudaStream_t st) {
+    if (maxSeg == 0) return FG_OK;
+    const int T = fg::qk_tab_len(maxKcc);
+    const int threads = std::min(fg::kQkMaxThreads, ((maxSeg + 31) / 32) * 32);
+    const int stage = std::max(1, std::min(fg::kQkMaxStage, 40960 / (T * 8)));
+    const size_t smem = fg::qk_rebuild_smem(stage, T, threads);
+    int rc = set_smem_attr((const void *)fg::qk_rebuild_kernel, smem);
+    if (rc) return rc;
+    // about four blocks per SM over all systems, at least 256 particles each
+    const long long want = 4LL * dh_sm_count();
+    int chunk = (int)std::max<long long>(256, ((long long)maxN * n + want - 1) / want);
+    chunk = ((chunk + stage - 1) / stage) * stage;
+    dim3 g((maxN + chunk - 1) / chunk, n);
+    fg::qk_rebuild_kernel<<<g, threads, smem, st>>>(descs, chunk, stage);
     fg::qk_rebuild_finish<<<n, 1024, 0, st>>>(descs, corr);
     CK(cudaGetLastError());
     return FG_OK;
@@ -643,7 +655,7 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
             CK(cudaEventRecord(b, h->stream));
             launches++;
             if (rebuilds) {
-                rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
+                rc = launch_rebuild(h->d_desc, 1, h->N, h->nseg, h->kc, h->corr, h->stream);
                 if (rc) return rc;
             }
         }
@@ -693,6 +705,31 @@ const char *fg_last_error(void) { return g_err.c_str(); }
 void fg_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
     fg::u4 r = fg::philox4x32_10(fg::u4{ctr[0], ctr[1], ctr[2], ctr[3]}, key[0], key[1]);
     out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+}
+
+// Largest |q eff| of the particles (charges, or the type charges when null).
+double qk_charge_bound(const fg_system *h, const double *charge) {
+    double qmax = 0;
+    if (charge) {
+        for (int i = 0; i < h->N; i++)
+            qmax = std::max(qmax, std::fabs(charge[i] * h->desc.eff[h->types[i]]));
+    } else {
+        for (int t = 0; t < h->P.n_types; t++)
+            qmax = std::max(qmax, std::fabs(h->P.type_charge[t] * h->desc.eff[t]));
+    }
+    return qmax;
+}
+
+// Grid 2^-g of the Q(k) contributions: the largest g <= 28 with
+// 2^g max|q eff| <= 2^24, so a term is at most 2^24 (plus float rounding) and
+// the 64 terms of a rebuild pass sum exactly in int32.
+int set_qk_scale(SysDesc &d, double qmax) {
+    if (!(qmax <= 16777216.0)) return FG_ERR_INVALID;
+    int g = 28;
+    while (g > 0 && std::ldexp(qmax, g) > 16777216.0) g--;
+    d.qk_scale = (float)std::ldexp(1.0, g);
+    d.qk_shift = 28 - g;
+    return FG_OK;
 }
 
 int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
@@ -793,6 +830,7 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         enumerate_k(P, n3, h->ak, kv3);
         h->K = (int)h->ak.size();
         h->kc = (int)std::ceil(P.ewald_cutoff_k);
+        if (h->kc > 127 || h->K >= (1 << 24)) return bail(fail(FG_ERR_INVALID, "k-space cutoff too large"));
         h->recip_c = 2 * PI / V * P.bjerrum;
         const double const_inf = (P.ewald_eps_surf < 1) ? 0.0 : 1.0;
         h->surf_c = const_inf * (2 * PI / ((2 * P.ewald_eps_surf + 1) * V)) * P.bjerrum;
@@ -850,6 +888,28 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         }
         cudaMemcpy(h->kvec, kv.data(), h->K * sizeof(float4), cudaMemcpyHostToDevice);
         cudaMemcpy(h->kpack, kp.data(), h->K * sizeof(uint32_t), cudaMemcpyHostToDevice);
+        // runs of consecutive k-vectors with the same (nx, ny) and consecutive
+        // nz, each cut into near-equal pieces of at most kQkRun, longest
+        // first (warps of the rebuild then run equal trip counts)
+        std::vector<int2> seg;
+        for (int k = 0; k < h->K;) {
+            int run = 1;
+            while (k + run < h->K && n3[3 * (k + run)] == n3[3 * k] && n3[3 * (k + run) + 1] == n3[3 * k + 1] &&
+                   n3[3 * (k + run) + 2] == n3[3 * k + 2] + run)
+                run++;
+            const int pieces = (run + fg::kQkRun - 1) / fg::kQkRun;
+            for (int p = 0, k0 = k; p < pieces; p++) {
+                const int len = run / pieces + (p < run % pieces ? 1 : 0);
+                seg.push_back(make_int2(k0 | (len << 24), (n3[3 * k0] & 0xFF) | ((n3[3 * k0 + 1] & 0xFF) << 8) |
+                                                              ((n3[3 * k0 + 2] & 0xFF) << 16)));
+                k0 += len;
+            }
+            k += run;
+        }
+        std::stable_sort(seg.begin(), seg.end(), [](const int2 &a, const int2 &b) { return (a.x >> 24) > (b.x >> 24); });
+        h->nseg = (int)seg.size();
+        ALLOC(h->kseg, seg.size() * sizeof(int2));
+        cudaMemcpy(h->kseg, seg.data(), seg.size() * sizeof(int2), cudaMemcpyHostToDevice);
         cudaMemset(h->qfix, 0, h->K * sizeof(longlong2));
         cudaMemset(h->qnew, 0, h->K * sizeof(longlong2));
     }
@@ -918,6 +978,11 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     d.p_slot = h->p_slot;
     d.kvec = h->kvec;
     d.kpack = h->kpack;
+    d.kseg = h->kseg;
+    d.nseg = h->nseg;
+    d.kcc = h->kc;
+    if (set_qk_scale(d, qk_charge_bound(h, nullptr)))
+        return bail(fail(FG_ERR_INVALID, "charges too large for the Q(k) fixed point"));
     d.qfix = h->qfix;
     d.qnew = h->qnew;
     d.sc = h->sc;
@@ -1017,14 +1082,19 @@ int fg_set_state(fg_system *h, const double *xyz, const double *charge, const in
     }
     int rc;
     if (h->K > 0) {
-        // Q(k) from scratch: adopt the rebuild without the equality check
+        // contribution grid for these charges, then Q(k) from scratch: adopt
+        // the rebuild without the equality check
+        if (set_qk_scale(h->desc, qk_charge_bound(h, charge)))
+            return fail(FG_ERR_INVALID, "charges too large for the Q(k) fixed point");
+        rc = push_desc(h);
+        if (rc) return rc;
         CK(cudaMemsetAsync(h->qfix, 0, (size_t)h->K * sizeof(longlong2), h->stream));
         CK(cudaMemsetAsync(h->qnew, 0, (size_t)h->K * sizeof(longlong2), h->stream));
         s0.rebuild_pending = 1;
         s0.verify_rebuild = 0;
         rc = write_scalars(h, s0);
         if (rc) return rc;
-        rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
+        rc = launch_rebuild(h->d_desc, 1, h->N, h->nseg, h->kc, h->corr, h->stream);
         if (rc) return rc;
     }
     s0.rebuild_pending = 0;
@@ -1118,7 +1188,7 @@ int fg_commit(fg_system *h, int32_t accepted, double *correction) {
             h->cnt_accepted_host = 0;
             const int one = 1;
             CK(cudaMemcpyAsync(&h->sc->rebuild_pending, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-            rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
+            rc = launch_rebuild(h->d_desc, 1, h->N, h->nseg, h->kc, h->corr, h->stream);
             if (rc) return rc;
             float2 e;
             CK(cudaMemcpyAsync(&e, h->corr, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
@@ -1139,7 +1209,7 @@ int fg_rebuild_qk(fg_system *h, double *correction) {
     if (h->K == 0) return FG_OK;
     const int one = 1;
     CK(cudaMemcpyAsync(&h->sc->rebuild_pending, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    int rc = launch_rebuild(h->d_desc, 1, h->N, h->K, h->corr, h->stream);
+    int rc = launch_rebuild(h->d_desc, 1, h->N, h->nseg, h->kc, h->corr, h->stream);
     if (rc) return rc;
     float2 e;
     CK(cudaMemcpyAsync(&e, h->corr, sizeof(e), cudaMemcpyDeviceToHost, h->stream));

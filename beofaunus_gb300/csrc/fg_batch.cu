@@ -99,7 +99,7 @@ struct fg_batch {
     int64_t *d_counts = nullptr;
     int threads = 0;
     LaunchCfg cfg{};
-    int maxN = 0, maxK = 0;
+    int maxN = 0, maxK = 0, maxSeg = 0, maxKcc = 0;
     bool rebuilds = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // parallel tempering
@@ -123,13 +123,15 @@ int batch_config(fg_batch *b) {
     b->cfg.fn = sweep_fn(h0);
     int T = b->threads;
     size_t sm = 0;
-    b->maxN = b->maxK = 0;
+    b->maxN = b->maxK = b->maxSeg = b->maxKcc = 0;
     for (fg_system *h : b->sys) {
         if (sweep_fn(h) != b->cfg.fn) return fail(FG_ERR_INVALID, "batch members need the same kernel variant");
         if (b->threads == 0 || ewald_block_ok(h)) T = std::max(T, sweep_launch_threads(h));
         sm = std::max(sm, sweep_launch_smem(h));
         b->maxN = std::max(b->maxN, h->N);
         b->maxK = std::max(b->maxK, h->K);
+        b->maxSeg = std::max(b->maxSeg, h->nseg);
+        b->maxKcc = std::max(b->maxKcc, h->kc);
     }
     b->cfg.threads = T;
     b->cfg.smem = sm;
@@ -203,7 +205,7 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
             launches++;
             kernels++;
             if (b->rebuilds) {
-                int rc = launch_rebuild(b->d_descs, n, b->maxN, b->maxK, b->d_corr, b->stream);
+                int rc = launch_rebuild(b->d_descs, n, b->maxN, b->maxSeg, b->maxKcc, b->d_corr, b->stream);
                 if (rc) return rc;
                 kernels += 2;
             }

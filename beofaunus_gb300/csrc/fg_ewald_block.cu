@@ -71,7 +71,7 @@ __device__ inline EbSmem eb_carve(char *base, const SysDesc &d, bool cells) {
     s.b.kvec = (float4 *)(base + off[0]);
     s.b.qfix = (longlong2 *)(base + off[1]);
     s.b.qf = nullptr;
-    s.b.eold = nullptr;
+    s.b.ktab = nullptr;
     s.b.kpack = (uint32_t *)(base + off[2]);
     s.b.pos = nullptr;
     s.b.pos_ext = nullptr;
@@ -460,24 +460,41 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
 #pragma unroll
             for (int x = 0; x < 3; x++) s.Mdf[x] = make_float2(M[x].hi, M[x].lo);
         }
-        if (accm & ((done >= 32) ? 0xffffffffu : ((1u << done) - 1u))) {
-            for (int k = tid; k < K; k += blockDim.x) {
-                int nx, ny, nz;
-                unpack_n(s.b.kpack[k], nx, ny, nz);
-                longlong2 q = s.b.qfix[k];
-                for (int a = 0; a < done; a++) {
-                    if (!((accm >> a) & 1u)) continue;
-                    const Move &A = s.mv[a];
-                    const float qa = A.q * d.eff[A.ti];
-                    const int2 cn = qk_contrib(qa, sincos_turns(phase(nx, ny, nz, A.hn), s.b.sc_tab));
-                    const int2 co = qk_contrib(qa, sincos_turns(phase(nx, ny, nz, A.ho), s.b.sc_tab));
-                    q.x += (long long)cn.x - (long long)co.x;
-                    q.y += (long long)cn.y - (long long)co.y;
+        const uint32_t live = accm & ((done >= 32) ? 0xffffffffu : ((1u << done) - 1u));
+        if (live) {
+            // Q(k) += sum over accepted trials of c_k(new) - c_k(old), with the
+            // axis tables of up to gmax trials at a time in the delta buffer
+            int *alist = reinterpret_cast<int *>(s.corr);   // free after the resolution
+            if (tid < kEbTrials && ((live >> tid) & 1u)) alist[__popc(live & ((1u << tid) - 1u))] = tid;
+            const int na = __popc(live);
+            const int T = qk_tab_len(d.kcc), T2 = 2 * T;
+            const int gmax = min(kEbTrials, (kEbKc * kEbTrials) / T2);
+            for (int g0 = 0; g0 < na; g0 += gmax) {
+                const int ng = min(gmax, na - g0);
+                __syncthreads();   // list written; the previous group's tables consumed
+                for (int t = tid; t < ng * T2; t += blockDim.x) {
+                    const int g = t / T2, e = t - g * T2;
+                    const Move &A = s.mv[alist[g0 + g]];
+                    s.delta[t] = e < T ? qk_tab_entry(e, d.kcc, A.hn, s.b.sc_tab)
+                                       : qk_tab_entry(e - T, d.kcc, A.ho, s.b.sc_tab);
                 }
-                s.b.qfix[k] = q;
-                const float2 qf = q_to_float(q);
-                s.b.kvec[k].y = qf.x;
-                s.b.kvec[k].z = qf.y;
+                __syncthreads();
+                for (int k = tid; k < K; k += blockDim.x) {
+                    int nx, ny, nz;
+                    unpack_n(s.b.kpack[k], nx, ny, nz);
+                    longlong2 q = s.b.qfix[k];
+                    for (int g = 0; g < ng; g++) {
+                        const Move &A = s.mv[alist[g0 + g]];
+                        const float2 *tn = s.delta + g * T2;
+                        const int2 c = qk_delta(nx, ny, nz, qk_charge(A.q, d.eff[A.ti], d), tn, tn + T, d.kcc);
+                        q.x += qk_widen(c.x, d.qk_shift);
+                        q.y += qk_widen(c.y, d.qk_shift);
+                    }
+                    s.b.qfix[k] = q;
+                    const float2 qf = q_to_float(q);
+                    s.b.kvec[k].y = qf.x;
+                    s.b.kvec[k].z = qf.y;
+                }
             }
         }
         cur += done;

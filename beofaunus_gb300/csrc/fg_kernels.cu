@@ -18,13 +18,18 @@
 // (potentials.h:2036-2040), NonbondedEwald::updateChange/update/external
 // (ewald.h:613-729), getSurfaceEnergy (ewald.h:277-291).
 //
-// Q(k) bookkeeping. Each particle contributes c_k(j) = round(2^28 q_j eff_j
-// e^{i k.r_j}) with e^{ik.r} from sincos_turns on the exact integer phase:
-// a deterministic function of the particle's fixed-point position. Q(k) is
-// kept as the exact int64 sum of these contributions, and an accepted move
-// adds c_k(new) - c_k(old). So Q(k) never drifts: a rebuild from scratch
+// Q(k) bookkeeping. Each particle contributes the integer
+// c_k(j) = round(w_j(nx, ny) e_z(nz)), w_j = (2^g q_j eff_j e_x(nx)) e_y(ny),
+// with e_a(n) = e^{i n 2 pi x_a / L_a} from sincos_turns on the exact integer
+// phase n h_a (its conjugate for n < 0) and every product rounded in a fixed
+// order (qk_w, qk_term): a deterministic function of the particle's
+// fixed-point position. Q(k) is kept as the exact int64 sum of these
+// contributions in units of 2^-28 (each shifted by 28 - g), and an accepted
+// move adds c_k(new) - c_k(old). So Q(k) never drifts: a rebuild from scratch
 // reproduces it bit for bit (qk_rebuild_* checks that), where the
 // reference's FP64 running sum needs the rebuild to undo accumulated error.
+// The factorised form lets the rebuild share one w per particle across the
+// run of k-vectors with the same (nx, ny).
 // The energy change itself uses the increment in the form
 // q e^{ik.r_old}(e^{ik.d} - 1), whose FP32 error is relative to |d|.
 #include <cstdint>
@@ -344,7 +349,7 @@ struct Smem {
     uint32_t *kpack;    // K: n vector
     longlong2 *qfix;    // K: Q(k), exact fixed point
     float2 *qf;         // K: Q(k) rounded to float (energy)
-    float2 *eold;       // K: e^{ik.r_old} of the current trial
+    float2 *ktab;       // axis tables (qk_tab_len) of a committed move: new, then old position
     int4 *pos;          // N (positions in shared memory)
     short4 *pos_ext;    // N
     uint8_t *ptype;     // N
@@ -355,15 +360,18 @@ struct Smem {
 __host__ __device__ __forceinline__ size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 // Byte layout of the dynamic shared memory; the host sizes launches with it.
-__host__ __device__ __forceinline__ size_t smem_layout(int N, int K, int ncell, bool kspace, bool pos_smem,
+// Entries of the per-position axis tables: e_x(0..kcc), e_y(-kcc..kcc), e_z(-kcc..kcc).
+__host__ __device__ __forceinline__ int qk_tab_len(int kcc) { return 5 * kcc + 3; }
+
+__host__ __device__ __forceinline__ size_t smem_layout(int N, int K, int kcc, int ncell, bool kspace, bool pos_smem,
                                                        bool cells, size_t off[8]) {
     size_t b = 256 * 8 + 32 * 8;
     off[0] = b;                                   // kvec
     if (kspace) b += (size_t)K * 16;
     off[1] = b;                                   // qfix
     if (kspace) b += (size_t)K * 16;
-    off[2] = b;                                   // qf, eold
-    if (kspace) b += (size_t)K * 16;
+    off[2] = b;                                   // qf, ktab
+    if (kspace) b = align16(b + (size_t)K * 8 + (size_t)2 * qk_tab_len(kcc) * 8);
     off[3] = b;                                   // kpack
     if (kspace) b = align16(b + (size_t)K * 4);
     off[4] = b;                                   // pos, pos_ext, ptype
@@ -378,14 +386,14 @@ __host__ __device__ __forceinline__ size_t smem_layout(int N, int K, int ncell, 
 
 __device__ __forceinline__ Smem carve(char *base, const SysDesc &d, bool kspace, bool pos_smem, bool cells) {
     size_t off[8];
-    smem_layout(d.N, d.K, d.nc[0] * d.nc[1] * d.nc[2], kspace, pos_smem, cells, off);
+    smem_layout(d.N, d.K, d.kcc, d.nc[0] * d.nc[1] * d.nc[2], kspace, pos_smem, cells, off);
     Smem s;
     s.sc_tab = (float2 *)base;
     s.red = (float2 *)(base + 256 * 8);
     s.kvec = (float4 *)(base + off[0]);
     s.qfix = (longlong2 *)(base + off[1]);
     s.qf = (float2 *)(base + off[2]);
-    s.eold = (float2 *)(base + off[2] + (size_t)d.K * 8);
+    s.ktab = (float2 *)(base + off[2] + (size_t)d.K * 8);
     s.kpack = (uint32_t *)(base + off[3]);
     s.pos = (int4 *)(base + off[4]);
     s.pos_ext = (short4 *)(base + off[4] + (size_t)d.N * 16);
@@ -503,7 +511,6 @@ __device__ __forceinline__ float kspace_energy(const Move &m, const SysDesc &d, 
         unpack_n(s.kpack[k], nx, ny, nz);
         const uint32_t ph = phase(nx, ny, nz, m.ho);
         const float2 e = sincos_turns(ph, s.sc_tab);
-        s.eold[k] = e;
         const float4 kv = s.kvec[k];
         const float phi = fmaf(kv.x, m.dxf[0], fmaf(kv.y, m.dxf[1], kv.z * m.dxf[2]));
         float2 w;
@@ -522,25 +529,88 @@ __device__ __forceinline__ float kspace_energy(const Move &m, const SysDesc &d, 
     return acc;
 }
 
-// One particle's exact contribution to Q(k) (see the file comment), from
-// e = sincos_turns of its phase: round(2^28 q eff e), a 32-bit integer for
-// |q eff| < 8.
-__device__ __forceinline__ int2 qk_contrib(float qe, float2 e) {
-    return make_int2(__float2int_rn(qe * e.x * 268435456.0f), __float2int_rn(qe * e.y * 268435456.0f));
+// cos/sin of a turn fraction as sincos_turns, with every operation an
+// explicit round-to-nearest intrinsic so that no call site can contract or
+// reorder it: Q(k) contributions must come out bit-identical in the
+// rebuild, the sweeps and the plain commit.
+__device__ __forceinline__ float2 sincos_turns_rn(uint32_t ph, const float2 *__restrict__ tab) {
+    const uint32_t i = (ph + (1u << 23)) >> 24;
+    const int32_t h = (int32_t)(ph << 8) >> 9;
+    const float d = __fmaf_rn(__int_as_float(0x4B400000 + h), 2.0f * kRadPerTurnUnit,
+                              -12582912.0f * (2.0f * kRadPerTurnUnit));
+    const float d2 = __fmul_rn(d, d);
+    const float sn = __fmaf_rn(__fmul_rn(d2, -1.0f / 6.0f), d, d);
+    const float cs = __fmaf_rn(d2, __fmaf_rn(d2, 1.0f / 24.0f, -0.5f), 1.0f);
+    const float2 t = tab[i & 255u];
+    return make_float2(__fmaf_rn(t.x, cs, -__fmul_rn(t.y, sn)), __fmaf_rn(t.x, sn, __fmul_rn(t.y, cs)));
 }
 
-// Accepted move: Q(k) += c_k(new) - c_k(old) for this thread's k-vectors;
-// e^{ik.r_old} was left in shared memory by kspace_energy.
+// Entry t of the axis tables of fixed-point position h (high words):
+// [0, kcc] e_x(n), [kcc+1, 3kcc+1] e_y(n - kcc), [3kcc+2, 5kcc+2] e_z(n - kcc).
+__device__ __forceinline__ float2 qk_tab_entry(int t, int kcc, const int h[3], const float2 *__restrict__ tab) {
+    int axis = 0, n = t;
+    if (t > 3 * kcc + 1) {
+        axis = 2;
+        n = t - (4 * kcc + 2);
+    } else if (t > kcc) {
+        axis = 1;
+        n = t - (2 * kcc + 1);
+    }
+    const int an = n < 0 ? -n : n;
+    const int ha = axis == 0 ? h[0] : (axis == 1 ? h[1] : h[2]);   // no dynamic register indexing
+    const float2 e = sincos_turns_rn((uint32_t)an * (uint32_t)ha, tab);
+    return n < 0 ? make_float2(e.x, -e.y) : e;
+}
+
+// w = (2^g q eff e_x) e_y, then the integer term round(w e_z), as one
+// fixed sequence of roundings.
+__device__ __forceinline__ float2 qk_w(float q2g, float2 ex, float2 ey) {
+    const float ax = __fmul_rn(q2g, ex.x), ay = __fmul_rn(q2g, ex.y);
+    return make_float2(__fmaf_rn(ax, ey.x, -__fmul_rn(ay, ey.y)), __fmaf_rn(ax, ey.y, __fmul_rn(ay, ey.x)));
+}
+__device__ __forceinline__ int2 qk_term(float2 w, float2 ez) {
+    return make_int2(__float2int_rn(__fmaf_rn(w.x, ez.x, -__fmul_rn(w.y, ez.y))),
+                     __float2int_rn(__fmaf_rn(w.x, ez.y, __fmul_rn(w.y, ez.x))));
+}
+// an integer contribution in units of 2^-28
+__device__ __forceinline__ long long qk_widen(int c, int shift) { return (long long)c * (1LL << shift); }
+// 2^g q eff of a particle (the power-of-two scaling is exact)
+__device__ __forceinline__ float qk_charge(float q, float eff, const SysDesc &d) {
+    return __fmul_rn(__fmul_rn(q, eff), d.qk_scale);
+}
+// c_k(new) - c_k(old) for k-vector n from the two positions' axis tables
+__device__ __forceinline__ int2 qk_delta(int nx, int ny, int nz, float q2g, const float2 *__restrict__ tn,
+                                        const float2 *__restrict__ to, int kcc) {
+    const int iy = 2 * kcc + 1 + ny, iz = 4 * kcc + 2 + nz;
+    const int2 cn = qk_term(qk_w(q2g, tn[nx], tn[iy]), tn[iz]);
+    const int2 co = qk_term(qk_w(q2g, to[nx], to[iy]), to[iz]);
+    return make_int2(cn.x - co.x, cn.y - co.y);
+}
+// Axis tables of a move's new and old positions into tn and to (all threads
+// of the block; the caller synchronises before use).
+__device__ __forceinline__ void qk_move_tables(const int hn[3], const int ho[3], int kcc, float2 *tn, float2 *to,
+                                               const float2 *__restrict__ tab) {
+    const int T = qk_tab_len(kcc);
+    for (int t = threadIdx.x; t < 2 * T; t += blockDim.x) {
+        if (t < T) tn[t] = qk_tab_entry(t, kcc, hn, tab);
+        else to[t - T] = qk_tab_entry(t - T, kcc, ho, tab);
+    }
+}
+
+// Accepted move: Q(k) += c_k(new) - c_k(old) for this thread's k-vectors.
+// Block-wide (uniform call): the axis tables go through shared memory.
 __device__ __forceinline__ void kspace_commit(const Move &m, const SysDesc &d, const Smem &s) {
-    const float qe = m.q * d.eff[m.ti];
+    const int T = qk_tab_len(d.kcc);
+    qk_move_tables(m.hn, m.ho, d.kcc, s.ktab, s.ktab + T, s.sc_tab);
+    __syncthreads();
+    const float q2g = qk_charge(m.q, d.eff[m.ti], d);
     for (int k = threadIdx.x; k < d.K; k += blockDim.x) {
         int nx, ny, nz;
         unpack_n(s.kpack[k], nx, ny, nz);
-        const int2 cn = qk_contrib(qe, sincos_turns(phase(nx, ny, nz, m.hn), s.sc_tab));
-        const int2 co = qk_contrib(qe, s.eold[k]);
+        const int2 c = qk_delta(nx, ny, nz, q2g, s.ktab, s.ktab + T, d.kcc);
         longlong2 q = s.qfix[k];
-        q.x += (long long)cn.x - (long long)co.x;
-        q.y += (long long)cn.y - (long long)co.y;
+        q.x += qk_widen(c.x, d.qk_shift);
+        q.y += qk_widen(c.y, d.qk_shift);
         s.qfix[k] = q;
         s.qf[k] = q_to_float(q);
     }
@@ -853,60 +923,115 @@ __global__ void __launch_bounds__(kSweepThreads) commit_kernel(const SysDesc *__
 
 // ------------------------------------------------------------------ Q(k) rebuild
 // updateAllComplexNumbers (ewald.h:388-415) as the exact integer sum of the
-// per-particle contributions; blockIdx.z selects the system of a batch.
-// Only systems with rebuild_pending set do work.
-// Each thread owns two k-vectors (kQkThreads threads, 2 kQkThreads k per
-// block) so one broadcast of a particle serves two phase evaluations; the
-// charge is staged as 2^28 q eff, which leaves qk_contrib's product unchanged
-// (scaling by a power of two is exact).
-constexpr int kQkThreads = 128;
-constexpr int kQkStage = 256;   // particles staged per pass
-__global__ void __launch_bounds__(kQkThreads) qk_rebuild_kernel(const SysDesc *__restrict__ descs, int chunk) {
+// per-particle contributions. One thread per run of k-vectors sharing
+// (nx, ny) (at most kQkRun of them, consecutive nz): per staged particle it
+// forms w once and one term per k. Terms (|c| <= 2^24) are summed exactly in
+// int32 over a pass of `stage` <= 64 particles, then added to the thread's
+// int64 totals in shared memory. Per pass the block stages the particles'
+// axis tables (stage x qk_tab_len) from positions prefetched during the
+// previous pass. blockIdx.x covers a chunk of particles, blockIdx.y selects
+// the system of a batch; only systems with rebuild_pending set do work.
+constexpr int kQkRun = 8;
+constexpr int kQkMaxThreads = 512;
+constexpr int kQkMaxStage = 64;
+__host__ __device__ __forceinline__ size_t qk_rebuild_smem(int stage, int T, int threads) {
+    return (size_t)stage * T * 8 + (size_t)2 * kQkRun * threads * 8 + (size_t)stage * (16 + 4);
+}
+__global__ void __launch_bounds__(kQkMaxThreads) qk_rebuild_kernel(const SysDesc *__restrict__ descs, int chunk, int stage) {
+    extern __shared__ __align__(16) char qk_smem[];
     __shared__ float2 tab[256];
-    __shared__ int4 pj[kQkStage];
-    __shared__ float qe[kQkStage];
-    const SysDesc &d = descs[blockIdx.z];
+    const SysDesc &d = descs[blockIdx.y];
     if (d.K == 0 || d.sc->rebuild_pending == 0) return;
-    const int j0 = blockIdx.y * chunk, j1 = min(d.N, j0 + chunk);
+    const int j0 = blockIdx.x * chunk, j1 = min(d.N, j0 + chunk);
     if (j0 >= d.N) return;
-    for (int t = threadIdx.x; t < 256; t += blockDim.x) tab[t] = d.sc_tab[t];
-    const int k0 = blockIdx.x * (2 * kQkThreads) + threadIdx.x, k1 = k0 + kQkThreads;
-    int n0[3] = {0, 0, 0}, n1[3] = {0, 0, 0};
-    if (k0 < d.K) unpack_n(d.kpack[k0], n0[0], n0[1], n0[2]);
-    if (k1 < d.K) unpack_n(d.kpack[k1], n1[0], n1[1], n1[2]);
-    long long s0x = 0, s0y = 0, s1x = 0, s1y = 0;
-    for (int b = j0; b < j1; b += kQkStage) {
-        __syncthreads();
-        for (int t = threadIdx.x; t < kQkStage; t += kQkThreads) {
-            const int j = b + t;
-            if (j < j1) {
-                const int4 p = d.pos4[j];
-                pj[t] = p;
-                qe[t] = __int_as_float(p.w) * d.eff[d.ptype[j]] * 268435456.0f;
+    const int kcc = d.kcc, T = qk_tab_len(kcc), tid = threadIdx.x, nt = blockDim.x;
+    float2 *et = (float2 *)qk_smem;                                          // stage x T
+    long long *tot = (long long *)(qk_smem + (size_t)stage * T * 8);          // [2 kQkRun][nt]
+    int4 *sp = (int4 *)(qk_smem + (size_t)stage * T * 8 + (size_t)2 * kQkRun * nt * 8);   // stage
+    float *q2g = (float *)(sp + stage);                                        // stage
+    for (int t = tid; t < 256; t += nt) tab[t] = d.sc_tab[t];
+    const int shift = d.qk_shift;
+    for (int r0 = 0; r0 < d.nseg; r0 += nt) {   // uniform over the block
+        const int r = r0 + tid;
+        int k0 = 0, len = 0, ix = 0, iy = 0, iz = 0;
+        if (r < d.nseg) {
+            const int2 sg = d.kseg[r];
+            k0 = sg.x & 0xFFFFFF;
+            len = sg.x >> 24;
+            ix = (int)(int8_t)(sg.y & 0xFF);
+            iy = 2 * kcc + 1 + (int)(int8_t)((sg.y >> 8) & 0xFF);
+            iz = 4 * kcc + 2 + (int)(int8_t)((sg.y >> 16) & 0xFF);
+        }
+#pragma unroll
+        for (int u = 0; u < 2 * kQkRun; u++) tot[u * nt + tid] = 0;
+        int4 pn = make_int4(0, 0, 0, 0);
+        float qn = 0.0f;
+        if (tid < stage && j0 + tid < j1) {
+            pn = d.pos4[j0 + tid];
+            qn = d.eff[d.ptype[j0 + tid]];
+        }
+        for (int b = j0; b < j1; b += stage) {
+            const int nb = min(stage, j1 - b);
+            __syncthreads();   // the previous pass is done with sp, q2g and et
+            if (tid < nb) {
+                sp[tid] = pn;
+                q2g[tid] = qk_charge(__int_as_float(pn.w), qn, d);
+            }
+            if (tid < stage && b + stage + tid < j1) {   // prefetch the next pass
+                pn = d.pos4[b + stage + tid];
+                qn = d.eff[d.ptype[b + stage + tid]];
+            }
+            __syncthreads();
+            {
+                int jj = tid / T, e = tid - jj * T;
+                const int djj = nt / T, de = nt - djj * T;
+                while (jj < nb) {
+                    const int4 p = sp[jj];
+                    const int h[3] = {p.x, p.y, p.z};
+                    et[jj * T + e] = qk_tab_entry(e, kcc, h, tab);
+                    jj += djj;
+                    e += de;
+                    if (e >= T) {
+                        e -= T;
+                        jj++;
+                    }
+                }
+            }
+            __syncthreads();
+            if (len > 0) {
+                // unsigned sums: the dropped lanes may wrap, harmlessly
+                unsigned ax[kQkRun], ay[kQkRun];
+#pragma unroll
+                for (int u = 0; u < kQkRun; u++) ax[u] = ay[u] = 0u;
+                // all kQkRun terms unconditionally (no branches in the hot
+                // loop); those past len read entries further along the
+                // buffer (at most kQkRun - 1 past the last record, still
+                // inside the shared allocation) and are dropped below
+                for (int jj = 0; jj < nb; jj++) {
+                    const float2 *e = et + jj * T;
+                    const float2 w = qk_w(q2g[jj], e[ix], e[iy]);
+#pragma unroll
+                    for (int u = 0; u < kQkRun; u++) {
+                        const int2 c = qk_term(w, e[iz + u]);
+                        ax[u] += (unsigned)c.x;
+                        ay[u] += (unsigned)c.y;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kQkRun; u++)
+                    if (u < len) {
+                        tot[(2 * u) * nt + tid] += qk_widen((int)ax[u], shift);
+                        tot[(2 * u + 1) * nt + tid] += qk_widen((int)ay[u], shift);
+                    }
             }
         }
-        __syncthreads();
-        const int nb = min(kQkStage, j1 - b);
-        if (k0 < d.K)
-            for (int t = 0; t < nb; t++) {
-                const int4 p = pj[t];
-                const int h[3] = {p.x, p.y, p.z};
-                const float q28 = qe[t];
-                const float2 e0 = sincos_turns(phase(n0[0], n0[1], n0[2], h), tab);
-                const float2 e1 = sincos_turns(phase(n1[0], n1[1], n1[2], h), tab);
-                s0x += __float2int_rn(q28 * e0.x);
-                s0y += __float2int_rn(q28 * e0.y);
-                s1x += __float2int_rn(q28 * e1.x);
-                s1y += __float2int_rn(q28 * e1.y);
+#pragma unroll
+        for (int u = 0; u < kQkRun; u++)
+            if (u < len) {
+                atomicAdd((unsigned long long *)&d.qnew[k0 + u].x, (unsigned long long)tot[(2 * u) * nt + tid]);
+                atomicAdd((unsigned long long *)&d.qnew[k0 + u].y, (unsigned long long)tot[(2 * u + 1) * nt + tid]);
             }
-    }
-    if (k0 < d.K) {
-        atomicAdd((unsigned long long *)&d.qnew[k0].x, (unsigned long long)s0x);
-        atomicAdd((unsigned long long *)&d.qnew[k0].y, (unsigned long long)s0y);
-    }
-    if (k1 < d.K) {
-        atomicAdd((unsigned long long *)&d.qnew[k1].x, (unsigned long long)s1x);
-        atomicAdd((unsigned long long *)&d.qnew[k1].y, (unsigned long long)s1y);
+        __syncthreads();   // tot and the staging buffers are reused by the next round
     }
 }
 

@@ -120,6 +120,13 @@ struct alignas(16) SysDesc {
     uint32_t seed;           // Philox key word (seed)
     int64_t stream_first;    // counter of trial 0 in the current stream
     longlong2 *qnew;         // rebuild target (K)
+    // Q(k) contributions: one particle adds round(2^g q eff e^{ik.r}) (an
+    // integer of magnitude <= 2^24) shifted left by qk_shift = 28 - g
+    int32_t kcc;             // |n_a| <= kcc for every k-vector
+    int32_t qk_shift;
+    float qk_scale;          // 2^g
+    int32_t nseg;            // runs of k-vectors that share (nx, ny), for the rebuild
+    const int2 *kseg;        // {k0 | len << 24, nx & 0xFF | (ny & 0xFF) << 8 | (nz0 & 0xFF) << 16}
 };
 
 }  // namespace fg
