@@ -93,6 +93,11 @@ __device__ inline EbSmem eb_carve(char *base, const SysDesc &d, bool cells) {
 
 // Real-space sum of one trial by one warp: every stencil cell (cell list) or
 // every particle (no cell list), lanes over the slots.
+// Barrier 1 over the block's warps 1.. (nthreads = blockDim - 32 threads).
+__device__ __forceinline__ void eb_qbar(int nthreads) {
+    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+
 template <bool CELLS>
 __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, const Smem &s, float &accf, df &accd) {
     const int lane = threadIdx.x & 31;
@@ -446,7 +451,11 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
         const uint32_t accm = (uint32_t)s.info[1];
         rebuild = s.info[2] != 0;
         cnt_acc = s.info[3];
-        // ---- apply the accepted trials in order
+        // ---- apply the accepted trials in order. Thread 0 commits the
+        // positions and cell lists (a serial chain of global updates) while
+        // warps 1.. update Q(k) in parallel, synchronising among themselves
+        // on named barrier 1; the block barrier below joins the two.
+        const uint32_t live = accm & ((done >= 32) ? 0xffffffffu : ((1u << done) - 1u));
         if (tid == 0) {
             df M[3] = {{s.Mdf[0].x, s.Mdf[0].y}, {s.Mdf[1].x, s.Mdf[1].y}, {s.Mdf[2].x, s.Mdf[2].y}};
             for (int a = 0; a < done; a++) {
@@ -459,27 +468,26 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             }
 #pragma unroll
             for (int x = 0; x < 3; x++) s.Mdf[x] = make_float2(M[x].hi, M[x].lo);
-        }
-        const uint32_t live = accm & ((done >= 32) ? 0xffffffffu : ((1u << done) - 1u));
-        if (live) {
+        } else if (tid >= 32 && live) {
             // Q(k) += sum over accepted trials of c_k(new) - c_k(old), with the
             // axis tables of up to gmax trials at a time in the delta buffer
+            const int qt = tid - 32, nq = blockDim.x - 32;
             int *alist = reinterpret_cast<int *>(s.corr);   // free after the resolution
-            if (tid < kEbTrials && ((live >> tid) & 1u)) alist[__popc(live & ((1u << tid) - 1u))] = tid;
+            if (qt < kEbTrials && ((live >> qt) & 1u)) alist[__popc(live & ((1u << qt) - 1u))] = qt;
             const int na = __popc(live);
             const int T = qk_tab_len(d.kcc), T2 = 2 * T;
             const int gmax = min(kEbTrials, (kEbKc * kEbTrials) / T2);
             for (int g0 = 0; g0 < na; g0 += gmax) {
                 const int ng = min(gmax, na - g0);
-                __syncthreads();   // list written; the previous group's tables consumed
-                for (int t = tid; t < ng * T2; t += blockDim.x) {
+                eb_qbar(nq);   // list written; the previous group's tables consumed
+                for (int t = qt; t < ng * T2; t += nq) {
                     const int g = t / T2, e = t - g * T2;
                     const Move &A = s.mv[alist[g0 + g]];
                     s.delta[t] = e < T ? qk_tab_entry(e, d.kcc, A.hn, s.b.sc_tab)
                                        : qk_tab_entry(e - T, d.kcc, A.ho, s.b.sc_tab);
                 }
-                __syncthreads();
-                for (int k = tid; k < K; k += blockDim.x) {
+                eb_qbar(nq);
+                for (int k = qt; k < K; k += nq) {
                     int nx, ny, nz;
                     unpack_n(s.b.kpack[k], nx, ny, nz);
                     longlong2 q = s.b.qfix[k];
