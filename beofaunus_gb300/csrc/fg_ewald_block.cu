@@ -27,7 +27,7 @@ constexpr int kEbKc = 128;   // k-vectors per chunk
 
 struct EbSmem {
     Smem b;          // sc_tab, qfix, kpack, cells as in the one-trial kernel; kvec here holds
-                     // {A'_k, Q(k) as float (re, im), 0}: k itself comes from the integer n
+                     // {A'_k, Q(k) as float (re, im), sqrt(A'_k)}: k itself comes from the integer n
     Move *mv;        // [32]
     float2 *thr;     // [32] threshold (df, times kT)
     uint32_t *col;   // [32] earlier trials on the same particle
@@ -93,6 +93,49 @@ __device__ inline EbSmem eb_carve(char *base, const SysDesc &d, bool cells) {
 
 // Real-space sum of one trial by one warp: every stencil cell (cell list) or
 // every particle (no cell list), lanes over the slots.
+// One k-step of the Gram matrix on the tensor cores: components c = 8 real
+// parts/imaginary parts of complex k-vectors kb .. kb+3 of the chunk buffer
+// X[k][trial] (float2 = re, im; sqrt(A') already applied). mma.sync
+// m16n8k8 TF32 with the three-product split (hi hi + hi lo + lo hi, each
+// operand split into a TF32 high part and the TF32 rounding of the rest)
+// keeps FP32-level accuracy. Lane (gq = lane / 4, gt = lane % 4) holds the
+// components gt and gt + 4 of trials gq + 8 r; these are the A fragments of
+// the two 16-row tiles and, G being X X^T, the B fragments of the four
+// 8-column tiles. Accumulated tiles (row tile, column tile): (0,0) (0,1)
+// (0,2) (0,3) (1,2) (1,3), every pair a < m lies in one of them.
+__device__ __forceinline__ uint32_t eb_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void eb_mma(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ void eb_gram_step(const float *X, int kb, int gq, int gt, float gc[6][4]) {
+    uint32_t hi[4][2], lo[4][2];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int k = kb + 2 * h + (gt >> 1);
+            const float x = X[(k * kEbTrials + gq + 8 * r) * 2 + (gt & 1)];
+            hi[r][h] = eb_tf32(x);
+            lo[r][h] = eb_tf32(x - __uint_as_float(hi[r][h]));
+        }
+#pragma unroll
+    for (int t = 0; t < 6; t++) {
+        const int mi = t < 4 ? 0 : 1, nj = t < 4 ? t : t - 2;
+        const uint32_t ah[4] = {hi[2 * mi][0], hi[2 * mi + 1][0], hi[2 * mi][1], hi[2 * mi + 1][1]};
+        const uint32_t al[4] = {lo[2 * mi][0], lo[2 * mi + 1][0], lo[2 * mi][1], lo[2 * mi + 1][1]};
+        eb_mma(gc[t], al, hi[nj][0], hi[nj][1]);
+        eb_mma(gc[t], ah, lo[nj][0], lo[nj][1]);
+        eb_mma(gc[t], ah, hi[nj][0], hi[nj][1]);
+    }
+}
+
 // Barrier 1 over the block's warps 1.. (nthreads = blockDim - 32 threads).
 __device__ __forceinline__ void eb_qbar(int nthreads) {
     asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
@@ -185,6 +228,12 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
     const SysDesc &d = sd;
     EbSmem s = eb_carve(eb_smem_raw, d, CELLS);
     SysScalars *sc = d.sc;
+    // the work split (16 threads per trial, two Gram k-steps per warp) is
+    // written for exactly kEbThreads threads
+    if (blockDim.x != kEbThreads) {
+        if (threadIdx.x == 0) atomicOr(&sc->error, kErrLaunch);
+        return;
+    }
     if (sc->rebuild_pending || sc->cursor >= min(end, sc->n_trials)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
     const int K = d.K;
@@ -193,7 +242,8 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
     for (int k = tid; k < K; k += blockDim.x) {
         const longlong2 q = d.qfix[k];
         const float2 qf = q_to_float(q);
-        s.b.kvec[k] = make_float4(d.kvec[k].w, qf.x, qf.y, 0.0f);
+        const float A = d.kvec[k].w;
+        s.b.kvec[k] = make_float4(A, qf.x, qf.y, sqrtf(A));
         s.b.kpack[k] = d.kpack[k];
         s.b.qfix[k] = q;
     }
@@ -218,17 +268,9 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
     int err = 0;
     // k-space work split: 16 threads per trial, each a fixed set of k-vectors
     const int mt = tid >> 4, sub = tid & 15;
-    // Gram tiles: 4 x 4 trial tiles on and above the diagonal (36), each split
-    // over 14 groups of k-vectors of a chunk
-    constexpr int kTiles = 36, kGroups = 14;
-    int ta = 0, tm = 0;
-    {
-        int t = tid % kTiles, r = 0;
-        while (t >= 8 - r) { t -= 8 - r; r++; }
-        ta = r;
-        tm = r + t;
-    }
-    const int tgroup = tid / kTiles;   // < kGroups for tid < 504
+    // Gram G = X X^T over the real components of X = sqrt(A') D on the tensor
+    // cores (eb_gram_step): warp w takes the k-steps w, w + 16 of each chunk
+    const int gq = lane >> 2, gt = lane & 3;
     while (cur < stop) {
         const int kb = (int)((stop - cur) < (int64_t)kEbTrials ? (stop - cur) : (int64_t)kEbTrials);
         // ---- trials of the block (old coordinates: the block start)
@@ -300,13 +342,35 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             qe = M.q * d.eff[M.ti];
         }
         float kacc = 0.0f;
-        float g[4][4];
+        float gc[6][4];
 #pragma unroll
-        for (int x = 0; x < 4; x++)
+        for (int x = 0; x < 6; x++)
 #pragma unroll
-            for (int y = 0; y < 4; y++) g[x][y] = 0.0f;
+            for (int y = 0; y < 4; y++) gc[x][y] = 0.0f;
+        // |k.d| <= kcc (|dxs_x| + |dxs_y| + |dxs_z|): when that bound is within
+        // the Taylor range of expm1_i_horner every k takes the same branch-free
+        // path, and the chunk loop below is unrolled for independent chains
+        const bool fast = (float)d.kcc * (fabsf(dxs[0]) + fabsf(dxs[1]) + fabsf(dxs[2])) <= 1.6f;
         for (int kc0 = 0; kc0 < K; kc0 += kEbKc) {
             __syncthreads();   // the previous chunk's Gram reads are done
+            if (fast) {
+#pragma unroll 2
+                for (int kl = sub; kl < kEbKc; kl += 16) {
+                    const int k = min(kc0 + kl, K - 1);
+                    const float live = (kc0 + kl < K) ? qe : 0.0f;   // 0 past K and for idle trials
+                    int nx, ny, nz;
+                    unpack_n(s.b.kpack[k], nx, ny, nz);
+                    const float2 e = sincos_turns(phase(nx, ny, nz, hm), s.b.sc_tab);
+                    const float4 kv = s.b.kvec[k];   // {A', Re Q, Im Q, sqrt A'}
+                    const float phi = fmaf(small_int_to_float(nx), dxs[0],
+                                           fmaf(small_int_to_float(ny), dxs[1], small_int_to_float(nz) * dxs[2]));
+                    float2 dd = cmul(e, expm1_i_horner(phi));
+                    dd.x *= live;
+                    dd.y *= live;
+                    kacc = fmaf(kv.x, fmaf(2.0f, fmaf(kv.y, dd.x, kv.z * dd.y), fmaf(dd.x, dd.x, dd.y * dd.y)), kacc);
+                    s.delta[kl * kEbTrials + mt] = make_float2(dd.x * kv.w, dd.y * kv.w);
+                }
+            } else
             for (int kl = sub; kl < kEbKc; kl += 16) {
                 const int k = kc0 + kl;
                 float2 dd = make_float2(0.0f, 0.0f);
@@ -315,7 +379,7 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                     unpack_n(s.b.kpack[k], nx, ny, nz);
                     const uint32_t ph = phase(nx, ny, nz, hm);
                     const float2 e = sincos_turns(ph, s.b.sc_tab);
-                    const float4 kv = s.b.kvec[k];   // {A', Re Q, Im Q, 0}
+                    const float4 kv = s.b.kvec[k];   // {A', Re Q, Im Q, sqrt A'}
                     const float phi = fmaf(small_int_to_float(nx), dxs[0],
                                            fmaf(small_int_to_float(ny), dxs[1], small_int_to_float(nz) * dxs[2]));
                     float2 w;
@@ -329,28 +393,17 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                     dd.x *= qe;
                     dd.y *= qe;
                     kacc = fmaf(kv.x, fmaf(2.0f, fmaf(kv.y, dd.x, kv.z * dd.y), fmaf(dd.x, dd.x, dd.y * dd.y)), kacc);
+                    // the Gram tiles see sqrt(A') D, so A' needs no product there
+                    dd.x *= kv.w;
+                    dd.y *= kv.w;
                 }
                 s.delta[kl * kEbTrials + mt] = dd;
             }
             __syncthreads();
-            if (tid < kTiles * kGroups) {
+            {
                 const int kend = min(kEbKc, K - kc0);
-                for (int kl = tgroup; kl < kend; kl += kGroups) {
-                    const float A = s.b.kvec[kc0 + kl].x;
-                    const float2 *row = s.delta + kl * kEbTrials;
-                    float2 va[4], vm[4];
-#pragma unroll
-                    for (int x = 0; x < 4; x++) {
-                        va[x] = row[4 * ta + x];
-                        vm[x] = row[4 * tm + x];
-                    }
-#pragma unroll
-                    for (int x = 0; x < 4; x++) {
-                        const float ax = A * va[x].x, ay = A * va[x].y;
-#pragma unroll
-                        for (int y = 0; y < 4; y++) g[x][y] = fmaf(ax, vm[y].x, fmaf(ay, vm[y].y, g[x][y]));
-                    }
-                }
+                for (int st = warp; 4 * st < kend; st += kEbThreads / 32)
+                    eb_gram_step(reinterpret_cast<const float *>(s.delta), 4 * st, gq, gt, gc);
             }
         }
         // reciprocal base: the 16 threads of trial mt, in df
@@ -365,26 +418,42 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             }
             if (sub == 0 && mt < kEbTrials) s.kbase[mt] = make_float2(v.hi, v.lo);
         }
-        // Gram tiles: the k groups' partial tiles meet in the (now free) chunk
-        // buffer and are summed in a fixed order, so the result does not
-        // depend on timing
+        // Gram: the 16 warps' partial tiles meet in the (now free) chunk buffer
+        // in two rounds and are summed in a fixed order, so the result does
+        // not depend on timing
         __syncthreads();
-        float *P = reinterpret_cast<float *>(s.delta);   // [kGroups][kTiles][16]
-        if (tid < kTiles * kGroups) {
-            const int tile = tid % kTiles;
+        float *P = reinterpret_cast<float *>(s.delta);   // [8 slots][6 tiles][32 lanes][4]
+        {
+            const int nw = kEbThreads / 32, slot = warp % (nw / 2);
+            float *q = P + slot * (6 * 32 * 4) + lane * 4;
+            if (warp < nw / 2) {
 #pragma unroll
-            for (int x = 0; x < 4; x++)
+                for (int x = 0; x < 6; x++)
+                    *reinterpret_cast<float4 *>(q + x * 128) = make_float4(gc[x][0], gc[x][1], gc[x][2], gc[x][3]);
+            }
+            __syncthreads();
+            if (warp >= nw / 2) {
 #pragma unroll
-                for (int y = 0; y < 4; y++) P[(tgroup * kTiles + tile) * 16 + 4 * x + y] = g[x][y];
-        }
-        __syncthreads();
-        for (int e = tid; e < kTiles * 16; e += blockDim.x) {
-            const int tile = e >> 4, xy = e & 15;
-            float v = 0.0f;
-            for (int gg = 0; gg < kGroups; gg++) v += P[(gg * kTiles + tile) * 16 + xy];
-            int t = tile, r = 0;
-            while (t >= 8 - r) { t -= 8 - r; r++; }
-            s.G[(4 * r + (xy >> 2)) * kEbTrials + 4 * (r + t) + (xy & 3)] = 2.0f * v;
+                for (int x = 0; x < 6; x++) {
+                    float4 v = *reinterpret_cast<float4 *>(q + x * 128);
+                    v.x += gc[x][0];
+                    v.y += gc[x][1];
+                    v.z += gc[x][2];
+                    v.w += gc[x][3];
+                    *reinterpret_cast<float4 *>(q + x * 128) = v;
+                }
+            }
+            __syncthreads();
+            // element e = (tile, lane, j) of the accumulator layout
+            for (int e = tid; e < 6 * 32 * 4; e += blockDim.x) {
+                float v = 0.0f;
+                for (int sl = 0; sl < nw / 2; sl++) v += P[sl * (6 * 32 * 4) + e];
+                const int x = e >> 7, ln = (e >> 2) & 31, j = e & 3;
+                const int mi = x < 4 ? 0 : 1, nj = x < 4 ? x : x - 2;
+                const int row = 16 * mi + (ln >> 2) + ((j & 2) ? 8 : 0);
+                const int col = 8 * nj + 2 * (ln & 3) + (j & 1);
+                s.G[row * kEbTrials + col] = 2.0f * v;
+            }
         }
         __syncthreads();
         // ---- resolve the block in order (warp 0; lane m = trial m)

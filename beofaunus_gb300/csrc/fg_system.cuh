@@ -29,7 +29,7 @@ enum : int32_t {
     kErrKCapacity = 4,      // more k-vectors than threads * kMaxKPerThread
     kErrNonFinite = 8,      // dU was NaN
     kErrQkMismatch = 16,    // a rebuild did not reproduce the incremental Q(k)
-    kErrLaunch = 64,        // a cluster kernel ran with another cluster shape than requested
+    kErrLaunch = 64,        // a kernel ran with another cluster or block shape than it was written for
 };
 
 // One trial of the stream (40 bytes): particle index, fixed-point
