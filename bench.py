@@ -32,9 +32,11 @@ e2e           the same batch through the C-ABI with host buffers: per step the
 single_chain  one system alone (one CTA), same kernel, same stream kind.
 plain_per_trial_api  fg_trial_du + fg_commit per trial from a host loop: the
               plain drop-in Energybase path.
-roofline      the sweep kernel against the FP32 pipe (pair and k-space terms
-              are FP32 arithmetic, no dense contraction): algorithmic FLOP per
-              trial (cost model below) x trials per launch / mean launch time.
+roofline      the Ewald block kernel against the FP32 pipe (pair and k-space
+              terms are FP32 arithmetic; the block's 32x32 Gram matrix is the
+              only contraction, a tenth of the kernel, on the tensor cores):
+              algorithmic FLOP per trial (cost model below) x trials per
+              launch / mean launch time.
 cpu_baseline  the FP64 oracle port of the reference's per-trial work, one
               process per host core, on a time-bounded sample.
 --impl reference   that CPU path alone, in the same units (its line is the
@@ -275,12 +277,12 @@ def fp32_gemm_tflops(torch, dev):
 
 
 def profiled_traffic():
-    """DRAM bytes per sweep-kernel launch from the committed ncu summary
-    (a line 'dram_bytes_per_launch_full: <n>'), or None."""
-    path = os.path.join(ROOT, "profiles", "sweep_kernel_rpm16k_batch.md")
+    """DRAM bytes per trial of the Ewald block kernel from the committed ncu
+    summary (a line 'dram_bytes_per_trial: <n>'), or None."""
+    path = os.path.join(ROOT, "profiles", "ewald_block_kernel_rpm16k_batch.md")
     try:
         for line in open(path):
-            m = re.match(r"\s*[-*]?\s*dram_bytes_per_launch_full:\s*([0-9.eE+]+)", line)
+            m = re.match(r"\s*[-*]?\s*dram_bytes_per_trial:\s*([0-9.eE+]+)", line)
             if m:
                 return float(m.group(1))
     except OSError:
@@ -399,7 +401,8 @@ def run_ours(args, rank, world):
     sm_mhz = (clk or {}).get("sm_mhz") or 1900.0
     mufu_peak = sms * 16 * sm_mhz * 1e6
     mufu_frac = PAIRS_PER_TRIAL * MUFU_PER_PAIR * trials_per_launch / avg_launch_s / mufu_peak
-    traffic = profiled_traffic()
+    per_trial = profiled_traffic()
+    traffic = per_trial * trials_per_launch if per_trial is not None else None
 
     # ---- single chain: one system, one CTA
     p, xyz, q, ids = workloads.rpm16k(seed=seeds[B], update_frequency=1000, start=xyzs[B])
@@ -452,8 +455,9 @@ def run_ours(args, rank, world):
                      "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (best of 5)",
                      "flop_per_trial": flop_per_trial, "trials_per_launch": trials_per_launch,
                      "mean_launch_ms": avg_launch_s * 1e3, "mufu_frac": mufu_frac,
-                     "note": "pair and k-space terms are FP32 arithmetic with no dense contraction; "
-                             "each system is a sequential Markov chain on one SM"},
+                     "note": "pair and k-space terms are FP32 arithmetic (the 32x32 Gram matrix of a "
+                             "trial block runs on the tensor cores, mma.sync TF32 x3); each system is a "
+                             "sequential Markov chain on one SM"},
         "single_chain": {"value": single, "unit": UNIT, "us_per_trial": 1e6 / single},
         "plain_per_trial_api": {"value": plain, "unit": UNIT},
         "batched_over_plain": value / plain,
