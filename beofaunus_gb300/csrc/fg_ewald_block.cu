@@ -164,23 +164,33 @@ __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, c
         len[a] = 3 + (delta != 0 ? 1 : 0);
     }
     const int ncell = len[0] * len[1] * len[2];
+    // the stencil position (ix, iy, iz) advances incrementally (no integer
+    // division per cell); wrapped cell coordinate per axis
+    auto wrap = [&](int c, int a) {
+        c += (c < 0) ? d.nc[a] : 0;
+        return c - ((c >= d.nc[a]) ? d.nc[a] : 0);
+    };
+    int ix = 0, iy = 0, iz = 0;
     // two stencil cells per pass: their loads are independent, so a warp
     // keeps two cell records in flight (four spill at 128 registers)
     for (int k0 = 0; k0 < ncell; k0 += 2) {
         int cid[2], cnt[2];
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            const int k = k0 + u;
             cid[u] = 0;
             cnt[u] = 0;
-            if (k < ncell) {
-                const int ix = k % len[0], iy = (k / len[0]) % len[1], iz = k / (len[0] * len[1]);
-                int cx = lo[0] + ix, cy = lo[1] + iy, cz = lo[2] + iz;
-                cx += (cx < 0) ? d.nc[0] : 0; cx -= (cx >= d.nc[0]) ? d.nc[0] : 0;
-                cy += (cy < 0) ? d.nc[1] : 0; cy -= (cy >= d.nc[1]) ? d.nc[1] : 0;
-                cz += (cz < 0) ? d.nc[2] : 0; cz -= (cz >= d.nc[2]) ? d.nc[2] : 0;
-                cid[u] = (cz * d.nc[1] + cy) * d.nc[0] + cx;
+            if (k0 + u < ncell) {
+                cid[u] = (wrap(lo[2] + iz, 2) * d.nc[1] + wrap(lo[1] + iy, 1)) * d.nc[0] + wrap(lo[0] + ix, 0);
                 cnt[u] = s.ccount[cid[u]];
+                ix++;
+                if (ix == len[0]) {
+                    ix = 0;
+                    iy++;
+                    if (iy == len[1]) {
+                        iy = 0;
+                        iz++;
+                    }
+                }
             }
         }
         const int cmax = max(cnt[0], cnt[1]);
