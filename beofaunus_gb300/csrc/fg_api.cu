@@ -821,6 +821,8 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
             if (d.s2[t] != d.s2[0] || d.eps4[t] != d.eps4[0] || d.qeqe[t] != d.qeqe[0]) uniform = false;
         }
     d.uniform_types = uniform ? 1 : 0;
+    d.reach2 = d.rc2;
+    for (int t = 0; t < nt * nt; t++) d.reach2 = std::max(d.reach2, std::max(d.wca2[t], d.s2[t]));
 
     // Ewald k-space
     std::vector<int> n3;

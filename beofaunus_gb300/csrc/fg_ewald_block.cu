@@ -141,14 +141,58 @@ __device__ __forceinline__ void eb_qbar(int nthreads) {
     asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
+// Real-space base of one trial by one warp. Candidates (cell stencil, or all
+// particles) are screened by distance first: only those within reach2 of the
+// old or the new position enter a 32-entry warp queue in shared memory (qp,
+// qm), which is evaluated with all lanes busy when the next batch would
+// overflow it. Skipped candidates contribute exactly zero (every pair term is
+// zero beyond reach2), so the sum is that of the full loop, in another order.
 template <bool CELLS>
-__device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, const Smem &s, float &accf, df &accd) {
+__device__ __forceinline__ void eb_flush(int qn, const int4 *qp, const int2 *qm, const Move &m, const SysDesc &d,
+                                         float &accf, df &accd) {
     const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (lane < qn) {
+        const int2 e = qm[lane];
+        pair_candidate<MODEL_EWALD>(m, qp[lane], e.y, (CELLS ? d.cell_ext : d.pos_ext) + e.x, d, accf, accd);
+    }
+    __syncwarp();
+}
+template <bool CELLS>
+__device__ __forceinline__ void eb_push(bool f, int4 pos, int idx, int t, int &qn, int4 *qp, int2 *qm,
+                                        const Move &m, const SysDesc &d, float &accf, df &accd) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t mask = __ballot_sync(0xffffffffu, f);
+    const int c = __popc(mask);
+    if (qn + c > 32) {
+        eb_flush<CELLS>(qn, qp, qm, m, d, accf, accd);
+        qn = 0;
+    }
+    if (f) {
+        const int r = qn + __popc(mask & ((1u << lane) - 1u));
+        qp[r] = pos;
+        qm[r] = make_int2(idx, t);
+    }
+    qn += c;
+}
+__device__ __forceinline__ bool eb_in_reach(int4 p, const Move &m, const SysDesc &d) {
+    return dist2(p, m.hn[0], m.hn[1], m.hn[2], d) <= d.reach2 || dist2(p, m.ho[0], m.ho[1], m.ho[2], d) <= d.reach2;
+}
+
+template <bool CELLS>
+__device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, const Smem &s, int4 *qp, int2 *qm,
+                                              float &accf, df &accd) {
+    const int lane = threadIdx.x & 31;
+    int qn = 0;
     if (!CELLS) {
-        for (int j = lane; j < d.N; j += 32) {
-            if (j == m.i) continue;
-            pair_candidate<MODEL_EWALD>(m, d.pos4[j], d.ptype[j], &d.pos_ext[j], d, accf, accd);
+        for (int b = 0; b < d.N; b += 32) {   // warp-uniform trip count
+            const int j = b + lane;
+            const bool v = j < d.N && j != m.i;
+            const int4 p = v ? d.pos4[j] : make_int4(0, 0, 0, 0);
+            const int t = v ? d.ptype[j] : 0;
+            eb_push<CELLS>(v && eb_in_reach(p, m, d), p, j, t, qn, qp, qm, m, d, accf, accd);
         }
+        eb_flush<CELLS>(qn, qp, qm, m, d, accf, accd);
         return;
     }
     int co[3], cn[3], lo[3], len[3];
@@ -172,7 +216,7 @@ __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, c
     };
     int ix = 0, iy = 0, iz = 0;
     // two stencil cells per pass: their loads are independent, so a warp
-    // keeps two cell records in flight (four spill at 128 registers)
+    // keeps two cell records in flight
     for (int k0 = 0; k0 < ncell; k0 += 2) {
         int cid[2], cnt[2];
 #pragma unroll
@@ -194,7 +238,8 @@ __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, c
             }
         }
         const int cmax = max(cnt[0], cnt[1]);
-        for (int slot = lane; slot < cmax; slot += 32) {
+        for (int b = 0; b < cmax; b += 32) {   // warp-uniform trip count
+            const int slot = b + lane;
             int pid[2];
             int4 pos[2];
 #pragma unroll
@@ -205,12 +250,13 @@ __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, c
             }
 #pragma unroll
             for (int u = 0; u < 2; u++) {
-                if (pid[u] < 0 || (pid[u] & 0xFFFFFF) == m.i) continue;
-                pair_candidate<MODEL_EWALD>(m, pos[u], pid[u] >> 24, &d.cell_ext[cid[u] * d.cap + slot], d, accf,
-                                            accd);
+                const bool v = pid[u] >= 0 && (pid[u] & 0xFFFFFF) != m.i;
+                eb_push<CELLS>(v && eb_in_reach(pos[u], m, d), pos[u], cid[u] * d.cap + slot, pid[u] >> 24, qn, qp,
+                               qm, m, d, accf, accd);
             }
         }
     }
+    eb_flush<CELLS>(qn, qp, qm, m, d, accf, accd);
 }
 
 // dU of trial m from one partner at high words p (charge bits in .w), type t,
@@ -329,12 +375,15 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             }
             s.corr[e] = out;
         }
-        // ---- real-space base: warp w sums trials w, w + nwarp, ...
+        // ---- real-space base: warp w sums trials w, w + nwarp, ...; its
+        // candidate queue lives in the (not yet used) increment buffer
         for (int m = warp; m < kb; m += nwarp) {
             const Move mv = s.mv[m];
             float accf = 0.0f;
             df accd = {0.0f, 0.0f};
-            eb_pairs_warp<CELLS>(mv, d, s.b, accf, accd);
+            int4 *qp = reinterpret_cast<int4 *>(s.delta) + warp * 48;
+            int2 *qm = reinterpret_cast<int2 *>(qp + 32);
+            eb_pairs_warp<CELLS>(mv, d, s.b, qp, qm, accf, accd);
             const df p = warp_sum_df(df_add_f(accd, accf));
             if (lane == 0) s.partR[m] = make_float2(p.hi, p.lo);
         }

@@ -127,6 +127,7 @@ struct alignas(16) SysDesc {
     float qk_scale;          // 2^g
     int32_t nseg;            // runs of k-vectors that share (nx, ny), for the rebuild
     const int2 *kseg;        // {k0 | len << 24, nx & 0xFF | (ny & 0xFF) << 8 | (nz0 & 0xFF) << 16}
+    float reach2;            // no pair term acts beyond r^2 = reach2 (cutoff, WCA range, core)
 };
 
 }  // namespace fg
