@@ -23,7 +23,7 @@ namespace fg {
 
 constexpr int kEbTrials = 32;
 constexpr int kEbThreads = 512;
-constexpr int kEbKc = 128;   // k-vectors per chunk
+constexpr int kEbKc = 128;   // scratch buffer rows (of 32 float2)
 
 struct EbSmem {
     Smem b;          // sc_tab, qfix, kpack, cells as in the one-trial kernel; kvec here holds
@@ -36,7 +36,8 @@ struct EbSmem {
     float2 *kbase;   // [32] reciprocal base (df)
     float2 *corr;    // [32][32] real-space + surface corrections (df)
     float *G;        // [32][32] reciprocal cross terms
-    float2 *delta;   // [kEbKc][32] increments of the current chunk
+    float2 *delta;   // [kEbKc x 32] scratch: real-space queues and k-space trial records, then
+                     // the Gram and reciprocal-base partials, then the commit's axis tables
     float2 *Mdf;     // [3] surface dipole M (df)
 };
 
@@ -93,9 +94,8 @@ __device__ inline EbSmem eb_carve(char *base, const SysDesc &d, bool cells) {
 
 // Real-space sum of one trial by one warp: every stencil cell (cell list) or
 // every particle (no cell list), lanes over the slots.
-// One k-step of the Gram matrix on the tensor cores: components c = 8 real
-// parts/imaginary parts of complex k-vectors kb .. kb+3 of the chunk buffer
-// X[k][trial] (float2 = re, im; sqrt(A') already applied). mma.sync
+// One k-step of the Gram matrix on the tensor cores: components c = the real
+// and imaginary parts of 4 consecutive k-vectors of X = sqrt(A') D. mma.sync
 // m16n8k8 TF32 with the three-product split (hi hi + hi lo + lo hi, each
 // operand split into a TF32 high part and the TF32 rounding of the rest)
 // keeps FP32-level accuracy. Lane (gq = lane / 4, gt = lane % 4) holds the
@@ -114,16 +114,14 @@ __device__ __forceinline__ void eb_mma(float c[4], const uint32_t a[4], uint32_t
                  : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
-__device__ __forceinline__ void eb_gram_step(const float *X, int kb, int gq, int gt, float gc[6][4]) {
+__device__ __forceinline__ void eb_gram_regs(const float xf[4][2], float gc[6][4]) {
     uint32_t hi[4][2], lo[4][2];
 #pragma unroll
     for (int r = 0; r < 4; r++)
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-            const int k = kb + 2 * h + (gt >> 1);
-            const float x = X[(k * kEbTrials + gq + 8 * r) * 2 + (gt & 1)];
-            hi[r][h] = eb_tf32(x);
-            lo[r][h] = eb_tf32(x - __uint_as_float(hi[r][h]));
+            hi[r][h] = eb_tf32(xf[r][h]);
+            lo[r][h] = eb_tf32(xf[r][h] - __uint_as_float(hi[r][h]));
         }
 #pragma unroll
     for (int t = 0; t < 6; t++) {
@@ -322,11 +320,15 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
     const int uf = d.update_frequency;
     bool rebuild = false;
     int err = 0;
-    // k-space work split: 16 threads per trial, each a fixed set of k-vectors
-    const int mt = tid >> 4, sub = tid & 15;
-    // Gram G = X X^T over the real components of X = sqrt(A') D on the tensor
-    // cores (eb_gram_step): warp w takes the k-steps w, w + 16 of each chunk
-    const int gq = lane >> 2, gt = lane & 3;
+    // k space: warp w takes the k-steps (4 k-vectors) w, w + 16, ...; lane
+    // (gq, gt) holds the Gram fragments of trials gq + 8 r, components gt and
+    // gt + 4 of the step (eb_gram_regs)
+    const int gq = lane >> 2, gt = lane & 3, gh = gt & 1, gk = gt >> 1;
+    // per-trial records of the k-space phase (in the increment buffer, past
+    // the real-space queues): {d 2pi/L, q eff}, {old high words, fast}, {new high words}
+    float4 *rA = reinterpret_cast<float4 *>(reinterpret_cast<char *>(s.delta) + 16384);
+    int4 *rB = reinterpret_cast<int4 *>(rA + kEbTrials);
+    int4 *rC = rB + kEbTrials;
     while (cur < stop) {
         const int kb = (int)((stop - cur) < (int64_t)kEbTrials ? (stop - cur) : (int64_t)kEbTrials);
         // ---- trials of the block (old coordinates: the block start)
@@ -352,6 +354,22 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             for (int a = 0; a < tid; a++)
                 if (s.mv[a].i == i) c |= 1u << a;
             s.col[tid] = c;
+        }
+        if (tid < kEbTrials) {
+            float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            int4 b = make_int4(0, 0, 0, 1), c = make_int4(0, 0, 0, 0);
+            if (tid < kb) {
+                const Move &M = s.mv[tid];
+                a = make_float4(M.dxf[0] * tpl[0], M.dxf[1] * tpl[1], M.dxf[2] * tpl[2], M.q * d.eff[M.ti]);
+                // |k.d| <= kcc (|d_x| + |d_y| + |d_z|) 2pi/L: within the Taylor
+                // range of expm1_i_horner every k takes the branch-free path
+                const bool fast = (float)d.kcc * (fabsf(a.x) + fabsf(a.y) + fabsf(a.z)) <= 1.6f;
+                b = make_int4(M.ho[0], M.ho[1], M.ho[2], fast ? 1 : 0);
+                c = make_int4(M.hn[0], M.hn[1], M.hn[2], 0);
+            }
+            rA[tid] = a;
+            rB[tid] = b;
+            rC[tid] = c;
         }
         // ---- real-space and surface corrections c(a, m), a < m
         for (int e = tid; e < kEbTrials * kEbTrials; e += blockDim.x) {
@@ -387,99 +405,68 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             const df p = warp_sum_df(df_add_f(accd, accf));
             if (lane == 0) s.partR[m] = make_float2(p.hi, p.lo);
         }
-        // ---- reciprocal base and Gram matrix, streaming the increments by chunks
-        int hm[3] = {0, 0, 0}, hn3[3] = {0, 0, 0};
-        float dxs[3] = {0.0f, 0.0f, 0.0f}, qe = 0.0f;   // displacement times 2 pi / L
-        if (mt < kb) {
-            const Move &M = s.mv[mt];
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                hm[a] = M.ho[a];
-                hn3[a] = M.hn[a];
-                dxs[a] = M.dxf[a] * tpl[a];
-            }
-            qe = M.q * d.eff[M.ti];
-        }
-        float kacc = 0.0f;
+        // ---- reciprocal base and Gram matrix. Lane (gq, gt) and its partner
+        // lane ^ 1 need the same increments sqrt(A') D[trial][k] (trials
+        // gq + 8 r, k-vectors 4 st + gk and 4 st + 2 + gk), one the real and
+        // one the imaginary part: each computes half (r = 2 gh, 2 gh + 1) and
+        // they swap the other part. No chunk buffer, no barriers in the loop.
+        __syncthreads();   // trial records written, real-space queues done
+        float kac[2] = {0.0f, 0.0f};   // reciprocal base of trials gq + 8 (2 gh + rr)
         float gc[6][4];
 #pragma unroll
         for (int x = 0; x < 6; x++)
 #pragma unroll
             for (int y = 0; y < 4; y++) gc[x][y] = 0.0f;
-        // |k.d| <= kcc (|dxs_x| + |dxs_y| + |dxs_z|): when that bound is within
-        // the Taylor range of expm1_i_horner every k takes the same branch-free
-        // path, and the chunk loop below is unrolled for independent chains
-        const bool fast = (float)d.kcc * (fabsf(dxs[0]) + fabsf(dxs[1]) + fabsf(dxs[2])) <= 1.6f;
-        for (int kc0 = 0; kc0 < K; kc0 += kEbKc) {
-            __syncthreads();   // the previous chunk's Gram reads are done
-            if (fast) {
-#pragma unroll 2
-                for (int kl = sub; kl < kEbKc; kl += 16) {
-                    const int k = min(kc0 + kl, K - 1);
-                    const float live = (kc0 + kl < K) ? qe : 0.0f;   // 0 past K and for idle trials
-                    int nx, ny, nz;
-                    unpack_n(s.b.kpack[k], nx, ny, nz);
-                    const float2 e = sincos_turns(phase(nx, ny, nz, hm), s.b.sc_tab);
-                    const float4 kv = s.b.kvec[k];   // {A', Re Q, Im Q, sqrt A'}
-                    const float phi = fmaf(small_int_to_float(nx), dxs[0],
-                                           fmaf(small_int_to_float(ny), dxs[1], small_int_to_float(nz) * dxs[2]));
-                    float2 dd = cmul(e, expm1_i_horner(phi));
-                    dd.x *= live;
-                    dd.y *= live;
-                    kacc = fmaf(kv.x, fmaf(2.0f, fmaf(kv.y, dd.x, kv.z * dd.y), fmaf(dd.x, dd.x, dd.y * dd.y)), kacc);
-                    s.delta[kl * kEbTrials + mt] = make_float2(dd.x * kv.w, dd.y * kv.w);
-                }
-            } else
-            for (int kl = sub; kl < kEbKc; kl += 16) {
-                const int k = kc0 + kl;
-                float2 dd = make_float2(0.0f, 0.0f);
-                if (mt < kb && k < K) {
-                    int nx, ny, nz;
-                    unpack_n(s.b.kpack[k], nx, ny, nz);
-                    const uint32_t ph = phase(nx, ny, nz, hm);
+        for (int st = warp; 4 * st < K; st += kEbThreads / 32) {
+            float xf[4][2];   // component gh of sqrt(A') D[gq + 8 r][k_j]
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int kraw = 4 * st + 2 * j + gk;
+                const int k = min(kraw, K - 1);
+                int nx, ny, nz;
+                unpack_n(s.b.kpack[k], nx, ny, nz);
+                const float4 kv = s.b.kvec[k];   // {A', Re Q, Im Q, sqrt A'}
+                const float fx = small_int_to_float(nx), fy = small_int_to_float(ny), fz = small_int_to_float(nz);
+#pragma unroll
+                for (int rr = 0; rr < 2; rr++) {
+                    const int t = gq + 8 * (2 * gh + rr);
+                    const float4 a = rA[t];
+                    const int4 b = rB[t];
+                    const int ho[3] = {b.x, b.y, b.z};
+                    const uint32_t ph = phase(nx, ny, nz, ho);
                     const float2 e = sincos_turns(ph, s.b.sc_tab);
-                    const float4 kv = s.b.kvec[k];   // {A', Re Q, Im Q, sqrt A'}
-                    const float phi = fmaf(small_int_to_float(nx), dxs[0],
-                                           fmaf(small_int_to_float(ny), dxs[1], small_int_to_float(nz) * dxs[2]));
+                    const float phi = fmaf(fx, a.x, fmaf(fy, a.y, fz * a.z));
                     float2 w;
-                    if (fabsf(phi) <= 1.6f) {
+                    if (b.w || fabsf(phi) <= 1.6f) {
                         w = expm1_i_horner(phi);
                     } else {
-                        const float2 en = sincos_turns(phase(nx, ny, nz, hn3) - ph, s.b.sc_tab);
+                        const int4 c = rC[t];
+                        const int hn[3] = {c.x, c.y, c.z};
+                        const float2 en = sincos_turns(phase(nx, ny, nz, hn) - ph, s.b.sc_tab);
                         w = make_float2(en.x - 1.0f, en.y);
                     }
-                    dd = cmul(e, w);
-                    dd.x *= qe;
-                    dd.y *= qe;
-                    kacc = fmaf(kv.x, fmaf(2.0f, fmaf(kv.y, dd.x, kv.z * dd.y), fmaf(dd.x, dd.x, dd.y * dd.y)), kacc);
-                    // the Gram tiles see sqrt(A') D, so A' needs no product there
-                    dd.x *= kv.w;
-                    dd.y *= kv.w;
+                    const float live = kraw < K ? a.w : 0.0f;   // q eff; 0 past K and for idle trials
+                    float2 dd = cmul(e, w);
+                    dd.x *= live;
+                    dd.y *= live;
+                    kac[rr] = fmaf(kv.x, fmaf(2.0f, fmaf(kv.y, dd.x, kv.z * dd.y), fmaf(dd.x, dd.x, dd.y * dd.y)),
+                                   kac[rr]);
+                    const float own = (gh ? dd.y : dd.x) * kv.w, other = (gh ? dd.x : dd.y) * kv.w;
+                    const float recv = __shfl_xor_sync(0xffffffffu, other, 1);
+                    xf[rr][j] = gh ? recv : own;
+                    xf[2 + rr][j] = gh ? own : recv;
                 }
-                s.delta[kl * kEbTrials + mt] = dd;
             }
-            __syncthreads();
-            {
-                const int kend = min(kEbKc, K - kc0);
-                for (int st = warp; 4 * st < kend; st += kEbThreads / 32)
-                    eb_gram_step(reinterpret_cast<const float *>(s.delta), 4 * st, gq, gt, gc);
-            }
+            eb_gram_regs(xf, gc);
         }
-        // reciprocal base: the 16 threads of trial mt, in df
-        {
-            df v = {kacc, 0.0f};
-#pragma unroll
-            for (int o = 8; o > 0; o >>= 1) {
-                df w;
-                w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
-                w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
-                v = df_add(v, w);
-            }
-            if (sub == 0 && mt < kEbTrials) s.kbase[mt] = make_float2(v.hi, v.lo);
-        }
-        // Gram: the 16 warps' partial tiles meet in the (now free) chunk buffer
-        // in two rounds and are summed in a fixed order, so the result does
-        // not depend on timing
+        // reciprocal base per trial: partials of (warp, lane, rr) summed in a
+        // fixed order in df
+        float *KP = reinterpret_cast<float *>(reinterpret_cast<char *>(s.delta) + 28672);   // [16][32][2]
+        KP[(warp * 32 + lane) * 2] = kac[0];
+        KP[(warp * 32 + lane) * 2 + 1] = kac[1];
+        // Gram: the 16 warps' partial tiles meet in the (now free) increment
+        // buffer in two rounds and are summed in a fixed order, so the result
+        // does not depend on timing
         __syncthreads();
         float *P = reinterpret_cast<float *>(s.delta);   // [8 slots][6 tiles][32 lanes][4]
         {
@@ -489,6 +476,15 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
 #pragma unroll
                 for (int x = 0; x < 6; x++)
                     *reinterpret_cast<float4 *>(q + x * 128) = make_float4(gc[x][0], gc[x][1], gc[x][2], gc[x][3]);
+            }
+            if (tid < kEbTrials) {
+                // trial t = gq' + 8 r': lanes gq' * 4 + (r' >> 1) + 2 gk', slot rr = r' & 1
+                const int tq = tid & 7, tr = tid >> 3;
+                df v = {0.0f, 0.0f};
+                for (int w = 0; w < nw; w++)
+                    for (int g2 = 0; g2 < 2; g2++)
+                        v = df_add_f(v, KP[(w * 32 + tq * 4 + (tr >> 1) + 2 * g2) * 2 + (tr & 1)]);
+                s.kbase[tid] = make_float2(v.hi, v.lo);
             }
             __syncthreads();
             if (warp >= nw / 2) {
