@@ -933,6 +933,21 @@ __global__ void __launch_bounds__(kSweepThreads) commit_kernel(const SysDesc *__
 // the system of a batch; only systems with rebuild_pending set do work.
 constexpr int kQkRun = 8;
 constexpr int kQkMaxThreads = 512;
+// One pass over nb staged particles for runs of (at most) L k-vectors.
+template <int L>
+__device__ __forceinline__ void qk_pass(const float2 *et, int T, const float *q2g, int nb, int ix, int iy, int iz,
+                                        unsigned ax[kQkRun], unsigned ay[kQkRun]) {
+    for (int jj = 0; jj < nb; jj++) {
+        const float2 *e = et + jj * T;
+        const float2 w = qk_w(q2g[jj], e[ix], e[iy]);
+#pragma unroll
+        for (int u = 0; u < L; u++) {
+            const int2 c = qk_term(w, e[iz + u]);
+            ax[u] += (unsigned)c.x;
+            ay[u] += (unsigned)c.y;
+        }
+    }
+}
 constexpr int kQkMaxStage = 64;
 __host__ __device__ __forceinline__ size_t qk_rebuild_smem(int stage, int T, int threads) {
     return (size_t)stage * T * 8 + (size_t)2 * kQkRun * threads * 8 + (size_t)stage * (16 + 4);
@@ -964,6 +979,7 @@ __global__ void __launch_bounds__(kQkMaxThreads) qk_rebuild_kernel(const SysDesc
         }
 #pragma unroll
         for (int u = 0; u < 2 * kQkRun; u++) tot[u * nt + tid] = 0;
+        const int wl = __reduce_max_sync(0xffffffffu, len);   // warp-uniform run length
         int4 pn = make_int4(0, 0, 0, 0);
         float qn = 0.0f;
         if (tid < stage && j0 + tid < j1) {
@@ -1003,19 +1019,20 @@ __global__ void __launch_bounds__(kQkMaxThreads) qk_rebuild_kernel(const SysDesc
                 unsigned ax[kQkRun], ay[kQkRun];
 #pragma unroll
                 for (int u = 0; u < kQkRun; u++) ax[u] = ay[u] = 0u;
-                // all kQkRun terms unconditionally (no branches in the hot
-                // loop); those past len read entries further along the
-                // buffer (at most kQkRun - 1 past the last record, still
-                // inside the shared allocation) and are dropped below
-                for (int jj = 0; jj < nb; jj++) {
-                    const float2 *e = et + jj * T;
-                    const float2 w = qk_w(q2g[jj], e[ix], e[iy]);
-#pragma unroll
-                    for (int u = 0; u < kQkRun; u++) {
-                        const int2 c = qk_term(w, e[iz + u]);
-                        ax[u] += (unsigned)c.x;
-                        ay[u] += (unsigned)c.y;
-                    }
+                // the warp's longest run sets the trip count (runs are sorted
+                // by length, so warps are nearly uniform); terms past a lane's
+                // len read entries further along the buffer (at most
+                // kQkRun - 1 past the last record, still inside the shared
+                // allocation) and are dropped below
+                switch (wl) {
+                    case 1: qk_pass<1>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 2: qk_pass<2>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 3: qk_pass<3>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 4: qk_pass<4>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 5: qk_pass<5>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 6: qk_pass<6>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 7: qk_pass<7>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    default: qk_pass<8>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
                 }
 #pragma unroll
                 for (int u = 0; u < kQkRun; u++)
