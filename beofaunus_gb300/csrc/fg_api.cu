@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <random>
 #include <string>
@@ -111,6 +112,8 @@ struct fg_system {
     std::vector<int32_t> types;
     double self_energy = 0, surf_c = 0, recip_c = 0;
     int threads = 0;
+    int ctas = 0;                  // block-kernel CTAs per system (0: tuned cache / heuristic)
+    std::vector<double> charges;   // host copy of the uploaded charges (clones for tuning)
     bool use_cells = false, pos_smem = false;
     int nc[3] = {0, 0, 0};
     int cap = 0;
@@ -294,12 +297,35 @@ int dh_block_max_cluster() {
     return best;
 }
 
-// CTAs for one system alone: about 2048 particles per CTA.
+// Launch shapes chosen by the autotuner (fg_tune.cu), process-wide:
+// CTAs per system for a DH+LJ system alone, per power-of-two size class, and
+// the least particles per CTA when a batch or the server shares the SMs out.
+std::mutex g_tune_mu;
+std::map<int, int> g_tune_dh_ctas;   // floor(log2 N) -> CTAs
+int g_tune_min_per_cta = 256;
+
+int size_class(int N) {
+    int c = 0;
+    while ((2 << c) <= N) c++;
+    return c;
+}
+
+// CTAs for one system alone: the tuned choice for its size class, else about
+// 2048 particles per CTA.
 int dh_block_ctas(int N) {
     const int maxc = dh_block_max_cluster();
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_dh_ctas.find(size_class(N));
+        if (it != g_tune_dh_ctas.end()) return std::max(1, std::min(it->second, maxc));
+    }
     int C = 1;
     while (C < maxc && (N + C - 1) / C > 2048) C <<= 1;
     return C;
+}
+int tuned_min_per_cta() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_tune_min_per_cta;
 }
 
 int dh_sm_count() {
@@ -312,8 +338,8 @@ int dh_sm_count() {
 // CTAs per system for systems run side by side: start at one each, then keep
 // doubling the system with the most work per CTA (weight / CTAs) while the
 // SMs hold every CTA at once, the device allows the cluster and each CTA keeps
-// at least 256 particles. weight ~ pair evaluations of the launch.
-std::vector<int> dh_block_ctas_many(const std::vector<int> &N, const std::vector<double> &w) {
+// at least min_per_cta particles. weight ~ pair evaluations of the launch.
+std::vector<int> dh_block_ctas_many(const std::vector<int> &N, const std::vector<double> &w, int min_per_cta) {
     const int n = (int)N.size();
     std::vector<int> C(n, 1);
     const int maxc = dh_block_max_cluster();
@@ -322,7 +348,7 @@ std::vector<int> dh_block_ctas_many(const std::vector<int> &N, const std::vector
         int best = -1;
         double bw = 0;
         for (int i = 0; i < n; i++) {
-            if (2 * C[i] > maxc || N[i] / (2 * C[i]) < 256 || C[i] > spare) continue;
+            if (2 * C[i] > maxc || N[i] / (2 * C[i]) < min_per_cta || C[i] > spare) continue;
             const double x = w[i] / C[i];
             if (x > bw) {
                 bw = x;
@@ -389,15 +415,15 @@ struct DhGroups {
 
 int dh_groups_build_c(DhGroups &g, const std::vector<int> &N, const std::vector<int> &C);
 
-int dh_groups_build(DhGroups &g, const std::vector<int> &N, const std::vector<double> &w) {
-    return dh_groups_build_c(g, N, dh_block_ctas_many(N, w));
+int dh_groups_build(DhGroups &g, const std::vector<int> &N, const std::vector<double> &w, int min_per_cta) {
+    return dh_groups_build_c(g, N, dh_block_ctas_many(N, w, min_per_cta));
 }
 
-// Largest CTA count a system of N particles is given (>= 256 particles per CTA).
-int dh_block_ctas_cap(int N) {
+// Largest CTA count a system of N particles is given (>= min_per_cta particles per CTA).
+int dh_block_ctas_cap(int N, int min_per_cta) {
     const int maxc = dh_block_max_cluster();
     int C = 1;
-    while (2 * C <= maxc && N / (2 * C) >= 256) C *= 2;
+    while (2 * C <= maxc && N / (2 * C) >= min_per_cta) C *= 2;
     return C;
 }
 
@@ -646,7 +672,8 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
             evs.push_back(b);
             CK(cudaEventRecord(a, h->stream));
             if (dh_block_ok(h)) {
-                rc = dh_block_launch(h->d_desc, nullptr, 1, dh_block_ctas(h->N), h->N, n, h->stream);
+                rc = dh_block_launch(h->d_desc, nullptr, 1, h->ctas > 0 ? h->ctas : dh_block_ctas(h->N), h->N, n,
+                                     h->stream);
                 if (rc) return rc;
             } else {
                 cfg.fn<<<1, cfg.threads, cfg.smem, h->stream>>>(h->d_desc, n, h->sc_tab);
@@ -1027,11 +1054,13 @@ int fg_set_state(fg_system *h, const double *xyz, const double *charge, const in
     std::vector<short4> pe(N);
     std::vector<uint8_t> pt(N);
     h->types.assign(type_ids, type_ids + N);
+    h->charges.resize(N);
     double self = 0, M[3] = {0, 0, 0};
     for (int i = 0; i < N; i++) {
         const int t = type_ids[i];
         if (t < 0 || t >= P.n_types) return fail(FG_ERR_INVALID, "type id %d out of range", t);
         const double q = charge ? charge[i] : P.type_charge[t];
+        h->charges[i] = q;
         int32_t hw[3];
         for (int a = 0; a < 3; a++) {
             if (!std::isfinite(xyz[3 * i + a])) return fail(FG_ERR_INVALID, "non-finite coordinate");
@@ -1359,3 +1388,4 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 #include "fg_batch.cu"
 #include "fg_noalloc.cu"
 #include "fg_mol.cu"
+#include "fg_tune.cu"

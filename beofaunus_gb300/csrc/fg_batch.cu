@@ -114,6 +114,7 @@ struct fg_batch {
     // Debye-Hueckel members without a cell list run the block kernel
     bool dh_block = false;
     DhGroups dh;
+    int min_per_cta = 0;   // schedule: least particles per CTA (0: the tuned process default)
 };
 
 namespace {
@@ -145,7 +146,7 @@ int batch_config(fg_batch *b) {
         w.push_back((double)h->N * h->N);   // a sweep of N trials over N partners
     }
     if (b->dh_block) {
-        int rc = dh_groups_build(b->dh, Ns, w);
+        int rc = dh_groups_build(b->dh, Ns, w, b->min_per_cta > 0 ? b->min_per_cta : tuned_min_per_cta());
         if (rc) return rc;
     }
     return set_smem_attr((const void *)b->cfg.fn, sm);
@@ -603,7 +604,7 @@ int server_grow(fg_server *s, int n) {
 int server_admit(fg_server *s, fg_job *j) {
     const int64_t Nj = (int64_t)j->ids.size();
     const bool blk = j->P.model == FG_MODEL_DH_LJ && !j->P.use_cell_list;
-    const int64_t rt = blk ? round_trials_dh(s, Nj, dh_block_ctas_cap((int)Nj), j->n_trials)
+    const int64_t rt = blk ? round_trials_dh(s, Nj, dh_block_ctas_cap((int)Nj, tuned_min_per_cta()), j->n_trials)
                            : std::min<int64_t>(j->n_trials, round_trials_for(s, Nj));
     j->bytes = job_bytes(j->P, (int)j->ids.size(), rt);
     if (s->used + (int64_t)j->bytes > s->max_bytes) return 1;   // does not fit now
@@ -678,7 +679,7 @@ int fg_server_submit(fg_server *s, const fg_params *params, int32_t n, const dou
     for (fg_job *o : s->jobs)
         if (o->P.model != params->model) return fail(FG_ERR_INVALID, "one model per server");
     const bool blk = params->model == FG_MODEL_DH_LJ && !params->use_cell_list;
-    const int64_t rt = blk ? round_trials_dh(s, n, dh_block_ctas_cap(n), n_trials)
+    const int64_t rt = blk ? round_trials_dh(s, n, dh_block_ctas_cap(n, tuned_min_per_cta()), n_trials)
                            : std::min<int64_t>(n_trials, round_trials_for(s, n));
     if ((int64_t)job_bytes(*params, n, rt) > s->max_bytes) return fail(FG_ERR_CAPACITY, "job larger than the budget");
     fg_job *j = new fg_job();
@@ -746,12 +747,12 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
             dh_n.push_back(run[i]->sys->N);
             dh_w.push_back((double)(run[i]->n_trials - run[i]->done) * run[i]->sys->N);
         }
-    if (!dh_n.empty()) dh_c = dh_block_ctas_many(dh_n, dh_w);
+    if (!dh_n.empty()) dh_c = dh_block_ctas_many(dh_n, dh_w, tuned_min_per_cta());
     int k_dh = 0;
     for (int i = 0; i < n; i++) {
         fg_job *j = run[i];
         fg_system *h = j->sys;
-        counts[i] = dh_block_ok(h) ? round_trials_dh(s, h->N, std::min(dh_c[k_dh++], dh_block_ctas_cap(h->N)),
+        counts[i] = dh_block_ok(h) ? round_trials_dh(s, h->N, std::min(dh_c[k_dh++], dh_block_ctas_cap(h->N, tuned_min_per_cta())),
                                                      j->n_trials - j->done)
                                    : round_trials_of(s, j);
         rc = ensure_trials(h, counts[i], false);
@@ -810,7 +811,7 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         CK(cudaStreamWaitEvent(s->stream, s->join, 0));
     }
     if (first_dh >= 0) {
-        for (size_t k = 0; k < dh_c.size(); k++) dh_c[k] = std::min(dh_c[k], dh_block_ctas_cap(dh_n[k]));
+        for (size_t k = 0; k < dh_c.size(); k++) dh_c[k] = std::min(dh_c[k], dh_block_ctas_cap(dh_n[k], tuned_min_per_cta()));
         rc = dh_groups_build_c(s->dh, dh_n, dh_c);
         if (rc) return rc;
         rc = dh_groups_launch(s->dh, s->d_descs + first_dh, INT64_MAX, s->stream);

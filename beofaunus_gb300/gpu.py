@@ -104,6 +104,10 @@ def lib(build_if_missing=True):
             "fg_mol_run_many": ([dp, i32, dp, dp], ctypes.c_int),
             "fg_mol_running_energy": ([vp, dp], ctypes.c_int),
             "fg_mol_device_bytes": ([vp], ctypes.c_int64),
+            "fg_autotune": ([vp, i64, dp], ctypes.c_int),
+            "fg_batch_autotune": ([vp, i64, dp], ctypes.c_int),
+            "fg_mol_autotune": ([vp, i64, dp], ctypes.c_int),
+            "fg_tune_reset": ([], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -115,6 +119,26 @@ def lib(build_if_missing=True):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("chosen", ctypes.c_int32), ("value", ctypes.c_int32 * 8),
+                ("us_per_trial", ctypes.c_double * 8)]
+
+    def as_dict(self):
+        c = [(int(self.value[i]), float(self.us_per_trial[i])) for i in range(self.n)]
+        return {"candidates": c, "chosen": c[self.chosen][0] if self.n else None}
+
+
+def _tune(fn, h, n_trials):
+    r = TuneReport()
+    _check(fn(h, int(n_trials), ctypes.byref(r)))
+    return r.as_dict()
+
+
+def tune_reset():
+    """Forget the autotuner's recorded launch shapes (fg_tune_reset)."""
+    _check(lib().fg_tune_reset())
 
 
 def _check(rc):
@@ -172,6 +196,11 @@ class System:
     @threads.setter
     def threads(self, t):
         _check(lib().fg_set_threads(self.h, int(t)))
+
+    def autotune(self, n_trials=2048):
+        """Time candidate launch shapes on a clone (fg_autotune) and apply the
+        fastest; returns {"candidates": [(value, us/trial)], "chosen": value}."""
+        return _tune(lib().fg_autotune, self.h, n_trials)
 
     def positions(self):
         out = np.empty((self.n, 3))
@@ -293,6 +322,11 @@ class Batch:
         c = np.ascontiguousarray(counts, dtype=np.int64)
         ids = None if stream_ids is None else np.ascontiguousarray(stream_ids, dtype=np.uint32)
         _check(lib().fg_batch_stream_philox(self.h, _p(c), seed, _p(ids)))
+
+    def autotune(self, n_trials=1024):
+        """Time schedules on clones of the members (fg_batch_autotune) and
+        apply the fastest; returns {"candidates": [...], "chosen": value}."""
+        return _tune(lib().fg_batch_autotune, self.h, n_trials)
 
     def stream_upload(self, member, idx, disp, u):
         idx = np.ascontiguousarray(idx, dtype=np.int32)
@@ -459,6 +493,10 @@ class MolSystem:
         c = np.zeros(2, np.int32)
         _check(lib().fg_mol_get_cluster(self.h, _p(c[:1]), _p(c[1:])))
         return int(c[1])
+
+    def autotune(self, n_trials=256):
+        """Time cluster sizes on a clone (fg_mol_autotune) and apply the fastest."""
+        return _tune(lib().fg_mol_autotune, self.h, n_trials)
 
     def trial_du(self, molecule, new_xyz, new_mu=None, new_cm=None):
         x = np.ascontiguousarray(new_xyz, dtype=np.float64).reshape(-1, 3)

@@ -290,6 +290,31 @@ int fg_mol_total_energy(fg_molsys *h, double *comp);
 int fg_mol_running_energy(fg_molsys *h, double *u);
 int64_t fg_mol_device_bytes(fg_molsys *h);
 
+/* ---------------------------------------------------------------- autotuner
+ * Launch shapes chosen by timing candidates on the device, on a clone of the
+ * caller's system(s): the caller's chains do not advance. Each call applies
+ * the fastest candidate and records it for the process (later systems of the
+ * same size class, later batches and the job server start from it). A shape
+ * changes only the order of floating-point sums. No counterpart in the
+ * reference (its loops have no launch shapes). */
+typedef struct {
+    int32_t n;                /* candidates timed (0: nothing to tune) */
+    int32_t chosen;           /* index of the applied candidate */
+    int32_t value[8];         /* the tuned quantity per candidate */
+    double us_per_trial[8];   /* device time per trial (per member trial for batches) */
+} fg_tune_report;
+
+/* DH+LJ block sweeps: CTAs per system (cluster size, powers of two); Ewald
+ * one-trial sweeps: threads per CTA. n_trials >= 32 per candidate. */
+int fg_autotune(fg_system *h, int64_t n_trials, fg_tune_report *report);
+/* DH+LJ batches: least particles per CTA when the SMs are shared out among
+ * members (128 .. 2048). */
+int fg_batch_autotune(fg_batch *b, int64_t n_trials, fg_tune_report *report);
+/* Rigid molecules: CTAs per system (cluster size). */
+int fg_mol_autotune(fg_molsys *h, int64_t n_trials, fg_tune_report *report);
+/* Forget the recorded choices (back to the built-in heuristics). */
+int fg_tune_reset(void);
+
 #ifdef __cplusplus
 }
 #endif
