@@ -624,6 +624,9 @@ def run_pt(args, rank, world):
         p, xyz, q, ids = workloads.dh_lj_salt(n, 100 + r + rank * 1000003, start="scatter")
         systems.append(System(p, xyz, q, ids))
     batch = Batch(systems)
+    # the schedule (least particles per CTA) chosen by the autotuner on
+    # clones of the 64 replicas, before any timing
+    tune = batch.autotune(args.tune_trials) if args.tune_trials else None
     batch.pt_setup(temps, 1234 + rank)
     steps, warm = args.steps, args.warmup
     for _ in range(warm):
@@ -644,7 +647,8 @@ def run_pt(args, rank, world):
     cfg = {"workload": WORKLOAD_NAMES["pt64"], "replicas": 64, "n_min": min(sizes), "n_max": max(sizes),
            "n_total": sum(sizes), "density_per_A3": 0.002, "debye_length_A": 10.0, "lj_sigma_A": 4.0,
            "lj_eps_kT": 0.2, "temperatures": [0.8, 2.0], "sweeps_per_swap": sweeps,
-           "launch": "one graph per round: Philox draws, persistent sweep over all replicas, swap kernel"}
+           "launch": "one graph per round: Philox draws, persistent sweep over all replicas, swap kernel",
+           "autotune": tune}
     out = base_line(value, steps, warm, ms / steps, world, cfg, "f32 pair terms; df sums",
                     "synthetic (seeded overlap-free starts, Philox streams)")
     out.update({"gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
@@ -823,6 +827,17 @@ def run_serving(args, rank, world):
         jobs = pool.map(_serving_job, [(n, t, 100 + i) for i, (n, t) in enumerate(zip(sizes, temps))])
     sweeps = args.job_sweeps
     budget = int(args.serve_gib * (1 << 30))
+    # the server's schedule threshold comes from the autotuner, timed on a
+    # batch of clones of the first 64 jobs (the process keeps the choice)
+    tune = None
+    if args.tune_trials:
+        from beofaunus_gb300.gpu import Batch, System
+        sample = [System(*jobs[j]) for j in range(min(64, n_jobs))]
+        tb = Batch(sample)
+        tune = tb.autotune(args.tune_trials)
+        tb.close()
+        for x in sample:
+            x.close()
 
     def run_stream(arrivals):
         srv = Server(budget, round_pairs=args.round_pairs)
@@ -874,7 +889,7 @@ def run_serving(args, rank, world):
            "arrival": "Poisson at 0.8 x measured capacity", "capacity_jobs_per_s": capacity,
            "capacity_definition": "completions per s between 10% and 70% of jobs done, all submitted at t=0",
            "all_at_once_makespan_s": span0,
-           "device_budget_GiB": args.serve_gib, "round_pairs": args.round_pairs}
+           "device_budget_GiB": args.serve_gib, "round_pairs": args.round_pairs, "autotune": tune}
     out = base_line(value, 1, 1, 1e3 * span, world, cfg, "f32 pair terms; df sums",
                     "synthetic (seeded overlap-free starts, Philox streams per job)")
     out.update({"latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
@@ -936,6 +951,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample per core")
     ap.add_argument("--ref-seconds", type=float, default=3.0, help="reference arm: seconds per step")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tune-trials", type=int, default=512,
+                    help="pt64/serving: trials per member per autotuner candidate (0: no tuning)")
     ap.add_argument("--value-only", action="store_true", help="device-resident value only (profiling)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -125,8 +125,11 @@ int batch_config(fg_batch *b) {
     int T = b->threads;
     size_t sm = 0;
     b->maxN = b->maxK = b->maxSeg = b->maxKcc = 0;
+    bool all_dh = true;   // DH+LJ block members run by CTA-count groups, whatever their one-CTA variant
+    for (fg_system *h : b->sys) all_dh = all_dh && dh_block_ok(h);
     for (fg_system *h : b->sys) {
-        if (sweep_fn(h) != b->cfg.fn) return fail(FG_ERR_INVALID, "batch members need the same kernel variant");
+        if (!all_dh && sweep_fn(h) != b->cfg.fn)
+            return fail(FG_ERR_INVALID, "batch members need the same kernel variant");
         if (b->threads == 0 || ewald_block_ok(h)) T = std::max(T, sweep_launch_threads(h));
         sm = std::max(sm, sweep_launch_smem(h));
         b->maxN = std::max(b->maxN, h->N);
@@ -145,10 +148,8 @@ int batch_config(fg_batch *b) {
         Ns.push_back(h->N);
         w.push_back((double)h->N * h->N);   // a sweep of N trials over N partners
     }
-    if (b->dh_block) {
-        int rc = dh_groups_build(b->dh, Ns, w, b->min_per_cta > 0 ? b->min_per_cta : tuned_min_per_cta());
-        if (rc) return rc;
-    }
+    if (b->dh_block)   // the one-CTA kernel (cfg.fn) is not launched for these members
+        return dh_groups_build(b->dh, Ns, w, b->min_per_cta > 0 ? b->min_per_cta : tuned_min_per_cta());
     return set_smem_attr((const void *)b->cfg.fn, sm);
 }
 

@@ -8,7 +8,8 @@
 //                      block kernel has one fixed shape: nothing to tune.)
 //   fg_batch_autotune  the batch schedule: least particles per CTA when the
 //                      SMs are shared out among members (also used by the
-//                      job server and batches created afterwards)
+//                      job server and batches created afterwards), timed on
+//                      equal sweeps of every member
 //   fg_mol_autotune    rigid molecules: CTAs per system (cluster size)
 //
 // Timing: each candidate runs a warm-up stream, then a timed stream of
@@ -123,7 +124,15 @@ int fg_batch_autotune(fg_batch *b, int64_t n_trials, fg_tune_report *report) {
     fg_batch *tb = nullptr;
     if (!rc) rc = fg_batch_create(cl.data(), n, &tb);
     std::vector<std::pair<int, double>> t;
-    const std::vector<int64_t> counts(n, n_trials), warm(n, std::max<int64_t>(32, n_trials / 4));
+    // equal sweeps for every member (trials in proportion to N, as in PT
+    // rounds and served jobs): n_trials for the largest member
+    int maxN = 1;
+    for (fg_system *h : b->sys) maxN = std::max(maxN, h->N);
+    std::vector<int64_t> counts(n), warm(n);
+    for (int i = 0; i < n; i++) {
+        counts[i] = std::max<int64_t>(32, n_trials * b->sys[i]->N / maxN);
+        warm[i] = std::max<int64_t>(32, counts[i] / 4);
+    }
     for (int m = 128; m <= 2048 && !rc; m *= 2) {
         tb->min_per_cta = m;
         rc = batch_config(tb);

@@ -308,7 +308,8 @@ typedef struct {
  * one-trial sweeps: threads per CTA. n_trials >= 32 per candidate. */
 int fg_autotune(fg_system *h, int64_t n_trials, fg_tune_report *report);
 /* DH+LJ batches: least particles per CTA when the SMs are shared out among
- * members (128 .. 2048). */
+ * members (128 .. 2048), timed on equal sweeps of the members (n_trials for
+ * the largest, in proportion to N for the others). */
 int fg_batch_autotune(fg_batch *b, int64_t n_trials, fg_tune_report *report);
 /* Rigid molecules: CTAs per system (cluster size). */
 int fg_mol_autotune(fg_molsys *h, int64_t n_trials, fg_tune_report *report);

@@ -105,3 +105,23 @@ def test_mol_tuning_keeps_reference_log():
     r = s.sweep(st)
     assert np.abs(r["du"] - g["du"]).max() < TOL_DU
     np.testing.assert_array_equal(r["acc"], g["acc"])
+
+
+def test_dh_batch_mixes_one_cta_variants():
+    """Members whose one-CTA sweep would differ (positions in shared memory
+    or not) batch together: DH+LJ members all run the block kernel."""
+    from beofaunus_gb300.gpu import Batch, System
+    specs = [workloads.dh_lj_salt(n, seed=300 + n, start="scatter") for n in (256, 12000)]
+    systems = [System(p, x, q, ids) for (p, x, q, ids) in specs]
+    b = Batch(systems)
+    rep = b.autotune(64)
+    assert rep["chosen"] is not None
+    b.stream_philox([512, 512], 3)
+    per, tot = b.run()
+    assert tot["trials"] == 1024 and tot["error_flags"] == 0
+    p, x, q, ids = specs[0]
+    o = OracleSystem(p, x, q, ids)
+    idx, disp, u = philox_stream(3, 0, 0, 512, ids, [p.type_dp[t] for t in range(p.n_types)], list(p.box))
+    ro = o.mc_run_stream(idx, disp, u)
+    assert per[0]["accepted"] == int(ro["acc"].sum())
+    np.testing.assert_allclose(systems[0].positions(), o.positions(), rtol=0, atol=1e-9)
