@@ -1389,3 +1389,4 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 #include "fg_noalloc.cu"
 #include "fg_mol.cu"
 #include "fg_tune.cu"
+#include "fg_rdf.cu"

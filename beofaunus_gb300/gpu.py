@@ -105,6 +105,7 @@ def lib(build_if_missing=True):
             "fg_mol_running_energy": ([vp, dp], ctypes.c_int),
             "fg_mol_device_bytes": ([vp], ctypes.c_int64),
             "fg_autotune": ([vp, i64, dp], ctypes.c_int),
+            "fg_rdf_sample": ([vp, i32, i32, ctypes.c_double, i32, dp, dp], ctypes.c_int),
             "fg_batch_autotune": ([vp, i64, dp], ctypes.c_int),
             "fg_mol_autotune": ([vp, i64, dp], ctypes.c_int),
             "fg_tune_reset": ([], ctypes.c_int),
@@ -201,6 +202,16 @@ class System:
         """Time candidate launch shapes on a clone (fg_autotune) and apply the
         fastest; returns {"candidates": [(value, us/trial)], "chosen": value}."""
         return _tune(lib().fg_autotune, self.h, n_trials)
+
+    def rdf_sample(self, type1, type2, dr, n_bins, hist=None):
+        """Add the current configuration's type1-type2 pair counts (AtomRDF
+        binning) to hist (int64[n_bins], new if None); returns (hist, pairs
+        at any distance counted by this call)."""
+        h = np.zeros(n_bins, np.int64) if hist is None else hist
+        assert h.dtype == np.int64 and h.flags.c_contiguous and len(h) == n_bins
+        tot = np.zeros(1, np.int64)
+        _check(lib().fg_rdf_sample(self.h, int(type1), int(type2), float(dr), int(n_bins), _p(h), _p(tot)))
+        return h, int(tot[0])
 
     def positions(self):
         out = np.empty((self.n, 3))

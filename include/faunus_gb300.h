@@ -290,6 +290,17 @@ int fg_mol_total_energy(fg_molsys *h, double *comp);
 int fg_mol_running_energy(fg_molsys *h, double *u);
 int64_t fg_mol_device_bytes(fg_molsys *h);
 
+/* ---------------------------------------------------------------- analysis
+ * AtomRDF::update (analysis.h:2116-2134): add the current configuration's
+ * pair counts between atom types type1 and type2 (each unordered pair i < j
+ * once) to hist[0 .. n_bins), bin = int(r / dr + 0.5) on the minimum-image
+ * distance (Table2D::round, auxiliary.h:831; Cuboid::sqdist,
+ * geometry.h:507-515). *n_pairs (may be NULL) grows by the pairs at any
+ * distance (the normalisation sum of PairFunctionBase::normalize,
+ * analysis.cpp:190-205). n_bins <= 8192. */
+int fg_rdf_sample(fg_system *h, int32_t type1, int32_t type2, double dr, int32_t n_bins, int64_t *hist,
+                  int64_t *n_pairs);
+
 /* ---------------------------------------------------------------- autotuner
  * Launch shapes chosen by timing candidates on the device, on a clone of the
  * caller's system(s): the caller's chains do not advance. Each call applies

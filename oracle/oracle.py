@@ -274,3 +274,41 @@ def mol_stream(seed, n_groups, dp, dprot, center_rotation, n):
     lib().or_mol_draw_stream(seed, n_groups, dp, dprot, 1 if center_rotation else 0, n, _ptr(g), _ptr(ax),
                              _ptr(ce), _ptr(an), _ptr(tr), _ptr(u))
     return dict(group=g, axis=ax, center=ce, angle=an, trans=tr, u=u)
+
+
+# ---------------------------------------------------------------- analysis
+def atom_rdf_counts(xyz, types, box, t1, t2, dr, n_bins):
+    """AtomRDF::update (analysis.h:2116-2134) on one configuration, FP64:
+    every pair i < j whose types are {t1, t2} counts once at the
+    minimum-image distance (Cuboid::sqdist, geometry.h:507-515: |a - b| per
+    axis, minus L where above L/2), in bin int(r / dr + 0.5) (Table2D::round,
+    auxiliary.h:831). Returns (counts of bins 0 .. n_bins-1, pairs at any
+    distance)."""
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    tp = np.asarray(types)
+    L = np.asarray(box, dtype=np.float64)
+    n = len(x)
+    hist = np.zeros(n_bins, np.int64)
+    total = 0
+    for i in range(n - 1):
+        j = np.arange(i + 1, n)
+        sel = ((tp[i] == t1) & (tp[j] == t2)) | ((tp[i] == t2) & (tp[j] == t1))
+        j = j[sel]
+        if len(j) == 0:
+            continue
+        d = np.abs(x[i] - x[j])
+        d = np.where(d > 0.5 * L, d - L, d)
+        r = np.sqrt((d * d).sum(axis=1))
+        b = (r / dr + 0.5).astype(np.int64)
+        total += len(j)
+        np.add.at(hist, b[b < n_bins], 1)
+    return hist, total
+
+
+def rdf_normalize(hist, total, volume, dr):
+    """PairFunctionBase::normalize (analysis.cpp:190-205) for dim = 3:
+    g(r_b) = N(r_b) / sum N * <V> / (4 pi r_b^2 dr), r_b = b dr (bin 0 has no
+    volume element: inf or nan there, as in the reference)."""
+    r = np.arange(len(hist)) * dr
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.asarray(hist, dtype=np.float64) / total * volume / (4.0 * np.pi * r * r * dr)

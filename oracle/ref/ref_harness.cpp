@@ -16,12 +16,16 @@
 //   "ewald_known" : the ion-ion part of the reference's Ewald unit test
 //              (src/examples/unittests.cpp:131-170) with charged atom types.
 //   "bench"  : like "mc" but logs nothing; prints trials/s.
+// With an "rdf" entry {t1, t2, dr}, "mc" also samples the reference's
+// Analysis::AtomRDF (analysis.h:2116-2134) after every sweep and writes its
+// raw histogram (bin keys and counts, before normalisation) and <V>.
 #include <faunus/faunus.h>
 #include <faunus/ewald.h>
 #include <chrono>
 #include <cstdio>
 #include <fstream>
 #include <map>
+#include <memory>
 
 using namespace Faunus;
 typedef Space<Geometry::Cuboid, PointParticle> Tspace;
@@ -49,6 +53,15 @@ struct Out {
         fprintf(f, "\n}\n");
         fclose(f);
     }
+};
+
+// Exposes AtomRDF's raw histogram (the reference normalises it only when
+// saving to disk) without changing how it samples.
+class RdfProbe : public Analysis::AtomRDF<Tspace> {
+  public:
+    RdfProbe(Tmjson j, Tspace &s) : Analysis::AtomRDF<Tspace>(j, s) {}
+    std::map<double, double> raw() { return this->datavec[0].hist.getMap(); }
+    double volume() { return this->V.avg(); }
 };
 
 // Logs what AtomicTranslation does without changing it: every override
@@ -143,9 +156,21 @@ static void run_mc(const Tmjson &in, Out &out, bool bench) {
     out.set("bjerrum", pot.pairpot.first.bjerrumLength());
     out.set("u0", Energy::systemEnergy(spc, pot, spc.p));
     const int sweeps = in.value("sweeps", 1);
+    std::unique_ptr<RdfProbe> rdf;
+    if (in.count("rdf")) {
+        const auto &r = in["rdf"];
+        Tmjson rj = {{"nstep", 1},
+                     {"pairs", {{{"name1", "T" + std::to_string(r["t1"].get<int>())},
+                                 {"name2", "T" + std::to_string(r["t2"].get<int>())},
+                                 {"dim", 3}, {"dr", r["dr"]}, {"file", "rdf.dat"}}}}};
+        rdf.reset(new RdfProbe(rj, spc));
+    }
     double usum = 0;
     auto t0 = std::chrono::steady_clock::now();
-    for (int s = 0; s < sweeps; s++) usum += mv.move();
+    for (int s = 0; s < sweeps; s++) {
+        usum += mv.move();
+        if (rdf) rdf->sample();
+    }
     auto t1 = std::chrono::steady_clock::now();
     double secs = std::chrono::duration<double>(t1 - t0).count();
     out.set("seconds", secs);
@@ -161,6 +186,16 @@ static void run_mc(const Tmjson &in, Out &out, bool bench) {
         std::vector<double> fin;
         for (auto &p : spc.p) { fin.push_back(p.x()); fin.push_back(p.y()); fin.push_back(p.z()); }
         out.set("final_positions", fin);
+    }
+    if (rdf) {
+        std::vector<double> key, cnt;
+        for (auto &kv : rdf->raw()) {
+            key.push_back(kv.first);
+            cnt.push_back(kv.second);
+        }
+        out.set("rdf_key", key);
+        out.set("rdf_count", cnt);
+        out.set("rdf_volume", rdf->volume());
     }
 }
 

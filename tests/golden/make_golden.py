@@ -61,7 +61,10 @@ CASES = {
     "ewald_rpm800": (lambda: workloads.rpm800(seed=13, update_frequency=1000), "ewald_wca", 103, 1),
     "dhlj_small": (lambda: workloads.dh_lj_salt(300, seed=14, density=0.004), "dh_lj", 104, 2),
     "dhlj_500": (lambda: workloads.dh_lj_salt(500, seed=15), "dh_lj", 105, 1),
+    "dhlj_rdf": (lambda: workloads.dh_lj_salt(400, seed=16, density=0.004), "dh_lj", 106, 4),
 }
+# AtomRDF sampled by the reference after every sweep: name -> (type1, type2, dr)
+RDF = {"dhlj_rdf": (0, 1, 0.5)}
 
 
 # rigid dipolar molecules: (n_molecules, workload seed, RNG seed, sweeps, center_rotation)
@@ -150,7 +153,16 @@ def main():
         if a.only and name != a.only:
             continue
         params, xyz, q, ids = builder()
-        out = run_harness(exe, harness_input("mc", params, xyz, ids, seed, sweeps, model))
+        d = harness_input("mc", params, xyz, ids, seed, sweeps, model)
+        extra = {}
+        if name in RDF:
+            t1, t2, dr = RDF[name]
+            d["rdf"] = dict(t1=t1, t2=t2, dr=dr)
+        out = run_harness(exe, d)
+        if name in RDF:
+            extra = dict(rdf_types=np.asarray(RDF[name][:2], dtype=np.int32), rdf_dr=np.float64(RDF[name][2]),
+                         rdf_key=np.asarray(out["rdf_key"]), rdf_count=np.asarray(out["rdf_count"]),
+                         rdf_volume=np.float64(out["rdf_volume"][0]))
         n = len(out["idx"])
         np.savez_compressed(
             os.path.join(HERE, name + ".npz"),
@@ -161,7 +173,7 @@ def main():
             idx=np.asarray(out["idx"], dtype=np.int32),
             trial_xyz=np.asarray(out["trial_xyz"]).reshape(n, 3),
             du=np.asarray(out["du"]), acc=np.asarray(out["acc"], dtype=np.uint8),
-            final_positions=np.asarray(out["final_positions"]).reshape(-1, 3))
+            final_positions=np.asarray(out["final_positions"]).reshape(-1, 3), **extra)
         print(name, "trials", n, "acceptance %.3f" % np.mean(out["acc"]), "u0 %.6f" % out["u0"][0])
 
 

@@ -7,11 +7,11 @@ import numpy as np
 import pytest
 
 from beofaunus_gb300.params import FG_MODEL_EWALD_WCA, FgParams, make_params
-from oracle.oracle import OracleSystem, translation_stream
+from oracle.oracle import OracleSystem, atom_rdf_counts, rdf_normalize, translation_stream
 
 from conftest import GOLDEN
 
-MC_CASES = ["ewald_small_uf1", "ewald_surface_uf5", "ewald_rpm800", "dhlj_small", "dhlj_500"]
+MC_CASES = ["ewald_small_uf1", "ewald_surface_uf5", "ewald_rpm800", "dhlj_small", "dhlj_500", "dhlj_rdf"]
 
 
 def load(name):
@@ -88,3 +88,36 @@ def test_translation_stream_matches_reference_draws(name):
     dpp = np.array([p.type_dp[i] for i in g["ids"]])
     idx, disp, u = translation_stream(int(g["seed"]), dpp, n)
     np.testing.assert_array_equal(idx, g["idx"])
+
+
+def rdf_bins(g, n_bins):
+    """The reference's AtomRDF keys (bin centres b dr) as bin counts."""
+    counts = np.zeros(n_bins, np.int64)
+    b = np.rint(g["rdf_key"] / float(g["rdf_dr"])).astype(np.int64)
+    counts[b] = g["rdf_count"].astype(np.int64)
+    return counts
+
+
+def test_rdf_matches_reference_analysis():
+    """AtomRDF (analysis.h:2116-2134) sampled by the reference after each
+    sweep of its own run: the oracle's restatement over the same trajectory
+    gives the same counts, and the normalised g(r) follows from them."""
+    g = load("dhlj_rdf")
+    p = params_of(g)
+    s = OracleSystem(p, g["xyz"], g["q"], g["ids"])
+    n, N = len(g["idx"]), len(g["ids"])
+    dpp = np.array([p.type_dp[i] for i in g["ids"]])
+    idx, disp, u = translation_stream(int(g["seed"]), dpp, n)
+    t1, t2 = (int(x) for x in g["rdf_types"])
+    dr = float(g["rdf_dr"])
+    n_bins = int(np.rint(g["rdf_key"].max() / dr)) + 1
+    hist, total = np.zeros(n_bins, np.int64), 0
+    for k in range(0, n, N):
+        s.mc_run_stream(idx[k:k + N], disp[k:k + N], u[k:k + N])
+        h, t = atom_rdf_counts(s.positions(), g["ids"], list(p.box), t1, t2, dr, n_bins)
+        hist += h
+        total += t
+    np.testing.assert_array_equal(hist, rdf_bins(g, n_bins))
+    assert total == int(g["rdf_count"].sum())
+    gr = rdf_normalize(hist, total, float(g["rdf_volume"]), dr)
+    assert np.all(np.isfinite(gr[1:])) and gr[-1] > 0
