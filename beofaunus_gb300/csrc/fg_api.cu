@@ -1390,3 +1390,4 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 #include "fg_mol.cu"
 #include "fg_tune.cu"
 #include "fg_rdf.cu"
+#include "fg_state.cu"

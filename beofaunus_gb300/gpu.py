@@ -106,6 +106,10 @@ def lib(build_if_missing=True):
             "fg_mol_device_bytes": ([vp], ctypes.c_int64),
             "fg_autotune": ([vp, i64, dp], ctypes.c_int),
             "fg_rdf_sample": ([vp, i32, i32, ctypes.c_double, i32, dp, dp], ctypes.c_int),
+            "fg_state_read": ([ctypes.c_char_p, i32, i32, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, i32, dp, dp, dp],
+                              ctypes.c_int),
+            "fg_state_write": ([ctypes.c_char_p, i32, dp, i32, dp, dp, dp, dp, dp, dp, dp, dp, i32, dp, dp, u32],
+                               ctypes.c_int),
             "fg_batch_autotune": ([vp, i64, dp], ctypes.c_int),
             "fg_mol_autotune": ([vp, i64, dp], ctypes.c_int),
             "fg_tune_reset": ([], ctypes.c_int),
@@ -135,6 +139,45 @@ def _tune(fn, h, n_trials):
     r = TuneReport()
     _check(fn(h, int(n_trials), ctypes.byref(r)))
     return r.as_dict()
+
+
+def read_state(path, kind=0, n_max=1 << 22, g_max=1 << 20):
+    """Read a reference state file (fg_state_read): dict of box, xyz, charge,
+    radius, mw, ids, hydrophobic (and mu_unit, mu_scalar for kind 1),
+    groups [G, 4] and group_cm [G, 3]. ids are the file's atom ids (the
+    reference's first atom type is id 1)."""
+    n = np.zeros(1, np.int32)
+    ng = np.zeros(1, np.int32)
+    box = np.zeros(3)
+    # first pass: counts only
+    _check(lib().fg_state_read(str(path).encode(), kind, n_max, _p(box), _p(n), None, None, None, None, None, None,
+                               None, None, 0, _p(ng), None, None))
+    N, G = int(n[0]), int(ng[0])
+    out = dict(box=box, xyz=np.zeros((N, 3)), charge=np.zeros(N), radius=np.zeros(N), mw=np.zeros(N),
+               ids=np.zeros(N, np.int32), hydrophobic=np.zeros(N, np.int32), groups=np.zeros((G, 4), np.int32),
+               group_cm=np.zeros((G, 3)))
+    mu = np.zeros((N, 3)) if kind == 1 else None
+    mus = np.zeros(N) if kind == 1 else None
+    _check(lib().fg_state_read(str(path).encode(), kind, N, _p(box), _p(n), _p(out["xyz"]), _p(out["charge"]),
+                               _p(out["radius"]), _p(out["mw"]), _p(out["ids"]), _p(out["hydrophobic"]), _p(mu),
+                               _p(mus), G, _p(ng), _p(out["groups"]), _p(out["group_cm"])))
+    if kind == 1:
+        out.update(mu_unit=mu, mu_scalar=mus)
+    return out
+
+
+def write_state(path, box, xyz, charge, radius, mw, ids, hydrophobic=None, mu_unit=None, mu_scalar=None,
+                groups=None, group_cm=None, rng_seed=5489, kind=None):
+    """Write a reference state file (fg_state_write); kind 1 (dipole
+    records) when mu_unit is given."""
+    f64 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+    i32 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+    x = f64(xyz).reshape(-1, 3)
+    g = i32(groups) if groups is not None else np.zeros((0, 4), np.int32)
+    k = (1 if mu_unit is not None else 0) if kind is None else kind
+    _check(lib().fg_state_write(str(path).encode(), k, _p(f64(box)), len(x), _p(x), _p(f64(charge)),
+                                _p(f64(radius)), _p(f64(mw)), _p(i32(ids)), _p(i32(hydrophobic)), _p(f64(mu_unit)),
+                                _p(f64(mu_scalar)), len(g), _p(g), _p(f64(group_cm)), int(rng_seed)))
 
 
 def tune_reset():
@@ -188,7 +231,19 @@ class System:
             type_ids = np.zeros(self.n, dtype=np.int32)
         self._ids = np.ascontiguousarray(type_ids, dtype=np.int32)
         q = None if charge is None else np.ascontiguousarray(charge, dtype=np.float64)
+        self._q = q if q is not None else np.array([self.params.type_charge[t] for t in self._ids])
         _check(lib().fg_set_state(self.h, _p(xyz), _p(q), _p(self._ids)))
+
+    def save_state(self, path, mw=None, rng_seed=5489, id_offset=1):
+        """The current configuration as a reference state file (one atomic
+        group; radius sigma/2 and mw per type, mw 1 when not given). Atom ids
+        are type + id_offset: the reference's atom list keeps a dummy entry at
+        id 0 (AtomMap(), species.h:493-503), so its first type is id 1."""
+        ids = self._ids
+        radius = np.array([0.5 * self.params.type_sigma[t] for t in ids])
+        m = None if mw is None else np.asarray([mw[t] for t in ids], dtype=np.float64)
+        write_state(path, np.array(self.params.box[:3]), self.positions(), self._q, radius, m, ids + id_offset,
+                    groups=np.array([[0, self.n - 1, 0, 1]], np.int32), rng_seed=rng_seed)   # atomic: molsize 1
 
     @property
     def threads(self):

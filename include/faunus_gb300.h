@@ -301,6 +301,29 @@ int64_t fg_mol_device_bytes(fg_molsys *h);
 int fg_rdf_sample(fg_system *h, int32_t type1, int32_t type2, double dr, int32_t n_bins, int64_t *hist,
                   int64_t *n_pairs);
 
+/* ---------------------------------------------------------------- state files
+ * The reference's Space::save/load text format (space.h:736-764, 807-880):
+ * box lengths, N particle records, G group records (front back molId molsize
+ * and the mass centre, group.h:388-407), "randomstate" and an mt19937 state.
+ * kind 0: PointParticle records (x y z charge radius mw id hydrophobic,
+ * point.h:544-566); kind 1: DipoleParticle records (the same, then the dipole
+ * unit vector, its scalar, the induced dipole and two 3x3 tensors,
+ * point.h:649-666). Host only.
+ *
+ * fg_state_read fills what it is given (any output may be NULL; groups take
+ * 4 int32 and group_cm 3 doubles per group) and fails with FG_ERR_CAPACITY
+ * past n_max particles or g_max groups. fg_state_write writes the records
+ * with 16 significant digits (NULL charge/radius/hydrophobic: 0, NULL mw: 1;
+ * dipole records carry no induced dipole and zero tensors) and the state of
+ * std::mt19937(rng_seed) for the reference to continue from. */
+int fg_state_read(const char *path, int32_t kind, int32_t n_max, double *box, int32_t *n, double *xyz,
+                  double *charge, double *radius, double *mw, int32_t *ids, int32_t *hydrophobic, double *mu_unit,
+                  double *mu_scalar, int32_t g_max, int32_t *n_groups, int32_t *groups, double *group_cm);
+int fg_state_write(const char *path, int32_t kind, const double *box, int32_t n, const double *xyz,
+                   const double *charge, const double *radius, const double *mw, const int32_t *ids,
+                   const int32_t *hydrophobic, const double *mu_unit, const double *mu_scalar, int32_t n_groups,
+                   const int32_t *groups, const double *group_cm, uint32_t rng_seed);
+
 /* ---------------------------------------------------------------- autotuner
  * Launch shapes chosen by timing candidates on the device, on a clone of the
  * caller's system(s): the caller's chains do not advance. Each call applies

@@ -187,6 +187,12 @@ static void run_mc(const Tmjson &in, Out &out, bool bench) {
         for (auto &p : spc.p) { fin.push_back(p.x()); fin.push_back(p.y()); fin.push_back(p.z()); }
         out.set("final_positions", fin);
     }
+    if (in.count("state_file")) {
+        // the particles were typed in place above: refresh the atom trackers
+        // Space::save checks (space.h:388-405), then save (space.h:736-764)
+        spc.initTracker();
+        spc.save(in["state_file"].get<std::string>());
+    }
     if (rdf) {
         std::vector<double> key, cnt;
         for (auto &kv : rdf->raw()) {

@@ -42,14 +42,19 @@ def harness_input(mode, params, xyz, ids, seed, sweeps, model):
     return d
 
 
-def run_harness(exe, d):
+def run_harness(exe, d, files=()):
+    """Run a harness on input d; with files, also return the contents of
+    those files the harness wrote in its working directory."""
     with tempfile.TemporaryDirectory() as tmp:
         fin, fout = os.path.join(tmp, "in.json"), os.path.join(tmp, "out.json")
         with open(fin, "w") as f:
             json.dump(d, f)
         subprocess.check_call([exe, fin, fout], cwd=tmp, stdout=subprocess.DEVNULL)
         with open(fout) as f:
-            return json.load(f)
+            out = json.load(f)
+        if not files:
+            return out
+        return out, [open(os.path.join(tmp, x), "rb").read() for x in files]
 
 
 CASES = {
@@ -158,11 +163,14 @@ def main():
         if name in RDF:
             t1, t2, dr = RDF[name]
             d["rdf"] = dict(t1=t1, t2=t2, dr=dr)
-        out = run_harness(exe, d)
-        if name in RDF:
+            d["state_file"] = "final.state"
+            out, (state,) = run_harness(exe, d, files=["final.state"])
             extra = dict(rdf_types=np.asarray(RDF[name][:2], dtype=np.int32), rdf_dr=np.float64(RDF[name][2]),
                          rdf_key=np.asarray(out["rdf_key"]), rdf_count=np.asarray(out["rdf_count"]),
-                         rdf_volume=np.float64(out["rdf_volume"][0]))
+                         rdf_volume=np.float64(out["rdf_volume"][0]),
+                         state_text=np.frombuffer(state, dtype=np.uint8))
+        else:
+            out = run_harness(exe, d)
         n = len(out["idx"])
         np.savez_compressed(
             os.path.join(HERE, name + ".npz"),
