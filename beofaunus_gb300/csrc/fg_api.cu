@@ -1391,3 +1391,5 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 #include "fg_tune.cu"
 #include "fg_rdf.cu"
 #include "fg_state.cu"
+#include "fg_energy64.cu"
+#include "fg_volume.cu"

@@ -105,6 +105,11 @@ def lib(build_if_missing=True):
             "fg_mol_running_energy": ([vp, dp], ctypes.c_int),
             "fg_mol_device_bytes": ([vp], ctypes.c_int64),
             "fg_autotune": ([vp, i64, dp], ctypes.c_int),
+            "fg_total_energy_fp64": ([vp, dp], ctypes.c_int),
+            "fg_volume_move": ([vp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, i32, dp, dp],
+                               ctypes.c_int),
+            "fg_get_box": ([vp, dp], ctypes.c_int),
+            "fg_slump_uniforms": ([u32, i64, dp], ctypes.c_int),
             "fg_rdf_sample": ([vp, i32, i32, ctypes.c_double, i32, dp, dp], ctypes.c_int),
             "fg_state_read": ([ctypes.c_char_p, i32, i32, dp, dp, dp, dp, dp, dp, dp, dp, dp, dp, i32, dp, dp, dp],
                               ctypes.c_int),
@@ -180,6 +185,13 @@ def write_state(path, box, xyz, charge, radius, mw, ids, hydrophobic=None, mu_un
                                 _p(f64(mu_scalar)), len(g), _p(g), _p(f64(group_cm)), int(rng_seed)))
 
 
+def slump_uniforms(seed, n):
+    """The reference's global slump() draws from seed (fg_slump_uniforms)."""
+    u = np.empty(int(n))
+    _check(lib().fg_slump_uniforms(int(seed), int(n), _p(u)))
+    return u
+
+
 def tune_reset():
     """Forget the autotuner's recorded launch shapes (fg_tune_reset)."""
     _check(lib().fg_tune_reset())
@@ -204,7 +216,7 @@ class System:
     def __init__(self, params, xyz, charge=None, type_ids=None, threads=0):
         if not isinstance(params, FgParams):
             raise TypeError("params must be FgParams")
-        self.params = params
+        self.params = FgParams.from_buffer_copy(bytes(params))   # own copy: volume moves change the box
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
         self.n = len(xyz)
         h = ctypes.c_void_p()
@@ -257,6 +269,33 @@ class System:
         """Time candidate launch shapes on a clone (fg_autotune) and apply the
         fastest; returns {"candidates": [(value, us/trial)], "chosen": value}."""
         return _tune(lib().fg_autotune, self.h, n_trials)
+
+    def total_energy_fp64(self):
+        """systemEnergy with every term in FP64 (fg_total_energy_fp64)."""
+        c = np.empty(5)
+        _check(lib().fg_total_energy_fp64(self.h, _p(c)))
+        return dict(pairs=c[0], reciprocal=c[1], self=c[2], surface=c[3], total=c[4])
+
+    def volume_move(self, half, dp, pressure, u, reference_quirk=False):
+        """Isobaric volume move (fg_volume_move): half = slump.half(), dp the
+        log-volume step, pressure in particles per cubic Angstrom, u the
+        Metropolis uniform. Returns (dU, accepted); the box follows."""
+        du = np.zeros(1)
+        acc = np.zeros(1, np.int32)
+        _check(lib().fg_volume_move(self.h, float(half), float(dp), float(pressure), float(u),
+                                    1 if reference_quirk else 0, _p(du), _p(acc)))
+        if acc[0]:
+            b = np.zeros(3)
+            _check(lib().fg_get_box(self.h, _p(b)))
+            for a in range(3):
+                self.params.box[a] = b[a]
+        return float(du[0]), bool(acc[0])
+
+    @property
+    def box(self):
+        b = np.zeros(3)
+        _check(lib().fg_get_box(self.h, _p(b)))
+        return b
 
     def rdf_sample(self, type1, type2, dr, n_bins, hist=None):
         """Add the current configuration's type1-type2 pair counts (AtomRDF

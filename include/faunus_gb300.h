@@ -290,6 +290,30 @@ int fg_mol_total_energy(fg_molsys *h, double *comp);
 int fg_mol_running_energy(fg_molsys *h, double *u);
 int64_t fg_mol_device_bytes(fg_molsys *h);
 
+/* ---------------------------------------------------------------- volume move
+ * Move::Isobaric (move.h:5529-5624) with Energy::ExternalPressure
+ * (energy.h:1817-1890) on one atomic group: V' = exp(ln V + half * dp) with
+ * half = slump.half() in [-0.5, 0.5), positions scaled by (V'/V)^(1/3) about
+ * the origin, dU = E(V') - E(V) + pressure (V' - V) - (N + 1) ln(V'/V) with
+ * pressure in particles per cubic Angstrom (the reference's mM input times
+ * 1.0_mM, physconst.h:170-173), Metropolis with u (move.h:567-573). On
+ * acceptance the system takes the new box (every box-dependent table is
+ * rebuilt); a staged trial stream is dropped, and a system in a batch or
+ * server must not be moved. reference_quirk (Ewald): take the trial's
+ * reciprocal energy as the reference computes it, from the positions before
+ * scaling in the new box (NonbondedEwald::setGeometry rebuilding Q(k) from
+ * spc->p, ewald.h:731-756), so dU and decisions match the reference's. */
+int fg_volume_move(fg_system *h, double half, double dp, double pressure, double u, int32_t reference_quirk,
+                   double *du, int32_t *accepted);
+/* systemEnergy (energy.h:169-180) in FP64 throughout: pairs and Q(k) on the
+ * device in double, reciprocal/self/surface on the host; components as
+ * fg_total_energy. The volume move's energies come from here. */
+int fg_total_energy_fp64(fg_system *h, double *components5);
+/* Current box lengths (Angstrom; changed by accepted volume moves). */
+int fg_get_box(fg_system *h, double *box);
+/* n draws of the reference's global slump() (slump.h:62-95) from seed: host only. */
+int fg_slump_uniforms(uint32_t seed, int64_t n, double *u);
+
 /* ---------------------------------------------------------------- analysis
  * AtomRDF::update (analysis.h:2116-2134): add the current configuration's
  * pair counts between atom types type1 and type2 (each unordered pair i < j

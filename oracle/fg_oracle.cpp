@@ -387,6 +387,13 @@ void or_boundary(void *h, double *xyz) {
 // `slump` (move.h:818-864, group.h:129-134, move.h:567-573):
 //   range(0, n_groups-1); range(0, N-1); 3 uniforms (x,y,z); 1 uniform (Metropolis).
 // Outputs per trial: particle index, displacement (dp*(u-0.5) per axis), u_metropolis.
+// The global slump() sequence (slump.h:62-95) for host-driven moves.
+int or_uniforms(uint32_t seed, int64_t n, double *u) {
+    Twister t(seed);
+    for (int64_t i = 0; i < n; i++) u[i] = t();
+    return 0;
+}
+
 int or_draw_translation_stream(uint32_t seed, int n_particles, const double *dp_per_particle,
                                int64_t n_trials, int32_t *idx, double *disp, double *umet) {
     Twister t(seed);

@@ -50,6 +50,7 @@ def lib():
         L.or_total_energy.argtypes = [vp, dp]
         L.or_boundary.argtypes = [vp, dp]
         L.or_draw_translation_stream.argtypes = [u32, i32, dp, i64, dp, dp, dp]
+        L.or_uniforms.argtypes = [u32, i64, dp]
         L.or_mc_run.restype = ctypes.c_double
         L.or_mc_run.argtypes = [vp, u32, i64, dp, dp, dp, dp]
         L.or_philox.argtypes = [dp, dp, dp]
@@ -312,3 +313,69 @@ def rdf_normalize(hist, total, volume, dr):
     r = np.arange(len(hist)) * dr
     with np.errstate(divide="ignore", invalid="ignore"):
         return np.asarray(hist, dtype=np.float64) / total * volume / (4.0 * np.pi * r * r * dr)
+
+
+# ---------------------------------------------------------------- volume move
+def slump_uniforms(seed, n):
+    """The reference's global slump() draws (slump.h:62-95) from seed."""
+    u = np.empty(int(n))
+    lib().or_uniforms(seed, int(n), _ptr(u))
+    return u
+
+
+# particles per cubic Angstrom in one mM (physconst.h:161-173, Nav = 6.022137e23)
+MILLIMOLAR = 1.0e-3 * 6.022137e23 / 1e27
+
+
+def reciprocal_unscaled(o_new, xyz_old, q, eff):
+    """The trial reciprocal energy the reference forms for a volume move:
+    the structure factor of the positions before scaling with the new box's
+    k-vectors and weights (NonbondedEwald::setGeometry rebuilding Q(k) from
+    spc->p, ewald.h:731-756; getReciprocalEnergy, ewald.h:298-311)."""
+    K = o_new.num_kvectors
+    qk, kv, ak = np.empty(2 * K), np.empty(3 * K), np.empty(K)
+    lib().or_get_qk(o_new.h, _ptr(qk), _ptr(kv), _ptr(ak))
+    kv = kv.reshape(K, 3)
+    qe = np.asarray(q) * np.asarray(eff)
+    Q = (qe[None, :] * np.exp(1j * (kv @ np.asarray(xyz_old).T))).sum(axis=1)
+    return float(np.sum(ak * np.abs(Q) ** 2))
+
+
+def volume_move(params, xyz, q, ids, half, dp, pressure, u, kT=1.0, reference_quirk=False):
+    """Move::Isobaric (move.h:5529-5624) with ExternalPressure
+    (energy.h:1817-1890) on one atomic group, FP64: V' = exp(ln V + half dp),
+    positions scaled by (V'/V)^(1/3) about the origin (Cuboid::scale,
+    geometry.cpp:325-332), dU = E(V') - E(V) + P (V' - V) - (N + 1) ln(V'/V)
+    with E the system energy and P in particles per cubic Angstrom;
+    Metropolis as move.h:567-573. Returns (dU, accepted, params, xyz) with
+    the new box and positions when accepted."""
+    from beofaunus_gb300.params import FgParams
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    L = np.array(params.box[:3], dtype=np.float64)
+    V = float(np.prod(L))
+    Vn = float(np.exp(np.log(V) + half * dp))
+    f = float(np.cbrt(Vn / V))
+    e0 = OracleSystem(params, x, q, ids).total_energy()["total"]
+    pn = FgParams.from_buffer_copy(bytes(params))
+    for a in range(3):
+        pn.box[a] = params.box[a] * f
+    xn = x * f
+    o1 = OracleSystem(pn, xn, q, ids)
+    en = o1.total_energy()
+    e1 = en["total"]
+    n = len(x)
+    du = e1 - e0 + pressure * (Vn - V) - (n + 1) * np.log(Vn / V)
+    if reference_quirk and params.model == 1:
+        # the reciprocal energy as returned carries the prefactor 2 pi lB / V';
+        # the raw sum is rescaled by the same factor
+        # effective charges (ewald.h:532-549): sinh(kappa R) / (kappa R), R = sigma / 2
+        kap = 1.0 / params.ewald_debye_length
+        eff = []
+        for t in ids:
+            kr = kap * 0.5 * params.type_sigma[t]
+            eff.append(np.sinh(kr) / kr if abs(kr) > 1e-9 else 1.0)
+        raw = reciprocal_unscaled(o1, x, q, eff)
+        prefactor = 2.0 * np.pi / Vn * pn.bjerrum
+        du += raw * prefactor - en["reciprocal"]
+    acc = not (u > np.exp(-du / kT))
+    return du, acc, (pn if acc else params), (xn if acc else x)

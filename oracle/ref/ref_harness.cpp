@@ -16,6 +16,10 @@
 //   "ewald_known" : the ion-ion part of the reference's Ewald unit test
 //              (src/examples/unittests.cpp:131-170) with charged atom types.
 //   "bench"  : like "mc" but logs nothing; prints trials/s.
+//   "isobaric" : the same Space and pair energy plus Energy::ExternalPressure
+//              (energy.h:1817-1890), driven by Move::Isobaric (move.h:5424-5640)
+//              as bulk.cpp wires them; logs every volume move: dU, acceptance
+//              and the volume after it.
 // With an "rdf" entry {t1, t2, dr}, "mc" also samples the reference's
 // Analysis::AtomRDF (analysis.h:2116-2134) after every sweep and writes its
 // raw histogram (bin keys and counts, before normalisation) and <V>.
@@ -62,6 +66,30 @@ class RdfProbe : public Analysis::AtomRDF<Tspace> {
     RdfProbe(Tmjson j, Tspace &s) : Analysis::AtomRDF<Tspace>(j, s) {}
     std::map<double, double> raw() { return this->datavec[0].hist.getMap(); }
     double volume() { return this->V.avg(); }
+};
+
+// Logs what Isobaric does without changing it (move.h:5529-5624).
+template<class Tsp>
+class LoggedIsobaric : public Move::Isobaric<Tsp> {
+    typedef Move::Isobaric<Tsp> base;
+  public:
+    std::vector<double> du;
+    std::vector<int> acc;
+    template<class Tenergy> LoggedIsobaric(Tenergy &e, Tsp &s, Tmjson &j) : base(e, s, j) {}
+  protected:
+    double _energyChange() override {
+        const double d = base::_energyChange();
+        du.push_back(d);
+        return d;
+    }
+    void _acceptMove() override {
+        base::_acceptMove();
+        acc.push_back(1);
+    }
+    void _rejectMove() override {
+        base::_rejectMove();
+        acc.push_back(0);
+    }
 };
 
 // Logs what AtomicTranslation does without changing it: every override
@@ -249,6 +277,58 @@ static void run_ewald_known(const Tmjson &in, Out &out) {
     out.set("total", Energy::systemEnergy(spc, pot, spc.p));
 }
 
+// Places the described particles into spc (types T0, T1, ... as faunus_input
+// named them) with the per-type parameters set directly.
+static void place_particles(const Tmjson &in, Tspace &spc) {
+    int t = 0;
+    for (auto &ty : in["types"]) {
+        auto &a = atom[atom["T" + std::to_string(t++)].id];
+        a.eps = ty["eps"];
+        a.sigma = ty["sigma"];
+        a.radius = 0.5 * a.sigma;
+        a.charge = ty["q"];
+        a.dp = ty["dp"];
+    }
+    const int N = in["positions"].size();
+    if ((int)spc.p.size() != N) throw std::runtime_error("particle count mismatch");
+    for (int i = 0; i < N; i++) {
+        int ty = in["type_ids"][i];
+        spc.p[i] = atom[atom["T" + std::to_string(ty)].id];
+        spc.p[i].x() = in["positions"][i][0];
+        spc.p[i].y() = in["positions"][i][1];
+        spc.p[i].z() = in["positions"][i][2];
+    }
+    spc.trial = spc.p;
+    spc.initTracker();
+}
+
+template<class Tenergy>
+static void run_isobaric(const Tmjson &in, Out &out) {
+    Tmjson j = faunus_input(in);
+    j["moves"]["isobaric"] = {{"dp", in["volume_dp"]}, {"pressure", in["pressure_mM"]}};
+    Tspace spc(j);
+    place_particles(in, spc);
+    auto pot = Tenergy(j) + Energy::ExternalPressure<Tspace>(j);
+    LoggedIsobaric<Tspace> mv(pot, spc, j["moves"]["isobaric"]);
+    slump.seed(in.value("seed", 5489u));
+    out.set("bjerrum", pot.first.pairpot.first.bjerrumLength());
+    out.set("v0", spc.geo.getVolume());
+    const int moves = in["moves"];
+    std::vector<double> vol;
+    double usum = 0;
+    for (int m = 0; m < moves; m++) {
+        usum += mv.move();
+        vol.push_back(spc.geo.getVolume());
+    }
+    out.set("du", mv.du);
+    out.set("acc", mv.acc);
+    out.set("volume", vol);
+    out.set("u_move_sum", usum);
+    std::vector<double> fin;
+    for (auto &p : spc.p) { fin.push_back(p.x()); fin.push_back(p.y()); fin.push_back(p.z()); }
+    out.set("final_positions", fin);
+}
+
 int main(int argc, char **argv) {
     if (argc != 3) { std::cerr << "usage: ref_harness in.json out.json\n"; return 2; }
     std::ifstream f(argv[1]);
@@ -262,6 +342,10 @@ int main(int argc, char **argv) {
             Potential::LennardJonesMixed<Potential::LorentzBerthelot>>> Tdhlj;
     if (mode == "ewald_known")
         run_ewald_known(in, out);
+    else if (mode == "isobaric" && in["model"] == "ewald_wca")
+        run_isobaric<Tewald>(in, out);
+    else if (mode == "isobaric" && in["model"] == "dh_lj")
+        run_isobaric<Tdhlj>(in, out);
     else if (in["model"] == "ewald_wca")
         run_mc<Tewald>(in, out, bench);
     else if (in["model"] == "dh_lj")

@@ -68,6 +68,13 @@ CASES = {
     "dhlj_500": (lambda: workloads.dh_lj_salt(500, seed=15), "dh_lj", 105, 1),
     "dhlj_rdf": (lambda: workloads.dh_lj_salt(400, seed=16, density=0.004), "dh_lj", 106, 4),
 }
+# Isobaric volume moves (ExternalPressure + Isobaric): name -> (builder, model,
+# seed, volume dp, pressure in mM, moves)
+ISO_CASES = {
+    "iso_dhlj": (lambda: workloads.dh_lj_salt(200, seed=21, density=0.004), "dh_lj", 107, 0.1, 100.0, 30),
+    "iso_ewald": (lambda: workloads.rpm_ewald(100, 25.0, 5, seed=22, update_frequency=4, cutoff=10.0),
+                  "ewald_wca", 108, 0.1, 100.0, 30),
+}
 # AtomRDF sampled by the reference after every sweep: name -> (type1, type2, dr)
 RDF = {"dhlj_rdf": (0, 1, 0.5)}
 
@@ -147,6 +154,25 @@ def main():
             continue
         make_mol(exe_mol, name, *case)
     if a.only and a.only in MOL_CASES:
+        return
+
+    for name, (builder, model, seed, vdp, pmm, moves) in ISO_CASES.items():
+        if a.only and name != a.only:
+            continue
+        params, xyz, q, ids = builder()
+        d = harness_input("isobaric", params, xyz, ids, seed, 0, model)
+        d.update(volume_dp=vdp, pressure_mM=pmm, moves=moves)
+        out = run_harness(exe, d)
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            params=np.frombuffer(bytes(params), dtype=np.uint8), xyz=xyz, q=q, ids=ids,
+            seed=np.int64(seed), volume_dp=np.float64(vdp), pressure_mM=np.float64(pmm), moves=np.int64(moves),
+            bjerrum=np.float64(out["bjerrum"][0]), v0=np.float64(out["v0"][0]), du=np.asarray(out["du"]),
+            acc=np.asarray(out["acc"], dtype=np.uint8), volume=np.asarray(out["volume"]),
+            u_move_sum=np.float64(out["u_move_sum"][0]),
+            final_positions=np.asarray(out["final_positions"]).reshape(-1, 3))
+        print(name, "moves", moves, "acceptance %.3f" % np.mean(out["acc"]))
+    if a.only and a.only in ISO_CASES:
         return
 
     known = run_harness(exe, dict(mode="ewald_known"))
