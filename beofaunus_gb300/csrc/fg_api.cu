@@ -113,6 +113,7 @@ struct fg_system {
     double self_energy = 0, surf_c = 0, recip_c = 0;
     int threads = 0;
     int ctas = 0;                  // block-kernel CTAs per system (0: tuned cache / heuristic)
+    int batches = 0;               // live batches holding this system
     std::vector<double> charges;   // host copy of the uploaded charges (clones for tuning)
     bool use_cells = false, pos_smem = false;
     int nc[3] = {0, 0, 0};

@@ -115,6 +115,7 @@ struct fg_batch {
     bool dh_block = false;
     DhGroups dh;
     int min_per_cta = 0;   // schedule: least particles per CTA (0: the tuned process default)
+    bool counted = false;  // members' batch counts include this batch
 };
 
 namespace {
@@ -312,6 +313,8 @@ int fg_batch_create(fg_system *const *systems, int32_t n, fg_batch **out) {
         return bail(fail(FG_ERR_CUDA, "batch allocation failed"));
     int rc = batch_config(b);
     if (rc) return bail(rc);
+    for (fg_system *h : b->sys) h->batches++;
+    b->counted = true;
     *out = b;
     return FG_OK;
 }
@@ -319,6 +322,8 @@ int fg_batch_create(fg_system *const *systems, int32_t n, fg_batch **out) {
 int fg_batch_destroy(fg_batch *b) {
     if (!b) return FG_OK;
     cudaStreamSynchronize(b->stream);
+    if (b->counted)
+        for (fg_system *h : b->sys) h->batches--;
     batch_free(b);
     delete b;
     return FG_OK;

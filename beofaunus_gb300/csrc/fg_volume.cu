@@ -55,6 +55,7 @@ extern "C" int fg_volume_move(fg_system *h, double half, double dp, double press
     if (!h || !du || !accepted) return fail(FG_ERR_INVALID, "null argument");
     if (h->types.empty()) return fail(FG_ERR_STATE, "fg_set_state first");
     if (h->trial_pending) return fail(FG_ERR_STATE, "a trial is pending: commit it first");
+    if (h->batches > 0) return fail(FG_ERR_STATE, "the system is in a batch: destroy the batch first");
     if (!(pressure >= 0.0) || !std::isfinite(half) || !std::isfinite(dp))
         return fail(FG_ERR_INVALID, "bad volume move arguments");
     const int N = h->N;

@@ -298,8 +298,8 @@ int64_t fg_mol_device_bytes(fg_molsys *h);
  * pressure in particles per cubic Angstrom (the reference's mM input times
  * 1.0_mM, physconst.h:170-173), Metropolis with u (move.h:567-573). On
  * acceptance the system takes the new box (every box-dependent table is
- * rebuilt); a staged trial stream is dropped, and a system in a batch or
- * server must not be moved. reference_quirk (Ewald): take the trial's
+ * rebuilt); a staged trial stream is dropped, and a system in a live batch
+ * is refused (FG_ERR_STATE). reference_quirk (Ewald): take the trial's
  * reciprocal energy as the reference computes it, from the positions before
  * scaling in the new box (NonbondedEwald::setGeometry rebuilding Q(k) from
  * spc->p, ewald.h:731-756), so dU and decisions match the reference's. */

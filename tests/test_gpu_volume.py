@@ -77,3 +77,14 @@ def test_translations_after_volume_moves_match_oracle():
         assert abs(ro["du"][t] + np.log(uu[t])) < 1e-6
         upto = t + 1
     assert np.abs(r["du"][:upto] - ro["du"][:upto]).max() < 1e-6
+
+
+def test_volume_move_refused_inside_a_batch():
+    from beofaunus_gb300.gpu import Batch, FgError, System
+    p, xyz, q, ids = workloads.dh_lj_salt(300, seed=5)
+    s = System(p, xyz, q, ids)
+    b = Batch([s])
+    with pytest.raises(FgError):
+        s.volume_move(0.1, 0.05, 1e-5, 0.5)
+    b.close()
+    s.volume_move(0.1, 0.05, 1e-5, 0.5)   # allowed again once the batch is gone
