@@ -371,6 +371,11 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             rB[tid] = b;
             rC[tid] = c;
         }
+        // the k-space records are the last shared input of the phases below:
+        // from here each warp runs its corrections, its real-space walks and
+        // its k-steps back to back, with no barrier between them (a warp
+        // done walking early starts on k space)
+        __syncthreads();
         // ---- real-space and surface corrections c(a, m), a < m
         for (int e = tid; e < kEbTrials * kEbTrials; e += blockDim.x) {
             const int a = e / kEbTrials, m = e - a * kEbTrials;
@@ -410,7 +415,6 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
         // gq + 8 r, k-vectors 4 st + gk and 4 st + 2 + gk), one the real and
         // one the imaginary part: each computes half (r = 2 gh, 2 gh + 1) and
         // they swap the other part. No chunk buffer, no barriers in the loop.
-        __syncthreads();   // trial records written, real-space queues done
         float kac[2] = {0.0f, 0.0f};   // reciprocal base of trials gq + 8 (2 gh + rr)
         float gc[6][4];
 #pragma unroll
