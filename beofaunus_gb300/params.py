@@ -9,6 +9,10 @@ import ctypes
 FG_MODEL_EWALD_WCA = 1
 FG_MODEL_DH_LJ = 2
 FG_MODEL_MULTIPOLE_RF = 3
+FG_MODEL_EWALD_DIPOLE = 4
+FG_EWALD_ION_ION = 1
+FG_EWALD_ION_DIPOLE = 2
+FG_EWALD_DIPOLE_DIPOLE = 4
 FG_MAX_TYPES = 16
 
 _D16 = ctypes.c_double * FG_MAX_TYPES
@@ -37,7 +41,9 @@ class FgParams(ctypes.Structure):
         ("rf_eps_r", ctypes.c_double),
         ("kT_scale", ctypes.c_double),
         ("use_cell_list", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("ewald_terms", ctypes.c_int32),
+        ("ewald_dipole_quirk", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
 

@@ -9,7 +9,8 @@ import math
 
 import numpy as np
 
-from .params import FG_MODEL_DH_LJ, FG_MODEL_EWALD_WCA, FG_MODEL_MULTIPOLE_RF, make_params
+from .params import (FG_EWALD_DIPOLE_DIPOLE, FG_EWALD_ION_ION, FG_MODEL_DH_LJ, FG_MODEL_EWALD_DIPOLE,
+                     FG_MODEL_EWALD_WCA, FG_MODEL_MULTIPOLE_RF, make_params)
 
 
 def rsa_positions(n, box, min_dist, seed):
@@ -216,3 +217,46 @@ def dipolar_molecules(n_mol=1000, seed=1, molsize=20, box=None, sigma=3.5, lj_ep
         mu_u[m * molsize] = v / np.linalg.norm(v)
         mu_s[m * molsize] = mu
     return p, xyz, mu_u, mu_s, ids
+
+
+# ---------------------------------------------------------------- point dipoles under Ewald
+def dipolar_fluid(n=100, seed=1, box=None, sigma=2.8863, eps_kjmol=1.97, mu=1.652, temperature=315.8,
+                  alpha=0.25, cutoff=None, kc=7.0, dp=0.7, n_ions=0, terms=FG_EWALD_ION_ION | FG_EWALD_DIPOLE_DIPOLE,
+                  quirk=0, eps_surf=1e11, update_frequency=1000):
+    """Lennard-Jones point dipoles with the shape of the reference's Stockmayer
+    example (stockmayer.json: 100 dipoles, |mu| 1.652 e A, sigma 2.8863 A,
+    eps 1.97 kJ/mol, L 29.6336 A at 100 particles, T 315.8 K, dp 0.7 A,
+    tin-foil surroundings), at that density for any n. The Ewald sum is
+    alpha 0.25 / A, real-space cutoff L/2 - 0.4 A and a spherical k-space
+    cutoff kc (the example's own cutoffK 0 leaves no reciprocal sum).
+
+    With n_ions > 0 the first n_ions particles are ions (charge +1 and -1 in
+    turn, no dipole) and the rest neutral dipoles. Type 0 carries +1 and type 1
+    -1: every type is charged, so the effective-charge ratio of ewald.h:539
+    is 1 (a neutral type makes it 0/0 in the reference); the per-particle
+    charges say which particles are ions.
+
+    Returns (params, xyz[n,3], mu_unit[n,3], mu_scalar[n], type_ids[n], charges[n])."""
+    rng = np.random.default_rng(seed)
+    if box is None:
+        box = 29.6336 * (n / 100.0) ** (1.0 / 3.0)
+    L = float(box)
+    if cutoff is None:
+        cutoff = 0.5 * L - 0.4
+    bjerrum = bjerrum_unit(temperature)
+    eps = eps_kjmol / (8.314462618e-3 * temperature)
+    types = [dict(q=1.0, sigma=sigma, eps=eps, dp=dp), dict(q=-1.0, sigma=sigma, eps=eps, dp=dp)]
+    p = make_params(FG_MODEL_EWALD_DIPOLE, L, bjerrum, types, ewald_alpha=alpha, ewald_cutoff=cutoff,
+                    ewald_cutoff_k=kc, ewald_eps_surf=eps_surf, ewald_update_frequency=update_frequency,
+                    ewald_terms=terms, ewald_dipole_quirk=quirk, kT_scale=1.0)
+    xyz = scatter_positions(n, L, 0.9 * sigma, int(rng.integers(1 << 31)))
+    v = rng.normal(size=(n, 3))
+    mu_u = v / np.linalg.norm(v, axis=1, keepdims=True)
+    mu_s = np.full(n, float(mu))
+    q = np.zeros(n)
+    ids = np.zeros(n, dtype=np.int32)
+    for i in range(n_ions):
+        q[i] = 1.0 if i % 2 == 0 else -1.0
+        ids[i] = 0 if i % 2 == 0 else 1
+        mu_s[i] = 0.0
+    return p, xyz, mu_u, mu_s, ids, q

@@ -30,8 +30,17 @@ enum {
     FG_MODEL_DH_LJ = 2,
     /* NonbondedVector<Tspace, CoulombGalore + IonDipole + DipoleDipoleGalore
      * (reaction field) + LennardJonesMixed> for rigid dipolar molecules. */
-    FG_MODEL_MULTIPOLE_RF = 3
+    FG_MODEL_MULTIPOLE_RF = 3,
+    /* NonbondedEwald<Tspace, LennardJonesLB, useIonIon, useIonDipole,
+     * useDipoleDipole> on point charges and point dipoles (DipoleParticle):
+     * EwaldReal + LJ pairs, reciprocal Q(k) of charges and dipoles, self and
+     * surface terms (ewald.h:28-32, 203-216). */
+    FG_MODEL_EWALD_DIPOLE = 4
 };
+
+/* ewald_terms bits: the useIonIon / useIonDipole / useDipoleDipole template
+ * flags of NonbondedEwald (ewald.h:231). */
+enum { FG_EWALD_ION_ION = 1, FG_EWALD_ION_DIPOLE = 2, FG_EWALD_DIPOLE_DIPOLE = 4 };
 
 #define FG_MAX_TYPES 16
 
@@ -65,7 +74,17 @@ typedef struct fg_params {
     double kT_scale;
     /* GPU execution options (the oracle ignores them) */
     int32_t use_cell_list;            /* 1 = cell list for the real-space sum */
-    int32_t reserved[7];
+    /* Dipolar Ewald (FG_MODEL_EWALD_DIPOLE) */
+    int32_t ewald_terms;              /* FG_EWALD_* bits */
+    int32_t ewald_dipole_quirk;       /* 0: the Ewald sum as ewald.h:28-32 and
+                                         203-216 state it (real-space ion-dipole
+                                         and dipole-dipole terms, reciprocal
+                                         |Q_ion + Q_dip|^2); 1: as the reference's
+                                         live code computes it: EwaldReal returns
+                                         after its ion-ion term (ewald.h:109-110)
+                                         and the reciprocal cross term is
+                                         2 Re(Q_ion Q_dip) (ewald.h:304-305) */
+    int32_t reserved[5];
 } fg_params;
 
 #ifdef __cplusplus

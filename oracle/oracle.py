@@ -12,7 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libfg_oracle.so")
-SRCS = [os.path.join(HERE, f) for f in ("fg_oracle.cpp", "fg_oracle_mol.cpp", "or_common.h")]
+SRCS = [os.path.join(HERE, f) for f in ("fg_oracle.cpp", "fg_oracle_mol.cpp", "fg_oracle_dip.cpp", "or_common.h")]
 
 
 def build(force=False):
@@ -72,6 +72,23 @@ def lib():
         L.or_mol_draw_stream.argtypes = [u32, i32, ctypes.c_double, ctypes.c_double, i32, i64, dp, dp, dp, dp, dp, dp]
         L.or_mol_run_stream.restype = ctypes.c_double
         L.or_mol_run_stream.argtypes = [vp, i64, dp, dp, dp, dp, dp, dp, i32, i32, dp, dp]
+        L.or_dip_create.restype = vp
+        L.or_dip_create.argtypes = [vp]
+        L.or_dip_destroy.argtypes = [vp]
+        L.or_dip_num_kvectors.argtypes = [vp]
+        L.or_dip_set_state.argtypes = [vp, i32, dp, dp, dp, dp, dp]
+        L.or_dip_get_state.argtypes = [vp, dp, dp]
+        L.or_dip_pair.restype = ctypes.c_double
+        L.or_dip_pair.argtypes = [vp, i32, i32, i32]
+        L.or_dip_trial_du.restype = ctypes.c_double
+        L.or_dip_trial_du.argtypes = [vp, i32, dp, dp]
+        L.or_dip_commit.restype = ctypes.c_double
+        L.or_dip_commit.argtypes = [vp, i32]
+        L.or_dip_total_energy.argtypes = [vp, dp]
+        L.or_dip_run_stream.restype = ctypes.c_double
+        L.or_dip_run_stream.argtypes = [vp, i64, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.or_dip_draw_stream.argtypes = [u32, i32, i64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         dp, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -379,3 +396,85 @@ def volume_move(params, xyz, q, ids, half, dp, pressure, u, kT=1.0, reference_qu
         du += raw * prefactor - en["reciprocal"]
     acc = not (u > np.exp(-du / kT))
     return du, acc, (pn if acc else params), (xn if acc else x)
+
+
+# ---------------------------------------------------------------- point dipoles
+class OracleDip:
+    """FP64 restatement of NonbondedEwald<Tspace, LennardJonesLB, ...> on point
+    charges and point dipoles with AtomicRotation / AtomicTranslation
+    (oracle/fg_oracle_dip.cpp)."""
+
+    def __init__(self, params, xyz, mu, mus, ids, q=None):
+        self.h = lib().or_dip_create(ctypes.byref(params))
+        if not self.h:
+            raise ValueError("bad dipole system")
+        self.n = len(ids)
+        self.set_state(xyz, mu, mus, ids, q)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_dip_destroy(self.h)
+            self.h = None
+
+    def set_state(self, xyz, mu, mus, ids, q=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        mu = np.ascontiguousarray(mu, dtype=np.float64).reshape(-1, 3)
+        mus = np.ascontiguousarray(mus, dtype=np.float64)
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        q = None if q is None else np.ascontiguousarray(q, dtype=np.float64)
+        self.n = len(ids)
+        lib().or_dip_set_state(self.h, self.n, _ptr(xyz), _ptr(mu), _ptr(mus), _ptr(q), _ptr(ids))
+
+    @property
+    def num_kvectors(self):
+        return lib().or_dip_num_kvectors(self.h)
+
+    def state(self):
+        xyz = np.empty((self.n, 3))
+        mu = np.empty((self.n, 3))
+        lib().or_dip_get_state(self.h, _ptr(xyz), _ptr(mu))
+        return xyz, mu
+
+    def pair(self, i, j, real_only=False):
+        return lib().or_dip_pair(self.h, i, j, 1 if real_only else 0)
+
+    def trial_du(self, i, xyz, mu=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        mu = None if mu is None else np.ascontiguousarray(mu, dtype=np.float64)
+        return lib().or_dip_trial_du(self.h, int(i), _ptr(xyz), _ptr(mu))
+
+    def commit(self, accepted):
+        return lib().or_dip_commit(self.h, 1 if accepted else 0)
+
+    def total_energy(self):
+        """{real-space Ewald pairs, LJ pairs, reciprocal, self, surface, total}"""
+        c = np.empty(6)
+        lib().or_dip_total_energy(self.h, _ptr(c))
+        return c
+
+    def run_stream(self, st):
+        n = len(st["idx"])
+        du = np.empty(n)
+        acc = np.empty(n, np.uint8)
+        arr = {k: np.ascontiguousarray(st[k], dtype=np.int32 if k in ("kind", "idx") else np.float64)
+               for k in ("kind", "idx", "axis", "angle", "disp", "u")}
+        s = lib().or_dip_run_stream(self.h, n, _ptr(arr["kind"]), _ptr(arr["idx"]), _ptr(arr["axis"]),
+                                    _ptr(arr["angle"]), _ptr(arr["disp"]), _ptr(arr["u"]), _ptr(du), _ptr(acc))
+        return dict(usum=s, du=du, acc=acc)
+
+
+def dip_stream(seed, n_particles, n, p_rotate, dp, dprot, kinds=None):
+    """Draws of n AtomicRotation / AtomicTranslation trials (see
+    or_dip_draw_stream): dict(kind, idx, axis, angle, disp, u). With kinds
+    given (1 rotation, 2 translation per trial) p_rotate is not used."""
+    kind = np.empty(n, np.int32) if kinds is None else np.array(kinds, dtype=np.int32)
+    if kinds is not None:
+        p_rotate = -1.0
+    idx = np.empty(n, np.int32)
+    axis = np.empty((n, 3))
+    angle = np.empty(n)
+    disp = np.empty((n, 3))
+    u = np.empty(n)
+    lib().or_dip_draw_stream(seed, n_particles, n, p_rotate, dp, dprot, _ptr(kind), _ptr(idx), _ptr(axis),
+                             _ptr(angle), _ptr(disp), _ptr(u))
+    return dict(kind=kind, idx=idx, axis=axis, angle=angle, disp=disp, u=u)

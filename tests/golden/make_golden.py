@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Runs the reference harnesses (oracle/ref/ref_harness.cpp and
-ref_harness_mol.cpp, linked against the reference library built from its own
+Runs the reference harnesses (oracle/ref/ref_harness.cpp,
+ref_harness_mol.cpp and ref_harness_dip.cpp, linked against the reference library built from its own
 sources by oracle/ref/Makefile) on seeded synthetic systems and stores what
 the reference computed: per-trial particle (or molecule) index, trial
 position, dU and acceptance, plus the total energies before and after. Needs
@@ -141,6 +141,54 @@ def make_mol(exe, name, n_mol, wseed, seed, sweeps, center_rotation):
     print(name, "trials", n, "acceptance %.3f" % np.mean(out["acc"]), "u0 %.6f" % out["u0"][0])
 
 
+# point dipoles: name -> (workload kwargs, harness template flags, seed, sweeps, dprot in radians)
+DIP_CASES = {
+    "dip_fluid": (dict(n=100, seed=3, kc=5.0), "ii_dd", 21, 4, 1.5),
+    "dip_mixture": (dict(n=60, seed=4, kc=5.0, n_ions=20, update_frequency=7), "ii_dd", 22, 4, 1.0),
+    "dip_mixture_id": (dict(n=60, seed=5, kc=5.0, n_ions=20, terms=7), "ii_id_dd", 23, 4, 1.0),
+}
+
+
+def dip_input(mode, params, xyz, mu, mus, ids, q, seed, sweeps, terms, dprot):
+    types = [dict(q=params.type_charge[t], sigma=params.type_sigma[t], eps=params.type_eps[t],
+                  dp=params.type_dp[t], dprot=dprot) for t in range(params.n_types)]
+    return dict(mode=mode, terms=terms, box=params.box[0], bjerrum=params.bjerrum, types=types,
+                positions=xyz.tolist(), type_ids=[int(i) for i in ids], charges=[float(c) for c in q],
+                mu=mu.tolist(), mus=[float(m) for m in mus], seed=seed, sweeps=sweeps,
+                alpha=params.ewald_alpha, cutoff=params.ewald_cutoff, cutoffK=params.ewald_cutoff_k,
+                eps_surf=params.ewald_eps_surf, debyelength=params.ewald_debye_length,
+                spherical_sum=bool(params.ewald_spherical_sum),
+                update_frequency=int(params.ewald_update_frequency))
+
+
+def make_dip(exe):
+    # the unit test's configurations on the live code (bjerrum 1: energies in units of lB)
+    p = workloads.make_params(workloads.FG_MODEL_EWALD_DIPOLE, 10.0, 1.0, [dict(q=1.0, sigma=0.0, eps=0.0)],
+                              ewald_alpha=0.894427190999916, ewald_cutoff=5.0, ewald_cutoff_k=11.0,
+                              ewald_eps_surf=1.0, ewald_update_frequency=10, ewald_terms=5)
+    xyz = np.array([[0.0, 0, 0], [1, 0, 0], [0, 0, 1], [1, 0, 1]])
+    known = run_harness(exe, dip_input("known", p, xyz, np.tile([1.0, 0, 0], (4, 1)), np.zeros(4),
+                                       np.zeros(4, np.int32), np.zeros(4), 0, 0, "ii_dd", 0.0))
+    np.savez_compressed(os.path.join(HERE, "dip_known.npz"),
+                        **{k: np.asarray(v, dtype=np.float64) for k, v in known.items()})
+    print("dip_known", {k: v[0] for k, v in known.items()})
+    for name, (kw, terms, seed, sweeps, dprot) in DIP_CASES.items():
+        params, xyz, mu, mus, ids, q = workloads.dipolar_fluid(quirk=1, **kw)
+        params.bjerrum = 60.0   # acceptance near one half at these step sizes
+        out = run_harness(exe, dip_input("mc", params, xyz, mu, mus, ids, q, seed, sweeps, terms, dprot))
+        n = len(out["idx"])
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            params=np.frombuffer(bytes(params), dtype=np.uint8), xyz=xyz, mu=mu, mus=mus, ids=ids, q=q,
+            seed=np.int64(seed), sweeps=np.int64(sweeps), dprot=np.float64(dprot),
+            bjerrum=np.float64(out["bjerrum"][0]), u0=np.float64(out["u0"][0]), u1=np.float64(out["u1"][0]),
+            u_move_sum=np.float64(out["u_move_sum"][0]), kind=np.asarray(out["kind"], dtype=np.int32),
+            idx=np.asarray(out["idx"], dtype=np.int32), trial_xyz=np.asarray(out["trial_xyz"]).reshape(n, 3),
+            trial_mu=np.asarray(out["trial_mu"]).reshape(n, 3), du=np.asarray(out["du"]),
+            acc=np.asarray(out["acc"], dtype=np.uint8))
+        print(name, "trials", n, "acceptance %.3f" % np.mean(out["acc"]), "u0 %.6f" % out["u0"][0])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -149,6 +197,10 @@ def main():
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "REF=" + a.ref])
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
     exe_mol = os.path.join(ROOT, "oracle", "_ref", "ref_harness_mol")
+    if a.only in (None, "dip"):
+        make_dip(os.path.join(ROOT, "oracle", "_ref", "ref_harness_dip"))
+        if a.only:
+            return
     for name, case in MOL_CASES.items():
         if a.only and name != a.only:
             continue
