@@ -1394,3 +1394,4 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 #include "fg_state.cu"
 #include "fg_energy64.cu"
 #include "fg_volume.cu"
+#include "fg_dip.cu"

@@ -1,0 +1,1151 @@
+// Point charges and point dipoles under Ewald summation: the AtomicRotation
+// (move.h:976-1072) and AtomicTranslation (move.h:818-901) trials on
+// DipoleParticle (point.h:591-680) with the energy change of
+// NonbondedEwald<Tspace, LennardJonesLB, useIonIon, useIonDipole,
+// useDipoleDipole> (ewald.h:228-757):
+//   real space   EwaldReal (ewald.h:97-129) + LennardJonesLB (no cutoff);
+//   k space      Q_ion(k) = sum q eff e^{ik.r}, Q_dip(k) = sum (k.mu) mu_s i e^{ik.r}
+//                (ewald.h:388-415, 651-705), energy ewald.h:298-311;
+//   surface      ewald.h:277-291 (running sums of q r and mu);
+//   self         ewald.h:259-270 (unchanged by either move).
+// fg_params.ewald_dipole_quirk selects the reading: 0 = the sum as ewald.h
+// states it (real-space ion-dipole and dipole-dipole terms, reciprocal
+// |Q_ion + Q_dip|^2); 1 = the reference's live code (EwaldReal returns after
+// its ion-ion line, ewald.h:109-110; cross term 2 Re(Q_ion Q_dip),
+// ewald.h:304-305; Q_dip rebuilt only with useDipoleDipole, ewald.h:400).
+//
+// Included by fg_api.cu (one translation unit).
+//
+// Work split. One system per CTA; a launch runs many systems (replicas,
+// independent chains) side by side, several CTAs per SM. A trial is a
+// block-wide pass: thread 0 forms the trial (quaternion rotation of mu or
+// fixed-point translation), the threads build the moved particle's per-axis
+// phase tables e^{2 pi i n x_a / L_a}, n = 0..kcc, old and new (one sincospi
+// each, from the exact 64-bit phase n X mod 2^64); then each thread sums its
+// share of the N - 1 pair changes and of the K k-vector changes (a k-vector's
+// phase is a product of three table entries), the block reduces in a fixed
+// order, thread 0 decides, and on acceptance the threads that computed a
+// k-vector's Q increments add them to Q(k).
+//
+// Precision. Everything on this path is FP64: the per-trial dU must match the
+// FP64 oracle to 1e-9 kT at Bjerrum lengths of hundreds of Angstrom, where
+// single dipole pairs carry tens of kT. Positions are 64-bit fixed point
+// (X = x/L 2^64): minimum image is the wrapped integer difference and every
+// translation is exact.
+namespace fgd {
+
+constexpr int kDipMaxThreads = 256;
+constexpr int kDipMaxKcc = 31;   // axis tables hold n = 0..kcc
+
+constexpr int kDipErrNonFinite = 8;
+constexpr int kDipErrLaunch = 64;
+
+struct DipTrial {
+    int32_t idx;   // particle
+    int32_t kind;  // 1 rotation (q), 2 translation (t), 3 explicit: position t (absolute), dipole q[1..3]
+    double u;      // Metropolis uniform: reject iff u > exp(-dU / kT) (Movebase::metropolis, move.h:567-573)
+    double q[4];   // rotation quaternion (w, x, y, z)
+    int64_t t[3];  // translation (fixed point)
+};
+
+struct DipScalars {
+    int64_t cursor;       // next trial of the staged stream
+    int64_t n_trials;     // end of the stream for this launch
+    int64_t n_accepted;   // cumulative
+    int64_t n_rebuilds;   // cumulative Q(k) rebuilds
+    int32_t error;
+    int32_t cnt_accepted; // NonbondedEwald::cnt_accepted (ewald.h:633)
+    int32_t pad[2];
+    double usum;          // accepted dU + rebuild corrections of the current stream
+    double utot;          // running total energy
+    double drift;         // NonbondedEwald::update_drift
+    double pend_du;       // dU of an evaluated explicit trial
+    double M[6];          // surface sums: sum q eff r (3), sum mu_s mu (3)
+};
+
+struct DipDesc {
+    int32_t N, K, kcc, nt;
+    int32_t ion_q;        // Q_ion kept (useIonIon || useIonDipole)
+    int32_t dip_q;        // Q_dip kept by trials (useIonDipole || useDipoleDipole)
+    int32_t dip_q_build;  // Q_dip built by rebuilds (quirk: useDipoleDipole only)
+    int32_t ii, id, dd, quirk, uf, small_kappa, any_term;
+    double L[3], s64[3], tpl[3];   // box, L / 2^64, 2 pi / L
+    double alpha, alpha2, rc2, kappa, lB, kT;
+    double recip_c;       // 2 pi lB / V
+    double surf_c;        // 2 pi lB / ((2 eps_surf + 1) V), 0 with tin-foil surroundings
+    double t1c, t2c;      // 2 alpha / sqrt(pi), 4 alpha^3 / (3 sqrt(pi))
+    double eff[FG_MAX_TYPES];
+    double qeqe[FG_MAX_TYPES * FG_MAX_TYPES], s2[FG_MAX_TYPES * FG_MAX_TYPES], eps4[FG_MAX_TYPES * FG_MAX_TYPES];
+    int64_t *pos;         // [3N] fixed point
+    double *mu;           // [3N] dipole unit vectors
+    double *mus;          // [N] dipole scalars
+    double *q;            // [N] charges
+    int32_t *type;        // [N]
+    char4 *kn;            // [K] n-vector of k
+    double *ak;           // [K] A_k with the half-space factor
+    double2 *qi, *qd;     // [K] Q_ion, Q_dip
+    double2 *dqi, *dqd;   // [K] increments of the trial in flight
+    DipTrial *trials;
+    double *log_du;       // [trials] or null
+    uint8_t *log_acc;
+    DipScalars *sc;
+};
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 conj_if(double2 a, bool c) { return c ? make_double2(a.x, -a.y) : a; }
+
+// e^{i k.r} from one particle's axis tables (tab[axis * (kcc+1) + |n|]);
+// negative components take the conjugate
+__device__ __forceinline__ double2 kphase(const double2 *tab, int stride, char4 n) {
+    const double2 ex = tab[n.x];
+    const double2 ey = conj_if(tab[stride + (n.y < 0 ? -n.y : n.y)], n.y < 0);
+    const double2 ez = conj_if(tab[2 * stride + (n.z < 0 ? -n.z : n.z)], n.z < 0);
+    return cmul(cmul(ex, ey), ez);
+}
+
+// cos, sin of 2 pi n X / 2^64: the phase reduced exactly in integers
+__device__ __forceinline__ double2 axis_entry(int n, int64_t X) {
+    const int64_t ph = (int64_t)((uint64_t)(int64_t)n * (uint64_t)X);
+    double s, c;
+    sincospi((double)ph * 1.0842021724855044e-19, &s, &c);   // 2^-63
+    return make_double2(c, s);
+}
+
+// Pair energy of particles a (moved) and b at r = a - b: EwaldReal + LJ
+// (CombinedPairPotential, potentials.h:3768-3771). real/lj split for totals.
+__device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry, double rz, double qa, int ta,
+                                         double mas, const double *ma, double qb, int tb, double mbs,
+                                         const double *mb, double &real, double &lj) {
+    const double r2 = rx * rx + ry * ry + rz * rz;
+    const int tt = ta * d.nt + tb;
+    double x = d.s2[tt] / r2;   // LennardJonesMixed (potentials.h:2036-2040)
+    x = x * x * x;
+    lj = d.eps4[tt] * (x * x - x);
+    real = 0.0;
+    if (!d.any_term || r2 > d.rc2) return;
+    const double r1 = sqrt(r2);
+    const double ar = d.alpha * r1;
+    const double ec = erfc(ar);
+    if (d.quirk || d.ii) {
+        double t;
+        if (d.small_kappa) {
+            t = ec / r1;   // erfc(ar +- kappa / 2 alpha) e^{+-kappa r} round to erfc(ar) here
+        } else {
+            const double h = d.kappa / 2.0 / d.alpha;
+            t = (erfc(ar + h) * exp(d.kappa * r1) + erfc(ar - h) * exp(-d.kappa * r1)) / (2.0 * r1);
+        }
+        real = qa * qb * t * d.qeqe[tt] * d.lB;
+    }
+    if (d.quirk || !(d.id || d.dd)) return;
+    const double ex = exp(-d.alpha2 * r2);
+    const double T1f = r1 * d.t1c * ex + ec;   // ewald.h:46
+    const double T1 = T1f / r1 / r2;
+    double Ed = 0.0;
+    if (d.id) {
+        Ed += qa * (rx * mb[0] + ry * mb[1] + rz * mb[2]) * mbs * T1;
+        Ed -= qb * (rx * ma[0] + ry * ma[1] + rz * ma[2]) * mas * T1;
+    }
+    if (d.dd) {
+        const double T2f = 3.0 * (T1f + d.t2c * r1 * r1 * r1 * ex);   // ewald.h:47
+        const double t3 = -(mb[0] * ma[0] + mb[1] * ma[1] + mb[2] * ma[2]) * T1;
+        const double t5 = (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (ma[0] * rx + ma[1] * ry + ma[2] * rz) * T2f / r2 /
+                          r2 / r1;
+        Ed += -(t5 + t3) * mbs * mas;
+    }
+    real += d.lB * Ed;
+}
+
+// Block sum in a fixed order (result valid in thread 0).
+__device__ __forceinline__ double block_sum(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nw; w++) s += red[w];
+    return s;
+}
+
+__device__ __forceinline__ double surface(const DipDesc &d, const double *M) {
+    return d.surf_c * (M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + 2.0 * (M[0] * M[3] + M[1] * M[4] + M[2] * M[5]) +
+                       M[3] * M[3] + M[4] * M[4] + M[5] * M[5]);
+}
+
+// Reciprocal energy sum_k A_k Q2(k) of this thread's k-vectors (before recip_c)
+__device__ __forceinline__ double q2(const DipDesc &d, double2 a, double2 b) {
+    double s = 0.0;
+    if (d.ii) s += a.x * a.x + a.y * a.y;
+    if (d.id) s += 2.0 * (d.quirk ? a.x * b.x - a.y * b.y : a.x * b.x + a.y * b.y);
+    if (d.dd) s += b.x * b.x + b.y * b.y;
+    return s;
+}
+
+struct DipShared {
+    int64_t po[3], pn[3];
+    double muo[3], mun[3];
+    double ro[3], rn[3];
+    double qa, qeff, mas, u, du, pend;
+    double M[6];
+    int idx, ta, kind, accept, rebuild;
+    double red[kDipMaxThreads / 32];
+    double2 tab[2][3 * (kDipMaxKcc + 1)];   // moved particle, old and new
+    double2 rtab[3 * (kDipMaxKcc + 1)];     // rebuild: one particle at a time
+    double rq, rmu[3];
+};
+
+// Q(k) from scratch (updateAllComplexNumbers, ewald.h:388-415). Returns the
+// reciprocal energy before and after in thread 0.
+__device__ void dip_rebuild(const DipDesc &d, DipShared &S, double &before, double &after) {
+    const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
+    double e = 0.0;
+    for (int k = tid; k < d.K; k += T) {
+        e += d.ak[k] * q2(d, d.qi[k], d.qd[k]);
+        d.qi[k] = make_double2(0.0, 0.0);
+        d.qd[k] = make_double2(0.0, 0.0);
+    }
+    before = block_sum(e, S.red) * d.recip_c;
+    for (int j = 0; j < d.N; j++) {
+        __syncthreads();   // previous particle's table consumed
+        for (int e = tid; e < 3 * st; e += T) {
+            const int a = e / st, n = e - a * st;
+            S.rtab[e] = axis_entry(n, d.pos[3 * j + a]);
+        }
+        if (tid == 0) {
+            S.rq = d.q[j] * d.eff[d.type[j]];
+            for (int a = 0; a < 3; a++) S.rmu[a] = d.mu[3 * j + a] * d.mus[j];
+        }
+        __syncthreads();
+        for (int k = tid; k < d.K; k += T) {
+            const char4 n = d.kn[k];
+            const double2 ph = kphase(S.rtab, st, n);
+            if (d.ion_q) {
+                double2 v = d.qi[k];
+                v.x += S.rq * ph.x;
+                v.y += S.rq * ph.y;
+                d.qi[k] = v;
+            }
+            if (d.dip_q_build) {
+                const double km = n.x * d.tpl[0] * S.rmu[0] + n.y * d.tpl[1] * S.rmu[1] + n.z * d.tpl[2] * S.rmu[2];
+                double2 v = d.qd[k];
+                v.x -= km * ph.y;
+                v.y += km * ph.x;
+                d.qd[k] = v;
+            }
+        }
+    }
+    e = 0.0;
+    for (int k = tid; k < d.K; k += T) e += d.ak[k] * q2(d, d.qi[k], d.qd[k]);
+    after = block_sum(e, S.red) * d.recip_c;
+}
+
+// Q(k) of the uploaded state (setSpace -> setGeometry, ewald.h:731-756)
+__global__ void __launch_bounds__(kDipMaxThreads) dip_build_kernel(const DipDesc *dp) {
+    __shared__ DipShared S;
+    double before, after;
+    dip_rebuild(*dp, S, before, after);
+}
+
+// mode 0: run the staged stream [cursor, n_trials) with Metropolis decisions;
+// mode 1: evaluate trials[0] (explicit) and keep it pending;
+// mode 2: apply the pending trials[0] as accepted.
+__global__ void __launch_bounds__(kDipMaxThreads) dip_sweep_kernel(const DipDesc *descs, int mode) {
+    const DipDesc &d = descs[blockIdx.x];
+    __shared__ DipShared S;
+    const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
+    if (T > kDipMaxThreads || (T & 31)) {
+        if (tid == 0) atomicOr(&d.sc->error, kDipErrLaunch);
+        return;
+    }
+    DipScalars sc;
+    if (tid == 0) {
+        sc = *d.sc;
+        for (int a = 0; a < 6; a++) S.M[a] = sc.M[a];
+    }
+    int64_t t0 = 0, t1 = 1;
+    if (mode == 0) {
+        t0 = d.sc->cursor;
+        t1 = d.sc->n_trials;
+    }
+    for (int64_t t = t0; t < t1; t++) {
+        // ---- the trial (thread 0)
+        if (tid == 0) {
+            const DipTrial tr = d.trials[mode == 0 ? t : 0];
+            const int i = tr.idx;
+            S.idx = i;
+            S.kind = tr.kind;
+            S.u = tr.u;
+            S.ta = d.type[i];
+            S.qa = d.q[i];
+            S.qeff = d.q[i] * d.eff[S.ta];
+            S.mas = d.mus[i];
+            for (int a = 0; a < 3; a++) {
+                S.po[a] = d.pos[3 * i + a];
+                S.muo[a] = d.mu[3 * i + a];
+                S.pn[a] = S.po[a];
+                S.mun[a] = S.muo[a];
+            }
+            if (tr.kind == 1) {
+                // Eigen's quaternion-vector product (QuaternionRotate, geometry.cpp:753-766)
+                const double w = tr.q[0], vx = tr.q[1], vy = tr.q[2], vz = tr.q[3];
+                const double px = S.muo[0], py = S.muo[1], pz = S.muo[2];
+                double ux = vy * pz - vz * py, uy = vz * px - vx * pz, uz = vx * py - vy * px;
+                ux += ux;
+                uy += uy;
+                uz += uz;
+                const double cx = vy * uz - vz * uy, cy = vz * ux - vx * uz, cz = vx * uy - vy * ux;
+                S.mun[0] = px + w * ux + cx;
+                S.mun[1] = py + w * uy + cy;
+                S.mun[2] = pz + w * uz + cz;
+            } else if (tr.kind == 2) {
+                for (int a = 0; a < 3; a++) S.pn[a] = (int64_t)((uint64_t)S.po[a] + (uint64_t)tr.t[a]);
+            } else if (tr.kind == 3) {
+                for (int a = 0; a < 3; a++) {
+                    S.pn[a] = tr.t[a];
+                    S.mun[a] = tr.q[1 + a];
+                }
+            }
+            for (int a = 0; a < 3; a++) {
+                S.ro[a] = (double)S.po[a] * d.s64[a];
+                S.rn[a] = (double)S.pn[a] * d.s64[a];
+            }
+        }
+        __syncthreads();
+        if (mode != 2) {
+            // ---- axis tables of the moved particle, old (w = 0) and new (w = 1)
+            for (int e = tid; e < 6 * st; e += T) {
+                const int w = e / (3 * st), r = e - w * 3 * st, a = r / st, n = r - a * st;
+                S.tab[w][r] = axis_entry(n, w ? S.pn[a] : S.po[a]);
+            }
+            __syncthreads();
+            const int i = S.idx, ta = S.ta;
+            const double qa = S.qa, mas = S.mas;
+            const double muo[3] = {S.muo[0], S.muo[1], S.muo[2]}, mun[3] = {S.mun[0], S.mun[1], S.mun[2]};
+            double acc = 0.0;
+            // ---- real space: the moved particle against every other one
+            for (int j = tid; j < d.N; j += T) {
+                if (j == i) continue;
+                int64_t pj[3];
+                double mb[3];
+                for (int a = 0; a < 3; a++) {
+                    pj[a] = d.pos[3 * j + a];
+                    mb[a] = d.mu[3 * j + a];
+                }
+                const double qb = d.q[j], mbs = d.mus[j];
+                const int tb = d.type[j];
+                double ro[3], rn[3];
+                for (int a = 0; a < 3; a++) {
+                    ro[a] = (double)(int64_t)((uint64_t)S.po[a] - (uint64_t)pj[a]) * d.s64[a];
+                    rn[a] = (double)(int64_t)((uint64_t)S.pn[a] - (uint64_t)pj[a]) * d.s64[a];
+                }
+                double eo, lo, en, ln;
+                dip_pair(d, ro[0], ro[1], ro[2], qa, ta, mas, muo, qb, tb, mbs, mb, eo, lo);
+                dip_pair(d, rn[0], rn[1], rn[2], qa, ta, mas, mun, qb, tb, mbs, mb, en, ln);
+                acc += (en - eo) + (ln - lo);
+            }
+            // ---- k space: increments of Q_ion and Q_dip and the energy change
+            double ek = 0.0;
+            const double qeff = S.qeff;
+            for (int k = tid; k < d.K; k += T) {
+                const char4 n = d.kn[k];
+                const double2 eo = kphase(S.tab[0], st, n), en = kphase(S.tab[1], st, n);
+                double2 dci = make_double2(0.0, 0.0), dcd = make_double2(0.0, 0.0);
+                if (d.ion_q) dci = make_double2(qeff * (en.x - eo.x), qeff * (en.y - eo.y));
+                if (d.dip_q) {
+                    const double kx = n.x * d.tpl[0], ky = n.y * d.tpl[1], kz = n.z * d.tpl[2];
+                    const double kmo = (kx * muo[0] + ky * muo[1] + kz * muo[2]) * mas;
+                    const double kmn = (kx * mun[0] + ky * mun[1] + kz * mun[2]) * mas;
+                    dcd = make_double2(-kmn * en.y + kmo * eo.y, kmn * en.x - kmo * eo.x);
+                }
+                const double2 Qi = d.qi[k], Qd = d.qd[k];
+                double s = 0.0;
+                if (d.ii) s += 2.0 * (Qi.x * dci.x + Qi.y * dci.y) + dci.x * dci.x + dci.y * dci.y;
+                if (d.id) {
+                    if (d.quirk)
+                        s += 2.0 * ((Qi.x * dcd.x - Qi.y * dcd.y) + (dci.x * Qd.x - dci.y * Qd.y) +
+                                    (dci.x * dcd.x - dci.y * dcd.y));
+                    else
+                        s += 2.0 * ((Qi.x * dcd.x + Qi.y * dcd.y) + (dci.x * Qd.x + dci.y * Qd.y) +
+                                    (dci.x * dcd.x + dci.y * dcd.y));
+                }
+                if (d.dd) s += 2.0 * (Qd.x * dcd.x + Qd.y * dcd.y) + dcd.x * dcd.x + dcd.y * dcd.y;
+                ek += d.ak[k] * s;
+                d.dqi[k] = dci;
+                d.dqd[k] = dcd;
+            }
+            acc += ek * d.recip_c;
+            const double sum = block_sum(acc, S.red);
+            if (tid == 0) {
+                // surface term: running sums before and after the move
+                double Mn[6];
+                for (int a = 0; a < 3; a++) {
+                    Mn[a] = S.M[a] + (d.ion_q ? S.qeff * (S.rn[a] - S.ro[a]) : 0.0);
+                    Mn[3 + a] = S.M[3 + a] + ((d.id || d.dd) ? S.mas * (S.mun[a] - S.muo[a]) : 0.0);
+                }
+                const double du = sum + (surface(d, Mn) - surface(d, S.M));
+                S.du = du;
+                if (!isfinite(du)) sc.error |= kDipErrNonFinite;
+                if (mode == 0) {
+                    const double kT = d.kT;
+                    S.accept = !(S.u > exp(-du / kT)) ? 1 : 0;
+                    if (d.log_du) {
+                        d.log_du[t] = du;
+                        d.log_acc[t] = (uint8_t)S.accept;
+                    }
+                } else {
+                    S.accept = 0;
+                    sc.pend_du = du;
+                }
+            }
+        } else if (tid == 0) {
+            S.accept = 1;
+            S.du = sc.pend_du;
+        }
+        __syncthreads();
+        if (!S.accept) continue;
+        // ---- accepted: Q(k), the particle, the sums
+        for (int k = tid; k < d.K; k += T) {
+            if (d.ion_q) {
+                const double2 a = d.qi[k], b = d.dqi[k];
+                d.qi[k] = make_double2(a.x + b.x, a.y + b.y);
+            }
+            if (d.dip_q) {
+                const double2 a = d.qd[k], b = d.dqd[k];
+                d.qd[k] = make_double2(a.x + b.x, a.y + b.y);
+            }
+        }
+        if (tid == 0) {
+            const int i = S.idx;
+            for (int a = 0; a < 3; a++) {
+                d.pos[3 * i + a] = S.pn[a];
+                d.mu[3 * i + a] = S.mun[a];
+                if (d.ion_q) S.M[a] += S.qeff * (S.rn[a] - S.ro[a]);
+                if (d.id || d.dd) S.M[3 + a] += S.mas * (S.mun[a] - S.muo[a]);
+            }
+            sc.n_accepted++;
+            sc.usum += S.du;
+            sc.utot += S.du;
+            S.rebuild = 0;
+            if (++sc.cnt_accepted > d.uf - 1) {   // NonbondedEwald::update (ewald.h:633)
+                sc.cnt_accepted = 0;
+                S.rebuild = 1;
+            }
+        }
+        __syncthreads();
+        if (S.rebuild) {
+            double before, after;
+            dip_rebuild(d, S, before, after);
+            if (tid == 0) {
+                sc.n_rebuilds++;
+                sc.drift += fabs(after - before);
+                sc.usum += after - before;
+                sc.utot += after - before;
+            }
+        }
+    }
+    if (tid == 0) {
+        if (mode == 0) sc.cursor = t1;
+        for (int a = 0; a < 6; a++) sc.M[a] = S.M[a];
+        // the host may have moved the stream end while this kernel was queued
+        sc.n_trials = d.sc->n_trials;
+        *d.sc = sc;
+    }
+}
+
+// Whole-system pair sums for the total energy: row i against j > i, one
+// block per row; out[2 i] = EwaldReal, out[2 i + 1] = LJ.
+__global__ void __launch_bounds__(kDipMaxThreads) dip_pairs_kernel(const DipDesc *dp, double *out) {
+    const DipDesc &d = *dp;
+    __shared__ double red[kDipMaxThreads / 32];
+    const int i = blockIdx.x;
+    double er = 0.0, el = 0.0;
+    double ma[3];
+    for (int a = 0; a < 3; a++) ma[a] = d.mu[3 * i + a];
+    for (int j = i + 1 + threadIdx.x; j < d.N; j += blockDim.x) {
+        double r[3], mb[3];
+        for (int a = 0; a < 3; a++) {
+            r[a] = (double)(int64_t)((uint64_t)d.pos[3 * i + a] - (uint64_t)d.pos[3 * j + a]) * d.s64[a];
+            mb[a] = d.mu[3 * j + a];
+        }
+        double e, l;
+        dip_pair(d, r[0], r[1], r[2], d.q[i], d.type[i], d.mus[i], ma, d.q[j], d.type[j], d.mus[j], mb, e, l);
+        er += e;
+        el += l;
+    }
+    const double s0 = block_sum(er, red);
+    const double s1 = block_sum(el, red);
+    if (threadIdx.x == 0) {
+        out[2 * i] = s0;
+        out[2 * i + 1] = s1;
+    }
+}
+
+}  // namespace fgd
+
+struct fg_dipsys {
+    fg_params P{};
+    int N = 0, K = 0, kcc = 0;
+    int device = 0;
+    int threads = 128;
+    cudaStream_t stream = nullptr;
+    fgd::DipDesc desc{};
+    fgd::DipDesc *d_desc = nullptr;
+    int64_t *pos = nullptr;
+    double *mu = nullptr, *mus = nullptr, *q = nullptr, *ak = nullptr, *pairs = nullptr;
+    int32_t *type = nullptr;
+    char4 *kn = nullptr;
+    double2 *qi = nullptr, *qd = nullptr, *dqi = nullptr, *dqd = nullptr;
+    fgd::DipTrial *trials = nullptr;
+    int64_t trials_cap = 0;
+    double *log_du = nullptr;
+    uint8_t *log_acc = nullptr;
+    int64_t log_cap = 0;
+    fgd::DipScalars *sc = nullptr;
+    int64_t n_stream = 0;
+    int64_t acc0 = 0;
+    bool pending = false;
+    bool state_set = false;
+    std::vector<double> ak_h, charges_h, mus_h;
+    std::vector<int32_t> types_h;
+    std::vector<char4> kn_h;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t device_bytes = 0;
+};
+
+namespace {
+
+void dip_free(fg_dipsys *h) {
+    void *ptrs[] = {h->d_desc, h->pos, h->mu, h->mus, h->q, h->ak, h->pairs, h->type, h->kn, h->qi, h->qd,
+                    h->dqi, h->dqd, h->trials, h->log_du, h->log_acc, h->sc};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+int dip_dmalloc(fg_dipsys *h, void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    h->device_bytes += bytes;
+    return FG_OK;
+}
+
+int dip_push_desc(fg_dipsys *h) {
+    CK(cudaMemcpyAsync(h->d_desc, &h->desc, sizeof(fgd::DipDesc), cudaMemcpyHostToDevice, h->stream));
+    return FG_OK;
+}
+
+int dip_read_scalars(fg_dipsys *h, fgd::DipScalars &s) {
+    CK(cudaMemcpyAsync(&s, h->sc, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+int dip_write_scalars(fg_dipsys *h, const fgd::DipScalars &s) {
+    CK(cudaMemcpyAsync(h->sc, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+int dip_ensure_trials(fg_dipsys *h, int64_t n, bool log) {
+    if (n > h->trials_cap) {
+        if (h->trials) cudaFree(h->trials);
+        h->trials = nullptr;
+        const int64_t cap = std::max<int64_t>(n, 1024);
+        int rc = dip_dmalloc(h, (void **)&h->trials, (size_t)cap * sizeof(fgd::DipTrial));
+        if (rc) return rc;
+        h->trials_cap = cap;
+        h->desc.trials = h->trials;
+    }
+    if (log && n > h->log_cap) {
+        if (h->log_du) cudaFree(h->log_du);
+        if (h->log_acc) cudaFree(h->log_acc);
+        h->log_du = nullptr;
+        h->log_acc = nullptr;
+        int rc = dip_dmalloc(h, (void **)&h->log_du, (size_t)n * sizeof(double));
+        if (!rc) rc = dip_dmalloc(h, (void **)&h->log_acc, (size_t)n);
+        if (rc) return rc;
+        h->log_cap = n;
+    }
+    h->desc.log_du = log ? h->log_du : nullptr;
+    h->desc.log_acc = log ? h->log_acc : nullptr;
+    return dip_push_desc(h);
+}
+
+// The reciprocal, self and surface energies from the host copies and Q(k).
+int dip_host_energies(fg_dipsys *h, const std::vector<double> &xyz, const std::vector<double> &mu, double &rec,
+                      double &self, double &surf) {
+    const fgd::DipDesc &d = h->desc;
+    std::vector<double2> qi(h->K), qd(h->K);
+    if (h->K) {
+        CK(cudaMemcpyAsync(qi.data(), h->qi, h->K * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(qd.data(), h->qd, h->K * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    rec = 0.0;
+    for (int k = 0; k < h->K; k++) {
+        double s = 0.0;
+        if (d.ii) s += qi[k].x * qi[k].x + qi[k].y * qi[k].y;
+        if (d.id) s += 2.0 * (d.quirk ? qi[k].x * qd[k].x - qi[k].y * qd[k].y : qi[k].x * qd[k].x + qi[k].y * qd[k].y);
+        if (d.dd) s += qd[k].x * qd[k].x + qd[k].y * qd[k].y;
+        rec += h->ak_h[k] * s;
+    }
+    rec *= d.recip_c;
+    double Eq = 0.0, Emu = 0.0, M[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < h->N; i++) {
+        const double qe = h->charges_h[i] * d.eff[h->types_h[i]];
+        if (d.ion_q) {
+            Eq += qe * qe;
+            for (int a = 0; a < 3; a++) M[a] += qe * xyz[3 * i + a];
+        }
+        if (d.id || d.dd) {
+            Emu += h->mus_h[i] * h->mus_h[i];
+            for (int a = 0; a < 3; a++) M[3 + a] += mu[3 * i + a] * h->mus_h[i];
+        }
+    }
+    self = (-d.alpha * (Eq + d.alpha2 * (2.0 / 3.0) * Emu) / std::sqrt(PI)) * d.lB;
+    surf = d.surf_c * (M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + 2.0 * (M[0] * M[3] + M[1] * M[4] + M[2] * M[5]) +
+                       M[3] * M[3] + M[4] * M[4] + M[5] * M[5]);
+    return FG_OK;
+}
+
+int dip_get_state(fg_dipsys *h, std::vector<double> &xyz, std::vector<double> &mu) {
+    std::vector<int64_t> X(3 * (size_t)h->N);
+    mu.resize(3 * (size_t)h->N);
+    CK(cudaMemcpyAsync(X.data(), h->pos, X.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(mu.data(), h->mu, mu.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    xyz.resize(X.size());
+    for (size_t k = 0; k < X.size(); k++) xyz[k] = from_fix(X[k], h->P.box[k % 3]);
+    return FG_OK;
+}
+
+// comp = {EwaldReal pairs, LJ pairs, reciprocal, self, surface, total}
+int dip_total(fg_dipsys *h, double *comp) {
+    fgd::dip_pairs_kernel<<<h->N, 128, 0, h->stream>>>(h->d_desc, h->pairs);
+    CK(cudaGetLastError());
+    std::vector<double> rows(2 * (size_t)h->N);
+    CK(cudaMemcpyAsync(rows.data(), h->pairs, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    double er = 0.0, el = 0.0;
+    for (int i = 0; i < h->N; i++) {
+        er += rows[2 * i];
+        el += rows[2 * i + 1];
+    }
+    std::vector<double> xyz, mu;
+    int rc = dip_get_state(h, xyz, mu);
+    if (rc) return rc;
+    double rec, self, surf;
+    rc = dip_host_energies(h, xyz, mu, rec, self, surf);
+    if (rc) return rc;
+    comp[0] = er;
+    comp[1] = el;
+    comp[2] = rec;
+    comp[3] = self;
+    comp[4] = surf;
+    comp[5] = er + el + rec + self + surf;
+    return FG_OK;
+}
+
+int dip_launch(fg_dipsys *h0, const fgd::DipDesc *descs, int n, int mode, cudaStream_t st) {
+    fgd::dip_sweep_kernel<<<n, h0->threads, 0, st>>>(descs, mode);
+    CK(cudaGetLastError());
+    return FG_OK;
+}
+
+int dip_run(fg_dipsys *const *sys, int n, fg_sweep_stats *per, fg_sweep_stats *total) {
+    if (!sys || n < 1) return fail(FG_ERR_INVALID, "bad argument");
+    fg_dipsys *h0 = sys[0];
+    int64_t maxn = 0;
+    for (int i = 0; i < n; i++) {
+        fg_dipsys *h = sys[i];
+        if (!h || !h->state_set) return fail(FG_ERR_STATE, "system %d has no state", i);
+        if (h->pending) return fail(FG_ERR_STATE, "system %d has a pending trial: commit it first", i);
+        if (h->device != h0->device) return fail(FG_ERR_INVALID, "systems must share the device");
+        if (h->threads != h0->threads) return fail(FG_ERR_INVALID, "systems must share the block size");
+        maxn = std::max(maxn, h->n_stream);
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    cudaStream_t st = h0->stream;
+    const fgd::DipDesc *descs = h0->d_desc;
+    fgd::DipDesc *tmp = nullptr;
+    if (n > 1) {
+        std::vector<fgd::DipDesc> v(n);
+        for (int i = 0; i < n; i++) v[i] = sys[i]->desc;
+        CK(cudaMalloc(&tmp, n * sizeof(fgd::DipDesc)));
+        CK(cudaMemcpyAsync(tmp, v.data(), n * sizeof(fgd::DipDesc), cudaMemcpyHostToDevice, st));
+        descs = tmp;
+    }
+    // launches of at most kChunk trials per system keep each kernel short
+    const int64_t kChunk = 16384;
+    const int64_t nl = (maxn + kChunk - 1) / kChunk;
+    std::vector<int64_t> ends((size_t)std::max<int64_t>(nl, 1) * n);
+    CK(cudaEventRecord(h0->ev0, st));
+    int rc = FG_OK;
+    for (int64_t c = 0; c < nl && !rc; c++) {
+        for (int i = 0; i < n; i++) {
+            int64_t &e = ends[(size_t)c * n + i];
+            e = std::min(sys[i]->n_stream, (c + 1) * kChunk);
+            CK(cudaMemcpyAsync(&sys[i]->sc->n_trials, &e, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        }
+        rc = dip_launch(h0, descs, n, 0, st);
+    }
+    CK(cudaEventRecord(h0->ev1, st));
+    CK(cudaEventSynchronize(h0->ev1));
+    if (tmp) cudaFree(tmp);
+    if (rc) return rc;
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, h0->ev0, h0->ev1));
+    std::vector<fgd::DipScalars> s1(n);
+    for (int i = 0; i < n; i++)
+        CK(cudaMemcpyAsync(&s1[i], sys[i]->sc, sizeof(fgd::DipScalars), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    fg_sweep_stats tot{};
+    int errs = 0;
+    for (int i = 0; i < n; i++) {
+        fg_sweep_stats x{};
+        x.trials = s1[i].cursor;
+        x.accepted = s1[i].n_accepted - sys[i]->acc0;
+        x.energy_change = s1[i].usum;
+        x.device_ms = ms;
+        x.sweep_kernel_ms = ms;
+        x.sweep_launches = (int32_t)nl;
+        x.error_flags = s1[i].error;
+        x.kernel_launches = nl;
+        x.rebuilds = s1[i].n_rebuilds;
+        errs |= s1[i].error;
+        if (per) per[i] = x;
+        tot.trials += x.trials;
+        tot.accepted += x.accepted;
+        tot.rebuilds += x.rebuilds;
+        tot.energy_change += x.energy_change;
+        sys[i]->n_stream = 0;
+    }
+    tot.device_ms = ms;
+    tot.sweep_kernel_ms = ms;
+    tot.sweep_launches = (int32_t)nl;
+    tot.kernel_launches = nl;
+    tot.error_flags = errs;
+    if (total) *total = tot;
+    if (errs) return fail(FG_ERR_DEVICE, "device error flags 0x%x", errs);
+    return FG_OK;
+}
+
+int dip_upload(fg_dipsys *h, int64_t n, const int32_t *kind, const int32_t *idx, const double *axis,
+               const double *angle, const double *disp, const double *u, bool log) {
+    if (!h || n < 0 || (n > 0 && (!kind || !idx || !u))) return fail(FG_ERR_INVALID, "bad argument");
+    if (!h->state_set) return fail(FG_ERR_STATE, "fg_dip_set_state first");
+    if (h->pending) return fail(FG_ERR_STATE, "a trial is pending: commit it first");
+    std::vector<fgd::DipTrial> tr(n);
+    for (int64_t k = 0; k < n; k++) {
+        fgd::DipTrial &t = tr[k];
+        t = fgd::DipTrial{};
+        if (idx[k] < 0 || idx[k] >= h->N) return fail(FG_ERR_INVALID, "trial %lld: particle out of range", (long long)k);
+        t.idx = idx[k];
+        t.kind = kind[k];
+        t.u = u[k];
+        t.q[0] = 1.0;
+        if (kind[k] == 1) {
+            if (!axis || !angle) return fail(FG_ERR_INVALID, "rotations need axis and angle");
+            double ax = axis[3 * k], ay = axis[3 * k + 1], az = axis[3 * k + 2];
+            const double nrm = std::sqrt(ax * ax + ay * ay + az * az);
+            if (!(nrm > 0)) return fail(FG_ERR_INVALID, "trial %lld: zero rotation axis", (long long)k);
+            ax /= nrm;
+            ay /= nrm;
+            az /= nrm;
+            // Eigen::AngleAxisd(angle, u) as a quaternion (geometry.cpp:762)
+            const double ha = 0.5 * angle[k], sh = std::sin(ha);
+            t.q[0] = std::cos(ha);
+            t.q[1] = sh * ax;
+            t.q[2] = sh * ay;
+            t.q[3] = sh * az;
+        } else if (kind[k] == 2) {
+            if (!disp) return fail(FG_ERR_INVALID, "translations need disp");
+            for (int a = 0; a < 3; a++) t.t[a] = to_fix(disp[3 * k + a], h->P.box[a]);
+        } else {
+            return fail(FG_ERR_INVALID, "trial %lld: kind must be 1 (rotation) or 2 (translation)", (long long)k);
+        }
+    }
+    int rc = dip_ensure_trials(h, n, log);
+    if (rc) return rc;
+    if (n) CK(cudaMemcpyAsync(h->trials, tr.data(), n * sizeof(fgd::DipTrial), cudaMemcpyHostToDevice, h->stream));
+    fgd::DipScalars s;
+    rc = dip_read_scalars(h, s);
+    if (rc) return rc;
+    s.cursor = 0;
+    s.n_trials = 0;
+    s.usum = 0.0;
+    s.error = 0;
+    h->acc0 = s.n_accepted;
+    h->n_stream = n;
+    return dip_write_scalars(h, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out) {
+    if (!params || !out) return fail(FG_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const fg_params &P = *params;
+    if (P.model != FG_MODEL_EWALD_DIPOLE) return fail(FG_ERR_INVALID, "fg_dip_create needs FG_MODEL_EWALD_DIPOLE");
+    if (n_particles < 2 || n_particles >= (1 << 24)) return fail(FG_ERR_INVALID, "particle count must be 2..2^24");
+    if (P.n_types < 1 || P.n_types > FG_MAX_TYPES) return fail(FG_ERR_INVALID, "bad type count");
+    if ((P.ewald_terms & ~7) != 0) return fail(FG_ERR_INVALID, "bad ewald_terms");
+    if (!(P.bjerrum > 0) || !(P.ewald_alpha > 0) || !(P.ewald_cutoff > 0) || !(P.ewald_debye_length > 0))
+        return fail(FG_ERR_INVALID, "bad Ewald parameters");
+    for (int a = 0; a < 3; a++)
+        if (!(P.box[a] > 0)) return fail(FG_ERR_INVALID, "bad box");
+    const int kcc = (int)std::ceil(P.ewald_cutoff_k);
+    if (kcc < 0 || kcc > fgd::kDipMaxKcc) return fail(FG_ERR_INVALID, "cutoffK must be 0..%d", fgd::kDipMaxKcc);
+    fg_dipsys *h = new fg_dipsys();
+    h->P = P;
+    h->N = n_particles;
+    h->kcc = kcc;
+    auto bail = [&](int rc) {
+        dip_free(h);
+        delete h;
+        return rc;
+    };
+    if (cudaGetDevice(&h->device) != cudaSuccess) return bail(fail(FG_ERR_CUDA, "no CUDA device"));
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(FG_ERR_CUDA, "stream"));
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    // k-vectors as kVectorChange enumerates them (ewald.h:330-378), n-vectors kept
+    std::vector<int> n3;
+    std::vector<double> ak, kv3;
+    enumerate_k(P, n3, ak, kv3);
+    h->K = (int)ak.size();
+    h->ak_h = ak;
+    h->kn_h.resize(h->K);
+    for (int k = 0; k < h->K; k++)
+        h->kn_h[k] = make_char4((signed char)n3[3 * k], (signed char)n3[3 * k + 1], (signed char)n3[3 * k + 2], 0);
+    fgd::DipDesc &d = h->desc;
+    d.N = h->N;
+    d.K = h->K;
+    d.kcc = kcc;
+    d.nt = P.n_types;
+    d.ii = (P.ewald_terms & FG_EWALD_ION_ION) ? 1 : 0;
+    d.id = (P.ewald_terms & FG_EWALD_ION_DIPOLE) ? 1 : 0;
+    d.dd = (P.ewald_terms & FG_EWALD_DIPOLE_DIPOLE) ? 1 : 0;
+    d.quirk = P.ewald_dipole_quirk ? 1 : 0;
+    d.any_term = (d.ii || d.id || d.dd) ? 1 : 0;
+    d.ion_q = (d.ii || d.id) ? 1 : 0;
+    d.dip_q = (d.id || d.dd) ? 1 : 0;
+    d.dip_q_build = d.quirk ? d.dd : d.dip_q;
+    d.uf = P.ewald_update_frequency;
+    const double V = P.box[0] * P.box[1] * P.box[2];
+    for (int a = 0; a < 3; a++) {
+        d.L[a] = P.box[a];
+        d.s64[a] = P.box[a] / TWO64;
+        d.tpl[a] = 2.0 * PI / P.box[a];
+    }
+    d.alpha = P.ewald_alpha;
+    d.alpha2 = d.alpha * d.alpha;
+    d.rc2 = P.ewald_cutoff * P.ewald_cutoff;
+    d.kappa = 1.0 / P.ewald_debye_length;
+    // kappa / 2 alpha and kappa rc below 1e-20: erfc(ar +- h) = erfc(ar) and
+    // e^{+-kappa r} = 1 in FP64, so the screened form is erfc(ar) / r exactly
+    d.small_kappa = (d.kappa / (2.0 * d.alpha) < 1e-20 && d.kappa * P.ewald_cutoff < 1e-20) ? 1 : 0;
+    d.lB = P.bjerrum;
+    d.kT = P.kT_scale > 0 ? P.kT_scale : 1.0;
+    d.recip_c = 2.0 * PI / V * d.lB;
+    d.surf_c = (P.ewald_eps_surf < 1) ? 0.0 : 2.0 * PI / ((2.0 * P.ewald_eps_surf + 1.0) * V) * d.lB;
+    d.t1c = 2.0 * d.alpha / std::sqrt(PI);
+    d.t2c = 4.0 * d.alpha2 * d.alpha / 3.0 / std::sqrt(PI);
+    const int nt = P.n_types;
+    auto qs = [&](int t) {   // effective charge (ewald.h:532-549)
+        const double r = 0.5 * P.type_sigma[t];
+        double q = P.type_charge[t];
+        if (std::fabs(d.kappa * r) > 1e-9) q *= std::sinh(r * d.kappa) / r / d.kappa;
+        return q;
+    };
+    for (int i = 0; i < nt; i++) {
+        // a neutral type has no effective charge (the reference's 0/0 is
+        // never used when no ion term is on)
+        d.eff[i] = P.type_charge[i] != 0.0 ? qs(i) / P.type_charge[i] : 0.0;
+        for (int j = 0; j < nt; j++) {
+            const double sig = 0.5 * (P.type_sigma[i] + P.type_sigma[j]);
+            d.s2[i * nt + j] = sig * sig;
+            d.eps4[i * nt + j] = 4 * std::sqrt(P.type_eps[i] * P.type_eps[j]);
+            d.qeqe[i * nt + j] = (P.type_charge[i] != 0.0 && P.type_charge[j] != 0.0)
+                                     ? qs(i) * qs(j) / P.type_charge[i] / P.type_charge[j] : 0.0;
+        }
+    }
+    int rc_;
+#define TRY(x)                     \
+    do {                           \
+        rc_ = (x);                 \
+        if (rc_) return bail(rc_); \
+    } while (0)
+    const size_t N = h->N, K = std::max(h->K, 1);
+    TRY(dip_dmalloc(h, (void **)&h->d_desc, sizeof(fgd::DipDesc)));
+    TRY(dip_dmalloc(h, (void **)&h->pos, 3 * N * sizeof(int64_t)));
+    TRY(dip_dmalloc(h, (void **)&h->mu, 3 * N * sizeof(double)));
+    TRY(dip_dmalloc(h, (void **)&h->mus, N * sizeof(double)));
+    TRY(dip_dmalloc(h, (void **)&h->q, N * sizeof(double)));
+    TRY(dip_dmalloc(h, (void **)&h->type, N * sizeof(int32_t)));
+    TRY(dip_dmalloc(h, (void **)&h->pairs, 2 * N * sizeof(double)));
+    TRY(dip_dmalloc(h, (void **)&h->kn, K * sizeof(char4)));
+    TRY(dip_dmalloc(h, (void **)&h->ak, K * sizeof(double)));
+    TRY(dip_dmalloc(h, (void **)&h->qi, K * sizeof(double2)));
+    TRY(dip_dmalloc(h, (void **)&h->qd, K * sizeof(double2)));
+    TRY(dip_dmalloc(h, (void **)&h->dqi, K * sizeof(double2)));
+    TRY(dip_dmalloc(h, (void **)&h->dqd, K * sizeof(double2)));
+    TRY(dip_dmalloc(h, (void **)&h->sc, sizeof(fgd::DipScalars)));
+    d.pos = h->pos;
+    d.mu = h->mu;
+    d.mus = h->mus;
+    d.q = h->q;
+    d.type = h->type;
+    d.kn = h->kn;
+    d.ak = h->ak;
+    d.qi = h->qi;
+    d.qd = h->qd;
+    d.dqi = h->dqi;
+    d.dqd = h->dqd;
+    d.sc = h->sc;
+    if (h->K) {
+        if (cudaMemcpyAsync(h->kn, h->kn_h.data(), h->K * sizeof(char4), cudaMemcpyHostToDevice, h->stream) ||
+            cudaMemcpyAsync(h->ak, ak.data(), h->K * sizeof(double), cudaMemcpyHostToDevice, h->stream))
+            return bail(fail(FG_ERR_CUDA, "upload of the k-vectors failed"));
+    }
+    TRY(dip_ensure_trials(h, 1, false));
+    fgd::DipScalars s{};
+    TRY(dip_write_scalars(h, s));
+#undef TRY
+    *out = h;
+    return FG_OK;
+}
+
+int fg_dip_destroy(fg_dipsys *h) {
+    if (!h) return FG_OK;
+    cudaStreamSynchronize(h->stream);
+    dip_free(h);
+    delete h;
+    return FG_OK;
+}
+
+int fg_dip_num_kvectors(fg_dipsys *h) { return h ? h->K : 0; }
+
+int fg_dip_set_state(fg_dipsys *h, const double *xyz, const double *mu_unit, const double *mu_scalar,
+                     const double *charges, const int32_t *type_ids) {
+    if (!h || !xyz || !mu_unit || !mu_scalar || !type_ids) return fail(FG_ERR_INVALID, "null argument");
+    const int N = h->N;
+    std::vector<int64_t> X(3 * (size_t)N);
+    h->types_h.assign(type_ids, type_ids + N);
+    h->charges_h.resize(N);
+    h->mus_h.assign(mu_scalar, mu_scalar + N);
+    for (int i = 0; i < N; i++) {
+        if (type_ids[i] < 0 || type_ids[i] >= h->P.n_types) return fail(FG_ERR_INVALID, "particle %d: bad type", i);
+        h->charges_h[i] = charges ? charges[i] : h->P.type_charge[type_ids[i]];
+        for (int a = 0; a < 3; a++) {
+            if (!std::isfinite(xyz[3 * i + a]) || !std::isfinite(mu_unit[3 * i + a]))
+                return fail(FG_ERR_INVALID, "particle %d: non-finite input", i);
+            X[3 * i + a] = to_fix(xyz[3 * i + a], h->P.box[a]);
+        }
+    }
+    CK(cudaMemcpyAsync(h->pos, X.data(), X.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->mu, mu_unit, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->mus, mu_scalar, (size_t)N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->q, h->charges_h.data(), (size_t)N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->type, type_ids, (size_t)N * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    int rc = dip_push_desc(h);
+    if (rc) return rc;
+    fgd::DipScalars s{};
+    std::vector<double> xyzw, muw;
+    rc = dip_write_scalars(h, s);
+    if (rc) return rc;
+    h->state_set = true;
+    h->pending = false;
+    // surface sums and energies on the host from the uploaded (wrapped) state
+    rc = dip_get_state(h, xyzw, muw);
+    if (rc) return rc;
+    for (int i = 0; i < N; i++) {
+        const double qe = h->charges_h[i] * h->desc.eff[h->types_h[i]];
+        for (int a = 0; a < 3; a++) {
+            if (h->desc.ion_q) s.M[a] += qe * xyzw[3 * i + a];
+            if (h->desc.id || h->desc.dd) s.M[3 + a] += muw[3 * i + a] * h->mus_h[i];
+        }
+    }
+    rc = dip_write_scalars(h, s);
+    if (rc) return rc;
+    fgd::dip_build_kernel<<<1, h->threads, 0, h->stream>>>(h->d_desc);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    double comp[6];
+    rc = dip_total(h, comp);
+    if (rc) return rc;
+    rc = dip_read_scalars(h, s);
+    if (rc) return rc;
+    s.utot = comp[5];
+    s.n_accepted = 0;
+    s.n_rebuilds = 0;
+    s.cnt_accepted = 0;
+    return dip_write_scalars(h, s);
+}
+
+int fg_dip_get_state(fg_dipsys *h, double *xyz, double *mu_unit) {
+    if (!h) return fail(FG_ERR_INVALID, "null argument");
+    if (!h->state_set) return fail(FG_ERR_STATE, "no state");
+    std::vector<double> x, m;
+    int rc = dip_get_state(h, x, m);
+    if (rc) return rc;
+    if (xyz) std::copy(x.begin(), x.end(), xyz);
+    if (mu_unit) std::copy(m.begin(), m.end(), mu_unit);
+    return FG_OK;
+}
+
+int fg_dip_set_threads(fg_dipsys *h, int32_t threads) {
+    if (!h) return fail(FG_ERR_INVALID, "null argument");
+    if (threads < 32 || threads > fgd::kDipMaxThreads || threads % 32)
+        return fail(FG_ERR_INVALID, "threads must be a multiple of 32 in 32..%d", fgd::kDipMaxThreads);
+    h->threads = threads;
+    return FG_OK;
+}
+
+int fg_dip_trial_du(fg_dipsys *h, int32_t i, const double *new_xyz, const double *new_mu_unit, double *du) {
+    if (!h || !new_xyz || !du) return fail(FG_ERR_INVALID, "null argument");
+    if (!h->state_set) return fail(FG_ERR_STATE, "fg_dip_set_state first");
+    if (h->pending) return fail(FG_ERR_STATE, "a trial is pending: commit it first");
+    if (i < 0 || i >= h->N) return fail(FG_ERR_INVALID, "particle out of range");
+    fgd::DipTrial t{};
+    t.idx = i;
+    t.kind = 3;
+    for (int a = 0; a < 3; a++) t.t[a] = to_fix(new_xyz[a], h->P.box[a]);
+    if (new_mu_unit) {
+        for (int a = 0; a < 3; a++) t.q[1 + a] = new_mu_unit[a];
+    } else {
+        CK(cudaMemcpyAsync(&t.q[1], h->mu + 3 * (size_t)i, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    int rc = dip_ensure_trials(h, 1, false);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->trials, &t, sizeof(t), cudaMemcpyHostToDevice, h->stream));
+    rc = dip_launch(h, h->d_desc, 1, 1, h->stream);
+    if (rc) return rc;
+    fgd::DipScalars s;
+    rc = dip_read_scalars(h, s);
+    if (rc) return rc;
+    if (s.error) return fail(FG_ERR_DEVICE, "device error flags 0x%x", s.error);
+    *du = s.pend_du;
+    h->pending = true;
+    return FG_OK;
+}
+
+int fg_dip_commit(fg_dipsys *h, int32_t accepted) {
+    if (!h) return fail(FG_ERR_INVALID, "null argument");
+    if (!h->pending) return fail(FG_ERR_STATE, "no pending trial");
+    h->pending = false;
+    if (!accepted) return FG_OK;
+    int rc = dip_launch(h, h->d_desc, 1, 2, h->stream);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    return FG_OK;
+}
+
+int fg_dip_stream_upload(fg_dipsys *h, int64_t n, const int32_t *kind, const int32_t *idx, const double *axis,
+                         const double *angle, const double *disp, const double *u) {
+    return dip_upload(h, n, kind, idx, axis, angle, disp, u, false);
+}
+
+int fg_dip_run_many(fg_dipsys *const *systems, int32_t n_systems, fg_sweep_stats *per_system, fg_sweep_stats *total) {
+    return dip_run(systems, n_systems, per_system, total);
+}
+
+int fg_dip_sweep(fg_dipsys *h, int64_t n, const int32_t *kind, const int32_t *idx, const double *axis,
+                 const double *angle, const double *disp, const double *u, uint8_t *acc, double *du,
+                 fg_sweep_stats *stats) {
+    const bool log = acc || du;
+    int rc = dip_upload(h, n, kind, idx, axis, angle, disp, u, log);
+    if (rc) return rc;
+    fg_sweep_stats st{};
+    rc = dip_run(&h, 1, nullptr, &st);
+    if (stats) *stats = st;
+    if (rc) return rc;
+    if (log && n > 0) {
+        std::vector<double> l(n);
+        std::vector<uint8_t> a(n);
+        CK(cudaMemcpyAsync(l.data(), h->log_du, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(a.data(), h->log_acc, n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (du) std::copy(l.begin(), l.end(), du);
+        if (acc) std::copy(a.begin(), a.end(), acc);
+    }
+    return FG_OK;
+}
+
+int fg_dip_total_energy(fg_dipsys *h, double *comp) {
+    if (!h || !comp) return fail(FG_ERR_INVALID, "null argument");
+    if (!h->state_set) return fail(FG_ERR_STATE, "no state");
+    return dip_total(h, comp);
+}
+
+int fg_dip_running_energy(fg_dipsys *h, double *u) {
+    if (!h || !u) return fail(FG_ERR_INVALID, "null argument");
+    fgd::DipScalars s;
+    int rc = dip_read_scalars(h, s);
+    if (rc) return rc;
+    *u = s.utot;
+    return FG_OK;
+}
+
+// Draws of n AtomicRotation / AtomicTranslation trials on one atomic group of
+// n_particles, as the reference takes them from slump (std::mt19937 seeded
+// with seed): per trial the move (rotation when a uniform falls below
+// p_rotate; with p_rotate < 0 the caller's kind[] says), then
+// slump.element over the one group, the particle (Group::random,
+// group.h:129-134), for a rotation a ranunit axis (point.h:74-88) and the
+// angle dprot * half() (move.h:1020-1030), for a translation three
+// dp * half() (move.h:830-840), and the Metropolis uniform.
+int fg_dip_draw_stream(uint32_t seed, int32_t n_particles, int64_t n, double p_rotate, double dp, double dprot,
+                       int32_t *kind, int32_t *idx, double *axis, double *angle, double *disp, double *u) {
+    if (n_particles < 1 || n < 0 || (n > 0 && (!kind || !idx || !axis || !angle || !disp || !u)))
+        return fail(FG_ERR_INVALID, "bad argument");
+    std::mt19937 eng(seed);
+    auto uni = [&]() {
+        std::uniform_real_distribution<double> U(0, 1);
+        return U(eng);
+    };
+    auto range = [&](int a, int b) {
+        std::uniform_int_distribution<int> D(a, b);
+        return D(eng);
+    };
+    for (int64_t t = 0; t < n; t++) {
+        const bool rot = p_rotate < 0 ? kind[t] == 1 : uni() < p_rotate;
+        kind[t] = rot ? 1 : 2;
+        range(0, 0);
+        idx[t] = range(0, n_particles - 1);
+        double v[3] = {0, 0, 0}, an = 0.0, d[3] = {0, 0, 0};
+        if (rot) {
+            double r2;
+            do {
+                for (int a = 0; a < 3; a++) v[a] = 2 * uni() - 1;
+                r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            } while (r2 > 1);
+            const double s = std::sqrt(r2);
+            for (int a = 0; a < 3; a++) v[a] /= s;
+            an = dprot * (uni() - 0.5);
+        } else {
+            for (int a = 0; a < 3; a++) d[a] = dp * (uni() - 0.5);
+        }
+        u[t] = uni();
+        for (int a = 0; a < 3; a++) {
+            axis[3 * t + a] = v[a];
+            disp[3 * t + a] = d[a];
+        }
+        angle[t] = an;
+    }
+    return FG_OK;
+}
+
+int64_t fg_dip_device_bytes(fg_dipsys *h) { return h ? (int64_t)h->device_bytes : 0; }
+
+}  // extern "C"

@@ -118,6 +118,22 @@ def lib(build_if_missing=True):
             "fg_batch_autotune": ([vp, i64, dp], ctypes.c_int),
             "fg_mol_autotune": ([vp, i64, dp], ctypes.c_int),
             "fg_tune_reset": ([], ctypes.c_int),
+            "fg_dip_create": ([vp, i32, ctypes.POINTER(vp)], ctypes.c_int),
+            "fg_dip_destroy": ([vp], ctypes.c_int),
+            "fg_dip_num_kvectors": ([vp], ctypes.c_int),
+            "fg_dip_set_state": ([vp, dp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_dip_get_state": ([vp, dp, dp], ctypes.c_int),
+            "fg_dip_set_threads": ([vp, i32], ctypes.c_int),
+            "fg_dip_trial_du": ([vp, i32, dp, dp, dp], ctypes.c_int),
+            "fg_dip_commit": ([vp, i32], ctypes.c_int),
+            "fg_dip_sweep": ([vp, i64, dp, dp, dp, dp, dp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_dip_stream_upload": ([vp, i64, dp, dp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_dip_run_many": ([dp, i32, dp, dp], ctypes.c_int),
+            "fg_dip_draw_stream": ([u32, i32, i64, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp, dp, dp,
+                                    dp, dp], ctypes.c_int),
+            "fg_dip_total_energy": ([vp, dp], ctypes.c_int),
+            "fg_dip_running_energy": ([vp, dp], ctypes.c_int),
+            "fg_dip_device_bytes": ([vp], ctypes.c_int64),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -654,3 +670,123 @@ class MolSystem:
     @property
     def device_bytes(self):
         return int(lib().fg_mol_device_bytes(self.h))
+
+
+# ---------------------------------------------------------------- point dipoles under Ewald
+def dip_draw_stream(seed, n_particles, n, p_rotate=0.5, dp=0.7, dprot=1.0, kinds=None):
+    """The reference's slump draws for n AtomicRotation / AtomicTranslation
+    trials (fg_dip_draw_stream): dict(kind, idx, axis, angle, disp, u). With
+    kinds given (1 rotation, 2 translation) p_rotate is not used."""
+    kind = np.empty(n, np.int32) if kinds is None else np.array(kinds, dtype=np.int32)
+    if kinds is not None:
+        p_rotate = -1.0
+    idx = np.empty(n, np.int32)
+    axis = np.empty((n, 3))
+    angle = np.empty(n)
+    disp = np.empty((n, 3))
+    u = np.empty(n)
+    _check(lib().fg_dip_draw_stream(int(seed), int(n_particles), int(n), float(p_rotate), float(dp), float(dprot),
+                                    _p(kind), _p(idx), _p(axis), _p(angle), _p(disp), _p(u)))
+    return dict(kind=kind, idx=idx, axis=axis, angle=angle, disp=disp, u=u)
+
+
+def _dip_stream_arrays(st):
+    return [np.ascontiguousarray(st[k], dtype=np.int32 if k in ("kind", "idx") else np.float64)
+            for k in ("kind", "idx", "axis", "angle", "disp", "u")]
+
+
+def dip_run_many(systems):
+    """Run the staged streams of several DipoleSystems in one launch sequence
+    (one CTA per system)."""
+    arr = (ctypes.c_void_p * len(systems))(*[s.h.value for s in systems])
+    per = (SweepStats * len(systems))()
+    tot = SweepStats()
+    _check(lib().fg_dip_run_many(ctypes.cast(arr, ctypes.c_void_p), len(systems), ctypes.cast(per, ctypes.c_void_p),
+                                 ctypes.byref(tot)))
+    return [p.as_dict() for p in per], tot.as_dict()
+
+
+class DipoleSystem:
+    """Point charges and point dipoles under Ewald summation on one GPU
+    (fg_dip_* C-ABI): AtomicRotation / AtomicTranslation with the energy of
+    NonbondedEwald<Tspace, LennardJonesLB, ...>."""
+
+    def __init__(self, params, xyz, mu_unit, mu_scalar, type_ids, charges=None, threads=None):
+        n = len(type_ids)
+        h = ctypes.c_void_p()
+        _check(lib().fg_dip_create(ctypes.byref(params), n, ctypes.byref(h)))
+        self.h = h
+        self.n = n
+        if threads:
+            _check(lib().fg_dip_set_threads(self.h, int(threads)))
+        self.set_state(xyz, mu_unit, mu_scalar, type_ids, charges)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fg_dip_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_kvectors(self):
+        return int(lib().fg_dip_num_kvectors(self.h))
+
+    def set_state(self, xyz, mu_unit, mu_scalar, type_ids, charges=None):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        mu = np.ascontiguousarray(mu_unit, dtype=np.float64).reshape(-1, 3)
+        ms = np.ascontiguousarray(mu_scalar, dtype=np.float64)
+        ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+        q = None if charges is None else np.ascontiguousarray(charges, dtype=np.float64)
+        _check(lib().fg_dip_set_state(self.h, _p(xyz), _p(mu), _p(ms), _p(q), _p(ids)))
+
+    def state(self):
+        xyz = np.empty((self.n, 3))
+        mu = np.empty((self.n, 3))
+        _check(lib().fg_dip_get_state(self.h, _p(xyz), _p(mu)))
+        return xyz, mu
+
+    def trial_du(self, i, new_xyz, new_mu=None):
+        x = np.ascontiguousarray(new_xyz, dtype=np.float64)
+        m = None if new_mu is None else np.ascontiguousarray(new_mu, dtype=np.float64)
+        du = np.zeros(1)
+        _check(lib().fg_dip_trial_du(self.h, int(i), _p(x), _p(m), _p(du)))
+        return float(du[0])
+
+    def commit(self, accepted):
+        _check(lib().fg_dip_commit(self.h, 1 if accepted else 0))
+
+    def sweep(self, st, log=True):
+        kind, idx, axis, angle, disp, u = _dip_stream_arrays(st)
+        n = len(idx)
+        acc = np.empty(n, np.uint8) if log else None
+        du = np.empty(n) if log else None
+        stats = SweepStats()
+        _check(lib().fg_dip_sweep(self.h, n, _p(kind), _p(idx), _p(axis), _p(angle), _p(disp), _p(u), _p(acc),
+                                  _p(du), ctypes.byref(stats)))
+        out = stats.as_dict()
+        out.update(acc=acc, du=du)
+        return out
+
+    def stream_upload(self, st):
+        kind, idx, axis, angle, disp, u = _dip_stream_arrays(st)
+        _check(lib().fg_dip_stream_upload(self.h, len(idx), _p(kind), _p(idx), _p(axis), _p(angle), _p(disp), _p(u)))
+
+    def total_energy(self):
+        """{EwaldReal pairs, LJ pairs, reciprocal, self, surface, total} in FP64."""
+        c = np.empty(6)
+        _check(lib().fg_dip_total_energy(self.h, _p(c)))
+        return c
+
+    def running_energy(self):
+        u = np.zeros(1)
+        _check(lib().fg_dip_running_energy(self.h, _p(u)))
+        return float(u[0])
+
+    @property
+    def device_bytes(self):
+        return int(lib().fg_dip_device_bytes(self.h))

@@ -374,6 +374,56 @@ int fg_mol_autotune(fg_molsys *h, int64_t n_trials, fg_tune_report *report);
 /* Forget the recorded choices (back to the built-in heuristics). */
 int fg_tune_reset(void);
 
+/* ---------------------------------------------------------------- point dipoles under Ewald
+ * Point charges and point dipoles (DipoleParticle, point.h:591-680) in one
+ * atomic group, energy NonbondedEwald<Tspace, LennardJonesLB, useIonIon,
+ * useIonDipole, useDipoleDipole> (ewald.h:228-757; params.ewald_terms holds
+ * the three flags, params.ewald_dipole_quirk selects the sum as ewald.h
+ * states it (0) or as its live code computes it (1)), moves AtomicRotation
+ * (move.h:976-1072) and AtomicTranslation (move.h:818-901). FP64 throughout;
+ * one CTA per system, many systems per launch (fg_dip_run_many). */
+typedef struct fg_dipsys fg_dipsys;
+
+/* Replaces: Space<Cuboid, DipoleParticle> + NonbondedEwald construction
+ * (ewald.h:507-550). model must be FG_MODEL_EWALD_DIPOLE; cutoffK <= 31. */
+int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out);
+int fg_dip_destroy(fg_dipsys *h);
+int fg_dip_num_kvectors(fg_dipsys *h);
+/* Positions (Angstrom), dipole unit vectors, dipole scalars (e Angstrom),
+ * charges (NULL: the type charges) and atom types. Q(k) is built from
+ * scratch (setSpace, ewald.h:746-756). */
+int fg_dip_set_state(fg_dipsys *h, const double *xyz, const double *mu_unit, const double *mu_scalar,
+                     const double *charges, const int32_t *type_ids);
+int fg_dip_get_state(fg_dipsys *h, double *xyz, double *mu_unit);
+/* Threads per CTA (multiple of 32, 32..256; default 128). */
+int fg_dip_set_threads(fg_dipsys *h, int32_t threads);
+/* Energy change of moving particle i to new_xyz with dipole new_mu_unit
+ * (NULL: unchanged); replaces Energy::energyChange after updateChange
+ * (energy.h:3577-3621, ewald.h:651-705). One trial may be pending. */
+int fg_dip_trial_du(fg_dipsys *h, int32_t i, const double *new_xyz, const double *new_mu_unit, double *du);
+/* acceptMove / rejectMove + NonbondedEwald::update (ewald.h:613-646). */
+int fg_dip_commit(fg_dipsys *h, int32_t accepted);
+/* n trials: kind[t] 1 = AtomicRotation of particle idx[t] by angle[t] about
+ * axis[t] (3 per trial), 2 = AtomicTranslation by disp[t] (3 per trial);
+ * Metropolis uniform u[t] (reject iff u > exp(-dU/kT)). acc/du may be NULL. */
+int fg_dip_sweep(fg_dipsys *h, int64_t n, const int32_t *kind, const int32_t *idx, const double *axis,
+                 const double *angle, const double *disp, const double *u, uint8_t *acc, double *du,
+                 fg_sweep_stats *stats);
+/* Stage a stream without running it; fg_dip_run_many runs the staged streams
+ * of many systems in one launch sequence (one CTA per system). */
+int fg_dip_stream_upload(fg_dipsys *h, int64_t n, const int32_t *kind, const int32_t *idx, const double *axis,
+                         const double *angle, const double *disp, const double *u);
+int fg_dip_run_many(fg_dipsys *const *systems, int32_t n_systems, fg_sweep_stats *per_system, fg_sweep_stats *total);
+/* The reference's slump draws for n trials (see fg_dip.cu); with p_rotate < 0
+ * kind[] is read (the caller's move order), else drawn. */
+int fg_dip_draw_stream(uint32_t seed, int32_t n_particles, int64_t n, double p_rotate, double dp, double dprot,
+                       int32_t *kind, int32_t *idx, double *axis, double *angle, double *disp, double *u);
+/* comp = {EwaldReal pairs, LJ pairs, reciprocal, self, surface, total}, FP64. */
+int fg_dip_total_energy(fg_dipsys *h, double *comp);
+/* Total energy at fg_dip_set_state plus accepted dU and rebuild corrections since. */
+int fg_dip_running_energy(fg_dipsys *h, double *u);
+int64_t fg_dip_device_bytes(fg_dipsys *h);
+
 #ifdef __cplusplus
 }
 #endif
