@@ -161,7 +161,10 @@ def _cpu_system(kind, seed):
     """One FP64 oracle system of the given workload kind (built once per process)."""
     import numpy as np
     from beofaunus_gb300 import workloads
-    from oracle.oracle import OracleMol, OracleSystem
+    from oracle.oracle import OracleDip, OracleMol, OracleSystem
+    if kind == "dipoles":
+        p, xyz, mu, mus, ids, q = dipole_fluid(seed)
+        return OracleDip(p, xyz, mu, mus, ids, q=q), None
     if kind == "molecules":
         p, xyz, mu, mus, ids = workloads.dipolar_molecules(1000, seed=seed)
         return OracleMol(p, xyz, mu, mus, ids, 20), None
@@ -181,7 +184,7 @@ def _cpu_task(args):
     """Time-bounded sample of the oracle port on one core: chunks of trials
     until ``seconds`` of trial time have passed. Returns (trials, seconds)."""
     kind, seed, seconds = args
-    from oracle.oracle import mol_stream, translation_stream
+    from oracle.oracle import dip_stream, mol_stream, translation_stream
     key = (kind, seed)
     if key not in _cpu_cache:
         _cpu_cache[key] = _cpu_system(kind, seed) + ([0],)
@@ -193,6 +196,11 @@ def _cpu_task(args):
             t0 = time.perf_counter()
             o.run_stream(st)
             k = 4
+        elif kind == "dipoles":
+            k = 64
+            st = dip_stream(seed * 100000 + chunk[0], DIP_N, k, 0.5, DIP_DP, DIP_DPROT)
+            t0 = time.perf_counter()
+            o.run_stream(st)
         else:
             k = 64 if kind == "rpm16k" else 256
             idx, disp, u = translation_stream(seed * 100000 + chunk[0], dpp, k)
@@ -494,7 +502,7 @@ def cpu_kinds(workload, cores=None):
     processes run and, for size mixes, each one's share of the trials (16
     quantiles of the mix; a size's trials are proportional to its N)."""
     cores = cores or os.cpu_count() or 1
-    if workload in ("rpm16k", "rpm800", "molecules"):
+    if workload in ("rpm16k", "rpm800", "molecules", "dipoles"):
         return [workload], None
     if workload == "pt64":
         sizes = sorted(_pt_sizes())
@@ -514,7 +522,8 @@ def cpu_kinds(workload, cores=None):
 
 
 WORKLOAD_NAMES = {"rpm16k": WORKLOAD, "rpm800": "rpm800_ewald_wca_batched", "pt64": "pt64_dh_lj_ladder",
-                  "molecules": "dipolar_molecules_1000x20_batched", "serving": "serving_dh_lj_poisson"}
+                  "molecules": "dipolar_molecules_1000x20_batched", "serving": "serving_dh_lj_poisson",
+                  "dipoles": "stockmayer100_dipolar_ewald_batched"}
 
 
 def base_line(metric_value, steps, warm, ms_per_step, world, config, dtype, data):
@@ -804,6 +813,154 @@ def run_molecules(args, rank, world):
         print(json.dumps(out))
 
 
+# ----------------------------------------------------------------- point dipoles under Ewald
+# The reference's Stockmayer example's shape (stockmayer.json): 100 LJ point
+# dipoles, |mu| 1.652 e A, sigma 2.8863 A, eps 1.97 kJ/mol, L 29.6336 A,
+# T 315.8 K (lB 529 A), dp 0.7 A, dprot 270 deg, AtomicRotation and
+# AtomicTranslation with equal probability; full dipolar Ewald (alpha
+# 0.25 / A, real-space cutoff 14.42 A, spherical kc 7: 783 k-vectors,
+# tin-foil surroundings).
+DIP_N, DIP_DP, DIP_DPROT = 100, 0.7, 270.0 * math.pi / 180.0
+
+
+def dipole_fluid(seed):
+    from beofaunus_gb300 import workloads
+    from beofaunus_gb300.params import FG_EWALD_DIPOLE_DIPOLE
+    return workloads.dipolar_fluid(n=DIP_N, seed=seed, kc=7.0, terms=FG_EWALD_DIPOLE_DIPOLE, quirk=0)
+
+
+# Cost model of one trial (algorithmic FP64 work, FMA = 2 FLOP; erfc and exp
+# counted as 20 FLOP each), old and new position of the moved particle:
+#   every other particle: distance and LJ, 15 FLOP;
+#   inside rc (the fraction 4/3 pi rc^3 / V of pairs): erfc, exp, sqrt and
+#     the T1/T2 dipole-dipole terms, 80 FLOP more;
+#   per k-vector: two three-factor phase products (24), k.mu twice (12), the
+#     Q increments (8) and the energy change (12): 56 FLOP.
+DIP_PAIR_FLOP, DIP_NEAR_FLOP, DIP_K_FLOP = 15, 80, 56
+
+
+def dip_flop_per_trial(n, K, rc, box):
+    near = min(1.0, 4.0 / 3.0 * math.pi * rc ** 3 / box ** 3)
+    return 2 * (n - 1) * (DIP_PAIR_FLOP + near * DIP_NEAR_FLOP) + K * DIP_K_FLOP
+
+
+def fp64_gemm_tflops(torch, dev):
+    """Measured FP64 peak: cuBLAS DGEMM 4096^3, best of 5."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best
+
+
+def run_dipoles(args, rank, world):
+    from beofaunus_gb300.gpu import DipoleSystem, dip_draw_stream, dip_run_many
+    torch, dev, local, sms = gpu_setup(args)
+    B = args.systems or 4 * sms
+    T = args.trials or 2000
+    steps, warm = args.steps, args.warmup
+    with mp.get_context("spawn").Pool(min(B, os.cpu_count() or 1)) as pool:
+        data = pool.map(dipole_fluid, [21 + rank * 1000003 + b for b in range(B)])
+    systems = [DipoleSystem(p, xyz, mu, mus, ids, charges=q) for (p, xyz, mu, mus, ids, q) in data]
+    p0 = data[0][0]
+    K = systems[0].num_kvectors
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def draws(seed, b):
+        return dip_draw_stream(seed * 1000 + b, DIP_N, T, 0.5, DIP_DP, DIP_DPROT)
+
+    def step(seed):
+        for b, s_ in enumerate(systems):
+            s_.stream_upload(draws(seed, b))
+        flush.fill_(seed & 0xFF)
+        torch.cuda.synchronize()
+        return dip_run_many(systems)[1]
+
+    for s_ in range(warm):
+        step(10 + s_)
+    clocks = ClockSampler(local)
+    clocks.start()
+    stats = [step(1000 + s_) for s_ in range(steps)]
+    clk = clocks.stop()
+    ms = sum(st["device_ms"] for st in stats)
+    trials = sum(st["trials"] for st in stats)
+    value = trials / (ms / 1e3)
+    acc = sum(st["accepted"] for st in stats) / trials
+    # e2e: the reference's draws made on the host and uploaded inside the timed region
+    e2e_s, e2e_t = 0.0, 0
+    for s_ in range(steps):
+        host = [draws(50000 + s_, b) for b in range(B)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b, s2 in enumerate(systems):
+            s2.stream_upload(host[b])
+        _, tot = dip_run_many(systems)
+        e2e_s += time.perf_counter() - t0
+        e2e_t += tot["trials"]
+    # one system alone: the single-chain latency
+    one = systems[0]
+    one.sweep(dip_draw_stream(99, DIP_N, 2000, 0.5, DIP_DP, DIP_DPROT), log=False)
+    r = one.sweep(dip_draw_stream(98, DIP_N, 4000, 0.5, DIP_DP, DIP_DPROT), log=False)
+    single = {"value": r["trials"] / (r["device_ms"] / 1e3), "unit": UNIT,
+              "us_per_trial": r["device_ms"] * 1e3 / r["trials"]}
+    # plain per-trial API: fg_dip_trial_du + fg_dip_commit per trial
+    import numpy as np
+    xyz, mu = one.state()
+    st = dip_draw_stream(77, DIP_N, 300, 0.5, DIP_DP, DIP_DPROT)
+    L = p0.box[0]
+    t0 = time.perf_counter()
+    for k in range(300):
+        i = int(st["idx"][k])
+        nx, nm = xyz[i].copy(), mu[i].copy()
+        if st["kind"][k] == 1:
+            ax, ang = st["axis"][k], st["angle"][k]
+            Km = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+            nm = (np.eye(3) + np.sin(ang) * Km + (1 - np.cos(ang)) * Km @ Km) @ nm
+        else:
+            nx = nx + st["disp"][k]
+            nx -= L * np.round(nx / L)
+        du = one.trial_du(i, nx, nm)
+        a = not (st["u"][k] > np.exp(-du))
+        one.commit(a)
+        if a:
+            xyz[i], mu[i] = nx, nm
+    plain = 300 / (time.perf_counter() - t0)
+    flop = dip_flop_per_trial(DIP_N, K, p0.ewald_cutoff, L)
+    achieved = flop * value / 1e12
+    fp64_peak = fp64_gemm_tflops(torch, dev)
+    cfg = {"workload": WORKLOAD_NAMES["dipoles"], "systems": B, "particles_per_system": DIP_N, "box_A": L,
+           "dipole_eA": 1.652, "sigma_A": 2.8863, "lj_eps_kT": float(p0.type_eps[0]), "bjerrum_A": p0.bjerrum,
+           "ewald_alpha": p0.ewald_alpha, "ewald_cutoff_A": p0.ewald_cutoff, "ewald_cutoff_k": p0.ewald_cutoff_k,
+           "k_vectors": K, "terms": "dipole-dipole (real + reciprocal + surface + self)",
+           "dp_A": DIP_DP, "dprot_rad": DIP_DPROT, "p_rotate": 0.5, "trials_per_system_per_step": T,
+           "acceptance": acc, "l2": "L2 flushed (256 MiB write) between timed steps"}
+    out = base_line(value, steps, warm, ms / steps, world, cfg, "f64",
+                    "synthetic (seeded dipolar fluid, reference mt19937 AtomicRotation/AtomicTranslation draws)")
+    out.update({"e2e": {"value": e2e_t / e2e_s, "unit": UNIT, "h2d_bytes_per_step": B * T * 72,
+                        "d2h_bytes_per_step": B * 2 * 96},
+                "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
+                "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                             "frac": achieved / fp64_peak, "traffic": None,
+                             "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (best of 5)",
+                             "flop_per_trial": flop,
+                             "note": "whole-launch rate over all systems; each system is one sequential chain"},
+                "single_system": single, "plain_per_trial_api": {"value": plain, "unit": UNIT},
+                "batched_over_plain": value / plain, "clocks": clk})
+    for s_ in systems:
+        s_.close()
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds, *cpu_kinds("dipoles"))
+    if rank == 0:
+        print(json.dumps(out))
+
+
 # ----------------------------------------------------------------- serving
 def _serving_job(args):
     n, temp, seed = args
@@ -939,7 +1096,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rpm16k", choices=["rpm16k", "rpm800", "pt64", "molecules", "serving"])
+    ap.add_argument("--workload", default="rpm16k", choices=["rpm16k", "rpm800", "pt64", "molecules", "serving",
+                                                                 "dipoles"])
     ap.add_argument("--systems", type=int, default=0, help="systems per GPU (default: SM count, or SMs / cluster)")
     ap.add_argument("--trials", type=int, default=0, help="trials per system per step (default: one sweep)")
     ap.add_argument("--cluster", type=int, default=4, help="molecules: CTAs per system")
@@ -969,7 +1127,8 @@ def main():
             import torch.distributed as dist
             import torch
             dist.init_process_group("nccl", device_id=torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
-        {"rpm800": run_rpm800, "pt64": run_pt, "molecules": run_molecules, "serving": run_serving}[args.workload](
+        {"rpm800": run_rpm800, "pt64": run_pt, "molecules": run_molecules, "serving": run_serving,
+         "dipoles": run_dipoles}[args.workload](
             args, rank, world)
 
 

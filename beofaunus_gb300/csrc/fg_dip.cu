@@ -105,6 +105,13 @@ __device__ __forceinline__ double2 kphase(const double2 *tab, int stride, char4 
     return cmul(cmul(ex, ey), ez);
 }
 
+// Dynamic shared memory of the sweep kernel: e^{i (ny k_y y + nz k_z z)} of
+// the moved particle for ny, nz in [-kcc, kcc], old then new; a k-vector's
+// phase is then one product with the x-axis entry.
+__host__ __device__ constexpr size_t dip_yz_bytes(int kcc) {
+    return (size_t)2 * (2 * kcc + 1) * (2 * kcc + 1) * sizeof(double2);
+}
+
 // cos, sin of 2 pi n X / 2^64: the phase reduced exactly in integers
 __device__ __forceinline__ double2 axis_entry(int n, int64_t X) {
     const int64_t ph = (int64_t)((uint64_t)(int64_t)n * (uint64_t)X);
@@ -120,18 +127,22 @@ __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry,
                                          const double *mb, double &real, double &lj) {
     const double r2 = rx * rx + ry * ry + rz * rz;
     const int tt = ta * d.nt + tb;
-    double x = d.s2[tt] / r2;   // LennardJonesMixed (potentials.h:2036-2040)
+    const bool near = d.any_term && r2 <= d.rc2;
+    // one sqrt and one division per pair; every 1/r^n below is a product of them
+    const double r1 = near ? sqrt(r2) : 1.0;
+    const double ir1 = near ? 1.0 / r1 : 0.0;
+    const double ir2 = near ? ir1 * ir1 : 1.0 / r2;
+    double x = d.s2[tt] * ir2;   // LennardJonesMixed (potentials.h:2036-2040)
     x = x * x * x;
     lj = d.eps4[tt] * (x * x - x);
     real = 0.0;
-    if (!d.any_term || r2 > d.rc2) return;
-    const double r1 = sqrt(r2);
+    if (!near) return;
     const double ar = d.alpha * r1;
     const double ec = erfc(ar);
     if (d.quirk || d.ii) {
         double t;
         if (d.small_kappa) {
-            t = ec / r1;   // erfc(ar +- kappa / 2 alpha) e^{+-kappa r} round to erfc(ar) here
+            t = ec * ir1;   // erfc(ar +- kappa / 2 alpha) e^{+-kappa r} round to erfc(ar) here
         } else {
             const double h = d.kappa / 2.0 / d.alpha;
             t = (erfc(ar + h) * exp(d.kappa * r1) + erfc(ar - h) * exp(-d.kappa * r1)) / (2.0 * r1);
@@ -141,7 +152,7 @@ __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry,
     if (d.quirk || !(d.id || d.dd)) return;
     const double ex = exp(-d.alpha2 * r2);
     const double T1f = r1 * d.t1c * ex + ec;   // ewald.h:46
-    const double T1 = T1f / r1 / r2;
+    const double T1 = T1f * ir1 * ir2;
     double Ed = 0.0;
     if (d.id) {
         Ed += qa * (rx * mb[0] + ry * mb[1] + rz * mb[2]) * mbs * T1;
@@ -150,8 +161,8 @@ __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry,
     if (d.dd) {
         const double T2f = 3.0 * (T1f + d.t2c * r1 * r1 * r1 * ex);   // ewald.h:47
         const double t3 = -(mb[0] * ma[0] + mb[1] * ma[1] + mb[2] * ma[2]) * T1;
-        const double t5 = (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (ma[0] * rx + ma[1] * ry + ma[2] * rz) * T2f / r2 /
-                          r2 / r1;
+        const double t5 =
+            (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (ma[0] * rx + ma[1] * ry + ma[2] * rz) * T2f * (ir2 * ir2 * ir1);
         Ed += -(t5 + t3) * mbs * mas;
     }
     real += d.lB * Ed;
@@ -252,10 +263,12 @@ __global__ void __launch_bounds__(kDipMaxThreads) dip_build_kernel(const DipDesc
 // mode 0: run the staged stream [cursor, n_trials) with Metropolis decisions;
 // mode 1: evaluate trials[0] (explicit) and keep it pending;
 // mode 2: apply the pending trials[0] as accepted.
-__global__ void __launch_bounds__(kDipMaxThreads) dip_sweep_kernel(const DipDesc *descs, int mode) {
+__global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipDesc *descs, int mode) {
     const DipDesc &d = descs[blockIdx.x];
     __shared__ DipShared S;
+    extern __shared__ double2 eyz[];
     const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
+    const int W = 2 * d.kcc + 1, W2 = W * W;
     if (T > kDipMaxThreads || (T & 31)) {
         if (tid == 0) atomicOr(&d.sc->error, kDipErrLaunch);
         return;
@@ -321,6 +334,13 @@ __global__ void __launch_bounds__(kDipMaxThreads) dip_sweep_kernel(const DipDesc
                 S.tab[w][r] = axis_entry(n, w ? S.pn[a] : S.po[a]);
             }
             __syncthreads();
+            for (int e = tid; e < 2 * W2; e += T) {
+                const int w = e >= W2 ? 1 : 0, r = e - w * W2, ny = r / W - d.kcc, nz = r - (ny + d.kcc) * W - d.kcc;
+                const double2 ey = conj_if(S.tab[w][st + (ny < 0 ? -ny : ny)], ny < 0);
+                const double2 ez = conj_if(S.tab[w][2 * st + (nz < 0 ? -nz : nz)], nz < 0);
+                eyz[e] = cmul(ey, ez);
+            }
+            __syncthreads();
             const int i = S.idx, ta = S.ta;
             const double qa = S.qa, mas = S.mas;
             const double muo[3] = {S.muo[0], S.muo[1], S.muo[2]}, mun[3] = {S.mun[0], S.mun[1], S.mun[2]};
@@ -351,7 +371,8 @@ __global__ void __launch_bounds__(kDipMaxThreads) dip_sweep_kernel(const DipDesc
             const double qeff = S.qeff;
             for (int k = tid; k < d.K; k += T) {
                 const char4 n = d.kn[k];
-                const double2 eo = kphase(S.tab[0], st, n), en = kphase(S.tab[1], st, n);
+                const int yz = (n.y + d.kcc) * W + n.z + d.kcc;
+                const double2 eo = cmul(S.tab[0][n.x], eyz[yz]), en = cmul(S.tab[1][n.x], eyz[W2 + yz]);
                 double2 dci = make_double2(0.0, 0.0), dcd = make_double2(0.0, 0.0);
                 if (d.ion_q) dci = make_double2(qeff * (en.x - eo.x), qeff * (en.y - eo.y));
                 if (d.dip_q) {
@@ -652,8 +673,11 @@ int dip_total(fg_dipsys *h, double *comp) {
     return FG_OK;
 }
 
-int dip_launch(fg_dipsys *h0, const fgd::DipDesc *descs, int n, int mode, cudaStream_t st) {
-    fgd::dip_sweep_kernel<<<n, h0->threads, 0, st>>>(descs, mode);
+int dip_launch(fg_dipsys *h0, const fgd::DipDesc *descs, int n, int mode, cudaStream_t st, int max_kcc) {
+    const size_t smem = fgd::dip_yz_bytes(max_kcc);
+    CK(cudaFuncSetAttribute((const void *)fgd::dip_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)smem));
+    fgd::dip_sweep_kernel<<<n, h0->threads, smem, st>>>(descs, mode);
     CK(cudaGetLastError());
     return FG_OK;
 }
@@ -662,8 +686,10 @@ int dip_run(fg_dipsys *const *sys, int n, fg_sweep_stats *per, fg_sweep_stats *t
     if (!sys || n < 1) return fail(FG_ERR_INVALID, "bad argument");
     fg_dipsys *h0 = sys[0];
     int64_t maxn = 0;
+    int max_kcc = 0;
     for (int i = 0; i < n; i++) {
         fg_dipsys *h = sys[i];
+        if (h) max_kcc = std::max(max_kcc, h->kcc);
         if (!h || !h->state_set) return fail(FG_ERR_STATE, "system %d has no state", i);
         if (h->pending) return fail(FG_ERR_STATE, "system %d has a pending trial: commit it first", i);
         if (h->device != h0->device) return fail(FG_ERR_INVALID, "systems must share the device");
@@ -693,7 +719,7 @@ int dip_run(fg_dipsys *const *sys, int n, fg_sweep_stats *per, fg_sweep_stats *t
             e = std::min(sys[i]->n_stream, (c + 1) * kChunk);
             CK(cudaMemcpyAsync(&sys[i]->sc->n_trials, &e, sizeof(int64_t), cudaMemcpyHostToDevice, st));
         }
-        rc = dip_launch(h0, descs, n, 0, st);
+        rc = dip_launch(h0, descs, n, 0, st, max_kcc);
     }
     CK(cudaEventRecord(h0->ev1, st));
     CK(cudaEventSynchronize(h0->ev1));
@@ -1029,7 +1055,7 @@ int fg_dip_trial_du(fg_dipsys *h, int32_t i, const double *new_xyz, const double
     int rc = dip_ensure_trials(h, 1, false);
     if (rc) return rc;
     CK(cudaMemcpyAsync(h->trials, &t, sizeof(t), cudaMemcpyHostToDevice, h->stream));
-    rc = dip_launch(h, h->d_desc, 1, 1, h->stream);
+    rc = dip_launch(h, h->d_desc, 1, 1, h->stream, h->kcc);
     if (rc) return rc;
     fgd::DipScalars s;
     rc = dip_read_scalars(h, s);
@@ -1045,7 +1071,7 @@ int fg_dip_commit(fg_dipsys *h, int32_t accepted) {
     if (!h->pending) return fail(FG_ERR_STATE, "no pending trial");
     h->pending = false;
     if (!accepted) return FG_OK;
-    int rc = dip_launch(h, h->d_desc, 1, 2, h->stream);
+    int rc = dip_launch(h, h->d_desc, 1, 2, h->stream, h->kcc);
     if (rc) return rc;
     CK(cudaStreamSynchronize(h->stream));
     return FG_OK;
