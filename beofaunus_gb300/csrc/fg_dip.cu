@@ -168,6 +168,30 @@ __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry,
     real += d.lB * Ed;
 }
 
+// Change of the pair energy when only a's dipole turns (mu_a -> mu_a + dmu,
+// the positions fixed): the terms linear in mu_a with dmu in its place; LJ,
+// ion-ion and the q_a mu_b term do not change.
+__device__ __forceinline__ double dip_turn(const DipDesc &d, double rx, double ry, double rz, double mas,
+                                           const double *dmu, double qb, double mbs, const double *mb) {
+    const double r2 = rx * rx + ry * ry + rz * rz;
+    if (d.quirk || !(d.id || d.dd) || r2 > d.rc2) return 0.0;
+    const double r1 = sqrt(r2);
+    const double ir1 = 1.0 / r1, ir2 = ir1 * ir1;
+    const double ex = exp(-d.alpha2 * r2);
+    const double T1f = r1 * d.t1c * ex + erfc(d.alpha * r1);
+    const double T1 = T1f * ir1 * ir2;
+    double Ed = 0.0;
+    if (d.id) Ed -= qb * (rx * dmu[0] + ry * dmu[1] + rz * dmu[2]) * mas * T1;
+    if (d.dd) {
+        const double T2f = 3.0 * (T1f + d.t2c * r1 * r1 * r1 * ex);
+        const double t3 = -(mb[0] * dmu[0] + mb[1] * dmu[1] + mb[2] * dmu[2]) * T1;
+        const double t5 =
+            (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (dmu[0] * rx + dmu[1] * ry + dmu[2] * rz) * T2f * (ir2 * ir2 * ir1);
+        Ed += -(t5 + t3) * mbs * mas;
+    }
+    return d.lB * Ed;
+}
+
 // Block sum in a fixed order (result valid in thread 0).
 __device__ __forceinline__ double block_sum(double v, double *red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -201,7 +225,7 @@ struct DipShared {
     double ro[3], rn[3];
     double qa, qeff, mas, u, du, pend;
     double M[6];
-    int idx, ta, kind, accept, rebuild;
+    int idx, ta, kind, accept, rebuild, fixed;
     double red[kDipMaxThreads / 32];
     double2 tab[2][3 * (kDipMaxKcc + 1)];   // moved particle, old and new
     double2 rtab[3 * (kDipMaxKcc + 1)];     // rebuild: one particle at a time
@@ -325,16 +349,20 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 S.ro[a] = (double)S.po[a] * d.s64[a];
                 S.rn[a] = (double)S.pn[a] * d.s64[a];
             }
+            S.fixed = (S.pn[0] == S.po[0] && S.pn[1] == S.po[1] && S.pn[2] == S.po[2]) ? 1 : 0;
         }
         __syncthreads();
         if (mode != 2) {
-            // ---- axis tables of the moved particle, old (w = 0) and new (w = 1)
-            for (int e = tid; e < 6 * st; e += T) {
+            // ---- axis tables of the moved particle, old (w = 0) and new (w = 1;
+            // a rotation keeps the position: old only)
+            const bool fixed = S.fixed;
+            const int nw = fixed ? 1 : 2;
+            for (int e = tid; e < nw * 3 * st; e += T) {
                 const int w = e / (3 * st), r = e - w * 3 * st, a = r / st, n = r - a * st;
                 S.tab[w][r] = axis_entry(n, w ? S.pn[a] : S.po[a]);
             }
             __syncthreads();
-            for (int e = tid; e < 2 * W2; e += T) {
+            for (int e = tid; e < nw * W2; e += T) {
                 const int w = e >= W2 ? 1 : 0, r = e - w * W2, ny = r / W - d.kcc, nz = r - (ny + d.kcc) * W - d.kcc;
                 const double2 ey = conj_if(S.tab[w][st + (ny < 0 ? -ny : ny)], ny < 0);
                 const double2 ez = conj_if(S.tab[w][2 * st + (nz < 0 ? -nz : nz)], nz < 0);
@@ -346,6 +374,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             const double muo[3] = {S.muo[0], S.muo[1], S.muo[2]}, mun[3] = {S.mun[0], S.mun[1], S.mun[2]};
             double acc = 0.0;
             // ---- real space: the moved particle against every other one
+            const double dmu[3] = {mun[0] - muo[0], mun[1] - muo[1], mun[2] - muo[2]};
             for (int j = tid; j < d.N; j += T) {
                 if (j == i) continue;
                 int64_t pj[3];
@@ -355,12 +384,15 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                     mb[a] = d.mu[3 * j + a];
                 }
                 const double qb = d.q[j], mbs = d.mus[j];
-                const int tb = d.type[j];
-                double ro[3], rn[3];
-                for (int a = 0; a < 3; a++) {
-                    ro[a] = (double)(int64_t)((uint64_t)S.po[a] - (uint64_t)pj[a]) * d.s64[a];
-                    rn[a] = (double)(int64_t)((uint64_t)S.pn[a] - (uint64_t)pj[a]) * d.s64[a];
+                double ro[3];
+                for (int a = 0; a < 3; a++) ro[a] = (double)(int64_t)((uint64_t)S.po[a] - (uint64_t)pj[a]) * d.s64[a];
+                if (fixed) {
+                    acc += dip_turn(d, ro[0], ro[1], ro[2], mas, dmu, qb, mbs, mb);
+                    continue;
                 }
+                const int tb = d.type[j];
+                double rn[3];
+                for (int a = 0; a < 3; a++) rn[a] = (double)(int64_t)((uint64_t)S.pn[a] - (uint64_t)pj[a]) * d.s64[a];
                 double eo, lo, en, ln;
                 dip_pair(d, ro[0], ro[1], ro[2], qa, ta, mas, muo, qb, tb, mbs, mb, eo, lo);
                 dip_pair(d, rn[0], rn[1], rn[2], qa, ta, mas, mun, qb, tb, mbs, mb, en, ln);
@@ -372,14 +404,23 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             for (int k = tid; k < d.K; k += T) {
                 const char4 n = d.kn[k];
                 const int yz = (n.y + d.kcc) * W + n.z + d.kcc;
-                const double2 eo = cmul(S.tab[0][n.x], eyz[yz]), en = cmul(S.tab[1][n.x], eyz[W2 + yz]);
+                const double2 eo = cmul(S.tab[0][n.x], eyz[yz]);
+                const double kx = n.x * d.tpl[0], ky = n.y * d.tpl[1], kz = n.z * d.tpl[2];
                 double2 dci = make_double2(0.0, 0.0), dcd = make_double2(0.0, 0.0);
-                if (d.ion_q) dci = make_double2(qeff * (en.x - eo.x), qeff * (en.y - eo.y));
-                if (d.dip_q) {
-                    const double kx = n.x * d.tpl[0], ky = n.y * d.tpl[1], kz = n.z * d.tpl[2];
-                    const double kmo = (kx * muo[0] + ky * muo[1] + kz * muo[2]) * mas;
-                    const double kmn = (kx * mun[0] + ky * mun[1] + kz * mun[2]) * mas;
-                    dcd = make_double2(-kmn * en.y + kmo * eo.y, kmn * en.x - kmo * eo.x);
+                if (fixed) {
+                    // the dipole turns in place: dQ_dip = i (k.dmu) mu_s e^{ik.r}
+                    if (d.dip_q) {
+                        const double kmd = (kx * dmu[0] + ky * dmu[1] + kz * dmu[2]) * mas;
+                        dcd = make_double2(-kmd * eo.y, kmd * eo.x);
+                    }
+                } else {
+                    const double2 en = cmul(S.tab[1][n.x], eyz[W2 + yz]);
+                    if (d.ion_q) dci = make_double2(qeff * (en.x - eo.x), qeff * (en.y - eo.y));
+                    if (d.dip_q) {
+                        const double kmo = (kx * muo[0] + ky * muo[1] + kz * muo[2]) * mas;
+                        const double kmn = (kx * mun[0] + ky * mun[1] + kz * mun[2]) * mas;
+                        dcd = make_double2(-kmn * en.y + kmo * eo.y, kmn * en.x - kmo * eo.x);
+                    }
                 }
                 const double2 Qi = d.qi[k], Qd = d.qd[k];
                 double s = 0.0;
