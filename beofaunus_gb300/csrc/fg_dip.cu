@@ -27,11 +27,15 @@
 // order, thread 0 decides, and on acceptance the threads that computed a
 // k-vector's Q increments add them to Q(k).
 //
-// Precision. Everything on this path is FP64: the per-trial dU must match the
-// FP64 oracle to 1e-9 kT at Bjerrum lengths of hundreds of Angstrom, where
-// single dipole pairs carry tens of kT. Positions are 64-bit fixed point
-// (X = x/L 2^64): minimum image is the wrapped integer difference and every
-// translation is exact.
+// Precision. The per-trial dU must match the FP64 oracle to 1e-9 kT at Bjerrum
+// lengths of hundreds of Angstrom, where single dipole pairs carry tens of kT.
+// Pair terms, phase tables, surface sums and decisions are FP64. The k-space
+// loop, K terms per trial, runs in double-float (df: an unevaluated sum of
+// two floats, ~48 significant bits) on the FP32 pipe, which on this part
+// issues far more operations per clock than the FP64 pipe: Q(k), its
+// increments, A_k, the phases and k.mu are all df. Positions are 64-bit fixed
+// point (X = x/L 2^64): minimum image is the wrapped integer difference and
+// every translation is exact.
 namespace fgd {
 
 constexpr int kDipMaxThreads = 256;
@@ -83,8 +87,10 @@ struct DipDesc {
     int32_t *type;        // [N]
     char4 *kn;            // [K] n-vector of k
     double *ak;           // [K] A_k with the half-space factor
-    double2 *qi, *qd;     // [K] Q_ion, Q_dip
-    double2 *dqi, *dqd;   // [K] increments of the trial in flight
+    double2 *qi, *qd;     // [K] FP64 accumulators of a rebuild
+    float4 *fqi, *fqd;    // [K] Q_ion, Q_dip as df complex {re.hi, re.lo, im.hi, im.lo}
+    float4 *dqi, *dqd;    // [K] increments of the trial in flight (df complex)
+    float2 *akf;          // [K] A_k as df
     DipTrial *trials;
     double *log_du;       // [trials] or null
     uint8_t *log_acc;
@@ -95,6 +101,53 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ double2 conj_if(double2 a, bool c) { return c ? make_double2(a.x, -a.y) : a; }
+
+// ---- double-float arithmetic (FP32 pipe)
+using fg::df;
+using fg::fast_two_sum;
+__device__ __forceinline__ df dsplit(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ double dval(df a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ df dneg(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df dadd(df a, df b) { return fg::df_add(a, b); }
+__device__ __forceinline__ df dsub(df a, df b) { return fg::df_add(a, dneg(b)); }
+__device__ __forceinline__ df dtwice(df a) { return {2.0f * a.hi, 2.0f * a.lo}; }
+// a * b: the exact product of the high words by FMA plus the cross terms
+__device__ __forceinline__ df dmul(df a, df b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+// a * n for a small integer n (exact in float)
+__device__ __forceinline__ df dmul_i(df a, int n) {
+    const float f = (float)n;
+    const float p = __fmul_rn(a.hi, f);
+    float e = __fmaf_rn(a.hi, f, -p);
+    e = __fmaf_rn(a.lo, f, e);
+    return fast_two_sum(p, e);
+}
+struct dc {
+    df re, im;
+};
+__device__ __forceinline__ dc dc_load(float4 v) { return {{v.x, v.y}, {v.z, v.w}}; }
+__device__ __forceinline__ float4 dc_pack(dc a) { return make_float4(a.re.hi, a.re.lo, a.im.hi, a.im.lo); }
+__device__ __forceinline__ dc dc_split(double2 a) { return {dsplit(a.x), dsplit(a.y)}; }
+__device__ __forceinline__ double2 dc_val(float4 v) { return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w); }
+__device__ __forceinline__ dc dc_mul(dc a, dc b) {
+    return {dsub(dmul(a.re, b.re), dmul(a.im, b.im)), dadd(dmul(a.re, b.im), dmul(a.im, b.re))};
+}
+__device__ __forceinline__ dc dc_conj_if(dc a, bool c) { return c ? dc{a.re, dneg(a.im)} : a; }
+// Re(a conj(b)) and Re(a b)
+__device__ __forceinline__ df dc_dot(dc a, dc b) { return dadd(dmul(a.re, b.re), dmul(a.im, b.im)); }
+__device__ __forceinline__ df dc_rprod(dc a, dc b) { return dsub(dmul(a.re, b.re), dmul(a.im, b.im)); }
+// n . m for a small integer vector n and df m
+__device__ __forceinline__ df dkdot(char4 n, const df *m) {
+    return dadd(dadd(dmul_i(m[0], n.x), dmul_i(m[1], n.y)), dmul_i(m[2], n.z));
+}
 
 // e^{i k.r} from one particle's axis tables (tab[axis * (kcc+1) + |n|]);
 // negative components take the conjugate
@@ -227,7 +280,9 @@ struct DipShared {
     double M[6];
     int idx, ta, kind, accept, rebuild, fixed;
     double red[kDipMaxThreads / 32];
-    double2 tab[2][3 * (kDipMaxKcc + 1)];   // moved particle, old and new
+    float4 tab[2][3 * (kDipMaxKcc + 1)];    // moved particle, old and new (df complex)
+    df mo[3], mn[3], md[3];                 // 2 pi / L_a mu_s times mu_old, mu_new, mu_new - mu_old
+    df qeffd;
     double2 rtab[3 * (kDipMaxKcc + 1)];     // rebuild: one particle at a time
     double rq, rmu[3];
 };
@@ -238,7 +293,7 @@ __device__ void dip_rebuild(const DipDesc &d, DipShared &S, double &before, doub
     const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
     double e = 0.0;
     for (int k = tid; k < d.K; k += T) {
-        e += d.ak[k] * q2(d, d.qi[k], d.qd[k]);
+        e += d.ak[k] * q2(d, dc_val(d.fqi[k]), dc_val(d.fqd[k]));
         d.qi[k] = make_double2(0.0, 0.0);
         d.qd[k] = make_double2(0.0, 0.0);
     }
@@ -273,12 +328,17 @@ __device__ void dip_rebuild(const DipDesc &d, DipShared &S, double &before, doub
         }
     }
     e = 0.0;
-    for (int k = tid; k < d.K; k += T) e += d.ak[k] * q2(d, d.qi[k], d.qd[k]);
+    for (int k = tid; k < d.K; k += T) {
+        const double2 a = d.qi[k], b = d.qd[k];
+        e += d.ak[k] * q2(d, a, b);
+        d.fqi[k] = dc_pack(dc_split(a));
+        d.fqd[k] = dc_pack(dc_split(b));
+    }
     after = block_sum(e, S.red) * d.recip_c;
 }
 
 // Q(k) of the uploaded state (setSpace -> setGeometry, ewald.h:731-756)
-__global__ void __launch_bounds__(kDipMaxThreads) dip_build_kernel(const DipDesc *dp) {
+__global__ void __launch_bounds__(kDipMaxThreads, 1) dip_build_kernel(const DipDesc *dp) {
     __shared__ DipShared S;
     double before, after;
     dip_rebuild(*dp, S, before, after);
@@ -290,7 +350,7 @@ __global__ void __launch_bounds__(kDipMaxThreads) dip_build_kernel(const DipDesc
 __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipDesc *descs, int mode) {
     const DipDesc &d = descs[blockIdx.x];
     __shared__ DipShared S;
-    extern __shared__ double2 eyz[];
+    extern __shared__ float4 eyz[];   // df complex
     const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
     const int W = 2 * d.kcc + 1, W2 = W * W;
     if (T > kDipMaxThreads || (T & 31)) {
@@ -359,14 +419,23 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             const int nw = fixed ? 1 : 2;
             for (int e = tid; e < nw * 3 * st; e += T) {
                 const int w = e / (3 * st), r = e - w * 3 * st, a = r / st, n = r - a * st;
-                S.tab[w][r] = axis_entry(n, w ? S.pn[a] : S.po[a]);
+                S.tab[w][r] = dc_pack(dc_split(axis_entry(n, w ? S.pn[a] : S.po[a])));
+            }
+            if (tid == 0) {
+                for (int a = 0; a < 3; a++) {
+                    const double f = d.tpl[a] * S.mas;
+                    S.mo[a] = dsplit(S.muo[a] * f);
+                    S.mn[a] = dsplit(S.mun[a] * f);
+                    S.md[a] = dsplit((S.mun[a] - S.muo[a]) * f);
+                }
+                S.qeffd = dsplit(S.qeff);
             }
             __syncthreads();
             for (int e = tid; e < nw * W2; e += T) {
                 const int w = e >= W2 ? 1 : 0, r = e - w * W2, ny = r / W - d.kcc, nz = r - (ny + d.kcc) * W - d.kcc;
-                const double2 ey = conj_if(S.tab[w][st + (ny < 0 ? -ny : ny)], ny < 0);
-                const double2 ez = conj_if(S.tab[w][2 * st + (nz < 0 ? -nz : nz)], nz < 0);
-                eyz[e] = cmul(ey, ez);
+                const dc ey = dc_conj_if(dc_load(S.tab[w][st + (ny < 0 ? -ny : ny)]), ny < 0);
+                const dc ez = dc_conj_if(dc_load(S.tab[w][2 * st + (nz < 0 ? -nz : nz)]), nz < 0);
+                eyz[e] = dc_pack(dc_mul(ey, ez));
             }
             __syncthreads();
             const int i = S.idx, ta = S.ta;
@@ -398,47 +467,52 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 dip_pair(d, rn[0], rn[1], rn[2], qa, ta, mas, mun, qb, tb, mbs, mb, en, ln);
                 acc += (en - eo) + (ln - lo);
             }
-            // ---- k space: increments of Q_ion and Q_dip and the energy change
-            double ek = 0.0;
-            const double qeff = S.qeff;
+            // ---- k space (df): increments of Q_ion and Q_dip and the energy change
+            df ek = {0.0f, 0.0f};
+            const df qeffd = S.qeffd;
+            const df mo[3] = {S.mo[0], S.mo[1], S.mo[2]}, mn[3] = {S.mn[0], S.mn[1], S.mn[2]},
+                     md[3] = {S.md[0], S.md[1], S.md[2]};
             for (int k = tid; k < d.K; k += T) {
                 const char4 n = d.kn[k];
                 const int yz = (n.y + d.kcc) * W + n.z + d.kcc;
-                const double2 eo = cmul(S.tab[0][n.x], eyz[yz]);
-                const double kx = n.x * d.tpl[0], ky = n.y * d.tpl[1], kz = n.z * d.tpl[2];
-                double2 dci = make_double2(0.0, 0.0), dcd = make_double2(0.0, 0.0);
+                const dc eo = dc_mul(dc_load(S.tab[0][n.x]), dc_load(eyz[yz]));
+                dc dci = {{0.0f, 0.0f}, {0.0f, 0.0f}}, dcd = dci;
                 if (fixed) {
                     // the dipole turns in place: dQ_dip = i (k.dmu) mu_s e^{ik.r}
                     if (d.dip_q) {
-                        const double kmd = (kx * dmu[0] + ky * dmu[1] + kz * dmu[2]) * mas;
-                        dcd = make_double2(-kmd * eo.y, kmd * eo.x);
+                        const df kmd = dkdot(n, md);
+                        dcd = {dneg(dmul(kmd, eo.im)), dmul(kmd, eo.re)};
                     }
                 } else {
-                    const double2 en = cmul(S.tab[1][n.x], eyz[W2 + yz]);
-                    if (d.ion_q) dci = make_double2(qeff * (en.x - eo.x), qeff * (en.y - eo.y));
+                    const dc en = dc_mul(dc_load(S.tab[1][n.x]), dc_load(eyz[W2 + yz]));
+                    if (d.ion_q) dci = {dmul(qeffd, dsub(en.re, eo.re)), dmul(qeffd, dsub(en.im, eo.im))};
                     if (d.dip_q) {
-                        const double kmo = (kx * muo[0] + ky * muo[1] + kz * muo[2]) * mas;
-                        const double kmn = (kx * mun[0] + ky * mun[1] + kz * mun[2]) * mas;
-                        dcd = make_double2(-kmn * en.y + kmo * eo.y, kmn * en.x - kmo * eo.x);
+                        const df kmo = dkdot(n, mo), kmn = dkdot(n, mn);
+                        dcd = {dsub(dmul(kmo, eo.im), dmul(kmn, en.im)), dsub(dmul(kmn, en.re), dmul(kmo, eo.re))};
                     }
                 }
-                const double2 Qi = d.qi[k], Qd = d.qd[k];
-                double s = 0.0;
-                if (d.ii) s += 2.0 * (Qi.x * dci.x + Qi.y * dci.y) + dci.x * dci.x + dci.y * dci.y;
-                if (d.id) {
-                    if (d.quirk)
-                        s += 2.0 * ((Qi.x * dcd.x - Qi.y * dcd.y) + (dci.x * Qd.x - dci.y * Qd.y) +
-                                    (dci.x * dcd.x - dci.y * dcd.y));
-                    else
-                        s += 2.0 * ((Qi.x * dcd.x + Qi.y * dcd.y) + (dci.x * Qd.x + dci.y * Qd.y) +
-                                    (dci.x * dcd.x + dci.y * dcd.y));
+                df sum = {0.0f, 0.0f};
+                if (d.ii) {
+                    const dc Qi = dc_load(d.fqi[k]);
+                    sum = dadd(dtwice(dc_dot(Qi, dci)), dc_dot(dci, dci));
                 }
-                if (d.dd) s += 2.0 * (Qd.x * dcd.x + Qd.y * dcd.y) + dcd.x * dcd.x + dcd.y * dcd.y;
-                ek += d.ak[k] * s;
-                d.dqi[k] = dci;
-                d.dqd[k] = dcd;
+                if (d.id) {
+                    const dc Qi = dc_load(d.fqi[k]), Qd = dc_load(d.fqd[k]);
+                    if (d.quirk)
+                        sum = dadd(sum, dtwice(dadd(dadd(dc_rprod(Qi, dcd), dc_rprod(dci, Qd)), dc_rprod(dci, dcd))));
+                    else
+                        sum = dadd(sum, dtwice(dadd(dadd(dc_dot(Qi, dcd), dc_dot(dci, Qd)), dc_dot(dci, dcd))));
+                }
+                if (d.dd) {
+                    const dc Qd = dc_load(d.fqd[k]);
+                    sum = dadd(sum, dadd(dtwice(dc_dot(Qd, dcd)), dc_dot(dcd, dcd)));
+                }
+                const float2 a = d.akf[k];
+                ek = dadd(ek, dmul(df{a.x, a.y}, sum));
+                d.dqi[k] = dc_pack(dci);
+                d.dqd[k] = dc_pack(dcd);
             }
-            acc += ek * d.recip_c;
+            acc += dval(ek) * d.recip_c;
             const double sum = block_sum(acc, S.red);
             if (tid == 0) {
                 // surface term: running sums before and after the move
@@ -471,12 +545,12 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         // ---- accepted: Q(k), the particle, the sums
         for (int k = tid; k < d.K; k += T) {
             if (d.ion_q) {
-                const double2 a = d.qi[k], b = d.dqi[k];
-                d.qi[k] = make_double2(a.x + b.x, a.y + b.y);
+                const dc a = dc_load(d.fqi[k]), b = dc_load(d.dqi[k]);
+                d.fqi[k] = dc_pack({dadd(a.re, b.re), dadd(a.im, b.im)});
             }
             if (d.dip_q) {
-                const double2 a = d.qd[k], b = d.dqd[k];
-                d.qd[k] = make_double2(a.x + b.x, a.y + b.y);
+                const dc a = dc_load(d.fqd[k]), b = dc_load(d.dqd[k]);
+                d.fqd[k] = dc_pack({dadd(a.re, b.re), dadd(a.im, b.im)});
             }
         }
         if (tid == 0) {
@@ -559,7 +633,9 @@ struct fg_dipsys {
     double *mu = nullptr, *mus = nullptr, *q = nullptr, *ak = nullptr, *pairs = nullptr;
     int32_t *type = nullptr;
     char4 *kn = nullptr;
-    double2 *qi = nullptr, *qd = nullptr, *dqi = nullptr, *dqd = nullptr;
+    double2 *qi = nullptr, *qd = nullptr;
+    float4 *fqi = nullptr, *fqd = nullptr, *dqi = nullptr, *dqd = nullptr;
+    float2 *akf = nullptr;
     fgd::DipTrial *trials = nullptr;
     int64_t trials_cap = 0;
     double *log_du = nullptr;
@@ -581,7 +657,7 @@ namespace {
 
 void dip_free(fg_dipsys *h) {
     void *ptrs[] = {h->d_desc, h->pos, h->mu, h->mus, h->q, h->ak, h->pairs, h->type, h->kn, h->qi, h->qd,
-                    h->dqi, h->dqd, h->trials, h->log_du, h->log_acc, h->sc};
+                    h->fqi, h->fqd, h->dqi, h->dqd, h->akf, h->trials, h->log_du, h->log_acc, h->sc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -643,11 +719,16 @@ int dip_ensure_trials(fg_dipsys *h, int64_t n, bool log) {
 int dip_host_energies(fg_dipsys *h, const std::vector<double> &xyz, const std::vector<double> &mu, double &rec,
                       double &self, double &surf) {
     const fgd::DipDesc &d = h->desc;
+    std::vector<float4> fi(h->K), fd(h->K);
     std::vector<double2> qi(h->K), qd(h->K);
     if (h->K) {
-        CK(cudaMemcpyAsync(qi.data(), h->qi, h->K * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
-        CK(cudaMemcpyAsync(qd.data(), h->qd, h->K * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(fi.data(), h->fqi, h->K * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(fd.data(), h->fqd, h->K * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
+    }
+    for (int k = 0; k < h->K; k++) {
+        qi[k] = make_double2((double)fi[k].x + (double)fi[k].y, (double)fi[k].z + (double)fi[k].w);
+        qd[k] = make_double2((double)fd[k].x + (double)fd[k].y, (double)fd[k].z + (double)fd[k].w);
     }
     rec = 0.0;
     for (int k = 0; k < h->K; k++) {
@@ -964,8 +1045,11 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     TRY(dip_dmalloc(h, (void **)&h->ak, K * sizeof(double)));
     TRY(dip_dmalloc(h, (void **)&h->qi, K * sizeof(double2)));
     TRY(dip_dmalloc(h, (void **)&h->qd, K * sizeof(double2)));
-    TRY(dip_dmalloc(h, (void **)&h->dqi, K * sizeof(double2)));
-    TRY(dip_dmalloc(h, (void **)&h->dqd, K * sizeof(double2)));
+    TRY(dip_dmalloc(h, (void **)&h->fqi, K * sizeof(float4)));
+    TRY(dip_dmalloc(h, (void **)&h->fqd, K * sizeof(float4)));
+    TRY(dip_dmalloc(h, (void **)&h->dqi, K * sizeof(float4)));
+    TRY(dip_dmalloc(h, (void **)&h->dqd, K * sizeof(float4)));
+    TRY(dip_dmalloc(h, (void **)&h->akf, K * sizeof(float2)));
     TRY(dip_dmalloc(h, (void **)&h->sc, sizeof(fgd::DipScalars)));
     d.pos = h->pos;
     d.mu = h->mu;
@@ -976,12 +1060,19 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     d.ak = h->ak;
     d.qi = h->qi;
     d.qd = h->qd;
+    d.fqi = h->fqi;
+    d.fqd = h->fqd;
     d.dqi = h->dqi;
     d.dqd = h->dqd;
+    d.akf = h->akf;
     d.sc = h->sc;
     if (h->K) {
+        std::vector<float2> akf(h->K);
+        for (int k = 0; k < h->K; k++) akf[k] = split_df(ak[k]);
         if (cudaMemcpyAsync(h->kn, h->kn_h.data(), h->K * sizeof(char4), cudaMemcpyHostToDevice, h->stream) ||
-            cudaMemcpyAsync(h->ak, ak.data(), h->K * sizeof(double), cudaMemcpyHostToDevice, h->stream))
+            cudaMemcpyAsync(h->ak, ak.data(), h->K * sizeof(double), cudaMemcpyHostToDevice, h->stream) ||
+            cudaMemcpyAsync(h->akf, akf.data(), h->K * sizeof(float2), cudaMemcpyHostToDevice, h->stream) ||
+            cudaStreamSynchronize(h->stream))
             return bail(fail(FG_ERR_CUDA, "upload of the k-vectors failed"));
     }
     TRY(dip_ensure_trials(h, 1, false));
