@@ -80,11 +80,17 @@ struct DipDesc {
     double t1c, t2c;      // 2 alpha / sqrt(pi), 4 alpha^3 / (3 sqrt(pi))
     double eff[FG_MAX_TYPES];
     double qeqe[FG_MAX_TYPES * FG_MAX_TYPES], s2[FG_MAX_TYPES * FG_MAX_TYPES], eps4[FG_MAX_TYPES * FG_MAX_TYPES];
+    // far pairs in FP32: beyond rf (rf2f = rf^2) no pair term exceeds the far
+    // bound, so the FP32 rounding of a far pair stays below 1e-10 kT
+    float rf2f, rc2f, alphaf, alpha2f, kappaf, lBf, t1cf, t2cf;
+    float qeqef[FG_MAX_TYPES * FG_MAX_TYPES], s2f[FG_MAX_TYPES * FG_MAX_TYPES], eps4f[FG_MAX_TYPES * FG_MAX_TYPES];
     int64_t *pos;         // [3N] fixed point
     double *mu;           // [3N] dipole unit vectors
     double *mus;          // [N] dipole scalars
     double *q;            // [N] charges
     int32_t *type;        // [N]
+    float4 *pf;           // [N] mu_s mu (x, y, z) and q as floats (far pairs)
+    int32_t *nearq;       // [N + kDipMaxThreads] near-pair queue of the trial in flight
     char4 *kn;            // [K] n-vector of k
     double *ak;           // [K] A_k with the half-space factor
     double2 *qi, *qd;     // [K] FP64 accumulators of a rebuild
@@ -221,6 +227,64 @@ __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry,
     real += d.lB * Ed;
 }
 
+// Far pair (r beyond rf) in FP32: EwaldReal + LJ of a and b, with
+// ma, mb = (mu_s mu, q). Same terms as dip_pair.
+__device__ __forceinline__ float far_pair(const DipDesc &d, float rx, float ry, float rz, int ta, float4 ma, int tb,
+                                          float4 mb) {
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    const int tt = ta * d.nt + tb;
+    const float ir2 = 1.0f / r2;
+    float x = d.s2f[tt] * ir2;
+    x = x * x * x;
+    float e = d.eps4f[tt] * (x * x - x);
+    if (!d.any_term || r2 > d.rc2f) return e;
+    const float r1 = sqrtf(r2), ir1 = 1.0f / r1;
+    const float ar = d.alphaf * r1, ec = erfcf(ar);
+    if (d.quirk || d.ii) {
+        float t;
+        if (d.small_kappa) {
+            t = ec * ir1;
+        } else {
+            const float h = d.kappaf / (2.0f * d.alphaf);
+            t = (erfcf(ar + h) * expf(d.kappaf * r1) + erfcf(ar - h) * expf(-d.kappaf * r1)) * 0.5f * ir1;
+        }
+        e += ma.w * mb.w * t * d.qeqef[tt] * d.lBf;
+    }
+    if (d.quirk || !(d.id || d.dd)) return e;
+    const float ex = expf(-d.alpha2f * r2);
+    const float T1f = r1 * d.t1cf * ex + ec, T1 = T1f * ir1 * ir2;
+    float Ed = 0.0f;
+    if (d.id) Ed += (ma.w * (rx * mb.x + ry * mb.y + rz * mb.z) - mb.w * (rx * ma.x + ry * ma.y + rz * ma.z)) * T1;
+    if (d.dd) {
+        const float T2f = 3.0f * (T1f + d.t2cf * r1 * r1 * r1 * ex);
+        Ed += (ma.x * mb.x + ma.y * mb.y + ma.z * mb.z) * T1 -
+              (mb.x * rx + mb.y * ry + mb.z * rz) * (ma.x * rx + ma.y * ry + ma.z * rz) * T2f * (ir2 * ir2 * ir1);
+    }
+    return e + d.lBf * Ed;
+}
+
+// Far pair when only a's dipole turns by dm (= mu_s dmu), FP32.
+__device__ __forceinline__ float far_turn(const DipDesc &d, float rx, float ry, float rz, float3 dm, float4 mb) {
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    if (d.quirk || !(d.id || d.dd) || r2 > d.rc2f) return 0.0f;
+    const float r1 = sqrtf(r2), ir1 = 1.0f / r1, ir2 = ir1 * ir1;
+    const float ex = expf(-d.alpha2f * r2);
+    const float T1f = r1 * d.t1cf * ex + erfcf(d.alphaf * r1), T1 = T1f * ir1 * ir2;
+    float Ed = 0.0f;
+    if (d.id) Ed -= mb.w * (rx * dm.x + ry * dm.y + rz * dm.z) * T1;
+    if (d.dd) {
+        const float T2f = 3.0f * (T1f + d.t2cf * r1 * r1 * r1 * ex);
+        Ed += (dm.x * mb.x + dm.y * mb.y + dm.z * mb.z) * T1 -
+              (mb.x * rx + mb.y * ry + mb.z * rz) * (dm.x * rx + dm.y * ry + dm.z * rz) * T2f * (ir2 * ir2 * ir1);
+    }
+    return d.lBf * Ed;
+}
+
+// float of the high word of a 64-bit fixed-point difference (units of L / 2^32)
+__device__ __forceinline__ float hi_diff(int64_t a, int64_t b) {
+    return (float)(int32_t)((uint64_t)(a - b) >> 32);
+}
+
 // Change of the pair energy when only a's dipole turns (mu_a -> mu_a + dmu,
 // the positions fixed): the terms linear in mu_a with dmu in its place; LJ,
 // ion-ion and the q_a mu_b term do not change.
@@ -279,6 +343,7 @@ struct DipShared {
     double qa, qeff, mas, u, du, pend;
     double M[6];
     int idx, ta, kind, accept, rebuild, fixed;
+    int qcnt[kDipMaxThreads / 32];
     double red[kDipMaxThreads / 32];
     float4 tab[2][3 * (kDipMaxKcc + 1)];    // moved particle, old and new (df complex)
     df mo[3], mn[3], md[3];                 // 2 pi / L_a mu_s times mu_old, mu_new, mu_new - mu_old
@@ -442,10 +507,58 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             const double qa = S.qa, mas = S.mas;
             const double muo[3] = {S.muo[0], S.muo[1], S.muo[2]}, mun[3] = {S.mun[0], S.mun[1], S.mun[2]};
             double acc = 0.0;
-            // ---- real space: the moved particle against every other one
+            // ---- real space: the moved particle against every other one. Far
+            // pairs (both distances beyond rf) in FP32 where they are found;
+            // near pairs queued per warp in order and evaluated afterwards in
+            // FP64 by consecutive threads, so only the warps they fill run FP64.
             const double dmu[3] = {mun[0] - muo[0], mun[1] - muo[1], mun[2] - muo[2]};
-            for (int j = tid; j < d.N; j += T) {
-                if (j == i) continue;
+            const float4 mao = make_float4((float)(muo[0] * mas), (float)(muo[1] * mas), (float)(muo[2] * mas), (float)qa);
+            const float4 man = make_float4((float)(mun[0] * mas), (float)(mun[1] * mas), (float)(mun[2] * mas), (float)qa);
+            const float3 dmf = make_float3((float)(dmu[0] * mas), (float)(dmu[1] * mas), (float)(dmu[2] * mas));
+            const float sx = (float)(d.L[0] * 2.3283064365386963e-10), sy = (float)(d.L[1] * 2.3283064365386963e-10),
+                        sz = (float)(d.L[2] * 2.3283064365386963e-10);   // L / 2^32
+            const int warp = tid >> 5, lane = tid & 31, iters = (d.N + T - 1) / T;
+            int32_t *wq = d.nearq + warp * iters * 32;
+            int nq = 0;
+            df accf = {0.0f, 0.0f};
+            for (int it = 0; it < iters; it++) {
+                const int j = it * T + tid;
+                bool nearp = false;
+                if (j < d.N && j != i) {
+                    const int64_t pj0 = d.pos[3 * j], pj1 = d.pos[3 * j + 1], pj2 = d.pos[3 * j + 2];
+                    const float ox = hi_diff(S.po[0], pj0) * sx, oy = hi_diff(S.po[1], pj1) * sy,
+                                oz = hi_diff(S.po[2], pj2) * sz;
+                    const float r2o = ox * ox + oy * oy + oz * oz;
+                    if (fixed) {
+                        nearp = r2o < d.rf2f;
+                        if (!nearp) accf = fg::df_add_f(accf, far_turn(d, ox, oy, oz, dmf, d.pf[j]));
+                    } else {
+                        const float nx = hi_diff(S.pn[0], pj0) * sx, ny = hi_diff(S.pn[1], pj1) * sy,
+                                    nz = hi_diff(S.pn[2], pj2) * sz;
+                        nearp = r2o < d.rf2f || nx * nx + ny * ny + nz * nz < d.rf2f;
+                        if (!nearp) {
+                            const float4 mb = d.pf[j];
+                            const int tb = d.type[j];
+                            accf = fg::df_add_f(accf, far_pair(d, nx, ny, nz, ta, man, tb, mb) -
+                                                          far_pair(d, ox, oy, oz, ta, mao, tb, mb));
+                        }
+                    }
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, nearp);
+                if (nearp) wq[nq + __popc(b & ((1u << lane) - 1u))] = j;
+                nq += __popc(b);
+            }
+            if (lane == 0) S.qcnt[warp] = nq;
+            __syncthreads();
+            int total = 0;
+            for (int w = 0; w < (T >> 5); w++) total += S.qcnt[w];
+            for (int e = tid; e < total; e += T) {
+                int w = 0, r = e;
+                while (r >= S.qcnt[w]) {
+                    r -= S.qcnt[w];
+                    w++;
+                }
+                const int j = d.nearq[w * iters * 32 + r];
                 int64_t pj[3];
                 double mb[3];
                 for (int a = 0; a < 3; a++) {
@@ -467,6 +580,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 dip_pair(d, rn[0], rn[1], rn[2], qa, ta, mas, mun, qb, tb, mbs, mb, en, ln);
                 acc += (en - eo) + (ln - lo);
             }
+            acc += (double)accf.hi + (double)accf.lo;
             // ---- k space (df): increments of Q_ion and Q_dip and the energy change
             df ek = {0.0f, 0.0f};
             const df qeffd = S.qeffd;
@@ -555,6 +669,8 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         }
         if (tid == 0) {
             const int i = S.idx;
+            d.pf[i] = make_float4((float)(S.mun[0] * S.mas), (float)(S.mun[1] * S.mas), (float)(S.mun[2] * S.mas),
+                                  (float)S.qa);
             for (int a = 0; a < 3; a++) {
                 d.pos[3 * i + a] = S.pn[a];
                 d.mu[3 * i + a] = S.mun[a];
@@ -631,7 +747,8 @@ struct fg_dipsys {
     fgd::DipDesc *d_desc = nullptr;
     int64_t *pos = nullptr;
     double *mu = nullptr, *mus = nullptr, *q = nullptr, *ak = nullptr, *pairs = nullptr;
-    int32_t *type = nullptr;
+    int32_t *type = nullptr, *nearq = nullptr;
+    float4 *pf = nullptr;
     char4 *kn = nullptr;
     double2 *qi = nullptr, *qd = nullptr;
     float4 *fqi = nullptr, *fqd = nullptr, *dqi = nullptr, *dqd = nullptr;
@@ -656,7 +773,7 @@ struct fg_dipsys {
 namespace {
 
 void dip_free(fg_dipsys *h) {
-    void *ptrs[] = {h->d_desc, h->pos, h->mu, h->mus, h->q, h->ak, h->pairs, h->type, h->kn, h->qi, h->qd,
+    void *ptrs[] = {h->d_desc, h->pos, h->mu, h->mus, h->q, h->ak, h->pairs, h->type, h->nearq, h->pf, h->kn, h->qi, h->qd,
                     h->fqi, h->fqd, h->dqi, h->dqd, h->akf, h->trials, h->log_du, h->log_acc, h->sc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -676,6 +793,54 @@ int dip_dmalloc(fg_dipsys *h, void **p, size_t bytes) {
 int dip_push_desc(fg_dipsys *h) {
     CK(cudaMemcpyAsync(h->d_desc, &h->desc, sizeof(fgd::DipDesc), cudaMemcpyHostToDevice, h->stream));
     return FG_OK;
+}
+
+// Squared far radius: beyond rf no pair term of this state (largest charge,
+// dipole, LJ and effective-charge factors) exceeds 1e-4 kT, so the FP32
+// rounding of a far pair (a few ulp) is below 1e-10 kT. Ewald terms end at
+// rc, LJ has no cutoff. Bisection on the decreasing bound.
+float dip_far_radius2(const fg_dipsys *h) {
+    const fgd::DipDesc &d = h->desc;
+    const int nt = d.nt;
+    double qm = 0.0, mm = 0.0, e4 = 0.0, s2 = 0.0, qq = 0.0;
+    for (int i = 0; i < h->N; i++) {
+        qm = std::max(qm, std::fabs(h->charges_h[i]));
+        mm = std::max(mm, std::fabs(h->mus_h[i]));
+    }
+    for (int k = 0; k < nt * nt; k++) {
+        e4 = std::max(e4, std::fabs(d.eps4[k]));
+        s2 = std::max(s2, d.s2[k]);
+        qq = std::max(qq, std::fabs(d.qeqe[k]));
+    }
+    auto bound = [&](double r) {
+        const double r2 = r * r, x = s2 / r2, x3 = x * x * x;
+        double b = e4 * (x3 * x3 + x3);
+        if (!d.any_term || r2 > d.rc2) return b;
+        const double ar = d.alpha * r, ec = std::erfc(ar), ex = std::exp(-d.alpha2 * r2);
+        if (d.quirk || d.ii) {
+            const double h2 = d.kappa / 2.0 / d.alpha;
+            const double t = d.small_kappa ? ec / r
+                                           : (std::erfc(ar + h2) * std::exp(d.kappa * r) +
+                                              std::erfc(ar - h2) * std::exp(-d.kappa * r)) / (2.0 * r);
+            b += d.lB * qm * qm * qq * t;
+        }
+        if (!d.quirk) {
+            const double T1f = r * d.t1c * ex + ec, T2f = 3.0 * (T1f + d.t2c * r * r * r * ex);
+            if (d.id) b += d.lB * 2.0 * qm * mm * T1f / r2;
+            if (d.dd) b += d.lB * mm * mm * (T1f + T2f) / (r2 * r);
+        }
+        return b;
+    };
+    const double eps = 1e-4;
+    double hi = 0.5 * std::sqrt(d.L[0] * d.L[0] + d.L[1] * d.L[1] + d.L[2] * d.L[2]) + 1.0, lo = 1e-3;
+    if (bound(hi) > eps) return 3.0e38f;   // nothing is far
+    for (int it = 0; it < 60; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (bound(mid) > eps) lo = mid;
+        else hi = mid;
+    }
+    const double rf = hi + 1e-3;   // covers the float distance of the high words
+    return (float)(rf * rf);
 }
 
 int dip_read_scalars(fg_dipsys *h, fgd::DipScalars &s) {
@@ -1027,6 +1192,19 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
                                      ? qs(i) * qs(j) / P.type_charge[i] / P.type_charge[j] : 0.0;
         }
     }
+    d.rc2f = (float)d.rc2;
+    d.alphaf = (float)d.alpha;
+    d.alpha2f = (float)d.alpha2;
+    d.kappaf = (float)d.kappa;
+    d.lBf = (float)d.lB;
+    d.t1cf = (float)d.t1c;
+    d.t2cf = (float)d.t2c;
+    for (int k = 0; k < nt * nt; k++) {
+        d.qeqef[k] = (float)d.qeqe[k];
+        d.s2f[k] = (float)d.s2[k];
+        d.eps4f[k] = (float)d.eps4[k];
+    }
+    d.rf2f = 3.0e38f;   // set with the state
     int rc_;
 #define TRY(x)                     \
     do {                           \
@@ -1040,6 +1218,8 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     TRY(dip_dmalloc(h, (void **)&h->mus, N * sizeof(double)));
     TRY(dip_dmalloc(h, (void **)&h->q, N * sizeof(double)));
     TRY(dip_dmalloc(h, (void **)&h->type, N * sizeof(int32_t)));
+    TRY(dip_dmalloc(h, (void **)&h->nearq, (N + fgd::kDipMaxThreads) * sizeof(int32_t)));
+    TRY(dip_dmalloc(h, (void **)&h->pf, N * sizeof(float4)));
     TRY(dip_dmalloc(h, (void **)&h->pairs, 2 * N * sizeof(double)));
     TRY(dip_dmalloc(h, (void **)&h->kn, K * sizeof(char4)));
     TRY(dip_dmalloc(h, (void **)&h->ak, K * sizeof(double)));
@@ -1056,6 +1236,8 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     d.mus = h->mus;
     d.q = h->q;
     d.type = h->type;
+    d.nearq = h->nearq;
+    d.pf = h->pf;
     d.kn = h->kn;
     d.ak = h->ak;
     d.qi = h->qi;
@@ -1115,6 +1297,12 @@ int fg_dip_set_state(fg_dipsys *h, const double *xyz, const double *mu_unit, con
     CK(cudaMemcpyAsync(h->mus, mu_scalar, (size_t)N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->q, h->charges_h.data(), (size_t)N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->type, type_ids, (size_t)N * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    std::vector<float4> pf(N);
+    for (int i = 0; i < N; i++)
+        pf[i] = make_float4((float)(mu_unit[3 * i] * mu_scalar[i]), (float)(mu_unit[3 * i + 1] * mu_scalar[i]),
+                            (float)(mu_unit[3 * i + 2] * mu_scalar[i]), (float)h->charges_h[i]);
+    CK(cudaMemcpyAsync(h->pf, pf.data(), (size_t)N * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    h->desc.rf2f = dip_far_radius2(h);
     int rc = dip_push_desc(h);
     if (rc) return rc;
     fgd::DipScalars s{};
