@@ -905,12 +905,13 @@ def run_dipoles(args, rank, world):
         _, tot = dip_run_many(systems)
         e2e_s += time.perf_counter() - t0
         e2e_t += tot["trials"]
-    # one system alone: the single-chain latency
+    # one system alone: the single-chain latency (a whole CTA of 256 threads)
     one = systems[0]
+    one.set_threads(256)
     one.sweep(dip_draw_stream(99, DIP_N, 2000, 0.5, DIP_DP, DIP_DPROT), log=False)
     r = one.sweep(dip_draw_stream(98, DIP_N, 4000, 0.5, DIP_DP, DIP_DPROT), log=False)
     single = {"value": r["trials"] / (r["device_ms"] / 1e3), "unit": UNIT,
-              "us_per_trial": r["device_ms"] * 1e3 / r["trials"]}
+              "us_per_trial": r["device_ms"] * 1e3 / r["trials"], "threads": 256}
     # plain per-trial API: fg_dip_trial_du + fg_dip_commit per trial
     import numpy as np
     xyz, mu = one.state()
@@ -1110,7 +1111,7 @@ def main():
     ap.add_argument("--round-pairs", type=int, default=1 << 24, help="serving: pair evaluations per job per round")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample per core")
     ap.add_argument("--ref-seconds", type=float, default=3.0, help="reference arm: seconds per step")
-    ap.add_argument("--dip-threads", type=int, default=128, help="dipoles: threads per system (one CTA)")
+    ap.add_argument("--dip-threads", type=int, default=64, help="dipoles: threads per system (one CTA)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tune-trials", type=int, default=512,
                     help="pt64/serving: trials per member per autotuner candidate (0: no tuning)")

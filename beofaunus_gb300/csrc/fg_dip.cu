@@ -91,6 +91,13 @@ struct DipDesc {
     int32_t *type;        // [N]
     float4 *pf;           // [N] mu_s mu (x, y, z) and q as floats (far pairs)
     int32_t *nearq;       // [N + kDipMaxThreads] near-pair queue of the trial in flight
+    // radial functions A, B, C of the real-space sum (see radial()) on
+    // s = r^2 in [ts0, rc^2]: tn intervals of width 1 / tinv, six
+    // coefficients per function per interval in the local variable
+    // t = (s - s_k) tinv; null: evaluated directly
+    const double *rtab;
+    double ts0, tinv;
+    int32_t tn, pad_tab;
     char4 *kn;            // [K] n-vector of k
     double *ak;           // [K] A_k with the half-space factor
     double2 *qi, *qd;     // [K] FP64 accumulators of a rebuild
@@ -179,6 +186,39 @@ __device__ __forceinline__ double2 axis_entry(int n, int64_t X) {
     return make_double2(c, s);
 }
 
+__device__ __forceinline__ double horner6(const double *c, double t) {
+    return fma(fma(fma(fma(fma(c[5], t, c[4]), t, c[3]), t, c[2]), t, c[1]), t, c[0]);
+}
+
+// Radial functions of the real-space sum at s = r^2 (r <= rc):
+//   A = ion-ion: erfc(a r) / r, or the kappa-screened form (ewald.h:109);
+//   B = T1f(r) / r^3, C = T2f(r) / r^5 (ewald.h:46-47),
+// from the interpolation table where it covers s, else from erfc and exp.
+__device__ __forceinline__ void radial(const DipDesc &d, double s, double &A, double &B, double &C) {
+    if (d.rtab && s >= d.ts0) {
+        const double u = (s - d.ts0) * d.tinv;
+        int k = (int)u;
+        k = k < d.tn - 1 ? k : d.tn - 1;
+        const double t = u - (double)k;
+        const double *c = d.rtab + 18 * k;
+        A = horner6(c, t);
+        B = horner6(c + 6, t);
+        C = horner6(c + 12, t);
+        return;
+    }
+    const double r1 = sqrt(s), ir1 = 1.0 / r1, ir2 = ir1 * ir1;
+    const double ar = d.alpha * r1, ec = erfc(ar), ex = exp(-d.alpha2 * s);
+    if (d.small_kappa) {
+        A = ec * ir1;
+    } else {
+        const double h = d.kappa / 2.0 / d.alpha;
+        A = (erfc(ar + h) * exp(d.kappa * r1) + erfc(ar - h) * exp(-d.kappa * r1)) / (2.0 * r1);
+    }
+    const double T1f = r1 * d.t1c * ex + ec;
+    B = T1f * ir1 * ir2;
+    C = 3.0 * (T1f + d.t2c * r1 * r1 * r1 * ex) * (ir2 * ir2 * ir1);
+}
+
 // Pair energy of particles a (moved) and b at r = a - b: EwaldReal + LJ
 // (CombinedPairPotential, potentials.h:3768-3771). real/lj split for totals.
 __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry, double rz, double qa, int ta,
@@ -186,42 +226,23 @@ __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry,
                                          const double *mb, double &real, double &lj) {
     const double r2 = rx * rx + ry * ry + rz * rz;
     const int tt = ta * d.nt + tb;
-    const bool near = d.any_term && r2 <= d.rc2;
-    // one sqrt and one division per pair; every 1/r^n below is a product of them
-    const double r1 = near ? sqrt(r2) : 1.0;
-    const double ir1 = near ? 1.0 / r1 : 0.0;
-    const double ir2 = near ? ir1 * ir1 : 1.0 / r2;
-    double x = d.s2[tt] * ir2;   // LennardJonesMixed (potentials.h:2036-2040)
+    double x = d.s2[tt] / r2;   // LennardJonesMixed (potentials.h:2036-2040)
     x = x * x * x;
     lj = d.eps4[tt] * (x * x - x);
     real = 0.0;
-    if (!near) return;
-    const double ar = d.alpha * r1;
-    const double ec = erfc(ar);
-    if (d.quirk || d.ii) {
-        double t;
-        if (d.small_kappa) {
-            t = ec * ir1;   // erfc(ar +- kappa / 2 alpha) e^{+-kappa r} round to erfc(ar) here
-        } else {
-            const double h = d.kappa / 2.0 / d.alpha;
-            t = (erfc(ar + h) * exp(d.kappa * r1) + erfc(ar - h) * exp(-d.kappa * r1)) / (2.0 * r1);
-        }
-        real = qa * qb * t * d.qeqe[tt] * d.lB;
-    }
+    if (!d.any_term || r2 > d.rc2) return;
+    double A, B, C;
+    radial(d, r2, A, B, C);
+    if (d.quirk || d.ii) real = qa * qb * A * d.qeqe[tt] * d.lB;
     if (d.quirk || !(d.id || d.dd)) return;
-    const double ex = exp(-d.alpha2 * r2);
-    const double T1f = r1 * d.t1c * ex + ec;   // ewald.h:46
-    const double T1 = T1f * ir1 * ir2;
     double Ed = 0.0;
     if (d.id) {
-        Ed += qa * (rx * mb[0] + ry * mb[1] + rz * mb[2]) * mbs * T1;
-        Ed -= qb * (rx * ma[0] + ry * ma[1] + rz * ma[2]) * mas * T1;
+        Ed += qa * (rx * mb[0] + ry * mb[1] + rz * mb[2]) * mbs * B;
+        Ed -= qb * (rx * ma[0] + ry * ma[1] + rz * ma[2]) * mas * B;
     }
     if (d.dd) {
-        const double T2f = 3.0 * (T1f + d.t2c * r1 * r1 * r1 * ex);   // ewald.h:47
-        const double t3 = -(mb[0] * ma[0] + mb[1] * ma[1] + mb[2] * ma[2]) * T1;
-        const double t5 =
-            (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (ma[0] * rx + ma[1] * ry + ma[2] * rz) * T2f * (ir2 * ir2 * ir1);
+        const double t3 = -(mb[0] * ma[0] + mb[1] * ma[1] + mb[2] * ma[2]) * B;
+        const double t5 = (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (ma[0] * rx + ma[1] * ry + ma[2] * rz) * C;
         Ed += -(t5 + t3) * mbs * mas;
     }
     real += d.lB * Ed;
@@ -292,18 +313,13 @@ __device__ __forceinline__ double dip_turn(const DipDesc &d, double rx, double r
                                            const double *dmu, double qb, double mbs, const double *mb) {
     const double r2 = rx * rx + ry * ry + rz * rz;
     if (d.quirk || !(d.id || d.dd) || r2 > d.rc2) return 0.0;
-    const double r1 = sqrt(r2);
-    const double ir1 = 1.0 / r1, ir2 = ir1 * ir1;
-    const double ex = exp(-d.alpha2 * r2);
-    const double T1f = r1 * d.t1c * ex + erfc(d.alpha * r1);
-    const double T1 = T1f * ir1 * ir2;
+    double A, B, C;
+    radial(d, r2, A, B, C);
     double Ed = 0.0;
-    if (d.id) Ed -= qb * (rx * dmu[0] + ry * dmu[1] + rz * dmu[2]) * mas * T1;
+    if (d.id) Ed -= qb * (rx * dmu[0] + ry * dmu[1] + rz * dmu[2]) * mas * B;
     if (d.dd) {
-        const double T2f = 3.0 * (T1f + d.t2c * r1 * r1 * r1 * ex);
-        const double t3 = -(mb[0] * dmu[0] + mb[1] * dmu[1] + mb[2] * dmu[2]) * T1;
-        const double t5 =
-            (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (dmu[0] * rx + dmu[1] * ry + dmu[2] * rz) * T2f * (ir2 * ir2 * ir1);
+        const double t3 = -(mb[0] * dmu[0] + mb[1] * dmu[1] + mb[2] * dmu[2]) * B;
+        const double t5 = (mb[0] * rx + mb[1] * ry + mb[2] * rz) * (dmu[0] * rx + dmu[1] * ry + dmu[2] * rz) * C;
         Ed += -(t5 + t3) * mbs * mas;
     }
     return d.lB * Ed;
@@ -766,13 +782,17 @@ struct fg_dipsys {
     std::vector<double> ak_h, charges_h, mus_h;
     std::vector<int32_t> types_h;
     std::vector<char4> kn_h;
+    std::vector<double> rtab_key;   // shared radial table in use
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     size_t device_bytes = 0;
 };
 
 namespace {
 
+void dip_radial_release(fg_dipsys *h);
+
 void dip_free(fg_dipsys *h) {
+    dip_radial_release(h);
     void *ptrs[] = {h->d_desc, h->pos, h->mu, h->mus, h->q, h->ak, h->pairs, h->type, h->nearq, h->pf, h->kn, h->qi, h->qd,
                     h->fqi, h->fqd, h->dqi, h->dqd, h->akf, h->trials, h->log_du, h->log_acc, h->sc};
     for (void *p : ptrs)
@@ -841,6 +861,110 @@ float dip_far_radius2(const fg_dipsys *h) {
     }
     const double rf = hi + 1e-3;   // covers the float distance of the high words
     return (float)(rf * rf);
+}
+
+// ---- interpolation tables of the radial functions, shared by every system
+// with the same (alpha, kappa, rc): a degree-5 polynomial per interval,
+// interpolating at the six Chebyshev points of the interval (computed in long
+// double), checked against the functions before use.
+struct RadialTab {
+    double *dev = nullptr;
+    int refs = 0;
+};
+std::mutex g_rtab_mu;
+std::map<std::vector<double>, RadialTab> g_rtab;
+
+constexpr int kRadialIntervals = 4096;
+
+void radial_exact(long double alpha, long double kappa, bool small_kappa, long double s, long double f[3]) {
+    const long double r = std::sqrt(s), ar = alpha * r;
+    const long double ec = std::erfc(ar), ex = std::exp(-alpha * alpha * s);
+    if (small_kappa) {
+        f[0] = ec / r;
+    } else {
+        const long double h = kappa / 2 / alpha;
+        f[0] = (std::erfc(ar + h) * std::exp(kappa * r) + std::erfc(ar - h) * std::exp(-kappa * r)) / (2 * r);
+    }
+    const long double pi = 3.141592653589793238462643383279502884L;
+    const long double T1f = r * 2 * alpha / std::sqrt(pi) * ex + ec;
+    f[1] = T1f / (r * s);
+    f[2] = 3 * (T1f + 4 * alpha * alpha * alpha / 3 / std::sqrt(pi) * r * s * ex) / (s * s * r);
+}
+
+// Builds (or finds) the table for h's parameters; returns 0 and sets the
+// descriptor fields, or leaves them null when the check fails.
+int dip_radial_table(fg_dipsys *h) {
+    fgd::DipDesc &d = h->desc;
+    d.rtab = nullptr;
+    if (!d.any_term) return FG_OK;
+    const double ts0 = 4.0;   // r >= 2 A from the table, closer pairs directly
+    if (!(d.rc2 > ts0 * 1.01)) return FG_OK;
+    std::vector<double> key = {d.alpha, d.kappa, d.rc2, (double)d.small_kappa};
+    std::lock_guard<std::mutex> lk(g_rtab_mu);
+    RadialTab &t = g_rtab[key];
+    const double w = (d.rc2 - ts0) / kRadialIntervals;
+    if (!t.dev) {
+        const int n = kRadialIntervals;
+        std::vector<double> c((size_t)n * 18);
+        const long double pi = 3.141592653589793238462643383279502884L;
+        bool ok = true;
+        for (int k = 0; k < n && ok; k++) {
+            // Chebyshev points of [0, 1], Newton divided differences, then monomial coefficients
+            long double tx[6], fy[3][6];
+            for (int j = 0; j < 6; j++) {
+                tx[j] = (1 - std::cos((2 * j + 1) * pi / 12)) / 2;
+                long double f[3];
+                radial_exact(d.alpha, d.kappa, d.small_kappa, ts0 + (k + tx[j]) * (long double)w, f);
+                for (int m = 0; m < 3; m++) fy[m][j] = f[m];
+            }
+            for (int m = 0; m < 3; m++) {
+                long double dd[6];
+                for (int j = 0; j < 6; j++) dd[j] = fy[m][j];
+                for (int o = 1; o < 6; o++)
+                    for (int j = 5; j >= o; j--) dd[j] = (dd[j] - dd[j - 1]) / (tx[j] - tx[j - o]);
+                long double poly[6] = {0, 0, 0, 0, 0, 0};
+                for (int j = 5; j >= 0; j--) {   // poly = poly * (t - tx[j]) + dd[j]
+                    for (int o = 5; o >= 1; o--) poly[o] = poly[o - 1] - tx[j] * poly[o];
+                    poly[0] = -tx[j] * poly[0] + dd[j];
+                }
+                for (int o = 0; o < 6; o++) c[(size_t)k * 18 + 6 * m + o] = (double)poly[o];
+            }
+            for (long double tt : {0.0L, 0.29L, 0.61L, 0.97L}) {
+                long double f[3];
+                radial_exact(d.alpha, d.kappa, d.small_kappa, ts0 + (k + tt) * (long double)w, f);
+                for (int m = 0; m < 3; m++) {
+                    const double *cc = &c[(size_t)k * 18 + 6 * m];
+                    const double tv = (double)tt;
+                    const double v = ((((cc[5] * tv + cc[4]) * tv + cc[3]) * tv + cc[2]) * tv + cc[1]) * tv + cc[0];
+                    if (std::fabs((long double)v - f[m]) > 1e-13L * std::fabs(f[m])) ok = false;
+                }
+            }
+        }
+        if (!ok) {
+            g_rtab.erase(key);
+            return FG_OK;   // direct evaluation
+        }
+        CK(cudaMalloc(&t.dev, c.size() * sizeof(double)));
+        CK(cudaMemcpy(t.dev, c.data(), c.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    t.refs++;
+    h->rtab_key = key;
+    d.rtab = t.dev;
+    d.ts0 = ts0;
+    d.tinv = 1.0 / w;
+    d.tn = kRadialIntervals;
+    return FG_OK;
+}
+
+void dip_radial_release(fg_dipsys *h) {
+    if (h->rtab_key.empty()) return;
+    std::lock_guard<std::mutex> lk(g_rtab_mu);
+    auto it = g_rtab.find(h->rtab_key);
+    if (it != g_rtab.end() && --it->second.refs <= 0) {
+        cudaFree(it->second.dev);
+        g_rtab.erase(it);
+    }
+    h->rtab_key.clear();
 }
 
 int dip_read_scalars(fg_dipsys *h, fgd::DipScalars &s) {
@@ -1205,6 +1329,7 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
         d.eps4f[k] = (float)d.eps4[k];
     }
     d.rf2f = 3.0e38f;   // set with the state
+    if (int rc0 = dip_radial_table(h)) return bail(rc0);
     int rc_;
 #define TRY(x)                     \
     do {                           \

@@ -736,6 +736,10 @@ class DipoleSystem:
     def num_kvectors(self):
         return int(lib().fg_dip_num_kvectors(self.h))
 
+    def set_threads(self, threads):
+        """Threads of the system's CTA (multiple of 32, 32..256)."""
+        _check(lib().fg_dip_set_threads(self.h, int(threads)))
+
     def set_state(self, xyz, mu_unit, mu_scalar, type_ids, charges=None):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
         mu = np.ascontiguousarray(mu_unit, dtype=np.float64).reshape(-1, 3)
