@@ -178,6 +178,43 @@ __host__ __device__ constexpr size_t dip_yz_bytes(int kcc) {
     return (size_t)2 * (2 * kcc + 1) * (2 * kcc + 1) * sizeof(double2);
 }
 
+// The arrays one sweep touches per trial. A sweep launch stages them in
+// shared memory (dip_stage_layout, after the yz table) when they fit, so the
+// k loop and the pair loop read no global memory; Q(k) goes back to global
+// memory at the end of the launch, positions and pf on every acceptance.
+struct DipArrays {
+    const char4 *kn;
+    const float2 *akf;
+    float4 *fqi, *fqd, *dqi, *dqd;
+    int64_t *pos;
+    float4 *pf;
+    const int32_t *type;
+};
+
+__host__ __device__ inline size_t dip_al16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline size_t dip_stage_layout(int K, int N, int kcc, int ion_q, int dip_q, size_t off[9]) {
+    size_t b = dip_yz_bytes(kcc);
+    off[0] = b;                               // kn
+    b = dip_al16(b + (size_t)K * 4);
+    off[1] = b;                               // akf
+    b = dip_al16(b + (size_t)K * 8);
+    off[2] = b;                               // fqi
+    if (ion_q) b += (size_t)K * 16;
+    off[3] = b;                               // fqd
+    if (dip_q) b += (size_t)K * 16;
+    off[4] = b;                               // dqi
+    if (ion_q) b += (size_t)K * 16;
+    off[5] = b;                               // dqd
+    if (dip_q) b += (size_t)K * 16;
+    off[6] = b;                               // pos
+    b = dip_al16(b + (size_t)N * 24);
+    off[7] = b;                               // pf
+    b += (size_t)N * 16;
+    off[8] = b;                               // type
+    return dip_al16(b + (size_t)N * 4);
+}
+
 // cos, sin of 2 pi n X / 2^64: the phase reduced exactly in integers
 __device__ __forceinline__ double2 axis_entry(int n, int64_t X) {
     const int64_t ph = (int64_t)((uint64_t)(int64_t)n * (uint64_t)X);
@@ -370,11 +407,11 @@ struct DipShared {
 
 // Q(k) from scratch (updateAllComplexNumbers, ewald.h:388-415). Returns the
 // reciprocal energy before and after in thread 0.
-__device__ void dip_rebuild(const DipDesc &d, DipShared &S, double &before, double &after) {
+__device__ void dip_rebuild(const DipDesc &d, const DipArrays &A, DipShared &S, double &before, double &after) {
     const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
     double e = 0.0;
     for (int k = tid; k < d.K; k += T) {
-        e += d.ak[k] * q2(d, dc_val(d.fqi[k]), dc_val(d.fqd[k]));
+        e += d.ak[k] * q2(d, dc_val(A.fqi[k]), dc_val(A.fqd[k]));
         d.qi[k] = make_double2(0.0, 0.0);
         d.qd[k] = make_double2(0.0, 0.0);
     }
@@ -383,15 +420,15 @@ __device__ void dip_rebuild(const DipDesc &d, DipShared &S, double &before, doub
         __syncthreads();   // previous particle's table consumed
         for (int e = tid; e < 3 * st; e += T) {
             const int a = e / st, n = e - a * st;
-            S.rtab[e] = axis_entry(n, d.pos[3 * j + a]);
+            S.rtab[e] = axis_entry(n, A.pos[3 * j + a]);
         }
         if (tid == 0) {
-            S.rq = d.q[j] * d.eff[d.type[j]];
+            S.rq = d.q[j] * d.eff[A.type[j]];
             for (int a = 0; a < 3; a++) S.rmu[a] = d.mu[3 * j + a] * d.mus[j];
         }
         __syncthreads();
         for (int k = tid; k < d.K; k += T) {
-            const char4 n = d.kn[k];
+            const char4 n = A.kn[k];
             const double2 ph = kphase(S.rtab, st, n);
             if (d.ion_q) {
                 double2 v = d.qi[k];
@@ -412,8 +449,8 @@ __device__ void dip_rebuild(const DipDesc &d, DipShared &S, double &before, doub
     for (int k = tid; k < d.K; k += T) {
         const double2 a = d.qi[k], b = d.qd[k];
         e += d.ak[k] * q2(d, a, b);
-        d.fqi[k] = dc_pack(dc_split(a));
-        d.fqd[k] = dc_pack(dc_split(b));
+        A.fqi[k] = dc_pack(dc_split(a));
+        A.fqd[k] = dc_pack(dc_split(b));
     }
     after = block_sum(e, S.red) * d.recip_c;
 }
@@ -422,21 +459,51 @@ __device__ void dip_rebuild(const DipDesc &d, DipShared &S, double &before, doub
 __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_build_kernel(const DipDesc *dp) {
     __shared__ DipShared S;
     double before, after;
-    dip_rebuild(*dp, S, before, after);
+    const DipDesc &d = *dp;
+    const DipArrays A = {d.kn, d.akf, d.fqi, d.fqd, d.dqi, d.dqd, d.pos, d.pf, d.type};
+    dip_rebuild(d, A, S, before, after);
 }
 
 // mode 0: run the staged stream [cursor, n_trials) with Metropolis decisions;
 // mode 1: evaluate trials[0] (explicit) and keep it pending;
 // mode 2: apply the pending trials[0] as accepted.
-__global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipDesc *descs, int mode) {
+__global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipDesc *descs, int mode, int stage) {
     const DipDesc &d = descs[blockIdx.x];
     __shared__ DipShared S;
-    extern __shared__ float4 eyz[];   // df complex
+    extern __shared__ __align__(16) unsigned char dsm[];
+    float4 *eyz = reinterpret_cast<float4 *>(dsm);   // df complex
     const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
     const int W = 2 * d.kcc + 1, W2 = W * W;
     if (T > kDipMaxThreads || (T & 31)) {
         if (tid == 0) atomicOr(&d.sc->error, kDipErrLaunch);
         return;
+    }
+    DipArrays A = {d.kn, d.akf, d.fqi, d.fqd, d.dqi, d.dqd, d.pos, d.pf, d.type};
+    if (stage) {
+        size_t off[9];
+        dip_stage_layout(d.K, d.N, d.kcc, d.ion_q, d.dip_q, off);
+        char4 *kn = reinterpret_cast<char4 *>(dsm + off[0]);
+        float2 *akf = reinterpret_cast<float2 *>(dsm + off[1]);
+        float4 *fqi = reinterpret_cast<float4 *>(dsm + off[2]), *fqd = reinterpret_cast<float4 *>(dsm + off[3]);
+        int64_t *pos = reinterpret_cast<int64_t *>(dsm + off[6]);
+        float4 *pf = reinterpret_cast<float4 *>(dsm + off[7]);
+        int32_t *typ = reinterpret_cast<int32_t *>(dsm + off[8]);
+        for (int k = tid; k < d.K; k += T) {
+            kn[k] = A.kn[k];
+            akf[k] = A.akf[k];
+            if (d.ion_q) fqi[k] = A.fqi[k];
+            if (d.dip_q) fqd[k] = A.fqd[k];
+        }
+        for (int j = tid; j < d.N; j += T) {
+            pos[3 * j] = A.pos[3 * j];
+            pos[3 * j + 1] = A.pos[3 * j + 1];
+            pos[3 * j + 2] = A.pos[3 * j + 2];
+            pf[j] = A.pf[j];
+            typ[j] = A.type[j];
+        }
+        A = {kn, akf, fqi, fqd, reinterpret_cast<float4 *>(dsm + off[4]), reinterpret_cast<float4 *>(dsm + off[5]), pos,
+             pf, typ};
+        __syncthreads();
     }
     DipScalars sc;
     if (tid == 0) {
@@ -456,12 +523,12 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             S.idx = i;
             S.kind = tr.kind;
             S.u = tr.u;
-            S.ta = d.type[i];
+            S.ta = A.type[i];
             S.qa = d.q[i];
             S.qeff = d.q[i] * d.eff[S.ta];
             S.mas = d.mus[i];
             for (int a = 0; a < 3; a++) {
-                S.po[a] = d.pos[3 * i + a];
+                S.po[a] = A.pos[3 * i + a];
                 S.muo[a] = d.mu[3 * i + a];
                 S.pn[a] = S.po[a];
                 S.mun[a] = S.muo[a];
@@ -541,20 +608,20 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 const int j = it * T + tid;
                 bool nearp = false;
                 if (j < d.N && j != i) {
-                    const int64_t pj0 = d.pos[3 * j], pj1 = d.pos[3 * j + 1], pj2 = d.pos[3 * j + 2];
+                    const int64_t pj0 = A.pos[3 * j], pj1 = A.pos[3 * j + 1], pj2 = A.pos[3 * j + 2];
                     const float ox = hi_diff(S.po[0], pj0) * sx, oy = hi_diff(S.po[1], pj1) * sy,
                                 oz = hi_diff(S.po[2], pj2) * sz;
                     const float r2o = ox * ox + oy * oy + oz * oz;
                     if (fixed) {
                         nearp = r2o < d.rf2f;
-                        if (!nearp) accf = fg::df_add_f(accf, far_turn(d, ox, oy, oz, dmf, d.pf[j]));
+                        if (!nearp) accf = fg::df_add_f(accf, far_turn(d, ox, oy, oz, dmf, A.pf[j]));
                     } else {
                         const float nx = hi_diff(S.pn[0], pj0) * sx, ny = hi_diff(S.pn[1], pj1) * sy,
                                     nz = hi_diff(S.pn[2], pj2) * sz;
                         nearp = r2o < d.rf2f || nx * nx + ny * ny + nz * nz < d.rf2f;
                         if (!nearp) {
-                            const float4 mb = d.pf[j];
-                            const int tb = d.type[j];
+                            const float4 mb = A.pf[j];
+                            const int tb = A.type[j];
                             accf = fg::df_add_f(accf, far_pair(d, nx, ny, nz, ta, man, tb, mb) -
                                                           far_pair(d, ox, oy, oz, ta, mao, tb, mb));
                         }
@@ -578,7 +645,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 int64_t pj[3];
                 double mb[3];
                 for (int a = 0; a < 3; a++) {
-                    pj[a] = d.pos[3 * j + a];
+                    pj[a] = A.pos[3 * j + a];
                     mb[a] = d.mu[3 * j + a];
                 }
                 const double qb = d.q[j], mbs = d.mus[j];
@@ -588,7 +655,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                     acc += dip_turn(d, ro[0], ro[1], ro[2], mas, dmu, qb, mbs, mb);
                     continue;
                 }
-                const int tb = d.type[j];
+                const int tb = A.type[j];
                 double rn[3];
                 for (int a = 0; a < 3; a++) rn[a] = (double)(int64_t)((uint64_t)S.pn[a] - (uint64_t)pj[a]) * d.s64[a];
                 double eo, lo, en, ln;
@@ -603,7 +670,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             const df mo[3] = {S.mo[0], S.mo[1], S.mo[2]}, mn[3] = {S.mn[0], S.mn[1], S.mn[2]},
                      md[3] = {S.md[0], S.md[1], S.md[2]};
             for (int k = tid; k < d.K; k += T) {
-                const char4 n = d.kn[k];
+                const char4 n = A.kn[k];
                 const int yz = (n.y + d.kcc) * W + n.z + d.kcc;
                 const dc eo = dc_mul(dc_load(S.tab[0][n.x]), dc_load(eyz[yz]));
                 dc dci = {{0.0f, 0.0f}, {0.0f, 0.0f}}, dcd = dci;
@@ -623,24 +690,24 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 }
                 df sum = {0.0f, 0.0f};
                 if (d.ii) {
-                    const dc Qi = dc_load(d.fqi[k]);
+                    const dc Qi = dc_load(A.fqi[k]);
                     sum = dadd(dtwice(dc_dot(Qi, dci)), dc_dot(dci, dci));
                 }
                 if (d.id) {
-                    const dc Qi = dc_load(d.fqi[k]), Qd = dc_load(d.fqd[k]);
+                    const dc Qi = dc_load(A.fqi[k]), Qd = dc_load(A.fqd[k]);
                     if (d.quirk)
                         sum = dadd(sum, dtwice(dadd(dadd(dc_rprod(Qi, dcd), dc_rprod(dci, Qd)), dc_rprod(dci, dcd))));
                     else
                         sum = dadd(sum, dtwice(dadd(dadd(dc_dot(Qi, dcd), dc_dot(dci, Qd)), dc_dot(dci, dcd))));
                 }
                 if (d.dd) {
-                    const dc Qd = dc_load(d.fqd[k]);
+                    const dc Qd = dc_load(A.fqd[k]);
                     sum = dadd(sum, dadd(dtwice(dc_dot(Qd, dcd)), dc_dot(dcd, dcd)));
                 }
-                const float2 a = d.akf[k];
+                const float2 a = A.akf[k];
                 ek = dadd(ek, dmul(df{a.x, a.y}, sum));
-                d.dqi[k] = dc_pack(dci);
-                d.dqd[k] = dc_pack(dcd);
+                A.dqi[k] = dc_pack(dci);
+                A.dqd[k] = dc_pack(dcd);
             }
             acc += dval(ek) * d.recip_c;
             const double sum = block_sum(acc, S.red);
@@ -675,20 +742,24 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         // ---- accepted: Q(k), the particle, the sums
         for (int k = tid; k < d.K; k += T) {
             if (d.ion_q) {
-                const dc a = dc_load(d.fqi[k]), b = dc_load(d.dqi[k]);
-                d.fqi[k] = dc_pack({dadd(a.re, b.re), dadd(a.im, b.im)});
+                const dc a = dc_load(A.fqi[k]), b = dc_load(A.dqi[k]);
+                A.fqi[k] = dc_pack({dadd(a.re, b.re), dadd(a.im, b.im)});
             }
             if (d.dip_q) {
-                const dc a = dc_load(d.fqd[k]), b = dc_load(d.dqd[k]);
-                d.fqd[k] = dc_pack({dadd(a.re, b.re), dadd(a.im, b.im)});
+                const dc a = dc_load(A.fqd[k]), b = dc_load(A.dqd[k]);
+                A.fqd[k] = dc_pack({dadd(a.re, b.re), dadd(a.im, b.im)});
             }
         }
         if (tid == 0) {
             const int i = S.idx;
-            d.pf[i] = make_float4((float)(S.mun[0] * S.mas), (float)(S.mun[1] * S.mas), (float)(S.mun[2] * S.mas),
+            A.pf[i] = make_float4((float)(S.mun[0] * S.mas), (float)(S.mun[1] * S.mas), (float)(S.mun[2] * S.mas),
                                   (float)S.qa);
+            if (stage) {
+                d.pf[i] = A.pf[i];
+                for (int a = 0; a < 3; a++) d.pos[3 * i + a] = S.pn[a];
+            }
             for (int a = 0; a < 3; a++) {
-                d.pos[3 * i + a] = S.pn[a];
+                A.pos[3 * i + a] = S.pn[a];
                 d.mu[3 * i + a] = S.mun[a];
                 if (d.ion_q) S.M[a] += S.qeff * (S.rn[a] - S.ro[a]);
                 if (d.id || d.dd) S.M[3 + a] += S.mas * (S.mun[a] - S.muo[a]);
@@ -705,7 +776,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         __syncthreads();
         if (S.rebuild) {
             double before, after;
-            dip_rebuild(d, S, before, after);
+            dip_rebuild(d, A, S, before, after);
             if (tid == 0) {
                 sc.n_rebuilds++;
                 sc.drift += fabs(after - before);
@@ -714,6 +785,11 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             }
         }
     }
+    if (stage)   // Q(k) back to global memory (each thread its own k-vectors)
+        for (int k = tid; k < d.K; k += T) {
+            if (d.ion_q) d.fqi[k] = A.fqi[k];
+            if (d.dip_q) d.fqd[k] = A.fqd[k];
+        }
     if (tid == 0) {
         if (mode == 0) sc.cursor = t1;
         for (int a = 0; a < 6; a++) sc.M[a] = S.M[a];
@@ -1084,11 +1160,33 @@ int dip_total(fg_dipsys *h, double *comp) {
     return FG_OK;
 }
 
-int dip_launch(fg_dipsys *h0, const fgd::DipDesc *descs, int n, int mode, cudaStream_t st, int max_kcc) {
-    const size_t smem = fgd::dip_yz_bytes(max_kcc);
+// Shared memory of a sweep launch over these systems: the staged layout
+// when every system's fits in kDipStageMax (two or more CTAs per SM), else
+// the yz table alone.
+constexpr size_t kDipStageMax = 110 * 1024;
+
+size_t dip_launch_smem(fg_dipsys *const *sys, int n, int &stage) {
+    size_t yz = 0, st = 0;
+    for (int i = 0; i < n; i++) {
+        const fgd::DipDesc &d = sys[i]->desc;
+        size_t off[9];
+        yz = std::max(yz, fgd::dip_yz_bytes(d.kcc));
+        st = std::max(st, fgd::dip_stage_layout(d.K, d.N, d.kcc, d.ion_q, d.dip_q, off));
+    }
+    stage = st <= kDipStageMax ? 1 : 0;
+    return stage ? st : yz;
+}
+
+int dip_launch(fg_dipsys *const *sys, const fgd::DipDesc *descs, int n, int mode, cudaStream_t st) {
+    int stage = 0;
+    size_t smem = dip_launch_smem(sys, n, stage);
+    if (mode != 0) {
+        stage = 0;
+        smem = fgd::dip_yz_bytes(sys[0]->kcc);
+    }
     CK(cudaFuncSetAttribute((const void *)fgd::dip_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)smem));
-    fgd::dip_sweep_kernel<<<n, h0->threads, smem, st>>>(descs, mode);
+    fgd::dip_sweep_kernel<<<n, sys[0]->threads, smem, st>>>(descs, mode, stage);
     CK(cudaGetLastError());
     return FG_OK;
 }
@@ -1097,10 +1195,8 @@ int dip_run(fg_dipsys *const *sys, int n, fg_sweep_stats *per, fg_sweep_stats *t
     if (!sys || n < 1) return fail(FG_ERR_INVALID, "bad argument");
     fg_dipsys *h0 = sys[0];
     int64_t maxn = 0;
-    int max_kcc = 0;
     for (int i = 0; i < n; i++) {
         fg_dipsys *h = sys[i];
-        if (h) max_kcc = std::max(max_kcc, h->kcc);
         if (!h || !h->state_set) return fail(FG_ERR_STATE, "system %d has no state", i);
         if (h->pending) return fail(FG_ERR_STATE, "system %d has a pending trial: commit it first", i);
         if (h->device != h0->device) return fail(FG_ERR_INVALID, "systems must share the device");
@@ -1130,7 +1226,7 @@ int dip_run(fg_dipsys *const *sys, int n, fg_sweep_stats *per, fg_sweep_stats *t
             e = std::min(sys[i]->n_stream, (c + 1) * kChunk);
             CK(cudaMemcpyAsync(&sys[i]->sc->n_trials, &e, sizeof(int64_t), cudaMemcpyHostToDevice, st));
         }
-        rc = dip_launch(h0, descs, n, 0, st, max_kcc);
+        rc = dip_launch(sys, descs, n, 0, st);
     }
     CK(cudaEventRecord(h0->ev1, st));
     CK(cudaEventSynchronize(h0->ev1));
@@ -1500,7 +1596,7 @@ int fg_dip_trial_du(fg_dipsys *h, int32_t i, const double *new_xyz, const double
     int rc = dip_ensure_trials(h, 1, false);
     if (rc) return rc;
     CK(cudaMemcpyAsync(h->trials, &t, sizeof(t), cudaMemcpyHostToDevice, h->stream));
-    rc = dip_launch(h, h->d_desc, 1, 1, h->stream, h->kcc);
+    rc = dip_launch(&h, h->d_desc, 1, 1, h->stream);
     if (rc) return rc;
     fgd::DipScalars s;
     rc = dip_read_scalars(h, s);
@@ -1516,7 +1612,7 @@ int fg_dip_commit(fg_dipsys *h, int32_t accepted) {
     if (!h->pending) return fail(FG_ERR_STATE, "no pending trial");
     h->pending = false;
     if (!accepted) return FG_OK;
-    int rc = dip_launch(h, h->d_desc, 1, 2, h->stream, h->kcc);
+    int rc = dip_launch(&h, h->d_desc, 1, 2, h->stream);
     if (rc) return rc;
     CK(cudaStreamSynchronize(h->stream));
     return FG_OK;
