@@ -178,3 +178,21 @@ def test_invalid_arguments():
                       ewald_cutoff=4.0, ewald_cutoff_k=40.0, ewald_terms=4)
     with pytest.raises(G.FgError):
         G.DipoleSystem(bad, xyz[:4], mu[:4], mus[:4], ids[:4])
+
+
+def test_large_system_unstaged():
+    """3000 particles: the sweep's arrays exceed the shared-memory staging
+    limit, so the launch reads them from global memory; the near-pair queue
+    spans many iterations per warp."""
+    G = gpu()
+    p, xyz, mu, mus, ids, q = workloads.dipolar_fluid(n=3000, seed=41, n_ions=600, terms=7, kc=5.0,
+                                                      update_frequency=30)
+    p.bjerrum = 60.0
+    s = G.DipoleSystem(p, xyz, mu, mus, ids, charges=q)
+    o = OracleDip(p, xyz, mu, mus, ids, q=q)
+    st = G.dip_draw_stream(77, 3000, 300, p_rotate=0.5, dp=0.7, dprot=2.0)
+    r = s.sweep(st)
+    ro = o.run_stream(st)
+    agree(r["du"], r["acc"], ro["du"], ro["acc"], st["u"])
+    assert r["accepted"] > 30
+    assert s.total_energy()[5] == pytest.approx(o.total_energy()[5], abs=1e-7)
