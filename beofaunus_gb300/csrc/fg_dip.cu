@@ -1607,14 +1607,19 @@ int fg_dip_trial_du(fg_dipsys *h, int32_t i, const double *new_xyz, const double
     return FG_OK;
 }
 
-int fg_dip_commit(fg_dipsys *h, int32_t accepted) {
+int fg_dip_commit(fg_dipsys *h, int32_t accepted, double *correction) {
     if (!h) return fail(FG_ERR_INVALID, "null argument");
     if (!h->pending) return fail(FG_ERR_STATE, "no pending trial");
     h->pending = false;
+    if (correction) *correction = 0.0;
     if (!accepted) return FG_OK;
-    int rc = dip_launch(&h, h->d_desc, 1, 2, h->stream);
+    fgd::DipScalars s0, s1;
+    int rc = dip_read_scalars(h, s0);
+    if (!rc) rc = dip_launch(&h, h->d_desc, 1, 2, h->stream);
+    if (!rc) rc = dip_read_scalars(h, s1);
     if (rc) return rc;
-    CK(cudaStreamSynchronize(h->stream));
+    // what update() returns: the reciprocal-energy change of a Q(k) rebuild
+    if (correction) *correction = s1.n_rebuilds > s0.n_rebuilds ? (s1.usum - s0.usum) - s0.pend_du : 0.0;
     return FG_OK;
 }
 

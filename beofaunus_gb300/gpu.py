@@ -125,7 +125,7 @@ def lib(build_if_missing=True):
             "fg_dip_get_state": ([vp, dp, dp], ctypes.c_int),
             "fg_dip_set_threads": ([vp, i32], ctypes.c_int),
             "fg_dip_trial_du": ([vp, i32, dp, dp, dp], ctypes.c_int),
-            "fg_dip_commit": ([vp, i32], ctypes.c_int),
+            "fg_dip_commit": ([vp, i32, dp], ctypes.c_int),
             "fg_dip_sweep": ([vp, i64, dp, dp, dp, dp, dp, dp, dp, dp, dp], ctypes.c_int),
             "fg_dip_stream_upload": ([vp, i64, dp, dp, dp, dp, dp, dp], ctypes.c_int),
             "fg_dip_run_many": ([dp, i32, dp, dp], ctypes.c_int),
@@ -762,7 +762,10 @@ class DipoleSystem:
         return float(du[0])
 
     def commit(self, accepted):
-        _check(lib().fg_dip_commit(self.h, 1 if accepted else 0))
+        """Returns the Q(k) rebuild correction (NonbondedEwald::update)."""
+        c = np.zeros(1)
+        _check(lib().fg_dip_commit(self.h, 1 if accepted else 0, _p(c)))
+        return float(c[0])
 
     def sweep(self, st, log=True):
         kind, idx, axis, angle, disp, u = _dip_stream_arrays(st)

@@ -401,8 +401,10 @@ int fg_dip_set_threads(fg_dipsys *h, int32_t threads);
  * (NULL: unchanged); replaces Energy::energyChange after updateChange
  * (energy.h:3577-3621, ewald.h:651-705). One trial may be pending. */
 int fg_dip_trial_du(fg_dipsys *h, int32_t i, const double *new_xyz, const double *new_mu_unit, double *du);
-/* acceptMove / rejectMove + NonbondedEwald::update (ewald.h:613-646). */
-int fg_dip_commit(fg_dipsys *h, int32_t accepted);
+/* acceptMove / rejectMove + NonbondedEwald::update (ewald.h:613-646);
+ * correction (may be NULL) = what update() returns: the reciprocal-energy
+ * change of a Q(k) rebuild on this accept, else 0. */
+int fg_dip_commit(fg_dipsys *h, int32_t accepted, double *correction);
 /* n trials: kind[t] 1 = AtomicRotation of particle idx[t] by angle[t] about
  * axis[t] (3 per trial), 2 = AtomicTranslation by disp[t] (3 per trial);
  * Metropolis uniform u[t] (reject iff u > exp(-dU/kT)). acc/du may be NULL. */

@@ -20,9 +20,12 @@
 // computed on the device; energyChangeConfiguration (energy.h:3521-3572)
 // therefore sums to the device's dU.
 //
-// AtomicTranslationGPU runs whole sweeps on the device with the same random
+// translateOnDevice runs whole sweeps on the device with the same random
 // draws the reference makes from the global `slump` (move.h:818-864,
-// group.h:129-134, move.h:567-573).
+// group.h:129-134, move.h:567-573). For point dipoles (Space of
+// DipoleParticle), NonbondedEwaldDipoleGPU replaces
+//     Energy::NonbondedEwald<Tspace, Potential::LennardJonesLB, ii, id, dd>
+// and dipoleMovesOnDevice runs AtomicRotation / AtomicTranslation sweeps.
 #ifndef FAUNUS_GB300_ENERGY_HPP
 #define FAUNUS_GB300_ENERGY_HPP
 
@@ -194,6 +197,134 @@ double translateOnDevice(Tspace &spc, NonbondedGPU<Tspace> &pot, int n) {
         spc.p[i].x() = xyz[3 * i];
         spc.p[i].y() = xyz[3 * i + 1];
         spc.p[i].z() = xyz[3 * i + 2];
+        spc.trial[i] = spc.p[i];
+    }
+    return st.energy_change;
+}
+
+// ---------------------------------------------------------------- point dipoles
+// fg_params for NonbondedEwald<Tspace, LennardJonesLB, useIonIon,
+// useIonDipole, useDipoleDipole> on DipoleParticle (ewald.h:228-550): terms is
+// FG_EWALD_ION_ION | FG_EWALD_ION_DIPOLE | FG_EWALD_DIPOLE_DIPOLE as the
+// template flags; quirk 1 computes the sum as the reference's live code does.
+inline fg_params gpuParamsEwaldDipole(Tmjson &j, int terms, int quirk = 0) {
+    fg_params p = gpuParamsEwaldWCA(j);
+    p.model = FG_MODEL_EWALD_DIPOLE;
+    p.ewald_terms = terms;
+    p.ewald_dipole_quirk = quirk;
+    return p;
+}
+
+// Replaces NonbondedEwald<Tspace, LennardJonesLB, ...> in a Space of
+// DipoleParticle for AtomicTranslation and AtomicRotation: the moved
+// particle's whole dU (position and dipole) comes from fg_dip_trial_du.
+template <class Tspace>
+class NonbondedEwaldDipoleGPU : public Energybase<Tspace> {
+    typedef Energybase<Tspace> Tbase;
+    typedef typename Tbase::Tpvec Tpvec;
+    fg_params P;
+    fg_dipsys *h = nullptr;
+    std::vector<int> moved;
+    int lastN = -1;
+    std::string _info() override { return "GB300 dipolar Ewald (faunus_gb300)\n"; }
+
+  public:
+    explicit NonbondedEwaldDipoleGPU(const fg_params &p) : P(p) { Tbase::name = "NonbondedEwald dipoles GB300"; }
+    ~NonbondedEwaldDipoleGPU() override {
+        if (h) fg_dip_destroy(h);
+    }
+    fg_dipsys *handle() { return h; }
+
+    void setSpace(Tspace &s) override {
+        Tbase::setSpace(s);
+        const int n = (int)s.p.size();
+        if (!h || n != lastN) {
+            if (h) fg_dip_destroy(h);
+            fg_check(fg_dip_create(&P, n, &h));
+            lastN = n;
+        }
+        std::vector<double> xyz(3 * n), mu(3 * n), mus(n), q(n);
+        std::vector<int32_t> ids(n);
+        for (int i = 0; i < n; i++) {
+            for (int a = 0; a < 3; a++) {
+                xyz[3 * i + a] = s.p[i][a];
+                mu[3 * i + a] = s.p[i].mu()[a];
+            }
+            mus[i] = s.p[i].muscalar();
+            q[i] = s.p[i].charge;
+            ids[i] = s.p[i].id;
+        }
+        fg_check(fg_dip_set_state(h, xyz.data(), mu.data(), mus.data(), q.data(), ids.data()));
+    }
+
+    double updateChange(const typename Tspace::Change &c) override {
+        moved.clear();
+        for (auto &m : c.mvGroup)
+            for (int i : m.second) moved.push_back(i);
+        return 0;
+    }
+
+    double external(const Tpvec &p) override {
+        if (!Tbase::isTrial(p) || moved.empty()) return 0;
+        if (moved.size() != 1) throw std::runtime_error("NonbondedEwaldDipoleGPU: one moved particle per trial");
+        const int i = moved[0];
+        const double xyz[3] = {p[i].x(), p[i].y(), p[i].z()};
+        const double mu[3] = {p[i].mu().x(), p[i].mu().y(), p[i].mu().z()};
+        double du = 0;
+        fg_check(fg_dip_trial_du(h, i, xyz, mu, &du));
+        return du;
+    }
+
+    double update(bool accepted) override {
+        if (moved.empty()) return 0;
+        double corr = 0;
+        fg_check(fg_dip_commit(h, accepted ? 1 : 0, &corr));
+        moved.clear();
+        return corr;
+    }
+
+    double systemEnergy(const Tpvec &) override {
+        double c[6];
+        fg_check(fg_dip_total_energy(h, c));
+        return c[5];
+    }
+};
+
+// AtomicRotation (rotate = true) or AtomicTranslation sweeps of n trials on
+// the device, with the draws those moves take from the global `slump`
+// (move.h:1008-1032, 818-864, 567-573); positions and dipoles are copied
+// back into Space.
+template <class Tspace>
+double dipoleMovesOnDevice(Tspace &spc, NonbondedEwaldDipoleGPU<Tspace> &pot, int n, bool rotate) {
+    const int N = (int)spc.p.size();
+    std::vector<int32_t> kind(n, rotate ? 1 : 2), idx(n);
+    std::vector<double> axis(3 * (size_t)n), angle(n), disp(3 * (size_t)n), u(n);
+    for (int t = 0; t < n; t++) {
+        slump.range(0, 0);                               // the one atomic group
+        const int i = slump.range(0, N - 1);             // Group::random
+        idx[t] = i;
+        if (rotate) {
+            Point v;
+            v.ranunit(slump);                            // point.h:74-88
+            double dprot = atom[spc.p[i].id].dprot;
+            angle[t] = dprot * slump.half();
+            for (int a = 0; a < 3; a++) axis[3 * t + a] = v[a];
+        } else {
+            const double dp = atom[spc.p[i].id].dp;
+            for (int a = 0; a < 3; a++) disp[3 * t + a] = dp * (slump() - 0.5);
+        }
+        u[t] = slump();                                  // Movebase::metropolis
+    }
+    fg_sweep_stats st{};
+    fg_check(fg_dip_sweep(pot.handle(), n, kind.data(), idx.data(), axis.data(), angle.data(), disp.data(), u.data(),
+                          nullptr, nullptr, &st));
+    std::vector<double> xyz(3 * (size_t)N), mu(3 * (size_t)N);
+    fg_check(fg_dip_get_state(pot.handle(), xyz.data(), mu.data()));
+    for (int i = 0; i < N; i++) {
+        for (int a = 0; a < 3; a++) {
+            spc.p[i][a] = xyz[3 * i + a];
+            spc.p[i].mu()[a] = mu[3 * i + a];
+        }
         spc.trial[i] = spc.p[i];
     }
     return st.energy_change;

@@ -10,6 +10,10 @@ using namespace Faunus;
 typedef Space<Geometry::Cuboid, PointParticle> Tspace;
 template class Faunus::Energy::NonbondedGPU<Tspace>;
 template double Faunus::Energy::translateOnDevice<Tspace>(Tspace &, Faunus::Energy::NonbondedGPU<Tspace> &, int);
+typedef Space<Geometry::Cuboid, DipoleParticle> Tdspace;
+template class Faunus::Energy::NonbondedEwaldDipoleGPU<Tdspace>;
+template double Faunus::Energy::dipoleMovesOnDevice<Tdspace>(Tdspace &, Faunus::Energy::NonbondedEwaldDipoleGPU<Tdspace> &,
+                                                            int, bool);
 
 int main(int argc, char **argv) {
     if (argc < 2) return 0;

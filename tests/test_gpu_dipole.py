@@ -126,7 +126,7 @@ def test_stream_against_oracle(terms, quirk):
 
 def test_plain_trial_commit():
     G = gpu()
-    p, xyz, mu, mus, ids, q = fluid()
+    p, xyz, mu, mus, ids, q = fluid(uf=4)
     s = G.DipoleSystem(p, xyz, mu, mus, ids, charges=q)
     o = OracleDip(p, xyz, mu, mus, ids, q=q)
     rng = np.random.default_rng(2)
@@ -139,8 +139,8 @@ def test_plain_trial_commit():
         du = s.trial_du(i, nx, nm)
         assert du == pytest.approx(o.trial_du(i, nx, nm), abs=DU_TOL)
         acc = bool(t % 4)
-        s.commit(acc)
-        o.commit(acc)
+        c = s.commit(acc)
+        assert c == pytest.approx(o.commit(acc), abs=1e-9)
     assert s.total_energy()[5] == pytest.approx(o.total_energy()[5], abs=1e-8)
 
 
