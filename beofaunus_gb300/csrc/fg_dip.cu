@@ -47,7 +47,8 @@ constexpr int kDipErrLaunch = 64;
 struct DipTrial {
     int32_t idx;   // particle
     int32_t kind;  // 1 rotation (q), 2 translation (t), 3 explicit: position t (absolute), dipole q[1..3]
-    double u;      // Metropolis uniform: reject iff u > exp(-dU / kT) (Movebase::metropolis, move.h:567-573)
+    double thr;    // -ln u of the Metropolis uniform u: reject iff dU > kT thr, i.e. u > exp(-dU / kT)
+                   // (Movebase::metropolis, move.h:567-573); +inf for u = 0
     double q[4];   // rotation quaternion (w, x, y, z)
     int64_t t[3];  // translation (fixed point)
 };
@@ -375,9 +376,11 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
     return s;
 }
 
-__device__ __forceinline__ double surface(const DipDesc &d, const double *M) {
-    return d.surf_c * (M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + 2.0 * (M[0] * M[3] + M[1] * M[4] + M[2] * M[5]) +
-                       M[3] * M[3] + M[4] * M[4] + M[5] * M[5]);
+// c (|Mq|^2 + 2 Mq.Mmu + |Mmu|^2) = c |Mq + Mmu|^2: its change when the sum
+// S = Mq + Mmu moves by D is c (2 S.D + D.D)
+__device__ __forceinline__ double surface_change(const DipDesc &d, const double *M, const double *D) {
+    const double s0 = M[0] + M[3], s1 = M[1] + M[4], s2 = M[2] + M[5];
+    return d.surf_c * (2.0 * (s0 * D[0] + s1 * D[1] + s2 * D[2]) + D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
 }
 
 // Reciprocal energy sum_k A_k Q2(k) of this thread's k-vectors (before recip_c)
@@ -393,7 +396,7 @@ struct DipShared {
     int64_t po[3], pn[3];
     double muo[3], mun[3];
     double ro[3], rn[3];
-    double qa, qeff, mas, u, du, pend;
+    double qa, qeff, mas, thr, du, pend;
     double M[6];
     int idx, ta, kind, accept, rebuild, fixed;
     int qcnt[kDipMaxThreads / 32];
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             const int i = tr.idx;
             S.idx = i;
             S.kind = tr.kind;
-            S.u = tr.u;
+            S.thr = tr.thr;
             S.ta = A.type[i];
             S.qa = d.q[i];
             S.qeff = d.q[i] * d.eff[S.ta];
@@ -569,14 +572,15 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 const int w = e / (3 * st), r = e - w * 3 * st, a = r / st, n = r - a * st;
                 S.tab[w][r] = dc_pack(dc_split(axis_entry(n, w ? S.pn[a] : S.po[a])));
             }
-            if (tid == 0) {
-                for (int a = 0; a < 3; a++) {
+            if (tid < 10) {   // one value per lane
+                if (tid == 9) {
+                    S.qeffd = dsplit(S.qeff);
+                } else {
+                    const int a = tid % 3, w = tid / 3;
                     const double f = d.tpl[a] * S.mas;
-                    S.mo[a] = dsplit(S.muo[a] * f);
-                    S.mn[a] = dsplit(S.mun[a] * f);
-                    S.md[a] = dsplit((S.mun[a] - S.muo[a]) * f);
+                    const double v = w == 0 ? S.muo[a] : (w == 1 ? S.mun[a] : S.mun[a] - S.muo[a]);
+                    (w == 0 ? S.mo : (w == 1 ? S.mn : S.md))[a] = dsplit(v * f);
                 }
-                S.qeffd = dsplit(S.qeff);
             }
             __syncthreads();
             for (int e = tid; e < nw * W2; e += T) {
@@ -712,18 +716,20 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             acc += dval(ek) * d.recip_c;
             const double sum = block_sum(acc, S.red);
             if (tid == 0) {
-                // surface term: running sums before and after the move
-                double Mn[6];
-                for (int a = 0; a < 3; a++) {
-                    Mn[a] = S.M[a] + (d.ion_q ? S.qeff * (S.rn[a] - S.ro[a]) : 0.0);
-                    Mn[3 + a] = S.M[3 + a] + ((d.id || d.dd) ? S.mas * (S.mun[a] - S.muo[a]) : 0.0);
+                // surface term from the running sums (nothing with tin-foil surroundings)
+                double du = sum;
+                if (d.surf_c != 0.0) {
+                    double D[3];
+                    for (int a = 0; a < 3; a++)
+                        D[a] = (d.ion_q ? S.qeff * (S.rn[a] - S.ro[a]) : 0.0) +
+                               ((d.id || d.dd) ? S.mas * (S.mun[a] - S.muo[a]) : 0.0);
+                    du += surface_change(d, S.M, D);
                 }
-                const double du = sum + (surface(d, Mn) - surface(d, S.M));
                 S.du = du;
                 if (!isfinite(du)) sc.error |= kDipErrNonFinite;
                 if (mode == 0) {
                     const double kT = d.kT;
-                    S.accept = !(S.u > exp(-du / kT)) ? 1 : 0;
+                    S.accept = !(du > kT * S.thr) ? 1 : 0;   // NaN dU accepts, as u > exp(NaN) is false
                     if (d.log_du) {
                         d.log_du[t] = du;
                         d.log_acc[t] = (uint8_t)S.accept;
@@ -1281,7 +1287,7 @@ int dip_upload(fg_dipsys *h, int64_t n, const int32_t *kind, const int32_t *idx,
         if (idx[k] < 0 || idx[k] >= h->N) return fail(FG_ERR_INVALID, "trial %lld: particle out of range", (long long)k);
         t.idx = idx[k];
         t.kind = kind[k];
-        t.u = u[k];
+        t.thr = u[k] > 0.0 ? -std::log(u[k]) : INFINITY;
         t.q[0] = 1.0;
         if (kind[k] == 1) {
             if (!axis || !angle) return fail(FG_ERR_INVALID, "rotations need axis and angle");
