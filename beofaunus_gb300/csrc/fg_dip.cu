@@ -190,11 +190,13 @@ struct DipArrays {
     int64_t *pos;
     float4 *pf;
     const int32_t *type;
+    double *mu;
+    const double *mus, *q;
 };
 
 __host__ __device__ inline size_t dip_al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-__host__ __device__ inline size_t dip_stage_layout(int K, int N, int kcc, int ion_q, int dip_q, size_t off[9]) {
+__host__ __device__ inline size_t dip_stage_layout(int K, int N, int kcc, int ion_q, int dip_q, size_t off[12]) {
     size_t b = dip_yz_bytes(kcc);
     off[0] = b;                               // kn
     b = dip_al16(b + (size_t)K * 4);
@@ -213,7 +215,13 @@ __host__ __device__ inline size_t dip_stage_layout(int K, int N, int kcc, int io
     off[7] = b;                               // pf
     b += (size_t)N * 16;
     off[8] = b;                               // type
-    return dip_al16(b + (size_t)N * 4);
+    b = dip_al16(b + (size_t)N * 4);
+    off[9] = b;                               // mu
+    b += (size_t)N * 24;
+    off[10] = b;                              // mus
+    b += (size_t)N * 8;
+    off[11] = b;                              // q
+    return dip_al16(b + (size_t)N * 8);
 }
 
 // cos, sin of 2 pi n X / 2^64: the phase reduced exactly in integers
@@ -426,8 +434,8 @@ __device__ void dip_rebuild(const DipDesc &d, const DipArrays &A, DipShared &S, 
             S.rtab[e] = axis_entry(n, A.pos[3 * j + a]);
         }
         if (tid == 0) {
-            S.rq = d.q[j] * d.eff[A.type[j]];
-            for (int a = 0; a < 3; a++) S.rmu[a] = d.mu[3 * j + a] * d.mus[j];
+            S.rq = A.q[j] * d.eff[A.type[j]];
+            for (int a = 0; a < 3; a++) S.rmu[a] = A.mu[3 * j + a] * A.mus[j];
         }
         __syncthreads();
         for (int k = tid; k < d.K; k += T) {
@@ -463,7 +471,7 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_build_kernel(const DipD
     __shared__ DipShared S;
     double before, after;
     const DipDesc &d = *dp;
-    const DipArrays A = {d.kn, d.akf, d.fqi, d.fqd, d.dqi, d.dqd, d.pos, d.pf, d.type};
+    const DipArrays A = {d.kn, d.akf, d.fqi, d.fqd, d.dqi, d.dqd, d.pos, d.pf, d.type, d.mu, d.mus, d.q};
     dip_rebuild(d, A, S, before, after);
 }
 
@@ -481,9 +489,9 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         if (tid == 0) atomicOr(&d.sc->error, kDipErrLaunch);
         return;
     }
-    DipArrays A = {d.kn, d.akf, d.fqi, d.fqd, d.dqi, d.dqd, d.pos, d.pf, d.type};
+    DipArrays A = {d.kn, d.akf, d.fqi, d.fqd, d.dqi, d.dqd, d.pos, d.pf, d.type, d.mu, d.mus, d.q};
     if (stage) {
-        size_t off[9];
+        size_t off[12];
         dip_stage_layout(d.K, d.N, d.kcc, d.ion_q, d.dip_q, off);
         char4 *kn = reinterpret_cast<char4 *>(dsm + off[0]);
         float2 *akf = reinterpret_cast<float2 *>(dsm + off[1]);
@@ -491,6 +499,8 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         int64_t *pos = reinterpret_cast<int64_t *>(dsm + off[6]);
         float4 *pf = reinterpret_cast<float4 *>(dsm + off[7]);
         int32_t *typ = reinterpret_cast<int32_t *>(dsm + off[8]);
+        double *smu = reinterpret_cast<double *>(dsm + off[9]), *smus = reinterpret_cast<double *>(dsm + off[10]),
+               *sq = reinterpret_cast<double *>(dsm + off[11]);
         for (int k = tid; k < d.K; k += T) {
             kn[k] = A.kn[k];
             akf[k] = A.akf[k];
@@ -503,9 +513,12 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             pos[3 * j + 2] = A.pos[3 * j + 2];
             pf[j] = A.pf[j];
             typ[j] = A.type[j];
+            for (int a = 0; a < 3; a++) smu[3 * j + a] = A.mu[3 * j + a];
+            smus[j] = A.mus[j];
+            sq[j] = A.q[j];
         }
         A = {kn, akf, fqi, fqd, reinterpret_cast<float4 *>(dsm + off[4]), reinterpret_cast<float4 *>(dsm + off[5]), pos,
-             pf, typ};
+             pf, typ, smu, smus, sq};
         __syncthreads();
     }
     DipScalars sc;
@@ -518,21 +531,24 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         t0 = d.sc->cursor;
         t1 = d.sc->n_trials;
     }
+    DipTrial nxt;   // thread 0: the next trial's record, loaded one trial ahead
+    if (tid == 0 && t0 < t1) nxt = d.trials[mode == 0 ? t0 : 0];
     for (int64_t t = t0; t < t1; t++) {
         // ---- the trial (thread 0)
         if (tid == 0) {
-            const DipTrial tr = d.trials[mode == 0 ? t : 0];
+            const DipTrial tr = nxt;
+            if (mode == 0 && t + 1 < t1) nxt = d.trials[t + 1];   // in flight during this trial
             const int i = tr.idx;
             S.idx = i;
             S.kind = tr.kind;
             S.thr = tr.thr;
             S.ta = A.type[i];
-            S.qa = d.q[i];
-            S.qeff = d.q[i] * d.eff[S.ta];
-            S.mas = d.mus[i];
+            S.qa = A.q[i];
+            S.qeff = A.q[i] * d.eff[S.ta];
+            S.mas = A.mus[i];
             for (int a = 0; a < 3; a++) {
                 S.po[a] = A.pos[3 * i + a];
-                S.muo[a] = d.mu[3 * i + a];
+                S.muo[a] = A.mu[3 * i + a];
                 S.pn[a] = S.po[a];
                 S.mun[a] = S.muo[a];
             }
@@ -556,10 +572,11 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                     S.mun[a] = tr.q[1 + a];
                 }
             }
-            for (int a = 0; a < 3; a++) {
-                S.ro[a] = (double)S.po[a] * d.s64[a];
-                S.rn[a] = (double)S.pn[a] * d.s64[a];
-            }
+            if (d.surf_c != 0.0)   // positions in Angstrom for the surface sums only
+                for (int a = 0; a < 3; a++) {
+                    S.ro[a] = (double)S.po[a] * d.s64[a];
+                    S.rn[a] = (double)S.pn[a] * d.s64[a];
+                }
             S.fixed = (S.pn[0] == S.po[0] && S.pn[1] == S.po[1] && S.pn[2] == S.po[2]) ? 1 : 0;
         }
         __syncthreads();
@@ -650,9 +667,9 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 double mb[3];
                 for (int a = 0; a < 3; a++) {
                     pj[a] = A.pos[3 * j + a];
-                    mb[a] = d.mu[3 * j + a];
+                    mb[a] = A.mu[3 * j + a];
                 }
-                const double qb = d.q[j], mbs = d.mus[j];
+                const double qb = A.q[j], mbs = A.mus[j];
                 double ro[3];
                 for (int a = 0; a < 3; a++) ro[a] = (double)(int64_t)((uint64_t)S.po[a] - (uint64_t)pj[a]) * d.s64[a];
                 if (fixed) {
@@ -766,8 +783,9 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             }
             for (int a = 0; a < 3; a++) {
                 A.pos[3 * i + a] = S.pn[a];
-                d.mu[3 * i + a] = S.mun[a];
-                if (d.ion_q) S.M[a] += S.qeff * (S.rn[a] - S.ro[a]);
+                A.mu[3 * i + a] = S.mun[a];
+                if (stage) d.mu[3 * i + a] = S.mun[a];
+                if (d.ion_q && d.surf_c != 0.0) S.M[a] += S.qeff * (S.rn[a] - S.ro[a]);
                 if (d.id || d.dd) S.M[3 + a] += S.mas * (S.mun[a] - S.muo[a]);
             }
             sc.n_accepted++;
@@ -1175,7 +1193,7 @@ size_t dip_launch_smem(fg_dipsys *const *sys, int n, int &stage) {
     size_t yz = 0, st = 0;
     for (int i = 0; i < n; i++) {
         const fgd::DipDesc &d = sys[i]->desc;
-        size_t off[9];
+        size_t off[12];
         yz = std::max(yz, fgd::dip_yz_bytes(d.kcc));
         st = std::max(st, fgd::dip_stage_layout(d.K, d.N, d.kcc, d.ion_q, d.dip_q, off));
     }
