@@ -9,14 +9,19 @@ this path). One "step" = one sweep (16384 AtomicTranslation trials) of every
 system.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload rpm16k|rpm800|pt64|molecules|serving]
+                  [--workload rpm16k|rpm800|pt64|molecules|serving|dipoles]
 
 The default workload is the batched 16384-ion Ewald one below; the others
 measure the remaining configurations of the path the same way (one JSON line
 each): rpm800 = 800-ion Ewald systems (L = 60, |n|^2 <= 49), pt64 = 64-replica
 Debye-Hueckel + LJ parallel tempering, molecules = 1000 rigid 20-site dipolar
 molecules per system (TranslateRotate), serving = Poisson job stream through
-the continuous-batching server with p50/p99 job latency.
+the continuous-batching server with p50/p99 job latency, dipoles = point
+dipoles under the dipolar Ewald sum (AtomicRotation + AtomicTranslation).
+
+Under torchrun (N > 1) every rank runs its own replicas (distinct seeds, no
+data-path exchange); value = all ranks' trials over the slowest rank's time
+(reduce_sum_max / reduce_rate).
 
 value         batched: B independent systems (default B = number of SMs, one
               persistent CTA per system) advanced by the batched sweep; each
@@ -356,15 +361,7 @@ def run_ours(args, rank, world):
     trials = sum(st["trials"] for st in stats)
     accepted = sum(st["accepted"] for st in stats)
     rebuilds = sum(st["rebuilds"] for st in stats)
-    if dist:
-        t = torch.tensor([float(trials), dev_ms], dtype=torch.float64, device=dev)
-        tr = t[:1].clone()
-        dist.all_reduce(tr)
-        mx = t[1:].clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        all_trials, max_ms = tr.item(), mx.item()
-    else:
-        all_trials, max_ms = float(trials), dev_ms
+    all_trials, max_ms = reduce_sum_max(dist, trials, dev_ms, dev)
     value = all_trials / (max_ms / 1e3)
 
     if args.value_only:
@@ -391,13 +388,7 @@ def run_ours(args, rank, world):
         e2e_gathers += tot["kernel_launches"] - 1 - 3 * tot["sweep_launches"]
         del host
     pool.shutdown()
-    e2e = e2e_trials / e2e_s
-    if dist:
-        t = torch.tensor([float(e2e_trials)], dtype=torch.float64, device=dev)
-        dist.all_reduce(t)
-        m = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(m, op=dist.ReduceOp.MAX)
-        e2e = t.item() / m.item()
+    e2e = reduce_rate(dist, e2e_trials, e2e_s, dev)
 
     # ---- roofline of the dominant kernel (sweep kernel), FP32 pipe
     K = systems[0].num_kvectors
@@ -542,6 +533,31 @@ def gpu_setup(args):
     return torch, dev, local, torch.cuda.get_device_properties(dev).multi_processor_count
 
 
+def reduce_sum_max(dist, total, slowest, device):
+    """(sum over ranks of total, max over ranks of slowest); dist None = one process."""
+    if dist is None:
+        return float(total), float(slowest)
+    import torch
+    t = torch.tensor([float(total)], dtype=torch.float64, device=device)
+    dist.all_reduce(t)
+    m = torch.tensor([float(slowest)], dtype=torch.float64, device=device)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    return t.item(), m.item()
+
+
+def reduce_rate(dist, trials, seconds, device):
+    """Whole-job rate over ranks (replicas only: no data-path exchange): all
+    ranks' trials over the slowest rank's time."""
+    n, t = reduce_sum_max(dist, trials, seconds, device)
+    return n / t
+
+
+def job_dist():
+    """torch.distributed when this run has more than one rank, else None."""
+    import torch.distributed as dist
+    return dist if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1 else None
+
+
 # ----------------------------------------------------------------- 800-ion Ewald
 def run_rpm800(args, rank, world):
     import numpy as np
@@ -573,7 +589,7 @@ def run_rpm800(args, rank, world):
     clk = clocks.stop()
     ms = sum(st["device_ms"] for st in stats)
     trials = sum(st["trials"] for st in stats)
-    value = trials / (ms / 1e3)
+    value = reduce_rate(job_dist(), trials, ms / 1e3, dev)
     # e2e: host mt19937 streams in, scalars out
     e2e_s, e2e_t = 0.0, 0
     for s_ in range(steps):
@@ -608,7 +624,7 @@ def run_rpm800(args, rank, world):
            "l2": "L2 flushed (256 MiB write) between timed steps"}
     out = base_line(value, steps, warm, ms / steps, world, cfg, "f32 pair and k terms; df sums; int64 Q(k)",
                     "synthetic (seeded overlap-free starts)")
-    out.update({"e2e": {"value": e2e_t / e2e_s, "unit": UNIT, "h2d_bytes_per_step": B * T * 40,
+    out.update({"e2e": {"value": reduce_rate(job_dist(), e2e_t, e2e_s, dev), "unit": UNIT, "h2d_bytes_per_step": B * T * 40,
                         "d2h_bytes_per_step": B * SYS_SCALARS_BYTES * 2},
                 "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
                 "single_chain": {"value": single, "unit": UNIT}, "plain_per_trial_api": {"value": plain, "unit": UNIT},
@@ -647,7 +663,7 @@ def run_pt(args, rank, world):
     clk = clocks.stop()
     ms = sum(st["device_ms"] for st in stats)
     trials = sum(st["trials"] for st in stats)
-    value = trials / (ms / 1e3)
+    value = reduce_rate(job_dist(), trials, ms / 1e3, dev)
     state = batch.pt_state()
     acc_swaps = [int(a) for a in state["accepts"][:63]]
     att_swaps = [int(a) for a in state["attempts"][:63]]
@@ -737,7 +753,7 @@ def run_molecules(args, rank, world):
     clk = clocks.stop()
     ms = sum(st["device_ms"] for st in stats)
     trials = sum(st["trials"] for st in stats)
-    value = trials / (ms / 1e3)
+    value = reduce_rate(job_dist(), trials, ms / 1e3, dev)
     # e2e: host draws (the reference's mt19937) uploaded inside the timed region
     e2e_s, e2e_t = 0.0, 0
     for s_ in range(steps):
@@ -795,7 +811,7 @@ def run_molecules(args, rank, world):
     out = base_line(value, steps, warm, ms / steps, world, cfg,
                     "f32 pair terms; exact int64 r^2 differences near; FP64 rigid rotation; df sums",
                     "synthetic (seeded molecules, reference mt19937 TranslateRotate draws)")
-    out.update({"e2e": {"value": e2e_t / e2e_s, "unit": UNIT, "h2d_bytes_per_step": B * T * 80,
+    out.update({"e2e": {"value": reduce_rate(job_dist(), e2e_t, e2e_s, dev), "unit": UNIT, "h2d_bytes_per_step": B * T * 80,
                         "d2h_bytes_per_step": B * 48},
                 "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -892,7 +908,7 @@ def run_dipoles(args, rank, world):
     clk = clocks.stop()
     ms = sum(st["device_ms"] for st in stats)
     trials = sum(st["trials"] for st in stats)
-    value = trials / (ms / 1e3)
+    value = reduce_rate(job_dist(), trials, ms / 1e3, dev)
     acc = sum(st["accepted"] for st in stats) / trials
     # e2e: the reference's draws made on the host and uploaded inside the timed region
     e2e_s, e2e_t = 0.0, 0
@@ -947,7 +963,7 @@ def run_dipoles(args, rank, world):
            "acceptance": acc, "l2": "L2 flushed (256 MiB write) between timed steps"}
     out = base_line(value, steps, warm, ms / steps, world, cfg, "f64 pairs near, double-float k-space, f32 far pairs",
                     "synthetic (seeded dipolar fluid, reference mt19937 AtomicRotation/AtomicTranslation draws)")
-    out.update({"e2e": {"value": e2e_t / e2e_s, "unit": UNIT, "h2d_bytes_per_step": B * T * 72,
+    out.update({"e2e": {"value": reduce_rate(job_dist(), e2e_t, e2e_s, dev), "unit": UNIT, "h2d_bytes_per_step": B * T * 72,
                         "d2h_bytes_per_step": B * 2 * 96},
                 "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
