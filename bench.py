@@ -590,19 +590,18 @@ def run_rpm800(args, rank, world):
     ms = sum(st["device_ms"] for st in stats)
     trials = sum(st["trials"] for st in stats)
     value = reduce_rate(job_dist(), trials, ms / 1e3, dev)
-    # e2e: host mt19937 streams in (uploads from a thread pool, as the
-    # default workload does), scalars out
+    # e2e: host mt19937 streams in, scalars out (800-trial streams: a thread
+    # pool costs more than it saves here)
     e2e_s, e2e_t = 0.0, 0
-    pool = cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1))
     for s_ in range(steps):
         host = [systems[b].draw_translation_stream(7000 + 100 * s_ + b, T) for b in range(B)]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        list(pool.map(lambda b: batch.stream_upload(b, *host[b]), range(B)))
+        for b in range(B):
+            batch.stream_upload(b, *host[b])
         _, tot = batch.run()
         e2e_s += time.perf_counter() - t0
         e2e_t += tot["trials"]
-    pool.shutdown()
     one = systems[0]
     one.stream_philox(4 * T, 5)
     r1 = one.stream_run()
