@@ -57,6 +57,7 @@ import re
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -103,7 +104,8 @@ class ClockSampler:
     def __init__(self, dev=0):
         self.p = None
         self.dev = dev
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % dev)
+        # raw samples; the summary goes into the JSON line
+        self.path = os.path.join(os.environ.get("FG_CLOCKS_DIR", tempfile.gettempdir()), "clocks_bench_%d.csv" % dev)
 
     def start(self):
         try:
