@@ -196,3 +196,33 @@ def test_large_system_unstaged():
     agree(r["du"], r["acc"], ro["du"], ro["acc"], st["u"])
     assert r["accepted"] > 30
     assert s.total_energy()[5] == pytest.approx(o.total_energy()[5], abs=1e-7)
+
+
+@pytest.mark.parametrize("case", ["stockmayer_input", "two_particles", "no_dipoles"])
+def test_edge_cases(case):
+    """The reference's Stockmayer input as written (useDipoleDipole only, the
+    live code, cutoffK 0: no k-vectors), the smallest system, and a system
+    whose dipoles are all zero."""
+    G = gpu()
+    if case == "stockmayer_input":
+        p, xyz, mu, mus, ids, q = workloads.dipolar_fluid(n=100, seed=5, kc=0.0, terms=4, quirk=1)
+        dprot = 270.0 * np.pi / 180.0
+    elif case == "two_particles":
+        p, xyz, mu, mus, ids, q = workloads.dipolar_fluid(n=2, seed=6, box=8.0, kc=3.0, terms=7, n_ions=1)
+        p.bjerrum = 60.0
+        dprot = 2.0
+    else:
+        p, xyz, mu, mus, ids, q = workloads.dipolar_fluid(n=80, seed=7, kc=4.0, terms=7, n_ions=80)
+        p.bjerrum = 20.0
+        dprot = 2.0
+    s = G.DipoleSystem(p, xyz, mu, mus, ids, charges=q)
+    o = OracleDip(p, xyz, mu, mus, ids, q=q)
+    assert s.num_kvectors == o.num_kvectors
+    if case == "stockmayer_input":
+        assert s.num_kvectors == 0
+    assert s.total_energy() == pytest.approx(o.total_energy(), abs=1e-8)
+    st = G.dip_draw_stream(3, len(ids), 1000, p_rotate=0.5, dp=0.7, dprot=dprot)
+    r = s.sweep(st)
+    ro = o.run_stream(st)
+    agree(r["du"], r["acc"], ro["du"], ro["acc"], st["u"])
+    assert r["accepted"] > 0
