@@ -404,9 +404,9 @@ struct DipShared {
     int64_t po[3], pn[3];
     double muo[3], mun[3];
     double ro[3], rn[3];
-    double qa, qeff, mas, thr, du, pend;
+    double qa, qeff, mas, thr, du;
     double M[6];
-    int idx, ta, kind, accept, rebuild, fixed;
+    int idx, ta, accept, rebuild, fixed;
     int qcnt[kDipMaxThreads / 32];
     double red[kDipMaxThreads / 32];
     float4 tab[2][3 * (kDipMaxKcc + 1)];    // moved particle, old and new (df complex)
@@ -540,7 +540,6 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             if (mode == 0 && t + 1 < t1) nxt = d.trials[t + 1];   // in flight during this trial
             const int i = tr.idx;
             S.idx = i;
-            S.kind = tr.kind;
             S.thr = tr.thr;
             S.ta = A.type[i];
             S.qa = A.q[i];
