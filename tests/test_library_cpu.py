@@ -65,3 +65,25 @@ def test_oracle_philox_matches_library():
         c = rng.integers(0, 2 ** 32, 4, dtype=np.uint64).astype(np.uint32)
         k = rng.integers(0, 2 ** 32, 2, dtype=np.uint64).astype(np.uint32)
         np.testing.assert_array_equal(philox(c, k), philox4x32_10(c, k))
+
+
+def test_dipole_draws_match_oracle():
+    """fg_dip_draw_stream (host code in the library) and the oracle's
+    restatement of the reference's AtomicRotation / AtomicTranslation draws
+    give the same trials, both with drawn and with given move kinds."""
+    from beofaunus_gb300.gpu import dip_draw_stream, mol_draw_stream
+    from oracle.oracle import dip_stream, mol_stream
+    a = dip_draw_stream(5489, 100, 4000, p_rotate=0.4, dp=0.7, dprot=4.7)
+    b = dip_stream(5489, 100, 4000, 0.4, 0.7, 4.7)
+    for k in ("kind", "idx", "axis", "angle", "disp", "u"):
+        np.testing.assert_array_equal(a[k], b[k])
+    kinds = np.tile([1] * 50 + [2] * 50, 20)
+    a = dip_draw_stream(7, 50, len(kinds), dp=0.5, dprot=1.0, kinds=kinds)
+    b = dip_stream(7, 50, len(kinds), 0.0, 0.5, 1.0, kinds=kinds)
+    for k in ("kind", "idx", "axis", "angle", "disp", "u"):
+        np.testing.assert_array_equal(a[k], b[k])
+    np.testing.assert_array_equal(a["kind"], kinds)
+    m1 = mol_draw_stream(11, 1000, 500, 1.0, 0.3, True)
+    m2 = mol_stream(11, 1000, 1.0, 0.3, True, 500)
+    for k in ("group", "axis", "angle", "trans", "u"):
+        np.testing.assert_array_equal(m1[k], m2[k])
