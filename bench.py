@@ -880,15 +880,19 @@ def fp64_gemm_tflops(torch, dev):
 
 
 def run_dipoles(args, rank, world):
-    from beofaunus_gb300.gpu import DipoleSystem, dip_draw_stream, dip_run_many
+    from beofaunus_gb300.gpu import DipoleSystem, dip_autotune, dip_draw_stream, dip_run_many
     torch, dev, local, sms = gpu_setup(args)
     B = args.systems or 4 * sms
     T = args.trials or 2000
     steps, warm = args.steps, args.warmup
     with mp.get_context("spawn").Pool(min(B, os.cpu_count() or 1)) as pool:
         data = pool.map(dipole_fluid, [21 + rank * 1000003 + b for b in range(B)])
-    systems = [DipoleSystem(p, xyz, mu, mus, ids, charges=q, threads=args.dip_threads)
+    systems = [DipoleSystem(p, xyz, mu, mus, ids, charges=q, threads=args.dip_threads or None)
                for (p, xyz, mu, mus, ids, q) in data]
+    # threads per system: the autotuner's choice on clones of these systems
+    # (untimed), unless given
+    tune = dip_autotune(systems, 256) if not args.dip_threads else None
+    threads = tune["chosen"] if tune else args.dip_threads
     p0 = data[0][0]
     K = systems[0].num_kvectors
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
@@ -959,7 +963,7 @@ def run_dipoles(args, rank, world):
     achieved = flop * value / 1e12
     fp32_peak = fp32_gemm_tflops(torch, dev)
     fp64_peak = fp64_gemm_tflops(torch, dev)
-    cfg = {"workload": WORKLOAD_NAMES["dipoles"], "systems": B, "threads_per_system": args.dip_threads,
+    cfg = {"workload": WORKLOAD_NAMES["dipoles"], "systems": B, "threads_per_system": threads, "autotune": tune,
            "particles_per_system": DIP_N, "box_A": L,
            "dipole_eA": 1.652, "sigma_A": 2.8863, "lj_eps_kT": float(p0.type_eps[0]), "bjerrum_A": p0.bjerrum,
            "ewald_alpha": p0.ewald_alpha, "ewald_cutoff_A": p0.ewald_cutoff, "ewald_cutoff_k": p0.ewald_cutoff_k,
@@ -1136,7 +1140,8 @@ def main():
     ap.add_argument("--round-pairs", type=int, default=1 << 24, help="serving: pair evaluations per job per round")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample per core")
     ap.add_argument("--ref-seconds", type=float, default=3.0, help="reference arm: seconds per step")
-    ap.add_argument("--dip-threads", type=int, default=64, help="dipoles: threads per system (one CTA)")
+    ap.add_argument("--dip-threads", type=int, default=0,
+                    help="dipoles: threads per system (one CTA); 0 = the autotuner's choice")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tune-trials", type=int, default=512,
                     help="pt64/serving: trials per member per autotuner candidate (0: no tuning)")

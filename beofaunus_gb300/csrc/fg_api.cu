@@ -304,6 +304,7 @@ int dh_block_max_cluster() {
 std::mutex g_tune_mu;
 std::map<int, int> g_tune_dh_ctas;   // floor(log2 N) -> CTAs
 int g_tune_min_per_cta = 256;
+int g_tune_dip_threads = 0;          // threads per point-dipole system (0: built-in default)
 
 int size_class(int N) {
     int c = 0;

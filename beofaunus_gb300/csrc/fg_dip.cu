@@ -856,7 +856,7 @@ struct fg_dipsys {
     fg_params P{};
     int N = 0, K = 0, kcc = 0;
     int device = 0;
-    int threads = 128;
+    int threads = 64;   // two warps per system: several systems share an SM
     cudaStream_t stream = nullptr;
     fgd::DipDesc desc{};
     fgd::DipDesc *d_desc = nullptr;
@@ -1364,6 +1364,10 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     h->P = P;
     h->N = n_particles;
     h->kcc = kcc;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (g_tune_dip_threads) h->threads = g_tune_dip_threads;
+    }
     auto bail = [&](int rc) {
         dip_free(h);
         delete h;
@@ -1742,5 +1746,68 @@ int fg_dip_draw_stream(uint32_t seed, int32_t n_particles, int64_t n, double p_r
 }
 
 int64_t fg_dip_device_bytes(fg_dipsys *h) { return h ? (int64_t)h->device_bytes : 0; }
+
+// Threads per system (32, 64, 128, 256) timed on clones of the caller's
+// systems run side by side, the way fg_dip_run_many runs them: every clone
+// takes the same host-drawn stream of n_trials (half rotations, half
+// translations) per candidate; the fastest aggregate rate is applied to the
+// caller's systems and recorded for systems created afterwards. The caller's
+// chains do not advance.
+int fg_dip_autotune(fg_dipsys *const *systems, int32_t n_systems, int64_t n_trials, fg_tune_report *report) {
+    if (!systems || n_systems < 1) return fail(FG_ERR_INVALID, "no systems");
+    if (n_trials < 32) return fail(FG_ERR_INVALID, "n_trials must be >= 32");
+    if (report) *report = fg_tune_report{};
+    std::vector<fg_dipsys *> c(n_systems, nullptr);
+    auto drop = [&](int rc) {
+        for (fg_dipsys *x : c)
+            if (x) fg_dip_destroy(x);
+        return rc;
+    };
+    for (int i = 0; i < n_systems; i++) {
+        fg_dipsys *h = systems[i];
+        if (!h || !h->state_set) return drop(fail(FG_ERR_STATE, "system %d has no state", i));
+        std::vector<double> xyz, mu;
+        int rc = dip_get_state(h, xyz, mu);
+        if (!rc) rc = fg_dip_create(&h->P, h->N, &c[i]);
+        if (!rc) rc = fg_dip_set_state(c[i], xyz.data(), mu.data(), h->mus_h.data(), h->charges_h.data(),
+                                       h->types_h.data());
+        if (rc) return drop(rc);
+    }
+    std::vector<std::pair<int, double>> t;
+    const int cand[4] = {32, 64, 128, 256};
+    for (int ci = 0; ci < 4; ci++) {
+        const int T = cand[ci];
+        int rc = FG_OK;
+        for (int pass = 0; pass < 2 && !rc; pass++) {   // warm-up, then timed
+            for (int i = 0; i < n_systems && !rc; i++) {
+                const int N = c[i]->N;
+                const int64_t n = pass ? n_trials : std::max<int64_t>(32, n_trials / 4);
+                std::vector<int32_t> kind(n), idx(n);
+                std::vector<double> axis(3 * n), angle(n), disp(3 * n), u(n);
+                rc = fg_dip_draw_stream(0x7e57u + 977u * (uint32_t)i + (uint32_t)pass, N, n, 0.5, 0.5, 1.0,
+                                        kind.data(), idx.data(), axis.data(), angle.data(), disp.data(), u.data());
+                if (!rc) rc = fg_dip_set_threads(c[i], T);
+                if (!rc) rc = fg_dip_stream_upload(c[i], n, kind.data(), idx.data(), axis.data(), angle.data(),
+                                                   disp.data(), u.data());
+            }
+            fg_sweep_stats st{};
+            if (!rc) rc = fg_dip_run_many(c.data(), n_systems, nullptr, &st);
+            if (!rc && pass) {
+                const double us = st.trials > 0 ? st.device_ms * 1e3 / (double)st.trials : 0.0;
+                t.push_back({T, us});
+                report_add(report, T, us);
+            }
+        }
+        if (rc) return drop(rc);
+    }
+    const int best = report_pick(report, t);
+    const int T = t[best].first;
+    for (int i = 0; i < n_systems; i++) systems[i]->threads = T;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_dip_threads = T;
+    }
+    return drop(FG_OK);
+}
 
 }  // extern "C"

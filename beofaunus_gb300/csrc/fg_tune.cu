@@ -212,6 +212,7 @@ int fg_tune_reset(void) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_dh_ctas.clear();
     g_tune_min_per_cta = 256;
+    g_tune_dip_threads = 0;
     return FG_OK;
 }
 

@@ -134,6 +134,7 @@ def lib(build_if_missing=True):
             "fg_dip_total_energy": ([vp, dp], ctypes.c_int),
             "fg_dip_running_energy": ([vp, dp], ctypes.c_int),
             "fg_dip_device_bytes": ([vp], ctypes.c_int64),
+            "fg_dip_autotune": ([dp, i32, i64, dp], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -693,6 +694,15 @@ def dip_draw_stream(seed, n_particles, n, p_rotate=0.5, dp=0.7, dprot=1.0, kinds
 def _dip_stream_arrays(st):
     return [np.ascontiguousarray(st[k], dtype=np.int32 if k in ("kind", "idx") else np.float64)
             for k in ("kind", "idx", "axis", "angle", "disp", "u")]
+
+
+def dip_autotune(systems, n_trials=256):
+    """Threads per system timed on clones of these DipoleSystems run together
+    (fg_dip_autotune); the fastest is applied to them and remembered."""
+    arr = (ctypes.c_void_p * len(systems))(*[s.h.value for s in systems])
+    r = TuneReport()
+    _check(lib().fg_dip_autotune(ctypes.cast(arr, ctypes.c_void_p), len(systems), int(n_trials), ctypes.byref(r)))
+    return r.as_dict()
 
 
 def dip_run_many(systems):

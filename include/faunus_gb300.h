@@ -425,6 +425,10 @@ int fg_dip_total_energy(fg_dipsys *h, double *comp);
 /* Total energy at fg_dip_set_state plus accepted dU and rebuild corrections since. */
 int fg_dip_running_energy(fg_dipsys *h, double *u);
 int64_t fg_dip_device_bytes(fg_dipsys *h);
+/* Autotuner (see fg_autotune): threads per system, timed on clones of the
+ * given systems run together (n_trials each per candidate); applied to them
+ * and recorded for dipole systems created afterwards. */
+int fg_dip_autotune(fg_dipsys *const *systems, int32_t n_systems, int64_t n_trials, fg_tune_report *report);
 
 #ifdef __cplusplus
 }

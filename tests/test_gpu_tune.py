@@ -125,3 +125,27 @@ def test_dh_batch_mixes_one_cta_variants():
     ro = o.mc_run_stream(idx, disp, u)
     assert per[0]["accepted"] == int(ro["acc"].sum())
     np.testing.assert_allclose(systems[0].positions(), o.positions(), rtol=0, atol=1e-9)
+
+
+def test_dipole_autotune_threads():
+    """fg_dip_autotune times 32..256 threads per system on clones run together,
+    applies the fastest to the caller's systems (whose chains do not advance)
+    and makes it the default for new dipole systems."""
+    from beofaunus_gb300 import gpu, workloads
+    systems = []
+    for k in range(6):
+        p, xyz, mu, mus, ids, q = workloads.dipolar_fluid(n=80, seed=50 + k, kc=4.0)
+        systems.append(gpu.DipoleSystem(p, xyz, mu, mus, ids, charges=q))
+    e0 = [s.total_energy()[5] for s in systems]
+    x0 = [s.state()[0] for s in systems]
+    r = gpu.dip_autotune(systems, 128)
+    assert [c[0] for c in r["candidates"]] == [32, 64, 128, 256]
+    assert all(c[1] > 0 for c in r["candidates"])
+    assert r["chosen"] == min(r["candidates"], key=lambda c: c[1])[0]
+    for s, e, x in zip(systems, e0, x0):
+        assert s.total_energy()[5] == e
+        assert (s.state()[0] == x).all()
+    # the tuned threads run the caller's systems, and new systems start from them
+    st = gpu.dip_draw_stream(1, 80, 200)
+    assert systems[0].sweep(st)["trials"] == 200
+    gpu.tune_reset()
