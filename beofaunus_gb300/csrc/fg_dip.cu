@@ -1609,6 +1609,7 @@ int fg_dip_trial_du(fg_dipsys *h, int32_t i, const double *new_xyz, const double
     if (!h || !new_xyz || !du) return fail(FG_ERR_INVALID, "null argument");
     if (!h->state_set) return fail(FG_ERR_STATE, "fg_dip_set_state first");
     if (h->pending) return fail(FG_ERR_STATE, "a trial is pending: commit it first");
+    if (h->n_stream > 0) return fail(FG_ERR_STATE, "a staged stream is waiting: run it first");
     if (i < 0 || i >= h->N) return fail(FG_ERR_INVALID, "particle out of range");
     fgd::DipTrial t{};
     t.idx = i;

@@ -170,6 +170,10 @@ def test_invalid_arguments():
     s = G.DipoleSystem(p, xyz, mu, mus, ids, charges=q)
     with pytest.raises(G.FgError):
         s.commit(True)   # nothing pending
+    s.stream_upload(G.dip_draw_stream(2, 20, 5))
+    with pytest.raises(G.FgError):
+        s.trial_du(0, xyz[0], mu[0])   # the staged stream would be overwritten
+    G.dip_run_many([s])
     st = G.dip_draw_stream(1, 20, 10)
     st["kind"][3] = 7
     with pytest.raises(G.FgError):
