@@ -864,6 +864,7 @@ struct fg_molsys {
     int pending = -1;   // molecule of an evaluated explicit trial awaiting fg_mol_commit
     double pending_du = 0.0;
     int64_t n_stream = 0;   // trials in the staged stream
+    bool staged = false;    // a stream is staged and not yet run (it occupies the trial buffer)
     int64_t acc0 = 0;       // accepted count when the stream was staged
     bool has_cm = false;
     bool state_set = false;
@@ -1131,6 +1132,7 @@ int mol_upload(fg_molsys *h, int64_t n, const int32_t *mol, const double *axis, 
     rc = mol_write_scalars(h, s);
     if (rc) return rc;
     h->n_stream = n;
+    h->staged = true;
     h->desc.log_du = log ? h->log_du : nullptr;
     h->desc.log_acc = log ? h->log_acc : nullptr;
     h->desc.expl_pos = nullptr;
@@ -1195,6 +1197,7 @@ int mol_run(fg_molsys *const *sys, int n, fg_sweep_stats *per, fg_sweep_stats *t
     }
     CK(cudaEventRecord(h0->ev1, st));
     CK(cudaEventSynchronize(h0->ev1));
+    for (int i = 0; i < n; i++) sys[i]->staged = false;
     if (tmp) cudaFree(tmp);
     if (rc) return rc;
     float ms = 0.0f;
@@ -1512,6 +1515,7 @@ int fg_mol_trial_du(fg_molsys *h, int32_t molecule, const double *new_xyz, const
     if (!h || !new_xyz || !du) return fail(FG_ERR_INVALID, "null argument");
     if (!h->state_set) return fail(FG_ERR_STATE, "fg_mol_set_state first");
     if (h->pending >= 0) return fail(FG_ERR_STATE, "a trial is pending: call fg_mol_commit");
+    if (h->staged) return fail(FG_ERR_STATE, "a staged stream is waiting: run it first");
     if (molecule < 0 || molecule >= h->M) return fail(FG_ERR_INVALID, "molecule index out of range");
     std::vector<int64_t> X(3 * (size_t)h->gs);
     for (int s = 0; s < h->gs; s++)

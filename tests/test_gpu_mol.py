@@ -150,6 +150,13 @@ def test_mol_invalid_arguments():
         s.commit(True)   # nothing pending
     with pytest.raises(FgError):
         s.cluster = 3
+    from beofaunus_gb300.gpu import mol_draw_stream, mol_run_many
+    s.stream_upload(mol_draw_stream(1, 10, 8, 1.0, 0.3, True))
+    with pytest.raises(FgError):
+        s.trial_du(0, xyz[:20])   # the staged stream would be overwritten
+    mol_run_many([s])
+    s.trial_du(0, xyz[:20])         # allowed once the stream has run
+    s.commit(False)
 
 
 @pytest.mark.gpu
