@@ -16,26 +16,35 @@
 //
 // Included by fg_api.cu (one translation unit).
 //
-// Work split. One system per CTA; a launch runs many systems (replicas,
-// independent chains) side by side, several CTAs per SM. A trial is a
-// block-wide pass: thread 0 forms the trial (quaternion rotation of mu or
-// fixed-point translation), the threads build the moved particle's per-axis
+// Work split. One system per CTA (64 threads by default; fg_dip_autotune
+// times the choices); a launch runs many systems (replicas, independent
+// chains) side by side, several CTAs per SM, with each system's k-vectors,
+// A_k, Q(k) and particle records staged in shared memory for the launch when
+// they fit. A trial is a block-wide pass: thread 0 forms the trial
+// (quaternion rotation of mu or fixed-point translation; the next trial's
+// record is already loaded), the threads build the moved particle's per-axis
 // phase tables e^{2 pi i n x_a / L_a}, n = 0..kcc, old and new (one sincospi
-// each, from the exact 64-bit phase n X mod 2^64); then each thread sums its
-// share of the N - 1 pair changes and of the K k-vector changes (a k-vector's
-// phase is a product of three table entries), the block reduces in a fixed
-// order, thread 0 decides, and on acceptance the threads that computed a
-// k-vector's Q increments add them to Q(k).
+// each, from the exact 64-bit phase n X mod 2^64) and their (n_y, n_z)
+// products; then the pair loop and the k loop: far pairs are summed where
+// they are found, near pairs are queued per warp in order and evaluated
+// afterwards by consecutive threads; a k-vector's phase is one product of a
+// table entry with an (n_y, n_z) entry. The block reduces in a fixed order,
+// thread 0 decides, and on acceptance the threads that computed a k-vector's
+// Q increments add them to Q(k). A rotation keeps the position: one phase per
+// k-vector and only the pair terms linear in the moved dipole.
 //
 // Precision. The per-trial dU must match the FP64 oracle to 1e-9 kT at Bjerrum
 // lengths of hundreds of Angstrom, where single dipole pairs carry tens of kT.
-// Pair terms, phase tables, surface sums and decisions are FP64. The k-space
-// loop, K terms per trial, runs in double-float (df: an unevaluated sum of
-// two floats, ~48 significant bits) on the FP32 pipe, which on this part
-// issues far more operations per clock than the FP64 pipe: Q(k), its
-// increments, A_k, the phases and k.mu are all df. Positions are 64-bit fixed
-// point (X = x/L 2^64): minimum image is the wrapped integer difference and
-// every translation is exact.
+// Near pairs (inside the radius beyond which no pair term of the state can
+// exceed 1e-4 kT) are FP64, their radial functions from degree-5 tables on
+// r^2 checked to 1e-13 against erfc/exp; far pairs are FP32, summed in
+// double-float. The k loop, K terms per trial, runs in double-float (df: an
+// unevaluated sum of two floats, ~48 significant bits) on the FP32 pipe, which
+// on this part issues far more operations per clock than the FP64 pipe: Q(k),
+// its increments, A_k, the phases and k.mu are all df. Phase tables, surface
+// sums and decisions are FP64. Positions are 64-bit fixed point
+// (X = x/L 2^64): minimum image is the wrapped integer difference and every
+// translation is exact.
 namespace fgd {
 
 constexpr int kDipMaxThreads = 256;
