@@ -378,6 +378,11 @@ def run_ours(args, rank, world):
     # ---- e2e: host streams in, scalars out, wall clock around upload + run
     pool = cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1))
     e2e_s, e2e_trials, e2e_gathers = 0.0, 0, 0
+    # one untimed pass first: upload buffers are allocated on first use
+    warm_host = [systems[b].draw_translation_stream(40000 + b, T) for b in range(B)]
+    list(pool.map(lambda b: batch.stream_upload(b, *warm_host[b]), range(B)))
+    batch.run()
+    del warm_host
     for s in range(steps):
         host = [systems[b].draw_translation_stream(50000 + 1000 * s + b, T) for b in range(B)]
         flush.fill_(s & 0xFF)
@@ -595,6 +600,9 @@ def run_rpm800(args, rank, world):
     # e2e: host mt19937 streams in, scalars out (800-trial streams: a thread
     # pool costs more than it saves here)
     e2e_s, e2e_t = 0.0, 0
+    for b in range(B):   # one untimed pass first: upload buffers are allocated on first use
+        batch.stream_upload(b, *systems[b].draw_translation_stream(6000 + b, T))
+    batch.run()
     for s_ in range(steps):
         host = [systems[b].draw_translation_stream(7000 + 100 * s_ + b, T) for b in range(B)]
         torch.cuda.synchronize()

@@ -104,6 +104,9 @@ struct fg_system {
     float2 *sc_tab = nullptr;
     Trial *trials = nullptr;
     int64_t trials_cap = 0, n_trials = 0;
+    int32_t *raw_idx = nullptr;          // host trial arrays as uploaded (converted on the device)
+    double *raw_disp = nullptr, *raw_u = nullptr;
+    int64_t raw_cap = 0;
     float2 *log_du = nullptr;
     uint8_t *log_acc = nullptr;
     int64_t log_cap = 0;
@@ -131,7 +134,7 @@ void free_all(fg_system *h) {
     void *ptrs[] = {h->d_desc, h->pos64, h->pos4, h->pos_ext, h->cell_ext, h->ptype, h->cell_count, h->cell_pid,
                     h->p_cell, h->p_slot, h->cell_pos, h->kvec, h->core_tab, h->core_tab2, h->kpack, h->qfix,
                     h->qnew, h->sc, h->trial_out, h->corr, h->pair_part, h->req, h->dp_fix, h->sc_tab, h->trials,
-                    h->log_du, h->log_acc, h->kseg};
+                    h->log_du, h->log_acc, h->kseg, h->raw_idx, h->raw_disp, h->raw_u};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -539,21 +542,6 @@ int push_desc(fg_system *h) {
 }
 
 // Host -> device trial records: fixed-point displacement and -ln(u) as df.
-void make_trials(const fg_system *h, int64_t n, const int32_t *idx, const double *disp, const double *u,
-                 std::vector<Trial> &out) {
-    out.resize(n);
-    for (int64_t t = 0; t < n; t++) {
-        Trial &tr = out[t];
-        tr.idx = idx[t];
-        tr.pad = 0;
-        for (int a = 0; a < 3; a++) tr.d[a] = to_fix(disp[3 * t + a], h->P.box[a]);
-        double thr = (u[t] > 0.0) ? -std::log(u[t]) : INFINITY;
-        float hi = (float)thr;
-        tr.thr_hi = hi;
-        tr.thr_lo = std::isfinite(thr) ? (float)(thr - (double)hi) : 0.0f;
-    }
-}
-
 // Pair part of the total energy (device) in kT.
 int pair_energy(fg_system *h, double &out) {
     const int nb = 1024;
@@ -1303,16 +1291,37 @@ int fg_draw_translation_stream(fg_system *h, uint32_t seed, int64_t n, int32_t *
     return FG_OK;
 }
 
+// The caller's arrays are copied as they are and turned into trial records
+// on the device (make_trials_kernel: to_fix for the displacement, -ln u as a
+// float pair for the threshold), so the host does no per-trial work; the copies are stream
+// ordered before any later launch on the system's stream.
 int fg_stream_upload(fg_system *h, int64_t n, const int32_t *idx, const double *disp, const double *u) {
     if (!h || n < 0 || (n > 0 && (!idx || !disp || !u))) return fail(FG_ERR_INVALID, "bad argument");
     for (int64_t t = 0; t < n; t++)
         if (idx[t] < 0 || idx[t] >= h->N) return fail(FG_ERR_INVALID, "particle index out of range at %lld", (long long)t);
     int rc = ensure_trials(h, n, false);
     if (rc) return rc;
-    std::vector<Trial> tr;
-    make_trials(h, n, idx, disp, u, tr);
-    if (n > 0) CK(cudaMemcpyAsync(h->trials, tr.data(), n * sizeof(Trial), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
+    if (n > h->raw_cap) {
+        void *ptrs[] = {h->raw_idx, h->raw_disp, h->raw_u};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+        h->raw_idx = nullptr;
+        h->raw_disp = h->raw_u = nullptr;
+        h->raw_cap = 0;
+        DMALLOC(h->raw_idx, n * sizeof(int32_t));
+        DMALLOC(h->raw_disp, 3 * n * sizeof(double));
+        DMALLOC(h->raw_u, n * sizeof(double));
+        h->raw_cap = n;
+    }
+    if (n > 0) {
+        CK(cudaMemcpyAsync(h->raw_idx, idx, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->raw_disp, disp, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->raw_u, u, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+        fg::make_trials_kernel<<<blocks, 256, 0, h->stream>>>(n, h->raw_idx, h->raw_disp, h->raw_u, h->P.box[0],
+                                                              h->P.box[1], h->P.box[2], h->trials);
+        CK(cudaGetLastError());
+    }
     h->n_trials = n;
     return FG_OK;
 }

@@ -1178,4 +1178,28 @@ __global__ void philox_stream_kernel(const SysDesc *__restrict__ dsc, uint32_t s
     }
 }
 
+// Trial records from the host's arrays (fg_stream_upload): x/L wrapped to [-1/2, 1/2), rounded to 2^-62 and
+// shifted to the 64-bit fixed point; the Metropolis threshold -ln u split
+// into a float pair (+inf for u = 0).
+__global__ void make_trials_kernel(int64_t n, const int32_t *idx, const double *disp, const double *u, double Lx,
+                                   double Ly, double Lz, Trial *out) {
+    const double L[3] = {Lx, Ly, Lz};
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        Trial tr;
+        tr.idx = idx[t];
+        tr.pad = 0;
+        for (int a = 0; a < 3; a++) {
+            double f = disp[3 * t + a] / L[a];
+            f -= floor(f + 0.5);
+            tr.d[a] = (int64_t)((uint64_t)(int64_t)llrint(f * 4611686018427387904.0) << 2);
+        }
+        const double ut = u[t];
+        const double thr = ut > 0.0 ? -log(ut) : __longlong_as_double(0x7ff0000000000000LL);   // +inf
+        const float hi = (float)thr;
+        tr.thr_hi = hi;
+        tr.thr_lo = isfinite(thr) ? (float)(thr - (double)hi) : 0.0f;
+        out[t] = tr;
+    }
+}
+
 }  // namespace fg
