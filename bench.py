@@ -450,7 +450,8 @@ def run_ours(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 pair and k terms; df (~48-bit) sums; int64 fixed-point Q(k)",
+        "dtype": "f32",
+        "precision": "f32 pair and k terms; df (~48-bit) sums; int64 fixed-point Q(k)",
         "data": "synthetic (seeded overlap-free starts; Philox streams, reference mt19937 for e2e)",
         "config": workload_config(B, T),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * T * 40,
@@ -527,7 +528,7 @@ WORKLOAD_NAMES = {"rpm16k": WORKLOAD, "rpm800": "rpm800_ewald_wca_batched", "pt6
 def base_line(metric_value, steps, warm, ms_per_step, world, config, dtype, data):
     return {"metric": METRIC, "value": metric_value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warm,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": dtype, "data": data, "config": config}
+            "dtype": dtype.split()[0], "precision": dtype, "data": data, "config": config}
 
 
 def gpu_setup(args):
@@ -978,7 +979,7 @@ def run_dipoles(args, rank, world):
            "k_vectors": K, "terms": "dipole-dipole (real + reciprocal + surface + self)",
            "dp_A": DIP_DP, "dprot_rad": DIP_DPROT, "p_rotate": 0.5, "trials_per_system_per_step": T,
            "acceptance": acc, "l2": "L2 flushed (256 MiB write) between timed steps"}
-    out = base_line(value, steps, warm, ms / steps, world, cfg, "f64 pairs near, double-float k-space, f32 far pairs",
+    out = base_line(value, steps, warm, ms / steps, world, cfg, "f64 near pairs, double-float k-space, f32 far pairs",
                     "synthetic (seeded dipolar fluid, reference mt19937 AtomicRotation/AtomicTranslation draws)")
     out.update({"e2e": {"value": reduce_rate(job_dist(), e2e_t, e2e_s, dev), "unit": UNIT, "h2d_bytes_per_step": B * T * 72,
                         "d2h_bytes_per_step": B * 2 * 96},
