@@ -230,3 +230,30 @@ def test_edge_cases(case):
     ro = o.run_stream(st)
     agree(r["du"], r["acc"], ro["du"], ro["acc"], st["u"])
     assert r["accepted"] > 0
+
+
+def test_translation_and_rotation_invariance():
+    """With tin-foil surroundings the device energies and every trial's dU are
+    the same for the system shifted through the box or turned by 90 degrees
+    about z (the cubic box, the pairs and the spherical k-set map onto
+    themselves)."""
+    G = gpu()
+    p, xyz, mu, mus, ids, q = fluid(n=90, n_ions=30, seed=12)
+    p.ewald_eps_surf = 0.5
+    L = p.box[0]
+    R = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    variants = [(xyz, mu), (xyz + np.array([2.3, -1.1, 4.7]), mu), (xyz @ R.T, mu @ R.T)]
+    st = G.dip_draw_stream(8, len(ids), 600, p_rotate=0.5, dp=0.7, dprot=2.0)
+    energies, dus = [], []
+    for k, (x, m) in enumerate(variants):
+        x = x - L * np.round(x / L)
+        s = G.DipoleSystem(p, x, m, mus, ids, charges=q)
+        energies.append(s.total_energy()[5])
+        sk = dict(st)
+        if k == 2:   # the same moves, turned with the system
+            sk["axis"] = st["axis"] @ R.T
+            sk["disp"] = st["disp"] @ R.T
+        dus.append(s.sweep(sk)["du"])
+    for e, d in zip(energies[1:], dus[1:]):
+        assert e == pytest.approx(energies[0], abs=1e-8)
+        np.testing.assert_allclose(d, dus[0], rtol=0, atol=1e-8)

@@ -182,3 +182,35 @@ def test_reference_stream_rerun(name):
     np.testing.assert_allclose(r["du"], g["du"], rtol=0, atol=1e-9)
     np.testing.assert_array_equal(r["acc"], g["acc"])
     assert r["usum"] == pytest.approx(float(g["u_move_sum"]), abs=1e-8)
+
+
+def _tinfoil_system(terms, quirk=0, seed=8):
+    p, xyz, mu, mus, ids, q = random_system(terms=terms, quirk=quirk, seed=seed)
+    p.ewald_eps_surf = 0.5   # < 1: tin-foil surroundings, no surface term
+    return p, xyz, mu, mus, ids, q
+
+
+@pytest.mark.parametrize("terms", [7, 5, 4])
+def test_energy_invariant_under_translation(terms):
+    """Periodic Ewald energy does not depend on where the box origin sits."""
+    p, xyz, mu, mus, ids, q = _tinfoil_system(terms)
+    e0 = OracleDip(p, xyz, mu, mus, ids, q=q).total_energy()
+    L = p.box[0]
+    shifted = xyz + np.array([1.37, -2.91, 0.55])
+    shifted -= L * np.round(shifted / L)
+    e1 = OracleDip(p, shifted, mu, mus, ids, q=q).total_energy()
+    np.testing.assert_allclose(e1, e0, rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("terms", [7, 4])
+def test_energy_invariant_under_cubic_rotation(terms):
+    """A 90-degree turn of positions and dipoles about z maps the cubic box,
+    the real-space pairs and the spherical k-set onto themselves."""
+    p, xyz, mu, mus, ids, q = _tinfoil_system(terms)
+    e0 = OracleDip(p, xyz, mu, mus, ids, q=q).total_energy()
+    R = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    L = p.box[0]
+    x1 = xyz @ R.T
+    x1 -= L * np.round(x1 / L)
+    e1 = OracleDip(p, x1, mu @ R.T, mus, ids, q=q).total_energy()
+    np.testing.assert_allclose(e1, e0, rtol=0, atol=1e-9)
