@@ -18,6 +18,7 @@
 //             move kind (1 rotation, 2 translation), particle, trial position
 //             and dipole vector, dU and acceptance.
 //   "bench" : like "mc" without logs; prints trials/s.
+// With "state_file", "mc" also saves the final state (Space::save).
 // "terms" selects the template flags: "ii_dd" (useIonIon, useDipoleDipole, as
 // the unit test) or "ii_id_dd" (all three).
 #include <faunus/faunus.h>
@@ -186,7 +187,20 @@ static void run_mc(const Tmjson &in, Out &out, bool bench) {
     out.set("trials_per_s", trials / secs);
     out.set("u_move_sum", usum);
     out.set("u1", Energy::systemEnergy(spc, pot, spc.p));
+    if (in.count("state_file")) {
+        // Space::save (space.h:736-764) of the final state, DipoleParticle records
+        spc.initTracker();
+        spc.save(in["state_file"].get<std::string>());
+    }
     if (!bench) {
+        std::vector<double> fx, fm;
+        for (auto &a : spc.p)
+            for (int k = 0; k < 3; k++) {
+                fx.push_back(a[k]);
+                fm.push_back(a.mu()[k]);
+            }
+        out.set("final_positions", fx);
+        out.set("final_mu", fm);
         out.set("kind", log.kind);
         out.set("idx", log.idx);
         out.set("trial_xyz", log.xyz);

@@ -175,7 +175,14 @@ def make_dip(exe):
     for name, (kw, terms, seed, sweeps, dprot) in DIP_CASES.items():
         params, xyz, mu, mus, ids, q = workloads.dipolar_fluid(quirk=1, **kw)
         params.bjerrum = 60.0   # acceptance near one half at these step sizes
-        out = run_harness(exe, dip_input("mc", params, xyz, mu, mus, ids, q, seed, sweeps, terms, dprot))
+        d = dip_input("mc", params, xyz, mu, mus, ids, q, seed, sweeps, terms, dprot)
+        extra = {}
+        if name == "dip_fluid":
+            d["state_file"] = "final.state"
+            out, (state,) = run_harness(exe, d, files=["final.state"])
+            extra = dict(state_text=np.frombuffer(state, dtype=np.uint8))
+        else:
+            out = run_harness(exe, d)
         n = len(out["idx"])
         np.savez_compressed(
             os.path.join(HERE, name + ".npz"),
@@ -185,7 +192,9 @@ def make_dip(exe):
             u_move_sum=np.float64(out["u_move_sum"][0]), kind=np.asarray(out["kind"], dtype=np.int32),
             idx=np.asarray(out["idx"], dtype=np.int32), trial_xyz=np.asarray(out["trial_xyz"]).reshape(n, 3),
             trial_mu=np.asarray(out["trial_mu"]).reshape(n, 3), du=np.asarray(out["du"]),
-            acc=np.asarray(out["acc"], dtype=np.uint8))
+            acc=np.asarray(out["acc"], dtype=np.uint8),
+            final_positions=np.asarray(out["final_positions"]).reshape(-1, 3),
+            final_mu=np.asarray(out["final_mu"]).reshape(-1, 3), **extra)
         print(name, "trials", n, "acceptance %.3f" % np.mean(out["acc"]), "u0 %.6f" % out["u0"][0])
 
 

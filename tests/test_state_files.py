@@ -108,3 +108,20 @@ def test_system_state_round_trip(tmp_path):
     np.testing.assert_array_equal(st["ids"], ids + 1)
     t = System(p, st["xyz"], st["charge"], st["ids"] - 1)
     assert t.total_energy()["total"] == pytest.approx(s.total_energy()["total"], abs=1e-9)
+
+
+def test_read_reference_dipole_state(tmp_path):
+    """The DipoleParticle records the reference saved after its AtomicRotation /
+    AtomicTranslation run (tests/golden/dip_fluid.npz) read back as that run's
+    final positions, dipole unit vectors and scalars."""
+    from beofaunus_gb300.gpu import read_state
+    g = np.load(os.path.join(GOLDEN, "dip_fluid.npz"))
+    path = tmp_path / "dip.state"
+    path.write_bytes(bytes(g["state_text"]))
+    st = read_state(path, kind=1)
+    np.testing.assert_allclose(st["xyz"], g["final_positions"], rtol=1e-15, atol=1e-13)
+    np.testing.assert_allclose(st["mu_unit"], g["final_mu"], rtol=1e-15, atol=1e-15)
+    np.testing.assert_array_equal(st["mu_scalar"], g["mus"])
+    np.testing.assert_array_equal(st["charge"], g["q"])
+    np.testing.assert_array_equal(st["ids"], g["ids"] + 1)
+    np.testing.assert_allclose(np.linalg.norm(st["mu_unit"], axis=1), 1.0, atol=1e-12)
