@@ -1293,8 +1293,9 @@ int fg_draw_translation_stream(fg_system *h, uint32_t seed, int64_t n, int32_t *
 
 // The caller's arrays are copied as they are and turned into trial records
 // on the device (make_trials_kernel: to_fix for the displacement, -ln u as a
-// float pair for the threshold), so the host does no per-trial work; the copies are stream
-// ordered before any later launch on the system's stream.
+// float pair for the threshold), so the host does no per-trial work. The call
+// returns when the records are in place: batches and parallel tempering run
+// them from their own stream, and the caller may reuse its arrays.
 int fg_stream_upload(fg_system *h, int64_t n, const int32_t *idx, const double *disp, const double *u) {
     if (!h || n < 0 || (n > 0 && (!idx || !disp || !u))) return fail(FG_ERR_INVALID, "bad argument");
     for (int64_t t = 0; t < n; t++)
@@ -1321,6 +1322,7 @@ int fg_stream_upload(fg_system *h, int64_t n, const int32_t *idx, const double *
         fg::make_trials_kernel<<<blocks, 256, 0, h->stream>>>(n, h->raw_idx, h->raw_disp, h->raw_u, h->P.box[0],
                                                               h->P.box[1], h->P.box[2], h->trials);
         CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(h->stream));
     }
     h->n_trials = n;
     return FG_OK;
