@@ -70,6 +70,10 @@ BOX = 163.0
 SIGMA = 4.0
 WORKLOAD = "rpm16k_ewald_wca_cells_batched"
 SYS_SCALARS_BYTES = 88          # sizeof(SysScalars): one system's per-step read-back
+# what fg_stream_upload copies per trial: the caller's int32 index, three
+# double displacements and one double uniform (the 40-byte trial records are
+# built from them on the device)
+UPLOAD_BYTES_PER_TRIAL = 4 + 3 * 8 + 8
 
 # Cost model of one trial (algorithmic work, FMA = 2 FLOP):
 #   pairs: 2 x 127 ion pairs within the 20 A cutoff (old and new position),
@@ -337,6 +341,14 @@ def run_ours(args, rank, world):
         p, xyz, q, ids = workloads.rpm16k(seed=seeds[b], update_frequency=1000, start=xyzs[b])
         systems.append(System(p, xyz, q, ids))
     batch = Batch(systems)
+    # accuracy inside the timed run: two members log every trial's dU on the
+    # device (a store per trial for 2 of the B systems); the last timed step's
+    # first trials are replayed by the FP64 oracle afterwards
+    chk = sorted({0, B - 1})
+    for m in chk:
+        batch.set_log(m)
+    e64_0 = [] if args.value_only else [s_.total_energy_fp64()["total"] for s_ in systems]
+    run_0 = [] if args.value_only else [s_.running_energy() for s_ in systems]
 
     def device_step(step_seed):
         batch.stream_philox([T] * B, step_seed)        # staged in HBM, untimed
@@ -351,7 +363,12 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
-    stats = [device_step(1000 + s) for s in range(steps)]
+    stats = []
+    for s in range(steps):
+        if s == steps - 1:
+            # start of the checked step (a host read between device-timed steps)
+            chk_start = {m: systems[m].positions() for m in chk}
+        stats.append(device_step(1000 + s))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -374,6 +391,12 @@ def run_ours(args, rank, world):
         if dist:
             dist.destroy_process_group()
         return
+
+    # ---- accuracy of the timed run (checker: the FP64 oracle, after timing)
+    accuracy = accuracy_check(systems, chk, chk_start, min(T, args.check_trials), e64_0, run_0,
+                              (warm + steps) * T)
+    for m in chk:
+        batch.set_log(m, False)
 
     # ---- e2e: host streams in, scalars out, wall clock around upload + run.
     # Each step's inputs (the reference's mt19937 draws, made on the host
@@ -465,7 +488,7 @@ def run_ours(args, rank, world):
         "precision": "f32 pair and k terms; df (~48-bit) sums; int64 fixed-point Q(k)",
         "data": "synthetic (seeded overlap-free starts; Philox streams, reference mt19937 for e2e)",
         "config": workload_config(B, T),
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * T * 40,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * T * UPLOAD_BYTES_PER_TRIAL,
                 "d2h_bytes_per_step": int(round(e2e_gathers / steps)) * B * SYS_SCALARS_BYTES},
         "gpu_launches": int(kernels),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -482,6 +505,8 @@ def run_ours(args, rank, world):
         "batched_over_single_chain": value / single,
         "acceptance": acc_rate,
         "qk_rebuilds": rebuilds,
+        "max_du_err": accuracy["max_du_err"],
+        "accuracy": accuracy,
         "clocks": clk,
     }
     batch.close()
@@ -493,6 +518,46 @@ def run_ours(args, rank, world):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
+
+
+def accuracy_check(systems, members, starts, n, e64_0, run_0, trials_per_system):
+    """dU error of the timed batched run against the FP64 oracle.
+
+    For each checked member the oracle replays the first n trials of the last
+    timed step (the member's Philox stream as staged, read back) from the
+    member's coordinates at the start of that step; the device's own logged
+    dU values of those trials are compared one by one (decisions must agree
+    except inside the 1e-6 kT band). Then every system's running energy is
+    compared with fg_total_energy_fp64: the drift is the difference between
+    the change of the running total (the sum of accepted dU and rebuild
+    corrections) and the change of the FP64 system energy since set-up."""
+    import numpy as np
+
+    from oracle.oracle import compare_chain, replay_chain
+    jobs, dev = [], []
+    for m in members:
+        s = systems[m]
+        idx, disp, u = s.stream_get(0, n)
+        du, acc = s.log_get(0, n)
+        dev.append((du, acc, u))
+        jobs.append((bytes(s.params), starts[m], s.charges, s.type_ids, idx, disp, u))
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        ref = pool.map(replay_chain, jobs)
+    res = [compare_chain(d[0], d[1], r[0], r[1], d[2], 1e-6) for d, r in zip(dev, ref)]
+    drift = []
+    for s, e0, r0 in zip(systems, e64_0, run_0):
+        drift.append(abs((s.running_energy() - r0) - (s.total_energy_fp64()["total"] - e0)))
+    return {"max_du_err": max(r["max_err"] for r in res),
+            "rms_du_err": float(np.sqrt(np.mean([r["rms_err"] ** 2 for r in res]))),
+            "members_checked": members, "trials_checked_per_member": n,
+            "trials_compared": sum(r["compared"] for r in res),
+            "decisions_identical": all(r["decisions_identical"] for r in res),
+            "divergence_in_band": all(r["divergence_in_band"] for r in res),
+            "checked": "the device's own logged dU of the last timed step's first trials of each checked member, "
+                       "against the FP64 oracle replaying the same Philox stream from the same start",
+            "max_energy_drift_kT": max(drift), "drift_systems": len(drift),
+            "drift_trials_per_system": trials_per_system,
+            "drift": "|change of the running total energy - change of the FP64 system energy| since set-up"}
 
 
 def _pt_sizes():
@@ -647,7 +712,7 @@ def run_rpm800(args, rank, world):
            "l2": "L2 flushed (256 MiB write) between timed steps"}
     out = base_line(value, steps, warm, ms / steps, world, cfg, "f32 pair and k terms; df sums; int64 Q(k)",
                     "synthetic (seeded overlap-free starts)")
-    out.update({"e2e": {"value": reduce_rate(job_dist(), e2e_t, e2e_s, dev), "unit": UNIT, "h2d_bytes_per_step": B * T * 40,
+    out.update({"e2e": {"value": reduce_rate(job_dist(), e2e_t, e2e_s, dev), "unit": UNIT, "h2d_bytes_per_step": B * T * UPLOAD_BYTES_PER_TRIAL,
                         "d2h_bytes_per_step": B * SYS_SCALARS_BYTES * 2},
                 "gpu_launches": int(sum(st["kernel_launches"] for st in stats)),
                 "single_chain": {"value": single, "unit": UNIT}, "plain_per_trial_api": {"value": plain, "unit": UNIT},
@@ -1166,6 +1231,8 @@ def main():
     ap.add_argument("--tune-trials", type=int, default=512,
                     help="pt64/serving: trials per member per autotuner candidate (0: no tuning)")
     ap.add_argument("--value-only", action="store_true", help="device-resident value only (profiling)")
+    ap.add_argument("--check-trials", type=int, default=3000,
+                    help="rpm16k: trials per checked member replayed by the FP64 oracle after timing")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

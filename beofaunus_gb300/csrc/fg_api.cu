@@ -110,6 +110,8 @@ struct fg_system {
     float2 *log_du = nullptr;
     uint8_t *log_acc = nullptr;
     int64_t log_cap = 0;
+    int64_t log_n = 0;             // trials of the last logged run (fg_log_get)
+    bool log_batch = false;        // log this member's trials in batch runs (fg_batch_set_log)
     // host-side values
     std::vector<double> ak;
     std::vector<int32_t> types;
@@ -640,6 +642,7 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
     h->desc.log_trials = log ? 1 : 0;
     h->desc.trial_du = h->log_du;
     h->desc.trial_acc = h->log_acc;
+    h->log_n = log ? n : 0;
     rc = push_desc(h);
     if (rc) return rc;
     LaunchCfg cfg;
@@ -1318,7 +1321,7 @@ int fg_stream_upload(fg_system *h, int64_t n, const int32_t *idx, const double *
         CK(cudaMemcpyAsync(h->raw_idx, idx, n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemcpyAsync(h->raw_disp, disp, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemcpyAsync(h->raw_u, u, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        const int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+        const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)dh_sm_count() * 8);
         fg::make_trials_kernel<<<blocks, 256, 0, h->stream>>>(n, h->raw_idx, h->raw_disp, h->raw_u, h->P.box[0],
                                                               h->P.box[1], h->P.box[2], h->trials);
         CK(cudaGetLastError());
@@ -1332,10 +1335,13 @@ int fg_stream_philox(fg_system *h, int64_t n, uint32_t seed, uint32_t stream_id)
     if (!h || n < 0) return fail(FG_ERR_INVALID, "bad argument");
     int rc = ensure_trials(h, n, false);
     if (rc) return rc;
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8));
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)dh_sm_count() * 8));
     if (n > 0)
         fg::philox_stream_kernel<<<blocks, 256, 0, h->stream>>>(h->d_desc, seed, stream_id, 0, n, h->dp_fix, h->trials);
     CK(cudaGetLastError());
+    // as fg_stream_upload: the records are in place on return, because
+    // batches and parallel tempering read them from their own stream
+    CK(cudaStreamSynchronize(h->stream));
     h->n_trials = n;
     return FG_OK;
 }
@@ -1385,6 +1391,20 @@ int fg_sweep(fg_system *h, int64_t n, const int32_t *idx, const double *disp, co
             if (accepted) accepted[t] = a[t];
         }
     }
+    return FG_OK;
+}
+
+int fg_log_get(fg_system *h, int64_t first, int64_t n, double *du, uint8_t *accepted) {
+    if (!h || first < 0 || n < 0) return fail(FG_ERR_INVALID, "bad argument");
+    if (first + n > h->log_n) return fail(FG_ERR_INVALID, "range outside the last logged run (%lld trials)",
+                                          (long long)h->log_n);
+    if (n == 0) return FG_OK;
+    std::vector<float2> d(n);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(d.data(), h->log_du + first, n * sizeof(float2), cudaMemcpyDeviceToHost));
+    if (accepted) CK(cudaMemcpy(accepted, h->log_acc + first, n, cudaMemcpyDeviceToHost));
+    if (du)
+        for (int64_t t = 0; t < n; t++) du[t] = df_val(d[t].x, d[t].y);
     return FG_OK;
 }
 

@@ -167,7 +167,12 @@ int batch_push_descs(fg_batch *b) {
     for (size_t s = 0; s < b->sys.size(); s++) {
         fg_system *h = b->sys[s];
         h->desc.trials = h->trials;
-        h->desc.log_trials = 0;
+        // per-trial log of selected members (fg_batch_set_log), where the
+        // buffers hold the member's whole stream
+        const bool log = h->log_batch && !b->pt && h->log_cap >= h->n_trials;
+        h->desc.log_trials = log ? 1 : 0;
+        h->desc.trial_du = h->log_du;
+        h->desc.trial_acc = h->log_acc;
         v[s] = h->desc;
     }
     CK(cudaMemcpyAsync(b->d_descs, v.data(), v.size() * sizeof(SysDesc), cudaMemcpyHostToDevice, b->stream));
@@ -373,11 +378,28 @@ int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total)
     if (!b) return fail(FG_ERR_INVALID, "null batch");
     const int n = (int)b->sys.size();
     std::vector<int64_t> counts(n);
-    for (int s = 0; s < n; s++) counts[s] = b->sys[s]->n_trials;
+    for (int s = 0; s < n; s++) {
+        fg_system *h = b->sys[s];
+        counts[s] = h->n_trials;
+        h->log_n = 0;
+        if (h->log_batch && !b->pt) {
+            int rc = ensure_trials(h, counts[s], true);
+            if (rc) return rc;
+        }
+    }
     int rc = batch_push_descs(b);
     if (rc) return rc;
     CK(cudaMemcpyAsync(b->d_counts, counts.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
-    return batch_run(b, counts, per_system, total);
+    rc = batch_run(b, counts, per_system, total);
+    for (int s = 0; s < n; s++)
+        if (b->sys[s]->desc.log_trials) b->sys[s]->log_n = counts[s];
+    return rc;
+}
+
+int fg_batch_set_log(fg_batch *b, int32_t member, int32_t on) {
+    if (!b || member < 0 || member >= (int)b->sys.size()) return fail(FG_ERR_INVALID, "bad member");
+    b->sys[member]->log_batch = on != 0;
+    return FG_OK;
 }
 
 // ---------------------------------------------------------------- parallel tempering
@@ -883,6 +905,27 @@ int fg_server_release(fg_server *s, int64_t job_id) {
         fg_job *j = s->jobs[k];
         if (j->id != job_id) continue;
         if (j->state == 1) return fail(FG_ERR_STATE, "job %lld is running", (long long)job_id);
+        delete j;
+        s->jobs.erase(s->jobs.begin() + k);
+        return FG_OK;
+    }
+    return fail(FG_ERR_INVALID, "unknown job %lld", (long long)job_id);
+}
+
+int fg_server_cancel(fg_server *s, int64_t job_id) {
+    if (!s) return fail(FG_ERR_INVALID, "null server");
+    for (size_t k = 0; k < s->jobs.size(); k++) {
+        fg_job *j = s->jobs[k];
+        if (j->id != job_id) continue;
+        // rounds end synchronised (fg_server_step), so no kernel of this job
+        // is in flight here; wait for both streams all the same
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->stream2) CK(cudaStreamSynchronize(s->stream2));
+        if (j->sys) {
+            s->used -= (int64_t)j->bytes;
+            fg_destroy(j->sys);
+            j->sys = nullptr;
+        }
         delete j;
         s->jobs.erase(s->jobs.begin() + k);
         return FG_OK;

@@ -12,7 +12,12 @@
 // The array is shared by all calls: calls that overlap on the GPU (on
 // different streams, or from different host threads) race on it and give
 // wrong results. Nothing in it has to start at zero: every call writes all of
-// it that it later reads.
+// it that it later reads, and clears its error word first.
+//
+// Type ids cannot be checked on the host (they are in device memory): the
+// conversion kernel checks 0 <= t < n_types, records a bad id in the error
+// word and stores type 0 in its place, so no table is read out of range;
+// the final kernel then writes NaN instead of the energy.
 
 namespace fg {
 
@@ -28,14 +33,15 @@ constexpr size_t kNoallocExt = kNoallocPos4 + (size_t)kNoallocMaxParticles * 16;
 constexpr size_t kNoallocType = kNoallocExt + (size_t)kNoallocMaxParticles * 8;
 constexpr size_t kNoallocQtype = noalloc_align16(kNoallocType + (size_t)kNoallocMaxParticles);
 constexpr size_t kNoallocPart = kNoallocQtype + (size_t)FG_MAX_TYPES * 4;
-constexpr size_t kNoallocBytes = kNoallocPart + (size_t)kNoallocBlocks * 8;
+constexpr size_t kNoallocErr = kNoallocPart + (size_t)kNoallocBlocks * 8;
+constexpr size_t kNoallocBytes = kNoallocErr + 16;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 // Caller coordinates (double, Angstrom) -> the fixed-point records the pair
 // kernels read, with the same rounding as the host upload (fg_set_state).
-__global__ void noalloc_convert_kernel(int n, const double *__restrict__ xyz, const double *__restrict__ charge,
-                                       const int32_t *__restrict__ types) {
+__global__ void noalloc_convert_kernel(int n, int n_types, const double *__restrict__ xyz,
+                                       const double *__restrict__ charge, const int32_t *__restrict__ types) {
     SysDesc &d = *reinterpret_cast<SysDesc *>(g_noalloc_scratch + kNoallocDesc);
     int4 *pos4 = reinterpret_cast<int4 *>(g_noalloc_scratch + kNoallocPos4);
     short4 *ext = reinterpret_cast<short4 *>(g_noalloc_scratch + kNoallocExt);
@@ -51,7 +57,11 @@ __global__ void noalloc_convert_kernel(int n, const double *__restrict__ xyz, co
             h[a] = hi32(X);
             e[a] = ext16(X);
         }
-        const int t = types[i];
+        int t = types[i];
+        if (t < 0 || t >= n_types) {
+            atomicOr(reinterpret_cast<int *>(g_noalloc_scratch + kNoallocErr), 1);
+            t = 0;
+        }
         const float q = charge ? (float)charge[i] : qtype[t];
         pos4[i] = make_int4(h[0], h[1], h[2], __float_as_int(q));
         ext[i] = make_short4((short)e[0], (short)e[1], (short)e[2], 0);
@@ -72,7 +82,8 @@ __global__ void noalloc_finish_kernel(double *__restrict__ out) {
         df t = {0.0f, 0.0f};
         if (lane < (int)(blockDim.x >> 5)) t = {red[lane].x, red[lane].y};
         t = warp_sum_df(t);
-        if (lane == 0) out[0] = (double)t.hi + (double)t.lo;
+        const int bad = *reinterpret_cast<const int *>(g_noalloc_scratch + kNoallocErr);
+        if (lane == 0) out[0] = bad ? __longlong_as_double(0x7ff8000000000000LL) : (double)t.hi + (double)t.lo;
     }
 }
 
@@ -220,11 +231,12 @@ int fg_pair_energy_noalloc(const fg_params *params, int32_t n, const double *d_x
     cudaStream_t st = (cudaStream_t)stream;
     CK(cudaMemcpyAsync(base + fg::kNoallocDesc, &d, sizeof(SysDesc), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(base + fg::kNoallocQtype, qtype, sizeof(qtype), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(base + fg::kNoallocErr, 0, 16, st));
     if (ntab > 0) {
         CK(cudaMemcpyAsync(base + fg::kNoallocTab0, t0.data(), ntab * sizeof(float4), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(base + fg::kNoallocTab1, t1.data(), ntab * sizeof(float4), cudaMemcpyHostToDevice, st));
     }
-    fg::noalloc_convert_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, d_xyz, d_charge, d_types);
+    fg::noalloc_convert_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, nt, d_xyz, d_charge, d_types);
     using PairFn = void (*)(const SysDesc *, float2 *);
     PairFn fn = P.model == FG_MODEL_EWALD_WCA ? fg::pair_total_kernel<fg::MODEL_EWALD>
                                                : fg::pair_total_kernel<fg::MODEL_DHLJ>;

@@ -78,6 +78,8 @@ def lib(build_if_missing=True):
             "fg_batch_stream_philox": ([vp, dp, u32, dp], ctypes.c_int),
             "fg_batch_run": ([vp, dp, dp], ctypes.c_int),
             "fg_batch_stream_upload": ([vp, i32, i64, dp, dp, dp], ctypes.c_int),
+            "fg_batch_set_log": ([vp, i32, i32], ctypes.c_int),
+            "fg_log_get": ([vp, i64, i64, dp, dp], ctypes.c_int),
             "fg_pt_setup": ([vp, dp, u32], ctypes.c_int),
             "fg_pt_run": ([vp, i32, i32, dp], ctypes.c_int),
             "fg_pt_get": ([vp, dp, dp, dp, dp], ctypes.c_int),
@@ -87,6 +89,7 @@ def lib(build_if_missing=True):
             "fg_server_step": ([vp, dp, dp, dp], ctypes.c_int),
             "fg_server_poll": ([vp, i64, dp, dp, dp, dp, dp], ctypes.c_int),
             "fg_server_release": ([vp, i64], ctypes.c_int),
+            "fg_server_cancel": ([vp, i64], ctypes.c_int),
             "fg_server_bytes_in_use": ([vp], ctypes.c_int64),
             "fg_mol_create": ([vp, i32, i32, ctypes.POINTER(vp)], ctypes.c_int),
             "fg_mol_destroy": ([vp], ctypes.c_int),
@@ -263,6 +266,15 @@ class System:
         self._q = q if q is not None else np.array([self.params.type_charge[t] for t in self._ids])
         _check(lib().fg_set_state(self.h, _p(xyz), _p(q), _p(self._ids)))
 
+    @property
+    def charges(self):
+        """Per-particle charges as uploaded (host copy)."""
+        return self._q
+
+    @property
+    def type_ids(self):
+        return self._ids
+
     def save_state(self, path, mw=None, rng_seed=5489, id_offset=1):
         """The current configuration as a reference state file (one atomic
         group; radius sigma/2 and mw per type, mw 1 when not given). Atom ids
@@ -401,6 +413,14 @@ class System:
         _check(lib().fg_stream_run(self.h, ctypes.byref(st)))
         return st.as_dict()
 
+    def log_get(self, first, n):
+        """dU and acceptance of trials [first, first + n) of the last logged
+        run (a logged sweep, or a batch run with set_log on)."""
+        du = np.empty(n)
+        acc = np.empty(n, np.uint8)
+        _check(lib().fg_log_get(self.h, int(first), int(n), _p(du), _p(acc)))
+        return du, acc
+
     def synchronize(self):
         _check(lib().fg_synchronize(self.h))
 
@@ -455,6 +475,11 @@ class Batch:
         disp = np.ascontiguousarray(disp, dtype=np.float64).reshape(-1, 3)
         u = np.ascontiguousarray(u, dtype=np.float64)
         _check(lib().fg_batch_stream_upload(self.h, member, len(idx), _p(idx), _p(disp), _p(u)))
+
+    def set_log(self, member, on=True):
+        """Log per-trial dU/acceptance of one member in later runs
+        (System.log_get reads it)."""
+        _check(lib().fg_batch_set_log(self.h, int(member), 1 if on else 0))
 
     def run(self):
         n = len(self.systems)
@@ -531,6 +556,10 @@ class Server:
 
     def release(self, job_id):
         _check(lib().fg_server_release(self.h, job_id))
+
+    def cancel(self, job_id):
+        """Drop a job in any state; a running one stops between rounds."""
+        _check(lib().fg_server_cancel(self.h, job_id))
 
     @property
     def bytes_in_use(self):

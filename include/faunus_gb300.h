@@ -165,6 +165,15 @@ int fg_batch_stream_upload(fg_batch *b, int32_t member, int64_t n, const int32_t
                            const double *u);
 /* Run every member's staged stream; per-member and summed statistics. */
 int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total);
+/* Record per-trial dU and acceptance of one member in the following
+ * fg_batch_run calls (on != 0), or stop (on == 0): the per-move record
+ * Movebase::move keeps (move.h:515-555, its dusum and acceptance counters)
+ * for one system of the batch, read back with fg_log_get. */
+int fg_batch_set_log(fg_batch *b, int32_t member, int32_t on);
+/* dU (kT, as the device computed it) and acceptance of trials
+ * [first, first + n) of the system's last logged run (fg_sweep, or an
+ * fg_batch_run with logging on for it); either output may be NULL. */
+int fg_log_get(fg_system *h, int64_t first, int64_t n, double *du, uint8_t *accepted);
 
 /* ---- parallel tempering over a batch ----------------------------------------
  * Replaces: Move::ParallelTempering (move.h:6542-6771) with MPI ranks as
@@ -195,6 +204,11 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
 int fg_server_poll(fg_server *s, int64_t job_id, int32_t *state, int64_t *trials_done, int64_t *accepted,
                    double *energy, double *xyz);
 int fg_server_release(fg_server *s, int64_t job_id);
+/* Drop a job in any state (a client that went away): a running job stops
+ * between rounds, its device memory returns to the budget at once and queued
+ * jobs may be admitted in the next round. The other jobs' results are
+ * unchanged (each keeps its own stream and state). */
+int fg_server_cancel(fg_server *s, int64_t job_id);
 int64_t fg_server_bytes_in_use(fg_server *s);
 
 /* ---- pair energy without device allocation ---------------------------------
@@ -207,7 +221,9 @@ int64_t fg_server_bytes_in_use(fg_server *s);
  * caller-owned DEVICE buffers: d_xyz[3n], d_charge[n] (or NULL for the type
  * charges), d_types[n]; writes one double to d_energy, on `stream` (a
  * cudaStream_t, or NULL for the default stream). Asynchronous: synchronize
- * the stream before reading d_energy.
+ * the stream before reading d_energy. Every d_types[i] must lie in
+ * [0, params->n_types); the ids are in device memory, so they are checked
+ * on the device: with any id outside that range d_energy receives NaN.
  * Every temporary lives in one fixed __device__ array of about 1.7 MB, held
  * by every GPU that loads this library until the process exits; the call
  * allocates nothing. n is limited to FG_NOALLOC_MAX_PARTICLES (larger n:

@@ -186,6 +186,43 @@ OracleSystem.mc_run_stream = _mc_run_stream
 OracleSystem.set_kT = lambda self, kT: lib().or_set_kT(self.h, float(kT))
 
 
+def replay_chain(args):
+    """FP64 replay of one AtomicTranslation chain (a process-pool worker:
+    start the pool with the spawn method). args = (params as bytes, xyz, q,
+    ids, idx, disp, u[, kT]); returns (du, acc) per trial."""
+    from beofaunus_gb300.params import FgParams
+    pb, xyz, q, ids, idx, disp, u = args[:7]
+    o = OracleSystem(FgParams.from_buffer_copy(pb), xyz, q, ids)
+    if len(args) > 7 and args[7] != 1.0:
+        o.set_kT(args[7])
+    r = o.mc_run_stream(idx, disp, u)
+    return r["du"], r["acc"]
+
+
+def compare_chain(du_dev, acc_dev, du_ref, acc_ref, u, tol):
+    """Trial-by-trial comparison of a device chain with the oracle's on the
+    same stream. The chains are compared up to and including the first trial
+    whose decision differs; a differing decision is legitimate only if the
+    threshold lies within tol of the oracle's dU (then the chains part from
+    there on). Returns dict(max_err, rms_err, compared, diverged_at,
+    divergence_in_band, decisions_identical)."""
+    du_dev = np.asarray(du_dev, dtype=np.float64)
+    du_ref = np.asarray(du_ref, dtype=np.float64)
+    n = len(du_ref)
+    mism = np.nonzero(np.asarray(acc_dev) != np.asarray(acc_ref))[0]
+    upto, at, in_band = n, None, True
+    if len(mism):
+        at = int(mism[0])
+        in_band = bool(abs(du_ref[at] + np.log(u[at])) < tol)
+        upto = at + 1
+    err = np.abs(du_dev[:upto] - du_ref[:upto])
+    finite = bool(np.all(np.isfinite(du_dev[:upto])))
+    return dict(max_err=float(err.max()) if finite and upto else float("inf"),
+                rms_err=float(np.sqrt(np.mean(err ** 2))) if finite and upto else float("inf"),
+                compared=int(upto), diverged_at=at, divergence_in_band=in_band,
+                decisions_identical=at is None)
+
+
 def philox(ctr, key):
     c = np.ascontiguousarray(ctr, dtype=np.uint32)
     k = np.ascontiguousarray(key, dtype=np.uint32)

@@ -7,7 +7,10 @@ the reference computed: per-trial particle (or molecule) index, trial
 position, dU and acceptance, plus the total energies before and after. Needs
 the reference checkout; the committed .npz files are what the tests read.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref <reference checkout>]
+
+(default: oracle/refdir.py's lookup: $FG_REFERENCE_DIR, else the staged copy
+in baseline/_ref/faunus)
 """
 import argparse
 import json
@@ -200,9 +203,14 @@ def make_dip(exe):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None)
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
+    if a.ref is None:
+        from oracle.refdir import reference_dir
+        a.ref = reference_dir()
+    if not a.ref:
+        sys.exit("no reference checkout: pass --ref or set FG_REFERENCE_DIR")
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "REF=" + a.ref])
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
     exe_mol = os.path.join(ROOT, "oracle", "_ref", "ref_harness_mol")

@@ -7,11 +7,12 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle.refdir import reference_dir
 
-REF = "/root/reference"
+REF = reference_dir()
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include", "faunus")), reason="reference checkout absent")
+@pytest.mark.skipif(REF is None, reason="reference sources absent (set FG_REFERENCE_DIR)")
 def test_adapter_compiles_against_reference_headers(tmp_path):
     cmd = ["g++", "-std=c++11", "-fsyntax-only", "-w",
            "-include", os.path.join(ROOT, "oracle", "ref", "compat.h"),
