@@ -88,6 +88,11 @@ FLOP_PER_PAIR = 40
 MUFU_PER_PAIR = 3
 FLOP_PER_K = 65
 FLOP_PER_K_COMMIT = 23
+#   rebuild (every 1000 accepted trials, inside the sweep launch): per
+#          particle and k-vector one complex product w e_z (6 FLOP) of its
+#          integer term (the per-axis tables and the w of a run of k-vectors
+#          are not counted).
+FLOP_PER_TERM_REBUILD = 6
 
 
 def workload_config(B, T):
@@ -427,7 +432,10 @@ def run_ours(args, rank, world):
         _, tot = batch.run()
         e2e_s += time.perf_counter() - t0
         e2e_trials += tot["trials"]
-        e2e_gathers += tot["kernel_launches"] - 1 - 3 * tot["sweep_launches"]
+        # every member's scalars are read back before the run and after it
+        # (one launch per run: the sweep kernel rebuilds Q(k) itself); a run
+        # with external rebuilds reads them once more per host check
+        e2e_gathers += 2 if tot["sweep_launches"] == 1 else tot["kernel_launches"] - 1 - 3 * tot["sweep_launches"]
     pool.shutdown()
     e2e = reduce_rate(dist, e2e_trials, e2e_s, dev)
 
@@ -437,7 +445,10 @@ def run_ours(args, rank, world):
     flop_per_trial = PAIRS_PER_TRIAL * FLOP_PER_PAIR + K * FLOP_PER_K + acc_rate * K * FLOP_PER_K_COMMIT
     avg_launch_s = sweep_ms / max(launches, 1) / 1e3
     trials_per_launch = trials / max(launches, 1)
-    achieved = flop_per_trial * trials_per_launch / avg_launch_s / 1e12
+    rebuilds_per_launch = rebuilds / max(launches, 1)
+    flop_rebuild = N_IONS * K * FLOP_PER_TERM_REBUILD   # one rebuild of one system
+    flop_per_launch = flop_per_trial * trials_per_launch + flop_rebuild * rebuilds_per_launch
+    achieved = flop_per_launch / avg_launch_s / 1e12
     sm_mhz = (clk or {}).get("sm_mhz") or 1900.0
     mufu_peak = sms * 16 * sm_mhz * 1e6
     mufu_frac = PAIRS_PER_TRIAL * MUFU_PER_PAIR * trials_per_launch / avg_launch_s / mufu_peak
@@ -495,8 +506,10 @@ def run_ours(args, rank, world):
                      "frac": achieved / fp32_peak, "traffic": traffic,
                      "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (best of 5)",
                      "flop_per_trial": flop_per_trial, "trials_per_launch": trials_per_launch,
+                     "flop_per_rebuild": flop_rebuild, "rebuilds_per_launch": rebuilds_per_launch,
                      "mean_launch_ms": avg_launch_s * 1e3, "mufu_frac": mufu_frac,
-                     "note": "pair and k-space terms are FP32 arithmetic (the 32x32 Gram matrix of a "
+                     "note": "one launch per step runs every system's sweep, its Q(k) rebuilds included; "
+                             "pair and k-space terms are FP32 arithmetic (the 32x32 Gram matrix of a "
                              "trial block runs on the tensor cores, mma.sync TF32 x3); each system is a "
                              "sequential Markov chain on one SM"},
         "single_chain": {"value": single, "unit": UNIT, "us_per_trial": 1e6 / single},

@@ -95,8 +95,8 @@ struct fg_system {
     int4 *cell_pos = nullptr;
     float4 *kvec = nullptr, *core_tab = nullptr, *core_tab2 = nullptr;
     uint32_t *kpack = nullptr;
-    int2 *kseg = nullptr;
-    int nseg = 0;
+    int2 *kseg = nullptr, *kseg_blk = nullptr;
+    int nseg = 0, nseg_blk = 0;
     longlong2 *qfix = nullptr, *qnew = nullptr;
     SysScalars *sc = nullptr;
     float2 *trial_out = nullptr, *corr = nullptr, *pair_part = nullptr;
@@ -136,7 +136,7 @@ void free_all(fg_system *h) {
     void *ptrs[] = {h->d_desc, h->pos64, h->pos4, h->pos_ext, h->cell_ext, h->ptype, h->cell_count, h->cell_pid,
                     h->p_cell, h->p_slot, h->cell_pos, h->kvec, h->core_tab, h->core_tab2, h->kpack, h->qfix,
                     h->qnew, h->sc, h->trial_out, h->corr, h->pair_part, h->req, h->dp_fix, h->sc_tab, h->trials,
-                    h->log_du, h->log_acc, h->kseg, h->raw_idx, h->raw_disp, h->raw_u};
+                    h->log_du, h->log_acc, h->kseg, h->kseg_blk, h->raw_idx, h->raw_disp, h->raw_u};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -180,6 +180,41 @@ void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &
 }
 
 // Threads of the per-system CTA (multiple of 32, <= kSweepThreads).
+// Runs of consecutive k-vectors with the same (nx, ny) and consecutive nz
+// (k-vectors as n-triples n3[3k..3k+2], in enumeration order), each cut into
+// near-equal pieces of at most L entries, for the smallest L <= kQkRun whose
+// piece count fits `slots` (kQkRun if none does); longest first. Encoded as
+// {k0 | len << 24, nx & 0xFF | (ny & 0xFF) << 8 | (nz0 & 0xFF) << 16}.
+std::vector<int2> kseg_pieces(const std::vector<int> &n3, int K, int slots) {
+    std::vector<std::pair<int, int>> runs;   // (k0, length)
+    for (int k = 0; k < K;) {
+        int run = 1;
+        while (k + run < K && n3[3 * (k + run)] == n3[3 * k] && n3[3 * (k + run) + 1] == n3[3 * k + 1] &&
+               n3[3 * (k + run) + 2] == n3[3 * k + 2] + run)
+            run++;
+        runs.push_back({k, run});
+        k += run;
+    }
+    int L = 1;
+    for (; L < fg::kQkRun; L++) {
+        size_t pieces = 0;
+        for (auto &r : runs) pieces += (r.second + L - 1) / L;
+        if (pieces <= (size_t)slots) break;
+    }
+    std::vector<int2> seg;
+    for (auto &r : runs) {
+        const int pieces = (r.second + L - 1) / L;
+        for (int p = 0, k0 = r.first; p < pieces; p++) {
+            const int len = r.second / pieces + (p < r.second % pieces ? 1 : 0);
+            seg.push_back(make_int2(k0 | (len << 24), (n3[3 * k0] & 0xFF) | ((n3[3 * k0 + 1] & 0xFF) << 8) |
+                                                          ((n3[3 * k0 + 2] & 0xFF) << 16)));
+            k0 += len;
+        }
+    }
+    std::stable_sort(seg.begin(), seg.end(), [](const int2 &a, const int2 &b) { return (a.x >> 24) > (b.x >> 24); });
+    return seg;
+}
+
 int sweep_threads(const fg_system *h) {
     int t = h->threads;
     if (t <= 0) {
@@ -567,9 +602,11 @@ int get_qk_host(fg_system *h, std::vector<double> &q) {
     std::vector<longlong2> v(h->K);
     CK(cudaMemcpyAsync(v.data(), h->qfix, v.size() * sizeof(longlong2), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    // units of 2^-28 / c, c = 4095/4096 (set_qk_scale)
+    const double unit = (1.0 / 268435456.0) * (4096.0 / 4095.0);
     for (int k = 0; k < h->K; k++) {
-        q[2 * k] = (double)v[k].x * (1.0 / 268435456.0);
-        q[2 * k + 1] = (double)v[k].y * (1.0 / 268435456.0);
+        q[2 * k] = (double)v[k].x * unit;
+        q[2 * k + 1] = (double)v[k].y * unit;
     }
     return FG_OK;
 }
@@ -648,7 +685,8 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
     LaunchCfg cfg;
     rc = sweep_config(h, cfg);
     if (rc) return rc;
-    const bool rebuilds = h->K > 0 && !h->desc.skip_rebuild;
+    // the Ewald block kernel rebuilds Q(k) itself: one launch runs the stream
+    const bool rebuilds = h->K > 0 && !h->desc.skip_rebuild && !ewald_block_ok(h);
     const int uf = std::max(h->P.ewald_update_frequency, 1);
     int launches = 0;
     std::vector<cudaEvent_t> evs;
@@ -740,14 +778,17 @@ double qk_charge_bound(const fg_system *h, const double *charge) {
     return qmax;
 }
 
-// Grid 2^-g of the Q(k) contributions: the largest g <= 28 with
-// 2^g max|q eff| <= 2^24, so a term is at most 2^24 (plus float rounding) and
-// the 64 terms of a rebuild pass sum exactly in int32.
+// Scale s = 2^g c of the Q(k) contributions (grid 1/s): g is the largest
+// value <= 28 with 2^g max|q eff| <= 2^22 and c = 4095/4096, so every term
+// |s q eff e_x e_y e_z| stays below 2^22 - 2^9 whatever the few-ulp rounding
+// of the unit factors, inside the range where qk_term rounds with one FP32
+// addition; 256 terms sum exactly in int32. Q(k) is held in units of
+// 2^-28 / c (each term shifted left by 28 - g).
 int set_qk_scale(SysDesc &d, double qmax) {
-    if (!(qmax <= 16777216.0)) return FG_ERR_INVALID;
+    if (!(qmax <= 4194304.0)) return FG_ERR_INVALID;
     int g = 28;
-    while (g > 0 && std::ldexp(qmax, g) > 16777216.0) g--;
-    d.qk_scale = (float)std::ldexp(1.0, g);
+    while (g > 0 && std::ldexp(qmax, g) > 4194304.0) g--;
+    d.qk_scale = (float)std::ldexp(4095.0 / 4096.0, g);
     d.qk_shift = 28 - g;
     return FG_OK;
 }
@@ -932,6 +973,13 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         h->nseg = (int)seg.size();
         ALLOC(h->kseg, seg.size() * sizeof(int2));
         cudaMemcpy(h->kseg, seg.data(), seg.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        // the same runs for the block kernel's in-kernel rebuild: the
+        // shortest pieces (at most kQkRun) whose count still fits one CTA's
+        // kEbThreads threads, so that every warp of the CTA takes a share
+        std::vector<int2> blk = kseg_pieces(n3, h->K, fg::kEbThreads);
+        h->nseg_blk = (int)blk.size();
+        ALLOC(h->kseg_blk, blk.size() * sizeof(int2));
+        cudaMemcpy(h->kseg_blk, blk.data(), blk.size() * sizeof(int2), cudaMemcpyHostToDevice);
         cudaMemset(h->qfix, 0, h->K * sizeof(longlong2));
         cudaMemset(h->qnew, 0, h->K * sizeof(longlong2));
     }
@@ -1002,6 +1050,8 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     d.kpack = h->kpack;
     d.kseg = h->kseg;
     d.nseg = h->nseg;
+    d.kseg_blk = h->kseg_blk;
+    d.nseg_blk = h->nseg_blk;
     d.kcc = h->kc;
     if (set_qk_scale(d, qk_charge_bound(h, nullptr)))
         return bail(fail(FG_ERR_INVALID, "charges too large for the Q(k) fixed point"));

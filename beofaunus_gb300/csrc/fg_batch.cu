@@ -111,6 +111,10 @@ struct fg_batch {
     bool pt = false;
     cudaGraphExec_t graph = nullptr;
     int64_t graph_sweeps = -1;
+    // fg_batch_run without external rebuilds: reset, sweep and gather of a
+    // run captured once and replayed
+    cudaGraphExec_t run_graph = nullptr;
+    int run_graph_kernels = 0;
     // Debye-Hueckel members without a cell list run the block kernel
     bool dh_block = false;
     DhGroups dh;
@@ -140,7 +144,12 @@ int batch_config(fg_batch *b) {
     }
     b->cfg.threads = T;
     b->cfg.smem = sm;
-    b->rebuilds = b->maxK > 0 && !h0->desc.skip_rebuild;
+    if (b->run_graph) {
+        cudaGraphExecDestroy(b->run_graph);
+        b->run_graph = nullptr;
+    }
+    // the Ewald block kernel rebuilds Q(k) inside the sweep
+    b->rebuilds = b->maxK > 0 && !h0->desc.skip_rebuild && !ewald_block_ok(h0);
     b->dh_block = true;
     std::vector<int> Ns;
     std::vector<double> w;
@@ -180,6 +189,32 @@ int batch_push_descs(fg_batch *b) {
     return FG_OK;
 }
 
+// One run as a CUDA graph: reset the members' stream cursors, the sweep
+// launch(es) over all members, gather the scalars. Captured on first use.
+int batch_run_graph(fg_batch *b) {
+    if (b->run_graph) return FG_OK;
+    const int n = (int)b->sys.size();
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_counts);
+    int rc = batch_sweep(b, INT64_MAX);
+    fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc) {
+        if (e == cudaSuccess) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    e = cudaGraphInstantiate(&b->run_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    b->run_graph_kernels = (int)(b->dh_block ? b->dh.C.size() + 2 : 3);
+    (void)nodes;
+    return FG_OK;
+}
+
 // Run every member's staged stream of counts[s] trials (also on the device).
 int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *per, fg_sweep_stats *total) {
     const int n = (int)b->sys.size();
@@ -187,16 +222,32 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
     fg::gather_scalars_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_gather);
     CK(cudaMemcpyAsync(s0.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
-    fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_counts);
-    CK(cudaEventRecord(b->ev0, b->stream));
     int launches = 0;
+    int64_t kernels = 1;   // the first gather
+    std::vector<cudaEvent_t> evs;
+    bool graphed = false;
+    if (!b->rebuilds) {
+        // no external rebuilds: one launch runs every member's whole stream
+        int rc = batch_run_graph(b);
+        if (rc) return rc;
+        CK(cudaEventRecord(b->ev0, b->stream));
+        CK(cudaGraphLaunch(b->run_graph, b->stream));
+        CK(cudaEventRecord(b->ev1, b->stream));
+        CK(cudaMemcpyAsync(s.data(), b->d_gather, n * sizeof(SysScalars), cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        launches = 1;
+        kernels += b->run_graph_kernels;
+        graphed = true;
+    } else {
+        fg::batch_reset_kernel<<<(n + 127) / 128, 128, 0, b->stream>>>(b->d_descs, n, b->d_counts);
+        CK(cudaEventRecord(b->ev0, b->stream));
+        kernels++;
+    }
     const int uf = std::max(b->sys[0]->P.ewald_update_frequency, 1);
     int64_t maxc = 0;
     for (auto c : counts) maxc = std::max(maxc, c);
     int64_t prev_done = -1;
-    int64_t kernels = 2;   // the reset and the first gather
-    std::vector<cudaEvent_t> evs;
-    while (true) {
+    while (!graphed) {
         const int pairs = b->rebuilds ? (int)std::min<int64_t>(maxc / uf + 1, 64) : 1;
         for (int p = 0; p < pairs; p++) {
             cudaEvent_t e0, e1;
@@ -233,10 +284,18 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
         if (sum == prev_done) return fail(FG_ERR_DEVICE, "batch made no progress");
         prev_done = sum;
     }
-    CK(cudaEventRecord(b->ev1, b->stream));
+    if (graphed) {
+        for (int i = 0; i < n; i++)
+            if (!s[i].error && s[i].cursor < counts[i])
+                return fail(FG_ERR_DEVICE, "batch member %d stopped at trial %lld of %lld", i,
+                            (long long)s[i].cursor, (long long)counts[i]);
+    } else {
+        CK(cudaEventRecord(b->ev1, b->stream));
+    }
     CK(cudaEventSynchronize(b->ev1));
     float ms = 0.0f, sweep_ms = 0.0f;
     CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    if (graphed) sweep_ms = ms;   // the graph's reset and gather take microseconds
     for (size_t e = 0; e + 1 < evs.size(); e += 2) {
         float t = 0.0f;
         CK(cudaEventElapsedTime(&t, evs[e], evs[e + 1]));
@@ -281,6 +340,7 @@ void batch_free(fg_batch *b) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->run_graph) cudaGraphExecDestroy(b->run_graph);
     b->dh.release();
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);

@@ -17,8 +17,9 @@
 // Q(k) itself stays the exact fixed-point sum: after the block each accepted
 // trial's integer contributions are applied in order. A trial whose particle
 // an accepted trial of the block already moved ends the block, and so does
-// the accepted trial that makes a Q(k) rebuild due (the kernel then exits for
-// the rebuild, as the one-trial kernel does).
+// the accepted trial that makes a Q(k) rebuild due: the CTA then rebuilds its
+// system's Q(k) from scratch in place (eb_rebuild) and carries on, so one
+// launch runs a system's whole stream.
 namespace fg {
 
 constexpr int kEbTrials = 32;
@@ -264,6 +265,118 @@ __device__ __forceinline__ df eb_pair(const Move &m, int4 p, int t, const short4
     df ad = {0.0f, 0.0f};
     pair_candidate<MODEL_EWALD>(m, p, t, e, d, a, ad);
     return df_add_f(ad, a);
+}
+
+// updateAllComplexNumbers (ewald.h:388-415) inside the sweep, every
+// update_frequency accepted trials (NonbondedEwald::update, ewald.h:633-640):
+// Q(k) from scratch as the exact sum of every particle's integer terms
+// (qk_term), compared with the running Q(k) in shared memory and adopted.
+// The two agree bit for bit unless the device misbehaved (the terms are a
+// deterministic function of the fixed-point positions), so the energy
+// correction is zero; a difference is recorded (kErrQkMismatch where the
+// system verifies) and its energy is added to the running sums, as the
+// reference adds the drift it removes.
+//   work split: thread t owns items t, t + blockDim, ... of the system's
+//   rebuild list (runs of <= kQkRun k-vectors sharing (nx, ny), cut so that
+//   the CTA's threads hold them, longest first); particles pass through the
+//   increment buffer in stages with their axis tables (8 threads build one
+//   particle's table); a stage's terms are summed exactly in 32 bits, then
+//   in int64 registers.
+// All threads call it (block-uniform). Returns the energy correction
+// (valid in thread 0) and whether any Q(k) differed.
+template <int L>
+__device__ __forceinline__ void eb_rebuild_pass(const float2 *et, int T, const float *q2g, int nb, int ix, int iy,
+                                                int iz, unsigned ax[kQkRun], unsigned ay[kQkRun]) {
+    qk_pass<L>(et, T, q2g, nb, ix, iy, iz, ax, ay);
+}
+__device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &corr) {
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+    const int T = qk_tab_len(d.kcc);
+    // the increment buffer holds the stage's axis tables plus kQkRun entries
+    // of headroom for the unused tail reads of qk_pass
+    const int stage = min(64, (kEbKc * kEbTrials - kQkRun) / T);
+    float2 *et = s.delta;
+    float *q2g = s.G;   // [stage], free between blocks
+    const int shift = d.qk_shift;
+    df e = {0.0f, 0.0f};
+    int bad = 0;
+    for (int r0 = 0; r0 < d.nseg_blk; r0 += nt) {   // uniform over the block
+        const int r = r0 + tid;
+        int k0 = 0, len = 0, ix = 0, iy = 0, iz = 0;
+        if (r < d.nseg_blk) {
+            const int2 sg = d.kseg_blk[r];
+            k0 = sg.x & 0xFFFFFF;
+            len = sg.x >> 24;
+            ix = (int)(int8_t)(sg.y & 0xFF);
+            iy = 2 * d.kcc + 1 + (int)(int8_t)((sg.y >> 8) & 0xFF);
+            iz = 4 * d.kcc + 2 + (int)(int8_t)((sg.y >> 16) & 0xFF);
+        }
+        const int wl = __reduce_max_sync(0xffffffffu, len);   // warp-uniform (items sorted by length)
+        long long tx[kQkRun], ty[kQkRun];
+#pragma unroll
+        for (int u = 0; u < kQkRun; u++) tx[u] = ty[u] = 0;
+        for (int j0 = 0; j0 < d.N; j0 += stage) {
+            const int nb = min(stage, d.N - j0);
+            __syncthreads();   // the previous stage's tables are consumed
+            for (int jj = tid >> 3; jj < nb; jj += nt >> 3) {
+                const int4 p = d.pos4[j0 + jj];
+                if ((tid & 7) == 0) q2g[jj] = qk_charge(__int_as_float(p.w), d.eff[d.ptype[j0 + jj]], d);
+                const int h[3] = {p.x, p.y, p.z};
+                for (int t = tid & 7; t < T; t += 8) et[jj * T + t] = qk_tab_entry(t, d.kcc, h, s.b.sc_tab);
+            }
+            __syncthreads();
+            if (wl > 0) {
+                unsigned ax[kQkRun], ay[kQkRun];
+#pragma unroll
+                for (int u = 0; u < kQkRun; u++) ax[u] = ay[u] = 0u;
+                switch (wl) {
+                    case 1: eb_rebuild_pass<1>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 2: eb_rebuild_pass<2>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 3: eb_rebuild_pass<3>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 4: eb_rebuild_pass<4>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 5: eb_rebuild_pass<5>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 6: eb_rebuild_pass<6>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 7: eb_rebuild_pass<7>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    default: eb_rebuild_pass<8>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                }
+                const unsigned off = (unsigned)nb * kQkMagicBits;
+#pragma unroll
+                for (int u = 0; u < kQkRun; u++) {
+                    tx[u] += qk_widen((int)(ax[u] - off), shift);
+                    ty[u] += qk_widen((int)(ay[u] - off), shift);
+                }
+            }
+        }
+        // compare with the running sums and adopt
+#pragma unroll
+        for (int u = 0; u < kQkRun; u++) {
+            if (u >= len) continue;
+            const int k = k0 + u;
+            const longlong2 qo = s.b.qfix[k];
+            if (qo.x != tx[u] || qo.y != ty[u]) {
+                bad = 1;
+                const longlong2 qn = make_longlong2(tx[u], ty[u]);
+                const float2 fo = q_to_float(qo), fn = q_to_float(qn);
+                const float dre = fix28_to_float(qn.x - qo.x), dim = fix28_to_float(qn.y - qo.y);
+                e = df_add_f(e, s.b.kvec[k].x * fmaf(dre, fo.x + fn.x, dim * (fo.y + fn.y)));
+                s.b.qfix[k] = qn;
+                s.b.kvec[k].y = fn.x;
+                s.b.kvec[k].z = fn.y;
+            }
+        }
+    }
+    // energy correction: warp sums, then warp 0 over the warps (fixed order)
+    e = warp_sum_df(e);
+    const int anybad = __syncthreads_or(bad);   // also: every thread is done with the buffers
+    if (lane == 0) s.b.red[tid >> 5] = make_float2(e.hi, e.lo);
+    __syncthreads();
+    if (tid < 32) {
+        df t = {0.0f, 0.0f};
+        if (lane < (nt >> 5)) t = {s.b.red[lane].x, s.b.red[lane].y};
+        corr = warp_sum_df(t);
+    }
+    __syncthreads();   // red is free again
+    return anybad != 0;
 }
 
 // Surface dipole change of a trial (Angstrom e), as surface_delta computes it.
@@ -635,7 +748,17 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
         }
         cur += done;
         __syncthreads();
-        if (rebuild) break;
+        if (rebuild) {
+            df corr;
+            const bool mism = eb_rebuild(d, s, corr);
+            if (tid == 0) {
+                U = df_add(U, corr);
+                Ut = df_add(Ut, corr);
+                sc->n_rebuilds++;
+                if (mism && sc->verify_rebuild) err |= kErrQkMismatch;
+            }
+            rebuild = false;
+        }
     }
     // write back Q(k), cells and the scalars
     store_back(d, s.b, true, CELLS);
@@ -651,7 +774,6 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             sc->m[a][1] = s.Mdf[a].y;
         }
         sc->cnt_accepted = cnt_acc;
-        if (rebuild) sc->rebuild_pending = 1;
         sc->error |= err;
     }
 }

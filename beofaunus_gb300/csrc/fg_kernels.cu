@@ -19,13 +19,15 @@
 // (ewald.h:613-729), getSurfaceEnergy (ewald.h:277-291).
 //
 // Q(k) bookkeeping. Each particle contributes the integer
-// c_k(j) = round(w_j(nx, ny) e_z(nz)), w_j = (2^g q_j eff_j e_x(nx)) e_y(ny),
-// with e_a(n) = e^{i n 2 pi x_a / L_a} from sincos_turns on the exact integer
-// phase n h_a (its conjugate for n < 0) and every product rounded in a fixed
-// order (qk_w, qk_term): a deterministic function of the particle's
-// fixed-point position. Q(k) is kept as the exact int64 sum of these
-// contributions in units of 2^-28 (each shifted by 28 - g), and an accepted
-// move adds c_k(new) - c_k(old). So Q(k) never drifts: a rebuild from scratch
+// c_k(j) = round(w_j(nx, ny) e_z(nz)), w_j = (s q_j eff_j e_x(nx)) e_y(ny),
+// s = 2^g c (c = 4095/4096), with e_a(n) = e^{i n 2 pi x_a / L_a} from
+// sincos_turns on the exact integer phase n h_a (its conjugate for n < 0) and
+// every product rounded in a fixed order (qk_w, qk_term): a deterministic
+// function of the particle's fixed-point position. g is chosen so that every
+// |w e_z| < 2^22, where adding 1.5 2^23 rounds to the nearest integer on the
+// FMA pipe (qk_term). Q(k) is kept as the exact int64 sum of these
+// contributions in units of 2^-28 / c (each shifted by 28 - g), and an
+// accepted move adds c_k(new) - c_k(old). So Q(k) never drifts: a rebuild from scratch
 // reproduces it bit for bit (qk_rebuild_* checks that), where the
 // reference's FP64 running sum needs the rebuild to undo accumulated error.
 // The factorised form lets the rebuild share one w per particle across the
@@ -411,11 +413,13 @@ __device__ __forceinline__ void load_desc(SysDesc &dst, const SysDesc *__restric
     __syncthreads();
 }
 
-// Q(k) fixed point (units of 2^-28) to float, by 32-bit halves.
+// Q(k) fixed point (units of 2^-28 / c, c = 4095/4096) to float, by 32-bit
+// halves.
+constexpr float kQkInvC = 4096.0f / 4095.0f;
 __device__ __forceinline__ float fix28_to_float(long long v) {
     const int hi = (int)(v >> 32);
     const unsigned lo = (unsigned)v;
-    return fmaf((float)hi, 16.0f, (float)lo * 3.7252902984619141e-09f);
+    return fmaf((float)hi, 16.0f * kQkInvC, (float)lo * (3.7252902984619141e-09f * kQkInvC));
 }
 __device__ __forceinline__ float2 q_to_float(longlong2 q) { return make_float2(fix28_to_float(q.x), fix28_to_float(q.y)); }
 
@@ -562,29 +566,44 @@ __device__ __forceinline__ float2 qk_tab_entry(int t, int kcc, const int h[3], c
     return n < 0 ? make_float2(e.x, -e.y) : e;
 }
 
-// w = (2^g q eff e_x) e_y, then the integer term round(w e_z), as one
+// w = (s q eff e_x) e_y, then the integer term round(w e_z), as one
 // fixed sequence of roundings.
 __device__ __forceinline__ float2 qk_w(float q2g, float2 ex, float2 ey) {
     const float ax = __fmul_rn(q2g, ex.x), ay = __fmul_rn(q2g, ex.y);
     return make_float2(__fmaf_rn(ax, ey.x, -__fmul_rn(ay, ey.y)), __fmaf_rn(ax, ey.y, __fmul_rn(ay, ey.x)));
 }
-__device__ __forceinline__ int2 qk_term(float2 w, float2 ez) {
-    return make_int2(__float2int_rn(__fmaf_rn(w.x, ez.x, -__fmul_rn(w.y, ez.y))),
-                     __float2int_rn(__fmaf_rn(w.x, ez.y, __fmul_rn(w.y, ez.x))));
+// For |x| < 2^22, x + 1.5 2^23 lies in [2^23, 2^24), where floats are the
+// integers: the sum is 1.5 2^23 + round(x) (to nearest, ties to even, as
+// __float2int_rn rounds), and its bit pattern minus that of 1.5 2^23 is
+// round(x). An FP32 addition instead of a conversion on the XU pipe.
+constexpr float kQkMagic = 12582912.0f;
+constexpr uint32_t kQkMagicBits = 0x4B400000u;
+// bit patterns of w e_z + 1.5 2^23 (real, imaginary): sums of n of them
+// minus n kQkMagicBits are sums of terms, exactly in 32-bit wrap-around
+__device__ __forceinline__ uint2 qk_term_bits(float2 w, float2 ez) {
+    const float re = __fmaf_rn(w.x, ez.x, -__fmul_rn(w.y, ez.y));
+    const float im = __fmaf_rn(w.x, ez.y, __fmul_rn(w.y, ez.x));
+    return make_uint2(__float_as_uint(__fadd_rn(re, kQkMagic)), __float_as_uint(__fadd_rn(im, kQkMagic)));
 }
-// an integer contribution in units of 2^-28
+__device__ __forceinline__ int2 qk_term(float2 w, float2 ez) {
+    const uint2 b = qk_term_bits(w, ez);
+    return make_int2((int)(b.x - kQkMagicBits), (int)(b.y - kQkMagicBits));
+}
+// an integer contribution in units of 2^-28 / c
 __device__ __forceinline__ long long qk_widen(int c, int shift) { return (long long)c * (1LL << shift); }
-// 2^g q eff of a particle (the power-of-two scaling is exact)
+// s q eff of a particle (s = 2^g c: products exact in the exponent and c's
+// 12-bit mantissa, then one rounding)
 __device__ __forceinline__ float qk_charge(float q, float eff, const SysDesc &d) {
     return __fmul_rn(__fmul_rn(q, eff), d.qk_scale);
 }
 // c_k(new) - c_k(old) for k-vector n from the two positions' axis tables
+// (the two terms' offsets cancel in the difference of their bit patterns)
 __device__ __forceinline__ int2 qk_delta(int nx, int ny, int nz, float q2g, const float2 *__restrict__ tn,
                                         const float2 *__restrict__ to, int kcc) {
     const int iy = 2 * kcc + 1 + ny, iz = 4 * kcc + 2 + nz;
-    const int2 cn = qk_term(qk_w(q2g, tn[nx], tn[iy]), tn[iz]);
-    const int2 co = qk_term(qk_w(q2g, to[nx], to[iy]), to[iz]);
-    return make_int2(cn.x - co.x, cn.y - co.y);
+    const uint2 cn = qk_term_bits(qk_w(q2g, tn[nx], tn[iy]), tn[iz]);
+    const uint2 co = qk_term_bits(qk_w(q2g, to[nx], to[iy]), to[iz]);
+    return make_int2((int)(cn.x - co.x), (int)(cn.y - co.y));
 }
 // Axis tables of a move's new and old positions into tn and to (all threads
 // of the block; the caller synchronises before use).
@@ -925,8 +944,8 @@ __global__ void __launch_bounds__(kSweepThreads) commit_kernel(const SysDesc *__
 // updateAllComplexNumbers (ewald.h:388-415) as the exact integer sum of the
 // per-particle contributions. One thread per run of k-vectors sharing
 // (nx, ny) (at most kQkRun of them, consecutive nz): per staged particle it
-// forms w once and one term per k. Terms (|c| <= 2^24) are summed exactly in
-// int32 over a pass of `stage` <= 64 particles, then added to the thread's
+// forms w once and one term per k. Terms (|c| < 2^22) are summed exactly in
+// 32 bits over a pass of `stage` <= 64 particles, then added to the thread's
 // int64 totals in shared memory. Per pass the block stages the particles'
 // axis tables (stage x qk_tab_len) from positions prefetched during the
 // previous pass. blockIdx.x covers a chunk of particles, blockIdx.y selects
@@ -934,6 +953,8 @@ __global__ void __launch_bounds__(kSweepThreads) commit_kernel(const SysDesc *__
 constexpr int kQkRun = 8;
 constexpr int kQkMaxThreads = 512;
 // One pass over nb staged particles for runs of (at most) L k-vectors.
+// Sums of the terms' bit patterns (qk_term_bits); the caller subtracts
+// nb kQkMagicBits per sum.
 template <int L>
 __device__ __forceinline__ void qk_pass(const float2 *et, int T, const float *q2g, int nb, int ix, int iy, int iz,
                                         unsigned ax[kQkRun], unsigned ay[kQkRun]) {
@@ -942,9 +963,9 @@ __device__ __forceinline__ void qk_pass(const float2 *et, int T, const float *q2
         const float2 w = qk_w(q2g[jj], e[ix], e[iy]);
 #pragma unroll
         for (int u = 0; u < L; u++) {
-            const int2 c = qk_term(w, e[iz + u]);
-            ax[u] += (unsigned)c.x;
-            ay[u] += (unsigned)c.y;
+            const uint2 c = qk_term_bits(w, e[iz + u]);
+            ax[u] += c.x;
+            ay[u] += c.y;
         }
     }
 }
@@ -1034,11 +1055,12 @@ __global__ void __launch_bounds__(kQkMaxThreads) qk_rebuild_kernel(const SysDesc
                     case 7: qk_pass<7>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
                     default: qk_pass<8>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
                 }
+                const unsigned off = (unsigned)nb * kQkMagicBits;
 #pragma unroll
                 for (int u = 0; u < kQkRun; u++)
                     if (u < len) {
-                        tot[(2 * u) * nt + tid] += qk_widen((int)ax[u], shift);
-                        tot[(2 * u + 1) * nt + tid] += qk_widen((int)ay[u], shift);
+                        tot[(2 * u) * nt + tid] += qk_widen((int)(ax[u] - off), shift);
+                        tot[(2 * u + 1) * nt + tid] += qk_widen((int)(ay[u] - off), shift);
                     }
             }
         }

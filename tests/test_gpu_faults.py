@@ -57,7 +57,7 @@ def test_non_finite_molecule_and_dipole_inputs_are_refused():
 
 def test_server_refuses_a_job_larger_than_its_whole_budget():
     from beofaunus_gb300.gpu import FgError, Server
-    budget = 4 << 20
+    budget = 256 << 10    # a 20000-ion job needs about 1 MB, a 300-ion one about 60 KB
     srv = Server(budget, threads=256, round_pairs=1 << 16)
     big = workloads.dh_lj_salt(20000, seed=5)
     with pytest.raises(FgError, match="budget"):

@@ -105,11 +105,16 @@ def test_sweep_rpm16k_cell_list_full_size():
     err = assert_same_chain(r["du"], r["acc"], ro["du"], ro["acc"], u)
     print("rpm16k: max |dU err| %.3g rms %.3g" % (err.max(), np.sqrt(np.mean(err ** 2))))
     np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
-    # Q(k) is the exact sum of FP32-accurate per-particle terms: its distance
-    # from the FP64 sum is bounded by ~sqrt(N) * 1e-7 (1.3e-5 here)
+    # Q(k) is the exact sum of per-particle terms on a 2^-22 grid (rounding
+    # error <= 1.2e-7 each, rms 6.9e-8) from FP32 products (~1e-7 each): its
+    # distance from the FP64 sum has rms ~ sqrt(N) * 1.2e-7 = 1.5e-5 per
+    # component here, and stays below 4 sigma = 6e-5 over the 2 x 2242
+    # components; the running energy sees it only through the FP32 Q(k)
     qg = s.qk()
     qo = o.qk()[0]
-    assert np.max(np.abs(qg - qo)) < 4e-5
+    dq = np.abs(qg - qo)
+    print("rpm16k Q(k) vs FP64: max %.3g rms %.3g" % (dq.max(), np.sqrt(np.mean(dq ** 2))))
+    assert dq.max() < 6e-5
 
 
 def test_total_energy_matches_oracle():

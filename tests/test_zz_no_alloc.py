@@ -83,8 +83,10 @@ def test_no_alloc_pair_energy_matches_existing_entry_point_and_oracle():
     for p, x, q, t in cases:
         want = _reference(p, x, q, t)
         got = _noalloc(p, x, q, t)
+        ref = _oracle(p, x, q, t)
+        print("no-alloc %.12f  fg_total_energy %.12f  oracle %.12f" % (got, want, ref))
         assert got == pytest.approx(want, abs=TOL)
-        assert got == pytest.approx(_oracle(p, x, q, t), abs=TOL_ORACLE)
+        assert got == pytest.approx(ref, abs=TOL_ORACLE)
     # the same system twice in a row, charges taken from the atom types
     p, x, q, t = cases[0]
     a = _noalloc(p, x, None, t)
