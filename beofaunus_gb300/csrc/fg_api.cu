@@ -183,7 +183,9 @@ void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &
 // Runs of consecutive k-vectors with the same (nx, ny) and consecutive nz
 // (k-vectors as n-triples n3[3k..3k+2], in enumeration order), each cut into
 // near-equal pieces of at most L entries, for the smallest L <= kQkRun whose
-// piece count fits `slots` (kQkRun if none does); longest first. Encoded as
+// piece count fits `slots` (kQkRun if none does); longest first, and among
+// equal lengths by first nz, so that the lanes of a warp read the same e_z
+// entries of a particle (shared-memory broadcasts). Encoded as
 // {k0 | len << 24, nx & 0xFF | (ny & 0xFF) << 8 | (nz0 & 0xFF) << 16}.
 std::vector<int2> kseg_pieces(const std::vector<int> &n3, int K, int slots) {
     std::vector<std::pair<int, int>> runs;   // (k0, length)
@@ -211,7 +213,11 @@ std::vector<int2> kseg_pieces(const std::vector<int> &n3, int K, int slots) {
             k0 += len;
         }
     }
-    std::stable_sort(seg.begin(), seg.end(), [](const int2 &a, const int2 &b) { return (a.x >> 24) > (b.x >> 24); });
+    std::stable_sort(seg.begin(), seg.end(), [](const int2 &a, const int2 &b) {
+        const int la = a.x >> 24, lb = b.x >> 24;
+        if (la != lb) return la > lb;
+        return (int)(int8_t)((a.y >> 16) & 0xFF) < (int)(int8_t)((b.y >> 16) & 0xFF);
+    });
     return seg;
 }
 
@@ -679,14 +685,14 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
     h->desc.log_trials = log ? 1 : 0;
     h->desc.trial_du = h->log_du;
     h->desc.trial_acc = h->log_acc;
+    h->desc.rebuild_in_kernel = 0;   // a system alone leaves its rebuilds to the rebuild kernel (all SMs)
     h->log_n = log ? n : 0;
     rc = push_desc(h);
     if (rc) return rc;
     LaunchCfg cfg;
     rc = sweep_config(h, cfg);
     if (rc) return rc;
-    // the Ewald block kernel rebuilds Q(k) itself: one launch runs the stream
-    const bool rebuilds = h->K > 0 && !h->desc.skip_rebuild && !ewald_block_ok(h);
+    const bool rebuilds = h->K > 0 && !h->desc.skip_rebuild;
     const int uf = std::max(h->P.ewald_update_frequency, 1);
     int launches = 0;
     std::vector<cudaEvent_t> evs;

@@ -55,27 +55,36 @@ __global__ void gather_scalars_kernel(const SysDesc *__restrict__ descs, int n, 
 }
 
 // Temperature exchange between neighbouring rungs (findPartner, move.h:6621-6633:
-// one shared uniform picks the pairing (0,1)(2,3).. or (1,2)(3,4)..; then per
-// pair the Metropolis test on (beta_i - beta_j)(U_a - U_b), U_a the running
-// total energy of the system at rung i). perm[rung] = system; the swap
-// exchanges perm entries and the systems' kT. One thread; n is small.
+// one uniform picks the pairing (0,1)(2,3).. or (1,2)(3,4)..; then per pair
+// the Metropolis test of _energyChange, move.h:6700-6722: the total
+// dU = [U_i(x_b) - U_i(x_a)] + [U_p(x_a) - U_p(x_b)] = (beta_i - beta_p)(E_b - E_a)
+// with E_a the energy of the system a at rung i, exchanged iff not u > exp(-dU)).
+// perm[rung] = system; the swap exchanges perm entries and the systems' kT
+// (the configurations stay where they are). By default the uniforms come from
+// Philox (counter = the round) and E from the systems' running totals; with
+// `given` = {u_direction, u_accept} every pair takes that one acceptance
+// uniform (the reference's ranks all draw the same one from their global
+// generator) and with `energies` E comes from that array (per system).
+// One thread; n is small.
 __global__ void pt_swap_kernel(SysDesc *__restrict__ descs, int n, int *__restrict__ perm,
                                const double *__restrict__ temps, uint32_t seed, int64_t *__restrict__ round,
-                               long long *__restrict__ attempts, long long *__restrict__ accepts) {
+                               long long *__restrict__ attempts, long long *__restrict__ accepts,
+                               const double *__restrict__ given, const double *__restrict__ energies) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int64_t rd = *round;
     const u4 r = philox4x32_10(u4{(uint32_t)rd, (uint32_t)(rd >> 32), 0u, 0x50540000u}, seed, 0x50545054u);
-    const int dr = ((double)r.x * (1.0 / 4294967296.0) > 0.5) ? 1 : -1;
+    const double udir = given ? given[0] : (double)r.x * (1.0 / 4294967296.0);
+    const int dr = udir > 0.5 ? 1 : -1;
     for (int i = 0; i < n; i++) {
         const int p = (i % 2 == 0) ? i + dr : i - dr;
         if (p <= i || p >= n) continue;
         const int a = perm[i], b = perm[p];
         const SysScalars *sa = descs[a].sc, *sb = descs[b].sc;
-        const double ua = (double)sa->utot_hi + (double)sa->utot_lo;
-        const double ub = (double)sb->utot_hi + (double)sb->utot_lo;
+        const double ua = energies ? energies[a] : (double)sa->utot_hi + (double)sa->utot_lo;
+        const double ub = energies ? energies[b] : (double)sb->utot_hi + (double)sb->utot_lo;
         const double arg = (1.0 / temps[i] - 1.0 / temps[p]) * (ua - ub);
         const u4 q = philox4x32_10(u4{(uint32_t)rd, (uint32_t)(rd >> 32), (uint32_t)i, 0x50540001u}, seed, 0x50545054u);
-        const double u = ((double)q.x + 0.5) * (1.0 / 4294967296.0);
+        const double u = given ? given[1] : ((double)q.x + 0.5) * (1.0 / 4294967296.0);
         attempts[i]++;
         if (!(u > exp(arg))) {
             accepts[i]++;
@@ -107,6 +116,7 @@ struct fg_batch {
     double *d_temps = nullptr;
     int64_t *d_round = nullptr;
     long long *d_att = nullptr, *d_acc = nullptr;
+    double *d_given = nullptr;        // fg_pt_swap: {u_direction, u_accept}, then per-system energies
     uint32_t pt_seed = 0;
     bool pt = false;
     cudaGraphExec_t graph = nullptr;
@@ -115,6 +125,8 @@ struct fg_batch {
     // run captured once and replayed
     cudaGraphExec_t run_graph = nullptr;
     int run_graph_kernels = 0;
+    bool in_kernel_rebuild = false;
+    int rebuild_mode = 0;   // 0: in-kernel when the batch fills the GPU, 1: always, 2: never
     // Debye-Hueckel members without a cell list run the block kernel
     bool dh_block = false;
     DhGroups dh;
@@ -148,8 +160,12 @@ int batch_config(fg_batch *b) {
         cudaGraphExecDestroy(b->run_graph);
         b->run_graph = nullptr;
     }
-    // the Ewald block kernel rebuilds Q(k) inside the sweep
-    b->rebuilds = b->maxK > 0 && !h0->desc.skip_rebuild && !ewald_block_ok(h0);
+    // the Ewald block kernel rebuilds Q(k) inside the sweep when the batch
+    // fills the GPU (at least one system per SM); smaller batches leave the
+    // rebuilds to the rebuild kernel, which spreads them over all SMs
+    b->in_kernel_rebuild = ewald_block_ok(h0) && (b->rebuild_mode == 1 ||
+                                                  (b->rebuild_mode == 0 && (int)b->sys.size() >= dh_sm_count()));
+    b->rebuilds = b->maxK > 0 && !h0->desc.skip_rebuild && !b->in_kernel_rebuild;
     b->dh_block = true;
     std::vector<int> Ns;
     std::vector<double> w;
@@ -180,6 +196,7 @@ int batch_push_descs(fg_batch *b) {
         // buffers hold the member's whole stream
         const bool log = h->log_batch && !b->pt && h->log_cap >= h->n_trials;
         h->desc.log_trials = log ? 1 : 0;
+        h->desc.rebuild_in_kernel = b->in_kernel_rebuild ? 1 : 0;
         h->desc.trial_du = h->log_du;
         h->desc.trial_acc = h->log_acc;
         v[s] = h->desc;
@@ -336,7 +353,7 @@ int batch_run(fg_batch *b, const std::vector<int64_t> &counts, fg_sweep_stats *p
 
 void batch_free(fg_batch *b) {
     void *ptrs[] = {b->d_descs, b->d_gather, b->d_corr, b->d_counts, b->d_perm, b->d_temps, b->d_round, b->d_att,
-                    b->d_acc};
+                    b->d_acc, b->d_given};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -456,6 +473,12 @@ int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total)
     return rc;
 }
 
+int fg_batch_set_rebuild_mode(fg_batch *b, int32_t mode) {
+    if (!b || mode < 0 || mode > 2) return fail(FG_ERR_INVALID, "mode must be 0, 1 or 2");
+    b->rebuild_mode = mode;
+    return batch_config(b);
+}
+
 int fg_batch_set_log(fg_batch *b, int32_t member, int32_t on) {
     if (!b || member < 0 || member >= (int)b->sys.size()) return fail(FG_ERR_INVALID, "bad member");
     b->sys[member]->log_batch = on != 0;
@@ -474,6 +497,7 @@ int fg_pt_setup(fg_batch *b, const double *temperatures, uint32_t seed) {
         CK(cudaMalloc(&b->d_round, sizeof(int64_t)));
         CK(cudaMalloc(&b->d_att, n * sizeof(long long)));
         CK(cudaMalloc(&b->d_acc, n * sizeof(long long)));
+        CK(cudaMalloc(&b->d_given, (2 + n) * sizeof(double)));
     }
     std::vector<int> perm(n);
     for (int i = 0; i < n; i++) {
@@ -551,7 +575,7 @@ int fg_pt_run(fg_batch *b, int32_t rounds, int32_t sweeps_per_round, fg_sweep_st
             }
         }
         fg::pt_swap_kernel<<<1, 32, 0, b->stream>>>(b->d_descs, n, b->d_perm, b->d_temps, b->pt_seed, b->d_round,
-                                                    b->d_att, b->d_acc);
+                                                    b->d_att, b->d_acc, nullptr, nullptr);
         cudaError_t e = cudaStreamEndCapture(b->stream, &g);
         if (e != cudaSuccess) return fail(FG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
         e = cudaGraphInstantiate(&b->graph, g, 0);
@@ -586,6 +610,40 @@ int fg_pt_run(fg_batch *b, int32_t rounds, int32_t sweeps_per_round, fg_sweep_st
     tot.kernel_launches = 4 * (int64_t)rounds + 2;   // philox, reset, sweep, swap per round
     if (total) *total = tot;
     if (errs) return fail(FG_ERR_DEVICE, "device error flags 0x%x", errs);
+    return FG_OK;
+}
+
+// One exchange attempt with caller-given randoms (and energies): the same
+// kernel as the captured rounds, run once; the host copies of the systems'
+// temperatures follow the new permutation, so that later fg_batch_run calls
+// (which push the host descriptors) keep them.
+int fg_pt_swap(fg_batch *b, double u_direction, double u_accept, const double *energies, int32_t *exchanged) {
+    if (!b || !b->pt) return fail(FG_ERR_STATE, "fg_pt_setup first");
+    if (!(u_direction >= 0.0 && u_direction <= 1.0) || !(u_accept >= 0.0 && u_accept <= 1.0))
+        return fail(FG_ERR_INVALID, "uniforms must lie in [0, 1]");
+    const int n = (int)b->sys.size();
+    std::vector<double> g(2 + n, 0.0);
+    g[0] = u_direction;
+    g[1] = u_accept;
+    if (energies)
+        for (int i = 0; i < n; i++) {
+            if (!std::isfinite(energies[i])) return fail(FG_ERR_INVALID, "non-finite energy of system %d", i);
+            g[2 + i] = energies[i];
+        }
+    std::vector<int> before(n), after(n);
+    CK(cudaMemcpyAsync(before.data(), b->d_perm, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaMemcpyAsync(b->d_given, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    fg::pt_swap_kernel<<<1, 32, 0, b->stream>>>(b->d_descs, n, b->d_perm, b->d_temps, b->pt_seed, b->d_round,
+                                                b->d_att, b->d_acc, b->d_given, energies ? b->d_given + 2 : nullptr);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(after.data(), b->d_perm, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    std::vector<double> temps(n);
+    CK(cudaMemcpyAsync(temps.data(), b->d_temps, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < n; i++) {
+        b->sys[after[i]]->desc.kT = (float)temps[i];
+        if (exchanged) exchanged[i] = before[i] != after[i] ? 1 : 0;
+    }
     return FG_OK;
 }
 
@@ -849,6 +907,7 @@ int fg_server_step(fg_server *s, int32_t *n_running, int32_t *n_finished, double
         h->desc.trials = h->trials;
         h->desc.log_trials = 0;
         h->desc.skip_rebuild = 1;
+        h->desc.rebuild_in_kernel = 0;
         h->desc.stream_first = j->done;
         descs[i] = h->desc;
         if (dh_block_ok(h)) {

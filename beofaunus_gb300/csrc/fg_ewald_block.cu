@@ -17,9 +17,11 @@
 // Q(k) itself stays the exact fixed-point sum: after the block each accepted
 // trial's integer contributions are applied in order. A trial whose particle
 // an accepted trial of the block already moved ends the block, and so does
-// the accepted trial that makes a Q(k) rebuild due: the CTA then rebuilds its
-// system's Q(k) from scratch in place (eb_rebuild) and carries on, so one
-// launch runs a system's whole stream.
+// the accepted trial that makes a Q(k) rebuild due. In a batch that fills the
+// GPU the CTA then rebuilds its system's Q(k) from scratch in place
+// (eb_rebuild) and carries on, so one launch runs every system's whole
+// stream; a system running alone exits instead and leaves the rebuild to the
+// rebuild kernel, which spreads it over all SMs.
 namespace fg {
 
 constexpr int kEbTrials = 32;
@@ -748,6 +750,7 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
         }
         cur += done;
         __syncthreads();
+        if (rebuild && !d.rebuild_in_kernel) break;   // the rebuild kernel takes it (rebuild_pending)
         if (rebuild) {
             df corr;
             const bool mism = eb_rebuild(d, s, corr);
@@ -774,6 +777,7 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             sc->m[a][1] = s.Mdf[a].y;
         }
         sc->cnt_accepted = cnt_acc;
+        if (rebuild) sc->rebuild_pending = 1;
         sc->error |= err;
     }
 }

@@ -40,9 +40,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 // Caller coordinates (double, Angstrom) -> the fixed-point records the pair
 // kernels read, with the same rounding as the host upload (fg_set_state).
-__global__ void noalloc_convert_kernel(int n, int n_types, const double *__restrict__ xyz,
+// The box comes in double precision (the descriptor holds it as float).
+__global__ void noalloc_convert_kernel(int n, int n_types, double3 box, const double *__restrict__ xyz,
                                        const double *__restrict__ charge, const int32_t *__restrict__ types) {
-    SysDesc &d = *reinterpret_cast<SysDesc *>(g_noalloc_scratch + kNoallocDesc);
     int4 *pos4 = reinterpret_cast<int4 *>(g_noalloc_scratch + kNoallocPos4);
     short4 *ext = reinterpret_cast<short4 *>(g_noalloc_scratch + kNoallocExt);
     uint8_t *pt = reinterpret_cast<uint8_t *>(g_noalloc_scratch + kNoallocType);
@@ -50,7 +50,7 @@ __global__ void noalloc_convert_kernel(int n, int n_types, const double *__restr
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int h[3], e[3];
         for (int a = 0; a < 3; a++) {
-            const double L = (double)d.L[a];
+            const double L = a == 0 ? box.x : (a == 1 ? box.y : box.z);
             double f = xyz[3 * i + a] / L;
             f -= floor(f + 0.5);
             const int64_t X = (int64_t)((uint64_t)(int64_t)__double2ll_rn(f * 4611686018427387904.0) << 2);
@@ -236,7 +236,8 @@ int fg_pair_energy_noalloc(const fg_params *params, int32_t n, const double *d_x
         CK(cudaMemcpyAsync(base + fg::kNoallocTab0, t0.data(), ntab * sizeof(float4), cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(base + fg::kNoallocTab1, t1.data(), ntab * sizeof(float4), cudaMemcpyHostToDevice, st));
     }
-    fg::noalloc_convert_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, nt, d_xyz, d_charge, d_types);
+    fg::noalloc_convert_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, nt, make_double3(P.box[0], P.box[1], P.box[2]),
+                                                                 d_xyz, d_charge, d_types);
     using PairFn = void (*)(const SysDesc *, float2 *);
     PairFn fn = P.model == FG_MODEL_EWALD_WCA ? fg::pair_total_kernel<fg::MODEL_EWALD>
                                                : fg::pair_total_kernel<fg::MODEL_DHLJ>;

@@ -80,6 +80,7 @@ struct alignas(16) SysDesc {
     float kT;                  // temperature scale of the Boltzmann factor
     int32_t update_frequency;
     int32_t skip_rebuild;      // do not stop sweeps for Q(k) rebuilds
+    int32_t rebuild_in_kernel; // the Ewald block kernel rebuilds Q(k) itself (else it exits for the rebuild kernel)
     int32_t log_trials;        // write per-trial dU/accept
     // per-type-pair tables (row-major nt*nt) and per-type effective charge
     float s2[kMaxTypes * kMaxTypes];

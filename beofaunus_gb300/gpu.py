@@ -79,10 +79,12 @@ def lib(build_if_missing=True):
             "fg_batch_run": ([vp, dp, dp], ctypes.c_int),
             "fg_batch_stream_upload": ([vp, i32, i64, dp, dp, dp], ctypes.c_int),
             "fg_batch_set_log": ([vp, i32, i32], ctypes.c_int),
+            "fg_batch_set_rebuild_mode": ([vp, i32], ctypes.c_int),
             "fg_log_get": ([vp, i64, i64, dp, dp], ctypes.c_int),
             "fg_pt_setup": ([vp, dp, u32], ctypes.c_int),
             "fg_pt_run": ([vp, i32, i32, dp], ctypes.c_int),
             "fg_pt_get": ([vp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_pt_swap": ([vp, ctypes.c_double, ctypes.c_double, dp, dp], ctypes.c_int),
             "fg_server_create": ([i64, i32, i64, ctypes.POINTER(vp)], ctypes.c_int),
             "fg_server_destroy": ([vp], ctypes.c_int),
             "fg_server_submit": ([vp, vp, i32, dp, dp, dp, u32, i64, dp], ctypes.c_int),
@@ -476,6 +478,11 @@ class Batch:
         u = np.ascontiguousarray(u, dtype=np.float64)
         _check(lib().fg_batch_stream_upload(self.h, member, len(idx), _p(idx), _p(disp), _p(u)))
 
+    def set_rebuild_mode(self, mode):
+        """0: Q(k) rebuilds inside the sweep launch when the batch fills the
+        GPU, 1: always inside, 2: always in the separate rebuild kernel."""
+        _check(lib().fg_batch_set_rebuild_mode(self.h, int(mode)))
+
     def set_log(self, member, on=True):
         """Log per-trial dU/acceptance of one member in later runs
         (System.log_get reads it)."""
@@ -497,6 +504,15 @@ class Batch:
         tot = SweepStats()
         _check(lib().fg_pt_run(self.h, rounds, sweeps_per_round, ctypes.byref(tot)))
         return tot.as_dict()
+
+    def pt_swap(self, u_direction, u_accept, energies=None):
+        """One exchange attempt with given uniforms (and per-system
+        energies); returns per rung whether its system changed."""
+        n = len(self.systems)
+        ex = np.zeros(n, np.int32)
+        e = None if energies is None else np.ascontiguousarray(energies, dtype=np.float64)
+        _check(lib().fg_pt_swap(self.h, float(u_direction), float(u_accept), _p(e), _p(ex)))
+        return ex
 
     def pt_state(self):
         n = len(self.systems)

@@ -165,6 +165,12 @@ int fg_batch_stream_upload(fg_batch *b, int32_t member, int64_t n, const int32_t
                            const double *u);
 /* Run every member's staged stream; per-member and summed statistics. */
 int fg_batch_run(fg_batch *b, fg_sweep_stats *per_system, fg_sweep_stats *total);
+/* Where the Ewald block kernel's Q(k) rebuilds (every update_frequency
+ * accepted trials, ewald.h:633-640) run: 0 (default) inside the sweep launch
+ * when the batch has at least one member per SM, else in the separate
+ * rebuild kernel spread over all SMs; 1 always inside; 2 never. Results are
+ * identical either way (the rebuild reproduces the exact Q(k)). */
+int fg_batch_set_rebuild_mode(fg_batch *b, int32_t mode);
 /* Record per-trial dU and acceptance of one member in the following
  * fg_batch_run calls (on != 0), or stop (on == 0): the per-move record
  * Movebase::move keeps (move.h:515-555, its dusum and acceptance counters)
@@ -184,6 +190,15 @@ int fg_pt_setup(fg_batch *b, const double *temperatures, uint32_t seed);
  * attempt between each neighbouring pair picked as in findPartner,
  * move.h:6621-6633); one CUDA graph per round. */
 int fg_pt_run(fg_batch *b, int32_t rounds, int32_t sweeps_per_round, fg_sweep_stats *total);
+/* One exchange attempt with the caller's randoms: the pairing from
+ * u_direction (> 0.5: rung 2i with 2i+1, else 2i with 2i-1, as findPartner
+ * draws it, move.h:6621-6633) and, for every pair, the test not
+ * u_accept > exp(-dU) of _energyChange (move.h:6700-6722), dU from
+ * energies[system] (kT at unit temperature; NULL: the running totals).
+ * Replaces the exchange step of Move::ParallelTempering::move when the host
+ * replays the reference's own random streams; exchanged[rung] (or NULL) is 1
+ * where the rung's system changed. */
+int fg_pt_swap(fg_batch *b, double u_direction, double u_accept, const double *energies, int32_t *exchanged);
 /* perm[rung] = member at that temperature; energies[member]; exchange
  * attempts/accepts per rung pair (rung, rung+1). Any pointer may be NULL. */
 int fg_pt_get(fg_batch *b, int32_t *perm, double *energies, int64_t *attempts, int64_t *accepts);

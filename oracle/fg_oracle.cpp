@@ -412,6 +412,37 @@ int or_draw_translation_stream(uint32_t seed, int n_particles, const double *dp_
     return 0;
 }
 
+// The random streams of the reference's parallel tempering run as every
+// rank sees them (all ranks seed the global slump alike, so they draw the
+// same sequence; move.h:558-566 relies on it): per round, trials_per_round
+// AtomicTranslation trials as or_draw_translation_stream draws them, then
+// the one uniform ParallelTempering's Metropolis test takes from the global
+// slump (move.h:567-573; drawn on every rank, with or without a partner),
+// and the uniform findPartner takes from the MPI controller's own generator
+// (default-seeded RandomTwister, move.h:6621-6633).
+int or_pt_streams(uint32_t seed, int n_particles, const double *dp_per_particle, int64_t trials_per_round,
+                  int rounds, int32_t *idx, double *disp, double *umet, double *u_accept, double *u_direction) {
+    Twister t(seed), mpi(5489u);
+    int64_t n = 0;
+    for (int r = 0; r < rounds; r++) {
+        for (int64_t k = 0; k < trials_per_round; k++, n++) {
+            t.range(0, 0);
+            int i = t.range(0, n_particles - 1);
+            double dp = dp_per_particle[i];
+            double tx = dp, ty = dp, tz = dp;
+            tx *= t() - 0.5;
+            ty *= t() - 0.5;
+            tz *= t() - 0.5;
+            idx[n] = i;
+            disp[3 * n] = tx; disp[3 * n + 1] = ty; disp[3 * n + 2] = tz;
+            umet[n] = t();
+        }
+        u_accept[r] = t();
+        u_direction[r] = mpi();
+    }
+    return 0;
+}
+
 // Full Metropolis run (Movebase::move, move.h:515-555, with AtomicTranslation
 // "peratom" on the single atomic group): n_trials trials from the global RNG
 // seeded with `seed`. Optional per-trial logs (any may be NULL). Returns the

@@ -51,6 +51,7 @@ def lib():
         L.or_boundary.argtypes = [vp, dp]
         L.or_draw_translation_stream.argtypes = [u32, i32, dp, i64, dp, dp, dp]
         L.or_uniforms.argtypes = [u32, i64, dp]
+        L.or_pt_streams.argtypes = [u32, i32, dp, i64, i32, dp, dp, dp, dp, dp]
         L.or_mc_run.restype = ctypes.c_double
         L.or_mc_run.argtypes = [vp, u32, i64, dp, dp, dp, dp]
         L.or_philox.argtypes = [dp, dp, dp]
@@ -254,6 +255,47 @@ def translation_stream(seed, dp_per_particle, n_trials):
     u = np.empty(n)
     lib().or_draw_translation_stream(seed, len(dpp), _ptr(dpp), n, _ptr(idx), _ptr(disp), _ptr(u))
     return idx, disp, u
+
+
+def pt_streams(seed, dp_per_particle, trials_per_round, rounds):
+    """The reference's parallel-tempering random streams (the same on every
+    rank): per round the AtomicTranslation trials (idx, disp, u), the
+    exchange's Metropolis uniform and findPartner's uniform."""
+    dpp = np.ascontiguousarray(dp_per_particle, dtype=np.float64)
+    n = int(trials_per_round) * int(rounds)
+    idx = np.empty(n, np.int32)
+    disp = np.empty((n, 3))
+    u = np.empty(n)
+    ua = np.empty(rounds)
+    ud = np.empty(rounds)
+    lib().or_pt_streams(seed, len(dpp), _ptr(dpp), int(trials_per_round), int(rounds), _ptr(idx), _ptr(disp),
+                        _ptr(u), _ptr(ua), _ptr(ud))
+    T = int(trials_per_round)
+    return [(idx[r * T:(r + 1) * T], disp[r * T:(r + 1) * T], u[r * T:(r + 1) * T]) for r in range(rounds)], ua, ud
+
+
+def pt_exchange(energies, temps, perm, u_direction, u_accept):
+    """One exchange attempt of Move::ParallelTempering (move.h:6621-6771)
+    restated over a ladder held in one process: rung i holds configuration
+    perm[i] with energy energies[perm[i]] (kT at unit temperature). findPartner:
+    dr = +1 if u_direction > 0.5 else -1; even rungs pair with i + dr, odd ones
+    with i - dr. Each pair tests dU = [U_i(x_p) - U_i(x_i)] + [U_p(x_i) - U_p(x_p)],
+    U_i = E / T_i, against the shared uniform: exchanged iff not u > exp(-dU).
+    Returns the new perm and, per rung, whether it exchanged."""
+    n = len(perm)
+    perm = list(perm)
+    dr = 1 if u_direction > 0.5 else -1
+    swapped = [0] * n
+    for i in range(n):
+        p = i + dr if i % 2 == 0 else i - dr
+        if p <= i or p >= n:
+            continue
+        ea, eb = energies[perm[i]], energies[perm[p]]
+        du = (eb - ea) / temps[i] + (ea - eb) / temps[p]
+        if not (u_accept > np.exp(-du)):
+            perm[i], perm[p] = perm[p], perm[i]
+            swapped[i] = swapped[p] = 1
+    return perm, swapped
 
 
 class OracleMol:

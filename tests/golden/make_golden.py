@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
 Runs the reference harnesses (oracle/ref/ref_harness.cpp,
-ref_harness_mol.cpp and ref_harness_dip.cpp, linked against the reference library built from its own
+ref_harness_mol.cpp, ref_harness_dip.cpp and ref_harness_pt.cpp, linked against the reference library built from its own
 sources by oracle/ref/Makefile) on seeded synthetic systems and stores what
 the reference computed: per-trial particle (or molecule) index, trial
 position, dU and acceptance, plus the total energies before and after. Needs
@@ -201,6 +201,58 @@ def make_dip(exe):
         print(name, "trials", n, "acceptance %.3f" % np.mean(out["acc"]), "u0 %.6f" % out["u0"][0])
 
 
+# Parallel tempering: ranks (rungs), ions per rank, seed, rounds, sweeps per
+# round, temperature ladder (geometric, reduced units)
+PT_CASE = dict(ranks=8, n=240, density=0.006, seed=7, rounds=16, sweeps=4, t_min=0.6, t_max=3.0)
+
+
+def make_pt(exe):
+    """The reference's own ParallelTempering (move.h:6520-6771) over one
+    process per rung (oracle/ref/ref_harness_pt.cpp with the stand-in MPI of
+    oracle/ref/fakempi), DH+LJ salt, AtomicTranslation sweeps between the
+    exchange attempts. Stores what each rank computed."""
+    c = PT_CASE
+    R, N = c["ranks"], c["n"]
+    temps = workloads.pt_temperatures(R, c["t_min"], c["t_max"])
+    cases = [workloads.dh_lj_salt(N, seed=100 + r, density=c["density"]) for r in range(R)]
+    params, _, q, ids = cases[0]
+    types = [dict(q=params.type_charge[t], sigma=params.type_sigma[t], eps=params.type_eps[t],
+                  dp=params.type_dp[t]) for t in range(params.n_types)]
+    d = dict(box=params.box[0], bjerrum=params.bjerrum, debyelength=params.dh_debye_length, types=types,
+             type_ids=[int(i) for i in ids], seed=c["seed"], rounds=c["rounds"], sweeps_per_round=c["sweeps"],
+             ranks=[dict(temperature=float(temps[r]), positions=cases[r][1].tolist()) for r in range(R)])
+    with tempfile.TemporaryDirectory() as tmp:
+        fin = os.path.join(tmp, "in.json")
+        with open(fin, "w") as f:
+            json.dump(d, f)
+        procs = []
+        for r in range(R):
+            env = dict(os.environ, FAKEMPI_RANK=str(r), FAKEMPI_SIZE=str(R), FAKEMPI_DIR=tmp,
+                       FAKEMPI_TIMEOUT="120")
+            procs.append(subprocess.Popen([exe, fin, os.path.join(tmp, "out")], cwd=tmp, env=env,
+                                          stdout=subprocess.DEVNULL))
+        rcs = [p.wait(timeout=600) for p in procs]
+        if any(rcs):
+            raise RuntimeError("parallel tempering ranks failed: %s" % rcs)
+        outs = []
+        for r in range(R):
+            with open(os.path.join(tmp, "out%d.json" % r)) as f:
+                outs.append(json.load(f))
+    stack = lambda k: np.asarray([o[k] for o in outs], dtype=np.float64)
+    # the base Bjerrum length (unit temperature) as the reference rounds it
+    lB = outs[0]["bjerrum"][0] * temps[0]
+    np.savez_compressed(
+        os.path.join(HERE, "pt_dhlj.npz"), params=np.frombuffer(bytes(params), dtype=np.uint8),
+        bjerrum=np.float64(lB), temps=np.asarray(temps), xyz=np.stack([cs[1] for cs in cases]), q=q, ids=ids,
+        seed=np.int64(c["seed"]), rounds=np.int64(c["rounds"]), sweeps=np.int64(c["sweeps"]),
+        u_direction=stack("u_direction"), u_accept=stack("u_accept"), uold=stack("uold"), unew=stack("unew"),
+        acc=stack("acc").astype(np.uint8), translations_accepted=stack("translations_accepted"),
+        u0=stack("u0")[:, 0], u1=stack("u1")[:, 0],
+        final_positions=stack("final_positions").reshape(R, N, 3))
+    acc = stack("acc")
+    print("pt_dhlj ranks", R, "rounds", c["rounds"], "exchange acceptance by rung", acc.mean(axis=1).round(2))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=None)
@@ -214,6 +266,10 @@ def main():
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "REF=" + a.ref])
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
     exe_mol = os.path.join(ROOT, "oracle", "_ref", "ref_harness_mol")
+    if a.only in (None, "pt"):
+        make_pt(os.path.join(ROOT, "oracle", "_ref", "ref_harness_pt"))
+        if a.only:
+            return
     if a.only in (None, "dip"):
         make_dip(os.path.join(ROOT, "oracle", "_ref", "ref_harness_dip"))
         if a.only:

@@ -39,38 +39,55 @@ def _check(res):
     assert res["max_err"] <= TOL_DU, res
 
 
-def test_batched_rpm16k_block_kernel_matches_oracle():
+def _batched_run(cases, T, mode):
+    """Run the cases as one batch with every trial logged; the rebuilds run
+    inside the sweep launch (mode 1) or in the rebuild kernel (mode 2)."""
     from beofaunus_gb300.gpu import Batch, System
-    B, T = 4, 1500
-    cases = [workloads.rpm16k(seed=300 + b, update_frequency=1000, start="scatter") for b in range(B)]
     systems = [System(p, x, q, i) for p, x, q, i in cases]
     batch = Batch(systems)
-    for m in range(B):
+    batch.set_rebuild_mode(mode)
+    for m in range(len(cases)):
         batch.set_log(m)
-    batch.stream_philox([T] * B, 4242)
+    batch.stream_philox([T] * len(cases), 4242)
     per, tot = batch.run()
-    assert tot["trials"] == B * T
-    assert tot["rebuilds"] >= B   # uf = 1000 accepted: every chain crosses a rebuild
-    jobs, dev = [], []
-    for m, (p, x, q, i) in enumerate(cases):
-        idx, disp, u = systems[m].stream_get(0, T)
-        du, acc = systems[m].log_get(0, T)
-        dev.append((du, acc, u))
-        jobs.append((bytes(p), x, q, i, idx, disp, u))
-    with _pool(B) as pool:
-        ref = pool.map(replay_chain, jobs)
-    worst = 0.0
-    for m in range(B):
-        du, acc, u = dev[m]
-        res = compare_chain(du, acc, ref[m][0], ref[m][1], u, TOL_DU)
-        print("member %d: max |dU err| %.3g rms %.3g over %d trials" % (m, res["max_err"], res["rms_err"],
-                                                                         res["compared"]))
-        _check(res)
-        assert per[m]["accepted"] == int(np.sum(acc))
-        worst = max(worst, res["max_err"])
+    out = []
+    for m, s in enumerate(systems):
+        idx, disp, u = s.stream_get(0, T)
+        du, acc = s.log_get(0, T)
+        out.append(dict(idx=idx, disp=disp, u=u, du=du, acc=acc, pos=s.positions(), qk=s.qk(),
+                        accepted=per[m]["accepted"]))
     batch.close()
     for s in systems:
         s.close()
+    return out, tot
+
+
+def test_batched_rpm16k_block_kernel_matches_oracle():
+    """Both places of the Q(k) rebuild (inside the persistent sweep, as the
+    bench's batch of one system per SM runs it, and the separate rebuild
+    kernel) give bit-identical chains, and those match the oracle."""
+    B, T = 4, 1500
+    cases = [workloads.rpm16k(seed=300 + b, update_frequency=1000, start="scatter") for b in range(B)]
+    inside, tot = _batched_run(cases, T, 1)
+    outside, tot2 = _batched_run(cases, T, 2)
+    assert tot["trials"] == B * T
+    assert tot["rebuilds"] >= B and tot["rebuilds"] == tot2["rebuilds"]   # uf = 1000 accepted: every chain rebuilds
+    assert tot["sweep_launches"] == 1
+    for a, b in zip(inside, outside):
+        np.testing.assert_array_equal(a["du"], b["du"])
+        np.testing.assert_array_equal(a["acc"], b["acc"])
+        np.testing.assert_array_equal(a["pos"], b["pos"])
+        np.testing.assert_array_equal(a["qk"], b["qk"])
+    jobs = [(bytes(p), x, q, i, r["idx"], r["disp"], r["u"]) for (p, x, q, i), r in zip(cases, inside)]
+    with _pool(B) as pool:
+        ref = pool.map(replay_chain, jobs)
+    for m in range(B):
+        r = inside[m]
+        res = compare_chain(r["du"], r["acc"], ref[m][0], ref[m][1], r["u"], TOL_DU)
+        print("member %d: max |dU err| %.3g rms %.3g over %d trials" % (m, res["max_err"], res["rms_err"],
+                                                                         res["compared"]))
+        _check(res)
+        assert r["accepted"] == int(np.sum(r["acc"]))
 
 
 def test_rpm16k_error_tail_over_1e5_trials():
