@@ -268,7 +268,91 @@ class CpuPath:
                 "value = %s" % (self.cores, ", ".join(ks[:6]) + (" ..." if len(ks) > 6 else ""), seconds, trials, how))
 
 
+# ----------------------------------------------------------------- the reference itself on the host
+REF_HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def _ref_input(kind, seed, seconds, steps, warmup):
+    """Input of the reference harness for one host process: the reference's
+    own Space, energy (NonbondedEwald<WCA> or Nonbonded<DH + LJ>) and
+    AtomicTranslation on the workload kind's system, time-bounded samples.
+    None where the kind has no reference run here (molecules, dipoles)."""
+    from beofaunus_gb300 import workloads
+    kT = 1.0
+    if kind == "rpm16k":
+        p, xyz, q, ids = workloads.rpm16k(seed=seed, update_frequency=1000, start="scatter")
+    elif kind == "rpm800":
+        p, xyz, q, ids = workloads.rpm800(seed=seed, update_frequency=1000)
+    elif kind.startswith("dhlj"):
+        n, t = kind[4:].split("@") if "@" in kind else (kind[4:], "1.0")
+        kT = float(t)
+        p, xyz, q, ids = workloads.dh_lj_salt(int(n), seed, start="scatter")
+    else:
+        return None
+    ewald = p.model == 1
+    # a temperature T scales every energy by 1/T: the Bjerrum length and the
+    # LJ epsilons are given at T
+    types = [dict(q=p.type_charge[t], sigma=p.type_sigma[t], eps=p.type_eps[t] / kT, dp=p.type_dp[t])
+             for t in range(p.n_types)]
+    d = dict(mode="bench", model="ewald_wca" if ewald else "dh_lj", box=p.box[0], bjerrum=p.bjerrum / kT,
+             types=types, positions=xyz.tolist(), type_ids=[int(i) for i in ids], seed=seed, sweeps=0,
+             seconds=seconds, steps=steps, warmup=warmup)
+    if ewald:
+        d.update(alpha=p.ewald_alpha, cutoff=p.ewald_cutoff, cutoffK=p.ewald_cutoff_k, eps_surf=p.ewald_eps_surf,
+                 debyelength=p.ewald_debye_length, spherical_sum=bool(p.ewald_spherical_sum),
+                 update_frequency=int(p.ewald_update_frequency))
+    else:
+        d.update(debyelength=p.dh_debye_length)
+    return d
+
+
+def ref_path_available(kinds):
+    return os.path.exists(REF_HARNESS) and all(not k.startswith(("molecules", "dipoles")) for k in kinds)
+
+
+def ref_cpu_rates(kinds, weights, seconds, steps, warmup, cores=None):
+    """The reference's own CPU path (oracle/_ref/ref_harness, the reference
+    built from its sources on this machine) on every host core: one process
+    per core, each its own system and seed. Returns per timed step the rate
+    of all cores (identical systems: the sum of the per-process rates; a size
+    mix: cores / trial-weighted mean time per trial), the total trials and
+    the core count."""
+    cores = cores or os.cpu_count() or 1
+    ks = [kinds[c % len(kinds)] for c in range(cores)]
+    ws = None if weights is None else [weights[c % len(weights)] for c in range(cores)]
+    with tempfile.TemporaryDirectory() as tmp:
+        procs = []
+        for c, k in enumerate(ks):
+            fin, fout = os.path.join(tmp, "in%d.json" % c), os.path.join(tmp, "out%d.json" % c)
+            with open(fin, "w") as f:
+                json.dump(_ref_input(k, 1000 + c, seconds, steps, warmup), f)
+            procs.append((subprocess.Popen([REF_HARNESS, fin, fout], cwd=tmp, stdout=subprocess.DEVNULL,
+                                           stderr=subprocess.DEVNULL), fout))
+        rates = []
+        for pr, fout in procs:
+            if pr.wait(timeout=600 + 2 * (steps + warmup) * seconds) != 0:
+                raise RuntimeError("reference harness failed")
+            with open(fout) as f:
+                rates.append(json.load(f)["rates"])
+    per_step = []
+    for s in range(steps):
+        r = [rates[c][s] for c in range(cores)]
+        if ws is None:
+            per_step.append(sum(r))
+        else:
+            per_step.append(cores * sum(ws) / sum(w / x for w, x in zip(ws, r)))
+    trials = int(sum(sum(x) for x in rates) * seconds)
+    return per_step, trials, cores, sorted(set(ks))
+
+
 def cpu_baseline(seconds, kinds=("rpm16k",), weights=None):
+    if ref_path_available(kinds):
+        vals, trials, cores, ks = ref_cpu_rates(list(kinds), weights, seconds, 1, 0)
+        return {"value": vals[0], "unit": UNIT, "cores": cores, "kind": "reference",
+                "sample": "the reference built from its own sources on this machine (oracle/_ref/ref_harness: "
+                          "Space, NonbondedEwald<WCA> or Nonbonded<DH+LJ>, AtomicTranslation), %d processes (one "
+                          "per host core), each its own system (%s), %.0f s of trials each (%d in total)"
+                          % (cores, ", ".join(ks[:6]), seconds, trials)}
     cp = CpuPath(list(kinds), weights)
     try:
         cp.sample(0.2)                      # build each process's system outside the sample
@@ -1191,9 +1275,29 @@ def run_serving(args, rank, world):
 
 
 def run_reference(args):
-    """The reference's CPU path on the host cores: the FP64 oracle port (the
-    reference binary built from source is x86-only here and does not travel)."""
+    """The reference's CPU path on the host cores: the reference itself,
+    built from its sources on this machine (oracle/_ref/ref_harness) where
+    the workload has a reference run here, else the FP64 oracle port."""
     warm, steps = args.warmup, args.steps
+    kinds, weights = cpu_kinds(args.workload)
+    if ref_path_available(kinds):
+        vals, trials, cores, ks = ref_cpu_rates(kinds, weights, args.ref_seconds, steps, warm)
+        value = statistics.mean(vals)
+        cfg = workload_config(cores, "time-bounded sample per step") if args.workload == "rpm16k" else \
+            {"workload": WORKLOAD_NAMES[args.workload], "systems": cores, "per_step": "time-bounded sample"}
+        out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+               "steps": steps, "warmup": warm, "ms_per_step": 1e3 * args.ref_seconds,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "data": "synthetic (seeded overlap-free starts, the reference's own mt19937 stream)",
+               "config": cfg,
+               "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "reference",
+                                "sample": "the reference built from its own sources on this machine "
+                                          "(oracle/_ref/ref_harness), %d processes (one per host core), each "
+                                          "its own system (%s); per step %.1f s of trials per process, %d "
+                                          "trials in all" % (cores, ", ".join(ks[:6]), args.ref_seconds, trials)},
+               "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
     cp = CpuPath(*cpu_kinds(args.workload))
     try:
         cp.sample(0.2)

@@ -15,7 +15,11 @@
 //              Logs every trial: particle index, trial position, dU, accept.
 //   "ewald_known" : the ion-ion part of the reference's Ewald unit test
 //              (src/examples/unittests.cpp:131-170) with charged atom types.
-//   "bench"  : like "mc" but logs nothing; prints trials/s.
+//   "bench"  : like "mc" but logs nothing; prints trials/s. With a "seconds"
+//              entry the move runs one trial per call ("peratom" off: the same
+//              draws per trial) and the run is `warmup` + `steps` samples of
+//              at least that many seconds each; "rates" lists the timed
+//              samples' trials/s (the CPU reference of the benchmark).
 //   "isobaric" : the same Space and pair energy plus Energy::ExternalPressure
 //              (energy.h:1817-1890), driven by Move::Isobaric (move.h:5424-5640)
 //              as bulk.cpp wires them; logs every volume move: dU, acceptance
@@ -131,12 +135,21 @@ static Tmjson faunus_input(const Tmjson &in) {
     int t = 0;
     for (auto &ty : in["types"]) {
         std::string name = "T" + std::to_string(t++);
-        j["atomlist"][name] = {{"q", ty["q"]}, {"sigma", ty["sigma"]}, {"dp", ty["dp"]}};
+        // the time-bounded bench builds the Space with point atoms: the
+        // reference then inserts the N particles without overlap tests (every
+        // position and atom parameter is set right after construction, and
+        // the global random stream is seeded after that)
+        const double sig = in.count("seconds") ? 0.0 : ty["sigma"].get<double>();
+        j["atomlist"][name] = {{"q", ty["q"]}, {"sigma", sig}, {"dp", ty["dp"]}};
         atoms += (atoms.empty() ? "" : " ") + name;
     }
     // one atomic group holding all N particles (Space::insert merges atomic groups)
     j["atomlist"]["T0"]["Ninit"] = 0;
-    j["moleculelist"]["salt"] = {{"atoms", "T0"}, {"Ninit", N}, {"atomic", true}};
+    // the time-bounded bench inserts one particle here and the other N - 1
+    // in one call after construction (run_mc): the reference's atom tracker
+    // re-registers the whole group on every insert, which is cubic in N when
+    // the N particles arrive one at a time
+    j["moleculelist"]["salt"] = {{"atoms", "T0"}, {"Ninit", in.count("seconds") ? 1 : N}, {"atomic", true}};
     double lB_target = in["bjerrum"];
     pc::setT(j["system"]["temperature"].get<double>());
     j["energy"]["nonbonded"]["epsr"] = pc::lB(1.0) / lB_target;
@@ -156,7 +169,15 @@ static Tmjson faunus_input(const Tmjson &in) {
 template<class Tenergy>
 static void run_mc(const Tmjson &in, Out &out, bool bench) {
     Tmjson j = faunus_input(in);
+    const bool timed = bench && in.count("seconds");
+    if (timed) j["moves"]["atomtranslate"]["salt"]["peratom"] = false;
     Tspace spc(j);
+    if (timed) {   // the rest of the atomic group in one Space::insert (space.h:950-1000)
+        const int N = in["positions"].size();
+        Tspace::ParticleVector more(N - 1);
+        for (auto &x : more) x = atom[atom["T0"].id];
+        spc.insert(spc.molList()["salt"].id, more);
+    }
     // per-type parameters straight into the atom map (eps in kT, no kJ/mol round trip)
     int t = 0;
     for (auto &ty : in["types"]) {
@@ -182,6 +203,24 @@ static void run_mc(const Tmjson &in, Out &out, bool bench) {
     mv.log = !bench;
     slump.seed(in.value("seed", 5489u));
     out.set("bjerrum", pot.pairpot.first.bjerrumLength());
+    if (timed) {
+        const double secs = in["seconds"];
+        const int steps = in.value("steps", 1), warm = in.value("warmup", 0);
+        std::vector<double> rates;
+        for (int s = 0; s < warm + steps; s++) {
+            long n = 0;
+            double el = 0;
+            auto t0 = std::chrono::steady_clock::now();
+            do {
+                for (int k = 0; k < 8; k++) mv.move();
+                n += 8;
+                el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            } while (el < secs);
+            if (s >= warm) rates.push_back(n / el);
+        }
+        out.set("rates", rates);
+        return;
+    }
     out.set("u0", Energy::systemEnergy(spc, pot, spc.p));
     const int sweeps = in.value("sweeps", 1);
     std::unique_ptr<RdfProbe> rdf;
