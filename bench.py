@@ -19,9 +19,11 @@ molecules per system (TranslateRotate), serving = Poisson job stream through
 the continuous-batching server with p50/p99 job latency, dipoles = point
 dipoles under the dipolar Ewald sum (AtomicRotation + AtomicTranslation).
 
-Under torchrun (N > 1) every rank runs its own replicas (distinct seeds, no
-data-path exchange); value = all ranks' trials over the slowest rank's time
-(reduce_sum_max / reduce_rate).
+With N > 1 every rank runs its own replicas (distinct seeds, no data-path
+exchange); value = all ranks' trials over the slowest rank's time
+(reduce_sum_max / reduce_rate). Started without a launcher, bench.py --gpus N
+starts its N ranks itself under torch.distributed.run (launch_ranks); a run
+whose rank count differs from --gpus stops with an error.
 
 value         batched: B independent systems (default B = number of SMs, one
               persistent CTA per system) advanced by the batched sweep; each
@@ -42,8 +44,10 @@ roofline      the Ewald block kernel against the FP32 pipe (pair and k-space
               only contraction, a tenth of the kernel, on the tensor cores):
               algorithmic FLOP per trial (cost model below) x trials per
               launch / mean launch time.
-cpu_baseline  the FP64 oracle port of the reference's per-trial work, one
-              process per host core, on a time-bounded sample.
+cpu_baseline  the reference's own CPU path, one process per host core, on a
+              time-bounded sample: the reference built from its sources on
+              this machine (oracle/_ref/ref_harness) for the Ewald and DH+LJ
+              workloads, else the FP64 oracle port of its per-trial work.
 --impl reference   that CPU path alone, in the same units (its line is the
               reference arm).
 """
@@ -733,6 +737,21 @@ def reduce_rate(dist, trials, seconds, device):
     return n / t
 
 
+def launch_ranks(n, argv):
+    """bench.py --gpus N started without a launcher: run the same command as
+    N ranks under torch.distributed.run on this node (rendezvous on
+    127.0.0.1, a free port). Returns the launcher's exit status, which is
+    non-zero when any rank failed or did not come up."""
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=%d" % n,
+           "--master-addr=127.0.0.1", "--master-port=%d" % port, os.path.abspath(__file__)] + list(argv)
+    return subprocess.call(cmd)
+
+
 def job_dist():
     """torch.distributed when this run has more than one rank, else None."""
     import torch.distributed as dist
@@ -1351,11 +1370,26 @@ def main():
     ap.add_argument("--check-trials", type=int, default=3000,
                     help="rpm16k: trials per checked member replayed by the FP64 oracle after timing")
     args = ap.parse_args()
+    if args.gpus < 1:
+        raise SystemExit("--gpus must be at least 1")
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # outside a launcher: start the N ranks here (one process per GPU)
+        sys.exit(launch_ranks(args.gpus, sys.argv[1:]))
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world != args.gpus:
+        raise SystemExit("bench.py --gpus %d is running with %d ranks" % (args.gpus, world))
     if args.impl == "reference":
+        if world > 1:
+            # every rank must have come up; rank 0 alone then runs the host path
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            dist.barrier()
         if rank == 0:
             run_reference(args)
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
         return
     if args.workload == "rpm16k":
         args.trials = args.trials or N_IONS

@@ -53,3 +53,30 @@ def test_one_process_needs_no_group():
     import bench
     assert bench.job_dist() is None
     assert bench.reduce_rate(None, 500, 2.0, "cpu") == 250.0
+
+
+def test_bench_gpus_n_starts_n_ranks():
+    """bench.py --gpus 2 started by hand launches its own two ranks (the
+    reference arm: rank 0 runs the host path after every rank has joined a
+    gloo group) and reports n_gpus 2."""
+    import json
+    import subprocess
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "rpm800", "--gpus", "2",
+                        "--steps", "1", "--warmup", "1", "--ref-seconds", "0.3"], cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == 2 and d["impl"] == "reference" and d["value"] > 0
+
+
+def test_bench_refuses_a_rank_count_other_than_gpus():
+    import subprocess
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="", WORLD_SIZE="3", RANK="0")
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1",
+                        "--warmup", "1"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "running with 3 ranks" in r.stderr
