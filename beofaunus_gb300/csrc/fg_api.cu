@@ -95,8 +95,9 @@ struct fg_system {
     int4 *cell_pos = nullptr;
     float4 *kvec = nullptr, *core_tab = nullptr, *core_tab2 = nullptr;
     uint32_t *kpack = nullptr;
-    int2 *kseg = nullptr, *kseg_blk = nullptr;
-    int nseg = 0, nseg_blk = 0;
+    int2 *kseg = nullptr;
+    int4 *rb_items = nullptr;
+    int nseg = 0, n_rb_items = 0;
     longlong2 *qfix = nullptr, *qnew = nullptr;
     SysScalars *sc = nullptr;
     float2 *trial_out = nullptr, *corr = nullptr, *pair_part = nullptr;
@@ -136,7 +137,7 @@ void free_all(fg_system *h) {
     void *ptrs[] = {h->d_desc, h->pos64, h->pos4, h->pos_ext, h->cell_ext, h->ptype, h->cell_count, h->cell_pid,
                     h->p_cell, h->p_slot, h->cell_pos, h->kvec, h->core_tab, h->core_tab2, h->kpack, h->qfix,
                     h->qnew, h->sc, h->trial_out, h->corr, h->pair_part, h->req, h->dp_fix, h->sc_tab, h->trials,
-                    h->log_du, h->log_acc, h->kseg, h->kseg_blk, h->raw_idx, h->raw_disp, h->raw_u};
+                    h->log_du, h->log_acc, h->kseg, h->rb_items, h->raw_idx, h->raw_disp, h->raw_u};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -180,45 +181,49 @@ void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &
 }
 
 // Threads of the per-system CTA (multiple of 32, <= kSweepThreads).
-// Runs of consecutive k-vectors with the same (nx, ny) and consecutive nz
-// (k-vectors as n-triples n3[3k..3k+2], in enumeration order), each cut into
-// near-equal pieces of at most L entries, for the smallest L <= kQkRun whose
-// piece count fits `slots` (kQkRun if none does); longest first, and among
-// equal lengths by first nz, so that the lanes of a warp read the same e_z
-// entries of a particle (shared-memory broadcasts). Encoded as
-// {k0 | len << 24, nx & 0xFF | (ny & 0xFF) << 8 | (nz0 & 0xFF) << 16}.
-std::vector<int2> kseg_pieces(const std::vector<int> &n3, int K, int slots) {
-    std::vector<std::pair<int, int>> runs;   // (k0, length)
+// Items of the block kernel's in-kernel rebuild (eb_rebuild). The k-vectors
+// of one (nx, ny) form a contiguous run of nz = -m..m in enumeration order
+// (kVectorChange's loop order, with nz = 0 missing from (0, 0)). An item
+// takes up to kRbLen values n = n0, n0 + 1, ... of one such column and both
+// k-vectors (nx, ny, +n) and (nx, ny, -n) of each (one for n = 0): e_z(-n) is
+// the conjugate of e_z(n), so the four rounded products of a contribution
+// serve both. Encoded as {kp0 | len << 24, kn0 | n0 << 24,
+// nx & 0xFF | (ny & 0xFF) << 8, 0}: k(+n) = kp0 + (n - n0),
+// k(-n) = kn0 - (n - n0). Sorted by length (longest first), then n0, so
+// that warps run equal trip counts and read the same e_z entries. Returns
+// false if a column is not symmetric in nz.
+bool rb_item_list(const std::vector<int> &n3, int K, std::vector<int4> &items) {
+    items.clear();
     for (int k = 0; k < K;) {
-        int run = 1;
-        while (k + run < K && n3[3 * (k + run)] == n3[3 * k] && n3[3 * (k + run) + 1] == n3[3 * k + 1] &&
-               n3[3 * (k + run) + 2] == n3[3 * k + 2] + run)
-            run++;
-        runs.push_back({k, run});
-        k += run;
-    }
-    int L = 1;
-    for (; L < fg::kQkRun; L++) {
-        size_t pieces = 0;
-        for (auto &r : runs) pieces += (r.second + L - 1) / L;
-        if (pieces <= (size_t)slots) break;
-    }
-    std::vector<int2> seg;
-    for (auto &r : runs) {
-        const int pieces = (r.second + L - 1) / L;
-        for (int p = 0, k0 = r.first; p < pieces; p++) {
-            const int len = r.second / pieces + (p < r.second % pieces ? 1 : 0);
-            seg.push_back(make_int2(k0 | (len << 24), (n3[3 * k0] & 0xFF) | ((n3[3 * k0 + 1] & 0xFF) << 8) |
-                                                          ((n3[3 * k0 + 2] & 0xFF) << 16)));
-            k0 += len;
+        int e = k + 1;
+        while (e < K && n3[3 * e] == n3[3 * k] && n3[3 * e + 1] == n3[3 * k + 1]) e++;
+        // column [k, e): nz ascending
+        std::map<int, int> kz;
+        for (int q = k; q < e; q++) kz[n3[3 * q + 2]] = q;
+        const int m = kz.rbegin()->first;
+        for (auto &z : kz)
+            if (!kz.count(-z.first)) return false;
+        for (int n = 1; n <= m; n++)
+            if (!kz.count(n)) return false;
+        if (kz.size() != (size_t)(2 * m + (kz.count(0) ? 1 : 0))) return false;
+        const int nlo = kz.count(0) ? 0 : 1;
+        for (int n0 = nlo; n0 <= m; n0 += fg::kRbLen) {
+            const int len = std::min(fg::kRbLen, m - n0 + 1);
+            const int kp0 = kz[n0], kn0 = kz[-n0];
+            // k(+n) and k(-n) run contiguously in the column
+            for (int u = 0; u < len; u++)
+                if (kz[n0 + u] != kp0 + u || kz[-(n0 + u)] != kn0 - u) return false;
+            items.push_back(make_int4(kp0 | (len << 24), kn0 | (n0 << 24),
+                                      (n3[3 * k] & 0xFF) | ((n3[3 * k + 1] & 0xFF) << 8), 0));
         }
+        k = e;
     }
-    std::stable_sort(seg.begin(), seg.end(), [](const int2 &a, const int2 &b) {
+    std::stable_sort(items.begin(), items.end(), [](const int4 &a, const int4 &b) {
         const int la = a.x >> 24, lb = b.x >> 24;
         if (la != lb) return la > lb;
-        return (int)(int8_t)((a.y >> 16) & 0xFF) < (int)(int8_t)((b.y >> 16) & 0xFF);
+        return (a.y >> 24) < (b.y >> 24);
     });
-    return seg;
+    return true;
 }
 
 int sweep_threads(const fg_system *h) {
@@ -979,13 +984,12 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         h->nseg = (int)seg.size();
         ALLOC(h->kseg, seg.size() * sizeof(int2));
         cudaMemcpy(h->kseg, seg.data(), seg.size() * sizeof(int2), cudaMemcpyHostToDevice);
-        // the same runs for the block kernel's in-kernel rebuild: the
-        // shortest pieces (at most kQkRun) whose count still fits one CTA's
-        // kEbThreads threads, so that every warp of the CTA takes a share
-        std::vector<int2> blk = kseg_pieces(n3, h->K, fg::kEbThreads);
-        h->nseg_blk = (int)blk.size();
-        ALLOC(h->kseg_blk, blk.size() * sizeof(int2));
-        cudaMemcpy(h->kseg_blk, blk.data(), blk.size() * sizeof(int2), cudaMemcpyHostToDevice);
+        // the block kernel's in-kernel rebuild: pairs (+n, -n) of k-vectors
+        std::vector<int4> rb;
+        if (!rb_item_list(n3, h->K, rb)) return bail(fail(FG_ERR_INVALID, "k-vector set is not symmetric in nz"));
+        h->n_rb_items = (int)rb.size();
+        ALLOC(h->rb_items, rb.size() * sizeof(int4));
+        cudaMemcpy(h->rb_items, rb.data(), rb.size() * sizeof(int4), cudaMemcpyHostToDevice);
         cudaMemset(h->qfix, 0, h->K * sizeof(longlong2));
         cudaMemset(h->qnew, 0, h->K * sizeof(longlong2));
     }
@@ -1056,8 +1060,8 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     d.kpack = h->kpack;
     d.kseg = h->kseg;
     d.nseg = h->nseg;
-    d.kseg_blk = h->kseg_blk;
-    d.nseg_blk = h->nseg_blk;
+    d.rb_items = h->rb_items;
+    d.n_rb_items = h->n_rb_items;
     d.kcc = h->kc;
     if (set_qk_scale(d, qk_charge_bound(h, nullptr)))
         return bail(fail(FG_ERR_INVALID, "charges too large for the Q(k) fixed point"));
@@ -1475,6 +1479,7 @@ int64_t fg_device_bytes(fg_system *h) { return h ? (int64_t)h->device_bytes : 0;
 }  // extern "C"
 
 #include "fg_batch.cu"
+#include "fg_snapshot.cu"
 #include "fg_noalloc.cu"
 #include "fg_mol.cu"
 #include "fg_tune.cu"

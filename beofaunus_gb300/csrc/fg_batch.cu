@@ -677,6 +677,7 @@ struct fg_job {
     int state = 0;   // 0 queued, 1 running, 2 done, 3 failed
     fg_system *sys = nullptr;
     std::vector<double> result;   // final coordinates, copied off the device
+    std::vector<unsigned char> snapshot;   // resumed job: its system's state (fg_server_resume)
     size_t bytes = 0;
     double energy = 0;
 };
@@ -758,11 +759,15 @@ int server_admit(fg_server *s, fg_job *j) {
     int rc = fg_create(&j->P, (int)j->ids.size(), &h);
     if (rc) return rc;
     if (s->threads) fg_set_threads(h, s->threads);
-    rc = fg_set_state(h, j->xyz.data(), j->q.empty() ? nullptr : j->q.data(), j->ids.data());
+    rc = j->snapshot.empty()
+             ? fg_set_state(h, j->xyz.data(), j->q.empty() ? nullptr : j->q.data(), j->ids.data())
+             : fg_restore(h, j->snapshot.data(), (int64_t)j->snapshot.size());
     if (rc) {
         fg_destroy(h);
         return rc;
     }
+    j->snapshot.clear();
+    j->snapshot.shrink_to_fit();
     // a job's stream depends on its seed only (Philox key (seed, 0)), so its
     // result does not depend on which other jobs share the GPU
     h->desc.seed = j->seed;

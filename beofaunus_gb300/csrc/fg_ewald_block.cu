@@ -271,52 +271,107 @@ __device__ __forceinline__ df eb_pair(const Move &m, int4 p, int t, const short4
 
 // updateAllComplexNumbers (ewald.h:388-415) inside the sweep, every
 // update_frequency accepted trials (NonbondedEwald::update, ewald.h:633-640):
-// Q(k) from scratch as the exact sum of every particle's integer terms
-// (qk_term), compared with the running Q(k) in shared memory and adopted.
-// The two agree bit for bit unless the device misbehaved (the terms are a
-// deterministic function of the fixed-point positions), so the energy
+// Q(k) from scratch as the exact sum of every particle's integer
+// contributions, compared with the running Q(k) in shared memory and adopted.
+// The two agree bit for bit unless the device misbehaved (a contribution is a
+// deterministic function of the fixed-point position), so the energy
 // correction is zero; a difference is recorded (kErrQkMismatch where the
 // system verifies) and its energy is added to the running sums, as the
 // reference adds the drift it removes.
 //   work split: thread t owns items t, t + blockDim, ... of the system's
-//   rebuild list (runs of <= kQkRun k-vectors sharing (nx, ny), cut so that
-//   the CTA's threads hold them, longest first); particles pass through the
+//   rebuild list (rb_items: up to kRbLen values n of one (nx, ny) column, each
+//   giving the k-vectors +n and -n). Per particle it forms w once (qk_w) and
+//   per n the four rounded products a, r, b, c of w e_z(n) (qk_rint_bits),
+//   whose sums give both contributions: (a - r, b + c) to +n and, e_z(-n)
+//   being the conjugate and the rounding symmetric, (a + r, c - b) to -n;
+//   term by term these are qk_term_bits' values. Particles pass through the
 //   increment buffer in stages with their axis tables (8 threads build one
-//   particle's table); a stage's terms are summed exactly in 32 bits, then
-//   in int64 registers.
+//   particle's table: e_x(0..kcc), e_y(-kcc..kcc), e_z(0..kcc)); the four
+//   sums run in 32 bits over a stage (two particles per step), then in int64
+//   registers.
 // All threads call it (block-uniform). Returns the energy correction
 // (valid in thread 0) and whether any Q(k) differed.
+constexpr int kRbLen = 4;
+__host__ __device__ __forceinline__ int rb_tab_len(int kcc) { return 4 * kcc + 3; }
+// entry t of the rebuild's axis tables: the e_x and e_y parts of qk_tab_len's
+// layout, then e_z for n >= 0 only
+__device__ __forceinline__ float2 rb_tab_entry(int t, int kcc, const int h[3], const float2 *__restrict__ tab) {
+    return qk_tab_entry(t <= 3 * kcc + 1 ? t : t + kcc, kcc, h, tab);
+}
 template <int L>
-__device__ __forceinline__ void eb_rebuild_pass(const float2 *et, int T, const float *q2g, int nb, int ix, int iy,
-                                                int iz, unsigned ax[kQkRun], unsigned ay[kQkRun]) {
-    qk_pass<L>(et, T, q2g, nb, ix, iy, iz, ax, ay);
+__device__ __forceinline__ void rb_pass(const float2 *et, int T, const float *q2g, int nb, int ix, int iy, int iz,
+                                        unsigned sa[kRbLen], unsigned sr[kRbLen], unsigned sb[kRbLen],
+                                        unsigned sc[kRbLen]) {
+    int jj = 0;
+    for (; jj + 1 < nb; jj += 2) {
+        const float2 *e0 = et + jj * T, *e1 = e0 + T;
+        const float2 w0 = qk_w(q2g[jj], e0[ix], e0[iy]);
+        const float2 w1 = qk_w(q2g[jj + 1], e1[ix], e1[iy]);
+#pragma unroll
+        for (int u = 0; u < L; u++) {
+            const float2 z0 = e0[iz + u], z1 = e1[iz + u];
+            sa[u] += qk_rint_bits(w0.x, z0.x) + qk_rint_bits(w1.x, z1.x);
+            sr[u] += qk_rint_bits(w0.y, z0.y) + qk_rint_bits(w1.y, z1.y);
+            sb[u] += qk_rint_bits(w0.x, z0.y) + qk_rint_bits(w1.x, z1.y);
+            sc[u] += qk_rint_bits(w0.y, z0.x) + qk_rint_bits(w1.y, z1.x);
+        }
+    }
+    if (jj < nb) {
+        const float2 *e0 = et + jj * T;
+        const float2 w0 = qk_w(q2g[jj], e0[ix], e0[iy]);
+#pragma unroll
+        for (int u = 0; u < L; u++) {
+            const float2 z0 = e0[iz + u];
+            sa[u] += qk_rint_bits(w0.x, z0.x);
+            sr[u] += qk_rint_bits(w0.y, z0.y);
+            sb[u] += qk_rint_bits(w0.x, z0.y);
+            sc[u] += qk_rint_bits(w0.y, z0.x);
+        }
+    }
+}
+// Compare one rebuilt Q(k) with the running value and adopt it; energy of
+// the difference into e.
+__device__ __forceinline__ void rb_adopt(const EbSmem &s, int k, long long tx, long long ty, df &e, int &bad) {
+    const longlong2 qo = s.b.qfix[k];
+    if (qo.x != tx || qo.y != ty) {
+        bad = 1;
+        const longlong2 qn = make_longlong2(tx, ty);
+        const float2 fo = q_to_float(qo), fn = q_to_float(qn);
+        const float dre = fix28_to_float(qn.x - qo.x), dim = fix28_to_float(qn.y - qo.y);
+        e = df_add_f(e, s.b.kvec[k].x * fmaf(dre, fo.x + fn.x, dim * (fo.y + fn.y)));
+        s.b.qfix[k] = qn;
+        s.b.kvec[k].y = fn.x;
+        s.b.kvec[k].z = fn.y;
+    }
 }
 __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &corr) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
-    const int T = qk_tab_len(d.kcc);
-    // the increment buffer holds the stage's axis tables plus kQkRun entries
-    // of headroom for the unused tail reads of qk_pass
-    const int stage = min(64, (kEbKc * kEbTrials - kQkRun) / T);
+    const int kcc = d.kcc, T = rb_tab_len(kcc);
+    // the increment buffer holds the stage's axis tables plus kRbLen entries
+    // of headroom for the unused tail reads of rb_pass
+    const int stage = min(64, (kEbKc * kEbTrials - kRbLen) / T);
     float2 *et = s.delta;
     float *q2g = s.G;   // [stage], free between blocks
     const int shift = d.qk_shift;
     df e = {0.0f, 0.0f};
     int bad = 0;
-    for (int r0 = 0; r0 < d.nseg_blk; r0 += nt) {   // uniform over the block
+    for (int r0 = 0; r0 < d.n_rb_items; r0 += nt) {   // uniform over the block
         const int r = r0 + tid;
-        int k0 = 0, len = 0, ix = 0, iy = 0, iz = 0;
-        if (r < d.nseg_blk) {
-            const int2 sg = d.kseg_blk[r];
-            k0 = sg.x & 0xFFFFFF;
-            len = sg.x >> 24;
-            ix = (int)(int8_t)(sg.y & 0xFF);
-            iy = 2 * d.kcc + 1 + (int)(int8_t)((sg.y >> 8) & 0xFF);
-            iz = 4 * d.kcc + 2 + (int)(int8_t)((sg.y >> 16) & 0xFF);
+        int kp0 = 0, kn0 = 0, len = 0, n0 = 0, ix = 0, iy = 0, iz = 0;
+        if (r < d.n_rb_items) {
+            const int4 it = d.rb_items[r];
+            kp0 = it.x & 0xFFFFFF;
+            len = it.x >> 24;
+            kn0 = it.y & 0xFFFFFF;
+            n0 = it.y >> 24;
+            ix = (int)(int8_t)(it.z & 0xFF);
+            iy = 2 * kcc + 1 + (int)(int8_t)((it.z >> 8) & 0xFF);
+            iz = 3 * kcc + 2 + n0;
         }
         const int wl = __reduce_max_sync(0xffffffffu, len);   // warp-uniform (items sorted by length)
-        long long tx[kQkRun], ty[kQkRun];
+        long long tpx[kRbLen], tpy[kRbLen], tnx[kRbLen], tny[kRbLen];   // +n and -n totals
 #pragma unroll
-        for (int u = 0; u < kQkRun; u++) tx[u] = ty[u] = 0;
+        for (int u = 0; u < kRbLen; u++) tpx[u] = tpy[u] = tnx[u] = tny[u] = 0;
         for (int j0 = 0; j0 < d.N; j0 += stage) {
             const int nb = min(stage, d.N - j0);
             __syncthreads();   // the previous stage's tables are consumed
@@ -324,47 +379,36 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
                 const int4 p = d.pos4[j0 + jj];
                 if ((tid & 7) == 0) q2g[jj] = qk_charge(__int_as_float(p.w), d.eff[d.ptype[j0 + jj]], d);
                 const int h[3] = {p.x, p.y, p.z};
-                for (int t = tid & 7; t < T; t += 8) et[jj * T + t] = qk_tab_entry(t, d.kcc, h, s.b.sc_tab);
+                for (int t = tid & 7; t < T; t += 8) et[jj * T + t] = rb_tab_entry(t, kcc, h, s.b.sc_tab);
             }
             __syncthreads();
             if (wl > 0) {
-                unsigned ax[kQkRun], ay[kQkRun];
+                unsigned sa[kRbLen], sr[kRbLen], sb[kRbLen], sc[kRbLen];
 #pragma unroll
-                for (int u = 0; u < kQkRun; u++) ax[u] = ay[u] = 0u;
+                for (int u = 0; u < kRbLen; u++) sa[u] = sr[u] = sb[u] = sc[u] = 0u;
                 switch (wl) {
-                    case 1: eb_rebuild_pass<1>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
-                    case 2: eb_rebuild_pass<2>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
-                    case 3: eb_rebuild_pass<3>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
-                    case 4: eb_rebuild_pass<4>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
-                    case 5: eb_rebuild_pass<5>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
-                    case 6: eb_rebuild_pass<6>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
-                    case 7: eb_rebuild_pass<7>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
-                    default: eb_rebuild_pass<8>(et, T, q2g, nb, ix, iy, iz, ax, ay); break;
+                    case 1: rb_pass<1>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
+                    case 2: rb_pass<2>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
+                    case 3: rb_pass<3>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
+                    default: rb_pass<4>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
                 }
-                const unsigned off = (unsigned)nb * kQkMagicBits;
+                // each of the four sums carries nb kQkMagicBits
+                const unsigned off2 = 2u * (unsigned)nb * kQkMagicBits;
 #pragma unroll
-                for (int u = 0; u < kQkRun; u++) {
-                    tx[u] += qk_widen((int)(ax[u] - off), shift);
-                    ty[u] += qk_widen((int)(ay[u] - off), shift);
+                for (int u = 0; u < kRbLen; u++) {
+                    tpx[u] += qk_widen((int)(sa[u] - sr[u]), shift);
+                    tpy[u] += qk_widen((int)(sb[u] + sc[u] - off2), shift);
+                    tnx[u] += qk_widen((int)(sa[u] + sr[u] - off2), shift);
+                    tny[u] += qk_widen((int)(sc[u] - sb[u]), shift);
                 }
             }
         }
         // compare with the running sums and adopt
 #pragma unroll
-        for (int u = 0; u < kQkRun; u++) {
+        for (int u = 0; u < kRbLen; u++) {
             if (u >= len) continue;
-            const int k = k0 + u;
-            const longlong2 qo = s.b.qfix[k];
-            if (qo.x != tx[u] || qo.y != ty[u]) {
-                bad = 1;
-                const longlong2 qn = make_longlong2(tx[u], ty[u]);
-                const float2 fo = q_to_float(qo), fn = q_to_float(qn);
-                const float dre = fix28_to_float(qn.x - qo.x), dim = fix28_to_float(qn.y - qo.y);
-                e = df_add_f(e, s.b.kvec[k].x * fmaf(dre, fo.x + fn.x, dim * (fo.y + fn.y)));
-                s.b.qfix[k] = qn;
-                s.b.kvec[k].y = fn.x;
-                s.b.kvec[k].z = fn.y;
-            }
+            rb_adopt(s, kp0 + u, tpx[u], tpy[u], e, bad);
+            if (n0 + u > 0) rb_adopt(s, kn0 - u, tnx[u], tny[u], e, bad);
         }
     }
     // energy correction: warp sums, then warp 0 over the warps (fixed order)

@@ -18,20 +18,25 @@
 // (potentials.h:2036-2040), NonbondedEwald::updateChange/update/external
 // (ewald.h:613-729), getSurfaceEnergy (ewald.h:277-291).
 //
-// Q(k) bookkeeping. Each particle contributes the integer
-// c_k(j) = round(w_j(nx, ny) e_z(nz)), w_j = (s q_j eff_j e_x(nx)) e_y(ny),
-// s = 2^g c (c = 4095/4096), with e_a(n) = e^{i n 2 pi x_a / L_a} from
-// sincos_turns on the exact integer phase n h_a (its conjugate for n < 0) and
-// every product rounded in a fixed order (qk_w, qk_term): a deterministic
-// function of the particle's fixed-point position. g is chosen so that every
-// |w e_z| < 2^22, where adding 1.5 2^23 rounds to the nearest integer on the
-// FMA pipe (qk_term). Q(k) is kept as the exact int64 sum of these
-// contributions in units of 2^-28 / c (each shifted by 28 - g), and an
-// accepted move adds c_k(new) - c_k(old). So Q(k) never drifts: a rebuild from scratch
-// reproduces it bit for bit (qk_rebuild_* checks that), where the
-// reference's FP64 running sum needs the rebuild to undo accumulated error.
-// The factorised form lets the rebuild share one w per particle across the
-// run of k-vectors with the same (nx, ny).
+// Q(k) bookkeeping. Each particle contributes the complex integer
+// c_k(j) = (rint(w.x e.x) - rint(w.y e.y), rint(w.x e.y) + rint(w.y e.x)),
+// the product w_j(nx, ny) e_z(nz) with each of its four real products rounded
+// to the nearest integer, where w_j = (s q_j eff_j e_x(nx)) e_y(ny),
+// s = 2^g c (c = 4095/4096), and e_a(n) = e^{i n 2 pi x_a / L_a} comes from
+// sincos_turns on the exact integer phase n h_a (its conjugate for n < 0),
+// every product rounded in a fixed order (qk_w, qk_term_bits): a
+// deterministic function of the particle's fixed-point position. g is chosen
+// so that every |w e_z| < 2^22, where one FMA with 1.5 2^23 as addend rounds
+// a product to the nearest integer on the FMA pipe (qk_rint_bits). Q(k) is
+// kept as the exact int64 sum of these contributions in units of 2^-28 / c
+// (each shifted by 28 - g), and an accepted move adds c_k(new) - c_k(old).
+// So Q(k) never drifts: a rebuild from scratch reproduces it bit for bit (the
+// rebuilds check that), where the reference's FP64 running sum needs the
+// rebuild to undo accumulated error. The factorised form lets a rebuild share
+// one w per particle across the k-vectors with the same (nx, ny); since the
+// rounding is symmetric, the four rounded products for e_z(n) also give the
+// contribution to -n (e_z(-n) = conj e_z(n)), so a rebuild forms them once
+// for both.
 // The energy change itself uses the increment in the form
 // q e^{ik.r_old}(e^{ik.d} - 1), whose FP32 error is relative to |d|.
 #include <cstdint>
@@ -573,17 +578,21 @@ __device__ __forceinline__ float2 qk_w(float q2g, float2 ex, float2 ey) {
     return make_float2(__fmaf_rn(ax, ey.x, -__fmul_rn(ay, ey.y)), __fmaf_rn(ax, ey.y, __fmul_rn(ay, ey.x)));
 }
 // For |x| < 2^22, x + 1.5 2^23 lies in [2^23, 2^24), where floats are the
-// integers: the sum is 1.5 2^23 + round(x) (to nearest, ties to even, as
-// __float2int_rn rounds), and its bit pattern minus that of 1.5 2^23 is
-// round(x). An FP32 addition instead of a conversion on the XU pipe.
+// integers: fma(a, b, 1.5 2^23) is 1.5 2^23 + rint(a b) (to nearest, ties to
+// even, as __float2int_rn rounds), and its bit pattern is that of 1.5 2^23
+// plus rint(a b). One FMA instead of a multiply and a conversion on the XU
+// pipe. Ties to even is symmetric, rint(-x) = -rint(x), which makes the
+// contribution of e_z(-n) = conj e_z(n) the same four rounded products.
 constexpr float kQkMagic = 12582912.0f;
 constexpr uint32_t kQkMagicBits = 0x4B400000u;
-// bit patterns of w e_z + 1.5 2^23 (real, imaginary): sums of n of them
-// minus n kQkMagicBits are sums of terms, exactly in 32-bit wrap-around
+__device__ __forceinline__ uint32_t qk_rint_bits(float a, float b) { return __float_as_uint(__fmaf_rn(a, b, kQkMagic)); }
+// (real, imaginary) contribution of w e_z, each plus kQkMagicBits: sums of n
+// of them minus n kQkMagicBits are sums of contributions, exactly in 32-bit
+// wrap-around
 __device__ __forceinline__ uint2 qk_term_bits(float2 w, float2 ez) {
-    const float re = __fmaf_rn(w.x, ez.x, -__fmul_rn(w.y, ez.y));
-    const float im = __fmaf_rn(w.x, ez.y, __fmul_rn(w.y, ez.x));
-    return make_uint2(__float_as_uint(__fadd_rn(re, kQkMagic)), __float_as_uint(__fadd_rn(im, kQkMagic)));
+    const uint32_t a = qk_rint_bits(w.x, ez.x), r = qk_rint_bits(w.y, ez.y);
+    const uint32_t b = qk_rint_bits(w.x, ez.y), c = qk_rint_bits(w.y, ez.x);
+    return make_uint2(a - r + kQkMagicBits, b + c - kQkMagicBits);
 }
 __device__ __forceinline__ int2 qk_term(float2 w, float2 ez) {
     const uint2 b = qk_term_bits(w, ez);

@@ -10,7 +10,7 @@
 //          int32 particle ids, plus counts; p_cell/p_slot locate each particle
 //   Ewald  kvec float4[K] {kx, ky, kz, A_k * 2*pi*lB/V}, kpack uint32[K] (n
 //          vector as signed bytes), qfix longlong2[K]: Q(k) as exact sums of
-//          per-particle integer contributions (see qk_term in fg_kernels.cu)
+//          per-particle integer contributions (see qk_term_bits in fg_kernels.cu)
 #pragma once
 #include <cstdint>
 
@@ -121,16 +121,17 @@ struct alignas(16) SysDesc {
     uint32_t seed;           // Philox key word (seed)
     int64_t stream_first;    // counter of trial 0 in the current stream
     longlong2 *qnew;         // rebuild target (K)
-    // Q(k) contributions: one particle adds round(2^g c q eff e^{ik.r}) (an
-    // integer of magnitude < 2^22, c = 4095/4096) shifted left by
-    // qk_shift = 28 - g; Q(k) is in units of 2^-28 / c
+    // Q(k) contributions: one particle adds 2^g c q eff e^{ik.r} with each
+    // of its four real products rounded to an integer (each of magnitude
+    // < 2^22, c = 4095/4096), shifted left by qk_shift = 28 - g; Q(k) is in
+    // units of 2^-28 / c
     int32_t kcc;             // |n_a| <= kcc for every k-vector
     int32_t qk_shift;
     float qk_scale;          // 2^g c
     int32_t nseg;            // runs of k-vectors that share (nx, ny), for the rebuild
     const int2 *kseg;        // {k0 | len << 24, nx & 0xFF | (ny & 0xFF) << 8 | (nz0 & 0xFF) << 16}
-    int32_t nseg_blk;        // the same runs cut for one CTA of the block kernel (in-kernel rebuild)
-    const int2 *kseg_blk;
+    int32_t n_rb_items;      // in-kernel rebuild of the block kernel: k-vector pairs (+n, -n) per item
+    const int4 *rb_items;    // {kp0 | len << 24, kn0 | n0 << 24, nx & 0xFF | (ny & 0xFF) << 8, 0}
     float reach2;            // no pair term acts beyond r^2 = reach2 (cutoff, WCA range, core)
 };
 

@@ -93,6 +93,13 @@ def lib(build_if_missing=True):
             "fg_server_release": ([vp, i64], ctypes.c_int),
             "fg_server_cancel": ([vp, i64], ctypes.c_int),
             "fg_server_bytes_in_use": ([vp], ctypes.c_int64),
+            "fg_snapshot_bytes": ([vp], ctypes.c_int64),
+            "fg_snapshot": ([vp, dp, i64], ctypes.c_int),
+            "fg_restore": ([vp, dp, i64], ctypes.c_int),
+            "fg_snapshot_info": ([dp, i64, dp, dp, dp, dp, dp, dp, dp], ctypes.c_int),
+            "fg_server_snapshot_bytes": ([vp, i64], ctypes.c_int64),
+            "fg_server_snapshot": ([vp, i64, dp, i64], ctypes.c_int),
+            "fg_server_resume": ([vp, dp, i64, dp], ctypes.c_int),
             "fg_mol_create": ([vp, i32, i32, ctypes.POINTER(vp)], ctypes.c_int),
             "fg_mol_destroy": ([vp], ctypes.c_int),
             "fg_mol_set_state": ([vp, dp, dp, dp, dp, dp], ctypes.c_int),
@@ -247,6 +254,37 @@ class System:
         if threads:
             _check(lib().fg_set_threads(self.h, threads))
         self.set_state(xyz, charge, type_ids)
+
+    @classmethod
+    def from_snapshot(cls, blob, threads=0):
+        """A new system holding the state of a snapshot (fg_snapshot_info,
+        fg_create, fg_restore)."""
+        buf = np.frombuffer(blob, dtype=np.uint8)
+        params, n = FgParams(), np.zeros(1, np.int32)
+        _check(lib().fg_snapshot_info(_p(buf), len(buf), ctypes.byref(params), _p(n), None, None, None, None, None))
+        ids, q = np.zeros(int(n[0]), np.int32), np.zeros(int(n[0]))
+        _check(lib().fg_snapshot_info(_p(buf), len(buf), None, None, None, None, None, _p(ids), _p(q)))
+        self = cls.__new__(cls)
+        self.params = params
+        self.n = int(n[0])
+        h = ctypes.c_void_p()
+        _check(lib().fg_create(ctypes.byref(params), self.n, ctypes.byref(h)))
+        self.h = h
+        if threads:
+            _check(lib().fg_set_threads(self.h, threads))
+        self._ids, self._q = ids, q
+        self.restore(blob)
+        return self
+
+    def snapshot(self):
+        """Device -> host snapshot of the whole state (bytes)."""
+        buf = np.zeros(int(lib().fg_snapshot_bytes(self.h)), np.uint8)
+        _check(lib().fg_snapshot(self.h, _p(buf), len(buf)))
+        return buf.tobytes()
+
+    def restore(self, blob):
+        buf = np.frombuffer(blob, dtype=np.uint8)
+        _check(lib().fg_restore(self.h, _p(buf), len(buf)))
 
     def close(self):
         if getattr(self, "h", None):
@@ -580,6 +618,23 @@ class Server:
     @property
     def bytes_in_use(self):
         return int(lib().fg_server_bytes_in_use(self.h))
+
+    def snapshot(self, job_id):
+        """A running job's snapshot (bytes), taken between steps."""
+        buf = np.zeros(int(lib().fg_server_snapshot_bytes(self.h, job_id)), np.uint8)
+        _check(lib().fg_server_snapshot(self.h, job_id, _p(buf), len(buf)))
+        return buf.tobytes()
+
+    def resume(self, blob):
+        """Queue a job that continues from a job snapshot; returns its id."""
+        buf = np.frombuffer(blob, dtype=np.uint8)
+        jid = np.zeros(1, np.int64)
+        _check(lib().fg_server_resume(self.h, _p(buf), len(buf), _p(jid)))
+        hdr = 48   # the job fields ahead of the system snapshot (JobSnapHeader)
+        n = np.zeros(1, np.int32)
+        _check(lib().fg_snapshot_info(_p(buf[hdr:]), len(buf) - hdr, None, _p(n), None, None, None, None, None))
+        self._n[int(jid[0])] = int(n[0])
+        return int(jid[0])
 
 
 def mol_run_many(systems):

@@ -226,6 +226,42 @@ int fg_server_release(fg_server *s, int64_t job_id);
 int fg_server_cancel(fg_server *s, int64_t job_id);
 int64_t fg_server_bytes_in_use(fg_server *s);
 
+/* ---- snapshots: stop a run and resume it bit for bit ------------------------
+ * Replaces: Space::save/load (space.h:376-377), which keep the particles as
+ * text, and the random state the reference writes to move_out.json
+ * (slump.h:111-124, move.h:7900) but never reads back. A snapshot holds
+ * everything that decides how a system continues: the fixed-point positions,
+ * charges and types, the cell lists in slot order, the exact integer Q(k),
+ * the running energies and surface dipole, the accept count toward the next
+ * update_frequency rebuild, and the key and counters of the system's Philox
+ * stream. It is taken between runs (no trial pending) and holds no staged
+ * trial stream. A system restored from it (fg_create with the same
+ * parameters and particle count, then fg_restore) and given the same trial
+ * streams runs exactly as the original does from that point: same positions,
+ * Q(k), decisions, dU and running energy, to the bit. fg_restore refuses
+ * another system's snapshot (particle count, parameters or cell grid) and a
+ * damaged one (checksum) before it changes anything; it then rebuilds Q(k)
+ * from the restored positions and refuses the snapshot unless the two agree
+ * bit for bit, after which the system needs fg_set_state or a good snapshot
+ * again. Binary, in the host's byte order. */
+int64_t fg_snapshot_bytes(fg_system *h);
+int fg_snapshot(fg_system *h, void *buf, int64_t size);
+int fg_restore(fg_system *h, const void *buf, int64_t size);
+/* Parameters, particle count, Philox key and next counter, type ids[N] and
+ * charges[N] of a snapshot (any output may be NULL): what is needed to create
+ * the system that fg_restore fills. */
+int fg_snapshot_info(const void *buf, int64_t size, fg_params *params, int32_t *n_particles, uint32_t *seed,
+                     uint32_t *stream_id, int64_t *next_counter, int32_t *type_ids, double *charges);
+/* A running job's snapshot (between fg_server_step calls): its system plus
+ * its seed, trial count, trials done, accepted count and energy. A job
+ * resumed from it (fg_server_resume, on this server or another, after the
+ * first was cancelled or its process ended) draws the remaining trials of
+ * the same Philox stream and finishes with the result the uninterrupted job
+ * would have had. */
+int64_t fg_server_snapshot_bytes(fg_server *s, int64_t job_id);
+int fg_server_snapshot(fg_server *s, int64_t job_id, void *buf, int64_t size);
+int fg_server_resume(fg_server *s, const void *buf, int64_t size, int64_t *job_id);
+
 /* ---- pair energy without device allocation ---------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc:
  * a plugin inside a host application that owns the whole GPU memory pool and
