@@ -819,9 +819,6 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     if (P.model == FG_MODEL_EWALD_WCA) {
         if (!(P.ewald_alpha > 0) || !(P.ewald_cutoff > 0) || !(P.ewald_debye_length > 0))
             return fail(FG_ERR_INVALID, "Ewald needs alpha, cutoff and debye_length > 0");
-        for (int i = 0; i < P.n_types; i++)
-            if (P.type_charge[i] == 0.0)
-                return fail(FG_ERR_INVALID, "Ewald effective charges need non-zero type charges (ewald.h:539)");
         if (std::ceil(P.ewald_cutoff_k) > 127) return fail(FG_ERR_INVALID, "cutoffK too large");
     } else if (!(P.dh_debye_length > 0)) {
         return fail(FG_ERR_INVALID, "dh_debye_length must be > 0");
@@ -871,7 +868,9 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     std::vector<double> eff(nt, 1.0);
     for (int i = 0; i < nt; i++) {
         double ri = 0.5 * P.type_sigma[i], qis = P.type_charge[i];
-        if (P.model == FG_MODEL_EWALD_WCA) {
+        // a neutral type's ratio is 0/0 in the reference (ewald.h:539); its
+        // particles carry no charge (fg_set_state), so any value serves: 1
+        if (P.model == FG_MODEL_EWALD_WCA && P.type_charge[i] != 0.0) {
             if (std::fabs(kappa * ri) > 1e-9) qis *= std::sinh(ri * kappa) / ri / kappa;
             eff[i] = qis / P.type_charge[i];
         }
@@ -1113,6 +1112,9 @@ int fg_set_state(fg_system *h, const double *xyz, const double *charge, const in
         const int t = type_ids[i];
         if (t < 0 || t >= P.n_types) return fail(FG_ERR_INVALID, "type id %d out of range", t);
         const double q = charge ? charge[i] : P.type_charge[t];
+        if (P.model == FG_MODEL_EWALD_WCA && P.type_charge[t] == 0.0 && q != 0.0)
+            return fail(FG_ERR_INVALID, "particle %d carries charge but its atom type is neutral: its Ewald effective "
+                                        "charge is 0/0 (ewald.h:539)", i);
         h->charges[i] = q;
         int32_t hw[3];
         for (int a = 0; a < 3; a++) {

@@ -157,9 +157,11 @@ class NonbondedGPU : public Energybase<Tspace> {
         return corr;
     }
 
+    // Energybase::systemEnergy (energy.h:169-180), every term in FP64 (the
+    // reference's drift bookkeeping compares it with the running sum)
     double systemEnergy(const Tpvec &) override {
         double c[5];
-        fg_check(fg_total_energy(h, c));
+        fg_check(fg_total_energy_fp64(h, c));
         return c[4];
     }
 

@@ -166,19 +166,9 @@ static Tmjson faunus_input(const Tmjson &in) {
     return j;
 }
 
-template<class Tenergy>
-static void run_mc(const Tmjson &in, Out &out, bool bench) {
-    Tmjson j = faunus_input(in);
-    const bool timed = bench && in.count("seconds");
-    if (timed) j["moves"]["atomtranslate"]["salt"]["peratom"] = false;
-    Tspace spc(j);
-    if (timed) {   // the rest of the atomic group in one Space::insert (space.h:950-1000)
-        const int N = in["positions"].size();
-        Tspace::ParticleVector more(N - 1);
-        for (auto &x : more) x = atom[atom["T0"].id];
-        spc.insert(spc.molList()["salt"].id, more);
-    }
-    // per-type parameters straight into the atom map (eps in kT, no kJ/mol round trip)
+// Per-type parameters straight into the atom map (eps in kT, no kJ/mol
+// round trip), then every particle's type and position.
+static void fill_space(const Tmjson &in, Tspace &spc) {
     int t = 0;
     for (auto &ty : in["types"]) {
         auto &a = atom[atom["T" + std::to_string(t++)].id];
@@ -198,6 +188,22 @@ static void run_mc(const Tmjson &in, Out &out, bool bench) {
         spc.p[i].z() = in["positions"][i][2];
     }
     spc.trial = spc.p;
+}
+
+template<class Tenergy>
+static void run_mc(const Tmjson &in, Out &out, bool bench) {
+    Tmjson j = faunus_input(in);
+    const bool timed = bench && in.count("seconds");
+    if (timed) j["moves"]["atomtranslate"]["salt"]["peratom"] = false;
+    Tspace spc(j);
+    if (timed) {   // the rest of the atomic group in one Space::insert (space.h:950-1000)
+        const int N = in["positions"].size();
+        Tspace::ParticleVector more(N - 1);
+        for (auto &x : more) x = atom[atom["T0"].id];
+        spc.insert(spc.molList()["salt"].id, more);
+    }
+    fill_space(in, spc);
+    const int N = spc.p.size();
     Tenergy pot(j);
     LoggedTranslation<Tspace> mv(pot, spc, j["moves"]["atomtranslate"]); // calls pot.setSpace(spc)
     mv.log = !bench;
@@ -368,6 +374,7 @@ static void run_isobaric(const Tmjson &in, Out &out) {
     out.set("final_positions", fin);
 }
 
+#ifndef FG_HARNESS_NO_MAIN
 int main(int argc, char **argv) {
     if (argc != 3) { std::cerr << "usage: ref_harness in.json out.json\n"; return 2; }
     std::ifstream f(argv[1]);
@@ -393,3 +400,4 @@ int main(int argc, char **argv) {
     out.write(argv[2]);
     return 0;
 }
+#endif
