@@ -1204,8 +1204,10 @@ def _serving_job(args):
 def run_serving(args, rank, world):
     """Poisson job stream through the continuous-batching server. Each job is
     a DH+LJ salt with N log-uniform in [256, 16384], its own temperature in
-    [0.8, 2.0] and seed, running ``--job-sweeps`` sweeps (the named 2000 are
-    scaled down so the run ends within minutes; the scale is in the line).
+    [0.8, 2.0] and seed, running ``--job-sweeps`` sweeps. The named 2000
+    sweeps per job cost about 2000 x 200 x E[N^2] = 1.3e13 pair terms for the
+    200-job mix (hours of GPU time), so the default is 20 and a run with
+    fewer than 2000 carries the job length in config.workload.
     Capacity is measured first with every job submitted at once; the timed
     run then feeds the same job mix at 80 % of that capacity."""
     import numpy as np
@@ -1274,7 +1276,9 @@ def run_serving(args, rank, world):
     clk = clocks.stop()
     lat = np.array([finish[j] - arrivals[j] for j in range(n_jobs)])
     value = total_trials / span
-    cfg = {"workload": WORKLOAD_NAMES["serving"], "jobs": n_jobs, "n_range": [256, 16384],
+    # the named job length is 2000 sweeps; a run with fewer says so in its name
+    wname = WORKLOAD_NAMES["serving"] + ("" if sweeps == 2000 else "_%dsweeps_per_job" % sweeps)
+    cfg = {"workload": wname, "jobs": n_jobs, "n_range": [256, 16384],
            "temperature_range": [0.8, 2.0], "sweeps_per_job": sweeps, "sweeps_per_job_named": 2000,
            "arrival": "Poisson at 0.8 x measured capacity", "capacity_jobs_per_s": capacity,
            "capacity_definition": "completions per s between 10% and 70% of jobs done, all submitted at t=0",
