@@ -136,7 +136,7 @@ def test_server_job_resumed_from_a_snapshot_finishes_as_if_never_stopped():
     srv1.cancel(jid)
     srv1.close()
 
-    srv2 = Server(1 << 30, threads=256, round_pairs=1 << 17)   # another round size
+    srv2 = Server(1 << 30, threads=256, round_pairs=1 << 18)
     po, xo, qo, io = workloads.dh_lj_salt(700, seed=10)
     other = srv2.submit(po, xo, qo, io, 10, 5000)
     jid2 = srv2.resume(blob)
