@@ -181,18 +181,8 @@ void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &
 }
 
 // Threads of the per-system CTA (multiple of 32, <= kSweepThreads).
-// Items of the block kernel's in-kernel rebuild (eb_rebuild). The k-vectors
-// of one (nx, ny) form a contiguous run of nz = -m..m in enumeration order
-// (kVectorChange's loop order, with nz = 0 missing from (0, 0)). An item
-// takes up to kRbLen values n = n0, n0 + 1, ... of one such column and both
-// k-vectors (nx, ny, +n) and (nx, ny, -n) of each (one for n = 0): e_z(-n) is
-// the conjugate of e_z(n), so the four rounded products of a contribution
-// serve both. Encoded as {kp0 | len << 24, kn0 | n0 << 24,
-// nx & 0xFF | (ny & 0xFF) << 8, 0}: k(+n) = kp0 + (n - n0),
-// k(-n) = kn0 - (n - n0). Sorted by length (longest first), then n0, so
-// that warps run equal trip counts and read the same e_z entries. Returns
-// false if a column is not symmetric in nz.
-bool rb_item_list(const std::vector<int> &n3, int K, std::vector<int4> &items) {
+// rb_item_list for items of at most L values of n.
+bool rb_item_list_len(const std::vector<int> &n3, int K, int L, std::vector<int4> &items) {
     items.clear();
     for (int k = 0; k < K;) {
         int e = k + 1;
@@ -207,8 +197,8 @@ bool rb_item_list(const std::vector<int> &n3, int K, std::vector<int4> &items) {
             if (!kz.count(n)) return false;
         if (kz.size() != (size_t)(2 * m + (kz.count(0) ? 1 : 0))) return false;
         const int nlo = kz.count(0) ? 0 : 1;
-        for (int n0 = nlo; n0 <= m; n0 += fg::kRbLen) {
-            const int len = std::min(fg::kRbLen, m - n0 + 1);
+        for (int n0 = nlo; n0 <= m; n0 += L) {
+            const int len = std::min(L, m - n0 + 1);
             const int kp0 = kz[n0], kn0 = kz[-n0];
             // k(+n) and k(-n) run contiguously in the column
             for (int u = 0; u < len; u++)
@@ -226,6 +216,25 @@ bool rb_item_list(const std::vector<int> &n3, int K, std::vector<int4> &items) {
     return true;
 }
 
+// Items of the block kernel's in-kernel rebuild (eb_rebuild). The k-vectors
+// of one (nx, ny) form a contiguous run of nz = -m..m in enumeration order
+// (kVectorChange's loop order, with nz = 0 missing from (0, 0)). An item
+// takes up to kRbLen values n = n0, n0 + 1, ... of one such column and both
+// k-vectors (nx, ny, +n) and (nx, ny, -n) of each (one for n = 0): e_z(-n) is
+// the conjugate of e_z(n), so the four rounded products of a contribution
+// serve both. The item length is the smallest (at most kRbLen) whose item
+// count fits `slots` threads, so that the most warps take a share. Encoded as
+// {kp0 | len << 24, kn0 | n0 << 24, nx & 0xFF | (ny & 0xFF) << 8, 0}:
+// k(+n) = kp0 + (n - n0), k(-n) = kn0 - (n - n0). Sorted by length (longest
+// first), then n0, so that warps run equal trip counts and read the same e_z
+// entries. Returns false if a column is not symmetric in nz.
+bool rb_item_list(const std::vector<int> &n3, int K, int slots, std::vector<int4> &items) {
+    for (int L = 1; L <= fg::kRbLen; L++) {
+        if (!rb_item_list_len(n3, K, L, items)) return false;
+        if ((int)items.size() <= slots) break;
+    }
+    return true;
+}
 int sweep_threads(const fg_system *h) {
     int t = h->threads;
     if (t <= 0) {
@@ -985,7 +994,7 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         cudaMemcpy(h->kseg, seg.data(), seg.size() * sizeof(int2), cudaMemcpyHostToDevice);
         // the block kernel's in-kernel rebuild: pairs (+n, -n) of k-vectors
         std::vector<int4> rb;
-        if (!rb_item_list(n3, h->K, rb)) return bail(fail(FG_ERR_INVALID, "k-vector set is not symmetric in nz"));
+        if (!rb_item_list(n3, h->K, fg::kEbThreads - 32, rb)) return bail(fail(FG_ERR_INVALID, "k-vector set is not symmetric in nz"));
         h->n_rb_items = (int)rb.size();
         ALLOC(h->rb_items, rb.size() * sizeof(int4));
         cudaMemcpy(h->rb_items, rb.data(), rb.size() * sizeof(int4), cudaMemcpyHostToDevice);

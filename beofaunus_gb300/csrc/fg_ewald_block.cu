@@ -143,11 +143,13 @@ __device__ __forceinline__ void eb_qbar(int nthreads) {
 }
 
 // Real-space base of one trial by one warp. Candidates (cell stencil, or all
-// particles) are screened by distance first: only those within reach2 of the
-// old or the new position enter a 32-entry warp queue in shared memory (qp,
-// qm), which is evaluated with all lanes busy when the next batch would
-// overflow it. Skipped candidates contribute exactly zero (every pair term is
-// zero beyond reach2), so the sum is that of the full loop, in another order.
+// particles) are screened by distance first: only those that may lie within
+// reach2 of the old or the new position (all particles: either distance; cell
+// stencil: the distance to the step's midpoint against reach + |d|/2) enter a
+// 32-entry warp queue in shared memory (qp, qm), which is evaluated with all
+// lanes busy when the next batch would overflow it. Skipped candidates
+// contribute exactly zero (every pair term is zero beyond reach2), so the sum
+// is that of the full loop, in another order.
 template <bool CELLS>
 __device__ __forceinline__ void eb_flush(int qn, const int4 *qp, const int2 *qm, const Move &m, const SysDesc &d,
                                          float &accf, df &accd) {
@@ -196,6 +198,13 @@ __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, c
         eb_flush<CELLS>(qn, qp, qm, m, d, accf, accd);
         return;
     }
+    // The stencil: the cells around the old cell, widened by one along each
+    // axis where the particle changed cells (at most 4 x 4 x 4). Lane c (and
+    // c + 32) takes stencil cell c: it drops the cell when no point of the
+    // cell box lies within reach of the old or the new position, so that the
+    // cell's particles cannot contribute, and the warp's prefix sum over the
+    // remaining cells' counts flattens their slots into one candidate list,
+    // which the warp then screens 32 candidates at a time with all lanes busy.
     int co[3], cn[3], lo[3], len[3];
     co[0] = m.co % d.nc[0]; co[1] = (m.co / d.nc[0]) % d.nc[1]; co[2] = m.co / (d.nc[0] * d.nc[1]);
     cn[0] = m.cn % d.nc[0]; cn[1] = (m.cn / d.nc[0]) % d.nc[1]; cn[2] = m.cn / (d.nc[0] * d.nc[1]);
@@ -208,54 +217,88 @@ __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, c
         lo[a] = co[a] + min(delta, 0) - 1;
         len[a] = 3 + (delta != 0 ? 1 : 0);
     }
-    const int ncell = len[0] * len[1] * len[2];
-    // the stencil position (ix, iy, iz) advances incrementally (no integer
-    // division per cell); wrapped cell coordinate per axis
-    auto wrap = [&](int c, int a) {
-        c += (c < 0) ? d.nc[a] : 0;
-        return c - ((c >= d.nc[a]) ? d.nc[a] : 0);
-    };
-    int ix = 0, iy = 0, iz = 0;
-    // two stencil cells per pass: their loads are independent, so a warp
-    // keeps two cell records in flight
-    for (int k0 = 0; k0 < ncell; k0 += 2) {
-        int cid[2], cnt[2];
+    const int ncell = len[0] * len[1] * len[2];   // <= 64
+    // reach of a cell box: squared distance (Angstrom^2) from the old and the
+    // new position, on unwrapped coordinates u = h + 2^31 (the new one as the
+    // old plus the minimum-image step, so that both lie on the stencil's side
+    // of the box edge); a small margin covers the float rounding of the box
+    // bounds (units of 2^32 / L carry ~2^8 units of rounding here)
+    const float reach2m = d.reach2 * 1.0001f + 1e-3f;
+    float uo[3], un[3];
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            cid[u] = 0;
-            cnt[u] = 0;
-            if (k0 + u < ncell) {
-                cid[u] = (wrap(lo[2] + iz, 2) * d.nc[1] + wrap(lo[1] + iy, 1)) * d.nc[0] + wrap(lo[0] + ix, 0);
-                cnt[u] = s.ccount[cid[u]];
-                ix++;
-                if (ix == len[0]) {
-                    ix = 0;
-                    iy++;
-                    if (iy == len[1]) {
-                        iy = 0;
-                        iz++;
-                    }
-                }
+    for (int a = 0; a < 3; a++) {
+        uo[a] = (float)((uint32_t)m.ho[a] + 0x80000000u);
+        un[a] = uo[a] + (float)(int)(m.hn[a] - m.ho[a]);
+    }
+    int cidv[2], cntv[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int c = lane + 32 * h;
+        cidv[h] = 0;
+        cntv[h] = 0;
+        if (c < ncell) {
+            const int i0 = c % len[0], i1 = (c / len[0]) % len[1], i2 = c / (len[0] * len[1]);
+            const int cu[3] = {lo[0] + i0, lo[1] + i1, lo[2] + i2};
+            float d2o = 0.0f, d2n = 0.0f;
+            int w[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const float W = 4294967296.0f / (float)d.nc[a];
+                const float A = (float)cu[a] * W, B = A + W;
+                const float xo = fmaxf(fmaxf(A - uo[a], uo[a] - B), 0.0f) * d.s32[a];
+                const float xn = fmaxf(fmaxf(A - un[a], un[a] - B), 0.0f) * d.s32[a];
+                d2o = fmaf(xo, xo, d2o);
+                d2n = fmaf(xn, xn, d2n);
+                w[a] = cu[a] + (cu[a] < 0 ? d.nc[a] : 0) - (cu[a] >= d.nc[a] ? d.nc[a] : 0);
             }
+            cidv[h] = (w[2] * d.nc[1] + w[1]) * d.nc[0] + w[0];
+            if (fminf(d2o, d2n) <= reach2m) cntv[h] = s.ccount[cidv[h]];
         }
-        const int cmax = max(cnt[0], cnt[1]);
-        for (int b = 0; b < cmax; b += 32) {   // warp-uniform trip count
-            const int slot = b + lane;
-            int pid[2];
-            int4 pos[2];
+    }
+    // inclusive prefix sums of the two halves; start = exclusive
+    int inc0 = cntv[0], inc1 = cntv[1];
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
-                const int idx = cid[u] * d.cap + slot;
-                pid[u] = slot < cnt[u] ? d.cell_pid[idx] : -1;
-                pos[u] = slot < cnt[u] ? d.cell_pos[idx] : make_int4(0, 0, 0, 0);
-            }
-#pragma unroll
-            for (int u = 0; u < 2; u++) {
-                const bool v = pid[u] >= 0 && (pid[u] & 0xFFFFFF) != m.i;
-                eb_push<CELLS>(v && eb_in_reach(pos[u], m, d), pos[u], cid[u] * d.cap + slot, pid[u] >> 24, qn, qp,
-                               qm, m, d, accf, accd);
-            }
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v0 = __shfl_up_sync(0xffffffffu, inc0, o), v1 = __shfl_up_sync(0xffffffffu, inc1, o);
+        if (lane >= o) {
+            inc0 += v0;
+            inc1 += v1;
         }
+    }
+    const int tot0 = __shfl_sync(0xffffffffu, inc0, 31);
+    const int st0 = inc0 - cntv[0], st1 = tot0 + inc1 - cntv[1];
+    const int total = tot0 + __shfl_sync(0xffffffffu, inc1, 31);
+    // screening against the midpoint hm of the step: a partner within reach
+    // of the old or the new position lies within reach + |d|/2 of hm
+    const int hm[3] = {m.ho[0] + ((int)(m.hn[0] - m.ho[0]) >> 1), m.ho[1] + ((int)(m.hn[1] - m.ho[1]) >> 1),
+                       m.ho[2] + ((int)(m.hn[2] - m.ho[2]) >> 1)};
+    const float hd = 0.5f * sqrtf(fmaf(m.dxf[0], m.dxf[0], fmaf(m.dxf[1], m.dxf[1], m.dxf[2] * m.dxf[2])));
+    const float rm = sqrtf(reach2m) + hd + 1e-3f, rm2 = rm * rm;
+    int c = 0;   // warp-uniform: the cell holding candidate b
+    for (int b = 0; b < total; b += 32) {
+        // the first stencil cell whose slots reach past b
+        while (true) {
+            const int e = (c < 32 ? __shfl_sync(0xffffffffu, st0, c) + __shfl_sync(0xffffffffu, cntv[0], c)
+                                  : __shfl_sync(0xffffffffu, st1, c - 32) + __shfl_sync(0xffffffffu, cntv[1], c - 32));
+            if (e > b) break;
+            c++;
+        }
+        const int g = b + lane;
+        int mc = c;
+        for (int cc = c + 1; cc < ncell; cc++) {   // warp-uniform
+            const int sc0 = cc < 32 ? __shfl_sync(0xffffffffu, st0, cc) : __shfl_sync(0xffffffffu, st1, cc - 32);
+            if (sc0 > b + 31) break;
+            if (sc0 <= g) mc = cc;
+        }
+        const int sA = __shfl_sync(0xffffffffu, st0, mc & 31), sB = __shfl_sync(0xffffffffu, st1, mc & 31);
+        const int cA = __shfl_sync(0xffffffffu, cidv[0], mc & 31), cB = __shfl_sync(0xffffffffu, cidv[1], mc & 31);
+        const int cid = mc < 32 ? cA : cB, slot = g - (mc < 32 ? sA : sB);
+        const bool in = g < total;
+        const int idx = cid * d.cap + slot;
+        const int pid = in ? d.cell_pid[idx] : -1;
+        const int4 pos = in ? d.cell_pos[idx] : make_int4(0, 0, 0, 0);
+        const bool v = pid >= 0 && (pid & 0xFFFFFF) != m.i && dist2(pos, hm[0], hm[1], hm[2], d) <= rm2;
+        eb_push<CELLS>(v, pos, idx, pid >> 24, qn, qp, qm, m, d, accf, accd);
     }
     eb_flush<CELLS>(qn, qp, qm, m, d, accf, accd);
 }
@@ -285,10 +328,11 @@ __device__ __forceinline__ df eb_pair(const Move &m, int4 p, int t, const short4
 //   whose sums give both contributions: (a - r, b + c) to +n and, e_z(-n)
 //   being the conjugate and the rounding symmetric, (a + r, c - b) to -n;
 //   term by term these are qk_term_bits' values. Particles pass through the
-//   increment buffer in stages with their axis tables (8 threads build one
-//   particle's table: e_x(0..kcc), e_y(-kcc..kcc), e_z(0..kcc)); the four
-//   sums run in 32 bits over a stage (two particles per step), then in int64
-//   registers.
+//   increment buffer in stages of 64 with their axis tables (8 threads build
+//   one particle's table: e_x(0..kcc), e_y(-kcc..kcc), e_z(0..kcc)), stored
+//   for pairs of particles so that one 16-byte load serves two; the four
+//   sums run in 32 bits over a stage, then in int64 registers. The same items
+//   carry the per-block Q(k) update (eb_commit_qk).
 // All threads call it (block-uniform). Returns the energy correction
 // (valid in thread 0) and whether any Q(k) differed.
 constexpr int kRbLen = 4;
@@ -298,34 +342,28 @@ __host__ __device__ __forceinline__ int rb_tab_len(int kcc) { return 4 * kcc + 3
 __device__ __forceinline__ float2 rb_tab_entry(int t, int kcc, const int h[3], const float2 *__restrict__ tab) {
     return qk_tab_entry(t <= 3 * kcc + 1 ? t : t + kcc, kcc, h, tab);
 }
+// One stage of the rebuild for this thread's item: np particle pairs, whose
+// axis tables sit as float4 {e_2p(t), e_2p+1(t)} at tab[p * T + t] (one
+// 16-byte load gives an entry of both particles) and whose charges are
+// q2[p]. The four sums carry 2 np kQkMagicBits (a padding particle has
+// charge 0 and zero tables and adds exactly that).
 template <int L>
-__device__ __forceinline__ void rb_pass(const float2 *et, int T, const float *q2g, int nb, int ix, int iy, int iz,
+__device__ __forceinline__ void rb_pass(const float4 *tab, int T, const float2 *q2, int np, int ix, int iy, int iz,
                                         unsigned sa[kRbLen], unsigned sr[kRbLen], unsigned sb[kRbLen],
                                         unsigned sc[kRbLen]) {
-    int jj = 0;
-    for (; jj + 1 < nb; jj += 2) {
-        const float2 *e0 = et + jj * T, *e1 = e0 + T;
-        const float2 w0 = qk_w(q2g[jj], e0[ix], e0[iy]);
-        const float2 w1 = qk_w(q2g[jj + 1], e1[ix], e1[iy]);
+    for (int p = 0; p < np; p++) {
+        const float4 *e = tab + p * T;
+        const float2 q = q2[p];
+        const float4 ex = e[ix], ey = e[iy];
+        const float2 w0 = qk_w(q.x, make_float2(ex.x, ex.y), make_float2(ey.x, ey.y));
+        const float2 w1 = qk_w(q.y, make_float2(ex.z, ex.w), make_float2(ey.z, ey.w));
 #pragma unroll
         for (int u = 0; u < L; u++) {
-            const float2 z0 = e0[iz + u], z1 = e1[iz + u];
-            sa[u] += qk_rint_bits(w0.x, z0.x) + qk_rint_bits(w1.x, z1.x);
-            sr[u] += qk_rint_bits(w0.y, z0.y) + qk_rint_bits(w1.y, z1.y);
-            sb[u] += qk_rint_bits(w0.x, z0.y) + qk_rint_bits(w1.x, z1.y);
-            sc[u] += qk_rint_bits(w0.y, z0.x) + qk_rint_bits(w1.y, z1.x);
-        }
-    }
-    if (jj < nb) {
-        const float2 *e0 = et + jj * T;
-        const float2 w0 = qk_w(q2g[jj], e0[ix], e0[iy]);
-#pragma unroll
-        for (int u = 0; u < L; u++) {
-            const float2 z0 = e0[iz + u];
-            sa[u] += qk_rint_bits(w0.x, z0.x);
-            sr[u] += qk_rint_bits(w0.y, z0.y);
-            sb[u] += qk_rint_bits(w0.x, z0.y);
-            sc[u] += qk_rint_bits(w0.y, z0.x);
+            const float4 z = e[iz + u];
+            sa[u] += qk_rint_bits(w0.x, z.x) + qk_rint_bits(w1.x, z.z);
+            sr[u] += qk_rint_bits(w0.y, z.y) + qk_rint_bits(w1.y, z.w);
+            sb[u] += qk_rint_bits(w0.x, z.y) + qk_rint_bits(w1.x, z.w);
+            sc[u] += qk_rint_bits(w0.y, z.x) + qk_rint_bits(w1.y, z.z);
         }
     }
 }
@@ -347,11 +385,11 @@ __device__ __forceinline__ void rb_adopt(const EbSmem &s, int k, long long tx, l
 __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &corr) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
     const int kcc = d.kcc, T = rb_tab_len(kcc);
-    // the increment buffer holds the stage's axis tables plus kRbLen entries
-    // of headroom for the unused tail reads of rb_pass
-    const int stage = min(64, (kEbKc * kEbTrials - kRbLen) / T);
-    float2 *et = s.delta;
-    float *q2g = s.G;   // [stage], free between blocks
+    // the increment buffer holds the stage's tables (pairs of particles) plus
+    // kRbLen entries of headroom for the unused tail reads of rb_pass
+    float4 *tab = reinterpret_cast<float4 *>(s.delta);
+    const int npair = min(kEbThreads / 16, (kEbKc * kEbTrials / 2 - kRbLen) / T), stage = 2 * npair;
+    float2 *q2 = reinterpret_cast<float2 *>(s.G);   // [npair], free between blocks
     const int shift = d.qk_shift;
     df e = {0.0f, 0.0f};
     int bad = 0;
@@ -372,14 +410,32 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
         long long tpx[kRbLen], tpy[kRbLen], tnx[kRbLen], tny[kRbLen];   // +n and -n totals
 #pragma unroll
         for (int u = 0; u < kRbLen; u++) tpx[u] = tpy[u] = tnx[u] = tny[u] = 0;
+        // 8 threads per particle build its table (stage <= nt / 8); each
+        // thread's particle record of the next stage is loaded during this
+        // stage's sums
+        const int jj = tid >> 3;
+        int4 pn = make_int4(0, 0, 0, 0);
+        int tn = 0;
+        if (jj < min(stage, d.N)) {
+            pn = d.pos4[jj];
+            tn = d.ptype[jj];
+        }
         for (int j0 = 0; j0 < d.N; j0 += stage) {
-            const int nb = min(stage, d.N - j0);
+            const int nb = min(stage, d.N - j0), np = (nb + 1) >> 1;
             __syncthreads();   // the previous stage's tables are consumed
-            for (int jj = tid >> 3; jj < nb; jj += nt >> 3) {
-                const int4 p = d.pos4[j0 + jj];
-                if ((tid & 7) == 0) q2g[jj] = qk_charge(__int_as_float(p.w), d.eff[d.ptype[j0 + jj]], d);
-                const int h[3] = {p.x, p.y, p.z};
-                for (int t = tid & 7; t < T; t += 8) et[jj * T + t] = rb_tab_entry(t, kcc, h, s.b.sc_tab);
+            float2 *tf = reinterpret_cast<float2 *>(tab);
+            if (jj < 2 * np) {
+                const bool live = jj < nb;
+                const float qv = live ? qk_charge(__int_as_float(pn.w), d.eff[tn], d) : 0.0f;
+                const int hp[3] = {pn.x, pn.y, pn.z};
+                if ((tid & 7) == 0) reinterpret_cast<float *>(q2)[jj] = qv;
+                for (int t = tid & 7; t < T; t += 8)
+                    tf[((jj >> 1) * T + t) * 2 + (jj & 1)] =
+                        live ? rb_tab_entry(t, kcc, hp, s.b.sc_tab) : make_float2(0.0f, 0.0f);
+            }
+            if (jj < stage && j0 + stage + jj < d.N) {
+                pn = d.pos4[j0 + stage + jj];
+                tn = d.ptype[j0 + stage + jj];
             }
             __syncthreads();
             if (wl > 0) {
@@ -387,13 +443,13 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
 #pragma unroll
                 for (int u = 0; u < kRbLen; u++) sa[u] = sr[u] = sb[u] = sc[u] = 0u;
                 switch (wl) {
-                    case 1: rb_pass<1>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
-                    case 2: rb_pass<2>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
-                    case 3: rb_pass<3>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
-                    default: rb_pass<4>(et, T, q2g, nb, ix, iy, iz, sa, sr, sb, sc); break;
+                    case 1: rb_pass<1>(tab, T, q2, np, ix, iy, iz, sa, sr, sb, sc); break;
+                    case 2: rb_pass<2>(tab, T, q2, np, ix, iy, iz, sa, sr, sb, sc); break;
+                    case 3: rb_pass<3>(tab, T, q2, np, ix, iy, iz, sa, sr, sb, sc); break;
+                    default: rb_pass<4>(tab, T, q2, np, ix, iy, iz, sa, sr, sb, sc); break;
                 }
-                // each of the four sums carries nb kQkMagicBits
-                const unsigned off2 = 2u * (unsigned)nb * kQkMagicBits;
+                // each of the four sums carries 2 np kQkMagicBits
+                const unsigned off2 = 4u * (unsigned)np * kQkMagicBits;
 #pragma unroll
                 for (int u = 0; u < kRbLen; u++) {
                     tpx[u] += qk_widen((int)(sa[u] - sr[u]), shift);
@@ -423,6 +479,91 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
     }
     __syncthreads();   // red is free again
     return anybad != 0;
+}
+
+// Q(k) after a block: every accepted trial a adds c_k(new_a) - c_k(old_a)
+// (ewald.h:665-705). Threads qt = 0..nq-1 (warps 1.. of the CTA, which
+// synchronise among themselves on named barrier 1) own the rebuild's items
+// (rb_items): per accepted trial they form w once for the new and the old
+// position and, per n of the item, the four rounded products of each (the
+// same integers the rebuild sums), accumulate the differences in 32 bits over
+// the block's trials (at most 32 x 2^23) and add them to the exact int64 Q(k)
+// of the item's (+n, -n) k-vectors at the end; integer sums, so the order of
+// the trials does not matter. The axis tables of the accepted trials'
+// new and old positions sit in the increment buffer as float4
+// {new.re, new.im, old.re, old.im}, trial-major (tab[g * T + t]).
+__device__ __noinline__ void eb_commit_qk(const SysDesc &d, const EbSmem &s, uint32_t live, int qt, int nq) {
+    int *alist = reinterpret_cast<int *>(s.corr);   // free after the resolution
+    float *qg = s.G;                                // [32], free after the resolution
+    if (qt < kEbTrials && ((live >> qt) & 1u)) {
+        const int g = __popc(live & ((1u << qt) - 1u));
+        alist[g] = qt;
+        const Move &A = s.mv[qt];
+        qg[g] = qk_charge(A.q, d.eff[A.ti], d);
+    }
+    const int na = __popc(live);
+    const int kcc = d.kcc, T = rb_tab_len(kcc);
+    float4 *tab = reinterpret_cast<float4 *>(s.delta);
+    const int gmax = min(kEbTrials, (kEbKc * kEbTrials / 2 - kRbLen) / T);
+    const int shift = d.qk_shift;
+    for (int g0 = 0; g0 < na; g0 += gmax) {
+        const int ng = min(gmax, na - g0);
+        eb_qbar(nq);   // list written; the previous group's tables consumed
+        for (int e = qt; e < ng * T; e += nq) {
+            const int g = e / T, t = e - g * T;
+            const Move &A = s.mv[alist[g0 + g]];
+            const float2 en = rb_tab_entry(t, kcc, A.hn, s.b.sc_tab), eo = rb_tab_entry(t, kcc, A.ho, s.b.sc_tab);
+            tab[e] = make_float4(en.x, en.y, eo.x, eo.y);
+        }
+        eb_qbar(nq);
+        for (int r = qt; r < d.n_rb_items; r += nq) {
+            const int4 it = d.rb_items[r];
+            const int kp0 = it.x & 0xFFFFFF, len = it.x >> 24, kn0 = it.y & 0xFFFFFF, n0 = it.y >> 24;
+            const int ix = (int)(int8_t)(it.z & 0xFF), iy = 2 * kcc + 1 + (int)(int8_t)((it.z >> 8) & 0xFF);
+            const int iz = 3 * kcc + 2 + n0;
+            unsigned da[kRbLen], dr[kRbLen], db[kRbLen], dc[kRbLen];
+#pragma unroll
+            for (int u = 0; u < kRbLen; u++) da[u] = dr[u] = db[u] = dc[u] = 0u;
+            for (int g = 0; g < ng; g++) {
+                const float4 *e = tab + g * T;
+                const float q2g = qg[g0 + g];
+                const float4 ex = e[ix], ey = e[iy];
+                const float2 wn = qk_w(q2g, make_float2(ex.x, ex.y), make_float2(ey.x, ey.y));
+                const float2 wo = qk_w(q2g, make_float2(ex.z, ex.w), make_float2(ey.z, ey.w));
+#pragma unroll
+                for (int u = 0; u < kRbLen; u++) {
+                    if (u < len) {
+                        const float4 z = e[iz + u];
+                        da[u] += qk_rint_bits(wn.x, z.x) - qk_rint_bits(wo.x, z.z);
+                        dr[u] += qk_rint_bits(wn.y, z.y) - qk_rint_bits(wo.y, z.w);
+                        db[u] += qk_rint_bits(wn.x, z.y) - qk_rint_bits(wo.x, z.w);
+                        dc[u] += qk_rint_bits(wn.y, z.x) - qk_rint_bits(wo.y, z.z);
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRbLen; u++) {
+                if (u >= len) continue;
+                // +n: (a - r, b + c); -n: (a + r, c - b)
+                longlong2 q = s.b.qfix[kp0 + u];
+                q.x += qk_widen((int)(da[u] - dr[u]), shift);
+                q.y += qk_widen((int)(db[u] + dc[u]), shift);
+                s.b.qfix[kp0 + u] = q;
+                float2 qf = q_to_float(q);
+                s.b.kvec[kp0 + u].y = qf.x;
+                s.b.kvec[kp0 + u].z = qf.y;
+                if (n0 + u > 0) {
+                    q = s.b.qfix[kn0 - u];
+                    q.x += qk_widen((int)(da[u] + dr[u]), shift);
+                    q.y += qk_widen((int)(dc[u] - db[u]), shift);
+                    s.b.qfix[kn0 - u] = q;
+                    qf = q_to_float(q);
+                    s.b.kvec[kn0 - u].y = qf.x;
+                    s.b.kvec[kn0 - u].z = qf.y;
+                }
+            }
+        }
+    }
 }
 
 // Surface dipole change of a trial (Angstrom e), as surface_delta computes it.
@@ -670,7 +811,10 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                 const int mi = x < 4 ? 0 : 1, nj = x < 4 ? x : x - 2;
                 const int row = 16 * mi + (ln >> 2) + ((j & 2) ? 8 : 0);
                 const int col = 8 * nj + 2 * (ln & 3) + (j & 1);
-                s.G[row * kEbTrials + col] = 2.0f * v;
+                // one correction per pair (a, m): real space + surface + reciprocal
+                const float2 c = s.corr[row * kEbTrials + col];
+                const df cs = df_add_f(df{c.x, c.y}, 2.0f * v);
+                s.corr[row * kEbTrials + col] = make_float2(cs.hi, cs.lo);
             }
         }
         __syncthreads();
@@ -689,31 +833,26 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             uint32_t accm = 0;
             int done = kb;
             for (int a = 0; a < kb; a++) {
-                const bool coll = __shfl_sync(0xffffffffu, (colm & accm) != 0u ? 1 : 0, a) != 0;
-                if (coll) {
+                // lane a decides: its S already holds the corrections of every
+                // accepted trial before it in the block. Movebase::metropolis
+                // (move.h:567-573): reject iff dU > kT (-ln u); a NaN dU
+                // compares false there: accepted
+                const float2 c = s.corr[a * kEbTrials + lane];   // loaded ahead of the decision
+                int f = 0;
+                if (lane == a) {
+                    const bool nan = !(S.hi == S.hi);
+                    f = ((colm & accm) != 0u ? 1 : 0) | (nan || !df_gt(S, df{th.x, th.y}) ? 2 : 0) | (nan ? 4 : 0);
+                }
+                f = __shfl_sync(0xffffffffu, f, a);
+                if (f & 1) {   // its particle was moved by an accepted trial of this block
                     done = a;
                     break;
                 }
-                const df du = {__shfl_sync(0xffffffffu, S.hi, a), __shfl_sync(0xffffffffu, S.lo, a)};
-                const df t = {__shfl_sync(0xffffffffu, th.x, a), __shfl_sync(0xffffffffu, th.y, a)};
-                const bool nan = !(du.hi == du.hi);
-                // Movebase::metropolis (move.h:567-573): reject iff dU > kT (-ln u);
-                // a NaN dU compares false there: accepted
-                const bool acc = nan || !df_gt(du, t);
-                if (nan) err |= kErrNonFinite;
-                if (lane == 0 && d.log_trials) {
-                    d.trial_du[cur + a] = make_float2(du.hi, du.lo);
-                    d.trial_acc[cur + a] = acc ? 1 : 0;
-                }
-                if (acc) {
+                if (f & 4) err |= kErrNonFinite;
+                if (f & 2) {
                     accm |= 1u << a;
-                    U = df_add(U, du);
-                    Ut = df_add(Ut, du);
                     nacc++;
-                    if (lane > a && lane < kb) {
-                        const float2 c = s.corr[a * kEbTrials + lane];
-                        S = df_add(df_add(S, df{c.x, c.y}), df{s.G[a * kEbTrials + lane], 0.0f});
-                    }
+                    if (lane > a && lane < kb) S = df_add_quick(S, df{c.x, c.y});
                     // NonbondedEwald::update (ewald.h:633): a rebuild after
                     // update_frequency accepted trials ends the block here
                     if (++cnt_acc > uf - 1) {
@@ -726,6 +865,16 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                     }
                 }
             }
+            // lane m's S is trial m's dU as decided: log it, and add the
+            // accepted ones to the running sums (a fixed-order warp sum)
+            const bool take = lane < done && ((accm >> lane) & 1u);
+            if (d.log_trials && lane < done) {
+                d.trial_du[cur + lane] = make_float2(S.hi, S.lo);
+                d.trial_acc[cur + lane] = take ? 1 : 0;
+            }
+            const df sum = warp_sum_df(take ? S : df{0.0f, 0.0f});
+            U = df_add(U, sum);
+            Ut = df_add(Ut, sum);
             if (lane == 0) {
                 s.info[0] = done;
                 s.info[1] = (int)accm;
@@ -756,41 +905,10 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
 #pragma unroll
             for (int x = 0; x < 3; x++) s.Mdf[x] = make_float2(M[x].hi, M[x].lo);
         } else if (tid >= 32 && live) {
-            // Q(k) += sum over accepted trials of c_k(new) - c_k(old), with the
-            // axis tables of up to gmax trials at a time in the delta buffer
-            const int qt = tid - 32, nq = blockDim.x - 32;
-            int *alist = reinterpret_cast<int *>(s.corr);   // free after the resolution
-            if (qt < kEbTrials && ((live >> qt) & 1u)) alist[__popc(live & ((1u << qt) - 1u))] = qt;
-            const int na = __popc(live);
-            const int T = qk_tab_len(d.kcc), T2 = 2 * T;
-            const int gmax = min(kEbTrials, (kEbKc * kEbTrials) / T2);
-            for (int g0 = 0; g0 < na; g0 += gmax) {
-                const int ng = min(gmax, na - g0);
-                eb_qbar(nq);   // list written; the previous group's tables consumed
-                for (int t = qt; t < ng * T2; t += nq) {
-                    const int g = t / T2, e = t - g * T2;
-                    const Move &A = s.mv[alist[g0 + g]];
-                    s.delta[t] = e < T ? qk_tab_entry(e, d.kcc, A.hn, s.b.sc_tab)
-                                       : qk_tab_entry(e - T, d.kcc, A.ho, s.b.sc_tab);
-                }
-                eb_qbar(nq);
-                for (int k = qt; k < K; k += nq) {
-                    int nx, ny, nz;
-                    unpack_n(s.b.kpack[k], nx, ny, nz);
-                    longlong2 q = s.b.qfix[k];
-                    for (int g = 0; g < ng; g++) {
-                        const Move &A = s.mv[alist[g0 + g]];
-                        const float2 *tn = s.delta + g * T2;
-                        const int2 c = qk_delta(nx, ny, nz, qk_charge(A.q, d.eff[A.ti], d), tn, tn + T, d.kcc);
-                        q.x += qk_widen(c.x, d.qk_shift);
-                        q.y += qk_widen(c.y, d.qk_shift);
-                    }
-                    s.b.qfix[k] = q;
-                    const float2 qf = q_to_float(q);
-                    s.b.kvec[k].y = qf.x;
-                    s.b.kvec[k].z = qf.y;
-                }
-            }
+            // Q(k) += sum over accepted trials of c_k(new) - c_k(old), over
+            // the rebuild's items (eb_commit_qk): each thread owns items of
+            // (+n, -n) k-vector pairs and adds every accepted trial's change
+            eb_commit_qk(d, s, live, tid - 32, blockDim.x - 32);
         }
         cur += done;
         __syncthreads();
