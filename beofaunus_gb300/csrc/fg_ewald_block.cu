@@ -367,21 +367,35 @@ __device__ __forceinline__ void rb_pass(const float4 *tab, int T, const float2 *
         }
     }
 }
-// Compare one rebuilt Q(k) with the running value and adopt it; energy of
-// the difference into e.
-__device__ __forceinline__ void rb_adopt(const EbSmem &s, int k, long long tx, long long ty, df &e, int &bad) {
+// Compare one rebuilt Q(k) (its total in the k-vector table's slot, see
+// eb_rebuild) with the running value and adopt it; energy of the difference
+// into e; the slot gets back its {A', Q as float, sqrt A'} from the k-vector
+// array in global memory.
+__device__ __forceinline__ void rb_adopt(const SysDesc &d, const EbSmem &s, int k, df &e, int &bad) {
+    const longlong2 qn = reinterpret_cast<const longlong2 *>(s.b.kvec)[k];
     const longlong2 qo = s.b.qfix[k];
-    if (qo.x != tx || qo.y != ty) {
+    const float A = d.kvec[k].w;
+    const float2 fn = q_to_float(qn);
+    if (qo.x != qn.x || qo.y != qn.y) {
         bad = 1;
-        const longlong2 qn = make_longlong2(tx, ty);
-        const float2 fo = q_to_float(qo), fn = q_to_float(qn);
+        const float2 fo = q_to_float(qo);
         const float dre = fix28_to_float(qn.x - qo.x), dim = fix28_to_float(qn.y - qo.y);
-        e = df_add_f(e, s.b.kvec[k].x * fmaf(dre, fo.x + fn.x, dim * (fo.y + fn.y)));
+        e = df_add_f(e, A * fmaf(dre, fo.x + fn.x, dim * (fo.y + fn.y)));
         s.b.qfix[k] = qn;
-        s.b.kvec[k].y = fn.x;
-        s.b.kvec[k].z = fn.y;
     }
+    s.b.kvec[k] = make_float4(A, fn.x, fn.y, sqrtf(A));
 }
+__device__ __forceinline__ void rb_add(const EbSmem &s, int k, long long x, long long y) {
+    longlong2 *t = reinterpret_cast<longlong2 *>(s.b.kvec) + k;
+    longlong2 v = *t;
+    v.x += x;
+    v.y += y;
+    *t = v;
+}
+// The int64 totals of the rebuilt Q(k) live in the k-vector table's own
+// 16-byte slots (kvec[k], free while the rebuild runs: nothing else reads it
+// until rb_adopt restores it), each owned by the thread of its item, so the
+// thread's registers hold only the 32-bit sums of a stage.
 __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &corr) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
     const int kcc = d.kcc, T = rb_tab_len(kcc);
@@ -393,6 +407,7 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
     const int shift = d.qk_shift;
     df e = {0.0f, 0.0f};
     int bad = 0;
+    __syncthreads();   // every thread is past its last read of kvec
     for (int r0 = 0; r0 < d.n_rb_items; r0 += nt) {   // uniform over the block
         const int r = r0 + tid;
         int kp0 = 0, kn0 = 0, len = 0, n0 = 0, ix = 0, iy = 0, iz = 0;
@@ -407,9 +422,10 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
             iz = 3 * kcc + 2 + n0;
         }
         const int wl = __reduce_max_sync(0xffffffffu, len);   // warp-uniform (items sorted by length)
-        long long tpx[kRbLen], tpy[kRbLen], tnx[kRbLen], tny[kRbLen];   // +n and -n totals
-#pragma unroll
-        for (int u = 0; u < kRbLen; u++) tpx[u] = tpy[u] = tnx[u] = tny[u] = 0;
+        for (int u = 0; u < len; u++) {
+            reinterpret_cast<longlong2 *>(s.b.kvec)[kp0 + u] = make_longlong2(0, 0);
+            reinterpret_cast<longlong2 *>(s.b.kvec)[kn0 - u] = make_longlong2(0, 0);
+        }
         // 8 threads per particle build its table (stage <= nt / 8); each
         // thread's particle record of the next stage is loaded during this
         // stage's sums
@@ -452,19 +468,19 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
                 const unsigned off2 = 4u * (unsigned)np * kQkMagicBits;
 #pragma unroll
                 for (int u = 0; u < kRbLen; u++) {
-                    tpx[u] += qk_widen((int)(sa[u] - sr[u]), shift);
-                    tpy[u] += qk_widen((int)(sb[u] + sc[u] - off2), shift);
-                    tnx[u] += qk_widen((int)(sa[u] + sr[u] - off2), shift);
-                    tny[u] += qk_widen((int)(sc[u] - sb[u]), shift);
+                    if (u >= len) continue;
+                    rb_add(s, kp0 + u, qk_widen((int)(sa[u] - sr[u]), shift),
+                           qk_widen((int)(sb[u] + sc[u] - off2), shift));
+                    if (n0 + u > 0)
+                        rb_add(s, kn0 - u, qk_widen((int)(sa[u] + sr[u] - off2), shift),
+                               qk_widen((int)(sc[u] - sb[u]), shift));
                 }
             }
         }
         // compare with the running sums and adopt
-#pragma unroll
-        for (int u = 0; u < kRbLen; u++) {
-            if (u >= len) continue;
-            rb_adopt(s, kp0 + u, tpx[u], tpy[u], e, bad);
-            if (n0 + u > 0) rb_adopt(s, kn0 - u, tnx[u], tny[u], e, bad);
+        for (int u = 0; u < len; u++) {
+            rb_adopt(d, s, kp0 + u, e, bad);
+            if (n0 + u > 0) rb_adopt(d, s, kn0 - u, e, bad);
         }
     }
     // energy correction: warp sums, then warp 0 over the warps (fixed order)
