@@ -582,6 +582,53 @@ __device__ __noinline__ void eb_commit_qk(const SysDesc &d, const EbSmem &s, uin
     }
 }
 
+// Accepted trial: master and pair coordinates, and (in_cell: the particle
+// stays in its cell) its record in the cell's slot array. Independent for
+// distinct particles.
+__device__ __forceinline__ void eb_commit_position(const Move &m, const SysDesc &d, const Smem &s, bool in_cell) {
+    const int4 rec = make_int4(m.hn[0], m.hn[1], m.hn[2], __float_as_int(m.q));
+    const short4 ext = make_short4((short)m.en[0], (short)m.en[1], (short)m.en[2], 0);
+    d.pos64[3 * m.i + 0] = m.xn[0];
+    d.pos64[3 * m.i + 1] = m.xn[1];
+    d.pos64[3 * m.i + 2] = m.xn[2];
+    d.pos4[m.i] = rec;
+    d.pos_ext[m.i] = ext;
+    if (d.use_cells && in_cell) {
+        const int slot = (int)(s.pcs[m.i] & 0xFFFu);
+        d.cell_pos[m.co * d.cap + slot] = rec;
+        d.cell_ext[m.co * d.cap + slot] = ext;
+    }
+}
+// A particle that changed cells: out of the old cell (the cell's last slot
+// fills the hole) and into the next free slot of the new one, as
+// commit_position does. One thread, accepted trials in order.
+__device__ __forceinline__ void eb_cell_move(const Move &m, const SysDesc &d, const Smem &s) {
+    const int4 rec = make_int4(m.hn[0], m.hn[1], m.hn[2], __float_as_int(m.q));
+    const short4 ext = make_short4((short)m.en[0], (short)m.en[1], (short)m.en[2], 0);
+    const int slot = (int)(s.pcs[m.i] & 0xFFFu);
+    const int last = s.ccount[m.co] - 1;
+    if (last != slot) {
+        const int src = m.co * d.cap + last, dst = m.co * d.cap + slot;
+        const int pid = d.cell_pid[src];
+        d.cell_pos[dst] = d.cell_pos[src];
+        d.cell_ext[dst] = d.cell_ext[src];
+        d.cell_pid[dst] = pid;
+        s.pcs[pid & 0xFFFFFF] = ((uint32_t)m.co << 12) | (uint32_t)slot;
+    }
+    s.ccount[m.co] = last;
+    int ns = s.ccount[m.cn];
+    if (ns >= d.cap) {
+        d.sc->error |= kErrCellOverflow;
+        ns = d.cap - 1;
+    } else {
+        s.ccount[m.cn] = ns + 1;
+    }
+    d.cell_pos[m.cn * d.cap + ns] = rec;
+    d.cell_ext[m.cn * d.cap + ns] = ext;
+    d.cell_pid[m.cn * d.cap + ns] = m.i | (m.ti << 24);
+    s.pcs[m.i] = ((uint32_t)m.cn << 12) | (uint32_t)ns;
+}
+
 // Surface dipole change of a trial (Angstrom e), as surface_delta computes it.
 __device__ __forceinline__ void eb_dM(const Move &m, const SysDesc &d, float dM[3]) {
     const float qe = m.q * d.eff[m.ti];
@@ -903,23 +950,37 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
         const uint32_t accm = (uint32_t)s.info[1];
         rebuild = s.info[2] != 0;
         cnt_acc = s.info[3];
-        // ---- apply the accepted trials in order. Thread 0 commits the
-        // positions and cell lists (a serial chain of global updates) while
-        // warps 1.. update Q(k) in parallel, synchronising among themselves
-        // on named barrier 1; the block barrier below joins the two.
+        // ---- apply the accepted trials. Warp 0 commits the positions and
+        // cell lists while warps 1.. update Q(k), synchronising among
+        // themselves on named barrier 1; the block barrier below joins the two.
         const uint32_t live = accm & ((done >= 32) ? 0xffffffffu : ((1u << done) - 1u));
-        if (tid == 0) {
-            df M[3] = {{s.Mdf[0].x, s.Mdf[0].y}, {s.Mdf[1].x, s.Mdf[1].y}, {s.Mdf[2].x, s.Mdf[2].y}};
-            for (int a = 0; a < done; a++) {
-                if (!((accm >> a) & 1u)) continue;
-                commit_position(s.mv[a], d, s.b, false, CELLS);
-                float dm[3];
-                eb_dM(s.mv[a], d, dm);
-#pragma unroll
-                for (int x = 0; x < 3; x++) M[x] = df_add_f(M[x], dm[x]);
+        if (warp == 0) {
+            // positions (and, for a particle that stays in its cell, its
+            // cell record) of the accepted trials, one lane each: the
+            // particles are distinct; then lane 0 moves, in order, the
+            // particles that changed cells
+            const bool mine = (live >> lane) & 1u;
+            bool mover = false;
+            if (mine) {
+                const Move &A = s.mv[lane];
+                mover = CELLS && A.cn != A.co;
+                eb_commit_position(A, d, s.b, !mover);
             }
+            const uint32_t movers = __ballot_sync(0xffffffffu, mover);
+            __syncwarp();   // the lanes' records are visible to lane 0
+            if (lane == 0) {
+                df M[3] = {{s.Mdf[0].x, s.Mdf[0].y}, {s.Mdf[1].x, s.Mdf[1].y}, {s.Mdf[2].x, s.Mdf[2].y}};
+                for (int a = 0; a < done; a++) {
+                    if (!((accm >> a) & 1u)) continue;
+                    if ((movers >> a) & 1u) eb_cell_move(s.mv[a], d, s.b);
+                    float dm[3];
+                    eb_dM(s.mv[a], d, dm);
 #pragma unroll
-            for (int x = 0; x < 3; x++) s.Mdf[x] = make_float2(M[x].hi, M[x].lo);
+                    for (int x = 0; x < 3; x++) M[x] = df_add_f(M[x], dm[x]);
+                }
+#pragma unroll
+                for (int x = 0; x < 3; x++) s.Mdf[x] = make_float2(M[x].hi, M[x].lo);
+            }
         } else if (tid >= 32 && live) {
             // Q(k) += sum over accepted trials of c_k(new) - c_k(old), over
             // the rebuild's items (eb_commit_qk): each thread owns items of
