@@ -901,12 +901,10 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                 // (move.h:567-573): reject iff dU > kT (-ln u); a NaN dU
                 // compares false there: accepted
                 const float2 c = s.corr[a * kEbTrials + lane];   // loaded ahead of the decision
-                int f = 0;
-                if (lane == a) {
-                    const bool nan = !(S.hi == S.hi);
-                    f = ((colm & accm) != 0u ? 1 : 0) | (nan || !df_gt(S, df{th.x, th.y}) ? 2 : 0) | (nan ? 4 : 0);
-                }
-                f = __shfl_sync(0xffffffffu, f, a);
+                // every lane forms its own flags; lane a's are the ones used
+                const bool nan = !(S.hi == S.hi);
+                const int fl = ((colm & accm) != 0u ? 1 : 0) | (nan || !df_gt(S, df{th.x, th.y}) ? 2 : 0) | (nan ? 4 : 0);
+                const int f = __shfl_sync(0xffffffffu, fl, a);
                 if (f & 1) {   // its particle was moved by an accepted trial of this block
                     done = a;
                     break;
@@ -915,7 +913,10 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                 if (f & 2) {
                     accm |= 1u << a;
                     nacc++;
-                    if (lane > a && lane < kb) S = df_add_quick(S, df{c.x, c.y});
+                    const df Sc = df_add_quick(S, df{c.x, c.y});
+                    const bool later = lane > a && lane < kb;
+                    S.hi = later ? Sc.hi : S.hi;
+                    S.lo = later ? Sc.lo : S.lo;
                     // NonbondedEwald::update (ewald.h:633): a rebuild after
                     // update_frequency accepted trials ends the block here
                     if (++cnt_acc > uf - 1) {
