@@ -147,8 +147,14 @@ __global__ void __launch_bounds__(kE64Threads) energy64_qk_kernel(const SysDesc 
 
 namespace {
 
-// {pairs, reciprocal, self, surface, total} in kT, FP64 throughout.
-int total_energy_fp64(fg_system *h, double *c) {
+// {pairs, reciprocal, self, surface, total} in kT, FP64 throughout, of the
+// current configuration in each of nbox boxes: boxes[b] (box b's lengths;
+// the fixed-point positions X = x / L 2^64 stand for x = X L / 2^64 in any
+// box, so scaling every position with the box is the same X). Q(k) comes
+// from one pass (its exact phases depend on X only), the pair sum from one
+// pass per box at that box's scale, and the k-vector weights, reciprocal
+// prefactor and surface term are those of each box (ewald.h:330-378, 277-311).
+int total_energy_fp64_boxes(fg_system *h, int nbox, const double (*boxes)[3], double (*c)[5]) {
     const int N = h->N, nt = h->P.n_types;
     const fg_params &P = h->P;
     const bool ewald = h->model == FG_MODEL_EWALD_WCA;
@@ -157,7 +163,7 @@ int total_energy_fp64(fg_system *h, double *c) {
     const double kappa = ewald ? 1.0 / P.ewald_debye_length : 1.0 / P.dh_debye_length;
     for (int i = 0; i < nt; i++) {
         const double ri = 0.5 * P.type_sigma[i];
-        if (ewald && std::fabs(kappa * ri) > 1e-9) eff[i] = std::sinh(ri * kappa) / ri / kappa;
+        if (ewald && P.type_charge[i] != 0.0 && std::fabs(kappa * ri) > 1e-9) eff[i] = std::sinh(ri * kappa) / ri / kappa;
     }
     for (int i = 0; i < nt; i++)
         for (int j = 0; j < nt; j++) {
@@ -184,7 +190,7 @@ int total_energy_fp64(fg_system *h, double *c) {
         cudaFree(d_tp);
     };
     if (cudaMalloc(&d_q, N * sizeof(double)) != cudaSuccess || cudaMalloc(&d_qe, N * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&d_part, nb * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&d_part, (size_t)nbox * nb * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&d_tp, tp.size() * sizeof(fg::E64Pair)) != cudaSuccess ||
         (K > 0 && cudaMalloc(&d_qk, (size_t)nchunk * K * sizeof(double2)) != cudaSuccess)) {
         release();
@@ -194,11 +200,12 @@ int total_energy_fp64(fg_system *h, double *c) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_qe, qe.data(), N * sizeof(double), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_tp, tp.data(), tp.size() * sizeof(fg::E64Pair), cudaMemcpyHostToDevice, h->stream);
-    const double3 sc = make_double3(std::ldexp(P.box[0], -64), std::ldexp(P.box[1], -64), std::ldexp(P.box[2], -64));
-    if (e == cudaSuccess) {
+    for (int b = 0; b < nbox && e == cudaSuccess; b++) {
+        const double3 sc = make_double3(std::ldexp(boxes[b][0], -64), std::ldexp(boxes[b][1], -64),
+                                        std::ldexp(boxes[b][2], -64));
         fg::energy64_pairs_kernel<<<nb, fg::kE64Threads, 0, h->stream>>>(
             h->d_desc, d_q, d_tp, nt, sc, P.bjerrum, ewald ? P.ewald_alpha : 0.0, kappa,
-            ewald ? P.ewald_cutoff * P.ewald_cutoff : 0.0, ewald ? 1 : 0, d_part);
+            ewald ? P.ewald_cutoff * P.ewald_cutoff : 0.0, ewald ? 1 : 0, d_part + (size_t)b * nb);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess && K > 0) {
@@ -206,41 +213,72 @@ int total_energy_fp64(fg_system *h, double *c) {
                                  h->stream>>>(h->d_desc, d_qe, chunk, d_qk);
         e = cudaGetLastError();
     }
-    std::vector<double> part(nb);
+    std::vector<double> part((size_t)nbox * nb);
     std::vector<double2> qk(K > 0 ? (size_t)nchunk * K : 0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), d_part, nb * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess && K > 0)
         e = cudaMemcpyAsync(qk.data(), d_qk, qk.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     release();
     if (e != cudaSuccess) return fail(FG_ERR_CUDA, "FP64 energy: %s", cudaGetErrorString(e));
-    double pairs = 0;
-    for (double x : part) pairs += x;
-    double rec = 0, self = 0, surf = 0;
+    std::vector<double> q2;   // |Q(k)|^2
+    double M0[3] = {0, 0, 0};  // sum q eff x in the current box
     if (K > 0) {
+        q2.resize(K);
         for (int k = 0; k < K; k++) {
             double re = 0, im = 0;
             for (int b = 0; b < nchunk; b++) {
                 re += qk[(size_t)b * K + k].x;
                 im += qk[(size_t)b * K + k].y;
             }
-            rec += h->ak[k] * (re * re + im * im);
+            q2[k] = re * re + im * im;
         }
-        rec *= h->recip_c;
-        self = h->self_energy;
         std::vector<double> xyz(3 * (size_t)N);
         int rc = fg_get_state(h, xyz.data());
         if (rc) return rc;
-        double M[3] = {0, 0, 0};
         for (int j = 0; j < N; j++)
-            for (int a = 0; a < 3; a++) M[a] += qe[j] * xyz[3 * j + a];
-        surf = h->surf_c * (M[0] * M[0] + M[1] * M[1] + M[2] * M[2]);
+            for (int a = 0; a < 3; a++) M0[a] += qe[j] * xyz[3 * j + a];
     }
-    c[0] = pairs;
-    c[1] = rec;
-    c[2] = self;
-    c[3] = surf;
-    c[4] = (surf + rec) + (self + pairs);
+    for (int b = 0; b < nbox; b++) {
+        double pairs = 0;
+        for (int i = 0; i < nb; i++) pairs += part[(size_t)b * nb + i];
+        double rec = 0, self = 0, surf = 0;
+        if (K > 0) {
+            fg_params Pb = P;
+            for (int a = 0; a < 3; a++) Pb.box[a] = boxes[b][a];
+            const double V = Pb.box[0] * Pb.box[1] * Pb.box[2];
+            std::vector<int> n3;
+            std::vector<double> ak, kv3;
+            enumerate_k(Pb, n3, ak, kv3);
+            if ((int)ak.size() != K) return fail(FG_ERR_INVALID, "the k-vector set changes with the box");
+            for (int k = 0; k < K; k++) rec += ak[k] * q2[k];
+            rec *= 2 * PI / V * P.bjerrum;
+            self = h->self_energy;
+            const double const_inf = (P.ewald_eps_surf < 1) ? 0.0 : 1.0;
+            const double surf_c = const_inf * (2 * PI / ((2 * P.ewald_eps_surf + 1) * V)) * P.bjerrum;
+            double M2 = 0;
+            for (int a = 0; a < 3; a++) {
+                const double m = M0[a] * (boxes[b][a] / P.box[a]);
+                M2 += m * m;
+            }
+            surf = surf_c * M2;
+        }
+        c[b][0] = pairs;
+        c[b][1] = rec;
+        c[b][2] = self;
+        c[b][3] = surf;
+        c[b][4] = (surf + rec) + (self + pairs);
+    }
+    return FG_OK;
+}
+
+int total_energy_fp64(fg_system *h, double *c) {
+    const double box[1][3] = {{h->P.box[0], h->P.box[1], h->P.box[2]}};
+    double out[1][5];
+    int rc = total_energy_fp64_boxes(h, 1, box, out);
+    if (rc) return rc;
+    for (int i = 0; i < 5; i++) c[i] = out[0][i];
     return FG_OK;
 }
 

@@ -1,4 +1,4 @@
-// Isobaric volume move (included by fg_api.cu; host driven).
+// Isobaric volume move (included by fg_api.cu).
 //
 // Restates Move::Isobaric (move.h:5529-5624) with Energy::ExternalPressure
 // (energy.h:1817-1890) for one atomic group, as the reference's bulk example
@@ -12,13 +12,20 @@
 //   g_external (-N ln V for N atoms);
 //   Metropolis as Movebase::metropolis (move.h:567-573): reject iff u > exp(-dU/kT).
 //
-// The trial box is a complete second system built with the new box (k-vector
-// weights, cell grid and displacement steps all follow from it; Q(k) is
-// rebuilt there from scratch, as NonbondedEwald::updateChange does for a
-// geometry change, ewald.h:651-659). An accepted move swaps the two systems'
-// contents, so the caller's handle keeps working. The running energy
+// On the device and in place: with positions in fixed point relative to the
+// box (X = x / L 2^64), scaling every position about the origin leaves every
+// X as it is, so the trial configuration is the current one read in the new
+// box. Both boxes' energies come from one FP64 pass over the fixed-point
+// positions (Q(k) once: its exact phases depend on X only; the pair sum at
+// each box's scale); an accepted move then changes only the box and what
+// follows from it (apply_box), and Q(k) stays exact and unchanged, where the
+// reference rebuilds it from scratch for the new geometry
+// (NonbondedEwald::updateChange, ewald.h:651-659). The running energy
 // continues by E(V') - E(V); the accepted-move counter of the Q(k) rebuild
-// cadence advances as NonbondedEwald::update counts (ewald.h:633).
+// cadence advances as NonbondedEwald::update counts (ewald.h:633). A trial
+// box with another cell grid (the cutoff fits a different number of times)
+// takes the general path instead: a second system at the trial box, swapped
+// in on acceptance (volume_move_rebuilt).
 //
 // Reference quirk (Ewald only). During the reference's energyChange for a
 // geometry change, NonbondedEwald::setSpace -> setGeometry rebuilds Q(k)
@@ -31,10 +38,10 @@
 // configurations. (Ours keeps the exact Q(k) of the scaled positions after
 // an accepted move either way; the reference carries the unscaled one until
 // its next update_frequency rebuild.)
-double recip_unscaled(const fg_system *h, const fg_system *t, const std::vector<double> &xyz_old) {
+double recip_unscaled(const fg_system *h, const fg_params &Pn, double recip_c, const std::vector<double> &xyz_old) {
     std::vector<int> n3;
     std::vector<double> ak, kv3;
-    enumerate_k(t->P, n3, ak, kv3);
+    enumerate_k(Pn, n3, ak, kv3);
     double rec = 0;
     for (size_t k = 0; k < ak.size(); k++) {
         double re = 0, im = 0;
@@ -47,21 +54,61 @@ double recip_unscaled(const fg_system *h, const fg_system *t, const std::vector<
         }
         rec += ak[k] * (re * re + im * im);
     }
-    return rec * t->recip_c;
+    return rec * recip_c;
 }
 
-extern "C" int fg_volume_move(fg_system *h, double half, double dp, double pressure, double u,
-                              int32_t reference_quirk, double *du, int32_t *accepted) {
-    if (!h || !du || !accepted) return fail(FG_ERR_INVALID, "null argument");
-    if (h->types.empty()) return fail(FG_ERR_STATE, "fg_set_state first");
-    if (h->trial_pending) return fail(FG_ERR_STATE, "a trial is pending: commit it first");
-    if (h->batches > 0) return fail(FG_ERR_STATE, "the system is in a batch: destroy the batch first");
-    if (!(pressure >= 0.0) || !std::isfinite(half) || !std::isfinite(dp))
-        return fail(FG_ERR_INVALID, "bad volume move arguments");
+namespace {
+
+// The system in a new box, in place. The fixed-point positions X = x / L 2^64
+// are the scaled positions in the new box as they are, and Q(k) = sum q eff
+// e^{2 pi i n.X / 2^64} does not change at all; what changes are the box
+// lengths and everything derived from them: the units of a coordinate word,
+// the k-vectors and their weights A_k and prefactor 2 pi lB / V
+// (kVectorChange, ewald.h:330-378), the surface prefactor, and the
+// displacement steps in fixed point. Requires the same cell grid.
+int apply_box(fg_system *h, const double box[3]) {
+    fg_params &P = h->P;
+    for (int a = 0; a < 3; a++) P.box[a] = box[a];
+    SysDesc &d = h->desc;
+    for (int a = 0; a < 3; a++) {
+        d.L[a] = (float)P.box[a];
+        d.s32[a] = (float)(P.box[a] / 4294967296.0);
+        d.dl32[a] = (float)(P.box[a] / TWO64);
+        d.s48_df[a] = split_df(P.box[a] / 281474976710656.0);
+    }
+    d.s32sq = (float)((P.box[0] / 4294967296.0) * (P.box[0] / 4294967296.0));
+    if (h->K > 0) {
+        std::vector<int> n3;
+        std::vector<double> ak, kv3;
+        enumerate_k(P, n3, ak, kv3);
+        if ((int)ak.size() != h->K) return fail(FG_ERR_INVALID, "the k-vector set changes with the box");
+        const double V = P.box[0] * P.box[1] * P.box[2];
+        h->ak = ak;
+        h->recip_c = 2 * PI / V * P.bjerrum;
+        const double const_inf = (P.ewald_eps_surf < 1) ? 0.0 : 1.0;
+        h->surf_c = const_inf * (2 * PI / ((2 * P.ewald_eps_surf + 1) * V)) * P.bjerrum;
+        d.surf_c = (float)h->surf_c;
+        std::vector<float4> kv(h->K);
+        for (int k = 0; k < h->K; k++)
+            kv[k] = make_float4((float)kv3[3 * k], (float)kv3[3 * k + 1], (float)kv3[3 * k + 2],
+                                (float)(h->ak[k] * h->recip_c));
+        CK(cudaMemcpyAsync(h->kvec, kv.data(), h->K * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    std::vector<int64_t> dpf(FG_MAX_TYPES * 3, 0);
+    for (int t = 0; t < P.n_types; t++)
+        for (int a = 0; a < 3; a++) dpf[3 * t + a] = (int64_t)llrint(P.type_dp[t] / P.box[a] * 4294967296.0);
+    CK(cudaMemcpyAsync(h->dp_fix, dpf.data(), dpf.size() * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    return push_desc(h);
+}
+
+// The move with the trial box as a complete second system (k-vectors, cell
+// grid and displacement steps from it; Q(k) rebuilt there), swapped in on
+// acceptance: for a trial box with another cell grid.
+int volume_move_rebuilt(fg_system *h, double Vn, double f, double pressure, double u, int32_t reference_quirk,
+                        double *du, int32_t *accepted) {
     const int N = h->N;
     const double V = h->P.box[0] * h->P.box[1] * h->P.box[2];
-    const double Vn = std::exp(std::log(V) + half * dp);
-    const double f = std::cbrt(Vn / V);
     std::vector<double> xyz(3 * (size_t)N);
     int rc = fg_get_state(h, xyz.data());
     if (rc) return rc;
@@ -79,20 +126,18 @@ extern "C" int fg_volume_move(fg_system *h, double half, double dp, double press
     };
     rc = fg_set_state(t, xyz.data(), h->charges.data(), h->types.data());
     if (rc) return drop(rc);
-    // whole-system energies in FP64: the move's dU is their difference
     double e0[5], e1[5];
     rc = total_energy_fp64(h, e0);
     if (!rc) rc = total_energy_fp64(t, e1);
     if (rc) return drop(rc);
     const double dE = e1[4] - e0[4];
     double d = dE + pressure * (Vn - V) - (N + 1) * std::log(Vn / V);
-    if (reference_quirk && h->K > 0) d += recip_unscaled(h, t, xyz_old) - e1[1];
+    if (reference_quirk && h->K > 0) d += recip_unscaled(h, t->P, t->recip_c, xyz_old) - e1[1];
     *du = d;
     const double kT = h->desc.kT;
     const bool acc = !(u > std::exp(-d / kT));   // NaN dU: accepted, as the reference's comparison
     *accepted = acc ? 1 : 0;
     if (!acc) return drop(FG_OK);
-    // carry the running energy, counters and settings over to the new box
     SysScalars s0, s1;
     rc = read_scalars(h, s0);
     if (!rc) rc = read_scalars(t, s1);
@@ -124,6 +169,81 @@ extern "C" int fg_volume_move(fg_system *h, double half, double dp, double press
     }
     std::swap(*h, *t);
     fg_destroy(t);   // the old box's arrays
+    return FG_OK;
+}
+
+}  // namespace
+
+extern "C" int fg_volume_move(fg_system *h, double half, double dp, double pressure, double u,
+                              int32_t reference_quirk, double *du, int32_t *accepted) {
+    if (!h || !du || !accepted) return fail(FG_ERR_INVALID, "null argument");
+    if (h->types.empty()) return fail(FG_ERR_STATE, "fg_set_state first");
+    if (h->trial_pending) return fail(FG_ERR_STATE, "a trial is pending: commit it first");
+    if (h->batches > 0) return fail(FG_ERR_STATE, "the system is in a batch: destroy the batch first");
+    if (!(pressure >= 0.0) || !std::isfinite(half) || !std::isfinite(dp))
+        return fail(FG_ERR_INVALID, "bad volume move arguments");
+    const int N = h->N;
+    const double V = h->P.box[0] * h->P.box[1] * h->P.box[2];
+    const double Vn = std::exp(std::log(V) + half * dp);
+    const double f = std::cbrt(Vn / V);
+    const double box1[3] = {h->P.box[0] * f, h->P.box[1] * f, h->P.box[2] * f};
+    bool same_grid = true;
+    if (h->use_cells)
+        for (int a = 0; a < 3; a++)
+            if ((int)std::floor(box1[a] / h->P.ewald_cutoff) != h->nc[a]) same_grid = false;
+    if (!same_grid) return volume_move_rebuilt(h, Vn, f, pressure, u, reference_quirk, du, accepted);
+    // both boxes' FP64 energies of the same fixed-point configuration
+    const double boxes[2][3] = {{h->P.box[0], h->P.box[1], h->P.box[2]}, {box1[0], box1[1], box1[2]}};
+    double e[2][5];
+    int rc = total_energy_fp64_boxes(h, 2, boxes, e);
+    if (rc) return rc;
+    const double dE = e[1][4] - e[0][4];
+    double d = dE + pressure * (Vn - V) - (N + 1) * std::log(Vn / V);
+    if (reference_quirk && h->K > 0) {
+        std::vector<double> xyz_old(3 * (size_t)N);
+        rc = fg_get_state(h, xyz_old.data());
+        if (rc) return rc;
+        fg_params Pn = h->P;
+        for (int a = 0; a < 3; a++) Pn.box[a] = box1[a];
+        d += recip_unscaled(h, Pn, 2 * PI / Vn * h->P.bjerrum, xyz_old) - e[1][1];
+    }
+    *du = d;
+    const double kT = h->desc.kT;
+    const bool acc = !(u > std::exp(-d / kT));   // NaN dU: accepted, as the reference's comparison
+    *accepted = acc ? 1 : 0;
+    if (!acc) return FG_OK;
+    rc = apply_box(h, box1);
+    if (rc) return rc;
+    SysScalars s0;
+    rc = read_scalars(h, s0);
+    if (rc) return rc;
+    const float2 ut = split_df(df_val(s0.utot_hi, s0.utot_lo) + dE);
+    s0.utot_hi = ut.x;
+    s0.utot_lo = ut.y;
+    for (int a = 0; a < 3; a++) {   // the surface dipole sum q eff x scales with the positions
+        const float2 m = split_df(df_val(s0.m[a][0], s0.m[a][1]) * f);
+        s0.m[a][0] = m.x;
+        s0.m[a][1] = m.y;
+    }
+    bool rebuild = false;
+    if (h->K > 0) {
+        // NonbondedEwald::update counts the accepted move (ewald.h:633);
+        // Q(k) is unchanged and exact, so a rebuild due here only verifies it
+        int cnt = s0.cnt_accepted + 1;
+        if (cnt > h->P.ewald_update_frequency - 1) {
+            cnt = 0;
+            rebuild = !h->desc.skip_rebuild;
+        }
+        s0.cnt_accepted = cnt;
+        h->cnt_accepted_host = cnt;
+    }
+    rc = write_scalars(h, s0);
+    if (rc) return rc;
+    if (rebuild) {
+        double corr = 0;
+        rc = fg_rebuild_qk(h, &corr);
+        if (rc) return rc;
+    }
     return FG_OK;
 }
 
