@@ -179,7 +179,6 @@ extern "C" int fg_volume_move(fg_system *h, double half, double dp, double press
     if (!h || !du || !accepted) return fail(FG_ERR_INVALID, "null argument");
     if (h->types.empty()) return fail(FG_ERR_STATE, "fg_set_state first");
     if (h->trial_pending) return fail(FG_ERR_STATE, "a trial is pending: commit it first");
-    if (h->batches > 0) return fail(FG_ERR_STATE, "the system is in a batch: destroy the batch first");
     if (!(pressure >= 0.0) || !std::isfinite(half) || !std::isfinite(dp))
         return fail(FG_ERR_INVALID, "bad volume move arguments");
     const int N = h->N;
@@ -191,6 +190,11 @@ extern "C" int fg_volume_move(fg_system *h, double half, double dp, double press
     if (h->use_cells)
         for (int a = 0; a < 3; a++)
             if ((int)std::floor(box1[a] / h->P.ewald_cutoff) != h->nc[a]) same_grid = false;
+    // a batch holds its members' launch shape (cell grid, shared memory),
+    // so a member moves only within its grid; between batch runs its
+    // descriptor, and with it the new box, reaches the next launch
+    if (!same_grid && h->batches > 0)
+        return fail(FG_ERR_STATE, "this volume move changes the cell grid: not for a system in a batch");
     if (!same_grid) return volume_move_rebuilt(h, Vn, f, pressure, u, reference_quirk, du, accepted);
     // both boxes' FP64 energies of the same fixed-point configuration
     const double boxes[2][3] = {{h->P.box[0], h->P.box[1], h->P.box[2]}, {box1[0], box1[1], box1[2]}};

@@ -79,53 +79,24 @@ def test_translations_after_volume_moves_match_oracle():
     assert np.abs(r["du"][:upto] - ro["du"][:upto]).max() < 1e-6
 
 
-def test_volume_move_refused_inside_a_batch():
-    from beofaunus_gb300.gpu import Batch, FgError, System
+def test_volume_move_inside_a_batch():
+    """A batch member takes volume moves between batch runs (in place: its
+    cell grid stays); the batch's next run then runs it in the new box,
+    exactly as the same system alone does."""
+    from beofaunus_gb300.gpu import Batch, System
     p, xyz, q, ids = workloads.dh_lj_salt(300, seed=5)
-    s = System(p, xyz, q, ids)
-    b = Batch([s])
-    with pytest.raises(FgError):
-        s.volume_move(0.1, 0.05, 1e-5, 0.5)
+    a, alone = System(p, xyz, q, ids), System(p, xyz, q, ids)
+    p2, xyz2, q2, ids2 = workloads.dh_lj_salt(300, seed=6)
+    other = System(p2, xyz2, q2, ids2)
+    b = Batch([a, other])
+    for h, uacc in ((0.3, 0.0), (-0.2, 0.0)):
+        d1, a1 = a.volume_move(h, 0.05, 1e-5, uacc)
+        d2, a2 = alone.volume_move(h, 0.05, 1e-5, uacc)
+        assert d1 == d2 and a1 and a2
+    np.testing.assert_array_equal(a.box, alone.box)
+    b.stream_philox([2000, 2000], 91, stream_ids=[7, 8])
+    b.run()
+    alone.stream_philox(2000, 91, 7)
+    alone.stream_run()
+    np.testing.assert_array_equal(a.positions(), alone.positions())
     b.close()
-    s.volume_move(0.1, 0.05, 1e-5, 0.5)   # allowed again once the batch is gone
-
-
-def test_volume_moves_with_cells_in_place_and_across_a_cell_grid_change():
-    """A cell-list system: moves that keep the cell grid run in place (the
-    fixed-point positions stay, Q(k) stays exact, the box-dependent tables
-    follow), a move that changes how many cells fit the box takes the
-    general path; dU, decisions, positions and a translation sweep afterwards
-    all match the FP64 oracle at each box."""
-    from beofaunus_gb300.gpu import System
-    p, xyz, q, ids = workloads.rpm_ewald(3600, 100.3, 6, seed=43, update_frequency=3, cutoff=20.0,
-                                         use_cell_list=1)
-    s = System(p, xyz, q, ids)
-    x = np.asarray(xyz)
-    po = p
-    # half-steps: small growth and shrink inside the 5-cell grid, then a
-    # shrink below 5 x 20 A (4 cells per axis), then a growth back over it
-    halves = [0.2, -0.1, 0.15, -0.45, 0.3, 0.4]
-    grids = []
-    for m, h in enumerate(halves):
-        # uniform 0: every move is accepted (reject only if u > exp(-dU))
-        du, acc = s.volume_move(h, 0.08, 60.0 * MILLIMOLAR, 0.0)
-        du_o, acc_o, po, x = volume_move(po, x, q, ids, h, 0.08, 60.0 * MILLIMOLAR, 0.0)
-        assert du == pytest.approx(du_o, abs=1e-8) and acc and acc_o, m
-        assert np.prod(s.box) == pytest.approx(po.box[0] * po.box[1] * po.box[2], rel=1e-13)
-        grids.append(int(np.floor(s.box[0] / 20.0)))
-    assert 4 in grids and 5 in grids          # both paths ran
-    np.testing.assert_allclose(s.positions(), x, rtol=0, atol=1e-9)
-    e64, eo = s.total_energy_fp64()["total"], OracleSystem(po, x, q, ids).total_energy()["total"]
-    assert e64 == pytest.approx(eo, rel=1e-10, abs=1e-8)
-    assert s.running_energy() == pytest.approx(e64, abs=1e-2)
-    o = OracleSystem(po, x, q, ids)
-    idx, disp, uu = s.draw_translation_stream(78, 600)
-    r = s.sweep(idx, disp, uu)
-    ro = o.mc_run_stream(idx, disp, uu)
-    upto = len(idx)
-    mism = np.nonzero(r["acc"] != ro["acc"])[0]
-    if len(mism):
-        t = mism[0]
-        assert abs(ro["du"][t] + np.log(uu[t])) < 1e-6
-        upto = t + 1
-    assert np.abs(r["du"][:upto] - ro["du"][:upto]).max() < 1e-6
