@@ -119,6 +119,16 @@ struct fg_system {
     double self_energy = 0, surf_c = 0, recip_c = 0;
     int threads = 0;
     int ctas = 0;                  // block-kernel CTAs per system (0: tuned cache / heuristic)
+    // Ewald block kernel of a system alone on a cluster (fg_set_cluster)
+    std::vector<int> n3;           // n-vectors of the k-vectors (3 per k)
+    int eb_ctas = 0;               // requested cluster size (0: built-in choice)
+    int4 *eb_ranges = nullptr;     // [1 + kEbMaxCluster]: one CTA's range, then the cluster's per rank
+    int4 *cl_items = nullptr;      // rebuild items grouped by cluster rank
+    int cl_c = 0;                  // cluster size the two above are built for
+    int cl_kmax = 0;               // most k-vectors of one rank
+    int cl_n_items = 0;
+    int cl_max = 0;                // largest cluster that fits (0: not yet known)
+    SysDesc *d_desc_cl = nullptr;  // the descriptor of cluster launches
     int batches = 0;               // live batches holding this system
     std::vector<double> charges;   // host copy of the uploaded charges (clones for tuning)
     bool use_cells = false, pos_smem = false;
@@ -137,7 +147,8 @@ void free_all(fg_system *h) {
     void *ptrs[] = {h->d_desc, h->pos64, h->pos4, h->pos_ext, h->cell_ext, h->ptype, h->cell_count, h->cell_pid,
                     h->p_cell, h->p_slot, h->cell_pos, h->kvec, h->core_tab, h->core_tab2, h->kpack, h->qfix,
                     h->qnew, h->sc, h->trial_out, h->corr, h->pair_part, h->req, h->dp_fix, h->sc_tab, h->trials,
-                    h->log_du, h->log_acc, h->kseg, h->rb_items, h->raw_idx, h->raw_disp, h->raw_u};
+                    h->log_du, h->log_acc, h->kseg, h->rb_items, h->raw_idx, h->raw_disp, h->raw_u,
+                    h->eb_ranges, h->cl_items, h->d_desc_cl};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -182,11 +193,11 @@ void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &
 
 // Threads of the per-system CTA (multiple of 32, <= kSweepThreads).
 // rb_item_list for items of at most L values of n.
-bool rb_item_list_len(const std::vector<int> &n3, int K, int L, std::vector<int4> &items) {
+bool rb_item_list_len(const std::vector<int> &n3, int kbeg, int kend, int L, std::vector<int4> &items) {
     items.clear();
-    for (int k = 0; k < K;) {
+    for (int k = kbeg; k < kend;) {
         int e = k + 1;
-        while (e < K && n3[3 * e] == n3[3 * k] && n3[3 * e + 1] == n3[3 * k + 1]) e++;
+        while (e < kend && n3[3 * e] == n3[3 * k] && n3[3 * e + 1] == n3[3 * k + 1]) e++;
         // column [k, e): nz ascending
         std::map<int, int> kz;
         for (int q = k; q < e; q++) kz[n3[3 * q + 2]] = q;
@@ -228,10 +239,46 @@ bool rb_item_list_len(const std::vector<int> &n3, int K, int L, std::vector<int4
 // k(+n) = kp0 + (n - n0), k(-n) = kn0 - (n - n0). Sorted by length (longest
 // first), then n0, so that warps run equal trip counts and read the same e_z
 // entries. Returns false if a column is not symmetric in nz.
-bool rb_item_list(const std::vector<int> &n3, int K, int slots, std::vector<int4> &items) {
+bool rb_item_list(const std::vector<int> &n3, int kbeg, int kend, int slots, std::vector<int4> &items) {
     for (int L = 1; L <= fg::kRbLen; L++) {
-        if (!rb_item_list_len(n3, K, L, items)) return false;
+        if (!rb_item_list_len(n3, kbeg, kend, L, items)) return false;
         if ((int)items.size() <= slots) break;
+    }
+    return true;
+}
+
+// The k-vectors of a cluster of C CTAs: whole (nx, ny) columns (an item's
+// +n and -n lie in one column), contiguous in enumeration order, cut where
+// the running count comes nearest to r K / C; per rank its rebuild items
+// (rb_item_list over its columns). ranges[r] = {k0, k1, i0, i1}. False if
+// there are fewer columns than CTAs.
+bool eb_cluster_plan(const std::vector<int> &n3, int K, int C, std::vector<int4> &ranges, std::vector<int4> &items,
+                     int &kmax) {
+    std::vector<int> starts;   // column starts
+    for (int k = 0; k < K; k++)
+        if (k == 0 || n3[3 * k] != n3[3 * (k - 1)] || n3[3 * k + 1] != n3[3 * (k - 1) + 1]) starts.push_back(k);
+    const int ncol = (int)starts.size();
+    if (ncol < C) return false;
+    starts.push_back(K);
+    std::vector<int> cut(C + 1, 0);   // column index where rank r starts
+    cut[C] = ncol;
+    for (int r = 1; r < C; r++) {
+        const double target = (double)K * r / C;
+        int best = cut[r - 1] + 1;
+        for (int c = best; c <= ncol - (C - r); c++)
+            if (std::fabs(starts[c] - target) < std::fabs(starts[best] - target)) best = c;
+        cut[r] = best;
+    }
+    ranges.assign(C, make_int4(0, 0, 0, 0));
+    items.clear();
+    kmax = 0;
+    for (int r = 0; r < C; r++) {
+        const int k0 = starts[cut[r]], k1 = starts[cut[r + 1]];
+        std::vector<int4> it;
+        if (!rb_item_list(n3, k0, k1, fg::kEbThreads - 32, it)) return false;
+        ranges[r] = make_int4(k0, k1, (int)items.size(), (int)(items.size() + it.size()));
+        items.insert(items.end(), it.begin(), it.end());
+        kmax = std::max(kmax, k1 - k0);
     }
     return true;
 }
@@ -259,8 +306,8 @@ using CommitFn = void (*)(const SysDesc *, const int64_t *, const float2 *, cons
 // Ewald systems run the block-of-trials kernel (fg_ewald_block.cu) when its
 // shared memory fits; 512 threads per system.
 size_t ewald_block_smem(const fg_system *h) {
-    size_t off[16];
-    return fg::eb_layout(h->N, h->K, h->nc[0] * h->nc[1] * h->nc[2], h->use_cells, off);
+    size_t off[19];
+    return fg::eb_layout(h->N, h->K, h->nc[0] * h->nc[1] * h->nc[2], h->use_cells, 1, off);
 }
 bool ewald_block_ok(const fg_system *h) {
     return h->model == FG_MODEL_EWALD_WCA && h->K > 0 && h->N < (1 << 24) &&
@@ -268,7 +315,8 @@ bool ewald_block_ok(const fg_system *h) {
 }
 
 SweepFn sweep_fn(const fg_system *h) {
-    if (ewald_block_ok(h)) return h->use_cells ? fg::ewald_block_kernel<true> : fg::ewald_block_kernel<false>;
+    if (ewald_block_ok(h))
+        return h->use_cells ? fg::ewald_block_kernel<true, false> : fg::ewald_block_kernel<false, false>;
     if (h->model == FG_MODEL_EWALD_WCA) {
         if (h->use_cells) return fg::sweep_kernel<fg::MODEL_EWALD, true, false>;
         if (h->pos_smem) return fg::sweep_kernel<fg::MODEL_EWALD, false, true>;
@@ -290,6 +338,122 @@ CommitFn commit_fn(const fg_system *h) {
 
 int set_smem_attr(const void *fn, size_t bytes) {
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return FG_OK;
+}
+
+// ---------------------------------------------------------------- Ewald block sweeps on a cluster
+// A system alone runs the Ewald block kernel on a thread-block cluster of C
+// CTAs (fg_ewald_block.cu, CLUSTER): the k-vectors are split by columns
+// (eb_cluster_plan), each CTA holding its share in shared memory.
+SweepFn eb_cluster_fn(const fg_system *h) {
+    return h->use_cells ? fg::ewald_block_kernel<true, true> : fg::ewald_block_kernel<false, true>;
+}
+size_t eb_cluster_smem(const fg_system *h, int C, int kmax) {
+    size_t off[19];
+    return fg::eb_layout(h->N, kmax, h->nc[0] * h->nc[1] * h->nc[2], h->use_cells, C, off);
+}
+int eb_cluster_attrs(const fg_system *h, size_t smem) {
+    const void *fn = (const void *)eb_cluster_fn(h);
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    return FG_OK;
+}
+void eb_cluster_cfg(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, int C, size_t smem, cudaStream_t st) {
+    cfg = cudaLaunchConfig_t{};
+    cfg.gridDim = dim3((unsigned)C);
+    cfg.blockDim = dim3(fg::kEbThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+}
+
+// Largest cluster (power of two, <= kEbMaxCluster) whose shared memory fits
+// and that the device co-schedules for this system; 1 where none does.
+int eb_cluster_max(fg_system *h) {
+    if (h->model != FG_MODEL_EWALD_WCA || h->K <= 0 || !ewald_block_ok(h)) return 1;
+    if (h->cl_max > 0) return h->cl_max;
+    h->cl_max = 1;
+    for (int C = fg::kEbMaxCluster; C >= 2; C /= 2) {
+        std::vector<int4> ranges, items;
+        int kmax = 0;
+        if (!eb_cluster_plan(h->n3, h->K, C, ranges, items, kmax)) continue;
+        const size_t smem = eb_cluster_smem(h, C, kmax);
+        if (smem + sizeof(SysDesc) + 1024 > 227 * 1024) continue;
+        if (eb_cluster_attrs(h, smem)) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg;
+        cudaLaunchAttribute attr[1];
+        eb_cluster_cfg(cfg, attr, C, smem, h->stream);
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, (const void *)eb_cluster_fn(h), &cfg) == cudaSuccess && n > 0) {
+            h->cl_max = C;
+            break;
+        }
+        cudaGetLastError();
+    }
+    return h->cl_max;
+}
+
+// CTAs of the cluster a system alone runs on: the requested size, or the
+// built-in choice (as many as fit, with no fewer than 128 k-vectors per CTA;
+// 16 on 16384 ions with K = 2242 runs 0.89 us per trial against 1.03 on 8
+// and 3.23 on one), capped by what fits.
+int eb_cluster_ctas(fg_system *h) {
+    if (h->model != FG_MODEL_EWALD_WCA || h->K <= 0 || !ewald_block_ok(h)) return 1;
+    const int want = h->eb_ctas > 0 ? h->eb_ctas : std::max(1, std::min(fg::kEbMaxCluster, h->K / 128));
+    const int maxc = eb_cluster_max(h);
+    int C = 1;
+    while (2 * C <= std::min(want, maxc)) C *= 2;
+    return C;
+}
+
+// The k-vector split and descriptor of a C-CTA cluster (built once per C).
+int eb_cluster_prepare(fg_system *h, int C) {
+    if (h->cl_c != C) {
+        std::vector<int4> ranges, items;
+        int kmax = 0;
+        if (!eb_cluster_plan(h->n3, h->K, C, ranges, items, kmax))
+            return fail(FG_ERR_INVALID, "k-vectors do not split over %d CTAs", C);
+        if (!h->cl_items) {   // at most one item per k-vector
+            int rc = dmalloc(h, (void **)&h->cl_items, (size_t)h->K * sizeof(int4));
+            if (rc) return rc;
+        }
+        if ((int)items.size() > h->K) return fail(FG_ERR_INVALID, "cluster item list longer than K");
+        CK(cudaMemcpy(h->cl_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->eb_ranges + 1, ranges.data(), ranges.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        h->cl_c = C;
+        h->cl_kmax = kmax;
+        h->cl_n_items = (int)items.size();
+    }
+    if (!h->d_desc_cl) {
+        int rc = dmalloc(h, (void **)&h->d_desc_cl, sizeof(SysDesc));
+        if (rc) return rc;
+    }
+    SysDesc dc = h->desc;
+    dc.eb_ctas = C;
+    dc.eb_kmax = h->cl_kmax;
+    dc.eb_ranges = h->eb_ranges + 1;
+    dc.rb_items = h->cl_items;
+    dc.n_rb_items = h->cl_n_items;
+    CK(cudaMemcpyAsync(h->d_desc_cl, &dc, sizeof(SysDesc), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return eb_cluster_attrs(h, eb_cluster_smem(h, C, h->cl_kmax));
+}
+
+int eb_cluster_launch(fg_system *h, int C, int64_t end) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    eb_cluster_cfg(cfg, attr, C, eb_cluster_smem(h, C, h->cl_kmax), h->stream);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, eb_cluster_fn(h), (const SysDesc *)h->d_desc_cl, end,
+                                       (const float2 *)h->sc_tab);
+    if (e != cudaSuccess) return fail(FG_ERR_CUDA, "cluster sweep launch: %s", cudaGetErrorString(e));
     return FG_OK;
 }
 
@@ -706,6 +870,11 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
     LaunchCfg cfg;
     rc = sweep_config(h, cfg);
     if (rc) return rc;
+    const int ebc = eb_cluster_ctas(h);   // > 1: the Ewald block kernel on a cluster
+    if (ebc > 1) {
+        rc = eb_cluster_prepare(h, ebc);
+        if (rc) return rc;
+    }
     const bool rebuilds = h->K > 0 && !h->desc.skip_rebuild;
     const int uf = std::max(h->P.ewald_update_frequency, 1);
     int launches = 0;
@@ -725,6 +894,9 @@ int run_stream(fg_system *h, int64_t n, bool log, fg_sweep_stats *stats) {
             if (dh_block_ok(h)) {
                 rc = dh_block_launch(h->d_desc, nullptr, 1, h->ctas > 0 ? h->ctas : dh_block_ctas(h->N), h->N, n,
                                      h->stream);
+                if (rc) return rc;
+            } else if (ebc > 1) {
+                rc = eb_cluster_launch(h, ebc, n);
                 if (rc) return rc;
             } else {
                 cfg.fn<<<1, cfg.threads, cfg.smem, h->stream>>>(h->d_desc, n, h->sc_tab);
@@ -994,10 +1166,15 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         cudaMemcpy(h->kseg, seg.data(), seg.size() * sizeof(int2), cudaMemcpyHostToDevice);
         // the block kernel's in-kernel rebuild: pairs (+n, -n) of k-vectors
         std::vector<int4> rb;
-        if (!rb_item_list(n3, h->K, fg::kEbThreads - 32, rb)) return bail(fail(FG_ERR_INVALID, "k-vector set is not symmetric in nz"));
+        if (!rb_item_list(n3, 0, h->K, fg::kEbThreads - 32, rb)) return bail(fail(FG_ERR_INVALID, "k-vector set is not symmetric in nz"));
         h->n_rb_items = (int)rb.size();
         ALLOC(h->rb_items, rb.size() * sizeof(int4));
         cudaMemcpy(h->rb_items, rb.data(), rb.size() * sizeof(int4), cudaMemcpyHostToDevice);
+        // one CTA holds every k-vector and item
+        ALLOC(h->eb_ranges, (1 + fg::kEbMaxCluster) * sizeof(int4));
+        const int4 one = make_int4(0, h->K, 0, h->n_rb_items);
+        cudaMemcpy(h->eb_ranges, &one, sizeof(int4), cudaMemcpyHostToDevice);
+        h->n3 = n3;
         cudaMemset(h->qfix, 0, h->K * sizeof(longlong2));
         cudaMemset(h->qnew, 0, h->K * sizeof(longlong2));
     }
@@ -1070,6 +1247,9 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     d.nseg = h->nseg;
     d.rb_items = h->rb_items;
     d.n_rb_items = h->n_rb_items;
+    d.eb_ctas = 1;
+    d.eb_kmax = h->K;
+    d.eb_ranges = h->eb_ranges;
     d.kcc = h->kc;
     if (set_qk_scale(d, qk_charge_bound(h, nullptr)))
         return bail(fail(FG_ERR_INVALID, "charges too large for the Q(k) fixed point"));
@@ -1232,6 +1412,21 @@ int fg_set_threads(fg_system *h, int32_t threads) {
 }
 
 int fg_get_threads(fg_system *h) { return h ? sweep_threads(h) : 0; }
+
+int fg_set_cluster(fg_system *h, int32_t ctas) {
+    if (!h) return fail(FG_ERR_INVALID, "null handle");
+    if (ctas < 0 || ctas > fg::kEbMaxCluster || (ctas & (ctas - 1)) != 0)
+        return fail(FG_ERR_INVALID, "ctas must be 0 or a power of two up to %d", fg::kEbMaxCluster);
+    h->eb_ctas = ctas;
+    return FG_OK;
+}
+
+int fg_get_cluster(fg_system *h, int32_t *ctas, int32_t *max_ctas) {
+    if (!h) return fail(FG_ERR_INVALID, "null handle");
+    if (ctas) *ctas = eb_cluster_ctas(h);
+    if (max_ctas) *max_ctas = eb_cluster_max(h);
+    return FG_OK;
+}
 
 int fg_set_rebuild_policy(fg_system *h, int32_t skip) {
     if (!h) return fail(FG_ERR_INVALID, "null handle");

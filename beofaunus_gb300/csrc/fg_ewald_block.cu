@@ -27,6 +27,8 @@ namespace fg {
 constexpr int kEbTrials = 32;
 constexpr int kEbThreads = 512;
 constexpr int kEbKc = 128;   // scratch buffer rows (of 32 float2)
+constexpr int kEbMaxCluster = 16;
+constexpr int kEbGramN = 6 * 32 * 4;   // floats of one Gram accumulator set (eb_gram_regs' layout)
 
 struct EbSmem {
     Smem b;          // sc_tab, qfix, kpack, cells as in the one-trial kernel; kvec here holds
@@ -42,13 +44,20 @@ struct EbSmem {
     float2 *delta;   // [kEbKc x 32] scratch: real-space queues and k-space trial records, then
                      // the Gram and reciprocal-base partials, then the commit's axis tables
     float2 *Mdf;     // [3] surface dipole M (df)
+    // cluster only (written by the other CTAs into the leader's copy): per
+    // rank its Gram sums [C][kEbGramN] and reciprocal bases [C][32], per trial
+    // and part the real-space partial sums [32][parts]
+    float *xgram;
+    float2 *xkbase;
+    float2 *xreal;
 };
 
-__host__ __device__ inline size_t eb_layout(int N, int K, int ncell, bool cells, size_t off[16]) {
+// Shared memory of one CTA holding Kl k-vectors, in a cluster of C CTAs.
+__host__ __device__ inline size_t eb_layout(int N, int Kl, int ncell, bool cells, int C, size_t off[19]) {
     size_t b = 256 * 8 + 32 * 8;            // sc_tab, red
-    off[0] = b; b += (size_t)K * 16;        // kvec
-    off[1] = b; b += (size_t)K * 16;        // qfix
-    off[2] = b; b = align16(b + (size_t)K * 4);            // kpack
+    off[0] = b; b += (size_t)Kl * 16;       // kvec
+    off[1] = b; b += (size_t)Kl * 16;       // qfix
+    off[2] = b; b = align16(b + (size_t)Kl * 4);           // kpack
     off[3] = b; if (cells) b = align16(b + (size_t)ncell * 4);   // ccount
     off[4] = b; if (cells) b = align16(b + (size_t)N * 4);       // pcs
     off[5] = b; b = align16(b + sizeof(Move) * kEbTrials);      // mv
@@ -61,14 +70,18 @@ __host__ __device__ inline size_t eb_layout(int N, int K, int ncell, bool cells,
     off[12] = b; b = align16(b + 4 * kEbTrials * kEbTrials);    // G
     off[13] = b; b = align16(b + 8 * kEbKc * kEbTrials);        // delta
     off[14] = b; b = align16(b + 8 * 3);                        // Mdf
-    off[15] = b;
+    const int cx = C > 1 ? C : 0;
+    off[15] = b; b = align16(b + (size_t)4 * kEbGramN * cx);    // xgram
+    off[16] = b; b = align16(b + (size_t)8 * kEbTrials * cx);   // xkbase
+    off[17] = b; b = align16(b + (size_t)8 * kEbTrials * (C > 1 ? (C + 1) / 2 : 0));   // xreal
+    off[18] = b;
     return b;
 }
 
 __device__ inline EbSmem eb_carve(char *base, const SysDesc &d, bool cells) {
-    size_t off[16];
+    size_t off[19];
     const int ncell = d.nc[0] * d.nc[1] * d.nc[2];
-    eb_layout(d.N, d.K, ncell, cells, off);
+    eb_layout(d.N, d.eb_kmax, ncell, cells, d.eb_ctas, off);
     EbSmem s;
     s.b.sc_tab = (float2 *)base;
     s.b.red = (float2 *)(base + 256 * 8);
@@ -92,6 +105,9 @@ __device__ inline EbSmem eb_carve(char *base, const SysDesc &d, bool cells) {
     s.G = (float *)(base + off[12]);
     s.delta = (float2 *)(base + off[13]);
     s.Mdf = (float2 *)(base + off[14]);
+    s.xgram = (float *)(base + off[15]);
+    s.xkbase = (float2 *)(base + off[16]);
+    s.xreal = (float2 *)(base + off[17]);
     return s;
 }
 
@@ -142,7 +158,26 @@ __device__ __forceinline__ void eb_qbar(int nthreads) {
     asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
-// Real-space base of one trial by one warp. Candidates (cell stencil, or all
+// Stores into CTA `rank`'s copy of a shared-memory variable (the cluster's
+// distributed shared memory).
+__device__ __forceinline__ uint32_t eb_remote(const void *p, unsigned rank) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    return ra;
+}
+__device__ __forceinline__ void eb_st_remote(float2 *p, unsigned rank, float2 v) {
+    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(eb_remote(p, rank)), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ void eb_st_remote(float *p, unsigned rank, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(eb_remote(p, rank)), "f"(v) : "memory");
+}
+__device__ __forceinline__ void eb_st_remote(int *p, unsigned rank, int v) {
+    asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(eb_remote(p, rank)), "r"(v) : "memory");
+}
+
+// Real-space base of one trial by one warp (or part `part` of `nparts`: the
+// candidate batches part, part + nparts, ...). Candidates (cell stencil, or all
 // particles) are screened by distance first: only those that may lie within
 // reach2 of the old or the new position (all particles: either distance; cell
 // stencil: the distance to the step's midpoint against reach + |d|/2) enter a
@@ -184,11 +219,11 @@ __device__ __forceinline__ bool eb_in_reach(int4 p, const Move &m, const SysDesc
 
 template <bool CELLS>
 __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, const Smem &s, int4 *qp, int2 *qm,
-                                              float &accf, df &accd) {
+                                              int part, int nparts, float &accf, df &accd) {
     const int lane = threadIdx.x & 31;
     int qn = 0;
     if (!CELLS) {
-        for (int b = 0; b < d.N; b += 32) {   // warp-uniform trip count
+        for (int b = 32 * part; b < d.N; b += 32 * nparts) {   // warp-uniform trip count
             const int j = b + lane;
             const bool v = j < d.N && j != m.i;
             const int4 p = v ? d.pos4[j] : make_int4(0, 0, 0, 0);
@@ -275,7 +310,7 @@ __device__ __forceinline__ void eb_pairs_warp(const Move &m, const SysDesc &d, c
     const float hd = 0.5f * sqrtf(fmaf(m.dxf[0], m.dxf[0], fmaf(m.dxf[1], m.dxf[1], m.dxf[2] * m.dxf[2])));
     const float rm = sqrtf(reach2m) + hd + 1e-3f, rm2 = rm * rm;
     int c = 0;   // warp-uniform: the cell holding candidate b
-    for (int b = 0; b < total; b += 32) {
+    for (int b = 32 * part; b < total; b += 32 * nparts) {
         // the first stencil cell whose slots reach past b
         while (true) {
             const int e = (c < 32 ? __shfl_sync(0xffffffffu, st0, c) + __shfl_sync(0xffffffffu, cntv[0], c)
@@ -508,7 +543,10 @@ __device__ __noinline__ bool eb_rebuild(const SysDesc &d, const EbSmem &s, df &c
 // the trials does not matter. The axis tables of the accepted trials'
 // new and old positions sit in the increment buffer as float4
 // {new.re, new.im, old.re, old.im}, trial-major (tab[g * T + t]).
-__device__ __noinline__ void eb_commit_qk(const SysDesc &d, const EbSmem &s, uint32_t live, int qt, int nq) {
+// On a cluster the CTA takes its own items [i0, i1), whose k-vectors it holds
+// from k0 on (shared-memory index = k - k0).
+__device__ __noinline__ void eb_commit_qk(const SysDesc &d, const EbSmem &s, uint32_t live, int qt, int nq, int i0,
+                                          int i1, int k0) {
     int *alist = reinterpret_cast<int *>(s.corr);   // free after the resolution
     float *qg = s.G;                                // [32], free after the resolution
     if (qt < kEbTrials && ((live >> qt) & 1u)) {
@@ -532,9 +570,9 @@ __device__ __noinline__ void eb_commit_qk(const SysDesc &d, const EbSmem &s, uin
             tab[e] = make_float4(en.x, en.y, eo.x, eo.y);
         }
         eb_qbar(nq);
-        for (int r = qt; r < d.n_rb_items; r += nq) {
+        for (int r = i0 + qt; r < i1; r += nq) {
             const int4 it = d.rb_items[r];
-            const int kp0 = it.x & 0xFFFFFF, len = it.x >> 24, kn0 = it.y & 0xFFFFFF, n0 = it.y >> 24;
+            const int kp0 = (it.x & 0xFFFFFF) - k0, len = it.x >> 24, kn0 = (it.y & 0xFFFFFF) - k0, n0 = it.y >> 24;
             const int ix = (int)(int8_t)(it.z & 0xFF), iy = 2 * kcc + 1 + (int)(int8_t)((it.z >> 8) & 0xFF);
             const int iz = 3 * kcc + 2 + n0;
             unsigned da[kRbLen], dr[kRbLen], db[kRbLen], dc[kRbLen];
@@ -629,6 +667,14 @@ __device__ __forceinline__ void eb_cell_move(const Move &m, const SysDesc &d, co
     s.pcs[m.i] = ((uint32_t)m.cn << 12) | (uint32_t)ns;
 }
 
+// The cell counts alone of eb_cell_move: the other CTAs of a cluster keep
+// their own copy for their stencil walks.
+__device__ __forceinline__ void eb_cell_count_move(const Move &m, const SysDesc &d, const Smem &s) {
+    s.ccount[m.co] -= 1;
+    const int ns = s.ccount[m.cn];
+    if (ns < d.cap) s.ccount[m.cn] = ns + 1;
+}
+
 // Surface dipole change of a trial (Angstrom e), as surface_delta computes it.
 __device__ __forceinline__ void eb_dM(const Move &m, const SysDesc &d, float dM[3]) {
     const float qe = m.q * d.eff[m.ti];
@@ -636,32 +682,56 @@ __device__ __forceinline__ void eb_dM(const Move &m, const SysDesc &d, float dM[
     for (int a = 0; a < 3; a++) dM[a] = qe * ((float)m.hn[a] * d.s32[a] - (float)m.ho[a] * d.s32[a]);
 }
 
-template <bool CELLS>
+// CLUSTER: one system on a thread-block cluster of C = eb_ctas CTAs (a
+// system alone, where one CTA would leave the other SMs idle). CTA r holds
+// the k-vectors [k0, k1) and their Q(k) (eb_ranges[r]) and runs the k-steps of
+// its own k-vectors, a 1/C share of the correction pairs and the real-space
+// walks of its warps (trial m in C/2 parts over the cluster's 16 C warps);
+// its partial sums go into CTA 0's shared memory (remote stores), and after a
+// cluster barrier CTA 0 alone completes the sums and resolves the block, and
+// hands the outcome to every CTA. Then CTA 0 writes the positions and cell
+// lists to global memory, every CTA updates its own Q(k) and cell counts, and
+// a cluster barrier makes the new positions visible to the whole cluster
+// before the next block reads them. A rebuild ends the launch (the rebuild
+// kernel takes it, as for any system alone). The sums run in another order
+// than on one CTA, so the dU agree to rounding, not bit for bit.
+template <bool CELLS, bool CLUSTER>
 __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDesc *__restrict__ descs, int64_t end,
                                                                     const float2 *__restrict__ sc_tab) {
     extern __shared__ __align__(16) char eb_smem_raw[];
     __shared__ __align__(16) SysDesc sd;
-    load_desc(sd, descs + blockIdx.x);
+    const int C = CLUSTER ? (int)blk_cluster_size() : 1;
+    const int rank = CLUSTER ? (int)blk_cluster_rank() : 0;
+    load_desc(sd, descs + (CLUSTER ? blockIdx.x / C : blockIdx.x));
     const SysDesc &d = sd;
     EbSmem s = eb_carve(eb_smem_raw, d, CELLS);
     SysScalars *sc = d.sc;
     // the work split (16 threads per trial, two Gram k-steps per warp) is
-    // written for exactly kEbThreads threads
-    if (blockDim.x != kEbThreads) {
+    // written for exactly kEbThreads threads; a cluster must match the
+    // system's k-vector split (the same for every CTA of the cluster)
+    if (blockDim.x != kEbThreads || (CLUSTER ? C != d.eb_ctas || C > kEbMaxCluster : d.eb_ctas != 1)) {
         if (threadIdx.x == 0) atomicOr(&sc->error, kErrLaunch);
         return;
     }
     if (sc->rebuild_pending || sc->cursor >= min(end, sc->n_trials)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-    const int K = d.K;
+    // this CTA's k-vectors [k0, k0 + K) and rebuild items [i0, i1)
+    int k0 = 0, K = d.K, i0 = 0, i1 = d.n_rb_items;
+    if (CLUSTER) {
+        const int4 rg = d.eb_ranges[rank];
+        k0 = rg.x;
+        K = rg.y - rg.x;
+        i0 = rg.z;
+        i1 = rg.w;
+    }
     // tables
     for (int t = tid; t < 256; t += blockDim.x) s.b.sc_tab[t] = sc_tab[t];
     for (int k = tid; k < K; k += blockDim.x) {
-        const longlong2 q = d.qfix[k];
+        const longlong2 q = d.qfix[k0 + k];
         const float2 qf = q_to_float(q);
-        const float A = d.kvec[k].w;
+        const float A = d.kvec[k0 + k].w;
         s.b.kvec[k] = make_float4(A, qf.x, qf.y, sqrtf(A));
-        s.b.kpack[k] = d.kpack[k];
+        s.b.kpack[k] = d.kpack[k0 + k];
         s.b.qfix[k] = q;
     }
     // 2 pi / L per axis: k.d = sum_a n_a (2 pi / L_a) d_a
@@ -673,7 +743,8 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             s.b.pcs[j] = ((uint32_t)d.p_cell[j] << 12) | (uint32_t)d.p_slot[j];
     }
     if (tid < 3) s.Mdf[tid] = make_float2(sc->m[tid][0], sc->m[tid][1]);
-    __syncthreads();
+    if (CLUSTER) blk_cluster_barrier();   // every CTA of the cluster runs before any remote store
+    else __syncthreads();
     int64_t cur = sc->cursor;
     const int64_t stop = min(end, sc->n_trials);
     df U = {sc->u_hi, sc->u_lo};
@@ -739,8 +810,11 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
         // its k-steps back to back, with no barrier between them (a warp
         // done walking early starts on k space)
         __syncthreads();
-        // ---- real-space and surface corrections c(a, m), a < m
-        for (int e = tid; e < kEbTrials * kEbTrials; e += blockDim.x) {
+        // ---- real-space and surface corrections c(a, m), a < m (cluster: a
+        // 1/C share per CTA, into CTA 0's table)
+        const int e_lo = CLUSTER ? rank * (kEbTrials * kEbTrials / C) : 0;
+        const int e_hi = CLUSTER ? e_lo + kEbTrials * kEbTrials / C : kEbTrials * kEbTrials;
+        for (int e = e_lo + tid; e < e_hi; e += blockDim.x) {
             const int a = e / kEbTrials, m = e - a * kEbTrials;
             float2 out = make_float2(0.0f, 0.0f);
             if (a < m && m < kb && s.mv[a].i != s.mv[m].i) {
@@ -759,19 +833,30 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                 }
                 out = make_float2(c.hi, c.lo);
             }
-            s.corr[e] = out;
+            if (CLUSTER) eb_st_remote(&s.corr[e], 0, out);
+            else s.corr[e] = out;
         }
         // ---- real-space base: warp w sums trials w, w + nwarp, ...; its
-        // candidate queue lives in the (not yet used) increment buffer
-        for (int m = warp; m < kb; m += nwarp) {
-            const Move mv = s.mv[m];
-            float accf = 0.0f;
-            df accd = {0.0f, 0.0f};
-            int4 *qp = reinterpret_cast<int4 *>(s.delta) + warp * 48;
-            int2 *qm = reinterpret_cast<int2 *>(qp + 32);
-            eb_pairs_warp<CELLS>(mv, d, s.b, qp, qm, accf, accd);
-            const df p = warp_sum_df(df_add_f(accd, accf));
-            if (lane == 0) s.partR[m] = make_float2(p.hi, p.lo);
+        // candidate queue lives in the (not yet used) increment buffer. On a
+        // cluster warp g = 16 r + w of the cluster takes part g % P of trial
+        // g / P (P = C / 2 parts per trial), into CTA 0's part table.
+        {
+            const int P = CLUSTER ? (C + 1) / 2 : 1;
+            const int u0 = CLUSTER ? rank * nwarp + warp : warp, du = CLUSTER ? C * nwarp : nwarp;
+            for (int u = u0; u < kb * P; u += du) {
+                const int m = u / P, part = u - m * P;
+                const Move mv = s.mv[m];
+                float accf = 0.0f;
+                df accd = {0.0f, 0.0f};
+                int4 *qp = reinterpret_cast<int4 *>(s.delta) + warp * 48;
+                int2 *qm = reinterpret_cast<int2 *>(qp + 32);
+                eb_pairs_warp<CELLS>(mv, d, s.b, qp, qm, part, P, accf, accd);
+                const df p = warp_sum_df(df_add_f(accd, accf));
+                if (lane == 0) {
+                    if (CLUSTER) eb_st_remote(&s.xreal[m * P + part], 0, make_float2(p.hi, p.lo));
+                    else s.partR[m] = make_float2(p.hi, p.lo);
+                }
+            }
         }
         // ---- reciprocal base and Gram matrix. Lane (gq, gt) and its partner
         // lane ^ 1 need the same increments sqrt(A') D[trial][k] (trials
@@ -851,7 +936,8 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                 for (int w = 0; w < nw; w++)
                     for (int g2 = 0; g2 < 2; g2++)
                         v = df_add_f(v, KP[(w * 32 + tq * 4 + (tr >> 1) + 2 * g2) * 2 + (tr & 1)]);
-                s.kbase[tid] = make_float2(v.hi, v.lo);
+                if (CLUSTER) eb_st_remote(&s.xkbase[rank * kEbTrials + tid], 0, make_float2(v.hi, v.lo));
+                else s.kbase[tid] = make_float2(v.hi, v.lo);
             }
             __syncthreads();
             if (warp >= nw / 2) {
@@ -867,9 +953,13 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             }
             __syncthreads();
             // element e = (tile, lane, j) of the accumulator layout
-            for (int e = tid; e < 6 * 32 * 4; e += blockDim.x) {
+            for (int e = tid; e < kEbGramN; e += blockDim.x) {
                 float v = 0.0f;
-                for (int sl = 0; sl < nw / 2; sl++) v += P[sl * (6 * 32 * 4) + e];
+                for (int sl = 0; sl < nw / 2; sl++) v += P[sl * kEbGramN + e];
+                if (CLUSTER) {   // CTA 0 adds the ranks' sums up below
+                    eb_st_remote(&s.xgram[rank * kEbGramN + e], 0, v);
+                    continue;
+                }
                 const int x = e >> 7, ln = (e >> 2) & 31, j = e & 3;
                 const int mi = x < 4 ? 0 : 1, nj = x < 4 ? x : x - 2;
                 const int row = 16 * mi + (ln >> 2) + ((j & 2) ? 8 : 0);
@@ -880,9 +970,41 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                 s.corr[row * kEbTrials + col] = make_float2(cs.hi, cs.lo);
             }
         }
+        if (CLUSTER) {
+            // every CTA's partial sums are in CTA 0: it completes them in a
+            // fixed order (ranks, parts)
+            blk_cluster_barrier();
+            if (rank == 0) {
+                for (int e = tid; e < kEbGramN; e += blockDim.x) {
+                    float v = 0.0f;
+                    for (int r = 0; r < C; r++) v += s.xgram[r * kEbGramN + e];
+                    const int x = e >> 7, ln = (e >> 2) & 31, j = e & 3;
+                    const int mi = x < 4 ? 0 : 1, nj = x < 4 ? x : x - 2;
+                    const int row = 16 * mi + (ln >> 2) + ((j & 2) ? 8 : 0);
+                    const int col = 8 * nj + 2 * (ln & 3) + (j & 1);
+                    const float2 c = s.corr[row * kEbTrials + col];
+                    const df cs = df_add_f(df{c.x, c.y}, 2.0f * v);
+                    s.corr[row * kEbTrials + col] = make_float2(cs.hi, cs.lo);
+                }
+                if (tid < kEbTrials) {
+                    const int P = (C + 1) / 2;
+                    df kv = {0.0f, 0.0f}, rv = {0.0f, 0.0f};
+                    for (int r = 0; r < C; r++) {
+                        const float2 x = s.xkbase[r * kEbTrials + tid];
+                        kv = df_add(kv, df{x.x, x.y});
+                    }
+                    for (int p = 0; p < P; p++) {
+                        const float2 x = s.xreal[tid * P + p];
+                        rv = df_add(rv, df{x.x, x.y});
+                    }
+                    s.kbase[tid] = make_float2(kv.hi, kv.lo);
+                    s.partR[tid] = make_float2(rv.hi, rv.lo);
+                }
+            }
+        }
         __syncthreads();
-        // ---- resolve the block in order (warp 0; lane m = trial m)
-        if (warp == 0) {
+        // ---- resolve the block in order (warp 0 of CTA 0; lane m = trial m)
+        if (warp == 0 && rank == 0) {
             df S = {0.0f, 0.0f};
             float dMl[3] = {0.0f, 0.0f, 0.0f};
             if (lane < kb) {
@@ -945,8 +1067,15 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
                 s.info[2] = rebuild ? 1 : 0;
                 s.info[3] = cnt_acc;
             }
+            if (CLUSTER && lane > 0 && lane < C) {   // the outcome, to the other CTAs
+                eb_st_remote(&s.info[0], lane, done);
+                eb_st_remote(&s.info[1], lane, (int)accm);
+                eb_st_remote(&s.info[2], lane, rebuild ? 1 : 0);
+                eb_st_remote(&s.info[3], lane, cnt_acc);
+            }
         }
-        __syncthreads();
+        if (CLUSTER) blk_cluster_barrier();
+        else __syncthreads();
         const int done = s.info[0];
         const uint32_t accm = (uint32_t)s.info[1];
         rebuild = s.info[2] != 0;
@@ -955,8 +1084,13 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
         // cell lists while warps 1.. update Q(k), synchronising among
         // themselves on named barrier 1; the block barrier below joins the two.
         const uint32_t live = accm & ((done >= 32) ? 0xffffffffu : ((1u << done) - 1u));
-        if (warp == 0) {
-            // positions (and, for a particle that stays in its cell, its
+        if (warp == 0 && rank != 0) {
+            // the other CTAs of a cluster: their cell counts alone
+            if (CELLS && lane == 0)
+                for (int a = 0; a < done; a++)
+                    if (((accm >> a) & 1u) && s.mv[a].cn != s.mv[a].co) eb_cell_count_move(s.mv[a], d, s.b);
+        } else if (warp == 0) {
+            // positions (and, for a particle that stays in its
             // cell record) of the accepted trials, one lane each: the
             // particles are distinct; then lane 0 moves, in order, the
             // particles that changed cells
@@ -986,9 +1120,15 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             // Q(k) += sum over accepted trials of c_k(new) - c_k(old), over
             // the rebuild's items (eb_commit_qk): each thread owns items of
             // (+n, -n) k-vector pairs and adds every accepted trial's change
-            eb_commit_qk(d, s, live, tid - 32, blockDim.x - 32);
+            eb_commit_qk(d, s, live, tid - 32, blockDim.x - 32, i0, i1, k0);
         }
         cur += done;
+        if (CLUSTER) {
+            // CTA 0's positions and cell lists are visible to the cluster
+            blk_cluster_barrier();
+            if (rebuild) break;   // the rebuild kernel takes it (rebuild_pending)
+            continue;
+        }
         __syncthreads();
         if (rebuild && !d.rebuild_in_kernel) break;   // the rebuild kernel takes it (rebuild_pending)
         if (rebuild) {
@@ -1003,9 +1143,15 @@ __global__ void __launch_bounds__(kEbThreads, 1) ewald_block_kernel(const SysDes
             rebuild = false;
         }
     }
-    // write back Q(k), cells and the scalars
-    store_back(d, s.b, true, CELLS);
-    if (tid == 0) {
+    // write back Q(k), cells and the scalars (a cluster: every CTA its own
+    // Q(k), CTA 0 the rest)
+    if (CLUSTER) {
+        for (int k = tid; k < K; k += blockDim.x) d.qfix[k0 + k] = s.b.qfix[k];
+        if (rank == 0) store_back(d, s.b, false, CELLS);
+    } else {
+        store_back(d, s.b, true, CELLS);
+    }
+    if (tid == 0 && rank == 0) {
         sc->cursor = cur;
         sc->u_hi = U.hi;
         sc->u_lo = U.lo;

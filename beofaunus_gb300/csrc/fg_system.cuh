@@ -133,6 +133,13 @@ struct alignas(16) SysDesc {
     int32_t n_rb_items;      // in-kernel rebuild of the block kernel: k-vector pairs (+n, -n) per item
     const int4 *rb_items;    // {kp0 | len << 24, kn0 | n0 << 24, nx & 0xFF | (ny & 0xFF) << 8, 0}
     float reach2;            // no pair term acts beyond r^2 = reach2 (cutoff, WCA range, core)
+    // Ewald block kernel on a thread-block cluster (a system alone): CTA rank r
+    // holds the k-vectors [k0, k1) and owns rb_items [i0, i1), eb_ranges[r] =
+    // {k0, k1, i0, i1}; eb_kmax = the most k-vectors one CTA holds. One CTA:
+    // eb_ctas = 1, eb_ranges[0] = {0, K, 0, n_rb_items}, eb_kmax = K.
+    int32_t eb_ctas;
+    int32_t eb_kmax;
+    const int4 *eb_ranges;
 };
 
 }  // namespace fg

@@ -77,11 +77,13 @@ int fg_autotune(fg_system *h, int64_t n_trials, fg_tune_report *report) {
     if (n_trials < 32) return fail(FG_ERR_INVALID, "n_trials must be >= 32");
     if (report) *report = fg_tune_report{};
     const bool dh = dh_block_ok(h);
-    if (!dh && h->model == FG_MODEL_EWALD_WCA && h->K > 0 && ewald_block_ok(h)) return FG_OK;
+    const bool eb = !dh && h->model == FG_MODEL_EWALD_WCA && h->K > 0 && ewald_block_ok(h);
     std::vector<int> cand;
     if (dh) {
         for (int C = 1; C <= dh_block_max_cluster(); C *= 2)
             if (C == 1 || h->N / C >= 64) cand.push_back(C);
+    } else if (eb) {
+        for (int C = 1; C <= eb_cluster_max(h); C *= 2) cand.push_back(C);
     } else {
         for (int T = 128; T <= fg::kSweepThreads; T *= 2) cand.push_back(T);
     }
@@ -91,6 +93,7 @@ int fg_autotune(fg_system *h, int64_t n_trials, fg_tune_report *report) {
     std::vector<std::pair<int, double>> t;
     for (int v : cand) {
         if (dh) c->ctas = v;
+        else if (eb) c->eb_ctas = v;
         else c->threads = v;
         double us = 0;
         rc = time_system(c, n_trials, 0x7e57u + (uint32_t)v, &us);
@@ -106,6 +109,8 @@ int fg_autotune(fg_system *h, int64_t n_trials, fg_tune_report *report) {
         h->ctas = t[best].first;
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune_dh_ctas[size_class(h->N)] = t[best].first;
+    } else if (eb) {
+        h->eb_ctas = t[best].first;
     } else {
         h->threads = t[best].first;
     }

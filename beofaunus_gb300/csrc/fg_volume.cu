@@ -157,6 +157,7 @@ int volume_move_rebuilt(fg_system *h, double Vn, double f, double pressure, doub
     if (rc) return drop(rc);
     t->threads = h->threads;
     t->ctas = h->ctas;
+    t->eb_ctas = h->eb_ctas;
     t->cnt_accepted_host = cnt;
     if (h->desc.skip_rebuild) {
         rc = fg_set_rebuild_policy(t, 1);

@@ -68,6 +68,8 @@ def lib(build_if_missing=True):
             "fg_synchronize": ([vp], ctypes.c_int),
             "fg_set_threads": ([vp, i32], ctypes.c_int),
             "fg_get_threads": ([vp], ctypes.c_int),
+            "fg_set_cluster": ([vp, i32], ctypes.c_int),
+            "fg_get_cluster": ([vp, dp, dp], ctypes.c_int),
             "fg_philox4x32_10": ([dp, dp, dp], None),
             "fg_set_rebuild_policy": ([vp, i32], ctypes.c_int),
             "fg_running_energy": ([vp, dp], ctypes.c_int),
@@ -333,6 +335,24 @@ class System:
     @threads.setter
     def threads(self, t):
         _check(lib().fg_set_threads(self.h, int(t)))
+
+    @property
+    def cluster(self):
+        """CTAs of the thread-block cluster an Ewald system run alone sweeps
+        on (fg_set_cluster / fg_get_cluster; 0 sets the built-in choice)."""
+        c = np.zeros(2, np.int32)
+        _check(lib().fg_get_cluster(self.h, _p(c[:1]), _p(c[1:])))
+        return int(c[0])
+
+    @cluster.setter
+    def cluster(self, c):
+        _check(lib().fg_set_cluster(self.h, int(c)))
+
+    @property
+    def max_cluster(self):
+        c = np.zeros(2, np.int32)
+        _check(lib().fg_get_cluster(self.h, _p(c[:1]), _p(c[1:])))
+        return int(c[1])
 
     def autotune(self, n_trials=2048):
         """Time candidate launch shapes on a clone (fg_autotune) and apply the

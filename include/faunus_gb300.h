@@ -131,6 +131,18 @@ int fg_synchronize(fg_system *h);
 int fg_set_threads(fg_system *h, int32_t threads);
 int fg_get_threads(fg_system *h);
 
+/* Ewald systems run alone (fg_stream_run, fg_sweep): CTAs of the
+ * thread-block cluster that runs the block-of-trials sweep (1, 2, 4, 8 or 16;
+ * 0 = the built-in choice: the most CTAs with at least 128 k-vectors each).
+ * The k-vectors are split over the CTAs; the
+ * size in effect is capped by what the device co-schedules and what fits in
+ * shared memory. Batches run one CTA per system. Replaces nothing of the
+ * reference (NonbondedEwald, ewald.h:269-715, runs on one host thread); a
+ * launch-shape setting like fg_set_threads. */
+int fg_set_cluster(fg_system *h, int32_t ctas);
+/* The size in effect (ctas) and the largest that fits (max_ctas). */
+int fg_get_cluster(fg_system *h, int32_t *ctas, int32_t *max_ctas);
+
 /* One Philox4x32-10 block, host side (for tests of the generator). */
 void fg_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
@@ -430,7 +442,8 @@ typedef struct {
 } fg_tune_report;
 
 /* DH+LJ block sweeps: CTAs per system (cluster size, powers of two); Ewald
- * one-trial sweeps: threads per CTA. n_trials >= 32 per candidate. */
+ * block sweeps: CTAs of the cluster a system alone runs on (fg_set_cluster);
+ * Ewald one-trial sweeps: threads per CTA. n_trials >= 32 per candidate. */
 int fg_autotune(fg_system *h, int64_t n_trials, fg_tune_report *report);
 /* DH+LJ batches: least particles per CTA when the SMs are shared out among
  * members (128 .. 2048), timed on equal sweeps of the members (n_trials for

@@ -11,12 +11,14 @@ pytestmark = pytest.mark.gpu
 
 def test_batch_equals_individual_runs():
     """Three 800-ion Ewald systems in one launch give bit-identical results
-    to the same systems run one at a time (same streams, same threads)."""
+    to the same systems run one at a time (same streams, same threads, one
+    CTA each as in the batch)."""
     from beofaunus_gb300.gpu import Batch, System
     specs = [workloads.rpm800(seed=s, update_frequency=200) for s in (1, 2, 3)]
     alone = []
     for i, (p, x, q, ids) in enumerate(specs):
         s = System(p, x, q, ids, threads=256)
+        s.cluster = 1
         s.stream_philox(1600, seed=9, stream_id=i)
         st = s.stream_run()
         alone.append((s.positions(), st["accepted"], st["rebuilds"], s.running_energy()))

@@ -54,12 +54,18 @@ def test_dh_system_tuning_keeps_state_and_parity():
         np.testing.assert_allclose(s.positions(), o.positions(), rtol=0, atol=1e-9)
 
 
-def test_ewald_block_kernel_has_nothing_to_tune():
+def test_ewald_block_kernel_tunes_its_cluster():
+    """An Ewald system alone: the candidates are the cluster sizes 1, 2, 4, ...
+    up to what fits; tuning runs on a clone, and the chosen size applies."""
     from beofaunus_gb300.gpu import System
     p, xyz, q, ids = workloads.rpm800(seed=5, update_frequency=200)
     s = System(p, xyz, q, ids)
+    x0 = s.positions()
     rep = s.autotune(256)
-    assert rep["candidates"] == [] and rep["chosen"] is None
+    vals = [v for v, _ in rep["candidates"]]
+    assert vals[0] == 1 and vals[-1] == s.max_cluster and all(b == 2 * a for a, b in zip(vals, vals[1:]))
+    assert rep["chosen"] in vals and s.cluster == rep["chosen"]
+    np.testing.assert_array_equal(s.positions(), x0)
 
 
 def test_batch_tuning_keeps_oracle_parity():
