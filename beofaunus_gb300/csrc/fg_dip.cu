@@ -16,22 +16,26 @@
 //
 // Included by fg_api.cu (one translation unit).
 //
-// Work split. One system per CTA (64 threads by default; fg_dip_autotune
-// times the choices); a launch runs many systems (replicas, independent
-// chains) side by side, several CTAs per SM, with each system's k-vectors,
-// A_k, Q(k) and particle records staged in shared memory for the launch when
-// they fit. A trial is a block-wide pass: thread 0 forms the trial
-// (quaternion rotation of mu or fixed-point translation; the next trial's
-// record is already loaded), the threads build the moved particle's per-axis
-// phase tables e^{2 pi i n x_a / L_a}, n = 0..kcc, old and new (one sincospi
-// each, from the exact 64-bit phase n X mod 2^64) and their (n_y, n_z)
-// products; then the pair loop and the k loop: far pairs are summed where
+// Work split. One system per CTA (128 threads by default, compiled for at
+// most 128 registers so that four systems, sixteen warps, share an SM;
+// fg_dip_autotune times the choices); a launch runs many systems (replicas,
+// independent chains) side by side, with each system's k-vectors, A_k, Q(k)
+// and particle records staged in shared memory for the launch when they fit.
+// A trial is a block-wide pass: lanes 0..2 of warp 0 form the trial, one axis
+// each (the quaternion rotation of mu or the fixed-point translation; the
+// next trial's record is already loaded), the threads build the moved
+// particle's per-axis phase tables e^{2 pi i n x_a / L_a}, n = 0..kcc, old and
+// new (axis_entry_df: the exact 64-bit phase n X mod 2^64 split into a table
+// angle and a short Taylor series, in df) and the (n_y, n_z) products the
+// k-vectors use; then the pair loop and the k loop: far pairs are summed where
 // they are found, near pairs are queued per warp in order and evaluated
-// afterwards by consecutive threads; a k-vector's phase is one product of a
-// table entry with an (n_y, n_z) entry. The block reduces in a fixed order,
-// thread 0 decides, and on acceptance the threads that computed a k-vector's
-// Q increments add them to Q(k). A rotation keeps the position: one phase per
-// k-vector and only the pair terms linear in the moved dipole.
+// afterwards by consecutive threads, a translation's old and new position on
+// two threads; a k-vector's phase is one product of a table entry with an
+// (n_y, n_z) entry. The block reduces in a fixed order, thread 0 decides, and
+// on acceptance the threads that computed a k-vector's Q increments add them
+// to Q(k). A rotation keeps the position: one phase per k-vector and only the
+// pair terms linear in the moved dipole; a translation keeps the dipole:
+// dQ_dip = i (k.mu) mu_s (e_new - e_old).
 //
 // Precision. The per-trial dU must match the FP64 oracle to 1e-9 kT at Bjerrum
 // lengths of hundreds of Angstrom, where single dipole pairs carry tens of kT.
@@ -41,9 +45,10 @@
 // double-float. The k loop, K terms per trial, runs in double-float (df: an
 // unevaluated sum of two floats, ~48 significant bits) on the FP32 pipe, which
 // on this part issues far more operations per clock than the FP64 pipe: Q(k),
-// its increments, A_k, the phases and k.mu are all df. Phase tables, surface
-// sums and decisions are FP64. Positions are 64-bit fixed point
-// (X = x/L 2^64): minimum image is the wrapped integer difference and every
+// its increments, A_k, the phases and k.mu are all df; its sums take one
+// TwoSum each (qadd), its error budget being absolute per k-vector. Surface
+// sums and decisions are FP64. Positions are 64-bit fixed point (X = x/L
+// 2^64): minimum image is the wrapped integer difference and every
 // translation is exact.
 namespace fgd {
 
@@ -108,6 +113,9 @@ struct DipDesc {
     const double *rtab;
     double ts0, tinv;
     int32_t tn, pad_tab;
+    const float4 *sctab;
+    const int16_t *yzl;   // the (n_y, n_z) table entries some k-vector uses ((n_y + kcc) W + n_z + kcc)
+    int32_t nyz, pad_yz;
     char4 *kn;            // [K] n-vector of k
     double *ak;           // [K] A_k with the half-space factor
     double2 *qi, *qd;     // [K] FP64 accumulators of a rebuild
@@ -164,12 +172,35 @@ __device__ __forceinline__ dc dc_mul(dc a, dc b) {
     return {dsub(dmul(a.re, b.re), dmul(a.im, b.im)), dadd(dmul(a.re, b.im), dmul(a.im, b.re))};
 }
 __device__ __forceinline__ dc dc_conj_if(dc a, bool c) { return c ? dc{a.re, dneg(a.im)} : a; }
-// Re(a conj(b)) and Re(a b)
-__device__ __forceinline__ df dc_dot(dc a, dc b) { return dadd(dmul(a.re, b.re), dmul(a.im, b.im)); }
-__device__ __forceinline__ df dc_rprod(dc a, dc b) { return dsub(dmul(a.re, b.re), dmul(a.im, b.im)); }
-// n . m for a small integer vector n and df m
-__device__ __forceinline__ df dkdot(char4 n, const df *m) {
-    return dadd(dadd(dmul_i(m[0], n.x), dmul_i(m[1], n.y)), dmul_i(m[2], n.z));
+// The k loop's forms: Re(a conj(b)) (dc_dotq), Re(a b) (dc_rprodq), n . m
+// for a small integer vector n (dkdotq), with sums of one TwoSum each
+// (fg::df_add_quick), whose error (~2^-47 of the larger operand) is of the
+// size of the operands' own rounding; the loop's error budget is absolute
+// (each term against the scale |Q| |dQ| A_k of its k-vector), so the exact
+// renormalisation of dadd buys nothing there.
+__device__ __forceinline__ df qadd(df a, df b) { return fg::df_add_quick(a, b); }
+__device__ __forceinline__ df qsub(df a, df b) { return fg::df_add_quick(a, dneg(b)); }
+// a * b left as the rounded product of the high words and its error (not
+// renormalised): only as an operand of qadd/qsub, whose TwoSum of the high
+// parts is exact for any pair of floats
+__device__ __forceinline__ df dmul_u(df a, df b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    return {p, __fmaf_rn(a.lo, b.hi, e)};
+}
+__device__ __forceinline__ df dmul_iu(df a, int n) {
+    const float f = (float)n;
+    const float p = __fmul_rn(a.hi, f);
+    return {p, __fmaf_rn(a.lo, f, __fmaf_rn(a.hi, f, -p))};
+}
+__device__ __forceinline__ dc dc_mulq(dc a, dc b) {
+    return {qsub(dmul_u(a.re, b.re), dmul_u(a.im, b.im)), qadd(dmul_u(a.re, b.im), dmul_u(a.im, b.re))};
+}
+__device__ __forceinline__ df dc_dotq(dc a, dc b) { return qadd(dmul_u(a.re, b.re), dmul_u(a.im, b.im)); }
+__device__ __forceinline__ df dc_rprodq(dc a, dc b) { return qsub(dmul_u(a.re, b.re), dmul_u(a.im, b.im)); }
+__device__ __forceinline__ df dkdotq(char4 n, const df *m) {
+    return qadd(qadd(dmul_iu(m[0], n.x), dmul_iu(m[1], n.y)), dmul_iu(m[2], n.z));
 }
 
 // e^{i k.r} from one particle's axis tables (tab[axis * (kcc+1) + |n|]);
@@ -256,7 +287,7 @@ __device__ __forceinline__ void radial(const DipDesc &d, double s, double &A, do
         k = k < d.tn - 1 ? k : d.tn - 1;
         const double t = u - (double)k;
         const double *c = d.rtab + 18 * k;
-        A = horner6(c, t);
+        A = (d.quirk || d.ii) ? horner6(c, t) : 0.0;   // the ion-ion function only where a term uses it
         B = horner6(c + 6, t);
         C = horner6(c + 12, t);
         return;
@@ -281,7 +312,13 @@ __device__ __forceinline__ void dip_pair(const DipDesc &d, double rx, double ry,
                                          const double *mb, double &real, double &lj) {
     const double r2 = rx * rx + ry * ry + rz * rz;
     const int tt = ta * d.nt + tb;
-    double x = d.s2[tt] / r2;   // LennardJonesMixed (potentials.h:2036-2040)
+    // LennardJonesMixed (potentials.h:2036-2040): s2 / r2 through 1 / r2 from
+    // its float value and two Newton steps (relative error ~1e-16, against
+    // the ~20 FP64 operations of a correctly rounded division)
+    double ir2 = (double)__frcp_rn((float)r2);
+    ir2 = ir2 * fma(-r2, ir2, 2.0);
+    ir2 = ir2 * fma(-r2, ir2, 2.0);
+    double x = d.s2[tt] * ir2;
     x = x * x * x;
     lj = d.eps4[tt] * (x * x - x);
     real = 0.0;
@@ -380,6 +417,27 @@ __device__ __forceinline__ double dip_turn(const DipDesc &d, double rx, double r
     return d.lB * Ed;
 }
 
+__device__ __forceinline__ df dsqr(df a) { return dmul(a, a); }
+// cos, sin of 2 pi n X / 2^64 as df without the FP64 pipe: the phase reduced
+// exactly in integers to the nearest of kDipScTab table angles plus a rest
+// |theta| <= pi / kDipScTab, whose sine and cosine come from their Taylor
+// series (sin: theta - theta^3/6 + theta^5/120, the last two in FP32; cos:
+// 1 - theta^2/2 in df + theta^4/24), rotated by the table entry.
+constexpr int kDipScTab = 1024;
+__device__ __forceinline__ float4 axis_entry_df(int n, int64_t X, const float4 *__restrict__ tab) {
+    const uint64_t ph = (uint64_t)(int64_t)n * (uint64_t)X;
+    const uint32_t idx = (uint32_t)((ph + (1ull << 53)) >> 54);   // mod 2^64: 0 .. kDipScTab - 1
+    const int64_t rem = (int64_t)(ph - ((uint64_t)idx << 54));    // |rem| <= 2^53
+    const float h = (float)rem, l = (float)(rem - (int64_t)h);
+    const df th = dmul(df{h, l}, df{0x1.921fb6p-62f, -0x1.777a5cp-87f});   // 2 pi / 2^64 as df
+    const float t2f = th.hi * th.hi;
+    const df sn = fg::df_add_f(th, th.hi * t2f * __fmaf_rn(t2f, 1.0f / 120.0f, -1.0f / 6.0f));
+    const df t2 = dsqr(th);
+    const df cs = fg::df_add_f(dsub(df{1.0f, 0.0f}, df{0.5f * t2.hi, 0.5f * t2.lo}), t2f * t2f * (1.0f / 24.0f));
+    const float4 e = __ldg(tab + (idx & (kDipScTab - 1)));
+    return dc_pack(dc_mul(dc{{e.x, e.y}, {e.z, e.w}}, dc{cs, sn}));
+}
+
 // Block sum in a fixed order (result valid in thread 0).
 __device__ __forceinline__ double block_sum(double v, double *red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -415,7 +473,7 @@ struct DipShared {
     double ro[3], rn[3];
     double qa, qeff, mas, thr, du;
     double M[6];
-    int idx, ta, accept, rebuild, fixed;
+    int idx, ta, accept, rebuild, fixed, same_mu;
     int qcnt[kDipMaxThreads / 32];
     double red[kDipMaxThreads / 32];
     float4 tab[2][3 * (kDipMaxKcc + 1)];    // moved particle, old and new (df complex)
@@ -487,14 +545,19 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_build_kernel(const DipD
 // mode 0: run the staged stream [cursor, n_trials) with Metropolis decisions;
 // mode 1: evaluate trials[0] (explicit) and keep it pending;
 // mode 2: apply the pending trials[0] as accepted.
-__global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipDesc *descs, int mode, int stage) {
+// MAXT: the launch bound. 128 threads per system at most 128 registers
+// (four systems, sixteen warps on an SM) or up to kDipMaxThreads at one CTA
+// per SM.
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, MAXT <= 128 ? 4 : 1) dip_sweep_kernel(const DipDesc *__restrict__ descs, int mode,
+                                                                               int stage) {
     const DipDesc &d = descs[blockIdx.x];
     __shared__ DipShared S;
     extern __shared__ __align__(16) unsigned char dsm[];
     float4 *eyz = reinterpret_cast<float4 *>(dsm);   // df complex
     const int tid = threadIdx.x, T = blockDim.x, st = d.kcc + 1;
     const int W = 2 * d.kcc + 1, W2 = W * W;
-    if (T > kDipMaxThreads || (T & 31)) {
+    if (T > MAXT || (T & 31)) {
         if (tid == 0) atomicOr(&d.sc->error, kDipErrLaunch);
         return;
     }
@@ -540,52 +603,58 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
         t0 = d.sc->cursor;
         t1 = d.sc->n_trials;
     }
-    DipTrial nxt;   // thread 0: the next trial's record, loaded one trial ahead
-    if (tid == 0 && t0 < t1) nxt = d.trials[mode == 0 ? t0 : 0];
+    DipTrial nxt;   // lanes 0..2: the next trial's record, loaded one trial ahead
+    if (tid < 3 && t0 < t1) nxt = d.trials[mode == 0 ? t0 : 0];
     for (int64_t t = t0; t < t1; t++) {
-        // ---- the trial (thread 0)
-        if (tid == 0) {
+        // ---- the trial: lane a of warp 0 takes axis a (a < 3), lane 0 the
+        // particle's scalars; a rotation is Eigen's quaternion-vector
+        // product (QuaternionRotate, geometry.cpp:753-766) one component per
+        // lane: uv = 2 v x p, mu' = p + w uv + v x uv
+        if (tid < 32) {
+            const int lane = tid;
             const DipTrial tr = nxt;
-            if (mode == 0 && t + 1 < t1) nxt = d.trials[t + 1];   // in flight during this trial
-            const int i = tr.idx;
-            S.idx = i;
-            S.thr = tr.thr;
-            S.ta = A.type[i];
-            S.qa = A.q[i];
-            S.qeff = A.q[i] * d.eff[S.ta];
-            S.mas = A.mus[i];
-            for (int a = 0; a < 3; a++) {
-                S.po[a] = A.pos[3 * i + a];
-                S.muo[a] = A.mu[3 * i + a];
-                S.pn[a] = S.po[a];
-                S.mun[a] = S.muo[a];
+            if (lane < 3 && mode == 0 && t + 1 < t1) nxt = d.trials[t + 1];   // in flight during this trial
+            const int i = __shfl_sync(0xffffffffu, tr.idx, 0), kind = __shfl_sync(0xffffffffu, tr.kind, 0);
+            const int a = lane < 3 ? lane : 0, a1 = a == 2 ? 0 : a + 1, a2 = a == 0 ? 2 : a - 1;
+            const int64_t po = A.pos[3 * i + a];
+            const double muo = A.mu[3 * i + a];
+            const double p1 = __shfl_sync(0xffffffffu, muo, a1), p2 = __shfl_sync(0xffffffffu, muo, a2);
+            int64_t pn = po;
+            double mun = muo;
+            if (kind == 1) {
+                const double w = tr.q[0], v1 = tr.q[1 + a1], v2 = tr.q[1 + a2];
+                double u = v1 * p2 - v2 * p1;
+                u += u;
+                const double u1 = __shfl_sync(0xffffffffu, u, a1), u2 = __shfl_sync(0xffffffffu, u, a2);
+                mun = muo + w * u + (v1 * u2 - v2 * u1);
+            } else if (kind == 2) {
+                pn = (int64_t)((uint64_t)po + (uint64_t)tr.t[a]);
+            } else if (kind == 3) {
+                pn = tr.t[a];
+                mun = tr.q[1 + a];
             }
-            if (tr.kind == 1) {
-                // Eigen's quaternion-vector product (QuaternionRotate, geometry.cpp:753-766)
-                const double w = tr.q[0], vx = tr.q[1], vy = tr.q[2], vz = tr.q[3];
-                const double px = S.muo[0], py = S.muo[1], pz = S.muo[2];
-                double ux = vy * pz - vz * py, uy = vz * px - vx * pz, uz = vx * py - vy * px;
-                ux += ux;
-                uy += uy;
-                uz += uz;
-                const double cx = vy * uz - vz * uy, cy = vz * ux - vx * uz, cz = vx * uy - vy * ux;
-                S.mun[0] = px + w * ux + cx;
-                S.mun[1] = py + w * uy + cy;
-                S.mun[2] = pz + w * uz + cz;
-            } else if (tr.kind == 2) {
-                for (int a = 0; a < 3; a++) S.pn[a] = (int64_t)((uint64_t)S.po[a] + (uint64_t)tr.t[a]);
-            } else if (tr.kind == 3) {
-                for (int a = 0; a < 3; a++) {
-                    S.pn[a] = tr.t[a];
-                    S.mun[a] = tr.q[1 + a];
+            if (lane < 3) {
+                S.po[a] = po;
+                S.pn[a] = pn;
+                S.muo[a] = muo;
+                S.mun[a] = mun;
+                if (d.surf_c != 0.0) {   // positions in Angstrom for the surface sums only
+                    S.ro[a] = (double)po * d.s64[a];
+                    S.rn[a] = (double)pn * d.s64[a];
                 }
             }
-            if (d.surf_c != 0.0)   // positions in Angstrom for the surface sums only
-                for (int a = 0; a < 3; a++) {
-                    S.ro[a] = (double)S.po[a] * d.s64[a];
-                    S.rn[a] = (double)S.pn[a] * d.s64[a];
-                }
-            S.fixed = (S.pn[0] == S.po[0] && S.pn[1] == S.po[1] && S.pn[2] == S.po[2]) ? 1 : 0;
+            const bool fixed = __all_sync(0xffffffffu, lane >= 3 || pn == po);
+            const bool same_mu = __all_sync(0xffffffffu, lane >= 3 || mun == muo);
+            if (lane == 0) {
+                S.idx = i;
+                S.thr = tr.thr;
+                S.ta = A.type[i];
+                S.qa = A.q[i];
+                S.qeff = A.q[i] * d.eff[S.ta];
+                S.mas = A.mus[i];
+                S.fixed = fixed ? 1 : 0;
+                S.same_mu = same_mu ? 1 : 0;
+            }
         }
         __syncthreads();
         if (mode != 2) {
@@ -595,24 +664,26 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             const int nw = fixed ? 1 : 2;
             for (int e = tid; e < nw * 3 * st; e += T) {
                 const int w = e / (3 * st), r = e - w * 3 * st, a = r / st, n = r - a * st;
-                S.tab[w][r] = dc_pack(dc_split(axis_entry(n, w ? S.pn[a] : S.po[a])));
+                S.tab[w][r] = axis_entry_df(n, w ? S.pn[a] : S.po[a], d.sctab);
             }
-            if (tid < 10) {   // one value per lane
-                if (tid == 9) {
+            const int sl = tid - (T - 32);   // the last warp, beside the axis tables
+            if (sl >= 0 && sl < 10) {   // one value per lane
+                if (sl == 9) {
                     S.qeffd = dsplit(S.qeff);
                 } else {
-                    const int a = tid % 3, w = tid / 3;
+                    const int a = sl % 3, w = sl / 3;
                     const double f = d.tpl[a] * S.mas;
                     const double v = w == 0 ? S.muo[a] : (w == 1 ? S.mun[a] : S.mun[a] - S.muo[a]);
                     (w == 0 ? S.mo : (w == 1 ? S.mn : S.md))[a] = dsplit(v * f);
                 }
             }
             __syncthreads();
-            for (int e = tid; e < nw * W2; e += T) {
-                const int w = e >= W2 ? 1 : 0, r = e - w * W2, ny = r / W - d.kcc, nz = r - (ny + d.kcc) * W - d.kcc;
+            for (int e = tid; e < nw * d.nyz; e += T) {   // the entries the k-vectors use
+                const int w = e >= d.nyz ? 1 : 0, r = __ldg(d.yzl + (e - w * d.nyz));
+                const int ny = r / W - d.kcc, nz = r - (ny + d.kcc) * W - d.kcc;
                 const dc ey = dc_conj_if(dc_load(S.tab[w][st + (ny < 0 ? -ny : ny)]), ny < 0);
                 const dc ez = dc_conj_if(dc_load(S.tab[w][2 * st + (nz < 0 ? -nz : nz)]), nz < 0);
-                eyz[e] = dc_pack(dc_mul(ey, ez));
+                eyz[w * W2 + r] = dc_pack(dc_mulq(ey, ez));
             }
             __syncthreads();
             const int i = S.idx, ta = S.ta;
@@ -664,8 +735,13 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
             __syncthreads();
             int total = 0;
             for (int w = 0; w < (T >> 5); w++) total += S.qcnt[w];
-            for (int e = tid; e < total; e += T) {
-                int w = 0, r = e;
+            // a translation's pair takes two threads, one for the old position
+            // (subtracted) and one for the new
+            const int ne = fixed ? total : 2 * total;
+            for (int e = tid; e < ne; e += T) {
+                const int pi = fixed ? e : (e >> 1);
+                const bool at_new = !fixed && (e & 1);
+                int w = 0, r = pi;
                 while (r >= S.qcnt[w]) {
                     r -= S.qcnt[w];
                     w++;
@@ -678,68 +754,83 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                     mb[a] = A.mu[3 * j + a];
                 }
                 const double qb = A.q[j], mbs = A.mus[j];
-                double ro[3];
-                for (int a = 0; a < 3; a++) ro[a] = (double)(int64_t)((uint64_t)S.po[a] - (uint64_t)pj[a]) * d.s64[a];
+                double rv[3];
+                for (int a = 0; a < 3; a++)
+                    rv[a] = (double)(int64_t)((uint64_t)(at_new ? S.pn[a] : S.po[a]) - (uint64_t)pj[a]) * d.s64[a];
                 if (fixed) {
-                    acc += dip_turn(d, ro[0], ro[1], ro[2], mas, dmu, qb, mbs, mb);
+                    acc += dip_turn(d, rv[0], rv[1], rv[2], mas, dmu, qb, mbs, mb);
                     continue;
                 }
                 const int tb = A.type[j];
-                double rn[3];
-                for (int a = 0; a < 3; a++) rn[a] = (double)(int64_t)((uint64_t)S.pn[a] - (uint64_t)pj[a]) * d.s64[a];
-                double eo, lo, en, ln;
-                dip_pair(d, ro[0], ro[1], ro[2], qa, ta, mas, muo, qb, tb, mbs, mb, eo, lo);
-                dip_pair(d, rn[0], rn[1], rn[2], qa, ta, mas, mun, qb, tb, mbs, mb, en, ln);
-                acc += (en - eo) + (ln - lo);
+                double ev, lv;
+                dip_pair(d, rv[0], rv[1], rv[2], qa, ta, mas, at_new ? mun : muo, qb, tb, mbs, mb, ev, lv);
+                acc += at_new ? ev + lv : -(ev + lv);
             }
             acc += (double)accf.hi + (double)accf.lo;
-            // ---- k space (df): increments of Q_ion and Q_dip and the energy change
+            // ---- k space (df): increments of Q_ion and Q_dip and the energy change.
+            // A translation keeps the dipole (k.mu_new = k.mu_old): dQ_dip =
+            // i (k.mu) mu_s (e_new - e_old), dQ_ion = q eff (e_new - e_old).
             df ek = {0.0f, 0.0f};
             const df qeffd = S.qeffd;
+            const bool same_mu = S.same_mu;
             const df mo[3] = {S.mo[0], S.mo[1], S.mo[2]}, mn[3] = {S.mn[0], S.mn[1], S.mn[2]},
                      md[3] = {S.md[0], S.md[1], S.md[2]};
             for (int k = tid; k < d.K; k += T) {
                 const char4 n = A.kn[k];
                 const int yz = (n.y + d.kcc) * W + n.z + d.kcc;
-                const dc eo = dc_mul(dc_load(S.tab[0][n.x]), dc_load(eyz[yz]));
+                const dc eo = dc_mulq(dc_load(S.tab[0][n.x]), dc_load(eyz[yz]));
                 dc dci = {{0.0f, 0.0f}, {0.0f, 0.0f}}, dcd = dci;
                 if (fixed) {
                     // the dipole turns in place: dQ_dip = i (k.dmu) mu_s e^{ik.r}
                     if (d.dip_q) {
-                        const df kmd = dkdot(n, md);
+                        const df kmd = dkdotq(n, md);
                         dcd = {dneg(dmul(kmd, eo.im)), dmul(kmd, eo.re)};
                     }
                 } else {
-                    const dc en = dc_mul(dc_load(S.tab[1][n.x]), dc_load(eyz[W2 + yz]));
-                    if (d.ion_q) dci = {dmul(qeffd, dsub(en.re, eo.re)), dmul(qeffd, dsub(en.im, eo.im))};
+                    const dc en = dc_mulq(dc_load(S.tab[1][n.x]), dc_load(eyz[W2 + yz]));
+                    const dc de = {qsub(en.re, eo.re), qsub(en.im, eo.im)};
+                    if (d.ion_q) dci = {dmul(qeffd, de.re), dmul(qeffd, de.im)};
                     if (d.dip_q) {
-                        const df kmo = dkdot(n, mo), kmn = dkdot(n, mn);
-                        dcd = {dsub(dmul(kmo, eo.im), dmul(kmn, en.im)), dsub(dmul(kmn, en.re), dmul(kmo, eo.re))};
+                        if (same_mu) {
+                            const df km = dkdotq(n, mo);
+                            dcd = {dneg(dmul(km, de.im)), dmul(km, de.re)};
+                        } else {
+                            const df kmo = dkdotq(n, mo), kmn = dkdotq(n, mn);
+                            dcd = {qsub(dmul(kmo, eo.im), dmul(kmn, en.im)), qsub(dmul(kmn, en.re), dmul(kmo, eo.re))};
+                        }
                     }
                 }
                 df sum = {0.0f, 0.0f};
                 if (d.ii) {
                     const dc Qi = dc_load(A.fqi[k]);
-                    sum = dadd(dtwice(dc_dot(Qi, dci)), dc_dot(dci, dci));
+                    sum = qadd(dtwice(dc_dotq(Qi, dci)), dc_dotq(dci, dci));
                 }
                 if (d.id) {
                     const dc Qi = dc_load(A.fqi[k]), Qd = dc_load(A.fqd[k]);
                     if (d.quirk)
-                        sum = dadd(sum, dtwice(dadd(dadd(dc_rprod(Qi, dcd), dc_rprod(dci, Qd)), dc_rprod(dci, dcd))));
+                        sum = qadd(sum, dtwice(qadd(qadd(dc_rprodq(Qi, dcd), dc_rprodq(dci, Qd)), dc_rprodq(dci, dcd))));
                     else
-                        sum = dadd(sum, dtwice(dadd(dadd(dc_dot(Qi, dcd), dc_dot(dci, Qd)), dc_dot(dci, dcd))));
+                        sum = qadd(sum, dtwice(qadd(qadd(dc_dotq(Qi, dcd), dc_dotq(dci, Qd)), dc_dotq(dci, dcd))));
                 }
                 if (d.dd) {
                     const dc Qd = dc_load(A.fqd[k]);
-                    sum = dadd(sum, dadd(dtwice(dc_dot(Qd, dcd)), dc_dot(dcd, dcd)));
+                    const df t = qadd(dtwice(dc_dotq(Qd, dcd)), dc_dotq(dcd, dcd));
+                    sum = (d.ii || d.id) ? qadd(sum, t) : t;
                 }
                 const float2 a = A.akf[k];
-                ek = dadd(ek, dmul(df{a.x, a.y}, sum));
-                A.dqi[k] = dc_pack(dci);
-                A.dqd[k] = dc_pack(dcd);
+                ek = qadd(ek, dmul_u(df{a.x, a.y}, sum));
+                if (d.ion_q) A.dqi[k] = dc_pack(dci);
+                if (d.dip_q) A.dqd[k] = dc_pack(dcd);
             }
             acc += dval(ek) * d.recip_c;
-            const double sum = block_sum(acc, S.red);
+            // the block sum without its leading barrier: red was last read
+            // before the previous trial's decision barrier
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0) S.red[warp] = acc;
+            __syncthreads();
+            double sum = 0.0;
+            if (tid == 0)
+                for (int w = 0; w < (T >> 5); w++) sum += S.red[w];
             if (tid == 0) {
                 // surface term from the running sums (nothing with tin-foil surroundings)
                 double du = sum;
@@ -781,21 +872,21 @@ __global__ void __launch_bounds__(kDipMaxThreads, 1) dip_sweep_kernel(const DipD
                 A.fqd[k] = dc_pack({dadd(a.re, b.re), dadd(a.im, b.im)});
             }
         }
-        if (tid == 0) {
-            const int i = S.idx;
-            A.pf[i] = make_float4((float)(S.mun[0] * S.mas), (float)(S.mun[1] * S.mas), (float)(S.mun[2] * S.mas),
-                                  (float)S.qa);
+        if (tid < 3) {   // lane a: axis a of the particle and of the sums
+            const int i = S.idx, a = tid;
+            const float pa = (float)(S.mun[a] * S.mas);
+            reinterpret_cast<float *>(&A.pf[i])[a] = pa;
+            A.pos[3 * i + a] = S.pn[a];
+            A.mu[3 * i + a] = S.mun[a];
             if (stage) {
-                d.pf[i] = A.pf[i];
-                for (int a = 0; a < 3; a++) d.pos[3 * i + a] = S.pn[a];
+                reinterpret_cast<float *>(&d.pf[i])[a] = pa;
+                d.pos[3 * i + a] = S.pn[a];
+                d.mu[3 * i + a] = S.mun[a];
             }
-            for (int a = 0; a < 3; a++) {
-                A.pos[3 * i + a] = S.pn[a];
-                A.mu[3 * i + a] = S.mun[a];
-                if (stage) d.mu[3 * i + a] = S.mun[a];
-                if (d.ion_q && d.surf_c != 0.0) S.M[a] += S.qeff * (S.rn[a] - S.ro[a]);
-                if (d.id || d.dd) S.M[3 + a] += S.mas * (S.mun[a] - S.muo[a]);
-            }
+            if (d.ion_q && d.surf_c != 0.0) S.M[a] += S.qeff * (S.rn[a] - S.ro[a]);
+            if (d.id || d.dd) S.M[3 + a] += S.mas * (S.mun[a] - S.muo[a]);
+        }
+        if (tid == 0) {
             sc.n_accepted++;
             sc.usum += S.du;
             sc.utot += S.du;
@@ -865,14 +956,15 @@ struct fg_dipsys {
     fg_params P{};
     int N = 0, K = 0, kcc = 0;
     int device = 0;
-    int threads = 64;   // two warps per system: several systems share an SM
+    int threads = 128;   // four warps per system at <= 128 registers: four systems share an SM
     cudaStream_t stream = nullptr;
     fgd::DipDesc desc{};
     fgd::DipDesc *d_desc = nullptr;
     int64_t *pos = nullptr;
     double *mu = nullptr, *mus = nullptr, *q = nullptr, *ak = nullptr, *pairs = nullptr;
     int32_t *type = nullptr, *nearq = nullptr;
-    float4 *pf = nullptr;
+    float4 *pf = nullptr, *sctab = nullptr;
+    int16_t *yzl = nullptr;
     char4 *kn = nullptr;
     double2 *qi = nullptr, *qd = nullptr;
     float4 *fqi = nullptr, *fqd = nullptr, *dqi = nullptr, *dqd = nullptr;
@@ -901,7 +993,8 @@ void dip_radial_release(fg_dipsys *h);
 
 void dip_free(fg_dipsys *h) {
     dip_radial_release(h);
-    void *ptrs[] = {h->d_desc, h->pos, h->mu, h->mus, h->q, h->ak, h->pairs, h->type, h->nearq, h->pf, h->kn, h->qi, h->qd,
+    void *ptrs[] = {h->d_desc, h->pos, h->mu, h->mus, h->q, h->ak, h->pairs, h->type, h->nearq, h->pf, h->sctab, h->yzl, h->kn,
+                    h->qi, h->qd,
                     h->fqi, h->fqd, h->dqi, h->dqd, h->akf, h->trials, h->log_du, h->log_acc, h->sc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1216,9 +1309,13 @@ int dip_launch(fg_dipsys *const *sys, const fgd::DipDesc *descs, int n, int mode
         stage = 0;
         smem = fgd::dip_yz_bytes(sys[0]->kcc);
     }
-    CK(cudaFuncSetAttribute((const void *)fgd::dip_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)smem));
-    fgd::dip_sweep_kernel<<<n, sys[0]->threads, smem, st>>>(descs, mode, stage);
+    const int T = sys[0]->threads;
+    const void *fn = T <= 128 ? (const void *)fgd::dip_sweep_kernel<128> : (const void *)fgd::dip_sweep_kernel<fgd::kDipMaxThreads>;
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (T <= 128)
+        fgd::dip_sweep_kernel<128><<<n, T, smem, st>>>(descs, mode, stage);
+    else
+        fgd::dip_sweep_kernel<fgd::kDipMaxThreads><<<n, T, smem, st>>>(descs, mode, stage);
     CK(cudaGetLastError());
     return FG_OK;
 }
@@ -1477,6 +1574,21 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     TRY(dip_dmalloc(h, (void **)&h->type, N * sizeof(int32_t)));
     TRY(dip_dmalloc(h, (void **)&h->nearq, (N + fgd::kDipMaxThreads) * sizeof(int32_t)));
     TRY(dip_dmalloc(h, (void **)&h->pf, N * sizeof(float4)));
+    TRY(dip_dmalloc(h, (void **)&h->sctab, fgd::kDipScTab * sizeof(float4)));
+    {   // the (n_y, n_z) entries of the phase table that some k-vector uses
+        const int W = 2 * h->kcc + 1;
+        std::vector<char> used((size_t)W * W, 0);
+        for (const char4 &n : h->kn_h) used[(size_t)(n.y + h->kcc) * W + n.z + h->kcc] = 1;
+        std::vector<int16_t> yz;
+        for (int r = 0; r < W * W; r++)
+            if (used[r]) yz.push_back((int16_t)r);
+        if (yz.empty()) yz.push_back(0);
+        TRY(dip_dmalloc(h, (void **)&h->yzl, yz.size() * sizeof(int16_t)));
+        if (cudaMemcpy(h->yzl, yz.data(), yz.size() * sizeof(int16_t), cudaMemcpyHostToDevice))
+            return bail(fail(FG_ERR_CUDA, "upload of the phase-table list failed"));
+        d.yzl = h->yzl;
+        d.nyz = (int)yz.size();
+    }
     TRY(dip_dmalloc(h, (void **)&h->pairs, 2 * N * sizeof(double)));
     TRY(dip_dmalloc(h, (void **)&h->kn, K * sizeof(char4)));
     TRY(dip_dmalloc(h, (void **)&h->ak, K * sizeof(double)));
@@ -1495,6 +1607,7 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     d.type = h->type;
     d.nearq = h->nearq;
     d.pf = h->pf;
+    d.sctab = h->sctab;
     d.kn = h->kn;
     d.ak = h->ak;
     d.qi = h->qi;
@@ -1513,6 +1626,17 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
             cudaMemcpyAsync(h->akf, akf.data(), h->K * sizeof(float2), cudaMemcpyHostToDevice, h->stream) ||
             cudaStreamSynchronize(h->stream))
             return bail(fail(FG_ERR_CUDA, "upload of the k-vectors failed"));
+    }
+    {   // cos, sin of 2 pi i / kDipScTab as df (axis_entry_df)
+        std::vector<float4> sct(fgd::kDipScTab);
+        for (int i = 0; i < fgd::kDipScTab; i++) {
+            const long double th = 2.0L * 3.141592653589793238462643383279502884L * i / fgd::kDipScTab;
+            const float2 c = split_df((double)std::cos(th)), sn = split_df((double)std::sin(th));
+            sct[i] = make_float4(c.x, c.y, sn.x, sn.y);
+        }
+        if (cudaMemcpyAsync(h->sctab, sct.data(), sct.size() * sizeof(float4), cudaMemcpyHostToDevice, h->stream) ||
+            cudaStreamSynchronize(h->stream))
+            return bail(fail(FG_ERR_CUDA, "upload of the phase table failed"));
     }
     TRY(dip_ensure_trials(h, 1, false));
     fgd::DipScalars s{};
