@@ -1193,7 +1193,7 @@ def run_dipoles(args, rank, world):
                              "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, TF32 off (best of 5)",
                              "flop_per_trial": flop, "fp64_peak_dgemm": fp64_peak,
                              "achieved_over_fp64_peak": achieved / fp64_peak,
-                             "note": "mixed precision: near pairs and phase tables FP64, k-space in double-float "
+                             "note": "mixed precision: near pairs FP64, phase tables and k-space in double-float "
                                      "and far pairs in FP32; whole-launch rate over all systems, each system one "
                                      "sequential chain"},
                 "single_system": single, "plain_per_trial_api": {"value": plain, "unit": UNIT},
