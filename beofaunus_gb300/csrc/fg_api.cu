@@ -169,18 +169,23 @@ int dmalloc(fg_system *h, void **p, size_t bytes) {
         if (rc_) return rc_;                                       \
     } while (0)
 
-// k-vectors exactly as NonbondedEwald::kVectorChange (ewald.h:330-378),
-// non-isotropic branch; returns n-vectors, k and A_k.
+// k-vectors exactly as NonbondedEwald::kVectorChange (ewald.h:330-378), with
+// its isotropic_pbc branch (n_y, n_z from 0, a factor 2 per positive
+// component); returns n-vectors, k and A_k.
 void enumerate_k(const fg_params &P, std::vector<int> &n3, std::vector<double> &ak, std::vector<double> &kv3) {
     double kc = P.ewald_cutoff_k, kc2 = kc * kc;
     int kcc = (int)std::ceil(kc);
     double maxL = std::max(P.box[0], std::max(P.box[1], P.box[2]));
     double check = 0.1 * (4 * PI * PI) / (maxL * maxL);
     double kappa = 1.0 / P.ewald_debye_length, alpha2 = P.ewald_alpha * P.ewald_alpha;
+    const bool iso = P.ewald_isotropic_pbc != 0;
+    const int lo = iso ? 0 : -kcc;
     for (int kx = 0; kx <= kcc; kx++)
-        for (int ky = -kcc; ky <= kcc; ky++)
-            for (int kz = -kcc; kz <= kcc; kz++) {
+        for (int ky = lo; ky <= kcc; ky++)
+            for (int kz = lo; kz <= kcc; kz++) {
                 double factor = kx > 0 ? 2.0 : 1.0;
+                if (iso && ky > 0) factor *= 2.0;
+                if (iso && kz > 0) factor *= 2.0;
                 double k[3] = {2 * PI * (kx / P.box[0]), 2 * PI * (ky / P.box[1]), 2 * PI * (kz / P.box[2])};
                 double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
                 if (k2 < check) continue;
@@ -310,7 +315,7 @@ size_t ewald_block_smem(const fg_system *h) {
     return fg::eb_layout(h->N, h->K, h->nc[0] * h->nc[1] * h->nc[2], h->use_cells, 1, off);
 }
 bool ewald_block_ok(const fg_system *h) {
-    return h->model == FG_MODEL_EWALD_WCA && h->K > 0 && h->N < (1 << 24) &&
+    return h->model == FG_MODEL_EWALD_WCA && h->K > 0 && h->N < (1 << 24) && !h->P.ewald_isotropic_pbc &&
            ewald_block_smem(h) + sizeof(SysDesc) + 1024 <= 227 * 1024;
 }
 
@@ -710,7 +715,9 @@ int launch_rebuild(const SysDesc *descs, int n, int maxN, int maxSeg, int maxKcc
     if (maxSeg == 0) return FG_OK;
     const int T = fg::qk_tab_len(maxKcc);
     const int threads = std::min(fg::kQkMaxThreads, ((maxSeg + 31) / 32) * 32);
-    const int stage = std::max(1, std::min(fg::kQkMaxStage, 40960 / (T * 8)));
+    // each thread stages (and prefetches) one particle of a pass: a pass holds
+    // at most as many particles as the block has threads
+    const int stage = std::max(1, std::min({fg::kQkMaxStage, 40960 / (T * 8), threads}));
     const size_t smem = fg::qk_rebuild_smem(stage, T, threads);
     int rc = set_smem_attr((const void *)fg::qk_rebuild_kernel, smem);
     if (rc) return rc;
@@ -1165,8 +1172,10 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
         ALLOC(h->kseg, seg.size() * sizeof(int2));
         cudaMemcpy(h->kseg, seg.data(), seg.size() * sizeof(int2), cudaMemcpyHostToDevice);
         // the block kernel's in-kernel rebuild: pairs (+n, -n) of k-vectors
+        // (the isotropic k-set holds n_z >= 0 only: no block kernel, no items)
         std::vector<int4> rb;
-        if (!rb_item_list(n3, 0, h->K, fg::kEbThreads - 32, rb)) return bail(fail(FG_ERR_INVALID, "k-vector set is not symmetric in nz"));
+        if (!P.ewald_isotropic_pbc && !rb_item_list(n3, 0, h->K, fg::kEbThreads - 32, rb))
+            return bail(fail(FG_ERR_INVALID, "k-vector set is not symmetric in nz"));
         h->n_rb_items = (int)rb.size();
         ALLOC(h->rb_items, rb.size() * sizeof(int4));
         cudaMemcpy(h->rb_items, rb.data(), rb.size() * sizeof(int4), cudaMemcpyHostToDevice);
@@ -1250,6 +1259,7 @@ int fg_create(const fg_params *params, int32_t n_particles, fg_system **out) {
     d.eb_ctas = 1;
     d.eb_kmax = h->K;
     d.eb_ranges = h->eb_ranges;
+    d.iso = P.ewald_isotropic_pbc ? 1 : 0;
     d.kcc = h->kc;
     if (set_qk_scale(d, qk_charge_bound(h, nullptr)))
         return bail(fail(FG_ERR_INVALID, "charges too large for the Q(k) fixed point"));

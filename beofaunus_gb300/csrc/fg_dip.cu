@@ -1460,6 +1460,7 @@ int fg_dip_create(const fg_params *params, int32_t n_particles, fg_dipsys **out)
     if (n_particles < 2 || n_particles >= (1 << 24)) return fail(FG_ERR_INVALID, "particle count must be 2..2^24");
     if (P.n_types < 1 || P.n_types > FG_MAX_TYPES) return fail(FG_ERR_INVALID, "bad type count");
     if ((P.ewald_terms & ~7) != 0) return fail(FG_ERR_INVALID, "bad ewald_terms");
+    if (P.ewald_isotropic_pbc) return fail(FG_ERR_INVALID, "isotropic_pbc is built for FG_MODEL_EWALD_WCA only");
     if (!(P.bjerrum > 0) || !(P.ewald_alpha > 0) || !(P.ewald_cutoff > 0) || !(P.ewald_debye_length > 0))
         return fail(FG_ERR_INVALID, "bad Ewald parameters");
     for (int a = 0; a < 3; a++)

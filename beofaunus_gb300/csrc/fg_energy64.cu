@@ -128,7 +128,15 @@ __global__ void __launch_bounds__(kE64Threads) energy64_qk_kernel(const SysDesc 
         __syncthreads();
         if (k >= d.K) continue;
         const int nb = min(kE64Tile, j1 - b);
-        for (int t = 0; t < nb; t++) {
+        for (int t = 0; t < nb && d.iso; t++) {   // isotropic_pbc: q eff cos cos cos, real
+            double c = qj[t];
+            const int nn[3] = {nx, ny, nz};
+            for (int a = 0; a < 3; a++)
+                c *= cos((double)(long long)((unsigned long long)(long long)nn[a] * (unsigned long long)pj[t][a]) *
+                         3.4061215800865545e-19);
+            re += c;
+        }
+        for (int t = 0; t < nb && !d.iso; t++) {
             const unsigned long long ph = (unsigned long long)(long long)nx * (unsigned long long)pj[t][0] +
                                           (unsigned long long)(long long)ny * (unsigned long long)pj[t][1] +
                                           (unsigned long long)(long long)nz * (unsigned long long)pj[t][2];

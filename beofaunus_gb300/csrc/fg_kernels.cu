@@ -510,14 +510,40 @@ __device__ __forceinline__ uint32_t phase(int nx, int ny, int nz, const int h[3]
     return (uint32_t)nx * (uint32_t)h[0] + (uint32_t)ny * (uint32_t)h[1] + (uint32_t)nz * (uint32_t)h[2];
 }
 
+// isotropic_pbc (ewald.h:669-675): D_k = q (c'_x c'_y c'_z - c_x c_y c_z),
+// c_a = cos(n_a 2 pi x_a / L_a), each axis difference taken as
+// cos a' - cos a = -2 sin((a' + a) / 2) sin((a' - a) / 2) so that a short
+// step keeps its relative accuracy.
+__device__ __forceinline__ float iso_delta(int nx, int ny, int nz, const Move &m, const float2 *__restrict__ tab) {
+    const int nn[3] = {nx, ny, nz};
+    float co[3], cn[3], dc[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const uint32_t po = (uint32_t)nn[a] * (uint32_t)m.ho[a], pn = (uint32_t)nn[a] * (uint32_t)m.hn[a];
+        const int32_t dp = (int32_t)(pn - po);
+        co[a] = sincos_turns(po, tab).x;
+        cn[a] = sincos_turns(pn, tab).x;
+        const float sm = sincos_turns(po + (uint32_t)(dp >> 1), tab).y;
+        const float sh = sinf((float)dp * (3.14159265f / 4294967296.0f));   // pi / 2^32 per unit
+        dc[a] = -2.0f * sm * sh;
+    }
+    return fmaf(dc[0], cn[1] * cn[2], co[0] * fmaf(dc[1], cn[2], co[1] * dc[2]));
+}
+
 // Reciprocal-space energy change of the trial for this thread's k-vectors:
-// A'_k (2 Re(conj(Q_k) D_k) + |D_k|^2), D_k = q e^{ik.r_old}(e^{ik.d} - 1).
+// A'_k (2 Re(conj(Q_k) D_k) + |D_k|^2), D_k = q e^{ik.r_old}(e^{ik.d} - 1)
+// (isotropic_pbc: Q and D real, iso_delta).
 __device__ __forceinline__ float kspace_energy(const Move &m, const SysDesc &d, const Smem &s) {
     float acc = 0.0f;
     const float qe = m.q * d.eff[m.ti];
     for (int k = threadIdx.x; k < d.K; k += blockDim.x) {
         int nx, ny, nz;
         unpack_n(s.kpack[k], nx, ny, nz);
+        if (d.iso) {
+            const float D = qe * iso_delta(nx, ny, nz, m, s.sc_tab);
+            acc = fmaf(s.kvec[k].w, fmaf(2.0f, s.qf[k].x * D, D * D), acc);
+            continue;
+        }
         const uint32_t ph = phase(nx, ny, nz, m.ho);
         const float2 e = sincos_turns(ph, s.sc_tab);
         const float4 kv = s.kvec[k];
@@ -556,7 +582,11 @@ __device__ __forceinline__ float2 sincos_turns_rn(uint32_t ph, const float2 *__r
 
 // Entry t of the axis tables of fixed-point position h (high words):
 // [0, kcc] e_x(n), [kcc+1, 3kcc+1] e_y(n - kcc), [3kcc+2, 5kcc+2] e_z(n - kcc).
-__device__ __forceinline__ float2 qk_tab_entry(int t, int kcc, const int h[3], const float2 *__restrict__ tab) {
+// iso (isotropic_pbc): the cosine alone, (cos, 0); the integer terms built on
+// it (qk_w, qk_term_bits) are then those of q cos cos cos with a zero
+// imaginary part, by the same roundings.
+__device__ __forceinline__ float2 qk_tab_entry(int t, int kcc, const int h[3], const float2 *__restrict__ tab,
+                                               bool iso = false) {
     int axis = 0, n = t;
     if (t > 3 * kcc + 1) {
         axis = 2;
@@ -568,6 +598,7 @@ __device__ __forceinline__ float2 qk_tab_entry(int t, int kcc, const int h[3], c
     const int an = n < 0 ? -n : n;
     const int ha = axis == 0 ? h[0] : (axis == 1 ? h[1] : h[2]);   // no dynamic register indexing
     const float2 e = sincos_turns_rn((uint32_t)an * (uint32_t)ha, tab);
+    if (iso) return make_float2(e.x, 0.0f);
     return n < 0 ? make_float2(e.x, -e.y) : e;
 }
 
@@ -617,11 +648,11 @@ __device__ __forceinline__ int2 qk_delta(int nx, int ny, int nz, float q2g, cons
 // Axis tables of a move's new and old positions into tn and to (all threads
 // of the block; the caller synchronises before use).
 __device__ __forceinline__ void qk_move_tables(const int hn[3], const int ho[3], int kcc, float2 *tn, float2 *to,
-                                               const float2 *__restrict__ tab) {
+                                               const float2 *__restrict__ tab, bool iso) {
     const int T = qk_tab_len(kcc);
     for (int t = threadIdx.x; t < 2 * T; t += blockDim.x) {
-        if (t < T) tn[t] = qk_tab_entry(t, kcc, hn, tab);
-        else to[t - T] = qk_tab_entry(t - T, kcc, ho, tab);
+        if (t < T) tn[t] = qk_tab_entry(t, kcc, hn, tab, iso);
+        else to[t - T] = qk_tab_entry(t - T, kcc, ho, tab, iso);
     }
 }
 
@@ -629,7 +660,7 @@ __device__ __forceinline__ void qk_move_tables(const int hn[3], const int ho[3],
 // Block-wide (uniform call): the axis tables go through shared memory.
 __device__ __forceinline__ void kspace_commit(const Move &m, const SysDesc &d, const Smem &s) {
     const int T = qk_tab_len(d.kcc);
-    qk_move_tables(m.hn, m.ho, d.kcc, s.ktab, s.ktab + T, s.sc_tab);
+    qk_move_tables(m.hn, m.ho, d.kcc, s.ktab, s.ktab + T, s.sc_tab, d.iso != 0);
     __syncthreads();
     const float q2g = qk_charge(m.q, d.eff[m.ti], d);
     for (int k = threadIdx.x; k < d.K; k += blockDim.x) {
@@ -957,8 +988,9 @@ __global__ void __launch_bounds__(kSweepThreads) commit_kernel(const SysDesc *__
 // 32 bits over a pass of `stage` <= 64 particles, then added to the thread's
 // int64 totals in shared memory. Per pass the block stages the particles'
 // axis tables (stage x qk_tab_len) from positions prefetched during the
-// previous pass. blockIdx.x covers a chunk of particles, blockIdx.y selects
-// the system of a batch; only systems with rebuild_pending set do work.
+// previous pass, one particle per thread (stage <= blockDim.x). blockIdx.x
+// covers a chunk of particles, blockIdx.y selects the system of a batch;
+// only systems with rebuild_pending set do work.
 constexpr int kQkRun = 8;
 constexpr int kQkMaxThreads = 512;
 // One pass over nb staged particles for runs of (at most) L k-vectors.
@@ -1034,7 +1066,7 @@ __global__ void __launch_bounds__(kQkMaxThreads) qk_rebuild_kernel(const SysDesc
                 while (jj < nb) {
                     const int4 p = sp[jj];
                     const int h[3] = {p.x, p.y, p.z};
-                    et[jj * T + e] = qk_tab_entry(e, kcc, h, tab);
+                    et[jj * T + e] = qk_tab_entry(e, kcc, h, tab, d.iso != 0);
                     jj += djj;
                     e += de;
                     if (e >= T) {

@@ -140,6 +140,9 @@ struct alignas(16) SysDesc {
     int32_t eb_ctas;
     int32_t eb_kmax;
     const int4 *eb_ranges;
+    // isotropic_pbc (ewald.h:347-360, 394-399): k-vectors in the positive
+    // octant, Q(k) real (cosine products); one-trial kernels only
+    int32_t iso;
 };
 
 }  // namespace fg

@@ -43,7 +43,8 @@ class FgParams(ctypes.Structure):
         ("use_cell_list", ctypes.c_int32),
         ("ewald_terms", ctypes.c_int32),
         ("ewald_dipole_quirk", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("ewald_isotropic_pbc", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 

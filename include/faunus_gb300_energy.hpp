@@ -72,6 +72,7 @@ inline fg_params gpuParamsEwaldWCA(Tmjson &j) {
     p.ewald_debye_length = e.at("debyelength");
     p.ewald_eps_surf = e.at("eps_surf");
     p.ewald_spherical_sum = e.value("spherical_sum", true) ? 1 : 0;
+    p.ewald_isotropic_pbc = e.value("isotropic_pbc", false) ? 1 : 0;
     p.ewald_update_frequency = e.value("update_frequency", -1);
     p.kT_scale = 1.0;
     gpuFillTypes(p);

@@ -84,7 +84,13 @@ typedef struct fg_params {
                                          after its ion-ion term (ewald.h:109-110)
                                          and the reciprocal cross term is
                                          2 Re(Q_ion Q_dip) (ewald.h:304-305) */
-    int32_t reserved[5];
+    int32_t ewald_isotropic_pbc;      /* "isotropic_pbc" (ewald.h:525): k-vectors
+                                         with n_x, n_y, n_z >= 0, a factor 2 per
+                                         positive component, and the real
+                                         Q(k) = sum q eff cos(k_x x) cos(k_y y)
+                                         cos(k_z z) (ewald.h:347-360, 394-399);
+                                         FG_MODEL_EWALD_WCA only */
+    int32_t reserved[4];
 } fg_params;
 
 #ifdef __cplusplus

@@ -96,8 +96,11 @@ struct System {
     }
 
     // ---- Ewald reciprocal space -----------------------------------------
-    // kVectorChange (ewald.h:330-378), non-isotropic branch
+    // kVectorChange (ewald.h:330-378); isotropic_pbc (ewald.h:347-360): n_y and
+    // n_z from 0 and a factor 2 for each positive component
     void kvectors() {
+        const bool iso = P.ewald_isotropic_pbc != 0;
+        const int start = iso ? 0 : 1;
         double kc = P.ewald_cutoff_k, kc2 = kc * kc;
         int kcc = (int)std::ceil(kc);
         double maxL = std::max(P.box[0], std::max(P.box[1], P.box[2]));
@@ -105,11 +108,13 @@ struct System {
         kv.clear(); Ak.clear();
         for (int kx = 0; kx <= kcc; kx++) {
             double dkx2 = double(kx * kx);
-            for (int ky = -kcc; ky <= kcc; ky++) {
+            for (int ky = -kcc * start; ky <= kcc; ky++) {
                 double dky2 = double(ky * ky);
-                for (int kz = -kcc; kz <= kcc; kz++) {
+                for (int kz = -kcc * start; kz <= kcc; kz++) {
                     double factor = 1.0;
                     if (kx > 0) factor = 2.0;
+                    if (ky > 0 && iso) factor = 2.0 * factor;
+                    if (kz > 0 && iso) factor = 2.0 * factor;
                     double dkz2 = double(kz * kz);
                     V3 k = {2 * PI * (kx / P.box[0]), 2 * PI * (ky / P.box[1]), 2 * PI * (kz / P.box[2])};
                     double k2 = k.x * k.x + k.y * k.y + k.z * k.z;
@@ -125,14 +130,19 @@ struct System {
         Q.assign(K, 0.0);
         Qt.assign(K, 0.0);
     }
+    // one particle's ion term of Q(k): q e^{ik.r} eff, or with isotropic_pbc
+    // the real q cos(k_x x) cos(k_y y) cos(k_z z) eff (ewald.h:394-399, 669-675)
+    std::complex<double> qk_term(const Particle &a, int k) const {
+        if (P.ewald_isotropic_pbc)
+            return a.q * std::cos(kv[k].x * a.r.x) * std::cos(kv[k].y * a.r.y) * std::cos(kv[k].z * a.r.z) * eff[a.id];
+        double dot = kv[k].x * a.r.x + kv[k].y * a.r.y + kv[k].z * a.r.z;
+        return a.q * std::complex<double>(std::cos(dot), std::sin(dot)) * eff[a.id];
+    }
     // updateAllComplexNumbers (ewald.h:388-415), ion part
     void rebuild(const std::vector<Particle> &pv, std::vector<std::complex<double>> &q) const {
         for (int k = 0; k < K; k++) {
             std::complex<double> s(0.0, 0.0);
-            for (int i = 0; i < N; i++) {
-                double dot = kv[k].x * pv[i].r.x + kv[k].y * pv[i].r.y + kv[k].z * pv[i].r.z;
-                s += pv[i].q * std::complex<double>(std::cos(dot), std::sin(dot)) * eff[pv[i].id];
-            }
+            for (int i = 0; i < N; i++) s += qk_term(pv[i], k);
             q[k] = s;
         }
     }
@@ -158,15 +168,13 @@ struct System {
         for (int i = 0; i < N; i++) Eq += pv[i].q * pv[i].q * eff[pv[i].id] * eff[pv[i].id];
         return (-alpha * (Eq) / std::sqrt(PI)) * lB;
     }
-    // updateChange (ewald.h:651-705), fixed volume, non-isotropic ion branch
+    // updateChange (ewald.h:651-705), fixed volume, ion branch
     void update_change() {
         for (int k = 0; k < K; k++) {
             std::complex<double> q2 = Q[k];
             for (int i : moved) {
-                double dotT = kv[k].x * trial[i].r.x + kv[k].y * trial[i].r.y + kv[k].z * trial[i].r.z;
-                double dot = kv[k].x * p[i].r.x + kv[k].y * p[i].r.y + kv[k].z * p[i].r.z;
-                q2 += trial[i].q * std::complex<double>(std::cos(dotT), std::sin(dotT)) * eff[trial[i].id];
-                q2 -= p[i].q * std::complex<double>(std::cos(dot), std::sin(dot)) * eff[p[i].id];
+                q2 += qk_term(trial[i], k);
+                q2 -= qk_term(p[i], k);
             }
             Qt[k] = q2;
         }

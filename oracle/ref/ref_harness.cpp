@@ -158,6 +158,7 @@ static Tmjson faunus_input(const Tmjson &in) {
             {"eps_surf", in["eps_surf"]}, {"alpha", in["alpha"]}, {"cutoff", in["cutoff"]},
             {"cutoffK", in["cutoffK"]}, {"debyelength", in.value("debyelength", 1e30)},
             {"spherical_sum", in.value("spherical_sum", true)},
+            {"isotropic_pbc", in.value("isotropic_pbc", false)},
             {"update_frequency", in.value("update_frequency", -1)}};
     } else {
         j["energy"]["nonbonded"]["debyelength"] = in["debyelength"];

@@ -54,7 +54,8 @@ def params_of(g):
     return p
 
 
-@pytest.mark.parametrize("name", ["ewald_small_uf1", "ewald_surface_uf5", "ewald_rpm800", "dhlj_small", "dhlj_500"])
+@pytest.mark.parametrize("name", ["ewald_small_uf1", "ewald_surface_uf5", "ewald_rpm800", "ewald_iso", "dhlj_small",
+                                  "dhlj_500"])
 def test_sweep_reproduces_reference_log(name):
     """Device sweep with the host replay of the reference's RNG reproduces the
     reference's own per-trial log (dU, acceptance) and final positions."""
@@ -206,3 +207,58 @@ def test_invalid_arguments_fail_loudly():
     bad.type_charge[0] = 0.0   # ewald.h:539 would divide by zero
     with pytest.raises(FgError):
         gpu_system(bad, xyz, q, ids)
+
+
+def test_isotropic_pbc_qk_exact_and_energies():
+    """isotropic_pbc (ewald.h:347-360, 394-399, 669-675): the positive-octant
+    k-set, a real Q(k) (zero imaginary parts, bit for bit) that a rebuild
+    reproduces exactly after a thousand trials, the plain per-trial path and
+    the totals against the FP64 oracle."""
+    p, xyz, q, ids = workloads.rpm_ewald(150, 26.0, 6, seed=41, update_frequency=50, cutoff=11.0, eps_surf=1.0)
+    p.ewald_isotropic_pbc = 1
+    s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
+    assert s.num_kvectors == o.num_kvectors
+    idx, disp, u = s.draw_translation_stream(9, 1200)
+    r = s.sweep(idx, disp, u)
+    ro = o.mc_run_stream(idx, disp, u)
+    assert_same_chain(r["du"], r["acc"], ro["du"], ro["acc"], u)
+    assert r["stats"]["rebuilds"] > 0 and r["stats"]["error_flags"] == 0
+    qk = s.qk()
+    assert np.all(qk.imag == 0.0)
+    assert s.rebuild_qk() == 0.0
+    np.testing.assert_array_equal(s.qk(), qk)
+    e64 = s.total_energy_fp64()
+    eo = o.total_energy()
+    assert e64["reciprocal"] == pytest.approx(eo["reciprocal"], abs=1e-9)
+    assert e64["total"] == pytest.approx(eo["total"], abs=1e-8)
+    # the plain drop-in path
+    pos = o.positions()
+    idx2, disp2, u2 = translation_stream(77, np.array([p.type_dp[i] for i in ids]), 100)
+    for t in range(100):
+        i = int(idx2[t])
+        new = o.boundary(pos[i] + disp2[t])
+        dg, do = s.trial_du(i, new), o.trial_du(i, new)
+        assert abs(dg - do) <= TOL_DU
+        acc = not (u2[t] > np.exp(-do))
+        s.commit(acc)
+        o.commit(acc)
+        if acc:
+            pos[i] = new
+
+
+def test_rebuild_with_few_kvector_runs():
+    """A k-set of fewer runs (k-vectors sharing n_x, n_y) than particles per
+    rebuild pass: the rebuild's block then has fewer threads than a pass has
+    particles, and each pass may hold no more particles than threads. 150
+    ions, |n| <= 2: every rebuild (update_frequency 5) reproduces the running
+    Q(k) exactly, and the chain is the oracle's."""
+    p, xyz, q, ids = workloads.rpm_ewald(150, 32.0, 2, seed=43, update_frequency=5, cutoff=12.0)
+    s = gpu_system(p, xyz, q, ids)
+    o = OracleSystem(p, xyz, q, ids)
+    idx, disp, u = s.draw_translation_stream(8, 600)
+    r = s.sweep(idx, disp, u)
+    ro = o.mc_run_stream(idx, disp, u)
+    assert_same_chain(r["du"], r["acc"], ro["du"], ro["acc"], u)
+    assert r["stats"]["rebuilds"] == r["stats"]["accepted"] // 5 and r["stats"]["error_flags"] == 0
+    assert s.rebuild_qk() == 0.0

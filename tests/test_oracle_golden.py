@@ -11,7 +11,7 @@ from oracle.oracle import OracleSystem, atom_rdf_counts, rdf_normalize, translat
 
 from conftest import GOLDEN
 
-MC_CASES = ["ewald_small_uf1", "ewald_surface_uf5", "ewald_rpm800", "dhlj_small", "dhlj_500", "dhlj_rdf"]
+MC_CASES = ["ewald_small_uf1", "ewald_surface_uf5", "ewald_rpm800", "ewald_iso", "dhlj_small", "dhlj_500", "dhlj_rdf"]
 
 
 def load(name):
